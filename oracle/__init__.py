@@ -1,0 +1,385 @@
+"""ctypes bindings of the C oracle (``oracle/*.c``): the FP64 restatement of the reference's
+Chorin-projection path.  Test infrastructure only — imported by ``tests/``, by
+``__graft_entry__.smoke()`` as the checker, and by ``bench.py``'s CPU-baseline leg; the product
+package never imports it.
+
+``reference()`` additionally loads ``oracle/_ref/libnsfref.so`` (the reference's own C++ built
+from its sources by ``oracle/Makefile.ref``) when it has been built on this machine.
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB = None
+_REF = None
+
+i32p = C.POINTER(C.c_int)
+f32p = C.POINTER(C.c_float)
+f64p = C.POINTER(C.c_double)
+
+
+class CsrS(C.Structure):
+    _fields_ = [("rows", C.c_int), ("cols", C.c_int), ("nnz", C.c_int),
+                ("rowStart", i32p), ("col", i32p), ("val", f64p)]
+
+
+class MeshS(C.Structure):
+    _fields_ = [("numCorner", C.c_int), ("numTri", C.c_int), ("numBorder", C.c_int), ("numGroups", C.c_int),
+                ("cornerXY", f32p), ("tri", i32p), ("border", i32p), ("groups", C.POINTER(C.c_char_p)),
+                ("numV", C.c_int), ("numP", C.c_int), ("vXY", f32p), ("vElem", i32p), ("vBorder", i32p),
+                ("pElem", i32p), ("pBorder", i32p), ("affine", f32p)]
+
+
+class ContextS(C.Structure):
+    _fields_ = [("N", C.c_int), ("P", C.c_int), ("nDir", C.c_int), ("dirIds", i32p), ("dirVx", f64p),
+                ("nDirP", C.c_int), ("dirPIds", i32p), ("nIntV", C.c_int), ("nIntP", C.c_int),
+                ("intV", i32p), ("intP", i32p),
+                ("M", CsrS), ("K", CsrS), ("Kp", CsrS), ("Kpi", CsrS), ("D", CsrS), ("G", CsrS), ("I", CsrS)]
+
+
+class ColoringS(C.Structure):
+    _fields_ = [("n", C.c_int), ("nColors", C.c_int), ("perm", i32p), ("partStart", i32p), ("slOrder", i32p)]
+
+
+class ChorinCfgS(C.Structure):
+    _fields_ = [("nu", C.c_double), ("tau", C.c_double), ("velMethod", C.c_int), ("velMaxIters", C.c_int),
+                ("velTol", C.c_double), ("presMaxIters", C.c_int), ("presTol", C.c_double)]
+
+
+def build(quiet: bool = True) -> str:
+    """Compile liboracle.so with make (plain C)."""
+    out = subprocess.run(["make", "-C", HERE, "-s"], capture_output=True, text=True)
+    if out.returncode != 0:
+        raise RuntimeError("oracle build failed:\n" + out.stdout + out.stderr)
+    return os.path.join(HERE, "_build", "liboracle.so")
+
+
+def lib():
+    global _LIB
+    if _LIB is None:
+        path = os.path.join(HERE, "_build", "liboracle.so")
+        if not os.path.exists(path):
+            build()
+        L = C.CDLL(path)
+        L.orc_last_error.restype = C.c_char_p
+        L.orc_mesh_load.restype = C.POINTER(MeshS)
+        L.orc_mesh_load.argtypes = [C.c_char_p]
+        L.orc_mesh_free.argtypes = [C.POINTER(MeshS)]
+        L.orc_group_id.argtypes = [C.POINTER(MeshS), C.c_char_p]
+        L.orc_channel_bcs.argtypes = [C.POINTER(MeshS), C.c_float, C.POINTER(ContextS)]
+        L.orc_assemble.argtypes = [C.POINTER(MeshS), C.POINTER(ContextS), C.c_int]
+        L.orc_context_free.argtypes = [C.POINTER(ContextS)]
+        L.orc_csr_free.argtypes = [C.POINTER(CsrS)]
+        L.orc_spmv.argtypes = [C.POINTER(CsrS), f64p, f64p]
+        L.orc_spmm2.argtypes = [C.POINTER(CsrS), f64p, f64p, f64p]
+        L.orc_slice.argtypes = [C.POINTER(CsrS), C.c_int, i32p, C.c_int, i32p, C.POINTER(CsrS)]
+        L.orc_coloring_build.argtypes = [C.POINTER(CsrS), C.POINTER(ColoringS)]
+        L.orc_coloring_free.argtypes = [C.POINTER(ColoringS)]
+        L.orc_gs_solve.argtypes = [C.POINTER(CsrS), C.POINTER(ColoringS), C.c_int, f64p, f64p, C.c_int,
+                                   C.c_double, C.c_int, f64p, i32p]
+        L.orc_pcg.argtypes = [C.POINTER(CsrS), C.POINTER(ColoringS), C.c_int, f64p, f64p, C.c_int, C.c_double,
+                              i32p, f64p]
+        L.orc_sgs_apply.argtypes = [C.POINTER(CsrS), C.POINTER(ColoringS), f64p, f64p]
+        L.orc_chorin_create.restype = C.c_void_p
+        L.orc_chorin_create.argtypes = [C.POINTER(ContextS), C.POINTER(ChorinCfgS)]
+        L.orc_chorin_free.argtypes = [C.c_void_p]
+        L.orc_chorin_get.argtypes = [C.c_void_p, f64p, f64p]
+        L.orc_chorin_set.argtypes = [C.c_void_p, f64p, f64p]
+        L.orc_chorin_step.argtypes = [C.c_void_p, f64p]
+        L.orc_fastconv.argtypes = [C.POINTER(ContextS), C.c_double, f64p, f64p]
+        _LIB = L
+    return _LIB
+
+
+def _arr(ptr, n, dtype):
+    if n == 0:
+        return np.zeros(0, dtype=dtype)
+    return np.ctypeslib.as_array(ptr, shape=(n,)).astype(dtype, copy=True)
+
+
+def _ptr(a: np.ndarray, ct):
+    return a.ctypes.data_as(C.POINTER(ct))
+
+
+class Csr:
+    """Host CSR copy: rows, cols, rowStart (int32), col (int32), val (float64)."""
+
+    def __init__(self, rows, cols, rowStart, col, val=None):
+        self.rows, self.cols = int(rows), int(cols)
+        self.rowStart = np.ascontiguousarray(rowStart, dtype=np.int32)
+        self.col = np.ascontiguousarray(col, dtype=np.int32)
+        self.val = None if val is None else np.ascontiguousarray(val, dtype=np.float64)
+
+    @property
+    def nnz(self):
+        return int(self.col.shape[0])
+
+    @staticmethod
+    def from_struct(s: CsrS) -> "Csr":
+        val = _arr(s.val, s.nnz, np.float64) if bool(s.val) else None
+        return Csr(s.rows, s.cols, _arr(s.rowStart, s.rows + 1, np.int32), _arr(s.col, s.nnz, np.int32), val)
+
+    def struct(self) -> CsrS:
+        s = CsrS()
+        s.rows, s.cols, s.nnz = self.rows, self.cols, self.nnz
+        s.rowStart = _ptr(self.rowStart, C.c_int)
+        s.col = _ptr(self.col, C.c_int)
+        if self.val is None:
+            self.val = np.zeros(self.nnz, dtype=np.float64)
+        s.val = _ptr(self.val, C.c_double)
+        return s
+
+    def to_scipy(self):
+        import scipy.sparse as sp
+        return sp.csr_matrix((self.val, self.col, self.rowStart), shape=(self.rows, self.cols))
+
+
+class Mesh:
+    """Oracle mesh: corner mesh, P2 velocity numbering and P1 pressure numbering."""
+
+    def __init__(self, path: str):
+        L = lib()
+        p = L.orc_mesh_load(path.encode())
+        if not p:
+            raise RuntimeError("oracle mesh load failed: " + L.orc_last_error().decode())
+        self._p = p
+        m = p.contents
+        self.num_corner, self.num_tri, self.num_border = m.numCorner, m.numTri, m.numBorder
+        self.groups = [m.groups[i].decode() for i in range(m.numGroups)]
+        self.corner_xy = _arr(m.cornerXY, 2 * m.numCorner, np.float32).reshape(-1, 2)
+        self.tri = _arr(m.tri, 3 * m.numTri, np.int32).reshape(-1, 3)
+        self.border = _arr(m.border, 3 * m.numBorder, np.int32).reshape(-1, 3)
+        self.N, self.P = m.numV, m.numP
+        self.v_xy = _arr(m.vXY, 2 * m.numV, np.float32).reshape(-1, 2)
+        self.v_elem = _arr(m.vElem, 6 * m.numTri, np.int32).reshape(-1, 6)
+        self.v_border = _arr(m.vBorder, 6 * m.numBorder, np.int32).reshape(-1, 6)
+        self.p_elem = _arr(m.pElem, 3 * m.numTri, np.int32).reshape(-1, 3)
+        self.p_border = _arr(m.pBorder, 5 * m.numBorder, np.int32).reshape(-1, 5)
+        self.affine = _arr(m.affine, 6 * m.numTri, np.float32).reshape(-1, 6)
+
+    def __del__(self):
+        try:
+            lib().orc_mesh_free(self._p)
+        except Exception:
+            pass
+
+
+class Context:
+    """Channel-problem context: Dirichlet/internal lists and the assembled FP64 matrices."""
+
+    NAMES = ("M", "K", "Kp", "Kpi", "D", "G", "I")
+
+    def __init__(self, mesh: Mesh, peak_velocity: float, with_convection: bool = True):
+        L = lib()
+        self._s = ContextS()
+        if L.orc_channel_bcs(mesh._p, C.c_float(peak_velocity), C.byref(self._s)) != 0:
+            raise RuntimeError(L.orc_last_error().decode())
+        L.orc_assemble(mesh._p, C.byref(self._s), int(with_convection))
+        s = self._s
+        self.N, self.P = s.N, s.P
+        self.dir_ids = _arr(s.dirIds, s.nDir, np.int32)
+        self.dir_vx = _arr(s.dirVx, s.nDir, np.float64)
+        self.dir_p_ids = _arr(s.dirPIds, s.nDirP, np.int32)
+        self.int_v = _arr(s.intV, s.nIntV, np.int32)
+        self.int_p = _arr(s.intP, s.nIntP, np.int32)
+        for name in self.NAMES:
+            cs = getattr(s, name)
+            setattr(self, name, Csr.from_struct(cs) if cs.rows > 0 else None)
+
+    def __del__(self):
+        try:
+            lib().orc_context_free(C.byref(self._s))
+        except Exception:
+            pass
+
+
+def coloring(a: Csr):
+    """(perm, partStart, slOrder) of the smallest-last + greedy coloring."""
+    L = lib()
+    s = a.struct()
+    c = ColoringS()
+    L.orc_coloring_build(C.byref(s), C.byref(c))
+    out = (_arr(c.perm, c.n, np.int32), _arr(c.partStart, c.nColors + 1, np.int32), _arr(c.slOrder, c.n, np.int32))
+    L.orc_coloring_free(C.byref(c))
+    return out
+
+
+def _col_struct(perm, part):
+    c = ColoringS()
+    c.n = len(perm)
+    c.nColors = len(part) - 1
+    c.perm = _ptr(perm, C.c_int)
+    c.partStart = _ptr(part, C.c_int)
+    c.slOrder = _ptr(perm, C.c_int)
+    return c
+
+
+def slice_csr(a: Csr, rows, cols) -> Csr:
+    L = lib()
+    rows = np.ascontiguousarray(rows, dtype=np.int32)
+    cols = np.ascontiguousarray(cols, dtype=np.int32)
+    s = a.struct()
+    o = CsrS()
+    L.orc_slice(C.byref(s), len(rows), _ptr(rows, C.c_int), len(cols), _ptr(cols, C.c_int), C.byref(o))
+    r = Csr.from_struct(o)
+    L.orc_csr_free(C.byref(o))
+    return r
+
+
+def spmv(a: Csr, x) -> np.ndarray:
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    y = np.zeros(a.rows, dtype=np.float64)
+    s = a.struct()
+    lib().orc_spmv(C.byref(s), _ptr(x, C.c_double), _ptr(y, C.c_double))
+    return y
+
+
+def spmm2(a: Csr, vals, x) -> np.ndarray:
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    vals = np.ascontiguousarray(vals, dtype=np.float64)
+    y = np.zeros(2 * a.rows, dtype=np.float64)
+    s = a.struct()
+    lib().orc_spmm2(C.byref(s), _ptr(vals, C.c_double), _ptr(x, C.c_double), _ptr(y, C.c_double))
+    return y
+
+
+def gs_solve(a: Csr, col, num_ch, b, x0, max_iters, target_rms, check_interval=1):
+    perm, part = col[0], col[1]
+    x = np.array(x0, dtype=np.float64, copy=True)
+    b = np.ascontiguousarray(b, dtype=np.float64)
+    rms = np.zeros(num_ch, dtype=np.float64)
+    it = C.c_int(0)
+    s = a.struct()
+    cs = _col_struct(perm, part)
+    rc = lib().orc_gs_solve(C.byref(s), C.byref(cs), num_ch, _ptr(b, C.c_double), _ptr(x, C.c_double), max_iters,
+                            target_rms, check_interval, _ptr(rms, C.c_double), C.byref(it))
+    if rc != 0:
+        raise RuntimeError("oracle GS failed (zero or missing diagonal)")
+    return x, rms, it.value
+
+
+def pcg(a: Csr, col, b, x0, max_iters, rel_tol, precond=1):
+    perm, part = col[0], col[1]
+    x = np.array(x0, dtype=np.float64, copy=True)
+    b = np.ascontiguousarray(b, dtype=np.float64)
+    it = C.c_int(0)
+    rr = C.c_double(0)
+    s = a.struct()
+    cs = _col_struct(perm, part)
+    st = lib().orc_pcg(C.byref(s), C.byref(cs), precond, _ptr(b, C.c_double), _ptr(x, C.c_double), max_iters,
+                       rel_tol, C.byref(it), C.byref(rr))
+    return x, st, it.value, rr.value
+
+
+def sgs_apply(a: Csr, col, r):
+    perm, part = col[0], col[1]
+    r = np.ascontiguousarray(r, dtype=np.float64)
+    z = np.zeros_like(r)
+    s = a.struct()
+    cs = _col_struct(perm, part)
+    lib().orc_sgs_apply(C.byref(s), C.byref(cs), _ptr(r, C.c_double), _ptr(z, C.c_double))
+    return z
+
+
+def fastconv(ctx: Context, nu: float, u) -> np.ndarray:
+    u = np.ascontiguousarray(u, dtype=np.float64)
+    out = np.zeros(ctx.K.nnz, dtype=np.float64)
+    lib().orc_fastconv(C.byref(ctx._s), nu, _ptr(u, C.c_double), _ptr(out, C.c_double))
+    return out
+
+
+class Chorin:
+    """FP64 Chorin stepper of the oracle.  vel_method 0 = multicolor GS (RMS target),
+    1 = CG + multicolor SGS (relative tolerance)."""
+
+    def __init__(self, ctx: Context, nu, tau, vel_method=1, vel_max_iters=200, vel_tol=1e-10,
+                 pres_max_iters=2000, pres_tol=1e-10):
+        self.ctx = ctx
+        cfg = ChorinCfgS(nu, tau, vel_method, vel_max_iters, vel_tol, pres_max_iters, pres_tol)
+        self._h = lib().orc_chorin_create(C.byref(ctx._s), C.byref(cfg))
+
+    def step(self):
+        st = np.zeros(6, dtype=np.float64)
+        rc = lib().orc_chorin_step(self._h, _ptr(st, C.c_double))
+        if rc != 0:
+            raise RuntimeError(f"oracle Chorin step failed with status {rc}")
+        return st
+
+    def state(self):
+        u = np.zeros(2 * self.ctx.N, dtype=np.float64)
+        p = np.zeros(self.ctx.P, dtype=np.float64)
+        lib().orc_chorin_get(self._h, _ptr(u, C.c_double), _ptr(p, C.c_double))
+        return u, p
+
+    def set_state(self, u, p):
+        u = np.ascontiguousarray(u, dtype=np.float64)
+        p = np.ascontiguousarray(p, dtype=np.float64)
+        lib().orc_chorin_set(self._h, _ptr(u, C.c_double), _ptr(p, C.c_double))
+
+    def __del__(self):
+        try:
+            lib().orc_chorin_free(self._h)
+        except Exception:
+            pass
+
+
+# ---------------------------------------------------------------- reference build (oracle/_ref)
+
+def reference_path() -> str:
+    return os.path.join(HERE, "_ref", "libnsfref.so")
+
+
+def build_reference(ref_root: str = "/root/reference/cpp") -> bool:
+    """Build oracle/_ref/libnsfref.so from the reference sources if they are present."""
+    if not os.path.isdir(ref_root):
+        return False
+    out = subprocess.run(["make", "-C", HERE, "-f", "Makefile.ref", "-s", "-j8", f"REF={ref_root}"],
+                         capture_output=True, text=True)
+    if out.returncode != 0:
+        raise RuntimeError("reference harness build failed:\n" + out.stdout + out.stderr)
+    return True
+
+
+def reference():
+    """The reference-code harness, or None if it has not been built on this machine."""
+    global _REF
+    if _REF is None:
+        p = reference_path()
+        if not os.path.exists(p):
+            return None
+        try:
+            R = C.CDLL(p)
+        except OSError:
+            return None
+        R.ref_last_error.restype = C.c_char_p
+        R.ref_mesh_load.restype = C.c_void_p
+        R.ref_mesh_load.argtypes = [C.c_char_p]
+        R.ref_mesh_free.argtypes = [C.c_void_p]
+        R.ref_mesh_counts.argtypes = [C.c_void_p, i32p]
+        R.ref_mesh_group.restype = C.c_char_p
+        R.ref_mesh_group.argtypes = [C.c_void_p, C.c_int]
+        R.ref_mesh_elements.argtypes = [C.c_void_p, C.c_int, i32p]
+        R.ref_mesh_nodes.argtypes = [C.c_void_p, C.c_int, f32p]
+        R.ref_mesh_border.argtypes = [C.c_void_p, C.c_int, i32p]
+        R.ref_dirichlet.argtypes = [C.c_void_p, C.c_float, i32p, i32p, f32p, i32p, i32p, i32p]
+        R.ref_prototype.restype = C.c_void_p
+        R.ref_prototype.argtypes = [C.c_void_p, C.c_int]
+        R.ref_csr_wrap.restype = C.c_void_p
+        R.ref_csr_wrap.argtypes = [C.c_int, C.c_int, C.c_int, i32p, i32p, f32p]
+        R.ref_csr_free.argtypes = [C.c_void_p]
+        R.ref_csr_dims.argtypes = [C.c_void_p, i32p]
+        R.ref_csr_arrays.argtypes = [C.c_void_p, i32p, i32p, f32p]
+        R.ref_csr_slice.restype = C.c_void_p
+        R.ref_csr_slice.argtypes = [C.c_void_p, C.c_int, i32p, C.c_int, i32p]
+        R.ref_coloring.restype = C.c_int
+        R.ref_coloring.argtypes = [C.c_void_p, i32p, i32p, i32p]
+        R.ref_gs2ch_double.argtypes = [C.c_int, i32p, i32p, f64p, f64p, f64p, C.c_int, C.c_double, f64p]
+        R.ref_rmult_double.argtypes = [C.c_int, C.c_int, i32p, i32p, f64p, f64p, f64p]
+        _REF = R
+    return _REF

@@ -1,0 +1,138 @@
+/*
+ * CPU oracle for the Chorin-projection hot path: a plain-C FP64 restatement of the reference's
+ * algorithms (kosyonikolov/NsFemOptim).  TEST INFRASTRUCTURE ONLY: it is the checker that the
+ * GPU path is compared against, and the CPU baseline that bench.py times.  The product never
+ * links or calls it.
+ *
+ * Parity status: the integer parts (gmsh parse, P1/P2 DOF numbering, Dirichlet and internal
+ * node lists, CSR sparsity patterns, smallest-last + greedy coloring, CSR slicing) and the
+ * double-precision Gauss-Seidel sweep are pinned against the reference's own C++ compiled from
+ * its sources (oracle/_ref).  The local element matrices (the reference computes them with
+ * OpenCV, not buildable here) and the Eigen direct solves are restated; their values are
+ * checked through physical identities (mass sums to the area, stiffness rows sum to zero,
+ * divergence/gradient transpose pair) and parity there is "unpinned".
+ */
+#ifndef NSF_ORACLE_H
+#define NSF_ORACLE_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct
+{
+    int rows, cols, nnz;
+    int *rowStart; /* rows + 1 */
+    int *col;      /* nnz, sorted within each row */
+    double *val;   /* nnz (may be NULL for a pattern) */
+} orc_csr;
+
+typedef struct
+{
+    /* corner mesh (mesh::TriangleMesh) */
+    int numCorner, numTri, numBorder, numGroups;
+    float *cornerXY;      /* 2 * numCorner */
+    int *tri;             /* 3 * numTri */
+    int *border;          /* 3 * numBorder: triangle, side, group */
+    char **groups;        /* numGroups names */
+    /* P2 velocity mesh and P1 pressure mesh (mesh::ConcreteMesh) */
+    int numV, numP;
+    float *vXY;           /* 2 * numV */
+    int *vElem;           /* 6 * numTri: c0, m01, c1, m12, c2, m20 */
+    int *vBorder;         /* 6 * numBorder: triangle, side, group, A, mid, B */
+    int *pElem;           /* 3 * numTri */
+    int *pBorder;         /* 5 * numBorder: triangle, side, group, A, B */
+    float *affine;        /* 6 * numTri: m00 m01 m10 m11 b0 b1 (float, as el::AffineTransform) */
+} orc_mesh;
+
+typedef struct
+{
+    int N, P;                 /* velocity nodes per component, pressure nodes */
+    int nDir;                 /* Dirichlet velocity nodes (same ids for x and y) */
+    int *dirIds;              /* sorted */
+    double *dirVx;            /* x values (float-rounded as the reference), y values are 0 */
+    int nDirP;
+    int *dirPIds;             /* pressure Dirichlet ids (Right border) */
+    int nIntV, nIntP;
+    int *intV, *intP;         /* internal node lists */
+    orc_csr M, K, Kp, Kpi, D, G, I; /* mass, stiffness, pressure stiffness, its internal slice,
+                                        divergence P x 2N, gradient 2N x P,
+                                        FastConvection integration nnz(K) x 2N */
+} orc_context;
+
+typedef struct
+{
+    int n, nColors;
+    int *perm;        /* new -> old row id (concatenated sorted partitions) */
+    int *partStart;   /* nColors + 1 */
+    int *slOrder;     /* smallest-last order (n) */
+} orc_coloring;
+
+/* ---------------- mesh ---------------- */
+const char *orc_last_error(void);
+orc_mesh *orc_mesh_load(const char *path);
+void orc_mesh_free(orc_mesh *m);
+int orc_group_id(const orc_mesh *m, const char *name);
+/* channel problem lists (buildContext.cpp:64-93); fills N, P and the node lists */
+int orc_channel_bcs(const orc_mesh *m, float peakVelocity, orc_context *ctx);
+
+/* ---------------- FEM ---------------- */
+/* assembles M, K, Kp, D, G, Kpi and (if withConvection) I; returns 0 on success */
+int orc_assemble(const orc_mesh *m, orc_context *ctx, int withConvection);
+void orc_context_free(orc_context *ctx);
+
+/* ---------------- linear algebra ---------------- */
+void orc_csr_free(orc_csr *a);
+void orc_spmv(const orc_csr *a, const double *x, double *y);
+int orc_slice(const orc_csr *a, int nr, const int *rows, int nc, const int *cols, orc_csr *out);
+int orc_coloring_build(const orc_csr *a, orc_coloring *out);
+void orc_coloring_free(orc_coloring *c);
+/* the color-permuted matrix P A P^T (rows and columns renumbered by coloring->perm) */
+int orc_permute(const orc_csr *a, const orc_coloring *c, orc_csr *out);
+
+/* multicolor Gauss-Seidel solve in the reference's cu::GaussSeidel semantics on the
+   color-permuted system: numCh planar channels, x in/out (original ordering), RMS residual
+   target checked every checkInterval iterations. Returns the last RMS per channel and
+   iteration index as cu::GaussSeidel reports it. */
+int orc_gs_solve(const orc_csr *a, const orc_coloring *c, int numCh, const double *b, double *x,
+                 int maxIters, double targetRms, int checkInterval, double *lastRms, int *lastIter);
+
+/* CG preconditioned by symmetric multicolor Gauss-Seidel (forward colors, then backward).
+   precond: 0 = none, 1 = multicolor SGS. Stops when ||r|| <= relTol * ||b||.
+   Returns 0 converged, 3 max iterations, 4 breakdown (p^T A p <= 0), 2 non-finite. */
+int orc_pcg(const orc_csr *a, const orc_coloring *c, int precond, const double *b, double *x,
+            int maxIters, double relTol, int *iters, double *relRes);
+
+/* y = (D+L) D^-1 (D+U) inverse applied to r in colored order (the preconditioner alone) */
+void orc_sgs_apply(const orc_csr *a, const orc_coloring *c, const double *r, double *z);
+
+/* ---------------- Chorin step ---------------- */
+typedef struct
+{
+    double nu, tau;
+    int velMethod;       /* 0 = multicolor GS (RMS target), 1 = PCG-SGS (relative tol) */
+    int velMaxIters;
+    double velTol;       /* RMS target for GS, relative tolerance for PCG */
+    int presMaxIters;
+    double presTol;      /* relative residual */
+} orc_chorin_cfg;
+
+typedef struct orc_chorin_s orc_chorin;
+orc_chorin *orc_chorin_create(const orc_context *ctx, const orc_chorin_cfg *cfg);
+void orc_chorin_free(orc_chorin *s);
+/* state access: u is planar [ux(N); uy(N)], p has P entries */
+void orc_chorin_get(const orc_chorin *s, double *u, double *p);
+void orc_chorin_set(orc_chorin *s, const double *u, const double *p);
+/* one time step; stats[0..5] = velocity iters (tentative), pressure iters, velocity iters
+   (final), pressure relative residual, tentative residual, final residual */
+int orc_chorin_step(orc_chorin *s, double *stats);
+
+/* the separate stages, exposed for parity tests */
+void orc_fastconv(const orc_context *ctx, double nu, const double *u, double *Avals);
+void orc_spmm2(const orc_csr *a, const double *vals, const double *x, double *y);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

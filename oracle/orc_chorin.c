@@ -1,0 +1,181 @@
+/*
+ * Oracle, Chorin projection time step in FP64.  Test infrastructure only.
+ *
+ * Order of operations per step (cpp/execs/NavierStokes/src/chorinCuda.cu:236-376, with the
+ * CPU twin cpp/execs/NavierStokes/src/chorinEigen.cpp:272-484):
+ *   C.values = I u;  A.values = nu K.values + C.values                 (:243-250)
+ *   rhs = A [ux uy];  acc = 0;  solve M acc = rhs (2 channels)         (:264-266)
+ *   u = u - tau acc;  impose Dirichlet velocity                        (:275-278)
+ *   div = -(1/tau) D u;  rhs_p = div[internal]                          (:297-298, :132-134)
+ *   solve Kp_int p_int = rhs_p, warm-started from the previous p_int   (:300; the reference's
+ *                                                                       solver keeps ioSol)
+ *   p = 0;  p[internal] = p_int                                        (:145-146)
+ *   g = G p;  acc = 0;  solve M acc = g;  u = u - tau acc;  Dirichlet   (:341-356)
+ * Velocity solves: method 0 is the multicolor Gauss-Seidel solver with an RMS target (the
+ * reference's "gs"), method 1 is CG with the multicolor SGS preconditioner to a relative
+ * tolerance.  Pressure: CG with the multicolor SGS preconditioner to a relative tolerance.
+ */
+#include "oracle.h"
+
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+
+struct orc_chorin_s
+{
+    const orc_context *ctx;
+    orc_chorin_cfg cfg;
+    orc_coloring colM, colP;
+    double *u, *p, *pInt, *Avals, *rhs, *acc, *div, *rhsP, *g;
+};
+
+orc_chorin *orc_chorin_create(const orc_context *ctx, const orc_chorin_cfg *cfg)
+{
+    orc_chorin *s = (orc_chorin *)calloc(1, sizeof *s);
+    s->ctx = ctx;
+    s->cfg = *cfg;
+    orc_coloring_build(&ctx->M, &s->colM);
+    orc_coloring_build(&ctx->Kpi, &s->colP);
+    const int N = ctx->N, P = ctx->P;
+    s->u = (double *)calloc(2 * N, sizeof(double));
+    s->p = (double *)calloc(P, sizeof(double));
+    s->pInt = (double *)calloc(ctx->nIntP + 1, sizeof(double));
+    s->Avals = (double *)calloc(ctx->K.nnz + 1, sizeof(double));
+    s->rhs = (double *)calloc(2 * N, sizeof(double));
+    s->acc = (double *)calloc(2 * N, sizeof(double));
+    s->div = (double *)calloc(P, sizeof(double));
+    s->rhsP = (double *)calloc(ctx->nIntP + 1, sizeof(double));
+    s->g = (double *)calloc(2 * N, sizeof(double));
+    for (int i = 0; i < ctx->nDir; i++)
+    {
+        s->u[ctx->dirIds[i]] = ctx->dirVx[i];
+        s->u[ctx->dirIds[i] + N] = 0.0;
+    }
+    return s;
+}
+
+void orc_chorin_free(orc_chorin *s)
+{
+    if (!s)
+        return;
+    orc_coloring_free(&s->colM);
+    orc_coloring_free(&s->colP);
+    free(s->u);
+    free(s->p);
+    free(s->pInt);
+    free(s->Avals);
+    free(s->rhs);
+    free(s->acc);
+    free(s->div);
+    free(s->rhsP);
+    free(s->g);
+    free(s);
+}
+
+void orc_chorin_get(const orc_chorin *s, double *u, double *p)
+{
+    if (u)
+        memcpy(u, s->u, sizeof(double) * 2 * s->ctx->N);
+    if (p)
+        memcpy(p, s->p, sizeof(double) * s->ctx->P);
+}
+
+void orc_chorin_set(orc_chorin *s, const double *u, const double *p)
+{
+    const orc_context *ctx = s->ctx;
+    if (u)
+        memcpy(s->u, u, sizeof(double) * 2 * ctx->N);
+    if (p)
+    {
+        memcpy(s->p, p, sizeof(double) * ctx->P);
+        for (int i = 0; i < ctx->nIntP; i++)
+            s->pInt[i] = p[ctx->intP[i]];
+    }
+}
+
+static void impose(orc_chorin *s)
+{
+    const orc_context *ctx = s->ctx;
+    for (int i = 0; i < ctx->nDir; i++)
+    {
+        s->u[ctx->dirIds[i]] = ctx->dirVx[i];
+        s->u[ctx->dirIds[i] + ctx->N] = 0.0;
+    }
+}
+
+/* mass solve for both channels; returns iterations (max over channels) and the residual */
+static int mass_solve(orc_chorin *s, const double *rhs, double *acc, double *res)
+{
+    const orc_context *ctx = s->ctx;
+    const int N = ctx->N;
+    memset(acc, 0, sizeof(double) * 2 * N);
+    if (s->cfg.velMethod == 0)
+    {
+        double rms[2];
+        int it = 0;
+        orc_gs_solve(&ctx->M, &s->colM, 2, rhs, acc, s->cfg.velMaxIters, s->cfg.velTol, 1, rms, &it);
+        *res = rms[0] > rms[1] ? rms[0] : rms[1];
+        return it;
+    }
+    int itMax = 0;
+    *res = 0;
+    for (int ch = 0; ch < 2; ch++)
+    {
+        int it = 0;
+        double rr = 0;
+        int st = orc_pcg(&ctx->M, &s->colM, 1, rhs + ch * N, acc + ch * N, s->cfg.velMaxIters, s->cfg.velTol, &it, &rr);
+        (void)st;
+        if (it > itMax)
+            itMax = it;
+        if (rr > *res)
+            *res = rr;
+    }
+    return itMax;
+}
+
+int orc_chorin_step(orc_chorin *s, double *stats)
+{
+    const orc_context *ctx = s->ctx;
+    const int N = ctx->N, P = ctx->P;
+    const double tau = s->cfg.tau;
+    double resT = 0, resF = 0, resP = 0;
+
+    orc_fastconv(ctx, s->cfg.nu, s->u, s->Avals);
+    orc_spmm2(&ctx->K, s->Avals, s->u, s->rhs);
+    int itT = mass_solve(s, s->rhs, s->acc, &resT);
+    for (int i = 0; i < 2 * N; i++)
+        s->u[i] -= tau * s->acc[i];
+    impose(s);
+
+    orc_spmv(&ctx->D, s->u, s->div);
+    const double invTau = -1.0 / tau;
+    for (int i = 0; i < P; i++)
+        s->div[i] *= invTau;
+    for (int i = 0; i < ctx->nIntP; i++)
+        s->rhsP[i] = s->div[ctx->intP[i]];
+    int itP = 0;
+    int st = orc_pcg(&ctx->Kpi, &s->colP, 1, s->rhsP, s->pInt, s->cfg.presMaxIters, s->cfg.presTol, &itP, &resP);
+    memset(s->p, 0, sizeof(double) * P);
+    for (int i = 0; i < ctx->nIntP; i++)
+        s->p[ctx->intP[i]] = s->pInt[i];
+
+    orc_spmv(&ctx->G, s->p, s->g);
+    int itF = mass_solve(s, s->g, s->acc, &resF);
+    for (int i = 0; i < 2 * N; i++)
+        s->u[i] -= tau * s->acc[i];
+    impose(s);
+
+    if (stats)
+    {
+        stats[0] = itT;
+        stats[1] = itP;
+        stats[2] = itF;
+        stats[3] = resP;
+        stats[4] = resT;
+        stats[5] = resF;
+    }
+    for (int i = 0; i < 2 * N; i++)
+        if (!isfinite(s->u[i]))
+            return 2;
+    return st == 2 ? 2 : 0;
+}
