@@ -1,0 +1,319 @@
+"""Benchmark of the Chorin projection time step on one GB300 (replicas on N GPUs).
+
+Workload (the DFG channel at h = 0.005): synthetic channel mesh with a cylinder, ~84k triangles,
+N = 169,672 P2 velocity nodes, P = 42,741 P1 pressure nodes; inflow peak 6.0 (U_max = 1.5),
+nu = 1e-3, tau = 5e-4, pressure solved to 1e-8 relative residual with CG preconditioned by multicolor
+symmetric Gauss-Seidel.  A "step" is one full time step (FastConvection + diffusion operator, SpMM,
+tentative mass solve, divergence, pressure solve, gradient, final mass solve, Dirichlet updates).
+
+``value`` is steps/s of the mixed-precision stepper (FP32 SpMV/sweeps/inner CG, FP64 refinement,
+dots and state) with everything resident in HBM; ``e2e`` is the same through the C ABI with the
+state uploaded from and downloaded to host memory every step.  The FP64 stepper is reported in
+``variants``.  ``--impl reference`` times the CPU restatement of the path (the C oracle, FP64).
+"""
+
+from __future__ import annotations
+
+import argparse
+import gzip
+import json
+import os
+import shutil
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+H = 0.005
+PEAK = 6.0        # reference inflow peakVelocity = 4 * U_max with U_max = 1.5
+NU = 1e-3
+TAU = 5e-4
+PRES_TOL = 1e-8
+VEL_TOL = 1e-8
+METRIC = "channel-flow steps/s: mixed-prec vs FP64 CG on 1 GB300 at 1e-8 rel; SpMV/CG HBM GB/s"
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def make_mesh(tmpdir: str, h: float, seed: int = 0) -> str:
+    from nsfemoptim_gb300 import meshgen
+    path = os.path.join(tmpdir, f"channel_h{h}_s{seed}.msh")
+    meshgen.write_gmsh41(path, meshgen.dfg_channel(h, seed=seed))
+    return path
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    def __init__(self, gpu: int):
+        self.proc = None
+        self.path = tempfile.mktemp(suffix=".csv")
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(gpu), f"--query-gpu={q}", "--format=csv,noheader,nounits",
+                                          "-lms", "200"], stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.f.close()
+        sm, mx, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        with open(self.path) as f:
+            for line in f:
+                parts = [x.strip() for x in line.split(",")]
+                if len(parts) < 9:
+                    continue
+                try:
+                    sm.append(float(parts[1]))
+                    mx = max(mx, float(parts[2]))
+                except ValueError:
+                    continue
+                for n, v in zip(names, parts[5:9]):
+                    if v.lower() == "active":
+                        reasons.add(n)
+        os.unlink(self.path)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def run_cpu_reference(mesh_path: str, steps: int, warmup: int):
+    """Time the oracle's FP64 Chorin step (the CPU restatement of the reference path)."""
+    import oracle
+    oracle.build()
+    m = oracle.Mesh(mesh_path)
+    ctx = oracle.Context(m, PEAK, True)
+    ch = oracle.Chorin(ctx, NU, TAU, vel_method=1, vel_max_iters=500, vel_tol=VEL_TOL, pres_max_iters=5000,
+                       pres_tol=PRES_TOL)
+    for _ in range(warmup):
+        ch.step()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        ch.step()
+    dt = time.perf_counter() - t0
+    return steps / dt, dt, ctx
+
+
+def bench_ours(args, rank, world, local_rank):
+    import numpy as np
+    import torch
+
+    import nsfemoptim_gb300 as G
+
+    torch.cuda.set_device(local_rank)
+    tmp = tempfile.mkdtemp()
+    try:
+        mesh_path = make_mesh(tmp, H, seed=rank)
+        t0 = time.perf_counter()
+        mesh = G.load_gmsh(mesh_path)
+        ctx = G.build_chorin_context(mesh, PEAK)
+        setup_s = time.perf_counter() - t0
+        N, P, nip = ctx.N, ctx.P, len(ctx.int_p)
+
+        def stepper(precision, graph=True):
+            return G.ChorinStepper(ctx, NU, TAU, precision=precision, vel_method=1, vel_max_iters=500,
+                                   vel_tol=VEL_TOL, pres_max_iters=5000, pres_tol=PRES_TOL, check_interval=8,
+                                   use_graph=graph, max_outer=4, inner_tol=1e-4)
+
+        stream = torch.cuda.Stream()
+        sp = stream.cuda_stream
+
+        def timed(st, steps, warm):
+            with torch.cuda.stream(stream):
+                st.step(warm, sp)
+                torch.cuda.synchronize()
+                if world > 1:
+                    torch.distributed.barrier()
+                torch.cuda.synchronize()
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                st.step(steps, sp)
+                e1.record(stream)
+                torch.cuda.synchronize()
+                if world > 1:
+                    torch.distributed.barrier()
+                return e0.elapsed_time(e1) / 1e3
+
+        # ---- main line: mixed precision, graph-captured steps, state resident in HBM
+        mixed = stepper(G.NSF_PREC_MIXED)
+        clocks = Clocks(local_rank) if rank == 0 else None
+        t_mixed = timed(mixed, args.steps, args.warmup)
+        clk = clocks.stop() if clocks else None
+        st_mixed = mixed.stats()
+
+        # ---- FP64 drop-in on the same workload
+        f64 = stepper(G.NSF_PREC_F64)
+        t_f64 = timed(f64, max(1, args.steps // 2), args.warmup)
+        st_f64 = f64.stats()
+        u_m, p_m = mixed.state()
+
+        # ---- e2e through the C ABI with host buffers: H2D state, step, D2H state every step
+        u_h = np.zeros(2 * N)
+        p_h = np.zeros(P)
+        mixed.get_state_into(u_h, p_h)
+        e2e_steps = max(3, args.steps // 4)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(e2e_steps):
+            mixed.set_state(u_h, p_h)
+            mixed.step(1, sp)
+            mixed.get_state_into(u_h, p_h)
+        t_e2e = time.perf_counter() - t0
+
+        # ---- dominant kernel alone: FastConvection SpMV (I: nnz(K) x 2N) fused with the nu K add
+        Ih = ctx.matrix("I")
+        Kh = ctx.matrix("K")
+        I32 = G.CsrF.from_host(Ih, dtype=G.NSF_F32)
+        u32 = torch.tensor(u_m, dtype=torch.float32, device="cuda")
+        K32 = torch.tensor(Kh.values, dtype=torch.float32, device="cuda")
+        A32 = torch.zeros_like(K32)
+        reps = 20
+        with torch.cuda.stream(stream):
+            for _ in range(3):
+                G.fastconv_apply(I32, K32, NU, u32, A32, sp)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            for _ in range(reps):
+                G.fastconv_apply(I32, K32, NU, u32, A32, sp)
+            e1.record(stream)
+            torch.cuda.synchronize()
+        t_fc = e0.elapsed_time(e1) / 1e3 / reps
+        nnzI, rowsI = Ih.nnz, Ih.rows
+        fc_bytes = nnzI * (4 + 4) + (rowsI + 1) * 4 + 2 * N * 4 + 2 * rowsI * 4
+
+        # kernels per step (one eager FP64 step counted exactly by the library's launch counter)
+        cnt = stepper(G.NSF_PREC_MIXED, graph=False)
+        cnt.set_state(u_m, p_m)
+        k0 = G.kernel_launches()
+        cnt.step(1)
+        per_step = G.kernel_launches() - k0
+
+        times = [t_mixed]
+        if world > 1:
+            tt = torch.tensor([t_mixed, t_f64, t_e2e], dtype=torch.float64, device="cuda")
+            torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+            t_mixed, t_f64, t_e2e = tt.tolist()
+        if rank != 0:
+            return None
+
+        hbm, kind = peaks()
+        achieved = fc_bytes / t_fc / 1e9
+        steps_s = world * args.steps / t_mixed
+        line = {
+            "metric": METRIC,
+            "value": round(steps_s, 3),
+            "unit": "steps/s",
+            "n_gpus": world,
+            "steps": args.steps,
+            "warmup": args.warmup,
+            "ms_per_step": round(1e3 * t_mixed / args.steps, 4),
+            "higher_is_better": True,
+            "scaling": "weak",
+            "vs_baseline": None,
+            "dtype": "f32-inner/f64-refine",
+            "data": "synthetic (seeded DFG channel mesh, h=0.005)",
+            "config": {"workload": "DFG channel h=0.005, Umax=1.5, nu=1e-3, tau=5e-4, P2/P1, "
+                                   "pressure PCG-SGS to 1e-8 rel", "triangles": mesh.num_tri, "N": N, "P": P,
+                       "internal_pressure": nip, "nnz_I": nnzI, "parallelism": f"replicas x{world}",
+                       "l2": "working set > L2 (FastConvection matrix %.0f MB FP32)" % (nnzI * 8 / 1e6),
+                       "graph": True, "setup_s": round(setup_s, 2)},
+            "e2e": {"value": round(world * e2e_steps / t_e2e, 3), "unit": "steps/s",
+                    "h2d_bytes_per_step": (2 * N + P) * 8, "d2h_bytes_per_step": (2 * N + P) * 8},
+            "gpu_launches": int(per_step * args.steps),
+            "roofline": {"bound": "hbm", "kernel": "kFastConv<float> (I u + nu K)", "achieved": round(achieved, 1),
+                         "peak": hbm, "unit": "GB/s", "frac": round(achieved / hbm, 4),
+                         "peak_kind": kind, "algorithmic_bytes": fc_bytes, "launch_us": round(t_fc * 1e6, 2),
+                         "traffic": None},
+            "variants": {"fp64": {"steps_per_s": round(world * max(1, args.steps // 2) / t_f64, 3),
+                                  "ms_per_step": round(1e3 * t_f64 / max(1, args.steps // 2), 4),
+                                  "stats": st_f64},
+                         "mixed_stats": st_mixed},
+        }
+        if clk:
+            line["clocks"] = clk
+        return line
+    finally:
+        shutil.rmtree(tmp, ignore_errors=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--cpu-sample-steps", type=int, default=3)
+    args = ap.parse_args()
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        tmp = tempfile.mkdtemp()
+        try:
+            path = make_mesh(tmp, H, 0)
+            k = max(1, min(args.steps, 10))
+            sps, dt, ctx = run_cpu_reference(path, k, min(args.warmup, 2))
+        finally:
+            shutil.rmtree(tmp, ignore_errors=True)
+        line = {"impl": "reference", "metric": METRIC, "value": round(sps, 4), "unit": "steps/s", "n_gpus": 0,
+                "steps": k, "warmup": min(args.warmup, 2), "ms_per_step": round(1e3 * dt / k, 2),
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+                "data": "synthetic (seeded DFG channel mesh, h=0.005)",
+                "config": {"workload": "DFG channel h=0.005, Umax=1.5, nu=1e-3, tau=5e-4, P2/P1, "
+                                       "pressure PCG-SGS to 1e-8 rel", "N": ctx.N, "P": ctx.P},
+                "cpu_baseline": {"value": round(sps, 4), "unit": "steps/s", "cores": 1, "kind": "port",
+                                 "sample": f"{k} time steps after {min(args.warmup, 2)} warm-up steps, FP64 C oracle"},
+                "e2e": {"value": round(sps, 4), "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line))
+        return
+
+    if world > 1:
+        import torch
+        torch.distributed.init_process_group("nccl")
+    line = bench_ours(args, rank, world, local_rank)
+    if rank == 0 and line is not None:
+        # CPU baseline on a bounded sample of the same workload (rank 0, N = 1 only)
+        if world == 1 and args.cpu_sample_steps > 0:
+            tmp = tempfile.mkdtemp()
+            try:
+                path = make_mesh(tmp, H, 0)
+                sps, dt, _ = run_cpu_reference(path, args.cpu_sample_steps, 1)
+                line["cpu_baseline"] = {"value": round(sps, 4), "unit": "steps/s", "cores": 1, "kind": "port",
+                                        "sample": f"{args.cpu_sample_steps} time steps (after 1 warm-up) of the same "
+                                                  f"workload, FP64 C oracle, single thread"}
+            finally:
+                shutil.rmtree(tmp, ignore_errors=True)
+        print(json.dumps(line))
+    if world > 1:
+        import torch
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

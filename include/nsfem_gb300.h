@@ -1,0 +1,181 @@
+/*
+ * nsfem_gb300 — C ABI of the GB300-native Chorin-projection path.
+ *
+ * Plain C: opaque handles, int32 indices, host or device pointers as documented per call,
+ * cudaStream_t passed as void*.  Every call returns an nsf_status; nsf_last_error() gives a
+ * one-line message for the calling thread.  Device pointers are owned by the caller unless a
+ * handle says otherwise.  Nothing here uses cuSPARSE, cuBLAS or any other vendor math library.
+ *
+ * Each entry point names the reference interface (kosyonikolov/NsFemOptim, paths inside that
+ * project) that it replaces.
+ */
+#ifndef NSFEM_GB300_H
+#define NSFEM_GB300_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum
+{
+    NSF_OK = 0,
+    NSF_ERR_INVALID_ARG = 1,  /* bad size, pointer, unsorted/out-of-range CSR, missing diagonal */
+    NSF_ERR_NONFINITE = 2,    /* a solver residual or the state became NaN/Inf */
+    NSF_ERR_MAXITER = 3,      /* the iteration cap was reached before the tolerance */
+    NSF_ERR_BREAKDOWN = 4,    /* CG breakdown: p^T A p <= 0 (matrix not SPD) */
+    NSF_ERR_CUDA = 5,         /* a CUDA runtime call failed */
+    NSF_ERR_IO = 6,           /* file not found / parse error */
+    NSF_ERR_NOT_SUPPORTED = 7
+} nsf_status;
+
+typedef enum
+{
+    NSF_F32 = 0,
+    NSF_F64 = 1
+} nsf_dtype;
+
+typedef enum
+{
+    NSF_PREC_F64 = 0,   /* everything in FP64 */
+    NSF_PREC_MIXED = 1  /* FP32 SpMV/sweeps/inner CG, FP64 residual refinement, dots and state */
+} nsf_precision;
+
+const char *nsf_last_error(void);
+const char *nsf_status_string(int status);
+int nsf_version(void);
+
+/* ======================================================================= host setup ===== */
+
+typedef struct nsf_mesh_s *nsf_mesh;
+
+/* gmsh MSH 4.1 ASCII file -> corner mesh -> P2 velocity and P1 pressure numbering.
+   Replaces mesh::parseGmsh (cpp/libs/Mesh/src/gmsh.cpp:451), mesh::parseTriangleGmsh
+   (cpp/libs/Mesh/src/io.cpp:65) and mesh::createMesh (cpp/libs/Mesh/src/concreteMesh.cpp:78). */
+int nsf_mesh_load_gmsh(const char *path, nsf_mesh *out);
+/* counts[0..5] = corner nodes, triangles, border elements, P2 nodes (N), P1 nodes (P), groups */
+int nsf_mesh_counts(nsf_mesh mesh, int *counts);
+/* copies: vElem[6*T] (c0, m01, c1, m12, c2, m20), pElem[3*T], vXY[2*N] float, vBorder[6*B]
+   (triangle, side, group, A, mid, B); any pointer may be NULL */
+int nsf_mesh_arrays(nsf_mesh mesh, int *vElem, int *pElem, float *vXY, int *vBorder);
+/* name of border group i (the string lives as long as the mesh) */
+const char *nsf_mesh_group(nsf_mesh mesh, int i);
+void nsf_mesh_destroy(nsf_mesh mesh);
+
+typedef struct nsf_context_s *nsf_context;
+
+/* Channel-flow context: Dirichlet velocity on Left/Top/Bottom/Circle with the parabolic inflow
+   u = peak*y*(0.41-y)/0.41^2 on Left, Dirichlet pressure on Right, FP64 assembly of the mass M,
+   stiffness K, pressure stiffness Kp (and its internal slice), divergence D (P x 2N), gradient
+   G (2N x P) and the FastConvection integration matrix I (nnz(K) x 2N).
+   Replaces buildChorinContext (cpp/execs/NavierStokes/src/buildContext.cpp:17-142) with
+   fem::buildChorinCsrMatrices (cpp/libs/Fem/src/chorinCsr.cpp:437-502) and fem::FastConvection
+   (cpp/libs/Fem/src/fastConvection.cpp:9-100).  nThreads <= 0 picks the hardware count. */
+int nsf_context_build(nsf_mesh mesh, float peakVelocity, int nThreads, nsf_context *out);
+/* sizes[0..12] = N, P, nDir, nDirP, nIntV, nIntP, nnz(M), nnz(K), nnz(Kp), nnz(Kpi), nnz(D),
+   nnz(G), nnz(I) */
+int nsf_context_sizes(nsf_context ctx, int *sizes);
+/* which: 0 M, 1 K, 2 Kp, 3 Kpi, 4 D, 5 G, 6 I; copies the host CSR (any pointer may be NULL) */
+int nsf_context_matrix(nsf_context ctx, int which, int *rowStart, int *col, double *val);
+/* dirIds[nDir] (sorted), dirVx[nDir] (x inflow values; y values are 0), dirPIds[nDirP],
+   intV[nIntV], intP[nIntP]; any pointer may be NULL */
+int nsf_context_lists(nsf_context ctx, int *dirIds, double *dirVx, int *dirPIds, int *intV, int *intP);
+void nsf_context_destroy(nsf_context ctx);
+
+/* Smallest-last + greedy coloring of the adjacency graph of a square CSR pattern, partitions
+   sorted by id and concatenated.  perm[n] (new -> old), partStart[n + 1] (first *nColors + 1
+   entries used).  Replaces the coloring in cu::GaussSeidel's constructor
+   (cpp/libs/CudaUtils/src/gaussSeidel.cu:132-155) over linalg::buildSmallestLastOrdering and
+   linalg::partitionGraphGreedy (cpp/libs/LinAlg/src/graphs.cpp:64-176). */
+int nsf_coloring(int n, const int *rowStart, const int *col, int *perm, int *partStart, int *nColors);
+
+/* ===================================================================== device CSR ======= */
+
+typedef struct nsf_csr_s *nsf_csr;
+
+/* Upload a host CSR (0-based, rowStart[rows] == nnz, columns sorted and in range, values in
+   dtype).  Validated before upload.  Replaces cu::csrF::csrF (cpp/libs/CudaUtils/src/csrF.cu:5-9). */
+int nsf_csr_create(int rows, int cols, int nnz, const int *rowStart, const int *col, const void *values,
+                   int dtype, nsf_csr *out);
+/* replace the values (host pointer when onDevice == 0, else a device pointer) */
+int nsf_csr_update_values(nsf_csr a, const void *values, int onDevice, void *stream);
+/* device pointers of the stored arrays */
+int nsf_csr_device(nsf_csr a, int **rowStart, int **col, void **values);
+void nsf_csr_destroy(nsf_csr a);
+
+/* y = alpha A x + beta y on device vectors of the matrix dtype.
+   Replaces cu::spmv::compute (cpp/libs/CudaUtils/src/spmv.cu:48-63). */
+int nsf_spmv(nsf_csr a, const void *x, void *y, double alpha, double beta, void *stream);
+/* Y[:, c] = A X[:, c] for nrhs planar channels (column c starts at c * ld).
+   Replaces cu::spmm::compute (cpp/libs/CudaUtils/src/spmm.cu:53-70). */
+int nsf_spmm(nsf_csr a, int nrhs, const void *X, int ldx, void *Y, int ldy, void *stream);
+/* Avals = nu * Kvals + I u, the linearised advection update fused with the diffusion add.
+   Replaces fcSpmv.compute + cublasSgeam (cpp/execs/NavierStokes/src/chorinCuda.cu:243-250). */
+int nsf_fastconv_apply(nsf_csr I, const void *Kvals, double nu, const void *u, void *Avals, void *stream);
+
+/* ======================================================================== solvers ======= */
+
+typedef struct nsf_solver_s *nsf_solver;
+
+/* Linear solver on a square SPD CSR given on the host (FP64 values).
+   method "gs": multicolor Gauss-Seidel iterated to an RMS residual target (the reference's
+                "gs", cu::GaussSeidel, cpp/libs/CudaUtils/src/gaussSeidel.cu:121-404);
+   method "pcg": CG preconditioned by symmetric multicolor Gauss-Seidel, stops at
+                ||b - A x|| <= target * ||b||.
+   precision NSF_PREC_MIXED runs the sweeps/CG in FP32 inside an FP64 refinement loop.
+   Replaces cu::createSolver (cpp/libs/CudaUtils/src/solvers/solverFactory.cu:209-237) and the
+   cu::AbstractSolver interface (cpp/libs/CudaUtils/include/cu/solvers/abstractSolver.h:8-32). */
+int nsf_solver_create(const char *method, int numCh, int n, const int *rowStart, const int *col,
+                      const double *values, int precision, int maxIters, double target, int checkInterval,
+                      nsf_solver *out);
+/* Solve A x = b for numCh planar channels; b and x are device FP64 vectors of numCh * n
+   entries; x holds the initial guess on entry.  Synchronous: returns the solver status. */
+int nsf_solver_solve(nsf_solver s, const double *b, double *x, void *stream);
+/* iters: iterations of the last solve; rms[numCh]: RMS residual per channel (getLastMse);
+   rel[numCh]: relative residual per channel; any pointer may be NULL */
+int nsf_solver_stats(nsf_solver s, int *iters, double *rms, double *rel);
+int nsf_solver_set(nsf_solver s, int maxIters, double target, int checkInterval);
+void nsf_solver_destroy(nsf_solver s);
+
+/* ================================================================= Chorin stepper ======= */
+
+typedef struct
+{
+    double nu;            /* viscosity */
+    double tau;           /* time step */
+    int precision;        /* nsf_precision */
+    int velMethod;        /* 0: "gs" (RMS target velTol, relative), 1: "pcg" (relative velTol) */
+    int velMaxIters;
+    double velTol;
+    int presMaxIters;
+    double presTol;       /* relative pressure residual */
+    int checkInterval;    /* eager mode: iterations between device->host convergence checks */
+    int useGraph;         /* 1: capture the step once into a CUDA graph whose solver loops are
+                             conditional while nodes (no host synchronisation); 0: eager */
+    int maxOuter;         /* mixed precision: FP64 refinement passes per solve */
+    double innerTol;      /* mixed precision: relative tolerance of each FP32 inner solve */
+} nsf_chorin_config;
+
+typedef struct nsf_chorin_s *nsf_chorin;
+
+/* Device-resident time stepper over a context: uploads the color-permuted operators once.
+   Replaces the setup and loop body of solveNsChorinCuda
+   (cpp/execs/NavierStokes/src/chorinCuda.cu:154-379). */
+int nsf_chorin_create(nsf_context ctx, const nsf_chorin_config *cfg, nsf_chorin *out);
+/* advance nSteps time steps on the stepper's stream (stream may be NULL: default stream) */
+int nsf_chorin_step(nsf_chorin s, int nSteps, void *stream);
+/* copy the state to/from host memory in the original numbering: u[2N] planar, p[P] */
+int nsf_chorin_get_state(nsf_chorin s, double *u, double *p, void *stream);
+int nsf_chorin_set_state(nsf_chorin s, const double *u, const double *p, void *stream);
+/* stats[0..7] of the last step: tentative iterations, pressure iterations, final iterations,
+   pressure relative residual, tentative relative residual, final relative residual,
+   pressure refinement sweeps (mixed), status */
+int nsf_chorin_stats(nsf_chorin s, double *stats);
+/* number of kernels this library launched since the process started */
+long long nsf_kernel_launches(void);
+void nsf_chorin_destroy(nsf_chorin s);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

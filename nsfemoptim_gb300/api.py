@@ -1,0 +1,383 @@
+"""Python mirror of the reference's matrix/solver interface over the C ABI.
+
+Names, argument meaning and error behaviour follow the reference's ``cu::`` classes
+(``cpp/libs/CudaUtils/include/cu/``) and setup functions:
+
+* ``load_gmsh``                  mesh::parseTriangleGmsh + mesh::createMesh (P2 and P1)
+* ``build_chorin_context``       buildChorinContext (cpp/execs/NavierStokes/src/buildContext.cpp:17)
+* ``CsrF``                       cu::csrF (device CSR; FP64 or FP32 values)
+* ``Spmv`` / ``Spmm``            cu::spmv / cu::spmm (default x/b members, ``compute()``)
+* ``create_solver``              cu::createSolver returning an ``AbstractSolver`` with
+                                 getNumCh / getLastMse / getLastIterations / getRhs / getSol /
+                                 solve / setMaxIters / setTargetMse / setMseCheckInterval
+* ``ChorinStepper``              the device time loop of solveNsChorinCuda
+
+Device vectors are torch CUDA tensors (used only as device memory); failures raise NsfError
+with the library's status code, as the reference throws std::runtime_error.
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from ._lib import (NSF_F32, NSF_F64, NSF_PREC_F64, NSF_PREC_MIXED, ChorinConfig, NsfError, check, lib, vp)
+
+
+def _i32(a):
+    return np.ascontiguousarray(a, dtype=np.int32)
+
+
+def _p(a, ct):
+    return a.ctypes.data_as(C.POINTER(ct))
+
+
+def _dptr(t):
+    return C.c_void_p(int(t.data_ptr()))
+
+
+def _torch():
+    import torch
+    return torch
+
+
+# ------------------------------------------------------------------------------------ host setup
+
+class Mesh:
+    """P2 velocity / P1 pressure mesh read from a gmsh MSH 4.1 file."""
+
+    def __init__(self, path: str):
+        h = vp()
+        check(lib().nsf_mesh_load_gmsh(path.encode(), C.byref(h)))
+        self._h = h
+        c = (C.c_int * 6)()
+        check(lib().nsf_mesh_counts(h, c))
+        self.num_corner, self.num_tri, self.num_border, self.N, self.P, n_groups = list(c)
+        self.groups = [lib().nsf_mesh_group(h, i).decode() for i in range(n_groups)]
+
+    def arrays(self):
+        T, B = self.num_tri, self.num_border
+        v_elem = np.zeros(6 * T, np.int32)
+        p_elem = np.zeros(3 * T, np.int32)
+        v_xy = np.zeros(2 * self.N, np.float32)
+        v_border = np.zeros(6 * B, np.int32)
+        check(lib().nsf_mesh_arrays(self._h, _p(v_elem, C.c_int), _p(p_elem, C.c_int), _p(v_xy, C.c_float),
+                                    _p(v_border, C.c_int)))
+        return v_elem.reshape(T, 6), p_elem.reshape(T, 3), v_xy.reshape(-1, 2), v_border.reshape(B, 6)
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            lib().nsf_mesh_destroy(self._h)
+            self._h = None
+
+
+def load_gmsh(path: str) -> Mesh:
+    return Mesh(path)
+
+
+class HostCsr:
+    def __init__(self, rows, cols, rowStart, column, values):
+        self.rows, self.cols = rows, cols
+        self.rowStart, self.column, self.values = rowStart, column, values
+
+    @property
+    def nnz(self):
+        return int(self.column.shape[0])
+
+
+class ChorinContext:
+    """Boundary lists and FP64 operators of the channel problem (fem::ChorinContextF)."""
+
+    MATRICES = ("M", "K", "Kp", "Kpi", "D", "G", "I")
+
+    def __init__(self, mesh: Mesh, peak_velocity: float, n_threads: int = 0):
+        h = vp()
+        check(lib().nsf_context_build(mesh._h, C.c_float(peak_velocity), n_threads, C.byref(h)))
+        self._h = h
+        s = (C.c_int * 13)()
+        check(lib().nsf_context_sizes(h, s))
+        s = list(s)
+        self.N, self.P, n_dir, n_dir_p, n_int_v, n_int_p = s[:6]
+        self._nnz = dict(zip(self.MATRICES, s[6:]))
+        self.dir_ids = np.zeros(n_dir, np.int32)
+        self.dir_vx = np.zeros(n_dir, np.float64)
+        self.dir_p_ids = np.zeros(n_dir_p, np.int32)
+        self.int_v = np.zeros(n_int_v, np.int32)
+        self.int_p = np.zeros(n_int_p, np.int32)
+        check(lib().nsf_context_lists(h, _p(self.dir_ids, C.c_int), _p(self.dir_vx, C.c_double),
+                                      _p(self.dir_p_ids, C.c_int), _p(self.int_v, C.c_int),
+                                      _p(self.int_p, C.c_int)))
+        self._cache = {}
+
+    def _shape(self, name):
+        N, P, nip = self.N, self.P, len(self.int_p)
+        return {"M": (N, N), "K": (N, N), "Kp": (P, P), "Kpi": (nip, nip), "D": (P, 2 * N), "G": (2 * N, P),
+                "I": (self._nnz["K"], 2 * N)}[name]
+
+    def matrix(self, name: str) -> HostCsr:
+        if name not in self._cache:
+            rows, cols = self._shape(name)
+            nnz = self._nnz[name]
+            rs = np.zeros(rows + 1, np.int32)
+            ci = np.zeros(nnz, np.int32)
+            va = np.zeros(nnz, np.float64)
+            check(lib().nsf_context_matrix(self._h, self.MATRICES.index(name), _p(rs, C.c_int), _p(ci, C.c_int),
+                                           _p(va, C.c_double)))
+            self._cache[name] = HostCsr(rows, cols, rs, ci, va)
+        return self._cache[name]
+
+    def __getattr__(self, name):
+        if name in ChorinContext.MATRICES:
+            return self.matrix(name)
+        raise AttributeError(name)
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            lib().nsf_context_destroy(self._h)
+            self._h = None
+
+
+def build_chorin_context(mesh: Mesh, peak_velocity: float, n_threads: int = 0) -> ChorinContext:
+    return ChorinContext(mesh, peak_velocity, n_threads)
+
+
+def coloring(rowStart, column):
+    """(perm, partStart) of the smallest-last + greedy coloring (cu::GaussSeidel's ordering)."""
+    rs, ci = _i32(rowStart), _i32(column)
+    n = len(rs) - 1
+    perm = np.zeros(n, np.int32)
+    part = np.zeros(n + 1, np.int32)
+    nc = C.c_int(0)
+    check(lib().nsf_coloring(n, _p(rs, C.c_int), _p(ci, C.c_int), _p(perm, C.c_int), _p(part, C.c_int),
+                             C.byref(nc)))
+    return perm, part[: nc.value + 1].copy()
+
+
+# ------------------------------------------------------------------------------------ device CSR
+
+class CsrF:
+    """Device CSR (cu::csrF).  ``values`` are FP64 or FP32 (``dtype``)."""
+
+    def __init__(self, rows, cols, rowStart, column, values, dtype=NSF_F64):
+        self.rows, self.cols = int(rows), int(cols)
+        rs, ci = _i32(rowStart), _i32(column)
+        self.nnz = int(ci.shape[0])
+        self.dtype = dtype
+        va = np.ascontiguousarray(values, dtype=np.float64 if dtype == NSF_F64 else np.float32)
+        h = vp()
+        check(lib().nsf_csr_create(self.rows, self.cols, self.nnz, _p(rs, C.c_int), _p(ci, C.c_int),
+                                   va.ctypes.data_as(vp), dtype, C.byref(h)))
+        self._h = h
+
+    @staticmethod
+    def from_host(a: HostCsr, dtype=NSF_F64) -> "CsrF":
+        return CsrF(a.rows, a.cols, a.rowStart, a.column, a.values, dtype)
+
+    @property
+    def torch_dtype(self):
+        t = _torch()
+        return t.float64 if self.dtype == NSF_F64 else t.float32
+
+    def update_values(self, values, stream=None):
+        t = _torch()
+        if isinstance(values, t.Tensor) and values.is_cuda:
+            check(lib().nsf_csr_update_values(self._h, _dptr(values), 1, vp(stream)))
+        else:
+            va = np.ascontiguousarray(values, dtype=np.float64 if self.dtype == NSF_F64 else np.float32)
+            check(lib().nsf_csr_update_values(self._h, va.ctypes.data_as(vp), 0, vp(stream)))
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            lib().nsf_csr_destroy(self._h)
+            self._h = None
+
+
+def spmv(a: CsrF, x, y, alpha=1.0, beta=0.0, stream=None):
+    check(lib().nsf_spmv(a._h, _dptr(x), _dptr(y), alpha, beta, vp(stream)))
+    return y
+
+
+def spmm(a: CsrF, X, Y, nrhs: int, stream=None):
+    check(lib().nsf_spmm(a._h, nrhs, _dptr(X), a.cols, _dptr(Y), a.rows, vp(stream)))
+    return Y
+
+
+def fastconv_apply(I: CsrF, K_values, nu: float, u, A_values, stream=None):
+    """A = nu * K + I u (the reference's FastConvection SpMV followed by the Sgeam add)."""
+    check(lib().nsf_fastconv_apply(I._h, _dptr(K_values), nu, _dptr(u), _dptr(A_values), vp(stream)))
+    return A_values
+
+
+class Spmv:
+    """cu::spmv: b = M x with default operand vectors."""
+
+    def __init__(self, mat: CsrF):
+        t = _torch()
+        self.mat = mat
+        self.x = t.zeros(mat.cols, dtype=mat.torch_dtype, device="cuda")
+        self.b = t.zeros(mat.rows, dtype=mat.torch_dtype, device="cuda")
+
+    def compute(self, x=None, b=None):
+        return spmv(self.mat, self.x if x is None else x, self.b if b is None else b)
+
+
+class Spmm:
+    """cu::spmm: planar multi-channel b = M x."""
+
+    def __init__(self, mat: CsrF, numCh: int):
+        t = _torch()
+        self.mat, self.numCh = mat, numCh
+        self.x = t.zeros(mat.cols * numCh, dtype=mat.torch_dtype, device="cuda")
+        self.b = t.zeros(mat.rows * numCh, dtype=mat.torch_dtype, device="cuda")
+
+    def compute(self, x=None, b=None):
+        return spmm(self.mat, self.x if x is None else x, self.b if b is None else b, self.numCh)
+
+
+# ------------------------------------------------------------------------------------ solvers
+
+class AbstractSolver:
+    """cu::AbstractSolver over nsf_solver.  getRhs()/getSol() are the device IO vectors; getSol()
+    is also the initial guess (zero it before solve() for a cold start, as the reference's callers
+    do)."""
+
+    def __init__(self, name, numCh, m: HostCsr, maxIters, targetMse, mseCheckInterval, precision=NSF_PREC_F64):
+        t = _torch()
+        if m.rows != m.cols:
+            raise NsfError(1, "matrix must be square")
+        h = vp()
+        rs, ci = _i32(m.rowStart), _i32(m.column)
+        va = np.ascontiguousarray(m.values, dtype=np.float64)
+        check(lib().nsf_solver_create(name.encode(), numCh, m.rows, _p(rs, C.c_int), _p(ci, C.c_int),
+                                      _p(va, C.c_double), precision, maxIters, targetMse, mseCheckInterval,
+                                      C.byref(h)))
+        self._h = h
+        self.name, self.numCh, self.n = name, numCh, m.rows
+        self.maxIters, self.targetMse, self.mseCheckInterval = maxIters, targetMse, mseCheckInterval
+        self._rhs = t.zeros(numCh * m.rows, dtype=t.float64, device="cuda")
+        self._sol = t.zeros(numCh * m.rows, dtype=t.float64, device="cuda")
+        self.last_status = 0
+
+    def getNumCh(self):
+        return self.numCh
+
+    def getRhs(self):
+        return self._rhs
+
+    def getSol(self):
+        return self._sol
+
+    def solve(self, raise_on_status: bool = False):
+        st = lib().nsf_solver_solve(self._h, _dptr(self._rhs), _dptr(self._sol), None)
+        self.last_status = st
+        if st != 0 and (raise_on_status or st not in (2, 3, 4)):
+            check(st)
+        return st
+
+    def _stats(self):
+        it = C.c_int(0)
+        rms = (C.c_double * self.numCh)()
+        rel = (C.c_double * self.numCh)()
+        check(lib().nsf_solver_stats(self._h, C.byref(it), rms, rel))
+        return it.value, list(rms), list(rel)
+
+    def getLastMse(self, ch: int = -1):
+        _, rms, _ = self._stats()
+        if ch < 0:
+            return float(np.sqrt(np.sum(np.square(rms))))
+        return rms[ch] if ch < self.numCh else -1.0
+
+    def getLastRelativeResidual(self, ch: int = 0):
+        return self._stats()[2][ch]
+
+    def getLastIterations(self):
+        return self._stats()[0]
+
+    def setMaxIters(self, n):
+        self.maxIters = n
+        check(lib().nsf_solver_set(self._h, self.maxIters, self.targetMse, self.mseCheckInterval))
+
+    def setTargetMse(self, mse):
+        self.targetMse = mse
+        check(lib().nsf_solver_set(self._h, self.maxIters, self.targetMse, self.mseCheckInterval))
+
+    def setMseCheckInterval(self, k):
+        if k < 1:
+            raise NsfError(1, "MSE check interval should be at least 1")
+        self.mseCheckInterval = k
+        check(lib().nsf_solver_set(self._h, self.maxIters, self.targetMse, self.mseCheckInterval))
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            lib().nsf_solver_destroy(self._h)
+            self._h = None
+
+
+def create_solver(name: str, numCh: int, m: HostCsr, maxIters: int, targetMse: float, mseCheckInterval: int,
+                  precision: int = NSF_PREC_F64) -> AbstractSolver:
+    """cu::createSolver: "gs" (multicolor Gauss-Seidel, absolute RMS target) or "pcg" (CG with the
+    multicolor symmetric Gauss-Seidel preconditioner, relative target)."""
+    if numCh < 1:
+        raise NsfError(1, f"Invalid number of channels for solver: {numCh}")
+    if mseCheckInterval < 1:
+        raise NsfError(1, f"Invalid MSE check interval for solver: {mseCheckInterval}")
+    if name not in ("gs", "pcg"):
+        raise NsfError(1, f"Invalid solver name: {name}")
+    return AbstractSolver(name, numCh, m, maxIters, targetMse, mseCheckInterval, precision)
+
+
+# ------------------------------------------------------------------------------------ stepper
+
+class ChorinStepper:
+    """Device-resident Chorin projection time stepper (the loop of solveNsChorinCuda)."""
+
+    def __init__(self, ctx: ChorinContext, nu: float, tau: float, precision: int = NSF_PREC_F64,
+                 vel_method: int = 1, vel_max_iters: int = 200, vel_tol: float = 1e-10,
+                 pres_max_iters: int = 2000, pres_tol: float = 1e-10, check_interval: int = 8,
+                 use_graph: bool = True, max_outer: int = 4, inner_tol: float = 1e-4):
+        self.ctx = ctx
+        self.cfg = ChorinConfig(nu, tau, precision, vel_method, vel_max_iters, vel_tol, pres_max_iters, pres_tol,
+                                check_interval, int(use_graph), max_outer, inner_tol)
+        h = vp()
+        check(lib().nsf_chorin_create(ctx._h, C.byref(self.cfg), C.byref(h)))
+        self._h = h
+        self.N, self.P = ctx.N, ctx.P
+
+    def step(self, n: int = 1, stream=None):
+        check(lib().nsf_chorin_step(self._h, n, vp(stream)))
+
+    def state(self):
+        u = np.zeros(2 * self.N, np.float64)
+        p = np.zeros(self.P, np.float64)
+        check(lib().nsf_chorin_get_state(self._h, _p(u, C.c_double), _p(p, C.c_double), None))
+        return u, p
+
+    def get_state_into(self, u: np.ndarray, p: np.ndarray):
+        check(lib().nsf_chorin_get_state(self._h, _p(u, C.c_double), _p(p, C.c_double), None))
+
+    def set_state(self, u, p):
+        u = np.ascontiguousarray(u, np.float64)
+        p = np.ascontiguousarray(p, np.float64)
+        check(lib().nsf_chorin_set_state(self._h, _p(u, C.c_double), _p(p, C.c_double), None))
+
+    def stats(self):
+        s = (C.c_double * 8)()
+        check(lib().nsf_chorin_stats(self._h, s))
+        keys = ("tent_iters", "pres_iters", "final_iters", "pres_rel", "tent_rel", "final_rel", "pres_passes",
+                "status")
+        return dict(zip(keys, list(s)))
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            lib().nsf_chorin_destroy(self._h)
+            self._h = None
+
+
+def kernel_launches() -> int:
+    return int(lib().nsf_kernel_launches())
+
+
+__all__ = ["Mesh", "load_gmsh", "ChorinContext", "build_chorin_context", "coloring", "CsrF", "Spmv", "Spmm",
+           "spmv", "spmm", "fastconv_apply", "AbstractSolver", "create_solver", "ChorinStepper", "kernel_launches",
+           "NSF_F32", "NSF_F64", "NSF_PREC_F64", "NSF_PREC_MIXED", "NsfError"]

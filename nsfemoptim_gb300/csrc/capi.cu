@@ -1,0 +1,1032 @@
+// C ABI of the GB300 Chorin path: host setup handles, device CSR operators, solvers and the
+// device-resident Chorin stepper.  See include/nsfem_gb300.h for the contract of each call.
+#include "../../include/nsfem_gb300.h"
+
+#include "solvers.cuh"
+
+#include <algorithm>
+#include <cstring>
+#include <memory>
+#include <numeric>
+#include <string>
+
+namespace nsf
+{
+    thread_local std::string lastError;
+
+    template <typename F>
+    int guarded(F && f)
+    {
+        try
+        {
+            f();
+            return ST_OK;
+        }
+        catch (const Error & e)
+        {
+            lastError = e.what();
+            return e.status;
+        }
+        catch (const std::bad_alloc & e)
+        {
+            lastError = std::string("host allocation failed: ") + e.what();
+            return ST_INVALID;
+        }
+        catch (const std::invalid_argument & e)
+        {
+            lastError = e.what();
+            return ST_INVALID;
+        }
+        catch (const std::exception & e)
+        {
+            lastError = e.what();
+            return ST_IO;
+        }
+    }
+
+    inline void require(bool ok, const std::string & what)
+    {
+        if (!ok)
+            throw Error(ST_INVALID, what);
+    }
+
+    inline cudaStream_t asStream(void * s) { return reinterpret_cast<cudaStream_t>(s); }
+
+    std::vector<int> inverse(const std::vector<int> & perm)
+    {
+        std::vector<int> inv(perm.size());
+        for (size_t i = 0; i < perm.size(); i++)
+            inv[perm[i]] = (int)i;
+        return inv;
+    }
+
+    // re-index rows (rowMap[newRow] = oldRow) and columns (colMap[oldCol] = newCol or -1 to drop)
+    HostCsr<double> renumber(const HostCsr<double> & a, const std::vector<int> & rowMap, const std::vector<int> & colMap,
+                             int newCols)
+    {
+        HostCsr<double> out;
+        out.rows = (int)rowMap.size();
+        out.cols = newCols;
+        out.rowStart.assign(out.rows + 1, 0);
+        std::vector<std::pair<int, double>> tmp;
+        for (int r = 0; r < out.rows; r++)
+        {
+            tmp.clear();
+            const int o = rowMap[r];
+            for (int j = a.rowStart[o]; j < a.rowStart[o + 1]; j++)
+            {
+                const int c = colMap[a.col[j]];
+                if (c >= 0)
+                    tmp.emplace_back(c, a.val[j]);
+            }
+            std::sort(tmp.begin(), tmp.end(), [](const auto & x, const auto & y) { return x.first < y.first; });
+            for (auto & [c, v] : tmp)
+            {
+                out.col.push_back(c);
+                out.val.push_back(v);
+            }
+            out.rowStart[r + 1] = (int)out.col.size();
+        }
+        return out;
+    }
+
+    template <typename T>
+    struct DevCsr
+    {
+        int rows = 0, cols = 0, nnz = 0, L = 4;
+        DevBuf<int> rs, ci;
+        DevBuf<T> v;
+
+        void upload(const HostCsr<double> & a)
+        {
+            rows = a.rows;
+            cols = a.cols;
+            nnz = a.nnz();
+            rs.upload(a.rowStart);
+            ci.upload(a.col);
+            std::vector<T> tv(a.val.begin(), a.val.end());
+            v.upload(tv);
+            L = lanesFor(nnz, rows);
+        }
+    };
+} // namespace nsf
+
+using namespace nsf;
+
+struct nsf_mesh_s
+{
+    Mesh m;
+};
+
+struct nsf_context_s
+{
+    Context c;
+};
+
+struct nsf_csr_s
+{
+    int rows = 0, cols = 0, nnz = 0, dtype = NSF_F64, L = 4;
+    DevBuf<int> rs, ci;
+    DevBuf<double> v64;
+    DevBuf<float> v32;
+};
+
+extern "C" const char * nsf_last_error(void) { return lastError.c_str(); }
+
+extern "C" const char * nsf_status_string(int s)
+{
+    switch (s)
+    {
+    case NSF_OK: return "ok";
+    case NSF_ERR_INVALID_ARG: return "invalid argument";
+    case NSF_ERR_NONFINITE: return "non-finite value";
+    case NSF_ERR_MAXITER: return "iteration cap reached";
+    case NSF_ERR_BREAKDOWN: return "CG breakdown (matrix not SPD)";
+    case NSF_ERR_CUDA: return "CUDA error";
+    case NSF_ERR_IO: return "I/O or parse error";
+    case NSF_ERR_NOT_SUPPORTED: return "not supported";
+    default: return "unknown status";
+    }
+}
+
+extern "C" int nsf_version(void) { return 1; }
+
+extern "C" long long nsf_kernel_launches(void) { return launchCounter().load(); }
+
+// ============================================================================ host setup
+
+extern "C" int nsf_mesh_load_gmsh(const char * path, nsf_mesh * out)
+{
+    return guarded([&] {
+        require(path && out, "null argument");
+        auto h = std::make_unique<nsf_mesh_s>();
+        try
+        {
+            h->m = loadGmsh(path);
+        }
+        catch (const std::runtime_error & e)
+        {
+            throw Error(ST_IO, e.what());
+        }
+        *out = h.release();
+    });
+}
+
+extern "C" int nsf_mesh_counts(nsf_mesh h, int * counts)
+{
+    return guarded([&] {
+        require(h && counts, "null argument");
+        const Mesh & m = h->m;
+        counts[0] = (int)m.cornerXY.size() / 2;
+        counts[1] = m.numTri();
+        counts[2] = m.numBorder();
+        counts[3] = m.N;
+        counts[4] = m.P;
+        counts[5] = (int)m.groups.size();
+    });
+}
+
+extern "C" int nsf_mesh_arrays(nsf_mesh h, int * vElem, int * pElem, float * vXY, int * vBorder)
+{
+    return guarded([&] {
+        require(h, "null mesh");
+        const Mesh & m = h->m;
+        if (vElem)
+            std::copy(m.vElem.begin(), m.vElem.end(), vElem);
+        if (pElem)
+            std::copy(m.pElem.begin(), m.pElem.end(), pElem);
+        if (vXY)
+            std::copy(m.vXY.begin(), m.vXY.end(), vXY);
+        if (vBorder)
+            std::copy(m.vBorder.begin(), m.vBorder.end(), vBorder);
+    });
+}
+
+extern "C" const char * nsf_mesh_group(nsf_mesh h, int i)
+{
+    if (!h || i < 0 || i >= (int)h->m.groups.size())
+        return nullptr;
+    return h->m.groups[i].c_str();
+}
+
+extern "C" void nsf_mesh_destroy(nsf_mesh h) { delete h; }
+
+extern "C" int nsf_context_build(nsf_mesh mesh, float peak, int nThreads, nsf_context * out)
+{
+    return guarded([&] {
+        require(mesh && out, "null argument");
+        auto h = std::make_unique<nsf_context_s>();
+        h->c = buildChannelContext(mesh->m, peak, nThreads);
+        *out = h.release();
+    });
+}
+
+extern "C" int nsf_context_sizes(nsf_context h, int * s)
+{
+    return guarded([&] {
+        require(h && s, "null argument");
+        const Context & c = h->c;
+        s[0] = c.N;
+        s[1] = c.P;
+        s[2] = (int)c.dirIds.size();
+        s[3] = (int)c.dirPIds.size();
+        s[4] = (int)c.intV.size();
+        s[5] = (int)c.intP.size();
+        s[6] = c.M.nnz();
+        s[7] = c.K.nnz();
+        s[8] = c.Kp.nnz();
+        s[9] = c.Kpi.nnz();
+        s[10] = c.D.nnz();
+        s[11] = c.G.nnz();
+        s[12] = c.I.nnz();
+    });
+}
+
+static const HostCsr<double> & contextMatrix(const Context & c, int which)
+{
+    switch (which)
+    {
+    case 0: return c.M;
+    case 1: return c.K;
+    case 2: return c.Kp;
+    case 3: return c.Kpi;
+    case 4: return c.D;
+    case 5: return c.G;
+    case 6: return c.I;
+    default: throw Error(ST_INVALID, "matrix index must be 0..6");
+    }
+}
+
+extern "C" int nsf_context_matrix(nsf_context h, int which, int * rowStart, int * col, double * val)
+{
+    return guarded([&] {
+        require(h, "null context");
+        const HostCsr<double> & a = contextMatrix(h->c, which);
+        if (rowStart)
+            std::copy(a.rowStart.begin(), a.rowStart.end(), rowStart);
+        if (col)
+            std::copy(a.col.begin(), a.col.end(), col);
+        if (val)
+            std::copy(a.val.begin(), a.val.end(), val);
+    });
+}
+
+extern "C" int nsf_context_lists(nsf_context h, int * dirIds, double * dirVx, int * dirPIds, int * intV, int * intP)
+{
+    return guarded([&] {
+        require(h, "null context");
+        const Context & c = h->c;
+        if (dirIds)
+            std::copy(c.dirIds.begin(), c.dirIds.end(), dirIds);
+        if (dirVx)
+            std::copy(c.dirVx.begin(), c.dirVx.end(), dirVx);
+        if (dirPIds)
+            std::copy(c.dirPIds.begin(), c.dirPIds.end(), dirPIds);
+        if (intV)
+            std::copy(c.intV.begin(), c.intV.end(), intV);
+        if (intP)
+            std::copy(c.intP.begin(), c.intP.end(), intP);
+    });
+}
+
+extern "C" void nsf_context_destroy(nsf_context h) { delete h; }
+
+extern "C" int nsf_coloring(int n, const int * rowStart, const int * col, int * perm, int * partStart, int * nColors)
+{
+    return guarded([&] {
+        require(n >= 0 && rowStart && perm && partStart && nColors, "null argument");
+        std::string why;
+        require(validCsr(n, n, rowStart[n], rowStart, col, why), "invalid CSR: " + why);
+        Coloring c = colorGraph(n, rowStart, col);
+        std::copy(c.perm.begin(), c.perm.end(), perm);
+        std::copy(c.partStart.begin(), c.partStart.end(), partStart);
+        *nColors = c.colors();
+    });
+}
+
+// ============================================================================ device CSR
+
+extern "C" int nsf_csr_create(int rows, int cols, int nnz, const int * rowStart, const int * col, const void * values,
+                              int dtype, nsf_csr * out)
+{
+    return guarded([&] {
+        require(out && values, "null argument");
+        require(dtype == NSF_F32 || dtype == NSF_F64, "dtype must be NSF_F32 or NSF_F64");
+        std::string why;
+        require(validCsr(rows, cols, nnz, rowStart, col, why), "invalid CSR: " + why);
+        auto h = std::make_unique<nsf_csr_s>();
+        h->rows = rows;
+        h->cols = cols;
+        h->nnz = nnz;
+        h->dtype = dtype;
+        h->rs.upload(rowStart, rows + 1);
+        h->ci.upload(col, nnz);
+        if (dtype == NSF_F64)
+        {
+            const double * v = static_cast<const double *>(values);
+            for (int i = 0; i < nnz; i++)
+                require(std::isfinite(v[i]), "non-finite CSR value at " + std::to_string(i));
+            h->v64.upload(v, nnz);
+        }
+        else
+        {
+            const float * v = static_cast<const float *>(values);
+            for (int i = 0; i < nnz; i++)
+                require(std::isfinite(v[i]), "non-finite CSR value at " + std::to_string(i));
+            h->v32.upload(v, nnz);
+        }
+        h->L = lanesFor(nnz, rows);
+        *out = h.release();
+    });
+}
+
+extern "C" int nsf_csr_update_values(nsf_csr a, const void * values, int onDevice, void * stream)
+{
+    return guarded([&] {
+        require(a && values, "null argument");
+        const size_t bytes = (size_t)a->nnz * (a->dtype == NSF_F64 ? 8 : 4);
+        void * dst = a->dtype == NSF_F64 ? (void *)a->v64.get() : (void *)a->v32.get();
+        NSF_CUDA(cudaMemcpyAsync(dst, values, bytes, onDevice ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice,
+                                 asStream(stream)));
+        if (!onDevice)
+            NSF_CUDA(cudaStreamSynchronize(asStream(stream)));
+    });
+}
+
+extern "C" int nsf_csr_device(nsf_csr a, int ** rowStart, int ** col, void ** values)
+{
+    return guarded([&] {
+        require(a, "null csr");
+        if (rowStart)
+            *rowStart = a->rs.get();
+        if (col)
+            *col = a->ci.get();
+        if (values)
+            *values = a->dtype == NSF_F64 ? (void *)a->v64.get() : (void *)a->v32.get();
+    });
+}
+
+extern "C" void nsf_csr_destroy(nsf_csr a) { delete a; }
+
+extern "C" int nsf_spmv(nsf_csr a, const void * x, void * y, double alpha, double beta, void * stream)
+{
+    return guarded([&] {
+        require(a && x && y, "null argument");
+        const int grid = blocksFor((long long)a->rows * a->L);
+        cudaStream_t s = asStream(stream);
+        if (a->dtype == NSF_F64)
+        {
+            NSF_LANES(a->L, NSF_LAUNCH((kSpmv<double, double, double, double, LL>), grid, s, a->rows, a->rs.get(),
+                                       a->ci.get(), a->v64.get(), (const double *)x, (double *)y, alpha, beta));
+        }
+        else
+        {
+            NSF_LANES(a->L, NSF_LAUNCH((kSpmv<float, float, float, float, LL>), grid, s, a->rows, a->rs.get(),
+                                       a->ci.get(), a->v32.get(), (const float *)x, (float *)y, alpha, beta));
+        }
+    });
+}
+
+extern "C" int nsf_spmm(nsf_csr a, int nrhs, const void * X, int ldx, void * Y, int ldy, void * stream)
+{
+    return guarded([&] {
+        require(a && X && Y && nrhs >= 1, "bad argument");
+        require(ldx >= a->cols && ldy >= a->rows, "leading dimensions too small");
+        const int grid = blocksFor((long long)a->rows * a->L);
+        cudaStream_t s = asStream(stream);
+        for (int c0 = 0; c0 < nrhs; c0 += 2)
+        {
+            const int k = std::min(2, nrhs - c0);
+            if (a->dtype == NSF_F64)
+            {
+                const double * xx = (const double *)X + (size_t)c0 * ldx;
+                double * yy = (double *)Y + (size_t)c0 * ldy;
+                if (k == 2)
+                    NSF_LANES(a->L, NSF_LAUNCH((kSpmm<double, double, double, double, LL, 2>), grid, s, a->rows,
+                                               a->rs.get(), a->ci.get(), a->v64.get(), xx, ldx, yy, ldy));
+                else
+                    NSF_LANES(a->L, NSF_LAUNCH((kSpmm<double, double, double, double, LL, 1>), grid, s, a->rows,
+                                               a->rs.get(), a->ci.get(), a->v64.get(), xx, ldx, yy, ldy));
+            }
+            else
+            {
+                const float * xx = (const float *)X + (size_t)c0 * ldx;
+                float * yy = (float *)Y + (size_t)c0 * ldy;
+                if (k == 2)
+                    NSF_LANES(a->L, NSF_LAUNCH((kSpmm<float, float, float, float, LL, 2>), grid, s, a->rows,
+                                               a->rs.get(), a->ci.get(), a->v32.get(), xx, ldx, yy, ldy));
+                else
+                    NSF_LANES(a->L, NSF_LAUNCH((kSpmm<float, float, float, float, LL, 1>), grid, s, a->rows,
+                                               a->rs.get(), a->ci.get(), a->v32.get(), xx, ldx, yy, ldy));
+            }
+        }
+    });
+}
+
+extern "C" int nsf_fastconv_apply(nsf_csr I, const void * K, double nu, const void * u, void * A, void * stream)
+{
+    return guarded([&] {
+        require(I && K && u && A, "null argument");
+        const int grid = blocksFor((long long)I->rows * I->L);
+        cudaStream_t s = asStream(stream);
+        if (I->dtype == NSF_F64)
+            NSF_LANES(I->L, NSF_LAUNCH((kFastConv<double, double, double, double, LL>), grid, s, I->rows, I->rs.get(),
+                                       I->ci.get(), I->v64.get(), (const double *)u, (const double *)K, nu, (double *)A));
+        else
+            NSF_LANES(I->L, NSF_LAUNCH((kFastConv<float, float, float, float, LL>), grid, s, I->rows, I->rs.get(),
+                                       I->ci.get(), I->v32.get(), (const float *)u, (const float *)K, (float)nu,
+                                       (float *)A));
+    });
+}
+
+// ============================================================================ solvers
+
+struct nsf_solver_s
+{
+    std::string method;
+    int numCh = 1, n = 0, precision = NSF_PREC_F64, maxIters = 200, checkInterval = 1;
+    double target = 1e-6;
+    Coloring col;
+    DevBuf<int> perm;
+    SweepSystem<double> s64;
+    SweepSystem<float> s32;
+    PcgSolver<double, 1> pcg1;
+    PcgSolver<double, 2> pcg2;
+    GsSolver<double, 1> gs1;
+    GsSolver<double, 2> gs2;
+    MixedPcg<1> mix1;
+    MixedPcg<2> mix2;
+    DevBuf<double> bp, xp;
+    cudaStream_t body = nullptr;
+    PinnedBuf<SolverState> stat{1};
+    SolverState last{};
+    int lastStatus = 0;
+
+    ~nsf_solver_s()
+    {
+        if (body)
+            cudaStreamDestroy(body);
+    }
+
+    const SolverState * devState() const
+    {
+        if (precision == NSF_PREC_MIXED)
+            return numCh == 1 ? mix1.st.get() : mix2.st.get();
+        if (method == "gs")
+            return numCh == 1 ? gs1.st.get() : gs2.st.get();
+        return numCh == 1 ? pcg1.st.get() : pcg2.st.get();
+    }
+};
+
+extern "C" int nsf_solver_create(const char * method, int numCh, int n, const int * rowStart, const int * col,
+                                 const double * values, int precision, int maxIters, double target, int checkInterval,
+                                 nsf_solver * out)
+{
+    return guarded([&] {
+        require(method && out && values, "null argument");
+        const std::string m(method);
+        require(m == "gs" || m == "pcg", "method must be \"gs\" or \"pcg\"");
+        require(numCh == 1 || numCh == 2, "numCh must be 1 or 2");
+        require(checkInterval >= 1, "checkInterval must be >= 1");
+        require(maxIters >= 0, "maxIters must be >= 0");
+        require(precision == NSF_PREC_F64 || precision == NSF_PREC_MIXED, "unknown precision");
+        require(!(precision == NSF_PREC_MIXED && m == "gs"), "mixed precision is provided for \"pcg\"");
+        std::string why;
+        require(validCsr(n, n, rowStart ? rowStart[n] : 0, rowStart, col, why), "invalid CSR: " + why);
+        auto s = std::make_unique<nsf_solver_s>();
+        s->method = m;
+        s->numCh = numCh;
+        s->n = n;
+        s->precision = precision;
+        s->maxIters = maxIters;
+        s->target = target;
+        s->checkInterval = checkInterval;
+        HostCsr<double> a;
+        a.rows = a.cols = n;
+        a.rowStart.assign(rowStart, rowStart + n + 1);
+        a.col.assign(col, col + rowStart[n]);
+        a.val.assign(values, values + rowStart[n]);
+        for (double v : a.val)
+            require(std::isfinite(v), "non-finite matrix value");
+        s->col = colorGraph(n, a.rowStart.data(), a.col.data());
+        HostCsr<double> ap = permuteSym(a, s->col.perm);
+        s->perm.upload(s->col.perm);
+        s->s64.build(ap, s->col.partStart);
+        if (precision == NSF_PREC_MIXED)
+        {
+            s->s32.build(ap, s->col.partStart);
+            if (numCh == 1)
+                s->mix1.setup(&s->s64, &s->s32, 1);
+            else
+                s->mix2.setup(&s->s64, &s->s32, 2);
+        }
+        else if (m == "gs")
+        {
+            if (numCh == 1)
+                s->gs1.setup(&s->s64, 1, checkInterval);
+            else
+                s->gs2.setup(&s->s64, 2, checkInterval);
+        }
+        else
+        {
+            if (numCh == 1)
+                s->pcg1.setup(&s->s64, 1);
+            else
+                s->pcg2.setup(&s->s64, 2);
+        }
+        s->bp.alloc((size_t)numCh * n);
+        s->xp.alloc((size_t)numCh * n);
+        NSF_CUDA(cudaStreamCreateWithFlags(&s->body, cudaStreamNonBlocking));
+        *out = s.release();
+    });
+}
+
+extern "C" int nsf_solver_set(nsf_solver s, int maxIters, double target, int checkInterval)
+{
+    return guarded([&] {
+        require(s && maxIters >= 0 && checkInterval >= 1, "bad argument");
+        s->maxIters = maxIters;
+        s->target = target;
+        s->checkInterval = checkInterval;
+        s->gs1.interval = s->gs2.interval = checkInterval;
+        s->gs1.P.interval = s->gs2.P.interval = checkInterval;
+    });
+}
+
+extern "C" int nsf_solver_solve(nsf_solver s, const double * b, double * x, void * stream)
+{
+    int st = guarded([&] {
+        require(s && b && x, "null argument");
+        cudaStream_t cs = asStream(stream);
+        const int n = s->n, grid = blocksFor(n);
+        NSF_LAUNCH(kGatherPerm<double>, grid, cs, n, s->numCh, s->perm.get(), b, s->bp.get());
+        NSF_LAUNCH(kGatherPerm<double>, grid, cs, n, s->numCh, s->perm.get(), x, s->xp.get());
+        const bool rel = true;
+        if (s->precision == NSF_PREC_MIXED)
+        {
+            const int outer = 6, innerIt = std::max(1, s->maxIters);
+            const double innerTol = std::max(1e-5, s->target);
+            if (s->numCh == 1)
+                s->mix1.enqueue(cs, s->body, s->bp.get(), s->xp.get(), outer, s->target, innerIt, innerTol,
+                                s->checkInterval);
+            else
+                s->mix2.enqueue(cs, s->body, s->bp.get(), s->xp.get(), outer, s->target, innerIt, innerTol,
+                                s->checkInterval);
+        }
+        else if (s->method == "gs")
+        {
+            // the reference's target is an absolute RMS residual (cu::GaussSeidel)
+            if (s->numCh == 1)
+                s->gs1.enqueue(cs, s->body, s->bp.get(), s->xp.get(), s->maxIters, s->target, true, 1);
+            else
+                s->gs2.enqueue(cs, s->body, s->bp.get(), s->xp.get(), s->maxIters, s->target, true, 1);
+        }
+        else
+        {
+            if (s->numCh == 1)
+                s->pcg1.enqueue(cs, s->body, s->bp.get(), s->xp.get(), s->maxIters, s->target, !rel, s->checkInterval);
+            else
+                s->pcg2.enqueue(cs, s->body, s->bp.get(), s->xp.get(), s->maxIters, s->target, !rel, s->checkInterval);
+        }
+        NSF_LAUNCH(kScatterPerm<double>, grid, cs, n, s->numCh, s->perm.get(), s->xp.get(), x);
+        NSF_CUDA(cudaMemcpyAsync(s->stat.get(), s->devState(), sizeof(SolverState), cudaMemcpyDeviceToHost, cs));
+        NSF_CUDA(cudaStreamSynchronize(cs));
+        s->last = *s->stat.get();
+        int worst = 0;
+        for (int c = 0; c < s->numCh; c++)
+            worst = std::max(worst, s->last.status[c]);
+        s->lastStatus = worst;
+        if (worst != 0)
+            throw Error(worst, std::string("solver finished with status ") + nsf_status_string(worst));
+    });
+    return st;
+}
+
+extern "C" int nsf_solver_stats(nsf_solver s, int * iters, double * rms, double * rel)
+{
+    return guarded([&] {
+        require(s, "null solver");
+        const SolverState & L = s->last;
+        int it = 0;
+        for (int c = 0; c < s->numCh; c++)
+        {
+            const int ci = s->precision == NSF_PREC_MIXED ? L.innerTotal[c] : L.iters[c];
+            it = std::max(it, ci);
+            if (rms)
+                rms[c] = std::sqrt(std::max(0.0, L.lastRR[c]) / (double)s->n);
+            if (rel)
+                rel[c] = L.bb[c] > 0 ? std::sqrt(std::max(0.0, L.lastRR[c]) / L.bb[c]) : std::sqrt(std::max(0.0, L.lastRR[c]));
+        }
+        if (iters)
+            *iters = it;
+    });
+}
+
+extern "C" void nsf_solver_destroy(nsf_solver s) { delete s; }
+
+// ============================================================================ Chorin stepper
+
+struct nsf_chorin_s
+{
+    nsf_chorin_config cfg{};
+    bool mixed = false;
+    int N = 0, P = 0, nIntP = 0;
+    std::vector<int> permV, permP, intP;
+    // operators in the color-permuted numbering
+    SweepSystem<double> M64, Kpi64;
+    SweepSystem<float> M32, Kpi32;
+    DevCsr<double> I64, D64, G64;
+    DevCsr<float> I32, D32, G32;
+    DevBuf<double> K64, A64;
+    DevBuf<float> K32, A32;
+    // state and work vectors
+    DevBuf<double> u, pInt, rhs, acc, rhsP;
+    DevBuf<unsigned char> isDir;
+    DevBuf<double> dirVal;
+    // solvers: separate objects for the tentative and the final mass solve keep both stats
+    PcgSolver<double, 2> velT, velF;
+    GsSolver<double, 2> gsT, gsF;
+    PcgSolver<double, 1> pres;
+    MixedPcg<2> mvelT, mvelF;
+    MixedPcg<1> mpres;
+    cudaStream_t stream = nullptr, body = nullptr;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    long long kernelsPerCapture = 0;
+    PinnedBuf<SolverState> stat{5};
+    std::unique_ptr<PinnedBuf<double>> stage;
+    size_t stageSize = 0;
+
+    double * staging(size_t need)
+    {
+        if (stageSize < need)
+        {
+            stage = std::make_unique<PinnedBuf<double>>(need);
+            stageSize = need;
+        }
+        return stage->get();
+    }
+    double stats[8] = {0};
+
+    ~nsf_chorin_s()
+    {
+        if (exec)
+            cudaGraphExecDestroy(exec);
+        if (graph)
+            cudaGraphDestroy(graph);
+        if (body)
+            cudaStreamDestroy(body);
+        if (stream)
+            cudaStreamDestroy(stream);
+    }
+
+    void enqueueMassSolve(cudaStream_t s, bool tentative)
+    {
+        double * b = rhs.get();
+        double * x = acc.get();
+        NSF_CUDA(cudaMemsetAsync(x, 0, sizeof(double) * 2 * N, s));
+        if (mixed)
+            (tentative ? mvelT : mvelF)
+                .enqueue(s, body, b, x, cfg.maxOuter, cfg.velTol, cfg.velMaxIters, cfg.innerTol, cfg.checkInterval);
+        else if (cfg.velMethod == 0)
+            (tentative ? gsT : gsF).enqueue(s, body, b, x, cfg.velMaxIters, cfg.velTol, false, cfg.checkInterval);
+        else
+            (tentative ? velT : velF).enqueue(s, body, b, x, cfg.velMaxIters, cfg.velTol, false, cfg.checkInterval);
+    }
+
+    void enqueueStep(cudaStream_t s)
+    {
+        const int nnzA = M64.nnzFull;
+        // 1. A = nu K + I u ;  rhs = A [ux uy]
+        if (mixed)
+        {
+            NSF_LANES(I32.L, NSF_LAUNCH((kFastConv<float, double, float, float, LL>), blocksFor((long long)nnzA * I32.L), s,
+                                        nnzA, I32.rs.get(), I32.ci.get(), I32.v.get(), u.get(), K32.get(),
+                                        (float)cfg.nu, A32.get()));
+            NSF_LANES(M32.L, NSF_LAUNCH((kSpmm<float, double, double, float, LL, 2>), blocksFor((long long)N * M32.L), s,
+                                        N, M32.rsF.get(), M32.ciF.get(), A32.get(), u.get(), N, rhs.get(), N));
+        }
+        else
+        {
+            NSF_LANES(I64.L, NSF_LAUNCH((kFastConv<double, double, double, double, LL>),
+                                        blocksFor((long long)nnzA * I64.L), s, nnzA, I64.rs.get(), I64.ci.get(),
+                                        I64.v.get(), u.get(), K64.get(), cfg.nu, A64.get()));
+            NSF_LANES(M64.L, NSF_LAUNCH((kSpmm<double, double, double, double, LL, 2>),
+                                        blocksFor((long long)N * M64.L), s, N, M64.rsF.get(), M64.ciF.get(),
+                                        A64.get(), u.get(), N, rhs.get(), N));
+        }
+        // 2. M acc = rhs ; u = u - tau acc ; Dirichlet
+        enqueueMassSolve(s, true);
+        NSF_LAUNCH(kUpdateVelocity<double>, blocksFor(N), s, N, u.get(), acc.get(), cfg.tau, isDir.get(), dirVal.get());
+        // 3. rhsP = -(1/tau) D u ; Kpi pInt = rhsP (warm start)
+        const double invTau = -1.0 / cfg.tau;
+        if (mixed)
+        {
+            NSF_LANES(D32.L, NSF_LAUNCH((kSpmv<float, double, double, float, LL>), blocksFor((long long)nIntP * D32.L),
+                                        s, nIntP, D32.rs.get(), D32.ci.get(), D32.v.get(), u.get(), rhsP.get(),
+                                        invTau, 0.0));
+            mpres.enqueue(s, body, rhsP.get(), pInt.get(), cfg.maxOuter, cfg.presTol, cfg.presMaxIters, cfg.innerTol,
+                          cfg.checkInterval);
+            NSF_LANES(G32.L, NSF_LAUNCH((kSpmv<float, double, double, float, LL>), blocksFor((long long)2 * N * G32.L),
+                                        s, 2 * N, G32.rs.get(), G32.ci.get(), G32.v.get(), pInt.get(), rhs.get(), 1.0,
+                                        0.0));
+        }
+        else
+        {
+            NSF_LANES(D64.L, NSF_LAUNCH((kSpmv<double, double, double, double, LL>),
+                                        blocksFor((long long)nIntP * D64.L), s, nIntP, D64.rs.get(), D64.ci.get(),
+                                        D64.v.get(), u.get(), rhsP.get(), invTau, 0.0));
+            pres.enqueue(s, body, rhsP.get(), pInt.get(), cfg.presMaxIters, cfg.presTol, false, cfg.checkInterval);
+            NSF_LANES(G64.L, NSF_LAUNCH((kSpmv<double, double, double, double, LL>),
+                                        blocksFor((long long)2 * N * G64.L), s, 2 * N, G64.rs.get(), G64.ci.get(),
+                                        G64.v.get(), pInt.get(), rhs.get(), 1.0, 0.0));
+        }
+        // 4. M acc = G p ; u = u - tau acc ; Dirichlet
+        enqueueMassSolve(s, false);
+        NSF_LAUNCH(kUpdateVelocity<double>, blocksFor(N), s, N, u.get(), acc.get(), cfg.tau, isDir.get(), dirVal.get());
+    }
+
+    void collectStats(cudaStream_t s)
+    {
+        const SolverState * src[3];
+        if (mixed)
+        {
+            src[0] = mvelT.st.get();
+            src[1] = mpres.st.get();
+            src[2] = mvelF.st.get();
+        }
+        else
+        {
+            src[0] = cfg.velMethod == 0 ? gsT.st.get() : velT.st.get();
+            src[1] = pres.st.get();
+            src[2] = cfg.velMethod == 0 ? gsF.st.get() : velF.st.get();
+        }
+        for (int i = 0; i < 3; i++)
+            NSF_CUDA(cudaMemcpyAsync(stat.get() + i, src[i], sizeof(SolverState), cudaMemcpyDeviceToHost, s));
+        NSF_CUDA(cudaStreamSynchronize(s));
+        int worst = 0;
+        for (int i = 0; i < 3; i++)
+        {
+            const SolverState & L = stat.get()[i];
+            const int nch = i == 1 ? 1 : 2;
+            int it = 0;
+            double rel = 0;
+            for (int c = 0; c < nch; c++)
+            {
+                it = std::max(it, mixed ? L.innerTotal[c] : L.iters[c]);
+                const double r = L.bb[c] > 0 ? std::sqrt(std::max(0.0, L.lastRR[c]) / L.bb[c]) : 0.0;
+                rel = std::max(rel, r);
+                worst = std::max(worst, L.status[c]);
+            }
+            const int idxIt[3] = {0, 1, 2};
+            const int idxRel[3] = {4, 3, 5};
+            stats[idxIt[i]] = it;
+            stats[idxRel[i]] = rel;
+            if (i == 1)
+                stats[6] = mixed ? L.iters[0] : 0;
+        }
+        stats[7] = worst;
+    }
+};
+
+static void buildChorin(nsf_chorin_s & S, const Context & c)
+{
+    const int N = c.N, P = c.P;
+    S.N = N;
+    S.P = P;
+    S.intP = c.intP;
+    S.nIntP = (int)c.intP.size();
+    require(S.nIntP > 0, "no internal pressure nodes");
+    // velocity numbering: coloring of M (shared by K, A); pressure: coloring of Kpi
+    Coloring cv = colorGraph(N, c.M.rowStart.data(), c.M.col.data());
+    Coloring cp = colorGraph(S.nIntP, c.Kpi.rowStart.data(), c.Kpi.col.data());
+    S.permV = cv.perm;
+    S.permP = cp.perm;
+    const std::vector<int> invV = inverse(cv.perm), invP = inverse(cp.perm);
+    HostCsr<double> Mp = permuteSym(c.M, cv.perm);
+    HostCsr<double> Kp = permuteSym(c.K, cv.perm);
+    HostCsr<double> Kpip = permuteSym(c.Kpi, cp.perm);
+    // velocity dof map (2N): old (node, ch) -> new
+    std::vector<int> dofMap(2 * (size_t)N);
+    for (int v = 0; v < N; v++)
+    {
+        dofMap[v] = invV[v];
+        dofMap[v + N] = invV[v] + N;
+    }
+    std::vector<int> dofRows(2 * (size_t)N);
+    for (int r = 0; r < N; r++)
+    {
+        dofRows[r] = cv.perm[r];
+        dofRows[r + N] = cv.perm[r] + N;
+    }
+    // I: rows follow the entries of the permuted K pattern
+    std::vector<int> iRows(Kp.nnz());
+    for (int r = 0; r < N; r++)
+        for (int e = Kp.rowStart[r]; e < Kp.rowStart[r + 1]; e++)
+        {
+            const int orow = cv.perm[r], ocol = cv.perm[Kp.col[e]];
+            const auto b = c.K.col.begin() + c.K.rowStart[orow], en = c.K.col.begin() + c.K.rowStart[orow + 1];
+            auto it = std::lower_bound(b, en, ocol);
+            require(it != en && *it == ocol, "K pattern mismatch while permuting I");
+            iRows[e] = (int)(it - c.K.col.begin());
+        }
+    HostCsr<double> Ip = renumber(c.I, iRows, dofMap, 2 * N);
+    // D: rows = internal pressure nodes in colored order; cols = velocity dofs
+    std::vector<int> dRows(S.nIntP);
+    for (int r = 0; r < S.nIntP; r++)
+        dRows[r] = c.intP[cp.perm[r]];
+    HostCsr<double> Dp = renumber(c.D, dRows, dofMap, 2 * N);
+    // G: rows = velocity dofs in colored order; cols = internal pressure (Dirichlet p = 0 dropped)
+    std::vector<int> pCol(P, -1);
+    for (int i = 0; i < S.nIntP; i++)
+        pCol[c.intP[i]] = invP[i];
+    HostCsr<double> Gp = renumber(c.G, dofRows, pCol, S.nIntP);
+
+    S.M64.build(Mp, cv.partStart);
+    S.Kpi64.build(Kpip, cp.partStart);
+    std::vector<double> knu(Kp.val.begin(), Kp.val.end());
+    if (S.mixed)
+    {
+        S.M32.build(Mp, cv.partStart);
+        S.Kpi32.build(Kpip, cp.partStart);
+        S.I32.upload(Ip);
+        S.D32.upload(Dp);
+        S.G32.upload(Gp);
+        std::vector<float> k32(knu.begin(), knu.end());
+        S.K32.upload(k32);
+        S.A32.alloc(knu.size());
+        S.mvelT.setup(&S.M64, &S.M32, 2);
+        S.mvelF.setup(&S.M64, &S.M32, 2);
+        S.mpres.setup(&S.Kpi64, &S.Kpi32, 1);
+    }
+    else
+    {
+        S.I64.upload(Ip);
+        S.D64.upload(Dp);
+        S.G64.upload(Gp);
+        S.K64.upload(knu);
+        S.A64.alloc(knu.size());
+        if (S.cfg.velMethod == 0)
+        {
+            S.gsT.setup(&S.M64, 2, 1);
+            S.gsF.setup(&S.M64, 2, 1);
+        }
+        else
+        {
+            S.velT.setup(&S.M64, 2);
+            S.velF.setup(&S.M64, 2);
+        }
+        S.pres.setup(&S.Kpi64, 1);
+    }
+    // Dirichlet rows in the colored numbering
+    std::vector<unsigned char> isDir(N, 0);
+    std::vector<double> dval(N, 0.0);
+    for (size_t i = 0; i < c.dirIds.size(); i++)
+    {
+        isDir[invV[c.dirIds[i]]] = 1;
+        dval[invV[c.dirIds[i]]] = c.dirVx[i];
+    }
+    S.isDir.upload(isDir);
+    S.dirVal.upload(dval);
+    // initial state: u = 0 with the Dirichlet values, p = 0
+    std::vector<double> u0(2 * (size_t)N, 0.0);
+    for (int r = 0; r < N; r++)
+        if (isDir[r])
+            u0[r] = dval[r];
+    S.u.upload(u0);
+    S.pInt.alloc(S.nIntP);
+    S.rhs.alloc(2 * (size_t)N);
+    S.acc.alloc(2 * (size_t)N);
+    S.rhsP.alloc(S.nIntP);
+}
+
+extern "C" int nsf_chorin_create(nsf_context ctx, const nsf_chorin_config * cfg, nsf_chorin * out)
+{
+    return guarded([&] {
+        require(ctx && cfg && out, "null argument");
+        require(cfg->tau > 0 && cfg->nu >= 0, "tau must be > 0 and nu >= 0");
+        require(cfg->precision == NSF_PREC_F64 || cfg->precision == NSF_PREC_MIXED, "unknown precision");
+        require(cfg->velMethod == 0 || cfg->velMethod == 1, "velMethod must be 0 (gs) or 1 (pcg)");
+        require(!(cfg->precision == NSF_PREC_MIXED && cfg->velMethod == 0), "mixed precision uses velMethod 1 (pcg)");
+        require(cfg->velMaxIters >= 1 && cfg->presMaxIters >= 1, "iteration caps must be >= 1");
+        auto S = std::make_unique<nsf_chorin_s>();
+        S->cfg = *cfg;
+        if (S->cfg.checkInterval < 1)
+            S->cfg.checkInterval = 1;
+        if (S->cfg.maxOuter < 1)
+            S->cfg.maxOuter = 4;
+        if (!(S->cfg.innerTol > 0))
+            S->cfg.innerTol = 1e-4;
+        S->mixed = cfg->precision == NSF_PREC_MIXED;
+        buildChorin(*S, ctx->c);
+        NSF_CUDA(cudaStreamCreateWithFlags(&S->stream, cudaStreamNonBlocking));
+        NSF_CUDA(cudaStreamCreateWithFlags(&S->body, cudaStreamNonBlocking));
+        NSF_CUDA(cudaDeviceSynchronize());
+        *out = S.release();
+    });
+}
+
+extern "C" int nsf_chorin_step(nsf_chorin S, int nSteps, void * stream)
+{
+    return guarded([&] {
+        require(S && nSteps >= 0, "bad argument");
+        cudaStream_t s = stream ? asStream(stream) : S->stream;
+        if (S->cfg.useGraph)
+        {
+            if (!S->exec)
+            {
+                const long long before = launchCounter().load();
+                NSF_CUDA(cudaStreamBeginCapture(S->stream, cudaStreamCaptureModeThreadLocal));
+                try
+                {
+                    S->enqueueStep(S->stream);
+                }
+                catch (...)
+                {
+                    cudaGraph_t g = nullptr;
+                    cudaStreamEndCapture(S->stream, &g);
+                    if (g)
+                        cudaGraphDestroy(g);
+                    throw;
+                }
+                NSF_CUDA(cudaStreamEndCapture(S->stream, &S->graph));
+                NSF_CUDA(cudaGraphInstantiate(&S->exec, S->graph, 0));
+                S->kernelsPerCapture = launchCounter().load() - before;
+                launchCounter().fetch_sub(S->kernelsPerCapture); // counted when replayed
+            }
+            for (int i = 0; i < nSteps; i++)
+                NSF_CUDA(cudaGraphLaunch(S->exec, s));
+        }
+        else
+        {
+            for (int i = 0; i < nSteps; i++)
+                S->enqueueStep(s);
+        }
+        if (nSteps > 0)
+            S->collectStats(s);
+        if (S->stats[7] == ST_NONFINITE)
+            throw Error(ST_NONFINITE, "non-finite solver residual in the time step");
+    });
+}
+
+extern "C" int nsf_chorin_get_state(nsf_chorin S, double * uOut, double * pOut, void * stream)
+{
+    return guarded([&] {
+        require(S, "null stepper");
+        cudaStream_t s = stream ? asStream(stream) : S->stream;
+        double * h = S->staging(2 * (size_t)S->N + S->nIntP);
+        NSF_CUDA(cudaMemcpyAsync(h, S->u.get(), sizeof(double) * 2 * S->N, cudaMemcpyDeviceToHost, s));
+        NSF_CUDA(cudaMemcpyAsync(h + 2 * S->N, S->pInt.get(), sizeof(double) * S->nIntP, cudaMemcpyDeviceToHost, s));
+        NSF_CUDA(cudaStreamSynchronize(s));
+        const int N = S->N;
+        if (uOut)
+            for (int r = 0; r < N; r++)
+            {
+                uOut[S->permV[r]] = h[r];
+                uOut[S->permV[r] + N] = h[r + N];
+            }
+        if (pOut)
+        {
+            std::fill(pOut, pOut + S->P, 0.0);
+            for (int r = 0; r < S->nIntP; r++)
+                pOut[S->intP[S->permP[r]]] = h[2 * N + r];
+        }
+    });
+}
+
+extern "C" int nsf_chorin_set_state(nsf_chorin S, const double * uIn, const double * pIn, void * stream)
+{
+    return guarded([&] {
+        require(S, "null stepper");
+        cudaStream_t s = stream ? asStream(stream) : S->stream;
+        double * h = S->staging(2 * (size_t)S->N + S->nIntP);
+        const int N = S->N;
+        NSF_CUDA(cudaStreamSynchronize(s)); // the staging buffer may still feed an earlier copy
+        if (uIn)
+        {
+            for (int r = 0; r < N; r++)
+            {
+                h[r] = uIn[S->permV[r]];
+                h[r + N] = uIn[S->permV[r] + N];
+            }
+            NSF_CUDA(cudaMemcpyAsync(S->u.get(), h, sizeof(double) * 2 * N, cudaMemcpyHostToDevice, s));
+        }
+        if (pIn)
+        {
+            for (int r = 0; r < S->nIntP; r++)
+                h[2 * N + r] = pIn[S->intP[S->permP[r]]];
+            NSF_CUDA(cudaMemcpyAsync(S->pInt.get(), h + 2 * N, sizeof(double) * S->nIntP, cudaMemcpyHostToDevice, s));
+        }
+        NSF_CUDA(cudaStreamSynchronize(s));
+    });
+}
+
+extern "C" int nsf_chorin_stats(nsf_chorin S, double * stats)
+{
+    return guarded([&] {
+        require(S && stats, "null argument");
+        std::copy(S->stats, S->stats + 8, stats);
+    });
+}
+
+extern "C" void nsf_chorin_destroy(nsf_chorin S) { delete S; }

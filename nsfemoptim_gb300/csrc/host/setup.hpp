@@ -1,0 +1,76 @@
+// Host-side setup of the Chorin path: mesh input, P1/P2 numbering, channel boundary lists,
+// FP64 operator assembly, CSR slicing and the Gauss-Seidel coloring.  Integer results
+// (numbering, patterns, lists, coloring) are bit-identical to the reference's; values are FP64.
+#pragma once
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+namespace nsf
+{
+    template <typename T>
+    struct HostCsr
+    {
+        int rows = 0, cols = 0;
+        std::vector<int> rowStart; // rows + 1
+        std::vector<int> col;      // sorted within each row
+        std::vector<T> val;
+
+        int nnz() const { return (int)col.size(); }
+    };
+
+    // Corner mesh + P2 (velocity) and P1 (pressure) numbering.
+    struct Mesh
+    {
+        // corner mesh (cpp/libs/Mesh/include/mesh/triMesh.h:46-52)
+        std::vector<float> cornerXY;      // 2 * V
+        std::vector<int> tri;             // 3 * T
+        std::vector<int> border;          // 3 * B: triangle, side, group
+        std::vector<std::string> groups;
+        // P2 / P1 (cpp/libs/Mesh/include/mesh/concreteMesh.h:11-58)
+        int N = 0, P = 0;
+        std::vector<float> vXY;           // 2 * N
+        std::vector<int> vElem;           // 6 * T
+        std::vector<int> vBorder;         // 6 * B: triangle, side, group, A, mid, B
+        std::vector<int> pElem;           // 3 * T
+        std::vector<int> pBorder;         // 5 * B
+        std::vector<float> affine;        // 6 * T: m00 m01 m10 m11 b0 b1
+
+        int numTri() const { return (int)tri.size() / 3; }
+        int numBorder() const { return (int)border.size() / 3; }
+        int groupId(const std::string & name) const;
+    };
+
+    // throws std::runtime_error with a message on parse errors
+    Mesh loadGmsh(const std::string & path);
+
+    struct Context
+    {
+        int N = 0, P = 0;
+        std::vector<int> dirIds;       // sorted Dirichlet velocity nodes (x and y share ids)
+        std::vector<double> dirVx;     // inflow values (float-rounded as the reference computes them)
+        std::vector<int> dirPIds;      // Dirichlet pressure nodes (Right border)
+        std::vector<int> intV, intP;   // complements
+        HostCsr<double> M, K, Kp, Kpi, D, G, I;
+    };
+
+    Context buildChannelContext(const Mesh & mesh, float peakVelocity, int nThreads);
+
+    HostCsr<double> sliceCsr(const HostCsr<double> & a, const std::vector<int> & rows, const std::vector<int> & cols);
+
+    struct Coloring
+    {
+        std::vector<int> perm;       // new -> old
+        std::vector<int> partStart;  // nColors + 1
+        int colors() const { return (int)partStart.size() - 1; }
+    };
+
+    Coloring colorGraph(int n, const int * rowStart, const int * col);
+
+    // P A P^T for a symmetric permutation perm (new -> old)
+    HostCsr<double> permuteSym(const HostCsr<double> & a, const std::vector<int> & perm);
+
+    // validates a CSR: sizes, rowStart monotone, columns sorted/unique/in range
+    bool validCsr(int rows, int cols, int nnz, const int * rowStart, const int * col, std::string & why);
+} // namespace nsf

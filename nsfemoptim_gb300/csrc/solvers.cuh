@@ -1,0 +1,322 @@
+// Host-side solver objects over the device kernels: a color-permuted sweep system, CG
+// preconditioned by multicolor symmetric Gauss-Seidel, the reference's multicolor Gauss-Seidel
+// solver, and an FP64 iterative-refinement wrapper around an FP32 inner CG.
+//
+// Every solve is a sequence of "init" kernels followed by a loop whose body is a fixed kernel
+// sequence.  Eagerly the host runs the body in chunks of `checkInterval` iterations and polls one
+// device flag; under stream capture the loop becomes a conditional WHILE node whose body the first
+// kernel of an iteration ends on the device (cudaGraphSetConditional), so a captured time step
+// runs with no host synchronisation at all.
+#pragma once
+
+#include "device.cuh"
+#include "host/setup.hpp"
+#include "kernels.cuh"
+
+#include <cmath>
+#include <functional>
+
+namespace nsf
+{
+    // Run `body(stream, conditionalHandle)` as a device-terminated loop.
+    inline void deviceLoop(cudaStream_t s, cudaStream_t bodyStream, SolverState * stDev, int maxIters,
+                           int checkInterval, PinnedBuf<int> & flag,
+                           const std::function<void(cudaStream_t, unsigned long long)> & body)
+    {
+        cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+        NSF_CUDA(cudaStreamIsCapturing(s, &cs));
+        if (cs == cudaStreamCaptureStatusActive)
+        {
+            cudaGraph_t g = nullptr;
+            const cudaGraphNode_t * deps = nullptr;
+            size_t nd = 0;
+            NSF_CUDA(cudaStreamGetCaptureInfo(s, &cs, nullptr, &g, &deps, nullptr, &nd));
+            cudaGraphConditionalHandle h;
+            NSF_CUDA(cudaGraphConditionalHandleCreate(&h, g, 1, cudaGraphCondAssignDefault));
+            cudaGraphNodeParams prm = {};
+            prm.type = cudaGraphNodeTypeConditional;
+            prm.conditional.handle = h;
+            prm.conditional.type = cudaGraphCondTypeWhile;
+            prm.conditional.size = 1;
+            cudaGraphNode_t node;
+            NSF_CUDA(cudaGraphAddNode(&node, g, deps, nullptr, nd, &prm));
+            cudaGraph_t bodyGraph = prm.conditional.phGraph_out[0];
+            NSF_CUDA(cudaStreamUpdateCaptureDependencies(s, &node, nullptr, 1, cudaStreamSetCaptureDependencies));
+            NSF_CUDA(cudaStreamBeginCaptureToGraph(bodyStream, bodyGraph, nullptr, nullptr, 0,
+                                                   cudaStreamCaptureModeRelaxed));
+            body(bodyStream, (unsigned long long)h);
+            NSF_CUDA(cudaStreamEndCapture(bodyStream, &bodyGraph));
+            return;
+        }
+        int it = 0;
+        const int chunk = checkInterval < 1 ? 1 : checkInterval;
+        while (it <= maxIters)
+        {
+            for (int j = 0; j < chunk && it <= maxIters; j++, it++)
+                body(s, 0ull);
+            NSF_CUDA(cudaMemcpyAsync(flag.get(), &stDev->anyActive, sizeof(int), cudaMemcpyDeviceToHost, s));
+            NSF_CUDA(cudaStreamSynchronize(s));
+            if (*flag.get() == 0)
+                break;
+        }
+    }
+
+    template <typename T>
+    struct SweepSystem
+    {
+        int n = 0, nnzFull = 0, nColors = 0, L = 4;
+        std::vector<int> ps; // color starts (host), nColors + 1
+        DevBuf<int> rsF, ciF, rsO, ciO;
+        DevBuf<T> vF, vO, invD;
+
+        // a: color-permuted square matrix (rows of color c contiguous), ps: color starts
+        void build(const HostCsr<double> & a, const std::vector<int> & partStart)
+        {
+            n = a.rows;
+            ps = partStart;
+            nColors = (int)ps.size() - 1;
+            nnzFull = a.nnz();
+            std::vector<int> ro(n + 1, 0), co;
+            std::vector<T> vo, vf(a.val.begin(), a.val.end()), id(n);
+            co.reserve(a.nnz());
+            vo.reserve(a.nnz());
+            for (int r = 0; r < n; r++)
+            {
+                bool diag = false;
+                for (int j = a.rowStart[r]; j < a.rowStart[r + 1]; j++)
+                {
+                    if (a.col[j] == r)
+                    {
+                        if (a.val[j] == 0)
+                            throw Error(ST_INVALID, "zero on the diagonal at row " + std::to_string(r));
+                        id[r] = (T)(1.0 / a.val[j]);
+                        diag = true;
+                    }
+                    else
+                    {
+                        co.push_back(a.col[j]);
+                        vo.push_back((T)a.val[j]);
+                    }
+                }
+                if (!diag)
+                    throw Error(ST_INVALID, "missing diagonal at row " + std::to_string(r));
+                ro[r + 1] = (int)co.size();
+            }
+            rsF.upload(a.rowStart);
+            ciF.upload(a.col);
+            vF.upload(vf);
+            rsO.upload(ro);
+            ciO.upload(co);
+            vO.upload(vo);
+            invD.upload(id);
+            L = lanesFor(a.nnz(), n);
+        }
+
+        int phaseBlocks(int c) const { return blocksFor((long long)(ps[c + 1] - ps[c]) * L); }
+    };
+
+    // ------------------------------------------------------------------ PCG with multicolor SGS
+    template <typename T, int NCH>
+    struct PcgSolver
+    {
+        const SweepSystem<T> * sys = nullptr;
+        int numCh = 1;
+        DevBuf<T> r, z, p, q;
+        DevBuf<double> rrPart, rzPart, pqPart, bbPart;
+        DevBuf<SolverState> st;
+        std::vector<int> slotBase;
+        PcgPtrs P{};
+        PinnedBuf<int> flag{1};
+
+        void setup(const SweepSystem<T> * s, int channels)
+        {
+            sys = s;
+            numCh = channels;
+            const int n = s->n;
+            r.alloc((size_t)NCH * n);
+            z.alloc((size_t)NCH * n);
+            p.alloc((size_t)2 * NCH * n);
+            q.alloc((size_t)NCH * n);
+            slotBase.assign(s->nColors + 1, 0);
+            for (int c = 0; c < s->nColors; c++)
+                slotBase[c + 1] = slotBase[c] + s->phaseBlocks(c);
+            const int slots = slotBase.back();
+            const int pqSlots = blocksFor((long long)n * s->L);
+            rrPart.alloc((size_t)MAXCH * slots);
+            rzPart.alloc((size_t)MAXCH * slots);
+            bbPart.alloc((size_t)MAXCH * slots);
+            pqPart.alloc((size_t)MAXCH * pqSlots);
+            st.alloc(1);
+            P.n = n;
+            P.slots = slots;
+            P.rrPart = rrPart.get();
+            P.rzPart = rzPart.get();
+            P.pqPart = pqPart.get();
+            P.pqSlots = pqSlots;
+            P.bbPart = bbPart.get();
+            P.st = st.get();
+            P.cond = 0;
+        }
+
+        void sgs(cudaStream_t s, PcgPtrs PP, int init, T * x, bool tickLast)
+        {
+            const SweepSystem<T> & S = *sys;
+            const int C = S.nColors;
+            T * pbuf = p.get();
+            NSF_LANES(S.L, {
+                for (int c = 0; c < C; c++)
+                    NSF_LAUNCH((kPcgForward<T, LL, NCH>), S.phaseBlocks(c), s, PP, numCh, init, S.ps[c], S.ps[c + 1],
+                               c == C - 1 ? 1 : 0, slotBase[c], S.rsO.get(), S.ciO.get(), S.vO.get(), S.invD.get(), x,
+                               r.get(), z.get(), pbuf, q.get());
+                for (int c = C - 2; c >= 0; c--)
+                    NSF_LAUNCH((kPcgBackward<T, LL, NCH>), S.phaseBlocks(c), s, PP, numCh, init, S.ps[c],
+                               S.ps[c + 1], slotBase[c], (tickLast && c == 0) ? 1 : 0, S.rsO.get(), S.ciO.get(),
+                               S.vO.get(), S.invD.get(), r.get(), z.get());
+            });
+            if (!init && C < 2)
+                NSF_LAUNCH(kTick, 1, s, PP.st);
+        }
+
+        // Solve A x = b (device, planar numCh * n, x = initial guess).  Configuration is passed
+        // through `cfg` (tolerance, iteration cap) and written to the device state by kernel args.
+        void enqueue(cudaStream_t s, cudaStream_t bodyStream, const T * b, T * x, int maxIters, double tol,
+                     bool absolute, int checkInterval)
+        {
+            const SweepSystem<T> & S = *sys;
+            SolverState init{};
+            init.maxIters = maxIters;
+            init.absMode = absolute ? 1 : 0;
+            init.tol2 = absolute ? tol * tol * (double)S.n : tol * tol;
+            // the config lives in kernel arguments: kSetConfig copies it before the init kernels
+            NSF_LAUNCH(kSetConfig, 1, s, st.get(), init.maxIters, init.absMode, init.tol2);
+            NSF_LANES(S.L, NSF_LAUNCH((kPcgInit<T, LL, NCH>), P.slots, s, P, S.rsF.get(), S.ciF.get(), S.vF.get(),
+                                      x, b, r.get()));
+            sgs(s, P, 1, x, false);
+            NSF_LAUNCH((kPcgStart<NCH>), 1, s, P, numCh);
+            deviceLoop(s, bodyStream, st.get(), maxIters, checkInterval, flag,
+                       [&](cudaStream_t bs, unsigned long long cond)
+                       {
+                           PcgPtrs PP = P;
+                           PP.cond = cond;
+                           NSF_LANES(S.L, NSF_LAUNCH((kPcgDirection<T, LL, NCH>), PP.pqSlots, bs, PP, numCh,
+                                                     S.rsF.get(), S.ciF.get(), S.vF.get(), z.get(), p.get(),
+                                                     q.get()));
+                           sgs(bs, PP, 0, x, true);
+                       });
+        }
+
+        int kernelsPerIteration() const { return 1 + 2 * sys->nColors - 1 + (sys->nColors < 2 ? 1 : 0); }
+        int initKernels() const { return 3 + 2 * sys->nColors - 1; }
+    };
+
+    // ------------------------------------------------------------------ multicolor GS ("gs")
+    template <typename T, int NCH>
+    struct GsSolver
+    {
+        const SweepSystem<T> * sys = nullptr;
+        int numCh = 1, interval = 1;
+        DevBuf<double> rrPart, bbPart;
+        DevBuf<SolverState> st;
+        GsPtrs P{};
+        PinnedBuf<int> flag{1};
+
+        void setup(const SweepSystem<T> * s, int channels, int checkInterval)
+        {
+            sys = s;
+            numCh = channels;
+            interval = checkInterval < 1 ? 1 : checkInterval;
+            const int slots = blocksFor((long long)s->n * s->L);
+            rrPart.alloc((size_t)MAXCH * slots);
+            bbPart.alloc((size_t)MAXCH * slots);
+            st.alloc(1);
+            P.n = s->n;
+            P.slots = slots;
+            P.rrPart = rrPart.get();
+            P.bbPart = bbPart.get();
+            P.st = st.get();
+            P.cond = 0;
+            P.interval = interval;
+        }
+
+        void enqueue(cudaStream_t s, cudaStream_t bodyStream, const T * b, T * x, int maxIters, double tol,
+                     bool absolute, int hostCheck)
+        {
+            const SweepSystem<T> & S = *sys;
+            const double tol2 = absolute ? tol * tol * (double)S.n : tol * tol;
+            NSF_LAUNCH(kSetConfig, 1, s, st.get(), maxIters, absolute ? 1 : 0, tol2);
+            NSF_LAUNCH((kGsInit<T, NCH>), P.slots, s, P, numCh, b);
+            NSF_LAUNCH((kGsStart<NCH>), 1, s, P, numCh);
+            deviceLoop(s, bodyStream, st.get(), maxIters, hostCheck, flag,
+                       [&](cudaStream_t bs, unsigned long long cond)
+                       {
+                           GsPtrs PP = P;
+                           PP.cond = cond;
+                           NSF_LANES(S.L, {
+                               for (int c = 0; c < S.nColors; c++)
+                                   NSF_LAUNCH((kGsPhase<T, LL, NCH>), S.phaseBlocks(c), bs, PP, numCh, S.ps[c],
+                                              S.ps[c + 1], c == 0 ? 1 : 0, S.rsO.get(), S.ciO.get(), S.vO.get(),
+                                              S.invD.get(), b, x);
+                               NSF_LAUNCH((kGsCheck<T, LL, NCH>), PP.slots, bs, PP, numCh, S.rsF.get(), S.ciF.get(),
+                                          S.vF.get(), b, x);
+                           });
+                       });
+        }
+
+        int kernelsPerIteration() const { return sys->nColors + 1; }
+        int initKernels() const { return 3; }
+    };
+
+    // ------------------------------------------------------------------ FP64 refinement, FP32 inner
+    template <int NCH>
+    struct MixedPcg
+    {
+        const SweepSystem<double> * sys64 = nullptr;
+        PcgSolver<float, NCH> inner;
+        int numCh = 1;
+        DevBuf<float> b32, d32;
+        DevBuf<double> rrPart, bbPart;
+        DevBuf<SolverState> st;
+        int slots = 0;
+        PinnedBuf<int> flag{1};
+
+        void setup(const SweepSystem<double> * s64, const SweepSystem<float> * s32, int channels)
+        {
+            sys64 = s64;
+            numCh = channels;
+            inner.setup(s32, channels);
+            b32.alloc((size_t)NCH * s64->n);
+            d32.alloc((size_t)NCH * s64->n);
+            slots = blocksFor((long long)s64->n * s64->L);
+            rrPart.alloc((size_t)MAXCH * slots);
+            bbPart.alloc((size_t)MAXCH * slots);
+            st.alloc(1);
+        }
+
+        // Passes of: r = b - A x in FP64 (also the FP32 inner right-hand side) -> stop decision ->
+        // FP32 inner PCG from zero -> x += d in FP64.  The stop decision is a sticky device flag
+        // (SolverState::skip) that turns the remaining passes into early exits, so the pass count
+        // is fixed at enqueue time and the whole solve can be captured.
+        void enqueue(cudaStream_t s, cudaStream_t bodyStream, const double * b, double * x, int maxOuter,
+                     double tol, int innerMaxIters, double innerTol, int checkInterval)
+        {
+            const SweepSystem<double> & S = *sys64;
+            const int n = S.n;
+            SolverState * sd = st.get();
+            NSF_LAUNCH(kSetConfig, 1, s, sd, maxOuter, 0, tol * tol);
+            NSF_LAUNCH(kOuterReset, 1, s, sd);
+            inner.P.skip = &sd->skip;
+            for (int pass = 0; pass <= maxOuter; pass++)
+            {
+                NSF_LANES(S.L, NSF_LAUNCH((kResidual<LL, NCH>), slots, s, n, slots, sd, S.rsF.get(), S.ciF.get(),
+                                          S.vF.get(), x, b, b32.get(), rrPart.get(), bbPart.get()));
+                NSF_LAUNCH((kOuterDecide<NCH>), 1, s, sd, inner.st.get(), numCh, slots, rrPart.get(), bbPart.get(),
+                           pass);
+                if (pass == maxOuter)
+                    break;
+                NSF_CUDA(cudaMemsetAsync(d32.get(), 0, sizeof(float) * NCH * n, s));
+                inner.enqueue(s, bodyStream, b32.get(), d32.get(), innerMaxIters, innerTol, false, checkInterval);
+                NSF_LAUNCH((kAddTo<float>), blocksFor((long long)NCH * n), s, NCH * n, x, d32.get(), &sd->skip);
+            }
+        }
+    };
+} // namespace nsf

@@ -1,0 +1,260 @@
+"""GPU parity of the sm_103a path against the FP64 C oracle, through the C ABI.
+
+Tolerances (FP64 kernels vs the FP64 oracle; differences come only from summation order):
+  SpMV / SpMM / FastConvection     max |diff| <= 1e-13 * max |y|
+  PCG-SGS (same algorithm)         iteration count within 1, solution rel. L2 diff <= 1e-8
+  multicolor GS (same algorithm)   identical iteration index, solution rel. L2 diff <= 1e-10
+  Chorin step FP64 vs oracle       velocity / pressure rel. L2 diff <= 1e-7 after 5 steps
+  Chorin mixed vs FP64 oracle      velocity rel. L2 <= 1e-5, pressure rel. L2 <= 1e-4 after 5 steps
+"""
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def torch_cuda():
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    return torch
+
+
+@pytest.fixture(scope="module")
+def setup(torch_cuda, channel_coarse, oracle_lib):
+    import nsfemoptim_gb300 as G
+    O = oracle_lib
+    mesh = G.load_gmsh(channel_coarse)
+    ctx = G.build_chorin_context(mesh, 1.2)
+    om = O.Mesh(channel_coarse)
+    oc = O.Context(om, 1.2, True)
+    return G, O, mesh, ctx, om, oc
+
+
+def _rel(a, b):
+    return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+
+
+def test_spmv_fp64(setup, torch_cuda):
+    G, O, mesh, ctx, om, oc = setup
+    t = torch_cuda
+    rng = np.random.default_rng(1)
+    for name in ("D", "G", "M", "Kpi"):
+        a = ctx.matrix(name)
+        x = rng.standard_normal(a.cols)
+        A = G.CsrF.from_host(a)
+        y = t.zeros(a.rows, dtype=t.float64, device="cuda")
+        G.spmv(A, t.tensor(x, device="cuda"), y)
+        ref = O.spmv(getattr(oc, name), x)
+        assert np.max(np.abs(y.cpu().numpy() - ref)) <= 1e-13 * np.max(np.abs(ref)), name
+
+
+def test_spmv_alpha_beta_and_fp32(setup, torch_cuda):
+    G, O, mesh, ctx, om, oc = setup
+    t = torch_cuda
+    a = ctx.matrix("D")
+    rng = np.random.default_rng(2)
+    x = rng.standard_normal(a.cols)
+    y0 = rng.standard_normal(a.rows)
+    A = G.CsrF.from_host(a)
+    y = t.tensor(y0, device="cuda")
+    G.spmv(A, t.tensor(x, device="cuda"), y, alpha=-2.0, beta=0.5)
+    ref = -2.0 * O.spmv(oc.D, x) + 0.5 * y0
+    assert np.max(np.abs(y.cpu().numpy() - ref)) <= 1e-13 * np.max(np.abs(ref))
+    A32 = G.CsrF.from_host(a, dtype=G.NSF_F32)
+    y32 = t.zeros(a.rows, dtype=t.float32, device="cuda")
+    G.spmv(A32, t.tensor(x, dtype=t.float32, device="cuda"), y32)
+    ref = O.spmv(oc.D, x)
+    assert np.max(np.abs(y32.cpu().numpy() - ref)) <= 1e-5 * np.max(np.abs(ref))
+
+
+def test_spmm_two_channels(setup, torch_cuda):
+    G, O, mesh, ctx, om, oc = setup
+    t = torch_cuda
+    k = ctx.matrix("K")
+    rng = np.random.default_rng(3)
+    x = rng.standard_normal(2 * k.cols)
+    A = G.CsrF.from_host(k)
+    y = t.zeros(2 * k.rows, dtype=t.float64, device="cuda")
+    G.spmm(A, t.tensor(x, device="cuda"), y, 2)
+    ref = O.spmm2(oc.K, oc.K.val, x)
+    assert np.max(np.abs(y.cpu().numpy() - ref)) <= 1e-13 * np.max(np.abs(ref))
+
+
+def test_fastconv(setup, torch_cuda):
+    G, O, mesh, ctx, om, oc = setup
+    t = torch_cuda
+    rng = np.random.default_rng(4)
+    u = rng.uniform(-1, 1.5, 2 * ctx.N)
+    I = G.CsrF.from_host(ctx.matrix("I"))
+    K = t.tensor(ctx.matrix("K").values, device="cuda")
+    A = t.zeros_like(K)
+    G.fastconv_apply(I, K, 1e-3, t.tensor(u, device="cuda"), A)
+    ref = O.fastconv(oc, 1e-3, u)
+    assert np.max(np.abs(A.cpu().numpy() - ref)) <= 1e-13 * np.max(np.abs(ref))
+
+
+def test_pcg_pressure_matches_oracle(setup, torch_cuda):
+    G, O, mesh, ctx, om, oc = setup
+    t = torch_cuda
+    kpi = ctx.matrix("Kpi")
+    rng = np.random.default_rng(5)
+    b = rng.standard_normal(kpi.rows)
+    s = G.create_solver("pcg", 1, kpi, 2000, 1e-10, 1)
+    s.getRhs().copy_(t.tensor(b))
+    s.getSol().zero_()
+    assert s.solve() == 0
+    x = s.getSol().cpu().numpy()
+    col = O.coloring(oc.Kpi)
+    xo, st, it, rr = O.pcg(oc.Kpi, col, b, np.zeros_like(b), 2000, 1e-10)
+    assert st == 0
+    assert abs(s.getLastIterations() - it) <= 1
+    assert s.getLastRelativeResidual(0) <= 1e-10
+    assert _rel(x, xo) <= 1e-8
+    r = b - O.spmv(oc.Kpi, x)
+    assert np.linalg.norm(r) <= 1.01e-10 * np.linalg.norm(b)
+
+
+def test_pcg_mass_two_channels_warm_start(setup, torch_cuda):
+    G, O, mesh, ctx, om, oc = setup
+    t = torch_cuda
+    m = ctx.matrix("M")
+    rng = np.random.default_rng(6)
+    b = rng.standard_normal(2 * m.rows)
+    x0 = 0.1 * rng.standard_normal(2 * m.rows)
+    s = G.create_solver("pcg", 2, m, 500, 1e-11, 4)
+    s.getRhs().copy_(t.tensor(b))
+    s.getSol().copy_(t.tensor(x0))
+    assert s.solve() == 0
+    x = s.getSol().cpu().numpy()
+    col = O.coloring(oc.M)
+    n = m.rows
+    for c in range(2):
+        xo, st, it, rr = O.pcg(oc.M, col, b[c * n:(c + 1) * n], x0[c * n:(c + 1) * n], 500, 1e-11)
+        assert st == 0
+        assert _rel(x[c * n:(c + 1) * n], xo) <= 1e-8
+
+
+def test_gs_solver_matches_oracle(setup, torch_cuda):
+    G, O, mesh, ctx, om, oc = setup
+    t = torch_cuda
+    m = ctx.matrix("M")
+    rng = np.random.default_rng(7)
+    b = rng.standard_normal(2 * m.rows) * 1e-4
+    target = 1e-12
+    s = G.create_solver("gs", 2, m, 300, target, 1)
+    s.getRhs().copy_(t.tensor(b))
+    s.getSol().zero_()
+    assert s.solve() == 0
+    x = s.getSol().cpu().numpy()
+    col = O.coloring(oc.M)
+    xo, rms, it = O.gs_solve(oc.M, col, 2, b, np.zeros_like(b), 300, target, 1)
+    assert s.getLastIterations() == it
+    assert _rel(x, xo) <= 1e-10
+    assert max(s.getLastMse(0), s.getLastMse(1)) < target
+
+
+def test_mixed_pcg_reaches_fp64_tolerance(setup, torch_cuda):
+    G, O, mesh, ctx, om, oc = setup
+    t = torch_cuda
+    kpi = ctx.matrix("Kpi")
+    rng = np.random.default_rng(8)
+    b = rng.standard_normal(kpi.rows)
+    s = G.create_solver("pcg", 1, kpi, 2000, 1e-10, 1, precision=G.NSF_PREC_MIXED)
+    s.getRhs().copy_(t.tensor(b))
+    s.getSol().zero_()
+    assert s.solve() == 0
+    x = s.getSol().cpu().numpy()
+    r = b - O.spmv(oc.Kpi, x)
+    assert np.linalg.norm(r) <= 1.01e-10 * np.linalg.norm(b)
+    xo, st, it, rr = O.pcg(oc.Kpi, O.coloring(oc.Kpi), b, np.zeros_like(b), 4000, 1e-13)
+    assert _rel(x, xo) <= 1e-7
+
+
+def test_solver_errors(setup, torch_cuda):
+    G, O, mesh, ctx, om, oc = setup
+    import nsfemoptim_gb300 as G2
+    kpi = ctx.matrix("Kpi")
+    with pytest.raises(G2.NsfError):
+        G.create_solver("lu", 1, kpi, 10, 1e-6, 1)
+    with pytest.raises(G2.NsfError):
+        G.create_solver("pcg", 1, kpi, 10, 1e-6, 0)
+    # iteration cap reached: status NSF_ERR_MAXITER, solve returns the status
+    s = G.create_solver("pcg", 1, kpi, 3, 1e-14, 1)
+    s.getRhs().copy_(torch_cuda.ones(kpi.rows, dtype=torch_cuda.float64))
+    s.getSol().zero_()
+    assert s.solve() == 3
+    # non-SPD (negated) matrix: breakdown
+    neg = G2.api.HostCsr(kpi.rows, kpi.cols, kpi.rowStart, kpi.column, -kpi.values)
+    with pytest.raises(G2.NsfError):
+        G.create_solver("pcg", 1, neg, 10, 1e-6, 1).solve(raise_on_status=True)
+
+
+def _oracle_steps(O, oc, nu, tau, steps, vel_method=1):
+    ch = O.Chorin(oc, nu, tau, vel_method=vel_method, vel_max_iters=300, vel_tol=1e-10 if vel_method else 1e-10,
+                  pres_max_iters=3000, pres_tol=1e-10)
+    for _ in range(steps):
+        ch.step()
+    return ch.state()
+
+
+@pytest.mark.parametrize("graph", [True, False])
+def test_chorin_fp64_matches_oracle(setup, torch_cuda, graph):
+    G, O, mesh, ctx, om, oc = setup
+    st = G.ChorinStepper(ctx, 1e-3, 1e-3, vel_method=1, vel_max_iters=300, vel_tol=1e-10, pres_max_iters=3000,
+                         pres_tol=1e-10, use_graph=graph)
+    st.step(5)
+    u, p = st.state()
+    uo, po = _oracle_steps(O, oc, 1e-3, 1e-3, 5)
+    assert _rel(u, uo) <= 1e-7
+    assert _rel(p, po) <= 1e-7
+    s = st.stats()
+    assert s["status"] == 0 and s["pres_rel"] <= 1e-10
+
+
+def test_chorin_graph_equals_eager_bitwise(setup, torch_cuda):
+    G, O, mesh, ctx, om, oc = setup
+    a = G.ChorinStepper(ctx, 1e-3, 1e-3, pres_tol=1e-9, use_graph=True)
+    b = G.ChorinStepper(ctx, 1e-3, 1e-3, pres_tol=1e-9, use_graph=False)
+    a.step(3)
+    b.step(3)
+    ua, pa = a.state()
+    ub, pb = b.state()
+    assert np.array_equal(ua, ub) and np.array_equal(pa, pb)
+
+
+def test_chorin_gs_velocity_matches_oracle(setup, torch_cuda):
+    G, O, mesh, ctx, om, oc = setup
+    st = G.ChorinStepper(ctx, 1e-3, 1e-3, vel_method=0, vel_max_iters=300, vel_tol=1e-10, pres_max_iters=3000,
+                         pres_tol=1e-10)
+    st.step(3)
+    u, p = st.state()
+    uo, po = _oracle_steps(O, oc, 1e-3, 1e-3, 3, vel_method=0)
+    assert _rel(u, uo) <= 1e-7
+    assert _rel(p, po) <= 1e-7
+
+
+def test_chorin_mixed_vs_fp64_oracle(setup, torch_cuda):
+    G, O, mesh, ctx, om, oc = setup
+    st = G.ChorinStepper(ctx, 1e-3, 1e-3, precision=G.NSF_PREC_MIXED, vel_max_iters=300, vel_tol=1e-10,
+                         pres_max_iters=3000, pres_tol=1e-10)
+    st.step(5)
+    u, p = st.state()
+    uo, po = _oracle_steps(O, oc, 1e-3, 1e-3, 5)
+    assert _rel(u, uo) <= 1e-5
+    assert _rel(p, po) <= 1e-4
+    assert st.stats()["pres_rel"] <= 1e-10
+
+
+def test_chorin_state_roundtrip(setup, torch_cuda):
+    G, O, mesh, ctx, om, oc = setup
+    st = G.ChorinStepper(ctx, 1e-3, 1e-3)
+    rng = np.random.default_rng(9)
+    u = rng.standard_normal(2 * ctx.N)
+    p = np.zeros(ctx.P)
+    p[ctx.int_p] = rng.standard_normal(len(ctx.int_p))
+    st.set_state(u, p)
+    u2, p2 = st.state()
+    assert np.array_equal(u, u2) and np.array_equal(p, p2)

@@ -1,0 +1,199 @@
+"""The oracle pinned against the reference's own code.
+
+* Golden fixtures (tests/golden/ref_*.json): digests of integer structures that the reference's
+  C++ produced from the committed synthetic meshes (tests/golden/make_golden.py).  These run
+  everywhere.
+* Live comparison against oracle/_ref/libnsfref.so (the reference sources compiled here) on the
+  committed meshes and on the reference's own shipped meshes when the reference tree is present.
+"""
+
+import hashlib
+import json
+import os
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN, REFERENCE_ASSETS
+
+
+def digest(a):
+    a = np.ascontiguousarray(a)
+    return hashlib.sha256(a.astype(a.dtype.newbyteorder("<")).tobytes()).hexdigest()
+
+
+def _golden(name):
+    with open(os.path.join(GOLDEN, f"ref_{name}.json")) as f:
+        return json.load(f)
+
+
+def _check_against_golden(O, path, g, with_bcs):
+    m = O.Mesh(path)
+    assert m.groups == g["groups"]
+    c = g["counts"]
+    assert (m.num_corner, m.num_tri, m.num_border, m.N, m.P) == (c["corner"], c["triangles"], c["border"], c["N"],
+                                                                  c["P"])
+    sh = g["sha256"]
+    assert digest(m.v_elem.ravel()) == sh["v_elem"]
+    assert digest(m.p_elem.ravel()) == sh["p_elem"]
+    assert digest(m.v_xy.ravel()) == sh["v_xy"]
+    assert digest(m.v_border.ravel()) == sh["v_border"]
+    ctx = O.Context(m, g.get("peak_velocity", 1.0), True)
+    if with_bcs:
+        assert digest(ctx.dir_ids) == sh["dir_ids"]
+        assert digest(ctx.dir_vx.astype(np.float32)) == sh["dir_vx"]
+        assert np.array_equal(ctx.dir_vx, ctx.dir_vx.astype(np.float32).astype(np.float64))
+        assert digest(ctx.dir_p_ids) == sh["dir_p_ids"]
+        assert digest(ctx.int_v) == sh["int_v"]
+        assert digest(ctx.int_p) == sh["int_p"]
+    for name in ("M", "Kp", "D", "G", "I"):
+        a = getattr(ctx, name)
+        assert digest(a.rowStart) == sh[f"{name}_rowStart"], name
+        assert digest(a.col) == sh[f"{name}_col"], name
+    perm, part, sl = O.coloring(ctx.M)
+    assert digest(perm) == sh["color_M_perm"]
+    assert digest(sl) == sh["color_M_slorder"]
+    assert part.tolist() == g["color_M_partStart"]
+    if with_bcs:
+        assert digest(ctx.Kpi.rowStart) == sh["Kpi_rowStart"]
+        assert digest(ctx.Kpi.col) == sh["Kpi_col"]
+        perm, part, sl = O.coloring(ctx.Kpi)
+        assert digest(perm) == sh["color_Kpi_perm"]
+        assert digest(sl) == sh["color_Kpi_slorder"]
+        assert part.tolist() == g["color_Kpi_partStart"]
+    return m, ctx
+
+
+def test_oracle_matches_reference_golden_channel(oracle_lib, channel_coarse):
+    _check_against_golden(oracle_lib, channel_coarse, _golden("channel_h0.025_s0"), True)
+
+
+def test_oracle_matches_reference_golden_square(oracle_lib, square_small):
+    _check_against_golden(oracle_lib, square_small, _golden("square_n33_s0"), True)
+
+
+def test_fem_identities(oracle_lib, channel_coarse):
+    """Values are restated (the reference integrator needs OpenCV): check the physics instead."""
+    O = oracle_lib
+    m = O.Mesh(channel_coarse)
+    ctx = O.Context(m, 1.2, True)
+    area = 2.2 * 0.41 - np.pi * 0.05 ** 2
+    # the mass matrix sums to the (polygonal) domain area; stiffness rows sum to zero
+    assert abs(ctx.M.val.sum() - area) < 2e-4
+    ones = np.ones(ctx.N)
+    assert np.max(np.abs(O.spmv(ctx.K, ones))) < 1e-11
+    assert np.max(np.abs(O.spmv(ctx.Kp, np.ones(ctx.P)))) < 1e-11
+    # symmetry of M, K, Kp
+    for a in (ctx.M, ctx.K, ctx.Kp):
+        s = a.to_scipy()
+        assert abs(s - s.T).max() < 1e-14 * abs(s).max()
+    # divergence of a constant field and gradient of a constant pressure vanish
+    assert np.max(np.abs(O.spmv(ctx.D, np.r_[ones, np.zeros(ctx.N)]))) < 1e-12
+    assert np.max(np.abs(O.spmv(ctx.G, np.ones(ctx.P)))) < 1e-12
+    # D u + G^T u is a boundary term: zero for a field vanishing on the boundary
+    # (integration by parts), checked with u = bubble-like interior field
+    xy = m.v_xy.astype(np.float64)
+    bub = xy[:, 0] * (2.2 - xy[:, 0]) * xy[:, 1] * (0.41 - xy[:, 1]) * \
+        np.maximum(0, (xy[:, 0] - 0.2) ** 2 + (xy[:, 1] - 0.2) ** 2 - 0.05 ** 2)
+    bub[ctx.dir_ids] = 0
+    onb = np.zeros(ctx.N, bool)
+    onb[ctx.dir_ids] = True
+    u = np.r_[bub, 0.5 * bub]
+    lhs = O.spmv(ctx.D, u)
+    rhs = -ctx.G.to_scipy().T @ u
+    assert np.max(np.abs(lhs[ctx.int_p] - rhs[ctx.int_p])) < 1e-12 * np.max(np.abs(lhs))
+    # FastConvection: I u gives the convection values C(u); C(u) applied to a constant is zero
+    rng = np.random.default_rng(0)
+    uu = rng.standard_normal(2 * ctx.N)
+    cvals = O.fastconv(ctx, 0.0, uu)
+    c = O.Csr(ctx.K.rows, ctx.K.cols, ctx.K.rowStart, ctx.K.col, cvals)
+    assert np.max(np.abs(O.spmv(c, ones))) < 1e-11 * np.max(np.abs(cvals))
+
+
+def _reference():
+    import oracle
+    R = oracle.reference()
+    if R is None:
+        pytest.skip("reference harness (oracle/_ref) not built on this machine")
+    return R
+
+
+def _ref_meshes():
+    out = []
+    for name in ("h_0.025.msh", "h_0.01.msh"):
+        p = os.path.join(REFERENCE_ASSETS, name)
+        if os.path.exists(p):
+            out.append(p)
+    return out
+
+
+@pytest.mark.parametrize("which", ["committed", "reference"])
+def test_oracle_matches_live_reference(oracle_lib, channel_coarse, which):
+    import ctypes as C
+    R = _reference()
+    O = oracle_lib
+    paths = [channel_coarse] if which == "committed" else _ref_meshes()
+    if not paths:
+        pytest.skip("reference meshes not present")
+    for path in paths:
+        h = R.ref_mesh_load(path.encode())
+        assert h, R.ref_last_error()
+        c = (C.c_int * 6)()
+        R.ref_mesh_counts(h, c)
+        m = O.Mesh(path)
+        assert list(c)[:5] == [m.num_corner, m.num_tri, m.num_border, m.N, m.P]
+        e2 = np.zeros(6 * m.num_tri, np.int32)
+        R.ref_mesh_elements(h, 2, O._ptr(e2, C.c_int))
+        assert np.array_equal(e2.reshape(-1, 6), m.v_elem)
+        ctx = O.Context(m, 1.2, True)
+        for w, name in enumerate(["M", "Kp", "D", "G", "I"]):
+            ph = R.ref_prototype(h, w)
+            dims = (C.c_int * 3)()
+            R.ref_csr_dims(ph, dims)
+            rs = np.zeros(dims[0] + 1, np.int32)
+            cl = np.zeros(dims[2], np.int32)
+            R.ref_csr_arrays(ph, O._ptr(rs, C.c_int), O._ptr(cl, C.c_int), None)
+            R.ref_csr_free(ph)
+            a = getattr(ctx, name)
+            assert np.array_equal(rs, a.rowStart) and np.array_equal(cl, a.col), name
+        a = ctx.Kpi
+        ph = R.ref_csr_wrap(a.rows, a.cols, a.nnz, O._ptr(a.rowStart, C.c_int), O._ptr(a.col, C.c_int), None)
+        nc = R.ref_coloring(ph, None, None, None)
+        order = np.zeros(a.rows, np.int32)
+        part = np.zeros(nc + 1, np.int32)
+        R.ref_coloring(ph, O._ptr(order, C.c_int), O._ptr(part, C.c_int), None)
+        R.ref_csr_free(ph)
+        perm, opart, _ = O.coloring(a)
+        assert np.array_equal(order, perm) and np.array_equal(part, opart)
+        R.ref_mesh_free(h)
+
+
+def test_multicolor_gs_matches_reference_gs2ch(oracle_lib, channel_coarse):
+    """A multicolor sweep equals a natural-order sweep of the color-permuted matrix; the reference's
+    double-precision gaussSeidel2ch on that matrix pins the oracle's sweep arithmetic."""
+    import ctypes as C
+    R = _reference()
+    O = oracle_lib
+    m = O.Mesh(channel_coarse)
+    ctx = O.Context(m, 1.2, False)
+    col = O.coloring(ctx.M)
+    perm = col[0]
+    Mp = O.slice_csr(ctx.M, perm, perm)
+    n = Mp.rows
+    rng = np.random.default_rng(3)
+    b = rng.standard_normal(2 * n)
+    x_ref = np.zeros(2 * n)
+    b_inter = np.empty(2 * n)
+    b_inter[0::2], b_inter[1::2] = b[:n], b[n:]
+    res = np.zeros(2)
+    iters = 7
+    R.ref_gs2ch_double(n, O._ptr(Mp.rowStart, C.c_int), O._ptr(Mp.col, C.c_int), O._ptr(Mp.val, C.c_double),
+                       O._ptr(x_ref, C.c_double), O._ptr(b_inter, C.c_double), iters, 0.0, O._ptr(res, C.c_double))
+    # oracle: the same 7 sweeps in the original numbering (target 0 -> never stops early)
+    b_orig = np.zeros(2 * n)
+    b_orig[perm], b_orig[n + perm] = b[:n], b[n:]
+    x, rms, it = O.gs_solve(ctx.M, col, 2, b_orig, np.zeros(2 * n), iters, 0.0, 1)
+    xo = np.r_[x[:n][perm], x[n:][perm]]
+    xr = np.r_[x_ref[0::2], x_ref[1::2]]
+    assert np.max(np.abs(xo - xr)) <= 1e-13 * np.max(np.abs(xr))
+    assert np.allclose(rms, res, rtol=1e-10)
