@@ -112,8 +112,59 @@ class _Builder:
                     self.tris.append((b, c, d))
 
 
-def dfg_channel(h: float, seed: int = 0, jitter: float = 0.15) -> TriMesh:
-    """DFG channel with cylinder; ``h`` is the gmsh-style characteristic length."""
+def dfg_channel(h: float, seed: int = 0, jitter: float = 0.12) -> TriMesh:
+    """DFG channel with cylinder: unstructured, near-equilateral triangles of side ~``h`` everywhere
+    (as gmsh meshes the reference's ``.geo`` files with lc = clc = h).
+
+    Points: a hexagonal lattice of spacing h jittered by U(+-jitter*h) from ``seed``, kept at least
+    0.5 h away from the walls and the cylinder, plus points every ~h along the four walls and the
+    cylinder; Delaunay triangulation (scipy) with the triangles inside the cylinder removed.  Every
+    cylinder chord is checked to be a mesh edge.
+    """
+    from scipy.spatial import Delaunay
+
+    L, H = 2.2, 0.41
+    cx, cy, r = 0.2, 0.2, 0.05
+    rng = np.random.Generator(np.random.PCG64(seed))
+    dy = h * math.sqrt(3.0) / 2.0
+    rows = []
+    for j in range(int(H / dy) + 2):
+        y = j * dy
+        off = 0.5 * h if (j % 2) else 0.0
+        xs = np.arange(off, L + h, h)
+        rows.append(np.stack([xs, np.full_like(xs, y)], axis=1))
+    lat = np.concatenate(rows)
+    lat += rng.uniform(-jitter * h, jitter * h, size=lat.shape)
+    d_wall = np.minimum.reduce([lat[:, 0], L - lat[:, 0], lat[:, 1], H - lat[:, 1]])
+    d_cyl = np.hypot(lat[:, 0] - cx, lat[:, 1] - cy) - r
+    lat = lat[(d_wall > 0.5 * h) & (d_cyl > 0.55 * h)]
+
+    def seg(p0, p1):
+        n = max(1, int(round(np.hypot(p1[0] - p0[0], p1[1] - p0[1]) / h)))
+        t = np.linspace(0.0, 1.0, n + 1)[:-1]
+        return np.stack([p0[0] + t * (p1[0] - p0[0]), p0[1] + t * (p1[1] - p0[1])], axis=1)
+
+    walls = np.concatenate([seg((0, 0), (L, 0)), seg((L, 0), (L, H)), seg((L, H), (0, H)), seg((0, H), (0, 0))])
+    nc = max(8, int(round(2 * math.pi * r / h)))
+    ang = np.linspace(0.0, 2 * math.pi, nc + 1)[:-1]
+    circ = np.stack([cx + r * np.cos(ang), cy + r * np.sin(ang)], axis=1)
+    pts = np.concatenate([walls, circ, lat])
+    tri = Delaunay(pts).simplices.astype(np.int64)
+    cen = pts[tri].mean(axis=1)
+    tri = tri[np.hypot(cen[:, 0] - cx, cen[:, 1] - cy) > r]
+    # every cylinder chord must be an edge of the triangulation
+    c0 = len(walls)
+    ed = np.sort(np.concatenate([tri[:, [0, 1]], tri[:, [1, 2]], tri[:, [2, 0]]]), axis=1)
+    edset = set(map(tuple, ed.tolist()))
+    for k in range(nc):
+        a, b = c0 + k, c0 + (k + 1) % nc
+        if (min(a, b), max(a, b)) not in edset:
+            raise RuntimeError("cylinder chord missing from the triangulation; try another seed")
+    return _finish(pts, tri, _channel_border(pts, tri, L, H, cx, cy, r))
+
+
+def dfg_channel_ogrid(h: float, seed: int = 0, jitter: float = 0.15) -> TriMesh:
+    """Structured variant: blocks around an O-grid ring at the cylinder (finer cells at the wall)."""
     L, H = 2.2, 0.41
     cx, cy, r = 0.2, 0.2, 0.05
     # equal area: right-isoceles cells s^2/2 == equilateral sqrt(3)/4 h^2

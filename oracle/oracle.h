@@ -96,6 +96,9 @@ int orc_permute(const orc_csr *a, const orc_coloring *c, orc_csr *out);
    iteration index as cu::GaussSeidel reports it. */
 int orc_gs_solve(const orc_csr *a, const orc_coloring *c, int numCh, const double *b, double *x,
                  int maxIters, double targetRms, int checkInterval, double *lastRms, int *lastIter);
+/* relative != 0: stop when ||r_c|| <= target * ||b_c|| for every channel */
+int orc_gs_solve_ex(const orc_csr *a, const orc_coloring *c, int numCh, const double *b, double *x,
+                    int maxIters, double target, int relative, int checkInterval, double *lastRms, int *lastIter);
 
 /* CG preconditioned by symmetric multicolor Gauss-Seidel (forward colors, then backward).
    precond: 0 = none, 1 = multicolor SGS. Stops when ||r|| <= relTol * ||b||.

@@ -113,7 +113,7 @@ static int mass_solve(orc_chorin *s, const double *rhs, double *acc, double *res
     {
         double rms[2];
         int it = 0;
-        orc_gs_solve(&ctx->M, &s->colM, 2, rhs, acc, s->cfg.velMaxIters, s->cfg.velTol, 1, rms, &it);
+        orc_gs_solve_ex(&ctx->M, &s->colM, 2, rhs, acc, s->cfg.velMaxIters, s->cfg.velTol, 1, 1, rms, &it);
         *res = rms[0] > rms[1] ? rms[0] : rms[1];
         return it;
     }

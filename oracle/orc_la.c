@@ -383,6 +383,13 @@ static void gs_phase(const gs_ctx *g, int r0, int r1, double *x, const double *b
 int orc_gs_solve(const orc_csr *a, const orc_coloring *c, int numCh, const double *b, double *x,
                  int maxIters, double targetRms, int checkInterval, double *lastRms, int *lastIter)
 {
+    return orc_gs_solve_ex(a, c, numCh, b, x, maxIters, targetRms, 0, checkInterval, lastRms, lastIter);
+}
+
+int orc_gs_solve_ex(const orc_csr *a, const orc_coloring *c, int numCh, const double *b, double *x,
+                    int maxIters, double target, int relative, int checkInterval, double *lastRms, int *lastIter)
+{
+    const double targetRms = target;
     gs_ctx g;
     memset(&g, 0, sizeof g);
     if (gs_ctx_build(a, c, &g))
@@ -400,6 +407,14 @@ int orc_gs_solve(const orc_csr *a, const orc_coloring *c, int numCh, const doubl
             xp[ch * n + i] = x[ch * n + c->perm[i]];
             bp[ch * n + i] = b[ch * n + c->perm[i]];
         }
+    double bRms[2] = {0, 0};
+    for (int ch = 0; ch < numCh && ch < 2; ch++)
+    {
+        double s = 0;
+        for (int i = 0; i < n; i++)
+            s += bp[ch * n + i] * bp[ch * n + i];
+        bRms[ch] = sqrt(s) / sqrt((double)n);
+    }
     for (int ch = 0; ch < numCh; ch++)
         lastRms[ch] = -1;
     int iter = 0;
@@ -421,7 +436,8 @@ int orc_gs_solve(const orc_csr *a, const orc_coloring *c, int numCh, const doubl
                     s += d * d;
                 }
                 lastRms[ch] = sqrt(s) / sqrt((double)n);
-                if (!(lastRms[ch] < targetRms))
+                /* absolute: RMS < target (cu::GaussSeidel); relative: ||r|| <= target * ||b|| */
+                if (relative ? !(lastRms[ch] <= targetRms * bRms[ch < 2 ? ch : 1]) : !(lastRms[ch] < targetRms))
                     done = 0;
             }
             if (done)
@@ -458,7 +474,7 @@ void orc_sgs_apply(const orc_csr *a, const orc_coloring *c, const double *r, dou
     memset(&g, 0, sizeof g);
     gs_ctx_build(a, c, &g);
     const int n = a->rows;
-    double *rp = (double *)malloc(sizeof(double) * n), *zp = (double *)malloc(sizeof(double) * n);
+    double *rp = (double *)calloc(n + 1, sizeof(double)), *zp = (double *)calloc(n + 1, sizeof(double));
     for (int i = 0; i < n; i++)
         rp[i] = r[c->perm[i]];
     sgs_colored(&g, c, rp, zp);

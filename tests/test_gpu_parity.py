@@ -186,10 +186,19 @@ def test_solver_errors(setup, torch_cuda):
     s.getRhs().copy_(torch_cuda.ones(kpi.rows, dtype=torch_cuda.float64))
     s.getSol().zero_()
     assert s.solve() == 3
-    # non-SPD (negated) matrix: breakdown
+    # non-SPD (negated) matrix: p^T A p < 0 at the first step -> NSF_ERR_BREAKDOWN
     neg = G2.api.HostCsr(kpi.rows, kpi.cols, kpi.rowStart, kpi.column, -kpi.values)
-    with pytest.raises(G2.NsfError):
-        G.create_solver("pcg", 1, neg, 10, 1e-6, 1).solve(raise_on_status=True)
+    sn = G.create_solver("pcg", 1, neg, 10, 1e-6, 1)
+    sn.getRhs().copy_(torch_cuda.ones(kpi.rows, dtype=torch_cuda.float64))
+    sn.getSol().zero_()
+    with pytest.raises(G2.NsfError) as e:
+        sn.solve(raise_on_status=True)
+    assert e.value.status == 4
+    # NaN right-hand side: NSF_ERR_NONFINITE, no hang
+    s2 = G.create_solver("pcg", 1, kpi, 10, 1e-6, 1)
+    s2.getRhs().fill_(float("nan"))
+    s2.getSol().zero_()
+    assert s2.solve() == 2
 
 
 def _oracle_steps(O, oc, nu, tau, steps, vel_method=1):

@@ -77,9 +77,13 @@ def test_fem_identities(oracle_lib, channel_coarse):
     O = oracle_lib
     m = O.Mesh(channel_coarse)
     ctx = O.Context(m, 1.2, True)
-    area = 2.2 * 0.41 - np.pi * 0.05 ** 2
-    # the mass matrix sums to the (polygonal) domain area; stiffness rows sum to zero
-    assert abs(ctx.M.val.sum() - area) < 2e-4
+    p = m.corner_xy.astype(np.float64)[m.tri]
+    area = 0.5 * np.abs((p[:, 1, 0] - p[:, 0, 0]) * (p[:, 2, 1] - p[:, 0, 1]) -
+                        (p[:, 2, 0] - p[:, 0, 0]) * (p[:, 1, 1] - p[:, 0, 1])).sum()
+    assert abs(area - (2.2 * 0.41 - np.pi * 0.05 ** 2)) < 1e-3
+    # the mass matrix sums to the (polygonal) domain area (the element maps use float edge
+    # vectors, as the reference's affine transforms do); stiffness rows sum to zero
+    assert abs(ctx.M.val.sum() - area) < 1e-9
     ones = np.ones(ctx.N)
     assert np.max(np.abs(O.spmv(ctx.K, ones))) < 1e-11
     assert np.max(np.abs(O.spmv(ctx.Kp, np.ones(ctx.P)))) < 1e-11
@@ -101,7 +105,7 @@ def test_fem_identities(oracle_lib, channel_coarse):
     u = np.r_[bub, 0.5 * bub]
     lhs = O.spmv(ctx.D, u)
     rhs = -ctx.G.to_scipy().T @ u
-    assert np.max(np.abs(lhs[ctx.int_p] - rhs[ctx.int_p])) < 1e-12 * np.max(np.abs(lhs))
+    assert np.max(np.abs(lhs[ctx.int_p] - rhs[ctx.int_p])) < 1e-9 * np.max(np.abs(lhs))
     # FastConvection: I u gives the convection values C(u); C(u) applied to a constant is zero
     rng = np.random.default_rng(0)
     uu = rng.standard_normal(2 * ctx.N)
