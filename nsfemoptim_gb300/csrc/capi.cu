@@ -90,14 +90,34 @@ namespace nsf
         return out;
     }
 
+    // Row blocks of the CSR-stream kernel: consecutive rows whose entries fit in STREAM_NNZ.
+    // Returns an empty vector if some row is longer than STREAM_NNZ (row-group kernel then).
+    std::vector<int> streamRowBlocks(const int * rowStart, int rows)
+    {
+        std::vector<int> rb{0};
+        int r = 0;
+        while (r < rows)
+        {
+            const int base = rowStart[r];
+            int e = r;
+            while (e < rows && rowStart[e + 1] - base <= STREAM_NNZ)
+                e++;
+            if (e == r)
+                return {};
+            rb.push_back(e);
+            r = e;
+        }
+        return rb;
+    }
+
     template <typename T>
     struct DevCsr
     {
-        int rows = 0, cols = 0, nnz = 0, L = 4;
-        DevBuf<int> rs, ci;
+        int rows = 0, cols = 0, nnz = 0, L = 4, nBlocks = 0;
+        DevBuf<int> rs, ci, rb;
         DevBuf<T> v;
 
-        void upload(const HostCsr<double> & a)
+        void upload(const HostCsr<double> & a, bool stream = false)
         {
             rows = a.rows;
             cols = a.cols;
@@ -107,6 +127,13 @@ namespace nsf
             std::vector<T> tv(a.val.begin(), a.val.end());
             v.upload(tv);
             L = lanesFor(nnz, rows);
+            if (stream)
+            {
+                std::vector<int> b = streamRowBlocks(a.rowStart.data(), rows);
+                nBlocks = (int)b.size() - 1;
+                if (nBlocks > 0)
+                    rb.upload(b);
+            }
         }
     };
 } // namespace nsf
@@ -125,8 +152,8 @@ struct nsf_context_s
 
 struct nsf_csr_s
 {
-    int rows = 0, cols = 0, nnz = 0, dtype = NSF_F64, L = 4;
-    DevBuf<int> rs, ci;
+    int rows = 0, cols = 0, nnz = 0, dtype = NSF_F64, L = 4, nBlocks = 0;
+    DevBuf<int> rs, ci, rb;
     DevBuf<double> v64;
     DevBuf<float> v32;
 };
@@ -336,6 +363,10 @@ extern "C" int nsf_csr_create(int rows, int cols, int nnz, const int * rowStart,
             h->v32.upload(v, nnz);
         }
         h->L = lanesFor(nnz, rows);
+        std::vector<int> rb = streamRowBlocks(rowStart, rows);
+        h->nBlocks = (int)rb.size() - 1;
+        if (h->nBlocks > 0)
+            h->rb.upload(rb);
         *out = h.release();
     });
 }
@@ -372,7 +403,7 @@ extern "C" int nsf_spmv(nsf_csr a, const void * x, void * y, double alpha, doubl
 {
     return guarded([&] {
         require(a && x && y, "null argument");
-        const int grid = blocksFor((long long)a->rows * a->L);
+        const int grid = cappedBlocks((long long)a->rows * a->L);
         cudaStream_t s = asStream(stream);
         if (a->dtype == NSF_F64)
         {
@@ -392,7 +423,7 @@ extern "C" int nsf_spmm(nsf_csr a, int nrhs, const void * X, int ldx, void * Y, 
     return guarded([&] {
         require(a && X && Y && nrhs >= 1, "bad argument");
         require(ldx >= a->cols && ldy >= a->rows, "leading dimensions too small");
-        const int grid = blocksFor((long long)a->rows * a->L);
+        const int grid = cappedBlocks((long long)a->rows * a->L);
         cudaStream_t s = asStream(stream);
         for (int c0 = 0; c0 < nrhs; c0 += 2)
         {
@@ -427,9 +458,18 @@ extern "C" int nsf_fastconv_apply(nsf_csr I, const void * K, double nu, const vo
 {
     return guarded([&] {
         require(I && K && u && A, "null argument");
-        const int grid = blocksFor((long long)I->rows * I->L);
+        const int grid = cappedBlocks((long long)I->rows * I->L);
         cudaStream_t s = asStream(stream);
-        if (I->dtype == NSF_F64)
+        if (I->nBlocks > 0)
+        {
+            if (I->dtype == NSF_F64)
+                NSF_LAUNCH((kFastConvStream<double, double, double, double>), I->nBlocks, s, I->rb.get(), I->rs.get(),
+                           I->ci.get(), I->v64.get(), (const double *)u, (const double *)K, nu, (double *)A);
+            else
+                NSF_LAUNCH((kFastConvStream<float, float, float, float>), I->nBlocks, s, I->rb.get(), I->rs.get(),
+                           I->ci.get(), I->v32.get(), (const float *)u, (const float *)K, (float)nu, (float *)A);
+        }
+        else if (I->dtype == NSF_F64)
             NSF_LANES(I->L, NSF_LAUNCH((kFastConv<double, double, double, double, LL>), grid, s, I->rows, I->rs.get(),
                                        I->ci.get(), I->v64.get(), (const double *)u, (const double *)K, nu, (double *)A));
         else
@@ -558,7 +598,7 @@ extern "C" int nsf_solver_solve(nsf_solver s, const double * b, double * x, void
     int st = guarded([&] {
         require(s && b && x, "null argument");
         cudaStream_t cs = asStream(stream);
-        const int n = s->n, grid = blocksFor(n);
+        const int n = s->n, grid = cappedBlocks(n);
         NSF_LAUNCH(kGatherPerm<double>, grid, cs, n, s->numCh, s->perm.get(), b, s->bp.get());
         NSF_LAUNCH(kGatherPerm<double>, grid, cs, n, s->numCh, s->perm.get(), x, s->xp.get());
         const bool rel = true;
@@ -696,54 +736,52 @@ struct nsf_chorin_s
 
     void enqueueStep(cudaStream_t s)
     {
-        const int nnzA = M64.nnzFull;
-        // 1. A = nu K + I u ;  rhs = A [ux uy]
+        // 1. A = nu K + I u (CSR-stream over the FastConvection matrix) ;  rhs = A [ux uy]
         if (mixed)
         {
-            NSF_LANES(I32.L, NSF_LAUNCH((kFastConv<float, double, float, float, LL>), blocksFor((long long)nnzA * I32.L), s,
-                                        nnzA, I32.rs.get(), I32.ci.get(), I32.v.get(), u.get(), K32.get(),
-                                        (float)cfg.nu, A32.get()));
-            NSF_LANES(M32.L, NSF_LAUNCH((kSpmm<float, double, double, float, LL, 2>), blocksFor((long long)N * M32.L), s,
-                                        N, M32.rsF.get(), M32.ciF.get(), A32.get(), u.get(), N, rhs.get(), N));
+            NSF_LAUNCH((kFastConvStream<float, double, float, float>), I32.nBlocks, s, I32.rb.get(), I32.rs.get(),
+                       I32.ci.get(), I32.v.get(), u.get(), K32.get(), (float)cfg.nu, A32.get());
+            NSF_LANES(M32.L, NSF_LAUNCH((kSpmm<float, double, double, float, LL, 2>), M32.fullBlocks(), s, N,
+                                        M32.rsF.get(), M32.ciF.get(), A32.get(), u.get(), N, rhs.get(), N));
         }
         else
         {
-            NSF_LANES(I64.L, NSF_LAUNCH((kFastConv<double, double, double, double, LL>),
-                                        blocksFor((long long)nnzA * I64.L), s, nnzA, I64.rs.get(), I64.ci.get(),
-                                        I64.v.get(), u.get(), K64.get(), cfg.nu, A64.get()));
-            NSF_LANES(M64.L, NSF_LAUNCH((kSpmm<double, double, double, double, LL, 2>),
-                                        blocksFor((long long)N * M64.L), s, N, M64.rsF.get(), M64.ciF.get(),
-                                        A64.get(), u.get(), N, rhs.get(), N));
+            NSF_LAUNCH((kFastConvStream<double, double, double, double>), I64.nBlocks, s, I64.rb.get(), I64.rs.get(),
+                       I64.ci.get(), I64.v.get(), u.get(), K64.get(), cfg.nu, A64.get());
+            NSF_LANES(M64.L, NSF_LAUNCH((kSpmm<double, double, double, double, LL, 2>), M64.fullBlocks(), s, N,
+                                        M64.rsF.get(), M64.ciF.get(), A64.get(), u.get(), N, rhs.get(), N));
         }
         // 2. M acc = rhs ; u = u - tau acc ; Dirichlet
         enqueueMassSolve(s, true);
-        NSF_LAUNCH(kUpdateVelocity<double>, blocksFor(N), s, N, u.get(), acc.get(), cfg.tau, isDir.get(), dirVal.get());
+        NSF_LAUNCH(kUpdateVelocity<double>, cappedBlocks(N), s, N, u.get(), acc.get(), cfg.tau, isDir.get(),
+                   dirVal.get());
         // 3. rhsP = -(1/tau) D u ; Kpi pInt = rhsP (warm start)
         const double invTau = -1.0 / cfg.tau;
         if (mixed)
         {
-            NSF_LANES(D32.L, NSF_LAUNCH((kSpmv<float, double, double, float, LL>), blocksFor((long long)nIntP * D32.L),
+            NSF_LANES(D32.L, NSF_LAUNCH((kSpmv<float, double, double, float, LL>), cappedBlocks((long long)nIntP * D32.L),
                                         s, nIntP, D32.rs.get(), D32.ci.get(), D32.v.get(), u.get(), rhsP.get(),
                                         invTau, 0.0));
             mpres.enqueue(s, body, rhsP.get(), pInt.get(), cfg.maxOuter, cfg.presTol, cfg.presMaxIters, cfg.innerTol,
                           cfg.checkInterval);
-            NSF_LANES(G32.L, NSF_LAUNCH((kSpmv<float, double, double, float, LL>), blocksFor((long long)2 * N * G32.L),
+            NSF_LANES(G32.L, NSF_LAUNCH((kSpmv<float, double, double, float, LL>), cappedBlocks((long long)2 * N * G32.L),
                                         s, 2 * N, G32.rs.get(), G32.ci.get(), G32.v.get(), pInt.get(), rhs.get(), 1.0,
                                         0.0));
         }
         else
         {
             NSF_LANES(D64.L, NSF_LAUNCH((kSpmv<double, double, double, double, LL>),
-                                        blocksFor((long long)nIntP * D64.L), s, nIntP, D64.rs.get(), D64.ci.get(),
+                                        cappedBlocks((long long)nIntP * D64.L), s, nIntP, D64.rs.get(), D64.ci.get(),
                                         D64.v.get(), u.get(), rhsP.get(), invTau, 0.0));
             pres.enqueue(s, body, rhsP.get(), pInt.get(), cfg.presMaxIters, cfg.presTol, false, cfg.checkInterval);
             NSF_LANES(G64.L, NSF_LAUNCH((kSpmv<double, double, double, double, LL>),
-                                        blocksFor((long long)2 * N * G64.L), s, 2 * N, G64.rs.get(), G64.ci.get(),
+                                        cappedBlocks((long long)2 * N * G64.L), s, 2 * N, G64.rs.get(), G64.ci.get(),
                                         G64.v.get(), pInt.get(), rhs.get(), 1.0, 0.0));
         }
         // 4. M acc = G p ; u = u - tau acc ; Dirichlet
         enqueueMassSolve(s, false);
-        NSF_LAUNCH(kUpdateVelocity<double>, blocksFor(N), s, N, u.get(), acc.get(), cfg.tau, isDir.get(), dirVal.get());
+        NSF_LAUNCH(kUpdateVelocity<double>, cappedBlocks(N), s, N, u.get(), acc.get(), cfg.tau, isDir.get(),
+                   dirVal.get());
     }
 
     void collectStats(cudaStream_t s)
@@ -849,7 +887,8 @@ static void buildChorin(nsf_chorin_s & S, const Context & c)
     {
         S.M32.build(Mp, cv.partStart);
         S.Kpi32.build(Kpip, cp.partStart);
-        S.I32.upload(Ip);
+        S.I32.upload(Ip, true);
+        require(S.I32.nBlocks > 0, "FastConvection row longer than the stream block");
         S.D32.upload(Dp);
         S.G32.upload(Gp);
         std::vector<float> k32(knu.begin(), knu.end());
@@ -861,7 +900,8 @@ static void buildChorin(nsf_chorin_s & S, const Context & c)
     }
     else
     {
-        S.I64.upload(Ip);
+        S.I64.upload(Ip, true);
+        require(S.I64.nBlocks > 0, "FastConvection row longer than the stream block");
         S.D64.upload(Dp);
         S.G64.upload(Gp);
         S.K64.upload(knu);

@@ -132,6 +132,28 @@ namespace nsf
         return (int)(b < 1 ? 1 : b);
     }
 
+    // Blocks per kernel are capped at 4 per SM (grid-stride loops cover the rest): enough warps to
+    // hide L2 latency while keeping the per-kernel reductions at O(#SM) block sums.
+    inline int smCount()
+    {
+        static int n = 0;
+        if (n == 0)
+        {
+            int dev = 0;
+            cudaGetDevice(&dev);
+            if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n <= 0)
+                n = 152;
+        }
+        return n;
+    }
+
+    inline int cappedBlocks(long long threads)
+    {
+        const long long cap = 4ll * smCount();
+        const long long b = (threads + 255) / 256;
+        return (int)(b < 1 ? 1 : (b > cap ? cap : b));
+    }
+
     // lanes per row from the average row length (power of two, 2..32)
     inline int lanesFor(long long nnz, long long rows)
     {

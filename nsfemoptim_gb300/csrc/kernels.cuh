@@ -1,13 +1,16 @@
 // sm_103a kernels of the Chorin path.  All sparse work is memory/latency bound (no tensor-core
 // shape), so the kernels are built around:
-//   * row groups of L lanes (L = 2..32) per CSR row: coalesced value/column streams, the
-//     row sum finished with width-L shuffles;
-//   * deterministic reductions: every block writes one FP64 partial per channel to a fixed
-//     slot, consumers sum the slot range in a fixed order (same bits on every run);
-//   * device-resident solver scalars and early-exit flags, so solver loops need no host sync
-//     and can run inside CUDA graphs (conditional while nodes end the loop on the device);
-//   * an iteration counter advanced by the last block of the last kernel of an iteration
-//     ("last block done"), so no kernel ever reads a counter that another block is writing.
+//   * CSR-stream SpMV for the big FastConvection matrix: a block streams a contiguous nnz chunk
+//     (coalesced, several independent loads per thread), multiplies into shared memory and then
+//     reduces its rows - full memory-level parallelism for rows of ~15 entries;
+//   * row groups of L lanes (L = 2..32) per CSR row for the sweeps and the solver SpMVs;
+//   * grids capped at a few blocks per SM (grid-stride loops), and one deterministic reduction per
+//     producing kernel: every block writes its block sum, the last block to finish (atomic ticket)
+//     sums them in a fixed order into a per-kernel scalar - same bits on every run, O(blocks) work;
+//   * device-resident solver scalars and early-exit flags, so solver loops need no host sync and
+//     can run inside CUDA graphs (conditional while nodes end the loop on the device);
+//   * the iteration counter advanced by that same last block of the last kernel of an iteration,
+//     after every block has read it.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -17,6 +20,8 @@ namespace nsf
 {
     constexpr int TPB = 256;      // threads per block of every kernel here
     constexpr int MAXCH = 2;      // planar channels handled by one solver instance
+    constexpr int MAXCOLORS = 64; // colors of a sweep system (smallest-last greedy gives < 10 here)
+    constexpr int STREAM_NNZ = 2048; // nnz per block of the CSR-stream kernel (8 per thread)
     constexpr unsigned FULL = 0xffffffffu;
 
     template <int L>
@@ -51,95 +56,82 @@ namespace nsf
         return __ldg(p);
     }
 
-    // ------------------------------------------------------------------ reductions
+    // ------------------------------------------------------------------ deterministic reductions
 
-    // Sum v over the block; thread 0 writes it to out[ch * stride + slot].
-    template <int NCH>
-    __device__ __forceinline__ void blockPartial(double (&v)[NCH], double * out, int stride, int slot)
+    // Where the totals of a grid reduction go (null entries are dropped).
+    template <int K>
+    struct Outs
     {
-        __shared__ double sm[TPB / 32][NCH];
+        double * p[K];
+    };
+
+    // Grid-wide sum of K per-thread values.  Block sums go to scratch[k * gridDim.x + block]; the
+    // last block to take a ticket sums them in a fixed order, writes out.p[k], resets the ticket
+    // and, if tick != null, advances *tick.  Call at most once per kernel, from every thread.
+    template <int K>
+    __device__ __forceinline__ void gridSum(const double (&v)[K], double * scratch, const Outs<K> & out,
+                                            unsigned * ticket, int * tick)
+    {
+        __shared__ double sm[TPB / 32][K];
+        __shared__ bool lastBlock;
         const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 #pragma unroll
-        for (int c = 0; c < NCH; c++)
+        for (int k = 0; k < K; k++)
         {
-            double s = v[c];
+            double s = v[k];
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1)
                 s += __shfl_xor_sync(FULL, s, o);
             if (lane == 0)
-                sm[warp][c] = s;
+                sm[warp][k] = s;
         }
-        __syncthreads();
-        if (warp == 0)
-        {
-#pragma unroll
-            for (int c = 0; c < NCH; c++)
-            {
-                double s = lane < (TPB / 32) ? sm[lane][c] : 0.0;
-#pragma unroll
-                for (int o = 16; o > 0; o >>= 1)
-                    s += __shfl_xor_sync(FULL, s, o);
-                if (lane == 0 && out)
-                    out[c * stride + slot] = s;
-            }
-        }
-        __syncthreads();
-    }
-
-    // Every thread of the block gets sum(p[ch * stride + 0 .. n)) per channel (fixed order).
-    template <int NCH>
-    __device__ __forceinline__ void sumSlots(const double * p, int stride, int n, double (&out)[NCH])
-    {
-        __shared__ double sm[TPB / 32][NCH];
-        __shared__ double res[NCH];
-        const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-#pragma unroll
-        for (int c = 0; c < NCH; c++)
-        {
-            double s = 0;
-            for (int i = threadIdx.x; i < n; i += blockDim.x)
-                s += p[c * stride + i];
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1)
-                s += __shfl_xor_sync(FULL, s, o);
-            if (lane == 0)
-                sm[warp][c] = s;
-        }
-        __syncthreads();
-        if (warp == 0)
-        {
-#pragma unroll
-            for (int c = 0; c < NCH; c++)
-            {
-                double s = lane < (TPB / 32) ? sm[lane][c] : 0.0;
-#pragma unroll
-                for (int o = 16; o > 0; o >>= 1)
-                    s += __shfl_xor_sync(FULL, s, o);
-                if (lane == 0)
-                    res[c] = s;
-            }
-        }
-        __syncthreads();
-#pragma unroll
-        for (int c = 0; c < NCH; c++)
-            out[c] = res[c];
-        __syncthreads();
-    }
-
-    // Last block to finish advances *counter (all blocks have read it before they finish).
-    __device__ __forceinline__ void lastBlockTick(unsigned * done, int * counter)
-    {
         __syncthreads();
         if (threadIdx.x == 0)
         {
-            __threadfence();
-            const unsigned prev = atomicAdd(done, 1u);
-            if (prev == gridDim.x - 1)
+#pragma unroll
+            for (int k = 0; k < K; k++)
             {
-                *done = 0;
-                *counter += 1;
-                __threadfence();
+                double s = 0;
+                for (int w = 0; w < TPB / 32; w++)
+                    s += sm[w][k];
+                scratch[k * gridDim.x + blockIdx.x] = s;
             }
+            __threadfence();
+            const unsigned prev = atomicAdd(ticket, 1u);
+            lastBlock = (prev == gridDim.x - 1);
+        }
+        __syncthreads();
+        if (!lastBlock)
+            return;
+        __threadfence();
+#pragma unroll
+        for (int k = 0; k < K; k++)
+        {
+            double s = 0;
+            for (int i = threadIdx.x; i < (int)gridDim.x; i += TPB)
+                s += __ldcg(scratch + k * gridDim.x + i);
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1)
+                s += __shfl_xor_sync(FULL, s, o);
+            if (lane == 0)
+                sm[warp][k] = s;
+        }
+        __syncthreads();
+        if (threadIdx.x == 0)
+        {
+#pragma unroll
+            for (int k = 0; k < K; k++)
+            {
+                double s = 0;
+                for (int w = 0; w < TPB / 32; w++)
+                    s += sm[w][k];
+                if (out.p[k])
+                    *out.p[k] = s;
+            }
+            *ticket = 0;
+            if (tick)
+                *tick += 1;
+            __threadfence();
         }
     }
 
@@ -201,7 +193,7 @@ namespace nsf
         }
     }
 
-    // A[k] = nu * K[k] + sum_j I[k, j] u[j]   (linearised advection + diffusion)
+    // A[k] = nu * K[k] + sum_j I[k, j] u[j]   (linearised advection + diffusion), row groups
     template <typename TI, typename TU, typename TK, typename TA, int L>
     __global__ void __launch_bounds__(TPB) kFastConv(int rows, const int * __restrict__ rs, const int * __restrict__ ci,
                                                       const TI * __restrict__ iv, const TU * __restrict__ u,
@@ -218,6 +210,79 @@ namespace nsf
             if (g.lane == 0)
                 a[r] = (TK)(nu * (TA)ldg(k + r) + s);
         }
+    }
+
+    // CSR-stream form of the same operator.  Block b owns rows [rb[b], rb[b+1]) whose entries form
+    // one contiguous chunk of at most STREAM_NNZ nonzeros (rows longer than that are never produced
+    // by the row blocking).  Stage 1 streams values and columns with coalesced loads, 8 independent
+    // loads and gathers per thread, products into shared memory; stage 2 sums each row in order.
+    template <typename TI, typename TU, typename TK, typename TA>
+    __global__ void __launch_bounds__(TPB) kFastConvStream(const int * __restrict__ rb, const int * __restrict__ rs,
+                                                            const int * __restrict__ ci, const TI * __restrict__ iv,
+                                                            const TU * __restrict__ u, const TK * __restrict__ k,
+                                                            TA nu, TK * __restrict__ a)
+    {
+        __shared__ TA prod[STREAM_NNZ];
+        const int r0 = ldg(rb + blockIdx.x), r1 = ldg(rb + blockIdx.x + 1);
+        const int s = ldg(rs + r0), e = ldg(rs + r1);
+        const int cnt = e - s;
+        TI vals[STREAM_NNZ / TPB];
+        int cols[STREAM_NNZ / TPB];
+#pragma unroll
+        for (int q = 0; q < STREAM_NNZ / TPB; q++)
+        {
+            const int j = threadIdx.x + q * TPB;
+            vals[q] = j < cnt ? ldg(iv + s + j) : (TI)0;
+            cols[q] = j < cnt ? ldg(ci + s + j) : 0;
+        }
+#pragma unroll
+        for (int q = 0; q < STREAM_NNZ / TPB; q++)
+        {
+            const int j = threadIdx.x + q * TPB;
+            if (j < cnt)
+                prod[j] = (TA)vals[q] * (TA)ldg(u + cols[q]);
+        }
+        __syncthreads();
+        for (int r = r0 + threadIdx.x; r < r1; r += TPB)
+        {
+            const int b = ldg(rs + r) - s, en = ldg(rs + r + 1) - s;
+            TA acc = 0;
+            for (int j = b; j < en; j++)
+                acc += prod[j];
+            a[r] = (TK)(nu * (TA)ldg(k + r) + acc);
+        }
+    }
+
+    // u <- Dirichlet value on boundary rows, u - tau * acc elsewhere (2 planar channels)
+    template <typename TA>
+    __global__ void __launch_bounds__(TPB) kUpdateVelocity(int n, double * __restrict__ u, const TA * __restrict__ acc,
+                                                            double tau, const unsigned char * __restrict__ isDir,
+                                                            const double * __restrict__ dirVal)
+    {
+        for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        {
+            if (isDir[i])
+            {
+                u[i] = dirVal[i];
+                u[i + n] = 0.0;
+            }
+            else
+            {
+                u[i] -= tau * (double)acc[i];
+                u[i + n] -= tau * (double)acc[i + n];
+            }
+        }
+    }
+
+    // x64 += d (mixed-precision refinement update)
+    template <typename TD>
+    __global__ void __launch_bounds__(TPB) kAddTo(int n, double * __restrict__ x, const TD * __restrict__ d,
+                                                   const int * __restrict__ skip)
+    {
+        if (skip && *skip)
+            return;
+        for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+            x[i] += (double)d[i];
     }
 
     // dst[c * n + i] = src[c * n + perm[i]]   (into the color-permuted numbering)
@@ -246,64 +311,29 @@ namespace nsf
         }
     }
 
-    // u <- Dirichlet value on boundary rows, u - tau * acc elsewhere (2 planar channels)
-    template <typename TA>
-    __global__ void __launch_bounds__(TPB) kUpdateVelocity(int n, double * __restrict__ u, const TA * __restrict__ acc,
-                                                            double tau, const unsigned char * __restrict__ isDir,
-                                                            const double * __restrict__ dirVal)
-    {
-        for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
-        {
-            if (isDir[i])
-            {
-                u[i] = dirVal[i];
-                u[i + n] = 0.0;
-            }
-            else
-            {
-                u[i] -= tau * (double)acc[i];
-                u[i + n] -= tau * (double)acc[i + n];
-            }
-        }
-    }
-
-    template <typename TS, typename TD>
-    __global__ void __launch_bounds__(TPB) kConvert(int n, const TS * __restrict__ s, TD * __restrict__ d)
-    {
-        for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
-            d[i] = (TD)s[i];
-    }
-
-    // x64 += d (mixed-precision refinement update)
-    template <typename TD>
-    __global__ void __launch_bounds__(TPB) kAddTo(int n, double * __restrict__ x, const TD * __restrict__ d,
-                                                   const int * __restrict__ skip)
-    {
-        if (skip && *skip)
-            return;
-        for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
-            x[i] += (double)d[i];
-    }
-
     // ------------------------------------------------------------------ solver state
 
     // Device-resident scalars of one solve (numCh planar channels).
     struct SolverState
     {
-        double rzHist[2][MAXCH]; // r.z of the last two iterations (index = iteration parity)
-        double bb[MAXCH];        // ||b||^2
-        double lastRR[MAXCH];    // ||r||^2 at the last convergence check
-        double tol2;             // relative tolerance squared (or absolute RMS^2 * n for abs mode)
-        int absMode;             // 1: stop on ||r||^2 < tol2 (absolute), 0: ||r||^2 <= tol2 * ||b||^2
+        double rzHist[2][MAXCH];      // r.z of the last two iterations (index = iteration parity)
+        double bb[MAXCH];             // ||b||^2
+        double lastRR[MAXCH];         // ||r||^2 at the last convergence check
+        double rrOut[MAXCOLORS][MAXCH]; // per color phase: ||r||^2 of its rows
+        double rzOut[MAXCOLORS][MAXCH]; // per color phase: r.z of its rows
+        double pqOut[MAXCH];          // p.Ap of the current iteration
+        double bbOut[MAXCH];          // ||b||^2 of the current solve
+        double tol2;                  // relative tolerance squared (or absolute RMS^2 * n)
+        int absMode;                  // 1: stop on ||r||^2 < tol2 (absolute), 0: ||r||^2 <= tol2 ||b||^2
         int active[MAXCH];
         int iters[MAXCH];
-        int status[MAXCH];       // 0 ok / converged, 2 non-finite, 3 max iterations, 4 breakdown
-        int iter;                // iterations started (advanced by the last block of an iteration)
+        int status[MAXCH];            // 0 ok / converged, 2 non-finite, 3 max iterations, 4 breakdown
+        int iter;                     // iterations started (advanced by the last block of an iteration)
         int maxIters;
-        int anyActive;           // 0 once every channel stopped (host polls this)
-        unsigned done;           // last-block counter
-        int skip;                // refinement: 1 once the outer loop has stopped
-        int innerTotal[MAXCH];   // refinement: inner iterations summed over passes
+        int anyActive;                // 0 once every channel stopped (host polls this)
+        unsigned ticket;              // last-block ticket of the grid reductions
+        int skip;                     // refinement: 1 once the outer loop has stopped
+        int innerTotal[MAXCH];        // refinement: inner iterations summed over passes
     };
 
     __global__ void kSetConfig(SolverState * st, int maxIters, int absMode, double tol2)
@@ -321,6 +351,7 @@ namespace nsf
         if (threadIdx.x == 0)
         {
             st->skip = 0;
+            st->ticket = 0;
             for (int c = 0; c < MAXCH; c++)
             {
                 st->status[c] = 0;
@@ -342,25 +373,29 @@ namespace nsf
         return r;
     }
 
+    // sum over the color phases of a per-phase quantity (fixed order)
+    __device__ __forceinline__ double phaseSum(const double (*a)[MAXCH], int nColors, int c)
+    {
+        double s = 0;
+        for (int k = 0; k < nColors; k++)
+            s += a[k][c];
+        return s;
+    }
+
     // ------------------------------------------------------------------ PCG with multicolor SGS
     // Work vectors are planar [ch * n + i] in the color-permuted numbering; color c owns rows
-    // [ps[c], ps[c+1]).  Partial-sum layout: slot ranges per color, same for rr and rz.
+    // [ps[c], ps[c+1]).
 
     struct PcgPtrs
     {
-        int n;
-        int slots;        // number of partial slots (sum of blocks over colors)
-        double * rrPart;  // [MAXCH][slots]  ||r||^2 partials (forward phases)
-        double * rzPart;  // [MAXCH][slots]  r.z partials (last forward phase + backward phases)
-        double * pqPart;  // [MAXCH][pqSlots]
-        int pqSlots;
-        double * bbPart;  // [MAXCH][slots]
+        int n, nColors;
+        double * scratch;        // block sums of the current kernel [2 * MAXCH * maxGrid]
         SolverState * st;
         unsigned long long cond; // graph conditional handle (0: none)
         const int * skip;        // when set and *skip != 0 the solve stops at start (refinement done)
     };
 
-    // r = b - A x (full matrix); bb partials; r and x in T
+    // r = b - A x (full matrix); ||b||^2
     template <typename T, int L, int NCH>
     __global__ void __launch_bounds__(TPB) kPcgInit(PcgPtrs P, const int * __restrict__ rs, const int * __restrict__ ci,
                                                      const T * __restrict__ v, const T * __restrict__ x,
@@ -399,44 +434,46 @@ namespace nsf
                 }
             }
         }
-        blockPartial<NCH>(bb, P.bbPart, P.slots, blockIdx.x);
+        Outs<NCH> o;
+#pragma unroll
+        for (int c = 0; c < NCH; c++)
+            o.p[c] = &P.st->bbOut[c];
+        gridSum<NCH>(bb, P.scratch, o, &P.st->ticket, nullptr);
     }
 
     // Finish the initial state once the SGS of r0 is done: bb, activity, iteration counter.
     template <int NCH>
     __global__ void kPcgStart(PcgPtrs P, int numCh)
     {
-        double bb[NCH], rr[NCH], rz[NCH];
-        sumSlots<NCH>(P.bbPart, P.slots, P.slots, bb);
-        sumSlots<NCH>(P.rrPart, P.slots, P.slots, rr);
-        sumSlots<NCH>(P.rzPart, P.slots, P.slots, rz);
-        if (threadIdx.x == 0)
+        if (threadIdx.x != 0)
+            return;
+        SolverState * st = P.st;
+        const bool skipAll = P.skip && *P.skip;
+        int any = 0;
+        for (int c = 0; c < NCH; c++)
         {
-            SolverState * st = P.st;
-            const bool skipAll = P.skip && *P.skip;
-            int any = 0;
-            for (int c = 0; c < NCH; c++)
-            {
-                st->bb[c] = bb[c];
-                st->lastRR[c] = rr[c];
-                st->rzHist[0][c] = rz[c];
-                st->rzHist[1][c] = rz[c];
-                const bool fin = isfinite(rr[c]) && isfinite(bb[c]);
-                const bool conv = st->absMode ? (rr[c] < st->tol2) : (rr[c] <= st->tol2 * bb[c]);
-                const bool act = c < numCh && fin && !conv && !skipAll;
-                st->active[c] = act;
-                st->iters[c] = 0;
-                st->status[c] = fin ? 0 : 2;
-                any |= act;
-            }
-            st->iter = 1;
-            st->done = 0;
-            st->anyActive = any;
+            const double bb = st->bbOut[c];
+            const double rr = phaseSum(st->rrOut, P.nColors, c);
+            const double rz = phaseSum(st->rzOut, P.nColors, c);
+            st->bb[c] = bb;
+            st->lastRR[c] = rr;
+            st->rzHist[0][c] = rz;
+            st->rzHist[1][c] = rz;
+            const bool fin = isfinite(rr) && isfinite(bb);
+            const bool conv = st->absMode ? (rr < st->tol2) : (rr <= st->tol2 * bb);
+            const bool act = c < numCh && fin && !conv && !skipAll;
+            st->active[c] = act;
+            st->iters[c] = 0;
+            st->status[c] = fin ? 0 : 2;
+            any |= act;
         }
+        st->iter = 1;
+        st->ticket = 0;
+        st->anyActive = any;
     }
 
     // Iteration kernel A: convergence decision from the previous iteration's ||r||^2, beta,
-    // p_new = z + beta p_old, q = A p_new, pq partials.
+    // p_new = z + beta p_old, q = A p_new, p.q.
     template <typename T, int L, int NCH>
     __global__ void __launch_bounds__(TPB) kPcgDirection(PcgPtrs P, int numCh, const int * __restrict__ rs,
                                                           const int * __restrict__ ci, const T * __restrict__ v,
@@ -445,98 +482,103 @@ namespace nsf
     {
         SolverState * st = P.st;
         const int k = st->iter; // stable for the whole iteration
-        double rr[NCH], rz[NCH];
-        sumSlots<NCH>(P.rrPart, P.slots, P.slots, rr);
-        sumSlots<NCH>(P.rzPart, P.slots, P.slots, rz);
         bool act[NCH];
         double beta[NCH];
         bool stopAll = true;
 #pragma unroll
         for (int c = 0; c < NCH; c++)
         {
+            const double rr = phaseSum(st->rrOut, P.nColors, c);
+            const double rz = phaseSum(st->rzOut, P.nColors, c);
             const bool wasActive = c < numCh && st->active[c] && st->status[c] == 0;
-            const bool fin = isfinite(rr[c]) && isfinite(rz[c]);
-            const bool conv = st->absMode ? (rr[c] < st->tol2) : (rr[c] <= st->tol2 * st->bb[c]);
+            const bool fin = isfinite(rr) && isfinite(rz);
+            const bool conv = st->absMode ? (rr < st->tol2) : (rr <= st->tol2 * st->bb[c]);
             act[c] = wasActive && fin && !conv && (k <= st->maxIters);
-            beta[c] = (k == 1) ? 0.0 : rz[c] / st->rzHist[(k - 1) & 1][c];
+            beta[c] = (k == 1) ? 0.0 : rz / st->rzHist[(k - 1) & 1][c];
             stopAll &= !act[c];
+            if (blockIdx.x == 0 && threadIdx.x == 0)
+            {
+                if (c < numCh && st->active[c] && !act[c])
+                {
+                    st->iters[c] = k - 1;
+                    st->lastRR[c] = rr;
+                    if (st->status[c] == 0)
+                        st->status[c] = !fin ? 2 : (conv ? 0 : 3);
+                }
+                st->rzHist[k & 1][c] = rz;
+            }
         }
+        __syncthreads(); // every block has read st->active before block 0 updates it
         if (blockIdx.x == 0 && threadIdx.x == 0)
         {
             int any = 0;
             for (int c = 0; c < NCH; c++)
             {
-                const bool wasActive = c < numCh && st->active[c];
-                if (wasActive && !act[c])
-                {
-                    st->iters[c] = k - 1;
-                    st->lastRR[c] = rr[c];
-                    const bool fin = isfinite(rr[c]) && isfinite(rz[c]);
-                    const bool conv = st->absMode ? (rr[c] < st->tol2) : (rr[c] <= st->tol2 * st->bb[c]);
-                    if (st->status[c] == 0)
-                        st->status[c] = !fin ? 2 : (conv ? 0 : 3);
-                }
                 st->active[c] = act[c];
-                st->rzHist[k & 1][c] = rz[c];
                 any |= act[c];
             }
             st->anyActive = any;
             if (!any && P.cond)
                 cudaGraphSetConditional(P.cond, 0);
         }
-        if (stopAll)
-            return;
-        const int n = P.n;
-        const T * pold = pbuf + (size_t)((k - 1) & 1) * NCH * n;
-        T * pnew = pbuf + (size_t)(k & 1) * NCH * n;
-        Group<L> g;
         double pq[NCH];
 #pragma unroll
         for (int c = 0; c < NCH; c++)
             pq[c] = 0;
-        for (int i = g.gid; i < n; i += g.ngroups)
+        if (!stopAll)
         {
-            const int s = ldg(rs + i), e = ldg(rs + i + 1);
-            double acc[NCH];
-#pragma unroll
-            for (int c = 0; c < NCH; c++)
-                acc[c] = 0;
-            for (int j = s + g.lane; j < e; j += L)
+            const int n = P.n;
+            const T * pold = pbuf + (size_t)((k - 1) & 1) * NCH * n;
+            T * pnew = pbuf + (size_t)(k & 1) * NCH * n;
+            Group<L> g;
+            for (int i = g.gid; i < n; i += g.ngroups)
             {
-                const double a = (double)ldg(v + j);
-                const int col = ldg(ci + j);
+                const int s = ldg(rs + i), e = ldg(rs + i + 1);
+                double acc[NCH];
 #pragma unroll
                 for (int c = 0; c < NCH; c++)
-                    if (act[c])
-                    {
-                        const size_t o = (size_t)c * n + col;
-                        acc[c] += a * (k == 1 ? (double)z[o] : (double)z[o] + beta[c] * (double)pold[o]);
-                    }
-            }
-#pragma unroll
-            for (int c = 0; c < NCH; c++)
-            {
-                const double t = g.sum(acc[c]);
-                if (g.lane == 0 && act[c])
+                    acc[c] = 0;
+                for (int j = s + g.lane; j < e; j += L)
                 {
-                    const size_t o = (size_t)c * n + i;
-                    const T pn = (T)(k == 1 ? (double)z[o] : (double)z[o] + beta[c] * (double)pold[o]);
-                    pnew[o] = pn;
-                    q[o] = (T)t;
-                    pq[c] += (double)pn * t;
+                    const double a = (double)ldg(v + j);
+                    const int col = ldg(ci + j);
+#pragma unroll
+                    for (int c = 0; c < NCH; c++)
+                        if (act[c])
+                        {
+                            const size_t o = (size_t)c * n + col;
+                            acc[c] += a * (k == 1 ? (double)z[o] : (double)z[o] + beta[c] * (double)pold[o]);
+                        }
+                }
+#pragma unroll
+                for (int c = 0; c < NCH; c++)
+                {
+                    const double t = g.sum(acc[c]);
+                    if (g.lane == 0 && act[c])
+                    {
+                        const size_t o = (size_t)c * n + i;
+                        const T pn = (T)(k == 1 ? (double)z[o] : (double)z[o] + beta[c] * (double)pold[o]);
+                        pnew[o] = pn;
+                        q[o] = (T)t;
+                        pq[c] += (double)pn * t;
+                    }
                 }
             }
         }
-        blockPartial<NCH>(pq, P.pqPart, P.pqSlots, blockIdx.x);
+        Outs<NCH> o;
+#pragma unroll
+        for (int c = 0; c < NCH; c++)
+            o.p[c] = &st->pqOut[c];
+        gridSum<NCH>(pq, P.scratch, o, &st->ticket, nullptr);
     }
 
     // Forward SGS phase over color rows [r0, r1) using only neighbours of earlier colors
     // (columns < r0; later colors are still zero in a forward sweep from z = 0).
-    // init == 0: first x += alpha p, r -= alpha q for these rows.  Writes rr partials (and the rz
-    // partials when this is the last color) at slot base + blockIdx.x.
+    // init == 0: first x += alpha p, r -= alpha q for these rows.  Writes ||r||^2 of the color
+    // (and r.z when this is the last color).  tick: last kernel of an iteration (one color only).
     template <typename T, int L, int NCH>
-    __global__ void __launch_bounds__(TPB) kPcgForward(PcgPtrs P, int numCh, int init, int r0, int r1, int last,
-                                                        int slotBase, const int * __restrict__ rs,
+    __global__ void __launch_bounds__(TPB) kPcgForward(PcgPtrs P, int numCh, int init, int color, int r0, int r1,
+                                                        int last, int tick, const int * __restrict__ rs,
                                                         const int * __restrict__ ci, const T * __restrict__ v,
                                                         const T * __restrict__ invD, T * __restrict__ x,
                                                         T * __restrict__ r, T * __restrict__ z,
@@ -547,36 +589,22 @@ namespace nsf
         double alpha[NCH];
         const int k = st->iter;
         const int n = P.n;
-        if (!init)
-        {
-            double pq[NCH];
-            sumSlots<NCH>(P.pqPart, P.pqSlots, P.pqSlots, pq);
-#pragma unroll
-            for (int c = 0; c < NCH; c++)
-            {
-                act[c] = c < numCh && st->active[c];
-                alpha[c] = st->rzHist[k & 1][c] / pq[c];
-            }
-            if (blockIdx.x == 0 && threadIdx.x == 0)
-                for (int c = 0; c < NCH; c++)
-                    if (act[c] && !(pq[c] > 0))
-                        st->status[c] = isfinite(pq[c]) ? 4 : 2; // reported after the solve
-        }
-        else
-        {
-#pragma unroll
-            for (int c = 0; c < NCH; c++)
-            {
-                act[c] = c < numCh;
-                alpha[c] = 0;
-            }
-        }
-        const T * p = pbuf + (size_t)(k & 1) * NCH * n;
-        Group<L> g;
-        double rr[NCH], rz[NCH];
 #pragma unroll
         for (int c = 0; c < NCH; c++)
-            rr[c] = rz[c] = 0;
+        {
+            act[c] = c < numCh && (init || st->active[c]);
+            alpha[c] = init ? 0.0 : st->rzHist[k & 1][c] / st->pqOut[c];
+        }
+        if (!init && blockIdx.x == 0 && threadIdx.x == 0)
+            for (int c = 0; c < NCH; c++)
+                if (act[c] && !(st->pqOut[c] > 0))
+                    st->status[c] = isfinite(st->pqOut[c]) ? 4 : 2; // stops at the next decision
+        const T * p = pbuf + (size_t)(k & 1) * NCH * n;
+        Group<L> g;
+        double red[2 * NCH];
+#pragma unroll
+        for (int c = 0; c < 2 * NCH; c++)
+            red[c] = 0;
         if (anyAct<NCH>(act))
             for (int i = r0 + g.gid; i < r1; i += g.ngroups)
             {
@@ -623,21 +651,26 @@ namespace nsf
                         const size_t o = (size_t)c * n + i;
                         const T zi = (T)((ri[c] - t) * (double)ldg(invD + i));
                         z[o] = zi;
-                        rr[c] += ri[c] * ri[c];
+                        red[c] += ri[c] * ri[c];
                         if (last)
-                            rz[c] += ri[c] * (double)zi;
+                            red[NCH + c] += ri[c] * (double)zi;
                     }
                 }
             }
-        blockPartial<NCH>(rr, P.rrPart, P.slots, slotBase + blockIdx.x);
-        if (last)
-            blockPartial<NCH>(rz, P.rzPart, P.slots, slotBase + blockIdx.x);
+        Outs<2 * NCH> o;
+#pragma unroll
+        for (int c = 0; c < NCH; c++)
+        {
+            o.p[c] = &st->rrOut[color][c];
+            o.p[NCH + c] = last ? &st->rzOut[color][c] : nullptr;
+        }
+        gridSum<2 * NCH>(red, P.scratch, o, &st->ticket, (tick && !init) ? &st->iter : nullptr);
     }
 
-    // Backward SGS phase over color rows [r0, r1) with all off-diagonal neighbours; rz partials.
-    // tick != 0: this is the last kernel of an iteration (advances the iteration counter).
+    // Backward SGS phase over color rows [r0, r1) with all off-diagonal neighbours; r.z of the
+    // color.  tick != 0: this is the last kernel of an iteration (advances the iteration counter).
     template <typename T, int L, int NCH>
-    __global__ void __launch_bounds__(TPB) kPcgBackward(PcgPtrs P, int numCh, int init, int r0, int r1, int slotBase,
+    __global__ void __launch_bounds__(TPB) kPcgBackward(PcgPtrs P, int numCh, int init, int color, int r0, int r1,
                                                          int tick, const int * __restrict__ rs,
                                                          const int * __restrict__ ci, const T * __restrict__ v,
                                                          const T * __restrict__ invD, const T * __restrict__ r,
@@ -685,104 +718,11 @@ namespace nsf
                     }
                 }
             }
-        blockPartial<NCH>(rz, P.rzPart, P.slots, slotBase + blockIdx.x);
-        if (tick && !init)
-            lastBlockTick(&st->done, &st->iter);
-    }
-
-    // single-block tick for systems with one color (no backward phase)
-    __global__ void kTick(SolverState * st)
-    {
-        if (threadIdx.x == 0)
-            st->iter += 1;
-    }
-
-    // ------------------------------------------------------------------ FP64 refinement
-
-    // r = b - A x in FP64; r is handed to the FP32 inner solve; rr and bb partials
-    template <int L, int NCH>
-    __global__ void __launch_bounds__(TPB) kResidual(int n, int slots, const SolverState * st,
-                                                      const int * __restrict__ rs, const int * __restrict__ ci,
-                                                      const double * __restrict__ v, const double * __restrict__ x,
-                                                      const double * __restrict__ b, float * __restrict__ r32,
-                                                      double * __restrict__ rrPart, double * __restrict__ bbPart)
-    {
-        if (st->skip)
-            return;
-        Group<L> g;
-        double rr[NCH], bb[NCH];
+        Outs<NCH> o;
 #pragma unroll
         for (int c = 0; c < NCH; c++)
-            rr[c] = bb[c] = 0;
-        for (int i = g.gid; i < n; i += g.ngroups)
-        {
-            const int s = ldg(rs + i), e = ldg(rs + i + 1);
-            double acc[NCH];
-#pragma unroll
-            for (int c = 0; c < NCH; c++)
-                acc[c] = 0;
-            for (int j = s + g.lane; j < e; j += L)
-            {
-                const double a = ldg(v + j);
-                const int col = ldg(ci + j);
-#pragma unroll
-                for (int c = 0; c < NCH; c++)
-                    acc[c] += a * x[(size_t)c * n + col];
-            }
-#pragma unroll
-            for (int c = 0; c < NCH; c++)
-            {
-                const double t = g.sum(acc[c]);
-                if (g.lane == 0)
-                {
-                    const double bi = b[(size_t)c * n + i];
-                    const double ri = bi - t;
-                    r32[(size_t)c * n + i] = (float)ri;
-                    rr[c] += ri * ri;
-                    bb[c] += bi * bi;
-                }
-            }
-        }
-        blockPartial<NCH>(rr, rrPart, slots, blockIdx.x);
-        blockPartial<NCH>(bb, bbPart, slots, blockIdx.x);
-    }
-
-    // stop decision of refinement pass `pass` (sticky); stats: iters = refinement updates applied
-    template <int NCH>
-    __global__ void kOuterDecide(SolverState * st, const SolverState * inner, int numCh, int slots,
-                                 const double * rrPart, const double * bbPart, int pass)
-    {
-        if (st->skip)
-            return;
-        double rr[NCH], bb[NCH];
-        sumSlots<NCH>(rrPart, slots, slots, rr);
-        sumSlots<NCH>(bbPart, slots, slots, bb);
-        if (threadIdx.x == 0)
-        {
-            bool all = true, bad = false;
-            for (int c = 0; c < NCH && c < numCh; c++)
-            {
-                if (pass > 0)
-                    st->innerTotal[c] += inner->iters[c];
-                const bool fin = isfinite(rr[c]) && isfinite(bb[c]);
-                const bool conv = rr[c] <= st->tol2 * bb[c];
-                bad |= !fin;
-                all &= conv;
-                st->bb[c] = bb[c];
-                st->lastRR[c] = rr[c];
-                st->iters[c] = pass;
-            }
-            if (all || bad || pass >= st->maxIters)
-            {
-                st->skip = 1;
-                st->anyActive = 0;
-                for (int c = 0; c < NCH; c++)
-                {
-                    st->active[c] = 0;
-                    st->status[c] = bad ? 2 : (all ? 0 : 3);
-                }
-            }
-        }
+            o.p[c] = &st->rzOut[color][c];
+        gridSum<NCH>(rz, P.scratch, o, &st->ticket, (tick && !init) ? &st->iter : nullptr);
     }
 
     // ------------------------------------------------------------------ multicolor Gauss-Seidel
@@ -792,15 +732,13 @@ namespace nsf
     struct GsPtrs
     {
         int n;
-        int slots;        // residual partial slots
-        double * rrPart;  // [MAXCH][slots]
-        double * bbPart;  // [MAXCH][slots]
+        double * scratch;
         SolverState * st;
         unsigned long long cond;
         int interval;
     };
 
-    // b norms (for relative mode) and state reset
+    // ||b||^2 (for the relative mode)
     template <typename T, int NCH>
     __global__ void __launch_bounds__(TPB) kGsInit(GsPtrs P, int numCh, const T * __restrict__ b)
     {
@@ -816,33 +754,33 @@ namespace nsf
                 const double t = (double)b[(size_t)c * n + i];
                 bb[c] += t * t;
             }
-        blockPartial<NCH>(bb, P.bbPart, P.slots, blockIdx.x);
+        Outs<NCH> o;
+#pragma unroll
+        for (int c = 0; c < NCH; c++)
+            o.p[c] = &P.st->bbOut[c];
+        gridSum<NCH>(bb, P.scratch, o, &P.st->ticket, nullptr);
     }
 
     template <int NCH>
     __global__ void kGsStart(GsPtrs P, int numCh)
     {
-        double bb[NCH];
-        sumSlots<NCH>(P.bbPart, P.slots, P.slots, bb);
-        if (threadIdx.x == 0)
+        if (threadIdx.x != 0)
+            return;
+        SolverState * st = P.st;
+        int any = 0;
+        for (int c = 0; c < NCH; c++)
         {
-            SolverState * st = P.st;
-            int any = 0;
-            for (int c = 0; c < NCH; c++)
-            {
-                st->bb[c] = bb[c];
-                st->lastRR[c] = -1;
-                st->active[c] = c < numCh;
-                st->iters[c] = 0;
-                st->status[c] = isfinite(bb[c]) ? 0 : 2;
-                if (!isfinite(bb[c]))
-                    st->active[c] = 0;
-                any |= st->active[c];
-            }
-            st->iter = 0;
-            st->done = 0;
-            st->anyActive = any;
+            const double bb = st->bbOut[c];
+            st->bb[c] = bb;
+            st->lastRR[c] = -1;
+            st->active[c] = c < numCh && isfinite(bb);
+            st->iters[c] = 0;
+            st->status[c] = isfinite(bb) ? 0 : 2;
+            any |= st->active[c];
         }
+        st->iter = 0;
+        st->ticket = 0;
+        st->anyActive = any;
     }
 
     // One color phase.  Phase 0 first decides on the residual of the previous check.
@@ -858,27 +796,25 @@ namespace nsf
         if (first)
         {
             const bool checked = k > 0 && ((k - 1) % P.interval) == 0;
-            double rr[NCH];
-            if (checked)
-                sumSlots<NCH>(P.rrPart, P.slots, P.slots, rr);
             bool stopAll = true;
+            bool was[NCH];
 #pragma unroll
             for (int c = 0; c < NCH; c++)
             {
-                const bool was = c < numCh && st->active[c];
-                bool conv = false, fin = true;
-                if (checked)
-                {
-                    fin = isfinite(rr[c]);
-                    conv = st->absMode ? (rr[c] < st->tol2) : (rr[c] <= st->tol2 * st->bb[c]);
-                }
-                act[c] = was && fin;
+                was[c] = c < numCh && st->active[c];
+                const double rr = checked ? st->rrOut[0][c] : 0.0;
+                const bool fin = !checked || isfinite(rr);
+                const bool conv = checked && (st->absMode ? (rr < st->tol2) : (rr <= st->tol2 * st->bb[c]));
+                act[c] = was[c] && fin;
                 // both channels stop together once both meet the target (reference semantics)
-                stopAll &= !(was && fin) || conv;
-                if (checked && blockIdx.x == 0 && threadIdx.x == 0)
-                    st->lastRR[c] = rr[c];
-                if (!fin && blockIdx.x == 0 && threadIdx.x == 0 && was)
-                    st->status[c] = 2;
+                stopAll &= !(was[c] && fin) || conv;
+                if (blockIdx.x == 0 && threadIdx.x == 0 && was[c])
+                {
+                    if (checked)
+                        st->lastRR[c] = rr;
+                    if (!fin)
+                        st->status[c] = 2;
+                }
             }
             const bool over = k >= st->maxIters;
             if (stopAll || over)
@@ -887,13 +823,13 @@ namespace nsf
                 for (int c = 0; c < NCH; c++)
                     act[c] = false;
             }
+            __syncthreads(); // every block has read st->active before block 0 updates it
             if (blockIdx.x == 0 && threadIdx.x == 0)
             {
                 int any = 0;
                 for (int c = 0; c < NCH; c++)
                 {
-                    const bool was = c < numCh && st->active[c];
-                    if (was && !act[c])
+                    if (was[c] && !act[c])
                     {
                         // index of the last iteration run, or the cap (reference's lastIterations)
                         st->iters[c] = (over && !stopAll) ? k : k - 1;
@@ -959,7 +895,9 @@ namespace nsf
 #pragma unroll
         for (int c = 0; c < NCH; c++)
             act[c] = c < numCh && st->active[c];
-        const bool doCheck = anyAct<NCH>(act) && (k % P.interval) == 0;
+        if (!anyAct<NCH>(act))
+            return; // the loop is ending; no tick needed
+        const bool doCheck = (k % P.interval) == 0;
         double rr[NCH];
 #pragma unroll
         for (int c = 0; c < NCH; c++)
@@ -994,9 +932,116 @@ namespace nsf
                     }
                 }
             }
-            blockPartial<NCH>(rr, P.rrPart, P.slots, blockIdx.x);
         }
-        if (anyAct<NCH>(act))
-            lastBlockTick(&st->done, &st->iter);
+        Outs<NCH> o;
+#pragma unroll
+        for (int c = 0; c < NCH; c++)
+            o.p[c] = doCheck ? &st->rrOut[0][c] : nullptr;
+        gridSum<NCH>(rr, P.scratch, o, &st->ticket, &st->iter);
+    }
+
+    // ------------------------------------------------------------------ FP64 refinement
+
+    // r = b - A x in FP64; r is handed to the FP32 inner solve; ||r||^2 and ||b||^2
+    template <int L, int NCH>
+    __global__ void __launch_bounds__(TPB) kResidual(int n, SolverState * st, double * scratch,
+                                                      const int * __restrict__ rs, const int * __restrict__ ci,
+                                                      const double * __restrict__ v, const double * __restrict__ x,
+                                                      const double * __restrict__ b, float * __restrict__ r32)
+    {
+        if (st->skip)
+            return;
+        Group<L> g;
+        double red[2 * NCH];
+#pragma unroll
+        for (int c = 0; c < 2 * NCH; c++)
+            red[c] = 0;
+        for (int i = g.gid; i < n; i += g.ngroups)
+        {
+            const int s = ldg(rs + i), e = ldg(rs + i + 1);
+            double acc[NCH];
+#pragma unroll
+            for (int c = 0; c < NCH; c++)
+                acc[c] = 0;
+            for (int j = s + g.lane; j < e; j += L)
+            {
+                const double a = ldg(v + j);
+                const int col = ldg(ci + j);
+#pragma unroll
+                for (int c = 0; c < NCH; c++)
+                    acc[c] += a * x[(size_t)c * n + col];
+            }
+#pragma unroll
+            for (int c = 0; c < NCH; c++)
+            {
+                const double t = g.sum(acc[c]);
+                if (g.lane == 0)
+                {
+                    const double bi = b[(size_t)c * n + i];
+                    const double ri = bi - t;
+                    r32[(size_t)c * n + i] = (float)ri;
+                    red[c] += ri * ri;
+                    red[NCH + c] += bi * bi;
+                }
+            }
+        }
+        Outs<2 * NCH> o;
+#pragma unroll
+        for (int c = 0; c < NCH; c++)
+        {
+            o.p[c] = &st->rrOut[0][c];
+            o.p[NCH + c] = &st->bbOut[c];
+        }
+        gridSum<2 * NCH>(red, scratch, o, &st->ticket, nullptr);
+    }
+
+    // Stop decision of refinement pass `pass` (sticky); stats: iters = refinement updates applied.
+    // The next inner solve only has to reach half the remaining distance to the target:
+    // inner relative tolerance = max(innerMin, 0.5 * tol * ||b|| / ||r||), written into the inner
+    // solver's state (its configuration is not reset by the host between passes).
+    template <int NCH>
+    __global__ void kOuterDecide(SolverState * st, SolverState * inner, int numCh, int pass, double innerMin,
+                                 int innerMaxIters)
+    {
+        if (threadIdx.x != 0 || st->skip)
+            return;
+        bool all = true, bad = false;
+        double rr[NCH], bb[NCH];
+        for (int c = 0; c < NCH && c < numCh; c++)
+        {
+            rr[c] = st->rrOut[0][c];
+            bb[c] = st->bbOut[c];
+            if (pass > 0)
+                st->innerTotal[c] += inner->iters[c];
+            const bool fin = isfinite(rr[c]) && isfinite(bb[c]);
+            const bool conv = rr[c] <= st->tol2 * bb[c];
+            bad |= !fin;
+            all &= conv;
+            st->bb[c] = bb[c];
+            st->lastRR[c] = rr[c];
+            st->iters[c] = pass;
+        }
+        if (all || bad || pass >= st->maxIters)
+        {
+            st->skip = 1;
+            st->anyActive = 0;
+            for (int c = 0; c < NCH; c++)
+            {
+                st->active[c] = 0;
+                st->status[c] = bad ? 2 : (all ? 0 : 3);
+            }
+        }
+        else
+        {
+            // loosest inner tolerance over the channels still above the target
+            double need = 1.0;
+            for (int c = 0; c < NCH && c < numCh; c++)
+                if (rr[c] > st->tol2 * bb[c] && rr[c] > 0)
+                    need = fmin(need, 0.5 * sqrt(st->tol2 * bb[c] / rr[c]));
+            const double t = fmax(innerMin, need);
+            inner->tol2 = t * t;
+            inner->absMode = 0;
+            inner->maxIters = innerMaxIters;
+        }
     }
 } // namespace nsf

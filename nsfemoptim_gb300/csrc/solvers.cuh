@@ -75,6 +75,8 @@ namespace nsf
             n = a.rows;
             ps = partStart;
             nColors = (int)ps.size() - 1;
+            if (nColors > MAXCOLORS)
+                throw Error(ST_NOTSUP, "more than " + std::to_string(MAXCOLORS) + " colors");
             nnzFull = a.nnz();
             std::vector<int> ro(n + 1, 0), co;
             std::vector<T> vo, vf(a.val.begin(), a.val.end()), id(n);
@@ -112,7 +114,9 @@ namespace nsf
             L = lanesFor(a.nnz(), n);
         }
 
-        int phaseBlocks(int c) const { return blocksFor((long long)(ps[c + 1] - ps[c]) * L); }
+        // capped grid of the phase kernel of color c and of whole-system kernels
+        int phaseBlocks(int c) const { return cappedBlocks((long long)(ps[c + 1] - ps[c]) * L); }
+        int fullBlocks() const { return cappedBlocks((long long)n * L); }
     };
 
     // ------------------------------------------------------------------ PCG with multicolor SGS
@@ -122,9 +126,8 @@ namespace nsf
         const SweepSystem<T> * sys = nullptr;
         int numCh = 1;
         DevBuf<T> r, z, p, q;
-        DevBuf<double> rrPart, rzPart, pqPart, bbPart;
+        DevBuf<double> scratch;
         DevBuf<SolverState> st;
-        std::vector<int> slotBase;
         PcgPtrs P{};
         PinnedBuf<int> flag{1};
 
@@ -137,23 +140,11 @@ namespace nsf
             z.alloc((size_t)NCH * n);
             p.alloc((size_t)2 * NCH * n);
             q.alloc((size_t)NCH * n);
-            slotBase.assign(s->nColors + 1, 0);
-            for (int c = 0; c < s->nColors; c++)
-                slotBase[c + 1] = slotBase[c] + s->phaseBlocks(c);
-            const int slots = slotBase.back();
-            const int pqSlots = blocksFor((long long)n * s->L);
-            rrPart.alloc((size_t)MAXCH * slots);
-            rzPart.alloc((size_t)MAXCH * slots);
-            bbPart.alloc((size_t)MAXCH * slots);
-            pqPart.alloc((size_t)MAXCH * pqSlots);
+            scratch.alloc((size_t)2 * MAXCH * cappedBlocks(1ll << 40));
             st.alloc(1);
             P.n = n;
-            P.slots = slots;
-            P.rrPart = rrPart.get();
-            P.rzPart = rzPart.get();
-            P.pqPart = pqPart.get();
-            P.pqSlots = pqSlots;
-            P.bbPart = bbPart.get();
+            P.nColors = s->nColors;
+            P.scratch = scratch.get();
             P.st = st.get();
             P.cond = 0;
         }
@@ -165,32 +156,28 @@ namespace nsf
             T * pbuf = p.get();
             NSF_LANES(S.L, {
                 for (int c = 0; c < C; c++)
-                    NSF_LAUNCH((kPcgForward<T, LL, NCH>), S.phaseBlocks(c), s, PP, numCh, init, S.ps[c], S.ps[c + 1],
-                               c == C - 1 ? 1 : 0, slotBase[c], S.rsO.get(), S.ciO.get(), S.vO.get(), S.invD.get(), x,
-                               r.get(), z.get(), pbuf, q.get());
+                    NSF_LAUNCH((kPcgForward<T, LL, NCH>), S.phaseBlocks(c), s, PP, numCh, init, c, S.ps[c],
+                               S.ps[c + 1], c == C - 1 ? 1 : 0, (tickLast && C == 1) ? 1 : 0, S.rsO.get(),
+                               S.ciO.get(), S.vO.get(), S.invD.get(), x, r.get(), z.get(), pbuf, q.get());
                 for (int c = C - 2; c >= 0; c--)
-                    NSF_LAUNCH((kPcgBackward<T, LL, NCH>), S.phaseBlocks(c), s, PP, numCh, init, S.ps[c],
-                               S.ps[c + 1], slotBase[c], (tickLast && c == 0) ? 1 : 0, S.rsO.get(), S.ciO.get(),
-                               S.vO.get(), S.invD.get(), r.get(), z.get());
+                    NSF_LAUNCH((kPcgBackward<T, LL, NCH>), S.phaseBlocks(c), s, PP, numCh, init, c, S.ps[c],
+                               S.ps[c + 1], (tickLast && c == 0) ? 1 : 0, S.rsO.get(), S.ciO.get(), S.vO.get(),
+                               S.invD.get(), r.get(), z.get());
             });
-            if (!init && C < 2)
-                NSF_LAUNCH(kTick, 1, s, PP.st);
         }
 
-        // Solve A x = b (device, planar numCh * n, x = initial guess).  Configuration is passed
-        // through `cfg` (tolerance, iteration cap) and written to the device state by kernel args.
+        // Solve A x = b (device, planar numCh * n, x = initial guess).
+        // setConfig == false: tolerance and cap are already in the device state (written by a
+        // preceding kernel, as the refinement loop does).
         void enqueue(cudaStream_t s, cudaStream_t bodyStream, const T * b, T * x, int maxIters, double tol,
-                     bool absolute, int checkInterval)
+                     bool absolute, int checkInterval, bool setConfig = true)
         {
             const SweepSystem<T> & S = *sys;
-            SolverState init{};
-            init.maxIters = maxIters;
-            init.absMode = absolute ? 1 : 0;
-            init.tol2 = absolute ? tol * tol * (double)S.n : tol * tol;
-            // the config lives in kernel arguments: kSetConfig copies it before the init kernels
-            NSF_LAUNCH(kSetConfig, 1, s, st.get(), init.maxIters, init.absMode, init.tol2);
-            NSF_LANES(S.L, NSF_LAUNCH((kPcgInit<T, LL, NCH>), P.slots, s, P, S.rsF.get(), S.ciF.get(), S.vF.get(),
-                                      x, b, r.get()));
+            if (setConfig)
+                NSF_LAUNCH(kSetConfig, 1, s, st.get(), maxIters, absolute ? 1 : 0,
+                           absolute ? tol * tol * (double)S.n : tol * tol);
+            NSF_LANES(S.L, NSF_LAUNCH((kPcgInit<T, LL, NCH>), S.fullBlocks(), s, P, S.rsF.get(), S.ciF.get(),
+                                      S.vF.get(), x, b, r.get()));
             sgs(s, P, 1, x, false);
             NSF_LAUNCH((kPcgStart<NCH>), 1, s, P, numCh);
             deviceLoop(s, bodyStream, st.get(), maxIters, checkInterval, flag,
@@ -198,14 +185,14 @@ namespace nsf
                        {
                            PcgPtrs PP = P;
                            PP.cond = cond;
-                           NSF_LANES(S.L, NSF_LAUNCH((kPcgDirection<T, LL, NCH>), PP.pqSlots, bs, PP, numCh,
+                           NSF_LANES(S.L, NSF_LAUNCH((kPcgDirection<T, LL, NCH>), S.fullBlocks(), bs, PP, numCh,
                                                      S.rsF.get(), S.ciF.get(), S.vF.get(), z.get(), p.get(),
                                                      q.get()));
                            sgs(bs, PP, 0, x, true);
                        });
         }
 
-        int kernelsPerIteration() const { return 1 + 2 * sys->nColors - 1 + (sys->nColors < 2 ? 1 : 0); }
+        int kernelsPerIteration() const { return 2 * sys->nColors; }
         int initKernels() const { return 3 + 2 * sys->nColors - 1; }
     };
 
@@ -215,7 +202,7 @@ namespace nsf
     {
         const SweepSystem<T> * sys = nullptr;
         int numCh = 1, interval = 1;
-        DevBuf<double> rrPart, bbPart;
+        DevBuf<double> scratch;
         DevBuf<SolverState> st;
         GsPtrs P{};
         PinnedBuf<int> flag{1};
@@ -225,14 +212,10 @@ namespace nsf
             sys = s;
             numCh = channels;
             interval = checkInterval < 1 ? 1 : checkInterval;
-            const int slots = blocksFor((long long)s->n * s->L);
-            rrPart.alloc((size_t)MAXCH * slots);
-            bbPart.alloc((size_t)MAXCH * slots);
+            scratch.alloc((size_t)2 * MAXCH * cappedBlocks(1ll << 40));
             st.alloc(1);
             P.n = s->n;
-            P.slots = slots;
-            P.rrPart = rrPart.get();
-            P.bbPart = bbPart.get();
+            P.scratch = scratch.get();
             P.st = st.get();
             P.cond = 0;
             P.interval = interval;
@@ -244,7 +227,7 @@ namespace nsf
             const SweepSystem<T> & S = *sys;
             const double tol2 = absolute ? tol * tol * (double)S.n : tol * tol;
             NSF_LAUNCH(kSetConfig, 1, s, st.get(), maxIters, absolute ? 1 : 0, tol2);
-            NSF_LAUNCH((kGsInit<T, NCH>), P.slots, s, P, numCh, b);
+            NSF_LAUNCH((kGsInit<T, NCH>), cappedBlocks(S.n), s, P, numCh, b);
             NSF_LAUNCH((kGsStart<NCH>), 1, s, P, numCh);
             deviceLoop(s, bodyStream, st.get(), maxIters, hostCheck, flag,
                        [&](cudaStream_t bs, unsigned long long cond)
@@ -256,8 +239,8 @@ namespace nsf
                                    NSF_LAUNCH((kGsPhase<T, LL, NCH>), S.phaseBlocks(c), bs, PP, numCh, S.ps[c],
                                               S.ps[c + 1], c == 0 ? 1 : 0, S.rsO.get(), S.ciO.get(), S.vO.get(),
                                               S.invD.get(), b, x);
-                               NSF_LAUNCH((kGsCheck<T, LL, NCH>), PP.slots, bs, PP, numCh, S.rsF.get(), S.ciF.get(),
-                                          S.vF.get(), b, x);
+                               NSF_LAUNCH((kGsCheck<T, LL, NCH>), S.fullBlocks(), bs, PP, numCh, S.rsF.get(),
+                                          S.ciF.get(), S.vF.get(), b, x);
                            });
                        });
         }
@@ -274,9 +257,8 @@ namespace nsf
         PcgSolver<float, NCH> inner;
         int numCh = 1;
         DevBuf<float> b32, d32;
-        DevBuf<double> rrPart, bbPart;
+        DevBuf<double> scratch;
         DevBuf<SolverState> st;
-        int slots = 0;
         PinnedBuf<int> flag{1};
 
         void setup(const SweepSystem<double> * s64, const SweepSystem<float> * s32, int channels)
@@ -286,9 +268,7 @@ namespace nsf
             inner.setup(s32, channels);
             b32.alloc((size_t)NCH * s64->n);
             d32.alloc((size_t)NCH * s64->n);
-            slots = blocksFor((long long)s64->n * s64->L);
-            rrPart.alloc((size_t)MAXCH * slots);
-            bbPart.alloc((size_t)MAXCH * slots);
+            scratch.alloc((size_t)2 * MAXCH * cappedBlocks(1ll << 40));
             st.alloc(1);
         }
 
@@ -307,15 +287,15 @@ namespace nsf
             inner.P.skip = &sd->skip;
             for (int pass = 0; pass <= maxOuter; pass++)
             {
-                NSF_LANES(S.L, NSF_LAUNCH((kResidual<LL, NCH>), slots, s, n, slots, sd, S.rsF.get(), S.ciF.get(),
-                                          S.vF.get(), x, b, b32.get(), rrPart.get(), bbPart.get()));
-                NSF_LAUNCH((kOuterDecide<NCH>), 1, s, sd, inner.st.get(), numCh, slots, rrPart.get(), bbPart.get(),
-                           pass);
+                NSF_LANES(S.L, NSF_LAUNCH((kResidual<LL, NCH>), S.fullBlocks(), s, n, sd, scratch.get(), S.rsF.get(),
+                                          S.ciF.get(), S.vF.get(), x, b, b32.get()));
+                NSF_LAUNCH((kOuterDecide<NCH>), 1, s, sd, inner.st.get(), numCh, pass, innerTol, innerMaxIters);
                 if (pass == maxOuter)
                     break;
                 NSF_CUDA(cudaMemsetAsync(d32.get(), 0, sizeof(float) * NCH * n, s));
-                inner.enqueue(s, bodyStream, b32.get(), d32.get(), innerMaxIters, innerTol, false, checkInterval);
-                NSF_LAUNCH((kAddTo<float>), blocksFor((long long)NCH * n), s, NCH * n, x, d32.get(), &sd->skip);
+                inner.enqueue(s, bodyStream, b32.get(), d32.get(), innerMaxIters, innerTol, false, checkInterval,
+                              false);
+                NSF_LAUNCH((kAddTo<float>), cappedBlocks((long long)NCH * n), s, NCH * n, x, d32.get(), &sd->skip);
             }
         }
     };
