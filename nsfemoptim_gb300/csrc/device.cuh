@@ -6,6 +6,7 @@
 #include "kernels.cuh"
 
 #include <atomic>
+#include <cstdlib>
 #include <stdexcept>
 #include <string>
 #include <utility>
@@ -184,6 +185,31 @@ namespace nsf
     }
 
 #define NSF_LAUNCH(kernel, grid, stream, ...) ::nsf::launchKernel(#kernel, kernel, (grid), (stream), __VA_ARGS__)
+
+    // launch a one-cluster kernel: cs CTAs of 1024 threads forming one thread-block cluster
+    template <typename Arg>
+    inline void launchCluster(void (*k)(Arg), int cs, cudaStream_t s, const Arg & a)
+    {
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3(cs);
+        cfg.blockDim = dim3(1024);
+        cfg.stream = s;
+        cudaLaunchAttribute at[1];
+        at[0].id = cudaLaunchAttributeClusterDimension;
+        at[0].val.clusterDim.x = cs;
+        at[0].val.clusterDim.y = 1;
+        at[0].val.clusterDim.z = 1;
+        cfg.attrs = at;
+        cfg.numAttrs = 1;
+        cudaCheck(cudaLaunchKernelEx(&cfg, k, a), "cluster launch");
+        launchCounter().fetch_add(1, std::memory_order_relaxed);
+    }
+
+    inline int envFlag(const char * name)
+    {
+        const char * v = std::getenv(name);
+        return (v && *v && *v != '0') ? 1 : 0;
+    }
 
 // dispatch a lanes-per-row value to a template parameter
 #define NSF_LANES(L, ...)                                                                                       \

@@ -9,6 +9,7 @@
 // runs with no host synchronisation at all.
 #pragma once
 
+#include "cluster.cuh"
 #include "device.cuh"
 #include "host/setup.hpp"
 #include "kernels.cuh"
@@ -130,12 +131,30 @@ namespace nsf
         DevBuf<SolverState> st;
         PcgPtrs P{};
         PinnedBuf<int> flag{1};
+        // cluster-resident variant (one launch per solve); 0 = multi-kernel path
+        int clusterSize = 0, clusterL = 2;
+        DevBuf<int> psDev;
 
-        void setup(const SweepSystem<T> * s, int channels)
+        // lanes per row in the cluster kernel: few lanes, many rows in flight per CTA
+        static int clusterLanes(const SweepSystem<T> * s)
+        {
+            const double avg = s->n > 0 ? (double)s->nnzFull / s->n : 1.0;
+            return avg <= 8 ? 2 : 4;
+        }
+
+        void setup(const SweepSystem<T> * s, int channels, bool tryCluster = true)
         {
             sys = s;
             numCh = channels;
             const int n = s->n;
+            psDev.upload(s->ps);
+            clusterSize = 0;
+            if (tryCluster && envFlag("NSF_NO_CLUSTER") == 0)
+            {
+                clusterL = clusterLanes(s);
+                clusterSize = clusterL == 2 ? pickClusterSize(kPcgCluster<T, 2, NCH>)
+                                            : pickClusterSize(kPcgCluster<T, 4, NCH>);
+            }
             r.alloc((size_t)NCH * n);
             z.alloc((size_t)NCH * n);
             p.alloc((size_t)2 * NCH * n);
@@ -176,6 +195,17 @@ namespace nsf
             if (setConfig)
                 NSF_LAUNCH(kSetConfig, 1, s, st.get(), maxIters, absolute ? 1 : 0,
                            absolute ? tol * tol * (double)S.n : tol * tol);
+            if (clusterSize > 0)
+            {
+                ClusterPcgArgs<T> A{S.n, S.nColors, numCh, psDev.get(), S.rsF.get(), S.ciF.get(), S.vF.get(),
+                                    S.rsO.get(), S.ciO.get(), S.vO.get(), S.invD.get(), b, x, r.get(), z.get(),
+                                    p.get(), q.get(), st.get(), P.skip};
+                if (clusterL == 2)
+                    launchCluster(kPcgCluster<T, 2, NCH>, clusterSize, s, A);
+                else
+                    launchCluster(kPcgCluster<T, 4, NCH>, clusterSize, s, A);
+                return;
+            }
             NSF_LANES(S.L, NSF_LAUNCH((kPcgInit<T, LL, NCH>), S.fullBlocks(), s, P, S.rsF.get(), S.ciF.get(),
                                       S.vF.get(), x, b, r.get()));
             sgs(s, P, 1, x, false);

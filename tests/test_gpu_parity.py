@@ -117,6 +117,33 @@ def test_pcg_pressure_matches_oracle(setup, torch_cuda):
     assert np.linalg.norm(r) <= 1.01e-10 * np.linalg.norm(b)
 
 
+@pytest.mark.parametrize("path", ["cluster", "multikernel"])
+def test_pcg_paths_match_oracle(setup, torch_cuda, path, monkeypatch):
+    """The cluster-resident solver and the multi-kernel solver run the same algorithm."""
+    G, O, mesh, ctx, om, oc = setup
+    t = torch_cuda
+    if path == "multikernel":
+        monkeypatch.setenv("NSF_NO_CLUSTER", "1")
+    else:
+        monkeypatch.delenv("NSF_NO_CLUSTER", raising=False)
+    for name, nch in (("Kpi", 1), ("M", 2)):
+        a = ctx.matrix(name)
+        rng = np.random.default_rng(11)
+        b = rng.standard_normal(nch * a.rows)
+        s = G.create_solver("pcg", nch, a, 3000, 1e-10, 1)
+        s.getRhs().copy_(t.tensor(b))
+        s.getSol().zero_()
+        assert s.solve() == 0, path
+        x = s.getSol().cpu().numpy()
+        col = O.coloring(getattr(oc, name))
+        n = a.rows
+        for c in range(nch):
+            xo, st, it, rr = O.pcg(getattr(oc, name), col, b[c * n:(c + 1) * n], np.zeros(n), 3000, 1e-10)
+            assert st == 0
+            assert _rel(x[c * n:(c + 1) * n], xo) <= 1e-8, (path, name, c)
+        assert abs(s.getLastIterations() - it) <= 1
+
+
 def test_pcg_mass_two_channels_warm_start(setup, torch_cuda):
     G, O, mesh, ctx, om, oc = setup
     t = torch_cuda
