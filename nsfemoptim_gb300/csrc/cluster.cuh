@@ -3,18 +3,30 @@
 // One launch per solve: a single thread-block cluster of CS CTAs (16 where the GPU allows
 // non-portable clusters, else 8) x 1024 threads runs the whole iteration loop.  CTA k owns chunk k
 // of every color block, so x, r and q are only touched by their owner; z and p are read at
-// neighbour rows of other CTAs through L2 (ld.global.cg).  Every color phase ends in a hardware
-// cluster barrier (barrier.cluster arrive.release / wait.acquire) instead of a kernel boundary,
-// and the dot products are cluster reductions: each CTA writes its block sum into its own shared
-// memory, and after the barrier every CTA reads the CS sums through distributed shared memory in
-// rank order, so all CTAs hold bit-identical scalars and take identical loop decisions (the
-// barrier count can never diverge).  The loop is bounded by maxIters.
+// neighbour rows of other CTAs through L2 (ld.global.cg).
 //
-// The state (tolerance, cap, mode) is read from the SolverState written by a preceding kernel,
-// so the FP64 refinement loop can set the inner tolerance on the device.
+// Measured on the GB300: a cluster barrier costs 0.3 us and a dependent L2 load ~150 ns, while a
+// kernel boundary with a grid reduction costs >= 3 us.  The kernel is therefore organised for one
+// L2 round trip per color phase:
+//   * one thread per row; the entries of a row are processed in fixed-width predicated batches so
+//     all value loads and neighbour gathers of a row are in flight together;
+//   * when the structure of a CTA's rows (row offsets, column indices of the off-diagonal part)
+//     fits in shared memory it is copied there at kernel start (SMEM = true), else it is read from
+//     global memory (the large mass matrix);
+//   * phases end in a hardware cluster barrier; dot products are cluster reductions: each CTA writes
+//     its block sum into its own shared memory, after the barrier one warp reads the CS sums
+//     through distributed shared memory in parallel (lane r <- rank r) and adds them with a fixed
+//     shuffle tree, so all CTAs hold bit-identical scalars and take identical loop decisions (the
+//     barrier count can never diverge).  The loop is bounded by the iteration cap.
+//
+// Tolerance, cap and mode are read from the SolverState written by a preceding kernel, so the FP64
+// refinement loop can set the inner tolerance on the device.
 #pragma once
 
 #include <cooperative_groups.h>
+
+#include <climits>
+#include <vector>
 
 #include "kernels.cuh"
 
@@ -22,18 +34,19 @@ namespace nsf
 {
     namespace cg = cooperative_groups;
 
-    constexpr int CTPB = 1024; // threads per CTA of the cluster solver
+    constexpr int CTPB = 1024;                    // threads per CTA of the cluster solver
+    constexpr size_t kClusterSmemCap = 200 * 1024; // dynamic shared memory ceiling per CTA
+    constexpr int RB = 8;                          // entries per predicated batch of a row
 
     template <typename T>
     struct ClusterPcgArgs
     {
         int n, nColors, numCh;
         const int * ps;                  // color starts (device), nColors + 1
-        const int *rsF, *ciF;            // full matrix
-        const T * vF;
         const int *rsO, *ciO;            // off-diagonal part
         const T * vO;
-        const T * invD;
+        const T * diag;                  // diagonal values
+        const T * invD;                  // their inverses
         const T * b;
         T *x, *r, *z, *p, *q;            // p holds two planes (ping-pong) of NCH * n
         SolverState * st;
@@ -59,21 +72,38 @@ namespace nsf
                 warpPart[warp][k] = s;
         }
         __syncthreads();
-        if (threadIdx.x < K)
+        if (warp == 0)
         {
-            double s = 0;
-            for (int w = 0; w < CTPB / 32; w++)
-                s += warpPart[w][threadIdx.x];
-            slot[buf][threadIdx.x] = s;
+#pragma unroll
+            for (int k = 0; k < K; k++)
+            {
+                double s = warpPart[lane][k];
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1)
+                    s += __shfl_xor_sync(FULL, s, o);
+                if (lane == 0)
+                    slot[buf][k] = s;
+            }
         }
         cl.sync();
-        if (threadIdx.x < K)
+        if (warp == 0)
         {
-            double s = 0;
             const int cs = (int)cl.num_blocks();
-            for (int rk = 0; rk < cs; rk++)
-                s += cl.map_shared_rank(&slot[buf][0], rk)[threadIdx.x];
-            total[threadIdx.x] = s;
+            double rv[K];
+            const double * remote = cl.map_shared_rank(&slot[buf][0], lane < cs ? lane : 0);
+#pragma unroll
+            for (int k = 0; k < K; k++)
+                rv[k] = lane < cs ? remote[k] : 0.0;
+#pragma unroll
+            for (int k = 0; k < K; k++)
+            {
+                double s = rv[k];
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1)
+                    s += __shfl_xor_sync(FULL, s, o);
+                if (lane == 0)
+                    total[k] = s;
+            }
         }
         __syncthreads();
 #pragma unroll
@@ -88,19 +118,102 @@ namespace nsf
         return a + (int)(((long long)len * rank) / cs);
     }
 
-    template <typename T, int L, int NCH>
+    // Shared-memory footprint (bytes) of CTA `rank`: local row offsets (own rows + 1) and the
+    // column indices of their off-diagonal entries.  Host and device compute it the same way.
+    inline size_t clusterSmemBytes(const std::vector<int> & ps, const std::vector<int> & rsO, int rank, int cs)
+    {
+        size_t rows = 0, nnz = 0;
+        for (size_t c = 0; c + 1 < ps.size(); c++)
+        {
+            const int len = ps[c + 1] - ps[c];
+            const int a0 = ps[c] + (int)(((long long)len * rank) / cs);
+            const int a1 = ps[c] + (int)(((long long)len * (rank + 1)) / cs);
+            rows += a1 - a0;
+            nnz += rsO[a1] - rsO[a0];
+        }
+        return 4 * (rows + 1 + nnz);
+    }
+
+    // Row structure of the CTA's own rows: shared-memory copy (SMEM) or the global CSR itself.
+    template <bool SMEM>
+    struct RowView;
+
+    template <>
+    struct RowView<true>
+    {
+        const int *lrs, *lci;
+        const int *chunkA, *chunkL, *chunkG, *nzBase;
+        __device__ __forceinline__ int begin(int, int l) const { return lrs[l]; }
+        __device__ __forceinline__ int end(int, int l) const { return lrs[l + 1]; }
+        __device__ __forceinline__ int col(int j) const { return lci[j]; }
+        __device__ __forceinline__ int gnz(int c, int j) const { return chunkG[c] + (j - nzBase[c]); }
+    };
+
+    template <>
+    struct RowView<false>
+    {
+        const int *rsO, *ciO;
+        const int *chunkA, *chunkL;
+        __device__ __forceinline__ int begin(int c, int l) const { return ldg(rsO + chunkA[c] + (l - chunkL[c])); }
+        __device__ __forceinline__ int end(int c, int l) const { return ldg(rsO + chunkA[c] + (l - chunkL[c]) + 1); }
+        __device__ __forceinline__ int col(int j) const { return ldg(ciO + j); }
+        __device__ __forceinline__ int gnz(int, int j) const { return j; }
+    };
+
+    // acc[c] += sum over entries j of the row with col < limit:  a_j * (v0[c][col] + w * v1[c][col])
+    // (v1 may be null).  Arithmetic in T (FP32 in the inner solver: GB300's FP64 rate is ~1/64 of
+    // FP32); fixed-width predicated batches keep RB loads in flight per thread.
+    template <typename T, int NCH, bool SMEM>
+    __device__ __forceinline__ void rowGather(const RowView<SMEM> & rv, int color, int jb, int je, int limit,
+                                              const T * vO, int n, const T * v0, const T * v1, const T * w,
+                                              const bool (&act)[NCH], T (&acc)[NCH])
+    {
+        for (int j0 = jb; j0 < je; j0 += RB)
+        {
+            int cols[RB];
+            T vals[RB];
+#pragma unroll
+            for (int t = 0; t < RB; t++)
+            {
+                const int j = j0 + t;
+                const bool ok = j < je;
+                cols[t] = ok ? rv.col(j) : 0;
+                vals[t] = (ok && cols[t] < limit) ? ldg(vO + rv.gnz(color, j)) : (T)0;
+            }
+#pragma unroll
+            for (int c = 0; c < NCH; c++)
+                if (act[c])
+                {
+                    T g[RB];
+#pragma unroll
+                    for (int t = 0; t < RB; t++)
+                    {
+                        const size_t o = (size_t)c * n + cols[t];
+                        g[t] = vals[t] != (T)0 ? __ldcg(v0 + o) : (T)0;
+                        if (v1 && vals[t] != (T)0)
+                            g[t] += w[c] * __ldcg(v1 + o);
+                    }
+#pragma unroll
+                    for (int t = 0; t < RB; t++)
+                        acc[c] += vals[t] * g[t];
+                }
+        }
+    }
+
+    template <typename T, int NCH, bool SMEM>
     __global__ void __launch_bounds__(CTPB, 1) kPcgCluster(ClusterPcgArgs<T> A)
     {
+        extern __shared__ int smemI[];
         cg::cluster_group cl = cg::this_cluster();
         const int rank = (int)cl.block_rank(), cs = (int)cl.num_blocks();
         __shared__ double slot[2][8];
+        __shared__ int chunkA[MAXCOLORS], chunkL[MAXCOLORS + 1], chunkG[MAXCOLORS], nzBase[MAXCOLORS + 1];
         int buf = 0;
         SolverState * st = A.st;
         const int n = A.n, C = A.nColors;
         const int maxIters = st->maxIters, absMode = st->absMode;
         const double tol2 = st->tol2;
-        const bool skipAll = A.skip && *A.skip;
-        if (skipAll)
+        if (A.skip && *A.skip)
         {
             if (rank == 0 && threadIdx.x == 0)
                 for (int c = 0; c < MAXCH; c++)
@@ -108,62 +221,96 @@ namespace nsf
                     st->active[c] = 0;
                     st->iters[c] = 0;
                 }
-            return; // uniform: every CTA reads the same flag
+            return; // uniform: every CTA reads the same flag before any barrier
         }
-        const int lane = threadIdx.x & (L - 1);
-        const int grp = threadIdx.x / L, ngrp = CTPB / L;
-        const unsigned mask = (L == 32) ? FULL : (((1u << L) - 1u) << (((threadIdx.x & 31) / L) * L));
-        auto gsum = [&](double v) {
-#pragma unroll
-            for (int o = L / 2; o > 0; o >>= 1)
-                v += __shfl_down_sync(mask, v, o, L);
-            return v;
-        };
+
+        // ---- own rows: chunk `rank` of every color.  Local row l of color c is global row
+        // chunkA[c] + (l - chunkL[c]); a color chunk is one contiguous range of the CSR.
+        if (threadIdx.x == 0)
+        {
+            int l = 0, nz = 0;
+            for (int c = 0; c < C; c++)
+            {
+                const int a0 = chunkStart(A.ps, c, rank, cs), a1 = chunkStart(A.ps, c, rank + 1, cs);
+                chunkA[c] = a0;
+                chunkL[c] = l;
+                chunkG[c] = A.rsO[a0];
+                nzBase[c] = nz;
+                l += a1 - a0;
+                nz += A.rsO[a1] - A.rsO[a0];
+            }
+            chunkL[C] = l;
+            nzBase[C] = nz;
+        }
+        __syncthreads();
+        const int R = chunkL[C];
+        RowView<SMEM> rv;
+        if constexpr (SMEM)
+        {
+            int * lrs = smemI;
+            int * lci = smemI + R + 1;
+            for (int c = 0; c < C; c++)
+            {
+                const int a0 = chunkA[c], nr = chunkL[c + 1] - chunkL[c], cnt = nzBase[c + 1] - nzBase[c];
+                for (int t = threadIdx.x; t < nr; t += CTPB)
+                    lrs[chunkL[c] + t] = A.rsO[a0 + t] - chunkG[c] + nzBase[c];
+                for (int t = threadIdx.x; t < cnt; t += CTPB)
+                    lci[nzBase[c] + t] = A.ciO[chunkG[c] + t];
+            }
+            if (threadIdx.x == 0)
+                lrs[R] = nzBase[C];
+            __syncthreads();
+            rv.lrs = lrs;
+            rv.lci = lci;
+            rv.chunkA = chunkA;
+            rv.chunkL = chunkL;
+            rv.chunkG = chunkG;
+            rv.nzBase = nzBase;
+        }
+        else
+        {
+            rv.rsO = A.rsO;
+            rv.ciO = A.ciO;
+            rv.chunkA = chunkA;
+            rv.chunkL = chunkL;
+        }
 
         bool act[NCH];
 #pragma unroll
         for (int c = 0; c < NCH; c++)
             act[c] = c < A.numCh;
 
-        // ---- r = b - A x over own rows; ||b||^2
+        // ---- r = b - A x over own rows; ||b||^2 (dot products accumulate in FP64)
         double bb[NCH];
 #pragma unroll
         for (int c = 0; c < NCH; c++)
             bb[c] = 0;
         for (int col = 0; col < C; col++)
-        {
-            const int a0 = chunkStart(A.ps, col, rank, cs), a1 = chunkStart(A.ps, col, rank + 1, cs);
-            for (int i = a0 + grp; i < a1; i += ngrp)
+            for (int l = chunkL[col] + threadIdx.x; l < chunkL[col + 1]; l += CTPB)
             {
-                const int s = ldg(A.rsF + i), e = ldg(A.rsF + i + 1);
-                double acc[NCH];
+                const int i = chunkA[col] + (l - chunkL[col]);
+                const T d = ldg(A.diag + i);
+                T acc[NCH];
 #pragma unroll
                 for (int c = 0; c < NCH; c++)
-                    acc[c] = 0;
-                for (int j = s + lane; j < e; j += L)
-                {
-                    const double a = (double)ldg(A.vF + j);
-                    const int cj = ldg(A.ciF + j);
-#pragma unroll
-                    for (int c = 0; c < NCH; c++)
-                        acc[c] += a * (double)A.x[(size_t)c * n + cj];
-                }
+                    acc[c] = d * A.x[(size_t)c * n + i];
+                rowGather<T, NCH, SMEM>(rv, col, rv.begin(col, l), rv.end(col, l), INT_MAX, A.vO, n, A.x,
+                                        (const T *)nullptr, nullptr, act, acc);
 #pragma unroll
                 for (int c = 0; c < NCH; c++)
-                {
-                    const double t = gsum(acc[c]);
-                    if (lane == 0)
+                    if (act[c])
                     {
-                        const double bi = (double)A.b[(size_t)c * n + i];
-                        A.r[(size_t)c * n + i] = (T)(bi - t);
-                        bb[c] += bi * bi;
+                        const T bi = A.b[(size_t)c * n + i];
+                        A.r[(size_t)c * n + i] = bi - acc[c];
+                        bb[c] += (double)(bi * bi);
                     }
-                }
             }
-        }
 
-        // ---- z = SGS(r); rr and rz.  init: no x/r update
-        double alpha[NCH] = {};
+        T alphaT[NCH];
+#pragma unroll
+        for (int c = 0; c < NCH; c++)
+            alphaT[c] = 0;
+        // z = SGS(r); init: no x/r update.  Forward phases use earlier colors only (limit).
         auto sgs = [&](bool init, const T * pcur, double (&rr)[NCH], double (&rz)[NCH]) {
 #pragma unroll
             for (int c = 0; c < NCH; c++)
@@ -171,93 +318,67 @@ namespace nsf
             for (int col = 0; col < C; col++)
             {
                 const int r0 = A.ps[col];
-                const int a0 = chunkStart(A.ps, col, rank, cs), a1 = chunkStart(A.ps, col, rank + 1, cs);
-                for (int i = a0 + grp; i < a1; i += ngrp)
+                for (int l = chunkL[col] + threadIdx.x; l < chunkL[col + 1]; l += CTPB)
                 {
-                    double ri[NCH];
-                    if (lane == 0)
-                    {
+                    const int i = chunkA[col] + (l - chunkL[col]);
+                    const int jb = rv.begin(col, l), je = rv.end(col, l);
+                    T ri[NCH];
 #pragma unroll
-                        for (int c = 0; c < NCH; c++)
-                            if (act[c])
+                    for (int c = 0; c < NCH; c++)
+                        if (act[c])
+                        {
+                            const size_t o = (size_t)c * n + i;
+                            T rvv = A.r[o];
+                            if (!init)
                             {
-                                const size_t o = (size_t)c * n + i;
-                                double rv = (double)A.r[o];
-                                if (!init)
-                                {
-                                    A.x[o] = (T)((double)A.x[o] + alpha[c] * (double)pcur[o]);
-                                    rv -= alpha[c] * (double)A.q[o];
-                                    A.r[o] = (T)rv;
-                                }
-                                ri[c] = (double)(T)rv;
+                                A.x[o] = A.x[o] + alphaT[c] * pcur[o];
+                                rvv -= alphaT[c] * A.q[o];
+                                A.r[o] = rvv;
                             }
-                    }
-                    const int s = ldg(A.rsO + i), e = ldg(A.rsO + i + 1);
-                    double acc[NCH];
+                            ri[c] = rvv;
+                        }
+                    T acc[NCH];
 #pragma unroll
                     for (int c = 0; c < NCH; c++)
                         acc[c] = 0;
-                    for (int j = s + lane; j < e; j += L)
-                    {
-                        const int cj = ldg(A.ciO + j);
-                        if (cj >= r0)
-                            break; // later colors: still zero in the forward sweep
-                        const double a = (double)ldg(A.vO + j);
-#pragma unroll
-                        for (int c = 0; c < NCH; c++)
-                            if (act[c])
-                                acc[c] += a * (double)__ldcg(A.z + (size_t)c * n + cj);
-                    }
+                    rowGather<T, NCH, SMEM>(rv, col, jb, je, r0, A.vO, n, A.z, (const T *)nullptr, nullptr, act, acc);
+                    const T id = ldg(A.invD + i);
 #pragma unroll
                     for (int c = 0; c < NCH; c++)
-                    {
-                        const double t = gsum(acc[c]);
-                        if (lane == 0 && act[c])
+                        if (act[c])
                         {
-                            const size_t o = (size_t)c * n + i;
-                            const T zi = (T)((ri[c] - t) * (double)ldg(A.invD + i));
-                            A.z[o] = zi;
-                            rr[c] += ri[c] * ri[c];
+                            const T zi = (ri[c] - acc[c]) * id;
+                            A.z[(size_t)c * n + i] = zi;
+                            rr[c] += (double)(ri[c] * ri[c]);
                             if (col == C - 1)
-                                rz[c] += ri[c] * (double)zi;
+                                rz[c] += (double)(ri[c] * zi);
                         }
-                    }
                 }
                 if (C > 1)
                     cl.sync(); // z of this color visible to the cluster
             }
             for (int col = C - 2; col >= 0; col--)
             {
-                const int a0 = chunkStart(A.ps, col, rank, cs), a1 = chunkStart(A.ps, col, rank + 1, cs);
-                for (int i = a0 + grp; i < a1; i += ngrp)
+                for (int l = chunkL[col] + threadIdx.x; l < chunkL[col + 1]; l += CTPB)
                 {
-                    const int s = ldg(A.rsO + i), e = ldg(A.rsO + i + 1);
-                    double acc[NCH];
+                    const int i = chunkA[col] + (l - chunkL[col]);
+                    T acc[NCH];
 #pragma unroll
                     for (int c = 0; c < NCH; c++)
                         acc[c] = 0;
-                    for (int j = s + lane; j < e; j += L)
-                    {
-                        const double a = (double)ldg(A.vO + j);
-                        const int cj = ldg(A.ciO + j);
-#pragma unroll
-                        for (int c = 0; c < NCH; c++)
-                            if (act[c])
-                                acc[c] += a * (double)__ldcg(A.z + (size_t)c * n + cj);
-                    }
+                    rowGather<T, NCH, SMEM>(rv, col, rv.begin(col, l), rv.end(col, l), INT_MAX, A.vO, n, A.z,
+                                            (const T *)nullptr, nullptr, act, acc);
+                    const T id = ldg(A.invD + i);
 #pragma unroll
                     for (int c = 0; c < NCH; c++)
-                    {
-                        const double t = gsum(acc[c]);
-                        if (lane == 0 && act[c])
+                        if (act[c])
                         {
                             const size_t o = (size_t)c * n + i;
-                            const double rv = (double)A.r[o];
-                            const T zi = (T)((rv - t) * (double)ldg(A.invD + i));
+                            const T rvv = A.r[o];
+                            const T zi = (rvv - acc[c]) * id;
                             A.z[o] = zi;
-                            rz[c] += rv * (double)zi;
+                            rz[c] += (double)(rvv * zi);
                         }
-                    }
                 }
                 if (col > 0)
                     cl.sync(); // the last phase's barrier is the reduction's
@@ -283,6 +404,7 @@ namespace nsf
             bbT[c] = tot[c];
             rrT[c] = tot[NCH + c];
             rzT[c] = tot[2 * NCH + c];
+            rzPrev[c] = rzT[c];
             const bool fin = isfinite(rrT[c]) && isfinite(bbT[c]);
             const bool conv = absMode ? (rrT[c] < tol2) : (rrT[c] <= tol2 * bbT[c]);
             status[c] = fin ? 0 : 2;
@@ -302,59 +424,46 @@ namespace nsf
             // direction: p_new = z + beta p_old ; q = A p_new ; p.q   (own rows of every color)
             const T * pold = A.p + (size_t)((k - 1) & 1) * NCH * n;
             T * pnew = A.p + (size_t)(k & 1) * NCH * n;
-            double beta[NCH], pq[NCH];
+            T betaT[NCH];
+            double pq[NCH];
 #pragma unroll
             for (int c = 0; c < NCH; c++)
             {
-                beta[c] = (k == 1) ? 0.0 : rzT[c] / rzPrev[c];
+                betaT[c] = (k == 1) ? (T)0 : (T)(rzT[c] / rzPrev[c]);
                 pq[c] = 0;
             }
             for (int col = 0; col < C; col++)
-            {
-                const int a0 = chunkStart(A.ps, col, rank, cs), a1 = chunkStart(A.ps, col, rank + 1, cs);
-                for (int i = a0 + grp; i < a1; i += ngrp)
+                for (int l = chunkL[col] + threadIdx.x; l < chunkL[col + 1]; l += CTPB)
                 {
-                    const int s = ldg(A.rsF + i), e = ldg(A.rsF + i + 1);
-                    double acc[NCH];
+                    const int i = chunkA[col] + (l - chunkL[col]);
+                    const T d = ldg(A.diag + i);
+                    T pn[NCH], acc[NCH];
 #pragma unroll
                     for (int c = 0; c < NCH; c++)
-                        acc[c] = 0;
-                    for (int j = s + lane; j < e; j += L)
                     {
-                        const double a = (double)ldg(A.vF + j);
-                        const int cj = ldg(A.ciF + j);
-#pragma unroll
-                        for (int c = 0; c < NCH; c++)
-                            if (act[c])
-                            {
-                                const size_t o = (size_t)c * n + cj;
-                                const double zz = (double)__ldcg(A.z + o);
-                                acc[c] += a * (k == 1 ? zz : zz + beta[c] * (double)__ldcg(pold + o));
-                            }
+                        const size_t o = (size_t)c * n + i;
+                        pn[c] = act[c] ? (k == 1 ? A.z[o] : A.z[o] + betaT[c] * pold[o]) : (T)0;
+                        acc[c] = d * pn[c];
                     }
+                    rowGather<T, NCH, SMEM>(rv, col, rv.begin(col, l), rv.end(col, l), INT_MAX, A.vO, n, A.z,
+                                            k == 1 ? (const T *)nullptr : pold, betaT, act, acc);
 #pragma unroll
                     for (int c = 0; c < NCH; c++)
-                    {
-                        const double t = gsum(acc[c]);
-                        if (lane == 0 && act[c])
+                        if (act[c])
                         {
                             const size_t o = (size_t)c * n + i;
-                            const double zz = (double)A.z[o];
-                            const T pn = (T)(k == 1 ? zz : zz + beta[c] * (double)pold[o]);
-                            pnew[o] = pn;
-                            A.q[o] = (T)t;
-                            pq[c] += (double)pn * t;
+                            pnew[o] = pn[c];
+                            A.q[o] = acc[c];
+                            pq[c] += (double)(pn[c] * acc[c]);
                         }
-                    }
                 }
-            }
             double pqT[NCH];
             clusterSum<NCH>(cl, pq, slot, buf, pqT);
 #pragma unroll
             for (int c = 0; c < NCH; c++)
             {
                 rzPrev[c] = rzT[c]; // defines this alpha; the previous r.z of the next beta
-                alpha[c] = rzT[c] / pqT[c];
+                alphaT[c] = (T)(rzT[c] / pqT[c]);
                 if (act[c] && !(pqT[c] > 0))
                 {
                     status[c] = isfinite(pqT[c]) ? 4 : 2;
@@ -413,12 +522,22 @@ namespace nsf
     }
 
     // Largest cluster (16, else 8, else 0 = unavailable) the device can co-schedule for kernel k
-    // with CTPB threads per CTA.
+    // with CTPB threads per CTA and `smem` bytes of dynamic shared memory per CTA.
     template <typename K>
-    inline int pickClusterSize(K kernel)
+    inline int pickClusterSize(K kernel, size_t smemFor16, size_t smemFor8)
     {
         for (int cs : {16, 8})
         {
+            const size_t smem = cs == 16 ? smemFor16 : smemFor8;
+            if (smem > kClusterSmemCap)
+                continue;
+            // a fixed ceiling: solvers of different sizes share this kernel instantiation
+            if (cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kClusterSmemCap) !=
+                cudaSuccess)
+            {
+                cudaGetLastError();
+                continue;
+            }
             if (cs > 8 && cudaFuncSetAttribute(kernel, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess)
             {
                 cudaGetLastError();
@@ -427,6 +546,7 @@ namespace nsf
             cudaLaunchConfig_t cfg = {};
             cfg.gridDim = dim3(cs);
             cfg.blockDim = dim3(CTPB);
+            cfg.dynamicSmemBytes = smem;
             cudaLaunchAttribute at[1];
             at[0].id = cudaLaunchAttributeClusterDimension;
             at[0].val.clusterDim.x = cs;

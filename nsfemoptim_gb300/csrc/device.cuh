@@ -6,6 +6,7 @@
 #include "kernels.cuh"
 
 #include <atomic>
+#include <cstdio>
 #include <cstdlib>
 #include <stdexcept>
 #include <string>
@@ -188,11 +189,12 @@ namespace nsf
 
     // launch a one-cluster kernel: cs CTAs of 1024 threads forming one thread-block cluster
     template <typename Arg>
-    inline void launchCluster(void (*k)(Arg), int cs, cudaStream_t s, const Arg & a)
+    inline void launchCluster(void (*k)(Arg), int cs, size_t smem, cudaStream_t s, const Arg & a)
     {
         cudaLaunchConfig_t cfg = {};
         cfg.gridDim = dim3(cs);
         cfg.blockDim = dim3(1024);
+        cfg.dynamicSmemBytes = smem;
         cfg.stream = s;
         cudaLaunchAttribute at[1];
         at[0].id = cudaLaunchAttributeClusterDimension;

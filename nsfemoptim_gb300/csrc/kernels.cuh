@@ -410,27 +410,27 @@ namespace nsf
         for (int i = g.gid; i < n; i += g.ngroups)
         {
             const int s = ldg(rs + i), e = ldg(rs + i + 1);
-            double acc[NCH];
+            T acc[NCH]; // row arithmetic in the solve precision; dot products in FP64
 #pragma unroll
             for (int c = 0; c < NCH; c++)
                 acc[c] = 0;
             for (int j = s + g.lane; j < e; j += L)
             {
-                const double a = (double)ldg(v + j);
+                const T a = ldg(v + j);
                 const int col = ldg(ci + j);
 #pragma unroll
                 for (int c = 0; c < NCH; c++)
-                    acc[c] += a * (double)x[(size_t)c * n + col];
+                    acc[c] += a * x[(size_t)c * n + col];
             }
 #pragma unroll
             for (int c = 0; c < NCH; c++)
             {
-                const double t = g.sum(acc[c]);
+                const T t = g.sum(acc[c]);
                 if (g.lane == 0)
                 {
-                    const double bi = (double)b[(size_t)c * n + i];
-                    r[(size_t)c * n + i] = (T)(bi - t);
-                    bb[c] += bi * bi;
+                    const T bi = b[(size_t)c * n + i];
+                    r[(size_t)c * n + i] = bi - t;
+                    bb[c] += (double)(bi * bi);
                 }
             }
         }
@@ -530,37 +530,41 @@ namespace nsf
             const int n = P.n;
             const T * pold = pbuf + (size_t)((k - 1) & 1) * NCH * n;
             T * pnew = pbuf + (size_t)(k & 1) * NCH * n;
+            T betaT[NCH];
+#pragma unroll
+            for (int c = 0; c < NCH; c++)
+                betaT[c] = (T)beta[c];
             Group<L> g;
             for (int i = g.gid; i < n; i += g.ngroups)
             {
                 const int s = ldg(rs + i), e = ldg(rs + i + 1);
-                double acc[NCH];
+                T acc[NCH];
 #pragma unroll
                 for (int c = 0; c < NCH; c++)
                     acc[c] = 0;
                 for (int j = s + g.lane; j < e; j += L)
                 {
-                    const double a = (double)ldg(v + j);
+                    const T a = ldg(v + j);
                     const int col = ldg(ci + j);
 #pragma unroll
                     for (int c = 0; c < NCH; c++)
                         if (act[c])
                         {
                             const size_t o = (size_t)c * n + col;
-                            acc[c] += a * (k == 1 ? (double)z[o] : (double)z[o] + beta[c] * (double)pold[o]);
+                            acc[c] += a * (k == 1 ? z[o] : z[o] + betaT[c] * pold[o]);
                         }
                 }
 #pragma unroll
                 for (int c = 0; c < NCH; c++)
                 {
-                    const double t = g.sum(acc[c]);
+                    const T t = g.sum(acc[c]);
                     if (g.lane == 0 && act[c])
                     {
                         const size_t o = (size_t)c * n + i;
-                        const T pn = (T)(k == 1 ? (double)z[o] : (double)z[o] + beta[c] * (double)pold[o]);
+                        const T pn = k == 1 ? z[o] : z[o] + betaT[c] * pold[o];
                         pnew[o] = pn;
-                        q[o] = (T)t;
-                        pq[c] += (double)pn * t;
+                        q[o] = t;
+                        pq[c] += (double)pn * (double)t;
                     }
                 }
             }
@@ -600,6 +604,10 @@ namespace nsf
                 if (act[c] && !(st->pqOut[c] > 0))
                     st->status[c] = isfinite(st->pqOut[c]) ? 4 : 2; // stops at the next decision
         const T * p = pbuf + (size_t)(k & 1) * NCH * n;
+        T alphaT[NCH];
+#pragma unroll
+        for (int c = 0; c < NCH; c++)
+            alphaT[c] = (T)alpha[c];
         Group<L> g;
         double red[2 * NCH];
 #pragma unroll
@@ -608,7 +616,7 @@ namespace nsf
         if (anyAct<NCH>(act))
             for (int i = r0 + g.gid; i < r1; i += g.ngroups)
             {
-                double ri[NCH];
+                T ri[NCH];
                 if (g.lane == 0)
                 {
 #pragma unroll
@@ -616,18 +624,18 @@ namespace nsf
                         if (act[c])
                         {
                             const size_t o = (size_t)c * n + i;
-                            double rv = (double)r[o];
+                            T rv = r[o];
                             if (!init)
                             {
-                                x[o] = (T)((double)x[o] + alpha[c] * (double)p[o]);
-                                rv -= alpha[c] * (double)q[o];
-                                r[o] = (T)rv;
+                                x[o] = x[o] + alphaT[c] * p[o];
+                                rv -= alphaT[c] * q[o];
+                                r[o] = rv;
                             }
-                            ri[c] = (double)(T)rv;
+                            ri[c] = rv;
                         }
                 }
                 const int s = ldg(rs + i), e = ldg(rs + i + 1);
-                double acc[NCH];
+                T acc[NCH];
 #pragma unroll
                 for (int c = 0; c < NCH; c++)
                     acc[c] = 0;
@@ -636,24 +644,24 @@ namespace nsf
                     const int col = ldg(ci + j);
                     if (col >= r0)
                         break; // sorted columns: the rest are later colors (zero)
-                    const double a = (double)ldg(v + j);
+                    const T a = ldg(v + j);
 #pragma unroll
                     for (int c = 0; c < NCH; c++)
                         if (act[c])
-                            acc[c] += a * (double)z[(size_t)c * n + col];
+                            acc[c] += a * z[(size_t)c * n + col];
                 }
 #pragma unroll
                 for (int c = 0; c < NCH; c++)
                 {
-                    const double t = g.sum(acc[c]);
+                    const T t = g.sum(acc[c]);
                     if (g.lane == 0 && act[c])
                     {
                         const size_t o = (size_t)c * n + i;
-                        const T zi = (T)((ri[c] - t) * (double)ldg(invD + i));
+                        const T zi = (ri[c] - t) * ldg(invD + i);
                         z[o] = zi;
-                        red[c] += ri[c] * ri[c];
+                        red[c] += (double)ri[c] * (double)ri[c];
                         if (last)
-                            red[NCH + c] += ri[c] * (double)zi;
+                            red[NCH + c] += (double)ri[c] * (double)zi;
                     }
                 }
             }
@@ -691,30 +699,30 @@ namespace nsf
             for (int i = r0 + g.gid; i < r1; i += g.ngroups)
             {
                 const int s = ldg(rs + i), e = ldg(rs + i + 1);
-                double acc[NCH];
+                T acc[NCH];
 #pragma unroll
                 for (int c = 0; c < NCH; c++)
                     acc[c] = 0;
                 for (int j = s + g.lane; j < e; j += L)
                 {
-                    const double a = (double)ldg(v + j);
+                    const T a = ldg(v + j);
                     const int col = ldg(ci + j);
 #pragma unroll
                     for (int c = 0; c < NCH; c++)
                         if (act[c])
-                            acc[c] += a * (double)z[(size_t)c * n + col];
+                            acc[c] += a * z[(size_t)c * n + col];
                 }
 #pragma unroll
                 for (int c = 0; c < NCH; c++)
                 {
-                    const double t = g.sum(acc[c]);
+                    const T t = g.sum(acc[c]);
                     if (g.lane == 0 && act[c])
                     {
                         const size_t o = (size_t)c * n + i;
-                        const double ri = (double)r[o];
-                        const T zi = (T)((ri - t) * (double)ldg(invD + i));
+                        const T ri = r[o];
+                        const T zi = (ri - t) * ldg(invD + i);
                         z[o] = zi;
-                        rz[c] += ri * (double)zi;
+                        rz[c] += (double)ri * (double)zi;
                     }
                 }
             }
@@ -857,27 +865,27 @@ namespace nsf
         for (int i = r0 + g.gid; i < r1; i += g.ngroups)
         {
             const int s = ldg(rs + i), e = ldg(rs + i + 1);
-            double acc[NCH];
+            T acc[NCH];
 #pragma unroll
             for (int c = 0; c < NCH; c++)
                 acc[c] = 0;
             for (int j = s + g.lane; j < e; j += L)
             {
-                const double a = (double)ldg(v + j);
+                const T a = ldg(v + j);
                 const int col = ldg(ci + j);
 #pragma unroll
                 for (int c = 0; c < NCH; c++)
                     if (act[c])
-                        acc[c] += a * (double)x[(size_t)c * n + col];
+                        acc[c] += a * x[(size_t)c * n + col];
             }
 #pragma unroll
             for (int c = 0; c < NCH; c++)
             {
-                const double t = g.sum(acc[c]);
+                const T t = g.sum(acc[c]);
                 if (g.lane == 0 && act[c])
                 {
                     const size_t o = (size_t)c * n + i;
-                    x[o] = (T)(((double)b[o] - t) * (double)ldg(invD + i));
+                    x[o] = (b[o] - t) * ldg(invD + i);
                 }
             }
         }
@@ -909,25 +917,25 @@ namespace nsf
             for (int i = g.gid; i < n; i += g.ngroups)
             {
                 const int s = ldg(rs + i), e = ldg(rs + i + 1);
-                double acc[NCH];
+                T acc[NCH];
 #pragma unroll
                 for (int c = 0; c < NCH; c++)
                     acc[c] = 0;
                 for (int j = s + g.lane; j < e; j += L)
                 {
-                    const double a = (double)ldg(v + j);
+                    const T a = ldg(v + j);
                     const int col = ldg(ci + j);
 #pragma unroll
                     for (int c = 0; c < NCH; c++)
-                        acc[c] += a * (double)x[(size_t)c * n + col];
+                        acc[c] += a * x[(size_t)c * n + col];
                 }
 #pragma unroll
                 for (int c = 0; c < NCH; c++)
                 {
-                    const double t = g.sum(acc[c]);
+                    const T t = g.sum(acc[c]);
                     if (g.lane == 0)
                     {
-                        const double d = t - (double)b[(size_t)c * n + i];
+                        const double d = (double)(t - b[(size_t)c * n + i]);
                         rr[c] += d * d;
                     }
                 }

@@ -66,9 +66,10 @@ namespace nsf
     struct SweepSystem
     {
         int n = 0, nnzFull = 0, nColors = 0, L = 4;
-        std::vector<int> ps; // color starts (host), nColors + 1
+        std::vector<int> ps;      // color starts (host), nColors + 1
+        std::vector<int> hostRsO; // off-diagonal row offsets (host copy, sizes the cluster kernel)
         DevBuf<int> rsF, ciF, rsO, ciO;
-        DevBuf<T> vF, vO, invD;
+        DevBuf<T> vF, vO, invD, diag;
 
         // a: color-permuted square matrix (rows of color c contiguous), ps: color starts
         void build(const HostCsr<double> & a, const std::vector<int> & partStart)
@@ -80,7 +81,7 @@ namespace nsf
                 throw Error(ST_NOTSUP, "more than " + std::to_string(MAXCOLORS) + " colors");
             nnzFull = a.nnz();
             std::vector<int> ro(n + 1, 0), co;
-            std::vector<T> vo, vf(a.val.begin(), a.val.end()), id(n);
+            std::vector<T> vo, vf(a.val.begin(), a.val.end()), id(n), dg(n);
             co.reserve(a.nnz());
             vo.reserve(a.nnz());
             for (int r = 0; r < n; r++)
@@ -93,6 +94,7 @@ namespace nsf
                         if (a.val[j] == 0)
                             throw Error(ST_INVALID, "zero on the diagonal at row " + std::to_string(r));
                         id[r] = (T)(1.0 / a.val[j]);
+                        dg[r] = (T)a.val[j];
                         diag = true;
                     }
                     else
@@ -112,6 +114,8 @@ namespace nsf
             ciO.upload(co);
             vO.upload(vo);
             invD.upload(id);
+            diag.upload(dg);
+            hostRsO = ro;
             L = lanesFor(a.nnz(), n);
         }
 
@@ -131,15 +135,20 @@ namespace nsf
         DevBuf<SolverState> st;
         PcgPtrs P{};
         PinnedBuf<int> flag{1};
-        // cluster-resident variant (one launch per solve); 0 = multi-kernel path
-        int clusterSize = 0, clusterL = 2;
+        // cluster-resident variant (one launch per solve); 0 = multi-kernel path.  Used when the
+        // structure of a CTA's rows fits in shared memory (the pressure system); large systems
+        // (the mass matrix) keep the multi-kernel path, which spreads over every SM.
+        int clusterSize = 0;
+        bool clusterShared = false; // row structure cached in shared memory
+        size_t clusterSmem = 0;
         DevBuf<int> psDev;
 
-        // lanes per row in the cluster kernel: few lanes, many rows in flight per CTA
-        static int clusterLanes(const SweepSystem<T> * s)
+        static size_t smemFor(const SweepSystem<T> * s, int cs)
         {
-            const double avg = s->n > 0 ? (double)s->nnzFull / s->n : 1.0;
-            return avg <= 8 ? 2 : 4;
+            size_t m = 0;
+            for (int rk = 0; rk < cs; rk++)
+                m = std::max(m, clusterSmemBytes(s->ps, s->hostRsO, rk, cs));
+            return m;
         }
 
         void setup(const SweepSystem<T> * s, int channels, bool tryCluster = true)
@@ -149,12 +158,28 @@ namespace nsf
             const int n = s->n;
             psDev.upload(s->ps);
             clusterSize = 0;
-            if (tryCluster && envFlag("NSF_NO_CLUSTER") == 0)
+            clusterShared = false;
+            clusterSmem = 0;
+            // FP64 arithmetic is scarce on GB300 (~2 DFMA/clock/SM): a large FP64 system keeps the
+            // multi-kernel path that spreads its FMAs over every SM; FP32 solves and small systems
+            // run cluster-resident.
+            const bool fp64Heavy = sizeof(T) == 8 && (size_t)s->nnzFull * NCH > 1000000;
+            if (tryCluster && !fp64Heavy && envFlag("NSF_NO_CLUSTER") == 0)
             {
-                clusterL = clusterLanes(s);
-                clusterSize = clusterL == 2 ? pickClusterSize(kPcgCluster<T, 2, NCH>)
-                                            : pickClusterSize(kPcgCluster<T, 4, NCH>);
+                const size_t s16 = smemFor(s, 16), s8 = smemFor(s, 8);
+                if (envFlag("NSF_CLUSTER_GLOBAL") == 0)
+                    clusterSize = pickClusterSize(kPcgCluster<T, NCH, true>, s16, s8);
+                if (clusterSize > 0)
+                {
+                    clusterShared = true;
+                    clusterSmem = clusterSize == 16 ? s16 : s8;
+                }
+                else
+                    clusterSize = pickClusterSize(kPcgCluster<T, NCH, false>, 0, 0);
             }
+            if (envFlag("NSF_VERBOSE"))
+                std::fprintf(stderr, "[nsf] PCG n=%d colors=%d cluster=%d shared=%d smem=%zu\n", n, s->nColors,
+                             clusterSize, (int)clusterShared, clusterSmem);
             r.alloc((size_t)NCH * n);
             z.alloc((size_t)NCH * n);
             p.alloc((size_t)2 * NCH * n);
@@ -197,13 +222,13 @@ namespace nsf
                            absolute ? tol * tol * (double)S.n : tol * tol);
             if (clusterSize > 0)
             {
-                ClusterPcgArgs<T> A{S.n, S.nColors, numCh, psDev.get(), S.rsF.get(), S.ciF.get(), S.vF.get(),
-                                    S.rsO.get(), S.ciO.get(), S.vO.get(), S.invD.get(), b, x, r.get(), z.get(),
-                                    p.get(), q.get(), st.get(), P.skip};
-                if (clusterL == 2)
-                    launchCluster(kPcgCluster<T, 2, NCH>, clusterSize, s, A);
+                ClusterPcgArgs<T> A{S.n, S.nColors, numCh, psDev.get(), S.rsO.get(), S.ciO.get(), S.vO.get(),
+                                    S.diag.get(), S.invD.get(), b, x, r.get(), z.get(), p.get(), q.get(), st.get(),
+                                    P.skip};
+                if (clusterShared)
+                    launchCluster(kPcgCluster<T, NCH, true>, clusterSize, clusterSmem, s, A);
                 else
-                    launchCluster(kPcgCluster<T, 4, NCH>, clusterSize, s, A);
+                    launchCluster(kPcgCluster<T, NCH, false>, clusterSize, 0, s, A);
                 return;
             }
             NSF_LANES(S.L, NSF_LAUNCH((kPcgInit<T, LL, NCH>), S.fullBlocks(), s, P, S.rsF.get(), S.ciF.get(),
