@@ -1,0 +1,709 @@
+// Cluster-resident CG with the multicolor symmetric Gauss-Seidel preconditioner, every vector in
+// distributed shared memory.
+//
+// The variant of the cluster solver for systems whose per-CTA share of the vectors and of the row
+// structure fits in shared memory (the pressure Laplacian of the channel meshes).  One thread-block
+// cluster of CS CTAs x 1024 threads runs the whole solve; CTA k owns chunk k of every color block.
+//   * All CG vectors of a CTA's rows (x, r, q, z, both planes of p) and the diagonal and its
+//     inverse live in that CTA's shared memory.  Every CTA uses the same byte layout.
+//   * At kernel start the column index of every off-diagonal entry is replaced by the
+//     shared::cluster address of that column's z entry in the CTA that owns the column (mapa).
+//     The other vectors sit at fixed byte offsets from z in every CTA, so a neighbour gather of any
+//     vector is one shared-memory load of the address plus one ld.shared::cluster.
+//   * Inside the iteration loop global memory is touched only for the matrix values when they do
+//     not fit (VALS = false); x is read at the start and written back at the end.
+//   * Row arithmetic and per-thread partial dot products are in T; warp partials are promoted to
+//     FP64 and summed across warps and CTAs in a fixed order, so every CTA holds bit-identical
+//     scalars and takes the same loop decisions.  (FP64 instructions run at ~1/64 of the FP32 rate
+//     on this GPU, so FP64 work is kept to one warp per reduction.)
+//   * Phases end in cluster barriers (barrier.cluster arrive.release / wait.acquire), which order
+//     the shared-memory stores of one phase before the remote loads of the next.
+#pragma once
+
+#include <cooperative_groups.h>
+
+#include <algorithm>
+#include <climits>
+#include <vector>
+
+#include "cluster.cuh"
+#include "kernels.cuh"
+
+namespace nsf
+{
+    // Byte layout of the dynamic shared memory of one CTA (identical in every CTA of the cluster).
+    struct DsLayout
+    {
+        int stride;                     // elements per vector plane (largest CTA share, rounded up)
+        unsigned offZ, offP, offX, offR, offQ, offInvD, offDiag, offRs, offAd, offV, bytes;
+    };
+
+    inline size_t dsAlign(size_t b) { return (b + 15) & ~(size_t)15; }
+
+    // rows / off-diagonal entries of the largest CTA share; tsize = sizeof(T); vals: values cached too
+    inline DsLayout dsLayout(int rowsMax, int nzMax, int nch, int tsize, bool vals)
+    {
+        DsLayout L{};
+        L.stride = (rowsMax + 3) & ~3;
+        const size_t plane = (size_t)L.stride * tsize;
+        size_t o = 0;
+        L.offZ = (unsigned)o;
+        o += dsAlign(plane * nch);
+        L.offP = (unsigned)o;
+        o += dsAlign(plane * nch * 2);
+        L.offX = (unsigned)o;
+        o += dsAlign(plane * nch);
+        L.offR = (unsigned)o;
+        o += dsAlign(plane * nch);
+        L.offQ = (unsigned)o;
+        o += dsAlign(plane * nch);
+        L.offInvD = (unsigned)o;
+        o += dsAlign(plane);
+        L.offDiag = (unsigned)o;
+        o += dsAlign(plane);
+        L.offRs = (unsigned)o; // packed row starts: local entry offset | (lower-color entries << 24)
+        o += dsAlign((size_t)4 * (rowsMax + 1));
+        L.offAd = (unsigned)o; // shared::cluster addresses of the z entries of the columns
+        o += dsAlign((size_t)4 * nzMax);
+        L.offV = (unsigned)o;
+        if (vals)
+            o += dsAlign((size_t)tsize * nzMax);
+        L.bytes = (unsigned)o;
+        return L;
+    }
+
+    template <typename T>
+    struct DsPcgArgs
+    {
+        int n, nColors, numCh;
+        const int * ps;    // color starts, nColors + 1
+        const int * rsO;   // off-diagonal part: row offsets, column indices, values
+        const int * ciO;
+        const T * vO;
+        const int * cmap;  // per off-diagonal entry: owner rank << 24 | local row in the owner
+        const T * diag;
+        const T * invD;
+        const T * b;
+        T * x;
+        SolverState * st;
+        const int * skip;
+        DsLayout lay;
+    };
+
+    __device__ __forceinline__ unsigned dsMapa(unsigned localAddr, int rank)
+    {
+        unsigned r;
+        asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(localAddr), "r"(rank));
+        return r;
+    }
+
+    __device__ __forceinline__ float dsLoad(unsigned a, float)
+    {
+        float v;
+        asm volatile("ld.shared::cluster.f32 %0, [%1];" : "=f"(v) : "r"(a));
+        return v;
+    }
+
+    __device__ __forceinline__ double dsLoad(unsigned a, double)
+    {
+        double v;
+        asm volatile("ld.shared::cluster.f64 %0, [%1];" : "=d"(v) : "r"(a));
+        return v;
+    }
+
+    // acc[c] += sum over local entries [jb, je) of a_j * (V0[c][col_j] + w[c] * V1[c][col_j]), the
+    // vectors at byte offsets off0 / off1 from z in the owner CTA (V1 only when TWO).
+    template <typename T, int NCH, bool VALS, bool TWO>
+    __device__ __forceinline__ void dsGather(const unsigned * lad, const T * lv, const T * vOg, int jb, int je,
+                                             unsigned off0, unsigned off1, unsigned chBytes, const T (&w)[NCH],
+                                             const bool (&act)[NCH], T (&acc)[NCH])
+    {
+        for (int j0 = jb; j0 < je; j0 += RB)
+        {
+            unsigned ad[RB];
+            T v[RB];
+#pragma unroll
+            for (int t = 0; t < RB; t++)
+            {
+                const int j = j0 + t;
+                const bool ok = j < je;
+                ad[t] = ok ? lad[j] : 0u;
+                v[t] = ok ? (VALS ? lv[j] : ldg(vOg + j)) : (T)0;
+            }
+#pragma unroll
+            for (int c = 0; c < NCH; c++)
+                if (act[c])
+                {
+                    T g[RB];
+#pragma unroll
+                    for (int t = 0; t < RB; t++)
+                    {
+                        g[t] = (T)0;
+                        if (j0 + t < je)
+                        {
+                            const unsigned a = ad[t] + c * chBytes;
+                            g[t] = dsLoad(a + off0, (T)0);
+                            if (TWO)
+                                g[t] += w[c] * dsLoad(a + off1, (T)0);
+                        }
+                    }
+#pragma unroll
+                    for (int t = 0; t < RB; t++)
+                        acc[c] += v[t] * g[t];
+                }
+        }
+    }
+
+    // Sum over the cluster of K per-thread values in T with a fixed tree (lanes, then the warps of a
+    // CTA, then the CTAs), so every CTA obtains bit-identical totals.  Thread 0 of each CTA then
+    // runs epi(totals) -- the scalar work of the iteration, done once per CTA instead of once per
+    // thread -- and the CTA synchronises so every thread can read what epi wrote to shared memory.
+    // slot: the CTA's two alternating K-slot buffers read by the other CTAs after the barrier.
+    template <typename T, int K, typename Epi>
+    __device__ __forceinline__ void dsClusterSum(cg::cluster_group & cl, const T (&v)[K], T (*slot)[8], int & buf,
+                                                 Epi && epi)
+    {
+        __shared__ T warpPart[CTPB / 32][K];
+        const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+#pragma unroll
+        for (int k = 0; k < K; k++)
+        {
+            T s = v[k];
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1)
+                s += __shfl_xor_sync(FULL, s, o);
+            if (lane == 0)
+                warpPart[warp][k] = s;
+        }
+        __syncthreads();
+        if (warp == 0)
+        {
+#pragma unroll
+            for (int k = 0; k < K; k++)
+            {
+                T s = warpPart[lane][k];
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1)
+                    s += __shfl_xor_sync(FULL, s, o);
+                if (lane == 0)
+                    slot[buf][k] = s;
+            }
+        }
+        cl.sync();
+        if (warp == 0)
+        {
+            const int cs = (int)cl.num_blocks();
+            T rv[K];
+            const T * remote = cl.map_shared_rank(&slot[buf][0], lane < cs ? lane : 0);
+#pragma unroll
+            for (int k = 0; k < K; k++)
+                rv[k] = lane < cs ? remote[k] : (T)0;
+            T tot[K];
+#pragma unroll
+            for (int k = 0; k < K; k++)
+            {
+                T s = rv[k];
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1)
+                    s += __shfl_xor_sync(FULL, s, o);
+                tot[k] = s;
+            }
+            if (lane == 0)
+                epi(tot);
+        }
+        __syncthreads();
+        buf ^= 1;
+    }
+
+    // Iteration scalars of the cluster solver, kept by thread 0 of every CTA (all CTAs compute the
+    // same values from the same totals) and read by the other threads after a CTA barrier.
+    template <typename T, int NCH>
+    struct DsScalars
+    {
+        T alpha[NCH], beta[NCH];
+        int act[NCH], status[NCH], iters[NCH], any;
+        double bb[NCH], rr[NCH], rz[NCH], rzPrev[NCH];
+    };
+
+    template <typename T, int NCH, bool VALS>
+    __global__ void __launch_bounds__(CTPB, 1) kPcgClusterDs(DsPcgArgs<T> A)
+    {
+        extern __shared__ __align__(16) unsigned char dsm[];
+        cg::cluster_group cl = cg::this_cluster();
+        const int rank = (int)cl.block_rank(), cs = (int)cl.num_blocks();
+        __shared__ T slot[2][8];
+        __shared__ int chunkA[MAXCOLORS], chunkL[MAXCOLORS + 1], chunkG[MAXCOLORS], nzBase[MAXCOLORS + 1];
+        __shared__ DsScalars<T, NCH> sc;
+        int buf = 0;
+        SolverState * st = A.st;
+        const int n = A.n, C = A.nColors, numCh = A.numCh;
+        const int maxIters = st->maxIters;
+        if (A.skip && *A.skip)
+        {
+            if (rank == 0 && threadIdx.x == 0)
+                for (int c = 0; c < MAXCH; c++)
+                {
+                    st->active[c] = 0;
+                    st->iters[c] = 0;
+                }
+            return; // uniform: every CTA reads the same flag before any barrier
+        }
+
+        // ---- own rows: chunk `rank` of every color (local row l of color c is global row
+        // chunkA[c] + (l - chunkL[c])), entries numbered locally in the same order
+        if (threadIdx.x == 0)
+        {
+            int l = 0, nz = 0;
+            for (int c = 0; c < C; c++)
+            {
+                const int a0 = chunkStart(A.ps, c, rank, cs), a1 = chunkStart(A.ps, c, rank + 1, cs);
+                chunkA[c] = a0;
+                chunkL[c] = l;
+                chunkG[c] = A.rsO[a0];
+                nzBase[c] = nz;
+                l += a1 - a0;
+                nz += A.rsO[a1] - A.rsO[a0];
+            }
+            chunkL[C] = l;
+            nzBase[C] = nz;
+        }
+        const DsLayout L = A.lay;
+        {
+            // vector planes start at zero (padding entries stay finite)
+            uint4 * v4 = reinterpret_cast<uint4 *>(dsm);
+            const int cnt = (int)(L.offRs / 16);
+            for (int t = threadIdx.x; t < cnt; t += CTPB)
+                v4[t] = make_uint4(0u, 0u, 0u, 0u);
+        }
+        __syncthreads();
+        const int S = L.stride;
+        const unsigned chBytes = (unsigned)(S * sizeof(T));
+        T * zs = reinterpret_cast<T *>(dsm + L.offZ);
+        T * pl = reinterpret_cast<T *>(dsm + L.offP);
+        T * xs = reinterpret_cast<T *>(dsm + L.offX);
+        T * rsv = reinterpret_cast<T *>(dsm + L.offR);
+        T * qs = reinterpret_cast<T *>(dsm + L.offQ);
+        T * invDs = reinterpret_cast<T *>(dsm + L.offInvD);
+        T * diags = reinterpret_cast<T *>(dsm + L.offDiag);
+        unsigned * lrs = reinterpret_cast<unsigned *>(dsm + L.offRs);
+        unsigned * lad = reinterpret_cast<unsigned *>(dsm + L.offAd);
+        const T * lv = reinterpret_cast<const T *>(dsm + L.offV);
+        const unsigned zBase = (unsigned)__cvta_generic_to_shared(zs);
+        const unsigned offX = L.offX - L.offZ, offP0 = L.offP - L.offZ;
+        const int R = chunkL[C];
+        for (int c = 0; c < C; c++)
+        {
+            const int a0 = chunkA[c], nr = chunkL[c + 1] - chunkL[c], g0 = chunkG[c], nb = nzBase[c];
+            const int lo = A.ps[c];
+            for (int t = threadIdx.x; t < nr; t += CTPB)
+            {
+                const int l = chunkL[c] + t, i = a0 + t;
+                const int jb = ldg(A.rsO + i), je = ldg(A.rsO + i + 1);
+                int sp = jb;
+                while (sp < je && ldg(A.ciO + sp) < lo) // sorted columns: earlier colors first
+                    sp++;
+                lrs[l] = (unsigned)(jb - g0 + nb) | ((unsigned)(sp - jb) << 24);
+                invDs[l] = ldg(A.invD + i);
+                diags[l] = ldg(A.diag + i);
+#pragma unroll
+                for (int ch = 0; ch < NCH; ch++)
+                    xs[ch * S + l] = ch < numCh ? A.x[(size_t)ch * n + i] : (T)0;
+            }
+            const int cnt = nzBase[c + 1] - nb;
+            for (int t = threadIdx.x; t < cnt; t += CTPB)
+            {
+                const int e = ldg(A.cmap + g0 + t);
+                lad[nb + t] = dsMapa(zBase + (unsigned)(e & 0xFFFFFF) * (unsigned)sizeof(T), e >> 24);
+                if (VALS)
+                    reinterpret_cast<T *>(dsm + L.offV)[nb + t] = ldg(A.vO + g0 + t);
+            }
+        }
+        if (threadIdx.x == 0)
+            lrs[R] = (unsigned)nzBase[C];
+        cl.sync(); // every CTA's x and row structure in place
+
+        bool act[NCH];
+#pragma unroll
+        for (int c = 0; c < NCH; c++)
+            act[c] = c < numCh;
+        T alpha[NCH];
+#pragma unroll
+        for (int c = 0; c < NCH; c++)
+            alpha[c] = (T)0;
+
+        // ---- r = b - A x over own rows; ||b||^2
+        T bbP[NCH];
+#pragma unroll
+        for (int c = 0; c < NCH; c++)
+            bbP[c] = (T)0;
+        for (int col = 0; col < C; col++)
+        {
+            const T * vOg = A.vO + (chunkG[col] - nzBase[col]);
+            for (int l = chunkL[col] + threadIdx.x; l < chunkL[col + 1]; l += CTPB)
+            {
+                const int i = chunkA[col] + (l - chunkL[col]);
+                const int jb = (int)(lrs[l] & 0xFFFFFFu), je = (int)(lrs[l + 1] & 0xFFFFFFu);
+                const T d = diags[l];
+                T acc[NCH];
+#pragma unroll
+                for (int c = 0; c < NCH; c++)
+                    acc[c] = d * xs[c * S + l];
+                dsGather<T, NCH, VALS, false>(lad, lv, vOg, jb, je, offX, 0u, chBytes, alpha, act, acc);
+#pragma unroll
+                for (int c = 0; c < NCH; c++)
+                    if (act[c])
+                    {
+                        const T bi = A.b[(size_t)c * n + i];
+                        rsv[c * S + l] = bi - acc[c];
+                        bbP[c] += bi * bi;
+                    }
+            }
+        }
+
+        // z = SGS(r) from z = 0.  init: no x / r update.  Forward phases use earlier colors only.
+        auto sgs = [&](bool init, int plane, T (&rr)[NCH], T (&rz)[NCH]) {
+            const T * pc = pl + (size_t)plane * NCH * S;
+#pragma unroll
+            for (int c = 0; c < NCH; c++)
+                rr[c] = rz[c] = (T)0;
+            for (int col = 0; col < C; col++)
+            {
+                const T * vOg = A.vO + (chunkG[col] - nzBase[col]);
+                for (int l = chunkL[col] + threadIdx.x; l < chunkL[col + 1]; l += CTPB)
+                {
+                    const unsigned pk = lrs[l];
+                    const int jb = (int)(pk & 0xFFFFFFu), jl = jb + (int)(pk >> 24);
+                    T ri[NCH];
+#pragma unroll
+                    for (int c = 0; c < NCH; c++)
+                    {
+                        ri[c] = (T)0;
+                        if (act[c])
+                        {
+                            const int o = c * S + l;
+                            T rv = rsv[o];
+                            if (!init)
+                            {
+                                xs[o] = xs[o] + alpha[c] * pc[o];
+                                rv -= alpha[c] * qs[o];
+                                rsv[o] = rv;
+                            }
+                            ri[c] = rv;
+                        }
+                    }
+                    T acc[NCH];
+#pragma unroll
+                    for (int c = 0; c < NCH; c++)
+                        acc[c] = (T)0;
+                    dsGather<T, NCH, VALS, false>(lad, lv, vOg, jb, jl, 0u, 0u, chBytes, alpha, act, acc);
+                    const T id = invDs[l];
+#pragma unroll
+                    for (int c = 0; c < NCH; c++)
+                        if (act[c])
+                        {
+                            const T zi = (ri[c] - acc[c]) * id;
+                            zs[c * S + l] = zi;
+                            rr[c] += ri[c] * ri[c];
+                            if (col == C - 1)
+                                rz[c] += ri[c] * zi;
+                        }
+                }
+                if (C > 1)
+                    cl.sync(); // z of this color visible to the cluster
+            }
+            for (int col = C - 2; col >= 0; col--)
+            {
+                const T * vOg = A.vO + (chunkG[col] - nzBase[col]);
+                for (int l = chunkL[col] + threadIdx.x; l < chunkL[col + 1]; l += CTPB)
+                {
+                    const int jb = (int)(lrs[l] & 0xFFFFFFu), je = (int)(lrs[l + 1] & 0xFFFFFFu);
+                    T acc[NCH];
+#pragma unroll
+                    for (int c = 0; c < NCH; c++)
+                        acc[c] = (T)0;
+                    dsGather<T, NCH, VALS, false>(lad, lv, vOg, jb, je, 0u, 0u, chBytes, alpha, act, acc);
+                    const T id = invDs[l];
+#pragma unroll
+                    for (int c = 0; c < NCH; c++)
+                        if (act[c])
+                        {
+                            const int o = c * S + l;
+                            const T rv = rsv[o];
+                            const T zi = (rv - acc[c]) * id;
+                            zs[o] = zi;
+                            rz[c] += rv * zi;
+                        }
+                }
+                if (col > 0)
+                    cl.sync(); // the last phase's barrier is the reduction's
+            }
+        };
+
+        T rr0[NCH], rz0[NCH];
+        sgs(true, 0, rr0, rz0);
+        T red[3 * NCH];
+#pragma unroll
+        for (int c = 0; c < NCH; c++)
+        {
+            red[c] = bbP[c];
+            red[NCH + c] = rr0[c];
+            red[2 * NCH + c] = rz0[c];
+        }
+        const int absMode = st->absMode;
+        const double tol2 = st->tol2;
+        // scalar decisions: thread 0 of each CTA, FP64 (identical in every CTA)
+        dsClusterSum<T, 3 * NCH>(cl, red, slot, buf, [&](const T (&tot)[3 * NCH]) {
+            int any = 0;
+            for (int c = 0; c < NCH; c++)
+            {
+                const double bb = (double)tot[c], rr = (double)tot[NCH + c], rz = (double)tot[2 * NCH + c];
+                sc.bb[c] = bb;
+                sc.rr[c] = rr;
+                sc.rz[c] = rz;
+                sc.rzPrev[c] = rz;
+                const bool fin = isfinite(rr) && isfinite(bb);
+                const bool conv = absMode ? (rr < tol2) : (rr <= tol2 * bb);
+                sc.status[c] = fin ? 0 : 2;
+                sc.iters[c] = 0;
+                sc.act[c] = (c < numCh) && fin && !conv;
+                sc.alpha[c] = (T)0;
+                sc.beta[c] = (T)0;
+                any |= sc.act[c];
+            }
+            sc.any = any;
+        });
+#pragma unroll
+        for (int c = 0; c < NCH; c++)
+            act[c] = sc.act[c] != 0;
+
+        int k = 1;
+        for (; k <= maxIters; k++)
+        {
+            if (!sc.any)
+                break; // same value in every CTA
+            // direction: p_new = z + beta p_old ; q = A p_new ; p.q   (own rows of every color)
+            const int po = (k - 1) & 1, pnI = k & 1;
+            const T * pold = pl + (size_t)po * NCH * S;
+            T * pnew = pl + (size_t)pnI * NCH * S;
+            const unsigned offPold = offP0 + (unsigned)po * NCH * chBytes;
+            T beta[NCH], pq[NCH];
+#pragma unroll
+            for (int c = 0; c < NCH; c++)
+            {
+                beta[c] = sc.beta[c];
+                pq[c] = (T)0;
+            }
+            for (int col = 0; col < C; col++)
+            {
+                const T * vOg = A.vO + (chunkG[col] - nzBase[col]);
+                for (int l = chunkL[col] + threadIdx.x; l < chunkL[col + 1]; l += CTPB)
+                {
+                    const int jb = (int)(lrs[l] & 0xFFFFFFu), je = (int)(lrs[l + 1] & 0xFFFFFFu);
+                    const T d = diags[l];
+                    T pn[NCH], acc[NCH];
+#pragma unroll
+                    for (int c = 0; c < NCH; c++)
+                    {
+                        const int o = c * S + l;
+                        pn[c] = act[c] ? (k == 1 ? zs[o] : zs[o] + beta[c] * pold[o]) : (T)0;
+                        acc[c] = d * pn[c];
+                    }
+                    if (k == 1)
+                        dsGather<T, NCH, VALS, false>(lad, lv, vOg, jb, je, 0u, 0u, chBytes, beta, act, acc);
+                    else
+                        dsGather<T, NCH, VALS, true>(lad, lv, vOg, jb, je, 0u, offPold, chBytes, beta, act, acc);
+#pragma unroll
+                    for (int c = 0; c < NCH; c++)
+                        if (act[c])
+                        {
+                            const int o = c * S + l;
+                            pnew[o] = pn[c];
+                            qs[o] = acc[c];
+                            pq[c] += pn[c] * acc[c];
+                        }
+                }
+            }
+            dsClusterSum<T, NCH>(cl, pq, slot, buf, [&](const T (&tot)[NCH]) {
+                for (int c = 0; c < NCH; c++)
+                {
+                    const double pqc = (double)tot[c];
+                    sc.rzPrev[c] = sc.rz[c]; // defines this alpha; the previous r.z of the next beta
+                    sc.alpha[c] = (T)(sc.rz[c] / pqc);
+                    if (sc.act[c] && !(pqc > 0))
+                    {
+                        sc.status[c] = isfinite(pqc) ? 4 : 2;
+                        sc.iters[c] = k - 1;
+                        sc.act[c] = 0;
+                    }
+                }
+            });
+#pragma unroll
+            for (int c = 0; c < NCH; c++)
+            {
+                alpha[c] = sc.alpha[c];
+                act[c] = sc.act[c] != 0;
+            }
+            T rrN[NCH], rzN[NCH];
+            sgs(false, pnI, rrN, rzN);
+            T red2[2 * NCH];
+#pragma unroll
+            for (int c = 0; c < NCH; c++)
+            {
+                red2[c] = rrN[c];
+                red2[NCH + c] = rzN[c];
+            }
+            dsClusterSum<T, 2 * NCH>(cl, red2, slot, buf, [&](const T (&tot)[2 * NCH]) {
+                int any = 0;
+                for (int c = 0; c < NCH; c++)
+                {
+                    if (sc.act[c])
+                    {
+                        const double rr = (double)tot[c], rz = (double)tot[NCH + c];
+                        sc.rr[c] = rr;
+                        sc.rz[c] = rz;
+                        const bool fin = isfinite(rr) && isfinite(rz);
+                        const bool conv = absMode ? (rr < tol2) : (rr <= tol2 * sc.bb[c]);
+                        if (!fin || conv)
+                        {
+                            sc.act[c] = 0;
+                            sc.iters[c] = k;
+                            sc.status[c] = fin ? 0 : 2;
+                        }
+                        else
+                            sc.beta[c] = (T)(rz / sc.rzPrev[c]);
+                    }
+                    any |= sc.act[c];
+                }
+                sc.any = any;
+            });
+#pragma unroll
+            for (int c = 0; c < NCH; c++)
+                act[c] = sc.act[c] != 0;
+        }
+
+        // ---- x back to global memory (own rows)
+        for (int col = 0; col < C; col++)
+            for (int l = chunkL[col] + threadIdx.x; l < chunkL[col + 1]; l += CTPB)
+            {
+                const int i = chunkA[col] + (l - chunkL[col]);
+#pragma unroll
+                for (int c = 0; c < NCH; c++)
+                    if (c < numCh)
+                        A.x[(size_t)c * n + i] = xs[c * S + l];
+            }
+        // results (rank 0 writes; every CTA holds identical values)
+        if (rank == 0 && threadIdx.x == 0)
+        {
+            for (int c = 0; c < NCH; c++)
+            {
+                if (sc.act[c])
+                {
+                    sc.status[c] = 3;
+                    sc.iters[c] = maxIters;
+                }
+                st->status[c] = c < numCh ? sc.status[c] : 0;
+                st->iters[c] = sc.iters[c];
+                st->bb[c] = sc.bb[c];
+                st->lastRR[c] = sc.rr[c];
+                st->active[c] = 0;
+            }
+            st->iter = k;
+            st->anyActive = 0;
+        }
+        // no CTA may leave while another can still read its shared memory
+        cl.sync();
+    }
+
+    // Per-CTA shares of a color-permuted system split as the cluster kernels split it.
+    struct DsShares
+    {
+        int rowsMax = 0, nzMax = 0;
+        std::vector<int> cmap; // per off-diagonal entry: owner rank << 24 | local row in the owner
+    };
+
+    // ps: color starts; rsO / ciO: off-diagonal CSR (host); cs: cluster size
+    inline DsShares dsShares(const std::vector<int> & ps, const std::vector<int> & rsO, const std::vector<int> & ciO,
+                             int cs)
+    {
+        DsShares D;
+        const int C = (int)ps.size() - 1, n = ps.back();
+        std::vector<int> owner(n), local(n);
+        for (int rk = 0; rk < cs; rk++)
+        {
+            int l = 0, nz = 0;
+            for (int c = 0; c < C; c++)
+            {
+                const int len = ps[c + 1] - ps[c];
+                const int a0 = ps[c] + (int)(((long long)len * rk) / cs);
+                const int a1 = ps[c] + (int)(((long long)len * (rk + 1)) / cs);
+                for (int i = a0; i < a1; i++)
+                {
+                    owner[i] = rk;
+                    local[i] = l++;
+                }
+                nz += rsO[a1] - rsO[a0];
+            }
+            D.rowsMax = std::max(D.rowsMax, l);
+            D.nzMax = std::max(D.nzMax, nz);
+        }
+        D.cmap.resize(ciO.size());
+        for (size_t j = 0; j < ciO.size(); j++)
+            D.cmap[j] = (owner[ciO[j]] << 24) | local[ciO[j]];
+        return D;
+    }
+
+    // Whether one cluster of cs CTAs of kernel k with `smem` bytes of dynamic shared memory each can
+    // be co-scheduled.  The kernel's dynamic shared memory ceiling is set to the device maximum
+    // (minus its static shared memory) once, so solvers of different sizes can share the kernel.
+    template <typename K>
+    inline bool clusterFits(K kernel, int cs, size_t smem)
+    {
+        cudaFuncAttributes fa{};
+        int dev = 0, optin = 0;
+        if (cudaFuncGetAttributes(&fa, kernel) != cudaSuccess || cudaGetDevice(&dev) != cudaSuccess ||
+            cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess)
+        {
+            cudaGetLastError();
+            return false;
+        }
+        if ((size_t)optin <= fa.sharedSizeBytes)
+            return false;
+        const size_t cap = (size_t)optin - fa.sharedSizeBytes;
+        if (smem > cap)
+            return false;
+        if (cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cap) != cudaSuccess ||
+            (cs > 8 && cudaFuncSetAttribute(kernel, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess))
+        {
+            cudaGetLastError();
+            return false;
+        }
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3(cs);
+        cfg.blockDim = dim3(CTPB);
+        cfg.dynamicSmemBytes = smem;
+        cudaLaunchAttribute at[1];
+        at[0].id = cudaLaunchAttributeClusterDimension;
+        at[0].val.clusterDim.x = cs;
+        at[0].val.clusterDim.y = 1;
+        at[0].val.clusterDim.z = 1;
+        cfg.attrs = at;
+        cfg.numAttrs = 1;
+        int num = 0;
+        if (cudaOccupancyMaxActiveClusters(&num, kernel, &cfg) == cudaSuccess && num >= 1)
+            return true;
+        cudaGetLastError();
+        return false;
+    }
+
+    // Whether the per-CTA shares fit the packed encodings (24-bit local offsets, < 256 entries of
+    // earlier colors in a row).
+    inline bool dsEncodable(const DsShares & D, const std::vector<int> & rsO)
+    {
+        if (D.rowsMax >= (1 << 24) || D.nzMax >= (1 << 24))
+            return false;
+        for (size_t i = 0; i + 1 < rsO.size(); i++)
+            if (rsO[i + 1] - rsO[i] > 255)
+                return false;
+        return true;
+    }
+} // namespace nsf

@@ -65,20 +65,30 @@ namespace nsf
         double * p[K];
     };
 
-    // Grid-wide sum of K per-thread values.  Block sums go to scratch[k * gridDim.x + block]; the
-    // last block to take a ticket sums them in a fixed order, writes out.p[k], resets the ticket
-    // and, if tick != null, advances *tick.  Call at most once per kernel, from every thread.
-    template <int K>
-    __device__ __forceinline__ void gridSum(const double (&v)[K], double * scratch, const Outs<K> & out,
-                                            unsigned * ticket, int * tick)
+    struct NoEpi
     {
-        __shared__ double sm[TPB / 32][K];
+        __device__ void operator()() const {}
+    };
+
+    // Grid-wide sum of K per-thread values, accumulated in TA (the solve precision: FP64 work runs at
+    // ~1/64 of the FP32 rate on this GPU, so an FP32 solve keeps its reductions in FP32).  Block
+    // sums go to scratch[k * gridDim.x + block] (scratch holds >= K * gridDim.x values of TA); the
+    // last block to take a ticket sums them in a fixed order, writes out.p[k] (as FP64), runs
+    // epi() on one thread -- the once-per-grid scalar work that depends on the totals -- resets
+    // the ticket and, if tick != null, advances *tick.  Call at most once per kernel, from every
+    // thread.
+    template <typename TA, int K, typename Epi = NoEpi>
+    __device__ __forceinline__ void gridSum(const TA (&v)[K], double * scratchD, const Outs<K> & out,
+                                            unsigned * ticket, int * tick, Epi epi = Epi())
+    {
+        TA * scratch = reinterpret_cast<TA *>(scratchD);
+        __shared__ TA sm[TPB / 32][K];
         __shared__ bool lastBlock;
         const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 #pragma unroll
         for (int k = 0; k < K; k++)
         {
-            double s = v[k];
+            TA s = v[k];
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1)
                 s += __shfl_xor_sync(FULL, s, o);
@@ -91,7 +101,7 @@ namespace nsf
 #pragma unroll
             for (int k = 0; k < K; k++)
             {
-                double s = 0;
+                TA s = 0;
                 for (int w = 0; w < TPB / 32; w++)
                     s += sm[w][k];
                 scratch[k * gridDim.x + blockIdx.x] = s;
@@ -107,7 +117,7 @@ namespace nsf
 #pragma unroll
         for (int k = 0; k < K; k++)
         {
-            double s = 0;
+            TA s = 0;
             for (int i = threadIdx.x; i < (int)gridDim.x; i += TPB)
                 s += __ldcg(scratch + k * gridDim.x + i);
 #pragma unroll
@@ -122,12 +132,13 @@ namespace nsf
 #pragma unroll
             for (int k = 0; k < K; k++)
             {
-                double s = 0;
+                TA s = 0;
                 for (int w = 0; w < TPB / 32; w++)
                     s += sm[w][k];
                 if (out.p[k])
-                    *out.p[k] = s;
+                    *out.p[k] = (double)s;
             }
+            epi();
             *ticket = 0;
             if (tick)
                 *tick += 1;
@@ -334,7 +345,14 @@ namespace nsf
         unsigned ticket;              // last-block ticket of the grid reductions
         int skip;                     // refinement: 1 once the outer loop has stopped
         int innerTotal[MAXCH];        // refinement: inner iterations summed over passes
+        // CG step lengths, computed once per grid by the thread that finishes a reduction and read
+        // by every thread in the solve precision
+        double alphaD[MAXCH], betaD[MAXCH];
+        float alphaF[MAXCH], betaF[MAXCH];
     };
+
+    __device__ __forceinline__ void loadScalar(float & v, const double *, const float * f, int c) { v = f[c]; }
+    __device__ __forceinline__ void loadScalar(double & v, const double * d, const float *, int c) { v = d[c]; }
 
     __global__ void kSetConfig(SolverState * st, int maxIters, int absMode, double tol2)
     {
@@ -402,7 +420,7 @@ namespace nsf
                                                      const T * __restrict__ b, T * __restrict__ r)
     {
         Group<L> g;
-        double bb[NCH];
+        T bb[NCH];
 #pragma unroll
         for (int c = 0; c < NCH; c++)
             bb[c] = 0;
@@ -410,7 +428,7 @@ namespace nsf
         for (int i = g.gid; i < n; i += g.ngroups)
         {
             const int s = ldg(rs + i), e = ldg(rs + i + 1);
-            T acc[NCH]; // row arithmetic in the solve precision; dot products in FP64
+            T acc[NCH]; // row arithmetic and reductions in the solve precision
 #pragma unroll
             for (int c = 0; c < NCH; c++)
                 acc[c] = 0;
@@ -430,7 +448,7 @@ namespace nsf
                 {
                     const T bi = b[(size_t)c * n + i];
                     r[(size_t)c * n + i] = bi - t;
-                    bb[c] += (double)(bi * bi);
+                    bb[c] += bi * bi;
                 }
             }
         }
@@ -438,10 +456,46 @@ namespace nsf
 #pragma unroll
         for (int c = 0; c < NCH; c++)
             o.p[c] = &P.st->bbOut[c];
-        gridSum<NCH>(bb, P.scratch, o, &P.st->ticket, nullptr);
+        gridSum<T, NCH>(bb, P.scratch, o, &P.st->ticket, nullptr);
     }
 
-    // Finish the initial state once the SGS of r0 is done: bb, activity, iteration counter.
+    // Decision before iteration k, taken by one thread once the SGS sweep that produced the phase
+    // sums of ||r||^2 and r.z is complete (end of iteration k - 1, or the initial sweep): stop the
+    // channels that converged, went non-finite, broke down or reached the cap; beta of iteration k;
+    // end the device loop when nothing is left.
+    template <int NCH>
+    __device__ void pcgDecide(SolverState * st, int nColors, int numCh, int k, unsigned long long cond)
+    {
+        int any = 0;
+        for (int c = 0; c < NCH; c++)
+        {
+            const double rr = phaseSum(st->rrOut, nColors, c);
+            const double rz = phaseSum(st->rzOut, nColors, c);
+            const bool wasActive = c < numCh && st->active[c] && st->status[c] == 0;
+            const bool fin = isfinite(rr) && isfinite(rz);
+            const bool conv = st->absMode ? (rr < st->tol2) : (rr <= st->tol2 * st->bb[c]);
+            const bool act = wasActive && fin && !conv && (k <= st->maxIters);
+            const double beta = (k == 1) ? 0.0 : rz / st->rzHist[(k - 1) & 1][c];
+            if (c < numCh && st->active[c] && !act)
+            {
+                st->iters[c] = k - 1;
+                st->lastRR[c] = rr;
+                if (st->status[c] == 0)
+                    st->status[c] = !fin ? 2 : (conv ? 0 : 3);
+            }
+            st->rzHist[k & 1][c] = rz;
+            st->betaD[c] = beta;
+            st->betaF[c] = (float)beta;
+            st->active[c] = act;
+            any |= act;
+        }
+        st->anyActive = any;
+        if (!any && cond)
+            cudaGraphSetConditional(cond, 0);
+    }
+
+    // Finish the initial state once the SGS of r0 is done: bb, activity, iteration counter, and the
+    // decision before the first iteration.
     template <int NCH>
     __global__ void kPcgStart(PcgPtrs P, int numCh)
     {
@@ -470,6 +524,7 @@ namespace nsf
         st->iter = 1;
         st->ticket = 0;
         st->anyActive = any;
+        pcgDecide<NCH>(st, P.nColors, numCh, 1, 0ull);
     }
 
     // Iteration kernel A: convergence decision from the previous iteration's ||r||^2, beta,
@@ -482,58 +537,29 @@ namespace nsf
     {
         SolverState * st = P.st;
         const int k = st->iter; // stable for the whole iteration
+        if (!st->anyActive)
+        {
+            // every channel stopped at the last decision (same value in every block): end the loop
+            if (blockIdx.x == 0 && threadIdx.x == 0 && P.cond)
+                cudaGraphSetConditional(P.cond, 0);
+            return;
+        }
         bool act[NCH];
-        double beta[NCH];
-        bool stopAll = true;
+        T betaT[NCH];
 #pragma unroll
         for (int c = 0; c < NCH; c++)
         {
-            const double rr = phaseSum(st->rrOut, P.nColors, c);
-            const double rz = phaseSum(st->rzOut, P.nColors, c);
-            const bool wasActive = c < numCh && st->active[c] && st->status[c] == 0;
-            const bool fin = isfinite(rr) && isfinite(rz);
-            const bool conv = st->absMode ? (rr < st->tol2) : (rr <= st->tol2 * st->bb[c]);
-            act[c] = wasActive && fin && !conv && (k <= st->maxIters);
-            beta[c] = (k == 1) ? 0.0 : rz / st->rzHist[(k - 1) & 1][c];
-            stopAll &= !act[c];
-            if (blockIdx.x == 0 && threadIdx.x == 0)
-            {
-                if (c < numCh && st->active[c] && !act[c])
-                {
-                    st->iters[c] = k - 1;
-                    st->lastRR[c] = rr;
-                    if (st->status[c] == 0)
-                        st->status[c] = !fin ? 2 : (conv ? 0 : 3);
-                }
-                st->rzHist[k & 1][c] = rz;
-            }
+            act[c] = c < numCh && st->active[c];
+            loadScalar(betaT[c], st->betaD, st->betaF, c);
         }
-        __syncthreads(); // every block has read st->active before block 0 updates it
-        if (blockIdx.x == 0 && threadIdx.x == 0)
-        {
-            int any = 0;
-            for (int c = 0; c < NCH; c++)
-            {
-                st->active[c] = act[c];
-                any |= act[c];
-            }
-            st->anyActive = any;
-            if (!any && P.cond)
-                cudaGraphSetConditional(P.cond, 0);
-        }
-        double pq[NCH];
+        T pq[NCH];
 #pragma unroll
         for (int c = 0; c < NCH; c++)
             pq[c] = 0;
-        if (!stopAll)
         {
             const int n = P.n;
             const T * pold = pbuf + (size_t)((k - 1) & 1) * NCH * n;
             T * pnew = pbuf + (size_t)(k & 1) * NCH * n;
-            T betaT[NCH];
-#pragma unroll
-            for (int c = 0; c < NCH; c++)
-                betaT[c] = (T)beta[c];
             Group<L> g;
             for (int i = g.gid; i < n; i += g.ngroups)
             {
@@ -564,7 +590,7 @@ namespace nsf
                         const T pn = k == 1 ? z[o] : z[o] + betaT[c] * pold[o];
                         pnew[o] = pn;
                         q[o] = t;
-                        pq[c] += (double)pn * (double)t;
+                        pq[c] += pn * t;
                     }
                 }
             }
@@ -573,7 +599,18 @@ namespace nsf
 #pragma unroll
         for (int c = 0; c < NCH; c++)
             o.p[c] = &st->pqOut[c];
-        gridSum<NCH>(pq, P.scratch, o, &st->ticket, nullptr);
+        // once per grid: alpha = r.z / p.q, breakdown when p.q <= 0 (the channel stops at the next decision)
+        gridSum<T, NCH>(pq, P.scratch, o, &st->ticket, nullptr, [&]() {
+            for (int c = 0; c < NCH; c++)
+            {
+                const double pqc = st->pqOut[c];
+                const double a = st->rzHist[k & 1][c] / pqc;
+                st->alphaD[c] = a;
+                st->alphaF[c] = (float)a;
+                if (c < numCh && st->active[c] && !(pqc > 0))
+                    st->status[c] = isfinite(pqc) ? 4 : 2;
+            }
+        });
     }
 
     // Forward SGS phase over color rows [r0, r1) using only neighbours of earlier colors
@@ -590,26 +627,20 @@ namespace nsf
     {
         SolverState * st = P.st;
         bool act[NCH];
-        double alpha[NCH];
+        T alphaT[NCH];
         const int k = st->iter;
         const int n = P.n;
 #pragma unroll
         for (int c = 0; c < NCH; c++)
         {
             act[c] = c < numCh && (init || st->active[c]);
-            alpha[c] = init ? 0.0 : st->rzHist[k & 1][c] / st->pqOut[c];
+            alphaT[c] = 0;
+            if (!init)
+                loadScalar(alphaT[c], st->alphaD, st->alphaF, c);
         }
-        if (!init && blockIdx.x == 0 && threadIdx.x == 0)
-            for (int c = 0; c < NCH; c++)
-                if (act[c] && !(st->pqOut[c] > 0))
-                    st->status[c] = isfinite(st->pqOut[c]) ? 4 : 2; // stops at the next decision
         const T * p = pbuf + (size_t)(k & 1) * NCH * n;
-        T alphaT[NCH];
-#pragma unroll
-        for (int c = 0; c < NCH; c++)
-            alphaT[c] = (T)alpha[c];
         Group<L> g;
-        double red[2 * NCH];
+        T red[2 * NCH];
 #pragma unroll
         for (int c = 0; c < 2 * NCH; c++)
             red[c] = 0;
@@ -659,9 +690,9 @@ namespace nsf
                         const size_t o = (size_t)c * n + i;
                         const T zi = (ri[c] - t) * ldg(invD + i);
                         z[o] = zi;
-                        red[c] += (double)ri[c] * (double)ri[c];
+                        red[c] += ri[c] * ri[c];
                         if (last)
-                            red[NCH + c] += (double)ri[c] * (double)zi;
+                            red[NCH + c] += ri[c] * zi;
                     }
                 }
             }
@@ -672,7 +703,11 @@ namespace nsf
             o.p[c] = &st->rrOut[color][c];
             o.p[NCH + c] = last ? &st->rzOut[color][c] : nullptr;
         }
-        gridSum<2 * NCH>(red, P.scratch, o, &st->ticket, (tick && !init) ? &st->iter : nullptr);
+        const bool ends = tick && !init; // last kernel of an iteration: decide the next one
+        gridSum<T, 2 * NCH>(red, P.scratch, o, &st->ticket, ends ? &st->iter : nullptr, [&]() {
+            if (ends)
+                pcgDecide<NCH>(st, P.nColors, numCh, k + 1, P.cond);
+        });
     }
 
     // Backward SGS phase over color rows [r0, r1) with all off-diagonal neighbours; r.z of the
@@ -690,8 +725,9 @@ namespace nsf
         for (int c = 0; c < NCH; c++)
             act[c] = c < numCh && (init || st->active[c]);
         const int n = P.n;
+        const int k = st->iter;
         Group<L> g;
-        double rz[NCH];
+        T rz[NCH];
 #pragma unroll
         for (int c = 0; c < NCH; c++)
             rz[c] = 0;
@@ -722,7 +758,7 @@ namespace nsf
                         const T ri = r[o];
                         const T zi = (ri - t) * ldg(invD + i);
                         z[o] = zi;
-                        rz[c] += (double)ri * (double)zi;
+                        rz[c] += ri * zi;
                     }
                 }
             }
@@ -730,7 +766,11 @@ namespace nsf
 #pragma unroll
         for (int c = 0; c < NCH; c++)
             o.p[c] = &st->rzOut[color][c];
-        gridSum<NCH>(rz, P.scratch, o, &st->ticket, (tick && !init) ? &st->iter : nullptr);
+        const bool ends = tick && !init; // last kernel of an iteration: decide the next one
+        gridSum<T, NCH>(rz, P.scratch, o, &st->ticket, ends ? &st->iter : nullptr, [&]() {
+            if (ends)
+                pcgDecide<NCH>(st, P.nColors, numCh, k + 1, P.cond);
+        });
     }
 
     // ------------------------------------------------------------------ multicolor Gauss-Seidel
@@ -750,7 +790,7 @@ namespace nsf
     template <typename T, int NCH>
     __global__ void __launch_bounds__(TPB) kGsInit(GsPtrs P, int numCh, const T * __restrict__ b)
     {
-        double bb[NCH];
+        T bb[NCH];
 #pragma unroll
         for (int c = 0; c < NCH; c++)
             bb[c] = 0;
@@ -759,14 +799,14 @@ namespace nsf
 #pragma unroll
             for (int c = 0; c < NCH; c++)
             {
-                const double t = (double)b[(size_t)c * n + i];
+                const T t = b[(size_t)c * n + i];
                 bb[c] += t * t;
             }
         Outs<NCH> o;
 #pragma unroll
         for (int c = 0; c < NCH; c++)
             o.p[c] = &P.st->bbOut[c];
-        gridSum<NCH>(bb, P.scratch, o, &P.st->ticket, nullptr);
+        gridSum<T, NCH>(bb, P.scratch, o, &P.st->ticket, nullptr);
     }
 
     template <int NCH>
@@ -906,7 +946,7 @@ namespace nsf
         if (!anyAct<NCH>(act))
             return; // the loop is ending; no tick needed
         const bool doCheck = (k % P.interval) == 0;
-        double rr[NCH];
+        T rr[NCH];
 #pragma unroll
         for (int c = 0; c < NCH; c++)
             rr[c] = 0;
@@ -935,7 +975,7 @@ namespace nsf
                     const T t = g.sum(acc[c]);
                     if (g.lane == 0)
                     {
-                        const double d = (double)(t - b[(size_t)c * n + i]);
+                        const T d = t - b[(size_t)c * n + i];
                         rr[c] += d * d;
                     }
                 }
@@ -945,7 +985,7 @@ namespace nsf
 #pragma unroll
         for (int c = 0; c < NCH; c++)
             o.p[c] = doCheck ? &st->rrOut[0][c] : nullptr;
-        gridSum<NCH>(rr, P.scratch, o, &st->ticket, &st->iter);
+        gridSum<T, NCH>(rr, P.scratch, o, &st->ticket, &st->iter);
     }
 
     // ------------------------------------------------------------------ FP64 refinement
@@ -1000,7 +1040,7 @@ namespace nsf
             o.p[c] = &st->rrOut[0][c];
             o.p[NCH + c] = &st->bbOut[c];
         }
-        gridSum<2 * NCH>(red, scratch, o, &st->ticket, nullptr);
+        gridSum<double, 2 * NCH>(red, scratch, o, &st->ticket, nullptr);
     }
 
     // Stop decision of refinement pass `pass` (sticky); stats: iters = refinement updates applied.

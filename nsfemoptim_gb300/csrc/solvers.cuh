@@ -10,6 +10,7 @@
 #pragma once
 
 #include "cluster.cuh"
+#include "cluster_dsmem.cuh"
 #include "device.cuh"
 #include "host/setup.hpp"
 #include "kernels.cuh"
@@ -68,6 +69,7 @@ namespace nsf
         int n = 0, nnzFull = 0, nColors = 0, L = 4;
         std::vector<int> ps;      // color starts (host), nColors + 1
         std::vector<int> hostRsO; // off-diagonal row offsets (host copy, sizes the cluster kernel)
+        std::vector<int> hostCiO; // off-diagonal column indices (host copy, maps columns to CTAs)
         DevBuf<int> rsF, ciF, rsO, ciO;
         DevBuf<T> vF, vO, invD, diag;
 
@@ -116,6 +118,7 @@ namespace nsf
             invD.upload(id);
             diag.upload(dg);
             hostRsO = ro;
+            hostCiO = co;
             L = lanesFor(a.nnz(), n);
         }
 
@@ -137,11 +140,44 @@ namespace nsf
         PinnedBuf<int> flag{1};
         // cluster-resident variant (one launch per solve); 0 = multi-kernel path.  Used when the
         // structure of a CTA's rows fits in shared memory (the pressure system); large systems
-        // (the mass matrix) keep the multi-kernel path, which spreads over every SM.
+        // (the mass matrix) keep the multi-kernel path, which spreads over every SM
+        // (NSF_CLUSTER_GLOBAL=1 forces the cluster variant that reads the structure from global memory).
         int clusterSize = 0;
         bool clusterShared = false; // row structure cached in shared memory
         size_t clusterSmem = 0;
         DevBuf<int> psDev;
+        // cluster variant with every vector in distributed shared memory (preferred when a CTA's
+        // share fits): -1 unused, 0 matrix values read from global memory, 1 values in shared memory
+        int dsVals = -1;
+        DsLayout dsLay{};
+        DevBuf<int> cmapDev;
+
+        bool setupDsmem(const SweepSystem<T> * s)
+        {
+            const bool allowVals = envFlag("NSF_DS_NOVALS") == 0;
+            for (int cs : {16, 8})
+            {
+                DsShares D = dsShares(s->ps, s->hostRsO, s->hostCiO, cs);
+                if (!dsEncodable(D, s->hostRsO))
+                    return false;
+                for (int vals = allowVals ? 1 : 0; vals >= 0; vals--)
+                {
+                    const DsLayout lay = dsLayout(D.rowsMax, D.nzMax, NCH, (int)sizeof(T), vals != 0);
+                    const bool fits = vals ? clusterFits(kPcgClusterDs<T, NCH, true>, cs, lay.bytes)
+                                           : clusterFits(kPcgClusterDs<T, NCH, false>, cs, lay.bytes);
+                    if (fits)
+                    {
+                        clusterSize = cs;
+                        dsVals = vals;
+                        dsLay = lay;
+                        clusterSmem = lay.bytes;
+                        cmapDev.upload(D.cmap);
+                        return true;
+                    }
+                }
+            }
+            return false;
+        }
 
         static size_t smemFor(const SweepSystem<T> * s, int cs)
         {
@@ -160,6 +196,7 @@ namespace nsf
             clusterSize = 0;
             clusterShared = false;
             clusterSmem = 0;
+            dsVals = -1;
             // FP64 arithmetic is scarce on GB300 (~2 DFMA/clock/SM): a large FP64 system keeps the
             // multi-kernel path that spreads its FMAs over every SM; FP32 solves and small systems
             // run cluster-resident.
@@ -167,19 +204,25 @@ namespace nsf
             if (tryCluster && !fp64Heavy && envFlag("NSF_NO_CLUSTER") == 0)
             {
                 const size_t s16 = smemFor(s, 16), s8 = smemFor(s, 8);
-                if (envFlag("NSF_CLUSTER_GLOBAL") == 0)
-                    clusterSize = pickClusterSize(kPcgCluster<T, NCH, true>, s16, s8);
-                if (clusterSize > 0)
+                if (envFlag("NSF_CLUSTER_GLOBAL") == 0 && envFlag("NSF_NO_DSMEM") == 0 && setupDsmem(s))
                 {
-                    clusterShared = true;
-                    clusterSmem = clusterSize == 16 ? s16 : s8;
+                    // vectors in distributed shared memory
                 }
-                else
+                else if (envFlag("NSF_CLUSTER_GLOBAL") == 0)
+                {
+                    clusterSize = pickClusterSize(kPcgCluster<T, NCH, true>, s16, s8);
+                    if (clusterSize > 0)
+                    {
+                        clusterShared = true;
+                        clusterSmem = clusterSize == 16 ? s16 : s8;
+                    }
+                }
+                else // structure read from global memory (a large system on 16 SMs: slower than multi-kernel)
                     clusterSize = pickClusterSize(kPcgCluster<T, NCH, false>, 0, 0);
             }
             if (envFlag("NSF_VERBOSE"))
-                std::fprintf(stderr, "[nsf] PCG n=%d colors=%d cluster=%d shared=%d smem=%zu\n", n, s->nColors,
-                             clusterSize, (int)clusterShared, clusterSmem);
+                std::fprintf(stderr, "[nsf] PCG n=%d colors=%d cluster=%d shared=%d dsmem=%d smem=%zu\n", n,
+                             s->nColors, clusterSize, (int)clusterShared, dsVals, clusterSmem);
             r.alloc((size_t)NCH * n);
             z.alloc((size_t)NCH * n);
             p.alloc((size_t)2 * NCH * n);
@@ -220,6 +263,17 @@ namespace nsf
             if (setConfig)
                 NSF_LAUNCH(kSetConfig, 1, s, st.get(), maxIters, absolute ? 1 : 0,
                            absolute ? tol * tol * (double)S.n : tol * tol);
+            if (dsVals >= 0)
+            {
+                DsPcgArgs<T> A{S.n,         S.nColors,    numCh,   psDev.get(), S.rsO.get(), S.ciO.get(),
+                               S.vO.get(),  cmapDev.get(), S.diag.get(), S.invD.get(), b,    x,
+                               st.get(),    P.skip,       dsLay};
+                if (dsVals)
+                    launchCluster(kPcgClusterDs<T, NCH, true>, clusterSize, dsLay.bytes, s, A);
+                else
+                    launchCluster(kPcgClusterDs<T, NCH, false>, clusterSize, dsLay.bytes, s, A);
+                return;
+            }
             if (clusterSize > 0)
             {
                 ClusterPcgArgs<T> A{S.n, S.nColors, numCh, psDev.get(), S.rsO.get(), S.ciO.get(), S.vO.get(),

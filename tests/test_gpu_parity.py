@@ -117,15 +117,20 @@ def test_pcg_pressure_matches_oracle(setup, torch_cuda):
     assert np.linalg.norm(r) <= 1.01e-10 * np.linalg.norm(b)
 
 
-@pytest.mark.parametrize("path", ["cluster", "multikernel"])
+@pytest.mark.parametrize("path", ["cluster-dsmem", "cluster-dsmem-novals", "cluster-l2", "cluster-global",
+                                  "multikernel"])
 def test_pcg_paths_match_oracle(setup, torch_cuda, path, monkeypatch):
-    """The cluster-resident solver and the multi-kernel solver run the same algorithm."""
+    """The cluster-resident solvers (vectors in distributed shared memory, vectors in L2 with the
+    structure in shared memory, everything in global memory) and the multi-kernel solver run the
+    same algorithm."""
     G, O, mesh, ctx, om, oc = setup
     t = torch_cuda
-    if path == "multikernel":
-        monkeypatch.setenv("NSF_NO_CLUSTER", "1")
-    else:
-        monkeypatch.delenv("NSF_NO_CLUSTER", raising=False)
+    for k in ("NSF_NO_CLUSTER", "NSF_NO_DSMEM", "NSF_DS_NOVALS", "NSF_CLUSTER_GLOBAL"):
+        monkeypatch.delenv(k, raising=False)
+    env = {"multikernel": ["NSF_NO_CLUSTER"], "cluster-l2": ["NSF_NO_DSMEM"], "cluster-dsmem-novals": ["NSF_DS_NOVALS"],
+           "cluster-global": ["NSF_CLUSTER_GLOBAL"], "cluster-dsmem": []}[path]
+    for k in env:
+        monkeypatch.setenv(k, "1")
     for name, nch in (("Kpi", 1), ("M", 2)):
         a = ctx.matrix(name)
         rng = np.random.default_rng(11)
@@ -183,9 +188,16 @@ def test_gs_solver_matches_oracle(setup, torch_cuda):
     assert max(s.getLastMse(0), s.getLastMse(1)) < target
 
 
-def test_mixed_pcg_reaches_fp64_tolerance(setup, torch_cuda):
+@pytest.mark.parametrize("path", ["cluster-dsmem", "cluster-l2", "multikernel"])
+def test_mixed_pcg_reaches_fp64_tolerance(setup, torch_cuda, path, monkeypatch):
     G, O, mesh, ctx, om, oc = setup
     t = torch_cuda
+    for k in ("NSF_NO_CLUSTER", "NSF_NO_DSMEM"):
+        monkeypatch.delenv(k, raising=False)
+    if path == "multikernel":
+        monkeypatch.setenv("NSF_NO_CLUSTER", "1")
+    elif path == "cluster-l2":
+        monkeypatch.setenv("NSF_NO_DSMEM", "1")
     kpi = ctx.matrix("Kpi")
     rng = np.random.default_rng(8)
     b = rng.standard_normal(kpi.rows)
