@@ -1,23 +1,23 @@
-// Cluster-resident CG with the multicolor symmetric Gauss-Seidel preconditioner.
-//
-// One launch per solve: a single thread-block cluster of CS CTAs (16 where the GPU allows
-// non-portable clusters, else 8) x 1024 threads runs the whole iteration loop.  CTA k owns chunk k
-// of every color block, so x, r and q are only touched by their owner; z and p are read at
-// neighbour rows of other CTAs through L2 (ld.global.cg).
-//
-// Measured on the GB300: a cluster barrier costs 0.3 us and a dependent L2 load ~150 ns, while a
-// kernel boundary with a grid reduction costs >= 3 us.  The kernel is therefore organised for one
-// L2 round trip per color phase:
+// Persistent CG with the multicolor symmetric Gauss-Seidel preconditioner: one launch runs a whole
+// solve, the vectors stay in global memory (L2-resident), and the color phases are separated by
+// barriers of one of two kinds (the `Sync` policy):
+//   * ClusterSync: a single thread-block cluster of CS CTAs (16 where the GPU allows non-portable
+//     clusters, else 8).  A cluster barrier costs ~0.3 us on the GB300.
+//   * GridSync: a cooperative grid of one 1024-thread CTA per SM with a software grid barrier
+//     (arrival counter + generation word, bounded waits).  Slower barriers, but every SM works,
+//     which is what a large system (the velocity mass matrix) or an FP64 solve (FP64 runs at ~1/64
+//     of the FP32 rate on this GPU) needs.
+// CTA k owns chunk k of every color block, so x, r and q are only touched by their owner; z and p
+// are read at neighbour rows of other CTAs through L2 (ld.global.cg).
 //   * one thread per row; the entries of a row are processed in fixed-width predicated batches so
 //     all value loads and neighbour gathers of a row are in flight together;
 //   * when the structure of a CTA's rows (row offsets, column indices of the off-diagonal part)
 //     fits in shared memory it is copied there at kernel start (SMEM = true), else it is read from
-//     global memory (the large mass matrix);
-//   * phases end in a hardware cluster barrier; dot products are cluster reductions: each CTA writes
-//     its block sum into its own shared memory, after the barrier one warp reads the CS sums
-//     through distributed shared memory in parallel (lane r <- rank r) and adds them with a fixed
-//     shuffle tree, so all CTAs hold bit-identical scalars and take identical loop decisions (the
-//     barrier count can never diverge).  The loop is bounded by the iteration cap.
+//     global memory;
+//   * dot products are reduced in the solve precision with a fixed tree (lanes, warps, CTAs), so
+//     every CTA holds bit-identical totals; the iteration scalars (alpha, beta, the stop decisions)
+//     are computed from them once per CTA by thread 0, in FP64, and broadcast through shared memory,
+//     so every CTA takes identical loop decisions and the barrier count never diverges.
 //
 // Tolerance, cap and mode are read from the SolverState written by a preceding kernel, so the FP64
 // refinement loop can set the inner tolerance on the device.
@@ -26,6 +26,7 @@
 #include <cooperative_groups.h>
 
 #include <climits>
+#include <type_traits>
 #include <vector>
 
 #include "kernels.cuh"
@@ -34,9 +35,10 @@ namespace nsf
 {
     namespace cg = cooperative_groups;
 
-    constexpr int CTPB = 1024;                    // threads per CTA of the cluster solver
+    constexpr int CTPB = 1024;                    // threads per CTA of the persistent solvers
     constexpr size_t kClusterSmemCap = 200 * 1024; // dynamic shared memory ceiling per CTA
     constexpr int RB = 8;                          // entries per predicated batch of a row
+    constexpr unsigned kGridSpinLimit = 1u << 22;  // polls of a grid barrier before it gives up (seconds)
 
     template <typename T>
     struct ClusterPcgArgs
@@ -52,65 +54,6 @@ namespace nsf
         SolverState * st;
         const int * skip;                // refinement: stop immediately when *skip != 0
     };
-
-    // sum over the cluster of K values per thread; every thread of every CTA gets the totals
-    template <int K>
-    __device__ __forceinline__ void clusterSum(cg::cluster_group & cl, const double (&v)[K], double (*slot)[8],
-                                               int & buf, double (&out)[K])
-    {
-        __shared__ double warpPart[CTPB / 32][K];
-        __shared__ double total[K];
-        const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-#pragma unroll
-        for (int k = 0; k < K; k++)
-        {
-            double s = v[k];
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1)
-                s += __shfl_xor_sync(FULL, s, o);
-            if (lane == 0)
-                warpPart[warp][k] = s;
-        }
-        __syncthreads();
-        if (warp == 0)
-        {
-#pragma unroll
-            for (int k = 0; k < K; k++)
-            {
-                double s = warpPart[lane][k];
-#pragma unroll
-                for (int o = 16; o > 0; o >>= 1)
-                    s += __shfl_xor_sync(FULL, s, o);
-                if (lane == 0)
-                    slot[buf][k] = s;
-            }
-        }
-        cl.sync();
-        if (warp == 0)
-        {
-            const int cs = (int)cl.num_blocks();
-            double rv[K];
-            const double * remote = cl.map_shared_rank(&slot[buf][0], lane < cs ? lane : 0);
-#pragma unroll
-            for (int k = 0; k < K; k++)
-                rv[k] = lane < cs ? remote[k] : 0.0;
-#pragma unroll
-            for (int k = 0; k < K; k++)
-            {
-                double s = rv[k];
-#pragma unroll
-                for (int o = 16; o > 0; o >>= 1)
-                    s += __shfl_xor_sync(FULL, s, o);
-                if (lane == 0)
-                    total[k] = s;
-            }
-        }
-        __syncthreads();
-#pragma unroll
-        for (int k = 0; k < K; k++)
-            out[k] = total[k];
-        buf ^= 1;
-    }
 
     __device__ __forceinline__ int chunkStart(const int * ps, int c, int rank, int cs)
     {
@@ -161,8 +104,7 @@ namespace nsf
     };
 
     // acc[c] += sum over entries j of the row with col < limit:  a_j * (v0[c][col] + w * v1[c][col])
-    // (v1 may be null).  Arithmetic in T (FP32 in the inner solver: GB300's FP64 rate is ~1/64 of
-    // FP32); fixed-width predicated batches keep RB loads in flight per thread.
+    // (v1 may be null).  Arithmetic in T; fixed-width predicated batches keep RB loads in flight.
     template <typename T, int NCH, bool SMEM>
     __device__ __forceinline__ void rowGather(const RowView<SMEM> & rv, int color, int jb, int je, int limit,
                                               const T * vO, int n, const T * v0, const T * v1, const T * w,
@@ -200,19 +142,215 @@ namespace nsf
         }
     }
 
-    template <typename T, int NCH, bool SMEM>
-    __global__ void __launch_bounds__(CTPB, 1) kPcgCluster(ClusterPcgArgs<T> A)
+    // K per-thread values summed over the CTA in a fixed order; the result is valid in every lane of
+    // warp 0.
+    template <typename T, int K>
+    __device__ __forceinline__ void blockSum(const T (&v)[K], T (&out)[K])
+    {
+        __shared__ T warpPart[CTPB / 32][K];
+        const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+#pragma unroll
+        for (int k = 0; k < K; k++)
+        {
+            T s = v[k];
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1)
+                s += __shfl_xor_sync(FULL, s, o);
+            if (lane == 0)
+                warpPart[warp][k] = s;
+        }
+        __syncthreads();
+        if (warp == 0)
+        {
+#pragma unroll
+            for (int k = 0; k < K; k++)
+            {
+                T s = warpPart[lane][k];
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1)
+                    s += __shfl_xor_sync(FULL, s, o);
+                out[k] = s;
+            }
+        }
+    }
+
+    // One thread-block cluster: hardware cluster barriers; reductions through distributed shared
+    // memory (each CTA publishes its block sums in its own shared memory, one warp of every CTA reads
+    // all of them after the barrier, lane r <- rank r).
+    template <typename T>
+    struct ClusterSync
+    {
+        T (*slot)[8] = nullptr; // two alternating 8-value buffers in the CTA's shared memory
+        int buf = 0;
+        __device__ __forceinline__ int rank() const { return (int)cg::this_cluster().block_rank(); }
+        __device__ __forceinline__ int size() const { return (int)cg::this_cluster().num_blocks(); }
+        __device__ __forceinline__ void sync() { cg::this_cluster().sync(); }
+        __device__ __forceinline__ bool failed() const { return false; }
+
+        // sum over the cluster of K per-thread values; thread 0 of every CTA runs epi(totals), then
+        // the CTA synchronises
+        template <int K, typename Epi>
+        __device__ __forceinline__ void reduce(const T (&v)[K], Epi && epi)
+        {
+            cg::cluster_group cl = cg::this_cluster();
+            T part[K];
+            blockSum<T, K>(v, part);
+            const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+            if (warp == 0 && lane == 0)
+#pragma unroll
+                for (int k = 0; k < K; k++)
+                    slot[buf][k] = part[k];
+            cl.sync();
+            if (warp == 0)
+            {
+                const int cs = (int)cl.num_blocks();
+                const T * remote = cl.map_shared_rank(&slot[buf][0], lane < cs ? lane : 0);
+                T tot[K];
+#pragma unroll
+                for (int k = 0; k < K; k++)
+                {
+                    T s = lane < cs ? remote[k] : (T)0;
+#pragma unroll
+                    for (int o = 16; o > 0; o >>= 1)
+                        s += __shfl_xor_sync(FULL, s, o);
+                    tot[k] = s;
+                }
+                if (lane == 0)
+                    epi(tot);
+            }
+            __syncthreads();
+            buf ^= 1;
+        }
+
+        // no CTA may leave while another can still read its shared memory
+        __device__ __forceinline__ void finish() { cg::this_cluster().sync(); }
+    };
+
+    __device__ __forceinline__ unsigned ldAcquireGpu(const unsigned * p)
+    {
+        unsigned v;
+        asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+        return v;
+    }
+
+    __device__ __forceinline__ void stReleaseGpu(unsigned * p, unsigned v)
+    {
+        asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+    }
+
+    __device__ __forceinline__ unsigned atomAddAcqRelGpu(unsigned * p, unsigned v)
+    {
+        unsigned old;
+        asm volatile("atom.acq_rel.gpu.global.add.u32 %0, [%1], %2;" : "=r"(old) : "l"(p), "r"(v) : "memory");
+        return old;
+    }
+
+    // A cooperative grid (every CTA co-resident): software grid barrier and reductions through
+    // global per-CTA slots.  ctl[0] = arrivals, ctl[1] = generation, ctl[2] = abort flag; all zero
+    // before the launch.  A wait that polls kGridSpinLimit times without the generation moving sets
+    // the abort flag; from then on every barrier returns at once, so the kernel ends (with a
+    // failure status) instead of hanging.
+    template <typename T>
+    struct GridSync
+    {
+        unsigned * ctl = nullptr;
+        T * slots = nullptr; // 2 buffers x 8 values x gridDim.x
+        int buf = 0;
+        __device__ __forceinline__ int rank() const { return (int)blockIdx.x; }
+        __device__ __forceinline__ int size() const { return (int)gridDim.x; }
+        __device__ __forceinline__ bool failed() const { return *(volatile unsigned *)(ctl + 2) != 0u; }
+
+        // The CTA barrier orders every thread's writes before thread 0's arrival, whose release
+        // (cumulative) publishes them at GPU scope; the acquire that observes the new generation,
+        // followed by the CTA barrier, orders the other CTAs' writes before this CTA's later reads.
+        __device__ __forceinline__ void sync()
+        {
+            __syncthreads();
+            if (threadIdx.x == 0 && !failed())
+            {
+                const unsigned gen = ldAcquireGpu(ctl + 1); // read before arriving
+                const unsigned prev = atomAddAcqRelGpu(ctl, 1u);
+                if (prev == gridDim.x - 1)
+                {
+                    atomicExch(ctl, 0u);
+                    stReleaseGpu(ctl + 1, gen + 1);
+                }
+                else
+                {
+                    unsigned polls = 0;
+                    while (ldAcquireGpu(ctl + 1) == gen)
+                    {
+                        if (++polls > kGridSpinLimit || failed())
+                        {
+                            atomicExch(ctl + 2, 1u);
+                            break;
+                        }
+                    }
+                }
+            }
+            __syncthreads();
+        }
+
+        template <int K, typename Epi>
+        __device__ __forceinline__ void reduce(const T (&v)[K], Epi && epi)
+        {
+            T part[K];
+            blockSum<T, K>(v, part);
+            const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+            const int G = (int)gridDim.x;
+            T * sl = slots + (size_t)buf * 8 * G;
+            if (warp == 0 && lane == 0)
+#pragma unroll
+                for (int k = 0; k < K; k++)
+                    sl[k * G + blockIdx.x] = part[k];
+            sync();
+            if (warp == 0)
+            {
+                T tot[K];
+#pragma unroll
+                for (int k = 0; k < K; k++)
+                {
+                    T s = 0;
+                    for (int i = lane; i < G; i += 32)
+                        s += __ldcg(sl + k * G + i);
+#pragma unroll
+                    for (int o = 16; o > 0; o >>= 1)
+                        s += __shfl_xor_sync(FULL, s, o);
+                    tot[k] = s;
+                }
+                if (lane == 0)
+                    epi(tot);
+            }
+            __syncthreads();
+            buf ^= 1;
+        }
+
+        __device__ __forceinline__ void finish() {}
+    };
+
+    // Iteration scalars of a persistent solve, kept by thread 0 of every CTA (all CTAs compute the
+    // same values from the same totals) and read by the other threads after a CTA barrier.
+    template <typename T, int NCH>
+    struct SweepScalars
+    {
+        T alpha[NCH], beta[NCH];
+        int act[NCH], status[NCH], iters[NCH], any;
+        double bb[NCH], rr[NCH], rz[NCH], rzPrev[NCH];
+    };
+
+    template <typename T, int NCH, bool SMEM, typename Sync>
+    __global__ void __launch_bounds__(CTPB, 1) kPcgSweep(ClusterPcgArgs<T> A, Sync S)
     {
         extern __shared__ int smemI[];
-        cg::cluster_group cl = cg::this_cluster();
-        const int rank = (int)cl.block_rank(), cs = (int)cl.num_blocks();
-        __shared__ double slot[2][8];
+        __shared__ T slotS[2][8];
         __shared__ int chunkA[MAXCOLORS], chunkL[MAXCOLORS + 1], chunkG[MAXCOLORS], nzBase[MAXCOLORS + 1];
-        int buf = 0;
+        __shared__ SweepScalars<T, NCH> sc;
+        if constexpr (std::is_same<Sync, ClusterSync<T>>::value)
+            S.slot = slotS;
+        const int rank = S.rank(), cs = S.size();
         SolverState * st = A.st;
-        const int n = A.n, C = A.nColors;
-        const int maxIters = st->maxIters, absMode = st->absMode;
-        const double tol2 = st->tol2;
+        const int n = A.n, C = A.nColors, numCh = A.numCh;
+        const int maxIters = st->maxIters;
         if (A.skip && *A.skip)
         {
             if (rank == 0 && threadIdx.x == 0)
@@ -276,15 +414,19 @@ namespace nsf
         }
 
         bool act[NCH];
+        T alpha[NCH];
 #pragma unroll
         for (int c = 0; c < NCH; c++)
-            act[c] = c < A.numCh;
+        {
+            act[c] = c < numCh;
+            alpha[c] = (T)0;
+        }
 
-        // ---- r = b - A x over own rows; ||b||^2 (dot products accumulate in FP64)
-        double bb[NCH];
+        // ---- r = b - A x over own rows; ||b||^2
+        T bbP[NCH];
 #pragma unroll
         for (int c = 0; c < NCH; c++)
-            bb[c] = 0;
+            bbP[c] = (T)0;
         for (int col = 0; col < C; col++)
             for (int l = chunkL[col] + threadIdx.x; l < chunkL[col + 1]; l += CTPB)
             {
@@ -302,19 +444,15 @@ namespace nsf
                     {
                         const T bi = A.b[(size_t)c * n + i];
                         A.r[(size_t)c * n + i] = bi - acc[c];
-                        bb[c] += (double)(bi * bi);
+                        bbP[c] += bi * bi;
                     }
             }
 
-        T alphaT[NCH];
-#pragma unroll
-        for (int c = 0; c < NCH; c++)
-            alphaT[c] = 0;
-        // z = SGS(r); init: no x/r update.  Forward phases use earlier colors only (limit).
-        auto sgs = [&](bool init, const T * pcur, double (&rr)[NCH], double (&rz)[NCH]) {
+        // z = SGS(r) from z = 0.  init: no x / r update.  Forward phases use earlier colors only.
+        auto sgs = [&](bool init, const T * pcur, T (&rr)[NCH], T (&rz)[NCH]) {
 #pragma unroll
             for (int c = 0; c < NCH; c++)
-                rr[c] = rz[c] = 0;
+                rr[c] = rz[c] = (T)0;
             for (int col = 0; col < C; col++)
             {
                 const int r0 = A.ps[col];
@@ -325,18 +463,21 @@ namespace nsf
                     T ri[NCH];
 #pragma unroll
                     for (int c = 0; c < NCH; c++)
+                    {
+                        ri[c] = (T)0;
                         if (act[c])
                         {
                             const size_t o = (size_t)c * n + i;
                             T rvv = A.r[o];
                             if (!init)
                             {
-                                A.x[o] = A.x[o] + alphaT[c] * pcur[o];
-                                rvv -= alphaT[c] * A.q[o];
+                                A.x[o] = A.x[o] + alpha[c] * pcur[o];
+                                rvv -= alpha[c] * A.q[o];
                                 A.r[o] = rvv;
                             }
                             ri[c] = rvv;
                         }
+                    }
                     T acc[NCH];
 #pragma unroll
                     for (int c = 0; c < NCH; c++)
@@ -349,13 +490,13 @@ namespace nsf
                         {
                             const T zi = (ri[c] - acc[c]) * id;
                             A.z[(size_t)c * n + i] = zi;
-                            rr[c] += (double)(ri[c] * ri[c]);
+                            rr[c] += ri[c] * ri[c];
                             if (col == C - 1)
-                                rz[c] += (double)(ri[c] * zi);
+                                rz[c] += ri[c] * zi;
                         }
                 }
                 if (C > 1)
-                    cl.sync(); // z of this color visible to the cluster
+                    S.sync(); // z of this color visible to every CTA
             }
             for (int col = C - 2; col >= 0; col--)
             {
@@ -377,60 +518,65 @@ namespace nsf
                             const T rvv = A.r[o];
                             const T zi = (rvv - acc[c]) * id;
                             A.z[o] = zi;
-                            rz[c] += (double)(rvv * zi);
+                            rz[c] += rvv * zi;
                         }
                 }
                 if (col > 0)
-                    cl.sync(); // the last phase's barrier is the reduction's
+                    S.sync(); // the last phase's barrier is the reduction's
             }
         };
 
-        double rr[NCH], rz[NCH], rzPrev[NCH];
-        sgs(true, A.p, rr, rz);
-        double red[3 * NCH], tot[3 * NCH];
+        T rr0[NCH], rz0[NCH];
+        sgs(true, A.p, rr0, rz0);
+        T red[3 * NCH];
 #pragma unroll
         for (int c = 0; c < NCH; c++)
         {
-            red[c] = bb[c];
-            red[NCH + c] = rr[c];
-            red[2 * NCH + c] = rz[c];
+            red[c] = bbP[c];
+            red[NCH + c] = rr0[c];
+            red[2 * NCH + c] = rz0[c];
         }
-        clusterSum<3 * NCH>(cl, red, slot, buf, tot);
-        double bbT[NCH], rrT[NCH], rzT[NCH];
-        int status[NCH], iters[NCH];
+        const int absMode = st->absMode;
+        const double tol2 = st->tol2;
+        // scalar decisions: thread 0 of each CTA, FP64 (identical in every CTA)
+        S.template reduce<3 * NCH>(red, [&](const T (&tot)[3 * NCH]) {
+            int any = 0;
+            for (int c = 0; c < NCH; c++)
+            {
+                const double bb = (double)tot[c], rr = (double)tot[NCH + c], rz = (double)tot[2 * NCH + c];
+                sc.bb[c] = bb;
+                sc.rr[c] = rr;
+                sc.rz[c] = rz;
+                sc.rzPrev[c] = rz;
+                const bool fin = isfinite(rr) && isfinite(bb);
+                const bool conv = absMode ? (rr < tol2) : (rr <= tol2 * bb);
+                sc.status[c] = fin ? 0 : 2;
+                sc.iters[c] = 0;
+                sc.act[c] = (c < numCh) && fin && !conv;
+                sc.alpha[c] = (T)0;
+                sc.beta[c] = (T)0;
+                any |= sc.act[c];
+            }
+            sc.any = any;
+        });
 #pragma unroll
         for (int c = 0; c < NCH; c++)
-        {
-            bbT[c] = tot[c];
-            rrT[c] = tot[NCH + c];
-            rzT[c] = tot[2 * NCH + c];
-            rzPrev[c] = rzT[c];
-            const bool fin = isfinite(rrT[c]) && isfinite(bbT[c]);
-            const bool conv = absMode ? (rrT[c] < tol2) : (rrT[c] <= tol2 * bbT[c]);
-            status[c] = fin ? 0 : 2;
-            iters[c] = 0;
-            act[c] = act[c] && fin && !conv;
-        }
+            act[c] = sc.act[c] != 0;
 
         int k = 1;
         for (; k <= maxIters; k++)
         {
-            bool any = false;
-#pragma unroll
-            for (int c = 0; c < NCH; c++)
-                any |= act[c];
-            if (!any)
-                break;
+            if (!sc.any)
+                break; // same value in every CTA
             // direction: p_new = z + beta p_old ; q = A p_new ; p.q   (own rows of every color)
             const T * pold = A.p + (size_t)((k - 1) & 1) * NCH * n;
             T * pnew = A.p + (size_t)(k & 1) * NCH * n;
-            T betaT[NCH];
-            double pq[NCH];
+            T beta[NCH], pq[NCH];
 #pragma unroll
             for (int c = 0; c < NCH; c++)
             {
-                betaT[c] = (k == 1) ? (T)0 : (T)(rzT[c] / rzPrev[c]);
-                pq[c] = 0;
+                beta[c] = sc.beta[c];
+                pq[c] = (T)0;
             }
             for (int col = 0; col < C; col++)
                 for (int l = chunkL[col] + threadIdx.x; l < chunkL[col + 1]; l += CTPB)
@@ -442,11 +588,11 @@ namespace nsf
                     for (int c = 0; c < NCH; c++)
                     {
                         const size_t o = (size_t)c * n + i;
-                        pn[c] = act[c] ? (k == 1 ? A.z[o] : A.z[o] + betaT[c] * pold[o]) : (T)0;
+                        pn[c] = act[c] ? (k == 1 ? A.z[o] : A.z[o] + beta[c] * pold[o]) : (T)0;
                         acc[c] = d * pn[c];
                     }
                     rowGather<T, NCH, SMEM>(rv, col, rv.begin(col, l), rv.end(col, l), INT_MAX, A.vO, n, A.z,
-                                            k == 1 ? (const T *)nullptr : pold, betaT, act, acc);
+                                            k == 1 ? (const T *)nullptr : pold, beta, act, acc);
 #pragma unroll
                     for (int c = 0; c < NCH; c++)
                         if (act[c])
@@ -454,71 +600,89 @@ namespace nsf
                             const size_t o = (size_t)c * n + i;
                             pnew[o] = pn[c];
                             A.q[o] = acc[c];
-                            pq[c] += (double)(pn[c] * acc[c]);
+                            pq[c] += pn[c] * acc[c];
                         }
                 }
-            double pqT[NCH];
-            clusterSum<NCH>(cl, pq, slot, buf, pqT);
+            S.template reduce<NCH>(pq, [&](const T (&tot)[NCH]) {
+                for (int c = 0; c < NCH; c++)
+                {
+                    const double pqc = (double)tot[c];
+                    sc.rzPrev[c] = sc.rz[c]; // defines this alpha; the previous r.z of the next beta
+                    sc.alpha[c] = (T)(sc.rz[c] / pqc);
+                    if (sc.act[c] && !(pqc > 0))
+                    {
+                        sc.status[c] = isfinite(pqc) ? 4 : 2;
+                        sc.iters[c] = k - 1;
+                        sc.act[c] = 0;
+                    }
+                }
+            });
 #pragma unroll
             for (int c = 0; c < NCH; c++)
             {
-                rzPrev[c] = rzT[c]; // defines this alpha; the previous r.z of the next beta
-                alphaT[c] = (T)(rzT[c] / pqT[c]);
-                if (act[c] && !(pqT[c] > 0))
-                {
-                    status[c] = isfinite(pqT[c]) ? 4 : 2;
-                    iters[c] = k - 1;
-                    act[c] = false;
-                }
+                alpha[c] = sc.alpha[c];
+                act[c] = sc.act[c] != 0;
             }
-            double rrN[NCH], rzN[NCH];
+            T rrN[NCH], rzN[NCH];
             sgs(false, pnew, rrN, rzN);
-            double red2[2 * NCH], tot2[2 * NCH];
+            T red2[2 * NCH];
 #pragma unroll
             for (int c = 0; c < NCH; c++)
             {
                 red2[c] = rrN[c];
                 red2[NCH + c] = rzN[c];
             }
-            clusterSum<2 * NCH>(cl, red2, slot, buf, tot2);
+            S.template reduce<2 * NCH>(red2, [&](const T (&tot)[2 * NCH]) {
+                int any = 0;
+                for (int c = 0; c < NCH; c++)
+                {
+                    if (sc.act[c])
+                    {
+                        const double rr = (double)tot[c], rz = (double)tot[NCH + c];
+                        sc.rr[c] = rr;
+                        sc.rz[c] = rz;
+                        const bool fin = isfinite(rr) && isfinite(rz);
+                        const bool conv = absMode ? (rr < tol2) : (rr <= tol2 * sc.bb[c]);
+                        if (!fin || conv)
+                        {
+                            sc.act[c] = 0;
+                            sc.iters[c] = k;
+                            sc.status[c] = fin ? 0 : 2;
+                        }
+                        else
+                            sc.beta[c] = (T)(rz / sc.rzPrev[c]);
+                    }
+                    any |= sc.act[c];
+                }
+                sc.any = any && !S.failed();
+            });
 #pragma unroll
             for (int c = 0; c < NCH; c++)
-            {
-                if (!act[c])
-                    continue;
-                rrT[c] = tot2[c];
-                rzT[c] = tot2[NCH + c];
-                const bool fin = isfinite(rrT[c]) && isfinite(rzT[c]);
-                const bool conv = absMode ? (rrT[c] < tol2) : (rrT[c] <= tol2 * bbT[c]);
-                if (!fin || conv)
-                {
-                    act[c] = false;
-                    iters[c] = k;
-                    status[c] = fin ? 0 : 2;
-                }
-            }
+                act[c] = sc.act[c] != 0;
         }
         // results (rank 0 writes; every CTA holds identical values)
         if (rank == 0 && threadIdx.x == 0)
         {
+            const bool failed = S.failed();
             for (int c = 0; c < NCH; c++)
             {
-                if (act[c])
+                if (sc.act[c])
                 {
-                    status[c] = 3;
-                    iters[c] = maxIters;
+                    sc.status[c] = 3;
+                    sc.iters[c] = maxIters;
                 }
-                st->status[c] = c < A.numCh ? status[c] : 0;
-                st->iters[c] = iters[c];
-                st->bb[c] = bbT[c];
-                st->lastRR[c] = rrT[c];
+                if (failed && c < numCh)
+                    sc.status[c] = 5; // a grid barrier gave up waiting: results are not valid
+                st->status[c] = c < numCh ? sc.status[c] : 0;
+                st->iters[c] = sc.iters[c];
+                st->bb[c] = sc.bb[c];
+                st->lastRR[c] = sc.rr[c];
                 st->active[c] = 0;
             }
             st->iter = k;
             st->anyActive = 0;
         }
-        // no CTA may leave while another can still read its shared memory
-        cl.sync();
+        S.finish();
     }
 
     // Largest cluster (16, else 8, else 0 = unavailable) the device can co-schedule for kernel k
@@ -560,5 +724,29 @@ namespace nsf
             cudaGetLastError();
         }
         return 0;
+    }
+
+    // Whether a cooperative grid of one CTA per SM with `smem` bytes of dynamic shared memory can be
+    // co-resident (1 = yes).  Sets the kernel's dynamic shared memory ceiling to kClusterSmemCap.
+    template <typename K>
+    inline bool gridFits(K kernel, size_t smem)
+    {
+        int dev = 0, coop = 0;
+        if (cudaGetDevice(&dev) != cudaSuccess ||
+            cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev) != cudaSuccess || !coop ||
+            smem > kClusterSmemCap ||
+            cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kClusterSmemCap) !=
+                cudaSuccess)
+        {
+            cudaGetLastError();
+            return false;
+        }
+        int nb = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kernel, CTPB, smem) != cudaSuccess)
+        {
+            cudaGetLastError();
+            return false;
+        }
+        return nb >= 1;
     }
 } // namespace nsf

@@ -188,8 +188,8 @@ namespace nsf
 #define NSF_LAUNCH(kernel, grid, stream, ...) ::nsf::launchKernel(#kernel, kernel, (grid), (stream), __VA_ARGS__)
 
     // launch a one-cluster kernel: cs CTAs of 1024 threads forming one thread-block cluster
-    template <typename Arg>
-    inline void launchCluster(void (*k)(Arg), int cs, size_t smem, cudaStream_t s, const Arg & a)
+    template <typename... KArgs, typename... Args>
+    inline void launchCluster(void (*k)(KArgs...), int cs, size_t smem, cudaStream_t s, const Args &... a)
     {
         cudaLaunchConfig_t cfg = {};
         cfg.gridDim = dim3(cs);
@@ -203,7 +203,25 @@ namespace nsf
         at[0].val.clusterDim.z = 1;
         cfg.attrs = at;
         cfg.numAttrs = 1;
-        cudaCheck(cudaLaunchKernelEx(&cfg, k, a), "cluster launch");
+        cudaCheck(cudaLaunchKernelEx(&cfg, k, a...), "cluster launch");
+        launchCounter().fetch_add(1, std::memory_order_relaxed);
+    }
+
+    // launch a cooperative grid of `blocks` CTAs of 1024 threads, all co-resident
+    template <typename... KArgs, typename... Args>
+    inline void launchCooperative(void (*k)(KArgs...), int blocks, size_t smem, cudaStream_t s, const Args &... a)
+    {
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3(blocks);
+        cfg.blockDim = dim3(1024);
+        cfg.dynamicSmemBytes = smem;
+        cfg.stream = s;
+        cudaLaunchAttribute at[1];
+        at[0].id = cudaLaunchAttributeCooperative;
+        at[0].val.cooperative = 1;
+        cfg.attrs = at;
+        cfg.numAttrs = 1;
+        cudaCheck(cudaLaunchKernelEx(&cfg, k, a...), "cooperative launch");
         launchCounter().fetch_add(1, std::memory_order_relaxed);
     }
 
@@ -211,6 +229,12 @@ namespace nsf
     {
         const char * v = std::getenv(name);
         return (v && *v && *v != '0') ? 1 : 0;
+    }
+
+    inline std::string envStr(const char * name, const char * dflt)
+    {
+        const char * v = std::getenv(name);
+        return (v && *v) ? std::string(v) : std::string(dflt);
     }
 
 // dispatch a lanes-per-row value to a template parameter

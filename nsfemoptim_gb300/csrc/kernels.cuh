@@ -419,6 +419,8 @@ namespace nsf
                                                      const T * __restrict__ v, const T * __restrict__ x,
                                                      const T * __restrict__ b, T * __restrict__ r)
     {
+        if (P.skip && *P.skip)
+            return; // refinement finished: the whole solve is a no-op (same in every block)
         Group<L> g;
         T bb[NCH];
 #pragma unroll
@@ -625,6 +627,8 @@ namespace nsf
                                                         T * __restrict__ r, T * __restrict__ z,
                                                         const T * __restrict__ pbuf, const T * __restrict__ q)
     {
+        if (P.skip && *P.skip)
+            return;
         SolverState * st = P.st;
         bool act[NCH];
         T alphaT[NCH];
@@ -719,6 +723,8 @@ namespace nsf
                                                          const T * __restrict__ invD, const T * __restrict__ r,
                                                          T * __restrict__ z)
     {
+        if (P.skip && *P.skip)
+            return;
         SolverState * st = P.st;
         bool act[NCH];
 #pragma unroll

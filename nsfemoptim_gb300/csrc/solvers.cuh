@@ -138,23 +138,38 @@ namespace nsf
         DevBuf<SolverState> st;
         PcgPtrs P{};
         PinnedBuf<int> flag{1};
-        // cluster-resident variant (one launch per solve); 0 = multi-kernel path.  Used when the
-        // structure of a CTA's rows fits in shared memory (the pressure system); large systems
-        // (the mass matrix) keep the multi-kernel path, which spreads over every SM
-        // (NSF_CLUSTER_GLOBAL=1 forces the cluster variant that reads the structure from global memory).
-        int clusterSize = 0;
-        bool clusterShared = false; // row structure cached in shared memory
+        // How a solve runs (one persistent launch per solve except MULTI):
+        //   DSMEM   one thread-block cluster, every vector in distributed shared memory (a CTA's
+        //           share of the vectors and of the row structure fits: the pressure system);
+        //   GRID    a cooperative grid of one CTA per SM, vectors in L2, grid barriers (large
+        //           systems: the velocity mass matrix, FP64 solves);
+        //   CLUSTER one thread-block cluster, vectors in L2;
+        //   MULTI   one kernel per color phase (no co-residency requirement).
+        // Chosen automatically in that order of preference (DSMEM, GRID, MULTI); NSF_PCG_PATH =
+        // dsmem | dsmem-novals | grid | grid-global | cluster | cluster-global | multikernel forces
+        // one (falling back to MULTI when it cannot run).
+        enum Path
+        {
+            MULTI = 0,
+            DSMEM = 1,
+            GRID = 2,
+            CLUSTER = 3
+        };
+        int path = MULTI;
+        int clusterSize = 0;        // CTAs of the cluster (DSMEM, CLUSTER) or of the grid (GRID)
+        bool clusterShared = false; // CLUSTER / GRID: row structure cached in shared memory
         size_t clusterSmem = 0;
         DevBuf<int> psDev;
-        // cluster variant with every vector in distributed shared memory (preferred when a CTA's
-        // share fits): -1 unused, 0 matrix values read from global memory, 1 values in shared memory
+        // DSMEM: 0 matrix values read from global memory, 1 values in shared memory
         int dsVals = -1;
         DsLayout dsLay{};
         DevBuf<int> cmapDev;
+        // GRID: barrier control words and the per-CTA reduction slots
+        DevBuf<unsigned> gridCtl;
+        DevBuf<T> gridSlots;
 
-        bool setupDsmem(const SweepSystem<T> * s)
+        bool setupDsmem(const SweepSystem<T> * s, bool allowVals)
         {
-            const bool allowVals = envFlag("NSF_DS_NOVALS") == 0;
             for (int cs : {16, 8})
             {
                 DsShares D = dsShares(s->ps, s->hostRsO, s->hostCiO, cs);
@@ -187,42 +202,77 @@ namespace nsf
             return m;
         }
 
-        void setup(const SweepSystem<T> * s, int channels, bool tryCluster = true)
+        bool setupCluster(const SweepSystem<T> * s, bool shared)
+        {
+            if (shared)
+            {
+                const size_t s16 = smemFor(s, 16), s8 = smemFor(s, 8);
+                clusterSize = pickClusterSize(kPcgSweep<T, NCH, true, ClusterSync<T>>, s16, s8);
+                clusterShared = clusterSize > 0;
+                clusterSmem = clusterSize == 16 ? s16 : (clusterSize == 8 ? s8 : 0);
+            }
+            else
+                clusterSize = pickClusterSize(kPcgSweep<T, NCH, false, ClusterSync<T>>, 0, 0);
+            return clusterSize > 0;
+        }
+
+        bool setupGrid(const SweepSystem<T> * s, bool allowShared)
+        {
+            // one CTA per SM (NSF_GRID_CTAS overrides, at most one per SM)
+            int G = smCount();
+            const int want = std::atoi(envStr("NSF_GRID_CTAS", "0").c_str());
+            if (want > 0 && want < G)
+                G = want;
+            const size_t sm = smemFor(s, G);
+            if (allowShared && gridFits(kPcgSweep<T, NCH, true, GridSync<T>>, sm))
+            {
+                clusterShared = true;
+                clusterSmem = sm;
+            }
+            else if (gridFits(kPcgSweep<T, NCH, false, GridSync<T>>, 0))
+            {
+                clusterShared = false;
+                clusterSmem = 0;
+            }
+            else
+                return false;
+            clusterSize = G;
+            gridCtl.alloc(4);
+            gridSlots.alloc((size_t)2 * 8 * G);
+            return true;
+        }
+
+        void setup(const SweepSystem<T> * s, int channels, bool tryPersistent = true)
         {
             sys = s;
             numCh = channels;
             const int n = s->n;
             psDev.upload(s->ps);
+            path = MULTI;
             clusterSize = 0;
             clusterShared = false;
             clusterSmem = 0;
             dsVals = -1;
-            // FP64 arithmetic is scarce on GB300 (~2 DFMA/clock/SM): a large FP64 system keeps the
-            // multi-kernel path that spreads its FMAs over every SM; FP32 solves and small systems
-            // run cluster-resident.
-            const bool fp64Heavy = sizeof(T) == 8 && (size_t)s->nnzFull * NCH > 1000000;
-            if (tryCluster && !fp64Heavy && envFlag("NSF_NO_CLUSTER") == 0)
+            const std::string want = envStr("NSF_PCG_PATH", "auto");
+            if (tryPersistent && want != "multikernel")
             {
-                const size_t s16 = smemFor(s, 16), s8 = smemFor(s, 8);
-                if (envFlag("NSF_CLUSTER_GLOBAL") == 0 && envFlag("NSF_NO_DSMEM") == 0 && setupDsmem(s))
+                const bool any = want == "auto";
+                if ((any || want == "dsmem" || want == "dsmem-novals") && setupDsmem(s, want != "dsmem-novals"))
+                    path = DSMEM;
+                else if ((want == "cluster" || want == "cluster-global") && setupCluster(s, want == "cluster"))
+                    path = CLUSTER;
+                else if ((any || want == "grid" || want == "grid-global") && setupGrid(s, want != "grid-global"))
+                    path = GRID;
+                if (path == MULTI)
                 {
-                    // vectors in distributed shared memory
+                    clusterSize = 0;
+                    clusterShared = false;
+                    clusterSmem = 0;
                 }
-                else if (envFlag("NSF_CLUSTER_GLOBAL") == 0)
-                {
-                    clusterSize = pickClusterSize(kPcgCluster<T, NCH, true>, s16, s8);
-                    if (clusterSize > 0)
-                    {
-                        clusterShared = true;
-                        clusterSmem = clusterSize == 16 ? s16 : s8;
-                    }
-                }
-                else // structure read from global memory (a large system on 16 SMs: slower than multi-kernel)
-                    clusterSize = pickClusterSize(kPcgCluster<T, NCH, false>, 0, 0);
             }
             if (envFlag("NSF_VERBOSE"))
-                std::fprintf(stderr, "[nsf] PCG n=%d colors=%d cluster=%d shared=%d dsmem=%d smem=%zu\n", n,
-                             s->nColors, clusterSize, (int)clusterShared, dsVals, clusterSmem);
+                std::fprintf(stderr, "[nsf] PCG n=%d nnz=%d colors=%d path=%d ctas=%d shared=%d dsvals=%d smem=%zu\n",
+                             n, s->nnzFull, s->nColors, path, clusterSize, (int)clusterShared, dsVals, clusterSmem);
             r.alloc((size_t)NCH * n);
             z.alloc((size_t)NCH * n);
             p.alloc((size_t)2 * NCH * n);
@@ -263,7 +313,7 @@ namespace nsf
             if (setConfig)
                 NSF_LAUNCH(kSetConfig, 1, s, st.get(), maxIters, absolute ? 1 : 0,
                            absolute ? tol * tol * (double)S.n : tol * tol);
-            if (dsVals >= 0)
+            if (path == DSMEM)
             {
                 DsPcgArgs<T> A{S.n,         S.nColors,    numCh,   psDev.get(), S.rsO.get(), S.ciO.get(),
                                S.vO.get(),  cmapDev.get(), S.diag.get(), S.invD.get(), b,    x,
@@ -274,15 +324,30 @@ namespace nsf
                     launchCluster(kPcgClusterDs<T, NCH, false>, clusterSize, dsLay.bytes, s, A);
                 return;
             }
-            if (clusterSize > 0)
+            if (path == CLUSTER || path == GRID)
             {
                 ClusterPcgArgs<T> A{S.n, S.nColors, numCh, psDev.get(), S.rsO.get(), S.ciO.get(), S.vO.get(),
                                     S.diag.get(), S.invD.get(), b, x, r.get(), z.get(), p.get(), q.get(), st.get(),
                                     P.skip};
+                if (path == CLUSTER)
+                {
+                    const ClusterSync<T> cs{};
+                    if (clusterShared)
+                        launchCluster(kPcgSweep<T, NCH, true, ClusterSync<T>>, clusterSize, clusterSmem, s, A, cs);
+                    else
+                        launchCluster(kPcgSweep<T, NCH, false, ClusterSync<T>>, clusterSize, 0, s, A, cs);
+                    return;
+                }
+                // barrier words start at zero for every solve (a solve that gave up waiting leaves
+                // them in an unknown state)
+                NSF_CUDA(cudaMemsetAsync(gridCtl.get(), 0, 4 * sizeof(unsigned), s));
+                GridSync<T> gs{};
+                gs.ctl = gridCtl.get();
+                gs.slots = gridSlots.get();
                 if (clusterShared)
-                    launchCluster(kPcgCluster<T, NCH, true>, clusterSize, clusterSmem, s, A);
+                    launchCooperative(kPcgSweep<T, NCH, true, GridSync<T>>, clusterSize, clusterSmem, s, A, gs);
                 else
-                    launchCluster(kPcgCluster<T, NCH, false>, clusterSize, 0, s, A);
+                    launchCooperative(kPcgSweep<T, NCH, false, GridSync<T>>, clusterSize, 0, s, A, gs);
                 return;
             }
             NSF_LANES(S.L, NSF_LAUNCH((kPcgInit<T, LL, NCH>), S.fullBlocks(), s, P, S.rsF.get(), S.ciF.get(),

@@ -117,25 +117,39 @@ def test_pcg_pressure_matches_oracle(setup, torch_cuda):
     assert np.linalg.norm(r) <= 1.01e-10 * np.linalg.norm(b)
 
 
-@pytest.mark.parametrize("path", ["cluster-dsmem", "cluster-dsmem-novals", "cluster-l2", "cluster-global",
-                                  "multikernel"])
-def test_pcg_paths_match_oracle(setup, torch_cuda, path, monkeypatch):
-    """The cluster-resident solvers (vectors in distributed shared memory, vectors in L2 with the
-    structure in shared memory, everything in global memory) and the multi-kernel solver run the
-    same algorithm."""
+PATH_CODES = {"dsmem": 1, "dsmem-novals": 1, "grid": 2, "grid-global": 2, "cluster": 3, "cluster-global": 3,
+              "multikernel": 0}
+
+
+def _force_path(monkeypatch, path):
+    monkeypatch.setenv("NSF_PCG_PATH", path)
+    monkeypatch.setenv("NSF_VERBOSE", "1")
+
+
+def _check_path(capfd, path):
+    """The first solver created since the last check ran on the forced path."""
+    err = capfd.readouterr().err
+    lines = [ln for ln in err.splitlines() if ln.startswith("[nsf] PCG")]
+    assert lines, err
+    assert f"path={PATH_CODES[path]} " in lines[0], lines
+
+
+@pytest.mark.parametrize("path", list(PATH_CODES))
+def test_pcg_paths_match_oracle(setup, torch_cuda, path, monkeypatch, capfd):
+    """Every way a solve can run -- one cluster with the vectors in distributed shared memory (matrix
+    values cached or not), a cooperative grid (structure cached or not), one cluster with the
+    vectors in L2 (structure cached or not), one kernel per color phase -- runs the same algorithm."""
     G, O, mesh, ctx, om, oc = setup
     t = torch_cuda
-    for k in ("NSF_NO_CLUSTER", "NSF_NO_DSMEM", "NSF_DS_NOVALS", "NSF_CLUSTER_GLOBAL"):
-        monkeypatch.delenv(k, raising=False)
-    env = {"multikernel": ["NSF_NO_CLUSTER"], "cluster-l2": ["NSF_NO_DSMEM"], "cluster-dsmem-novals": ["NSF_DS_NOVALS"],
-           "cluster-global": ["NSF_CLUSTER_GLOBAL"], "cluster-dsmem": []}[path]
-    for k in env:
-        monkeypatch.setenv(k, "1")
+    _force_path(monkeypatch, path)
+    capfd.readouterr()
     for name, nch in (("Kpi", 1), ("M", 2)):
         a = ctx.matrix(name)
         rng = np.random.default_rng(11)
         b = rng.standard_normal(nch * a.rows)
         s = G.create_solver("pcg", nch, a, 3000, 1e-10, 1)
+        if name == "Kpi":
+            _check_path(capfd, path)
         s.getRhs().copy_(t.tensor(b))
         s.getSol().zero_()
         assert s.solve() == 0, path
@@ -188,20 +202,17 @@ def test_gs_solver_matches_oracle(setup, torch_cuda):
     assert max(s.getLastMse(0), s.getLastMse(1)) < target
 
 
-@pytest.mark.parametrize("path", ["cluster-dsmem", "cluster-l2", "multikernel"])
-def test_mixed_pcg_reaches_fp64_tolerance(setup, torch_cuda, path, monkeypatch):
+@pytest.mark.parametrize("path", ["dsmem", "grid", "cluster", "multikernel"])
+def test_mixed_pcg_reaches_fp64_tolerance(setup, torch_cuda, path, monkeypatch, capfd):
     G, O, mesh, ctx, om, oc = setup
     t = torch_cuda
-    for k in ("NSF_NO_CLUSTER", "NSF_NO_DSMEM"):
-        monkeypatch.delenv(k, raising=False)
-    if path == "multikernel":
-        monkeypatch.setenv("NSF_NO_CLUSTER", "1")
-    elif path == "cluster-l2":
-        monkeypatch.setenv("NSF_NO_DSMEM", "1")
+    _force_path(monkeypatch, path)
+    capfd.readouterr()
     kpi = ctx.matrix("Kpi")
     rng = np.random.default_rng(8)
     b = rng.standard_normal(kpi.rows)
     s = G.create_solver("pcg", 1, kpi, 2000, 1e-10, 1, precision=G.NSF_PREC_MIXED)
+    _check_path(capfd, path)
     s.getRhs().copy_(t.tensor(b))
     s.getSol().zero_()
     assert s.solve() == 0
@@ -262,15 +273,22 @@ def test_chorin_fp64_matches_oracle(setup, torch_cuda, graph):
     assert s["status"] == 0 and s["pres_rel"] <= 1e-10
 
 
-def test_chorin_graph_equals_eager_bitwise(setup, torch_cuda):
+@pytest.mark.parametrize("path", ["auto", "grid", "cluster", "multikernel"])
+@pytest.mark.parametrize("precision", ["f64", "mixed"])
+def test_chorin_graph_equals_eager_bitwise(setup, torch_cuda, path, precision, monkeypatch):
+    """A captured step (device-terminated loops, persistent solver launches inside the graph) gives
+    bit-identical results to the same step run eagerly, on every solver path."""
     G, O, mesh, ctx, om, oc = setup
-    a = G.ChorinStepper(ctx, 1e-3, 1e-3, pres_tol=1e-9, use_graph=True)
-    b = G.ChorinStepper(ctx, 1e-3, 1e-3, pres_tol=1e-9, use_graph=False)
+    monkeypatch.setenv("NSF_PCG_PATH", path)
+    prec = G.NSF_PREC_F64 if precision == "f64" else G.NSF_PREC_MIXED
+    a = G.ChorinStepper(ctx, 1e-3, 1e-3, precision=prec, pres_tol=1e-9, use_graph=True)
+    b = G.ChorinStepper(ctx, 1e-3, 1e-3, precision=prec, pres_tol=1e-9, use_graph=False)
     a.step(3)
     b.step(3)
     ua, pa = a.state()
     ub, pb = b.state()
     assert np.array_equal(ua, ub) and np.array_equal(pa, pb)
+    assert a.stats()["status"] == 0
 
 
 def test_chorin_gs_velocity_matches_oracle(setup, torch_cuda):
