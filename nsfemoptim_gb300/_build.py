@@ -36,7 +36,8 @@ def _newer(target, deps):
 
 def build(verbose: bool = False, force: bool = False) -> str:
     os.makedirs(OUT, exist_ok=True)
-    headers = [os.path.join(CSRC, f) for f in ("kernels.cuh", "device.cuh", "solvers.cuh", "host/setup.hpp")]
+    headers = [os.path.join(CSRC, f) for f in sorted(os.listdir(CSRC)) if f.endswith((".cuh", ".h", ".hpp"))]
+    headers.append(os.path.join(CSRC, "host", "setup.hpp"))
     headers.append(os.path.join(HERE, "..", "include", "nsfem_gb300.h"))
     jobs = []
     objs = []

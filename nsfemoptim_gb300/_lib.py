@@ -81,10 +81,11 @@ def lib():
     """Load libnsfem_gb300.so, building it in-tree on first use if it is missing."""
     global _LIB
     if _LIB is None:
-        if not os.path.exists(LIB_PATH):
+        path = os.environ.get("NSF_LIBRARY") or LIB_PATH  # an alternative build of the same ABI
+        if path == LIB_PATH and not os.path.exists(LIB_PATH):
             from . import _build
             _build.build()
-        L = C.CDLL(LIB_PATH)
+        L = C.CDLL(path)
         for name, (res, args) in _SIGS.items():
             f = getattr(L, name)
             f.restype = res

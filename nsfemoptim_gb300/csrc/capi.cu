@@ -995,7 +995,12 @@ extern "C" int nsf_chorin_step(nsf_chorin S, int nSteps, void * stream)
                 launchCounter().fetch_sub(S->kernelsPerCapture); // counted when replayed
             }
             for (int i = 0; i < nSteps; i++)
+            {
                 NSF_CUDA(cudaGraphLaunch(S->exec, s));
+                // kernel nodes of one replay (a device-terminated loop body, used only by the
+                // multi-kernel solver path, is counted once)
+                launchCounter().fetch_add(S->kernelsPerCapture, std::memory_order_relaxed);
+            }
         }
         else
         {

@@ -142,6 +142,77 @@ namespace nsf
         }
     }
 
+    // LG consecutive lanes of a warp share one row (LG = 1: one thread per row).
+    template <int LG>
+    struct RowLanes
+    {
+        int lane, group;
+        unsigned mask;
+        static constexpr int groups = CTPB / LG;
+        __device__ __forceinline__ RowLanes()
+        {
+            lane = threadIdx.x & (LG - 1);
+            group = threadIdx.x / LG;
+            const int w = (threadIdx.x & 31) / LG;
+            mask = (LG == 32) ? FULL : (((1u << LG) - 1u) << (w * LG));
+        }
+        // sum over the lanes of the group, valid in every lane (fixed order)
+        template <typename T>
+        __device__ __forceinline__ T sum(T v) const
+        {
+#pragma unroll
+            for (int o = LG / 2; o > 0; o >>= 1)
+                v += __shfl_xor_sync(mask, v, o, LG);
+            return v;
+        }
+    };
+
+    // rowGather for a row shared by LG lanes: lane k takes the entries jb + k, jb + k + LG, ... in
+    // predicated batches of 4 (so a row of up to 4 * LG entries has all its loads in flight at
+    // once); the caller sums acc over the group.
+    template <typename T, int NCH, bool SMEM, int LG>
+    __device__ __forceinline__ void rowGatherLanes(const RowView<SMEM> & rv, int color, int jb, int je, int limit,
+                                                   const T * vO, int n, const T * v0, const T * v1, const T * w,
+                                                   const bool (&act)[NCH], T (&acc)[NCH], int lane)
+    {
+        if constexpr (LG == 1)
+            rowGather<T, NCH, SMEM>(rv, color, jb, je, limit, vO, n, v0, v1, w, act, acc);
+        else
+        {
+            constexpr int RBL = 4;
+            for (int j0 = jb + lane; j0 < je; j0 += RBL * LG)
+            {
+                int cols[RBL];
+                T vals[RBL];
+#pragma unroll
+                for (int t = 0; t < RBL; t++)
+                {
+                    const int j = j0 + t * LG;
+                    const bool ok = j < je;
+                    cols[t] = ok ? rv.col(j) : 0;
+                    vals[t] = (ok && cols[t] < limit) ? ldg(vO + rv.gnz(color, j)) : (T)0;
+                }
+#pragma unroll
+                for (int c = 0; c < NCH; c++)
+                    if (act[c])
+                    {
+                        T g[RBL];
+#pragma unroll
+                        for (int t = 0; t < RBL; t++)
+                        {
+                            const size_t o = (size_t)c * n + cols[t];
+                            g[t] = vals[t] != (T)0 ? __ldcg(v0 + o) : (T)0;
+                            if (v1 && vals[t] != (T)0)
+                                g[t] += w[c] * __ldcg(v1 + o);
+                        }
+#pragma unroll
+                        for (int t = 0; t < RBL; t++)
+                            acc[c] += vals[t] * g[t];
+                    }
+            }
+        }
+    }
+
     // K per-thread values summed over the CTA in a fixed order; the result is valid in every lane of
     // warp 0.
     template <typename T, int K>
@@ -422,30 +493,41 @@ namespace nsf
             alpha[c] = (T)0;
         }
 
+        // rows shared by LG lanes on the grid path (many short phases spread over every SM: one
+        // round of gathers per row); one thread per row in a cluster
+        constexpr int LG = std::is_same<Sync, GridSync<T>>::value ? 4 : 1;
+        const RowLanes<LG> RL;
+
         // ---- r = b - A x over own rows; ||b||^2
         T bbP[NCH];
 #pragma unroll
         for (int c = 0; c < NCH; c++)
             bbP[c] = (T)0;
         for (int col = 0; col < C; col++)
-            for (int l = chunkL[col] + threadIdx.x; l < chunkL[col + 1]; l += CTPB)
+            for (int l = chunkL[col] + RL.group; l < chunkL[col + 1]; l += RL.groups)
             {
                 const int i = chunkA[col] + (l - chunkL[col]);
-                const T d = ldg(A.diag + i);
                 T acc[NCH];
 #pragma unroll
                 for (int c = 0; c < NCH; c++)
-                    acc[c] = d * A.x[(size_t)c * n + i];
-                rowGather<T, NCH, SMEM>(rv, col, rv.begin(col, l), rv.end(col, l), INT_MAX, A.vO, n, A.x,
-                                        (const T *)nullptr, nullptr, act, acc);
+                    acc[c] = 0;
+                rowGatherLanes<T, NCH, SMEM, LG>(rv, col, rv.begin(col, l), rv.end(col, l), INT_MAX, A.vO, n, A.x,
+                                                 (const T *)nullptr, nullptr, act, acc, RL.lane);
 #pragma unroll
                 for (int c = 0; c < NCH; c++)
-                    if (act[c])
-                    {
-                        const T bi = A.b[(size_t)c * n + i];
-                        A.r[(size_t)c * n + i] = bi - acc[c];
-                        bbP[c] += bi * bi;
-                    }
+                    acc[c] = RL.sum(acc[c]);
+                if (RL.lane == 0)
+                {
+                    const T d = ldg(A.diag + i);
+#pragma unroll
+                    for (int c = 0; c < NCH; c++)
+                        if (act[c])
+                        {
+                            const T bi = A.b[(size_t)c * n + i];
+                            A.r[(size_t)c * n + i] = bi - (d * A.x[(size_t)c * n + i] + acc[c]);
+                            bbP[c] += bi * bi;
+                        }
+                }
             }
 
         // z = SGS(r) from z = 0.  init: no x / r update.  Forward phases use earlier colors only.
@@ -456,7 +538,7 @@ namespace nsf
             for (int col = 0; col < C; col++)
             {
                 const int r0 = A.ps[col];
-                for (int l = chunkL[col] + threadIdx.x; l < chunkL[col + 1]; l += CTPB)
+                for (int l = chunkL[col] + RL.group; l < chunkL[col + 1]; l += RL.groups)
                 {
                     const int i = chunkA[col] + (l - chunkL[col]);
                     const int jb = rv.begin(col, l), je = rv.end(col, l);
@@ -465,7 +547,7 @@ namespace nsf
                     for (int c = 0; c < NCH; c++)
                     {
                         ri[c] = (T)0;
-                        if (act[c])
+                        if (act[c] && RL.lane == 0)
                         {
                             const size_t o = (size_t)c * n + i;
                             T rvv = A.r[o];
@@ -482,33 +564,45 @@ namespace nsf
 #pragma unroll
                     for (int c = 0; c < NCH; c++)
                         acc[c] = 0;
-                    rowGather<T, NCH, SMEM>(rv, col, jb, je, r0, A.vO, n, A.z, (const T *)nullptr, nullptr, act, acc);
-                    const T id = ldg(A.invD + i);
+                    rowGatherLanes<T, NCH, SMEM, LG>(rv, col, jb, je, r0, A.vO, n, A.z, (const T *)nullptr, nullptr,
+                                                     act, acc, RL.lane);
 #pragma unroll
                     for (int c = 0; c < NCH; c++)
-                        if (act[c])
-                        {
-                            const T zi = (ri[c] - acc[c]) * id;
-                            A.z[(size_t)c * n + i] = zi;
-                            rr[c] += ri[c] * ri[c];
-                            if (col == C - 1)
-                                rz[c] += ri[c] * zi;
-                        }
+                        acc[c] = RL.sum(acc[c]);
+                    if (RL.lane == 0)
+                    {
+                        const T id = ldg(A.invD + i);
+#pragma unroll
+                        for (int c = 0; c < NCH; c++)
+                            if (act[c])
+                            {
+                                const T zi = (ri[c] - acc[c]) * id;
+                                A.z[(size_t)c * n + i] = zi;
+                                rr[c] += ri[c] * ri[c];
+                                if (col == C - 1)
+                                    rz[c] += ri[c] * zi;
+                            }
+                    }
                 }
                 if (C > 1)
                     S.sync(); // z of this color visible to every CTA
             }
             for (int col = C - 2; col >= 0; col--)
             {
-                for (int l = chunkL[col] + threadIdx.x; l < chunkL[col + 1]; l += CTPB)
+                for (int l = chunkL[col] + RL.group; l < chunkL[col + 1]; l += RL.groups)
                 {
                     const int i = chunkA[col] + (l - chunkL[col]);
                     T acc[NCH];
 #pragma unroll
                     for (int c = 0; c < NCH; c++)
                         acc[c] = 0;
-                    rowGather<T, NCH, SMEM>(rv, col, rv.begin(col, l), rv.end(col, l), INT_MAX, A.vO, n, A.z,
-                                            (const T *)nullptr, nullptr, act, acc);
+                    rowGatherLanes<T, NCH, SMEM, LG>(rv, col, rv.begin(col, l), rv.end(col, l), INT_MAX, A.vO, n,
+                                                     A.z, (const T *)nullptr, nullptr, act, acc, RL.lane);
+#pragma unroll
+                    for (int c = 0; c < NCH; c++)
+                        acc[c] = RL.sum(acc[c]);
+                    if (RL.lane != 0)
+                        continue;
                     const T id = ldg(A.invD + i);
 #pragma unroll
                     for (int c = 0; c < NCH; c++)
@@ -579,29 +673,41 @@ namespace nsf
                 pq[c] = (T)0;
             }
             for (int col = 0; col < C; col++)
-                for (int l = chunkL[col] + threadIdx.x; l < chunkL[col + 1]; l += CTPB)
+                for (int l = chunkL[col] + RL.group; l < chunkL[col + 1]; l += RL.groups)
                 {
                     const int i = chunkA[col] + (l - chunkL[col]);
-                    const T d = ldg(A.diag + i);
                     T pn[NCH], acc[NCH];
 #pragma unroll
                     for (int c = 0; c < NCH; c++)
                     {
-                        const size_t o = (size_t)c * n + i;
-                        pn[c] = act[c] ? (k == 1 ? A.z[o] : A.z[o] + beta[c] * pold[o]) : (T)0;
-                        acc[c] = d * pn[c];
-                    }
-                    rowGather<T, NCH, SMEM>(rv, col, rv.begin(col, l), rv.end(col, l), INT_MAX, A.vO, n, A.z,
-                                            k == 1 ? (const T *)nullptr : pold, beta, act, acc);
-#pragma unroll
-                    for (int c = 0; c < NCH; c++)
-                        if (act[c])
+                        pn[c] = (T)0;
+                        acc[c] = (T)0;
+                        if (act[c] && RL.lane == 0)
                         {
                             const size_t o = (size_t)c * n + i;
-                            pnew[o] = pn[c];
-                            A.q[o] = acc[c];
-                            pq[c] += pn[c] * acc[c];
+                            pn[c] = k == 1 ? A.z[o] : A.z[o] + beta[c] * pold[o];
                         }
+                    }
+                    rowGatherLanes<T, NCH, SMEM, LG>(rv, col, rv.begin(col, l), rv.end(col, l), INT_MAX, A.vO, n,
+                                                     A.z, k == 1 ? (const T *)nullptr : pold, beta, act, acc,
+                                                     RL.lane);
+#pragma unroll
+                    for (int c = 0; c < NCH; c++)
+                        acc[c] = RL.sum(acc[c]);
+                    if (RL.lane == 0)
+                    {
+                        const T d = ldg(A.diag + i);
+#pragma unroll
+                        for (int c = 0; c < NCH; c++)
+                            if (act[c])
+                            {
+                                const size_t o = (size_t)c * n + i;
+                                const T qi = d * pn[c] + acc[c];
+                                pnew[o] = pn[c];
+                                A.q[o] = qi;
+                                pq[c] += pn[c] * qi;
+                            }
+                    }
                 }
             S.template reduce<NCH>(pq, [&](const T (&tot)[NCH]) {
                 for (int c = 0; c < NCH; c++)

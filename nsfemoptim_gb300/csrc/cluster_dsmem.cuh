@@ -29,8 +29,21 @@
 #include "cluster.cuh"
 #include "kernels.cuh"
 
+#ifndef NSF_DS_TPB
+#define NSF_DS_TPB 1024
+#endif
+#ifndef NSF_DS_RB
+#define NSF_DS_RB 8
+#endif
+#ifndef NSF_DS_EXACT
+#define NSF_DS_EXACT 0
+#endif
+
 namespace nsf
 {
+    constexpr int DTPB = NSF_DS_TPB; // threads per CTA
+    constexpr int DRB = NSF_DS_RB;   // entries per predicated gather batch of a row
+
     // Byte layout of the dynamic shared memory of one CTA (identical in every CTA of the cluster).
     struct DsLayout
     {
@@ -88,6 +101,18 @@ namespace nsf
         SolverState * st;
         const int * skip;
         DsLayout lay;
+        // FP64 residual replacement ("reliable updates", T = float only): when ru != 0 the solve is
+        // of the FP64 system (values vO64 / diag64 on the same structure) for the FP64 right-hand
+        // side b64 and in/out solution x64; the FP32 CG accumulates its increment in shared memory
+        // and, whenever the iterated ||r||^2 has dropped by ruDelta2 since the last replacement (or
+        // met the tolerance), adds it into x64 and replaces r by b64 - A64 x64 computed in FP64.
+        // The solve stops on the FP64 residual.  b and x are unused then.
+        int ru;
+        double ruDelta2;
+        const double * b64;
+        const double * vO64;
+        const double * diag64;
+        double * x64;
     };
 
     __device__ __forceinline__ unsigned dsMapa(unsigned localAddr, int rank)
@@ -118,12 +143,59 @@ namespace nsf
                                              unsigned off0, unsigned off1, unsigned chBytes, const T (&w)[NCH],
                                              const bool (&act)[NCH], T (&acc)[NCH])
     {
-        for (int j0 = jb; j0 < je; j0 += RB)
-        {
-            unsigned ad[RB];
-            T v[RB];
+#if NSF_DS_EXACT
+        // exact-length batches: full DRB-wide batches, then one batch of the remaining count
+        // (dispatched to a fixed width), no per-entry predicates
+        auto batch = [&](int j0, auto width) {
+            constexpr int N = decltype(width)::value;
+            unsigned ad[N];
+            T v[N];
 #pragma unroll
-            for (int t = 0; t < RB; t++)
+            for (int t = 0; t < N; t++)
+            {
+                ad[t] = lad[j0 + t];
+                v[t] = VALS ? lv[j0 + t] : ldg(vOg + j0 + t);
+            }
+#pragma unroll
+            for (int c = 0; c < NCH; c++)
+                if (act[c])
+                {
+                    T g[N];
+#pragma unroll
+                    for (int t = 0; t < N; t++)
+                    {
+                        const unsigned a = ad[t] + c * chBytes;
+                        g[t] = dsLoad(a + off0, (T)0);
+                        if (TWO)
+                            g[t] += w[c] * dsLoad(a + off1, (T)0);
+                    }
+#pragma unroll
+                    for (int t = 0; t < N; t++)
+                        acc[c] += v[t] * g[t];
+                }
+        };
+        int j0 = jb;
+        for (; j0 + DRB <= je; j0 += DRB)
+            batch(j0, std::integral_constant<int, DRB>{});
+        switch (je - j0)
+        {
+        case 1: batch(j0, std::integral_constant<int, 1>{}); break;
+        case 2: batch(j0, std::integral_constant<int, 2>{}); break;
+        case 3: batch(j0, std::integral_constant<int, 3>{}); break;
+        case 4: batch(j0, std::integral_constant<int, 4>{}); break;
+        case 5: batch(j0, std::integral_constant<int, 5>{}); break;
+        case 6: batch(j0, std::integral_constant<int, 6>{}); break;
+        case 7: batch(j0, std::integral_constant<int, 7>{}); break;
+        default: break;
+        }
+        return;
+#endif
+        for (int j0 = jb; j0 < je; j0 += DRB)
+        {
+            unsigned ad[DRB];
+            T v[DRB];
+#pragma unroll
+            for (int t = 0; t < DRB; t++)
             {
                 const int j = j0 + t;
                 const bool ok = j < je;
@@ -134,9 +206,9 @@ namespace nsf
             for (int c = 0; c < NCH; c++)
                 if (act[c])
                 {
-                    T g[RB];
+                    T g[DRB];
 #pragma unroll
-                    for (int t = 0; t < RB; t++)
+                    for (int t = 0; t < DRB; t++)
                     {
                         g[t] = (T)0;
                         if (j0 + t < je)
@@ -148,7 +220,7 @@ namespace nsf
                         }
                     }
 #pragma unroll
-                    for (int t = 0; t < RB; t++)
+                    for (int t = 0; t < DRB; t++)
                         acc[c] += v[t] * g[t];
                 }
         }
@@ -163,7 +235,7 @@ namespace nsf
     __device__ __forceinline__ void dsClusterSum(cg::cluster_group & cl, const T (&v)[K], T (*slot)[8], int & buf,
                                                  Epi && epi)
     {
-        __shared__ T warpPart[CTPB / 32][K];
+        __shared__ T warpPart[DTPB / 32][K];
         const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 #pragma unroll
         for (int k = 0; k < K; k++)
@@ -181,7 +253,7 @@ namespace nsf
 #pragma unroll
             for (int k = 0; k < K; k++)
             {
-                T s = warpPart[lane][k];
+                T s = lane < DTPB / 32 ? warpPart[lane][k] : (T)0;
 #pragma unroll
                 for (int o = 16; o > 0; o >>= 1)
                     s += __shfl_xor_sync(FULL, s, o);
@@ -223,10 +295,12 @@ namespace nsf
         T alpha[NCH], beta[NCH];
         int act[NCH], status[NCH], iters[NCH], any;
         double bb[NCH], rr[NCH], rz[NCH], rzPrev[NCH];
+        int replace, replacements; // residual replacement due in this iteration; count
+        double rrRef[NCH];         // ||r||^2 at the last replacement
     };
 
     template <typename T, int NCH, bool VALS>
-    __global__ void __launch_bounds__(CTPB, 1) kPcgClusterDs(DsPcgArgs<T> A)
+    __global__ void __launch_bounds__(DTPB, 1) kPcgClusterDs(DsPcgArgs<T> A)
     {
         extern __shared__ __align__(16) unsigned char dsm[];
         cg::cluster_group cl = cg::this_cluster();
@@ -272,7 +346,7 @@ namespace nsf
             // vector planes start at zero (padding entries stay finite)
             uint4 * v4 = reinterpret_cast<uint4 *>(dsm);
             const int cnt = (int)(L.offRs / 16);
-            for (int t = threadIdx.x; t < cnt; t += CTPB)
+            for (int t = threadIdx.x; t < cnt; t += DTPB)
                 v4[t] = make_uint4(0u, 0u, 0u, 0u);
         }
         __syncthreads();
@@ -295,7 +369,7 @@ namespace nsf
         {
             const int a0 = chunkA[c], nr = chunkL[c + 1] - chunkL[c], g0 = chunkG[c], nb = nzBase[c];
             const int lo = A.ps[c];
-            for (int t = threadIdx.x; t < nr; t += CTPB)
+            for (int t = threadIdx.x; t < nr; t += DTPB)
             {
                 const int l = chunkL[c] + t, i = a0 + t;
                 const int jb = ldg(A.rsO + i), je = ldg(A.rsO + i + 1);
@@ -307,10 +381,10 @@ namespace nsf
                 diags[l] = ldg(A.diag + i);
 #pragma unroll
                 for (int ch = 0; ch < NCH; ch++)
-                    xs[ch * S + l] = ch < numCh ? A.x[(size_t)ch * n + i] : (T)0;
+                    xs[ch * S + l] = (ch < numCh && !A.ru) ? A.x[(size_t)ch * n + i] : (T)0; // ru: increment
             }
             const int cnt = nzBase[c + 1] - nb;
-            for (int t = threadIdx.x; t < cnt; t += CTPB)
+            for (int t = threadIdx.x; t < cnt; t += DTPB)
             {
                 const int e = ldg(A.cmap + g0 + t);
                 lad[nb + t] = dsMapa(zBase + (unsigned)(e & 0xFFFFFF) * (unsigned)sizeof(T), e >> 24);
@@ -331,15 +405,77 @@ namespace nsf
         for (int c = 0; c < NCH; c++)
             alpha[c] = (T)0;
 
+        // ---- FP64 residual replacement helpers (ru)
+        // x64 += x (the FP32 increment), x = 0, own rows
+        auto flushX = [&]() {
+            for (int col = 0; col < C; col++)
+                for (int l = chunkL[col] + threadIdx.x; l < chunkL[col + 1]; l += DTPB)
+                {
+                    const int i = chunkA[col] + (l - chunkL[col]);
+#pragma unroll
+                    for (int c = 0; c < NCH; c++)
+                        if (c < numCh)
+                        {
+                            double * px = A.x64 + (size_t)c * n + i;
+                            *px = __ldcg(px) + (double)xs[c * S + l];
+                            xs[c * S + l] = (T)0;
+                        }
+                }
+        };
+        // r = b64 - A64 x64 in FP64 for own rows (neighbours' x64 through L2), rounded into r;
+        // bbAcc += ||b64||^2 when withBb
+        auto trueResidual = [&](T (&bbAcc)[NCH], bool withBb) {
+            for (int col = 0; col < C; col++)
+                for (int l = chunkL[col] + threadIdx.x; l < chunkL[col + 1]; l += DTPB)
+                {
+                    const int i = chunkA[col] + (l - chunkL[col]);
+                    const int jb = ldg(A.rsO + i), je = ldg(A.rsO + i + 1);
+                    const double d = ldg(A.diag64 + i);
+#pragma unroll
+                    for (int c = 0; c < NCH; c++)
+                        if (c < numCh)
+                        {
+                            const double * xc = A.x64 + (size_t)c * n;
+                            double acc = d * __ldcg(xc + i);
+                            // predicated batches: all loads of a row in flight together
+                            for (int j0 = jb; j0 < je; j0 += DRB)
+                            {
+                                int cols[DRB];
+                                double v[DRB], g[DRB];
+#pragma unroll
+                                for (int t = 0; t < DRB; t++)
+                                {
+                                    const bool ok = j0 + t < je;
+                                    cols[t] = ok ? ldg(A.ciO + j0 + t) : i;
+                                    v[t] = ok ? ldg(A.vO64 + j0 + t) : 0.0;
+                                }
+#pragma unroll
+                                for (int t = 0; t < DRB; t++)
+                                    g[t] = __ldcg(xc + cols[t]);
+#pragma unroll
+                                for (int t = 0; t < DRB; t++)
+                                    acc += v[t] * g[t];
+                            }
+                            const double bi = ldg(A.b64 + (size_t)c * n + i);
+                            rsv[c * S + l] = (T)(bi - acc);
+                            if (withBb)
+                                bbAcc[c] += (T)bi * (T)bi;
+                        }
+                }
+        };
+
         // ---- r = b - A x over own rows; ||b||^2
         T bbP[NCH];
 #pragma unroll
         for (int c = 0; c < NCH; c++)
             bbP[c] = (T)0;
+        if (A.ru)
+            trueResidual(bbP, true);
+        else
         for (int col = 0; col < C; col++)
         {
             const T * vOg = A.vO + (chunkG[col] - nzBase[col]);
-            for (int l = chunkL[col] + threadIdx.x; l < chunkL[col + 1]; l += CTPB)
+            for (int l = chunkL[col] + threadIdx.x; l < chunkL[col + 1]; l += DTPB)
             {
                 const int i = chunkA[col] + (l - chunkL[col]);
                 const int jb = (int)(lrs[l] & 0xFFFFFFu), je = (int)(lrs[l + 1] & 0xFFFFFFu);
@@ -369,7 +505,7 @@ namespace nsf
             for (int col = 0; col < C; col++)
             {
                 const T * vOg = A.vO + (chunkG[col] - nzBase[col]);
-                for (int l = chunkL[col] + threadIdx.x; l < chunkL[col + 1]; l += CTPB)
+                for (int l = chunkL[col] + threadIdx.x; l < chunkL[col + 1]; l += DTPB)
                 {
                     const unsigned pk = lrs[l];
                     const int jb = (int)(pk & 0xFFFFFFu), jl = jb + (int)(pk >> 24);
@@ -414,7 +550,7 @@ namespace nsf
             for (int col = C - 2; col >= 0; col--)
             {
                 const T * vOg = A.vO + (chunkG[col] - nzBase[col]);
-                for (int l = chunkL[col] + threadIdx.x; l < chunkL[col + 1]; l += CTPB)
+                for (int l = chunkL[col] + threadIdx.x; l < chunkL[col + 1]; l += DTPB)
                 {
                     const int jb = (int)(lrs[l] & 0xFFFFFFu), je = (int)(lrs[l + 1] & 0xFFFFFFu);
                     T acc[NCH];
@@ -468,9 +604,12 @@ namespace nsf
                 sc.act[c] = (c < numCh) && fin && !conv;
                 sc.alpha[c] = (T)0;
                 sc.beta[c] = (T)0;
+                sc.rrRef[c] = rr;
                 any |= sc.act[c];
             }
             sc.any = any;
+            sc.replace = 0;
+            sc.replacements = 0;
         });
 #pragma unroll
         for (int c = 0; c < NCH; c++)
@@ -496,7 +635,7 @@ namespace nsf
             for (int col = 0; col < C; col++)
             {
                 const T * vOg = A.vO + (chunkG[col] - nzBase[col]);
-                for (int l = chunkL[col] + threadIdx.x; l < chunkL[col + 1]; l += CTPB)
+                for (int l = chunkL[col] + threadIdx.x; l < chunkL[col + 1]; l += DTPB)
                 {
                     const int jb = (int)(lrs[l] & 0xFFFFFFu), je = (int)(lrs[l + 1] & 0xFFFFFFu);
                     const T d = diags[l];
@@ -544,7 +683,23 @@ namespace nsf
                 act[c] = sc.act[c] != 0;
             }
             T rrN[NCH], rzN[NCH];
-            sgs(false, pnI, rrN, rzN);
+            if (A.ru && sc.replace) // same value in every CTA
+            {
+                // the CG step x += alpha p, folded into x64; r replaced by the FP64 residual
+#pragma unroll
+                for (int c = 0; c < NCH; c++)
+                    if (act[c])
+                        for (int col = 0; col < C; col++)
+                            for (int l = chunkL[col] + threadIdx.x; l < chunkL[col + 1]; l += DTPB)
+                                xs[c * S + l] += alpha[c] * pnew[c * S + l];
+                flushX();
+                cl.sync(); // every CTA's x64 in global memory
+                T unused[NCH];
+                trueResidual(unused, false);
+                sgs(true, pnI, rrN, rzN);
+            }
+            else
+                sgs(false, pnI, rrN, rzN);
             T red2[2 * NCH];
 #pragma unroll
             for (int c = 0; c < NCH; c++)
@@ -554,6 +709,9 @@ namespace nsf
             }
             dsClusterSum<T, 2 * NCH>(cl, red2, slot, buf, [&](const T (&tot)[2 * NCH]) {
                 int any = 0;
+                const bool replaced = A.ru && sc.replace;
+                sc.replace = 0;
+                sc.replacements += replaced ? 1 : 0;
                 for (int c = 0; c < NCH; c++)
                 {
                     if (sc.act[c])
@@ -563,7 +721,14 @@ namespace nsf
                         sc.rz[c] = rz;
                         const bool fin = isfinite(rr) && isfinite(rz);
                         const bool conv = absMode ? (rr < tol2) : (rr <= tol2 * sc.bb[c]);
-                        if (!fin || conv)
+                        // with replacement the solve stops only on an FP64 residual; a converged
+                        // or sufficiently reduced iterated residual schedules a replacement
+                        const bool stop = !fin || (conv && (!A.ru || replaced));
+                        if (replaced)
+                            sc.rrRef[c] = rr;
+                        else if (A.ru && fin && (conv || rr <= A.ruDelta2 * sc.rrRef[c]))
+                            sc.replace = 1;
+                        if (stop)
                         {
                             sc.act[c] = 0;
                             sc.iters[c] = k;
@@ -581,17 +746,21 @@ namespace nsf
                 act[c] = sc.act[c] != 0;
         }
 
-        // ---- x back to global memory (own rows)
-        for (int col = 0; col < C; col++)
-            for (int l = chunkL[col] + threadIdx.x; l < chunkL[col + 1]; l += CTPB)
-            {
-                const int i = chunkA[col] + (l - chunkL[col]);
+        // ---- x back to global memory (own rows); ru: the remaining increment into x64
+        if (A.ru)
+            flushX();
+        else
+            for (int col = 0; col < C; col++)
+                for (int l = chunkL[col] + threadIdx.x; l < chunkL[col + 1]; l += DTPB)
+                {
+                    const int i = chunkA[col] + (l - chunkL[col]);
 #pragma unroll
-                for (int c = 0; c < NCH; c++)
-                    if (c < numCh)
-                        A.x[(size_t)c * n + i] = xs[c * S + l];
-            }
-        // results (rank 0 writes; every CTA holds identical values)
+                    for (int c = 0; c < NCH; c++)
+                        if (c < numCh)
+                            A.x[(size_t)c * n + i] = xs[c * S + l];
+                }
+        // results (rank 0 writes; every CTA holds identical values).  ru: the refinement's view --
+        // iters = replacements ("passes"), innerTotal = CG iterations
         if (rank == 0 && threadIdx.x == 0)
         {
             for (int c = 0; c < NCH; c++)
@@ -602,7 +771,9 @@ namespace nsf
                     sc.iters[c] = maxIters;
                 }
                 st->status[c] = c < numCh ? sc.status[c] : 0;
-                st->iters[c] = sc.iters[c];
+                st->iters[c] = A.ru ? sc.replacements : sc.iters[c];
+                if (A.ru)
+                    st->innerTotal[c] = sc.iters[c];
                 st->bb[c] = sc.bb[c];
                 st->lastRR[c] = sc.rr[c];
                 st->active[c] = 0;
@@ -679,7 +850,7 @@ namespace nsf
         }
         cudaLaunchConfig_t cfg = {};
         cfg.gridDim = dim3(cs);
-        cfg.blockDim = dim3(CTPB);
+        cfg.blockDim = dim3(DTPB);
         cfg.dynamicSmemBytes = smem;
         cudaLaunchAttribute at[1];
         at[0].id = cudaLaunchAttributeClusterDimension;

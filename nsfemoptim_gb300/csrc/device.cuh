@@ -187,13 +187,14 @@ namespace nsf
 
 #define NSF_LAUNCH(kernel, grid, stream, ...) ::nsf::launchKernel(#kernel, kernel, (grid), (stream), __VA_ARGS__)
 
-    // launch a one-cluster kernel: cs CTAs of 1024 threads forming one thread-block cluster
+    // launch a one-cluster kernel: cs CTAs of `threads` threads forming one thread-block cluster
     template <typename... KArgs, typename... Args>
-    inline void launchCluster(void (*k)(KArgs...), int cs, size_t smem, cudaStream_t s, const Args &... a)
+    inline void launchCluster(void (*k)(KArgs...), int cs, int threads, size_t smem, cudaStream_t s,
+                              const Args &... a)
     {
         cudaLaunchConfig_t cfg = {};
         cfg.gridDim = dim3(cs);
-        cfg.blockDim = dim3(1024);
+        cfg.blockDim = dim3(threads);
         cfg.dynamicSmemBytes = smem;
         cfg.stream = s;
         cudaLaunchAttribute at[1];

@@ -317,11 +317,12 @@ namespace nsf
             {
                 DsPcgArgs<T> A{S.n,         S.nColors,    numCh,   psDev.get(), S.rsO.get(), S.ciO.get(),
                                S.vO.get(),  cmapDev.get(), S.diag.get(), S.invD.get(), b,    x,
-                               st.get(),    P.skip,       dsLay};
+                               st.get(),    P.skip,       dsLay,   0,     0.0,         nullptr,     nullptr,
+                               nullptr,     nullptr};
                 if (dsVals)
-                    launchCluster(kPcgClusterDs<T, NCH, true>, clusterSize, dsLay.bytes, s, A);
+                    launchCluster(kPcgClusterDs<T, NCH, true>, clusterSize, DTPB, dsLay.bytes, s, A);
                 else
-                    launchCluster(kPcgClusterDs<T, NCH, false>, clusterSize, dsLay.bytes, s, A);
+                    launchCluster(kPcgClusterDs<T, NCH, false>, clusterSize, DTPB, dsLay.bytes, s, A);
                 return;
             }
             if (path == CLUSTER || path == GRID)
@@ -333,9 +334,10 @@ namespace nsf
                 {
                     const ClusterSync<T> cs{};
                     if (clusterShared)
-                        launchCluster(kPcgSweep<T, NCH, true, ClusterSync<T>>, clusterSize, clusterSmem, s, A, cs);
+                        launchCluster(kPcgSweep<T, NCH, true, ClusterSync<T>>, clusterSize, CTPB, clusterSmem, s, A,
+                                      cs);
                     else
-                        launchCluster(kPcgSweep<T, NCH, false, ClusterSync<T>>, clusterSize, 0, s, A, cs);
+                        launchCluster(kPcgSweep<T, NCH, false, ClusterSync<T>>, clusterSize, CTPB, 0, s, A, cs);
                     return;
                 }
                 // barrier words start at zero for every solve (a solve that gave up waiting leaves
@@ -368,6 +370,26 @@ namespace nsf
 
         int kernelsPerIteration() const { return 2 * sys->nColors; }
         int initKernels() const { return 3 + 2 * sys->nColors - 1; }
+
+        // Whether solveReplaced can run (the DSMEM path of an FP32 solver).
+        bool canReplace() const { return path == DSMEM && sizeof(T) == 4 && envFlag("NSF_NO_RU") == 0; }
+
+        // FP32 CG with FP64 residual replacement on the FP64 system s64 (same structure and
+        // numbering): b64, x64 (in/out) planar NCH * n doubles; results and statistics written to
+        // stOut, whose tolerance and cap a preceding kernel has set.
+        void solveReplaced(cudaStream_t s, const SweepSystem<double> & s64, const double * b64, double * x64,
+                           SolverState * stOut, double delta2)
+        {
+            const SweepSystem<T> & S = *sys;
+            DsPcgArgs<T> A{S.n,          S.nColors,     numCh,          psDev.get(),    S.rsO.get(), S.ciO.get(),
+                           S.vO.get(),   cmapDev.get(), S.diag.get(),   S.invD.get(),   nullptr,     nullptr,
+                           stOut,        nullptr,       dsLay,          1,              delta2,      b64,
+                           s64.vO.get(), s64.diag.get(), x64};
+            if (dsVals)
+                launchCluster(kPcgClusterDs<T, NCH, true>, clusterSize, DTPB, dsLay.bytes, s, A);
+            else
+                launchCluster(kPcgClusterDs<T, NCH, false>, clusterSize, DTPB, dsLay.bytes, s, A);
+        }
     };
 
     // ------------------------------------------------------------------ multicolor GS ("gs")
@@ -456,6 +478,16 @@ namespace nsf
             const SweepSystem<double> & S = *sys64;
             const int n = S.n;
             SolverState * sd = st.get();
+            if (inner.canReplace())
+            {
+                // one launch: FP32 CG whose residual is replaced by the FP64 one whenever it has
+                // dropped by a factor 10 (and before stopping), so the Krylov recurrence survives
+                // the precision corrections that a restarted refinement pass would discard
+                const double delta = std::atof(envStr("NSF_RU_DELTA", "0.1").c_str());
+                NSF_LAUNCH(kSetConfig, 1, s, sd, innerMaxIters * (maxOuter > 0 ? maxOuter : 1), 0, tol * tol);
+                inner.solveReplaced(s, S, b, x, sd, delta * delta);
+                return;
+            }
             NSF_LAUNCH(kSetConfig, 1, s, sd, maxOuter, 0, tol * tol);
             NSF_LAUNCH(kOuterReset, 1, s, sd);
             inner.P.skip = &sd->skip;

@@ -202,10 +202,17 @@ def test_gs_solver_matches_oracle(setup, torch_cuda):
     assert max(s.getLastMse(0), s.getLastMse(1)) < target
 
 
-@pytest.mark.parametrize("path", ["dsmem", "grid", "cluster", "multikernel"])
+@pytest.mark.parametrize("path", ["dsmem", "dsmem-restart", "grid", "cluster", "multikernel"])
 def test_mixed_pcg_reaches_fp64_tolerance(setup, torch_cuda, path, monkeypatch, capfd):
+    """FP32 inner CG + FP64 correction reaches the FP64 tolerance on the true residual: with FP64
+    residual replacement inside the cluster solve (dsmem) and with restarted refinement passes."""
     G, O, mesh, ctx, om, oc = setup
     t = torch_cuda
+    if path == "dsmem-restart":
+        monkeypatch.setenv("NSF_NO_RU", "1")
+        path = "dsmem"
+    else:
+        monkeypatch.delenv("NSF_NO_RU", raising=False)
     _force_path(monkeypatch, path)
     capfd.readouterr()
     kpi = ctx.matrix("Kpi")
