@@ -112,6 +112,30 @@ int nsf_spmm(nsf_csr a, int nrhs, const void *X, int ldx, void *Y, int ldy, void
    Replaces fcSpmv.compute + cublasSgeam (cpp/execs/NavierStokes/src/chorinCuda.cu:243-250). */
 int nsf_fastconv_apply(nsf_csr I, const void *Kvals, double nu, const void *u, void *Avals, void *stream);
 
+/* Largest nrhs nsf_residual_noalloc accepts (its scratch is sized for it). */
+#define NSF_NOALLOC_MAX_RHS 4
+
+/* FP64 residual with no device allocation: r[c] = b[c] - A x[c] for nrhs planar channels of
+   a->rows doubles (device pointers), and the squared norms written to the device array norms2:
+   norms2[c] = ||r[c]||^2, norms2[nrhs + c] = ||b[c]||^2 (c < nrhs).  r is bit-identical to
+   nsf_spmv(a, x, y = copy of b, -1, 1).
+   No counterpart in the reference.  It exists for callers that may not allocate device memory
+   during the call: code that runs while another component holds the allocator (a caching
+   allocator or a memory pool it does not own), real-time loops where an allocation would
+   synchronise the device, and embedders with a fixed device-memory budget.  The block partial
+   sums of the norm reduction and the last-block counter live in one statically sized device
+   array (64 KiB + the counter) inside the library instead of buffers made per handle.
+   Limits and rules:
+     - a must be FP64 and square; 1 <= nrhs <= NSF_NOALLOC_MAX_RHS, else NSF_ERR_INVALID_ARG;
+     - the first call on a device looks the array up (cudaGetSymbolAddress); make that first
+       call before any stream capture on that device;
+     - the counter starts at zero when the library is loaded and every completed call leaves it
+       at zero; nothing else needs clearing between calls;
+     - all calls on one device share the array: calls that overlap in time (other streams or
+       host threads) race and give wrong norms.  Order them on one stream. */
+int nsf_residual_noalloc(nsf_csr a, int nrhs, const double *x, const double *b, double *r, double *norms2,
+                         void *stream);
+
 /* ======================================================================== solvers ======= */
 
 typedef struct nsf_solver_s *nsf_solver;

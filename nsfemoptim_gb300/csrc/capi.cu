@@ -7,6 +7,7 @@
 #include <algorithm>
 #include <cstring>
 #include <memory>
+#include <mutex>
 #include <numeric>
 #include <string>
 
@@ -1075,3 +1076,107 @@ extern "C" int nsf_chorin_stats(nsf_chorin S, double * stats)
 }
 
 extern "C" void nsf_chorin_destroy(nsf_chorin S) { delete S; }
+
+// ============================================================ allocation-free FP64 residual
+
+namespace
+{
+    constexpr int kNoAllocMaxBlocks = 1024;                 // grid cap of nsf_residual_noalloc
+    constexpr int kNoAllocK = 2 * NSF_NOALLOC_MAX_RHS;      // reduced values per block
+    constexpr int kNoAllocMaxDevices = 64;
+
+    // Scratch of nsf_residual_noalloc: the per-block partial sums of the grid reduction
+    // (kNoAllocK x kNoAllocMaxBlocks doubles = 64 KiB) and the last-block counter.  Static device
+    // memory: zero when the module loads; each completed call leaves the counter at zero again.
+    struct NoAllocScratch
+    {
+        double part[kNoAllocK * kNoAllocMaxBlocks];
+        unsigned ticket;
+    };
+    static __device__ __align__(256) NoAllocScratch g_noallocScratch;
+
+    // r = b - A x per channel and its squared norms (kSpmv's row arithmetic, so r matches
+    // nsf_spmv(alpha = -1, beta = 1) bit for bit), then one deterministic grid reduction.
+    template <int L>
+    __global__ void __launch_bounds__(TPB) kResidualNoAlloc(int rows, const int * __restrict__ rs,
+                                                            const int * __restrict__ ci,
+                                                            const double * __restrict__ v, int nrhs,
+                                                            const double * __restrict__ x,
+                                                            const double * __restrict__ b, double * __restrict__ r,
+                                                            double * norms2, NoAllocScratch * sc)
+    {
+        Group<L> g;
+        double red[kNoAllocK];
+#pragma unroll
+        for (int k = 0; k < kNoAllocK; k++)
+            red[k] = 0;
+        for (int row = g.gid; row < rows; row += g.ngroups)
+        {
+            const int jb = ldg(rs + row), je = ldg(rs + row + 1);
+#pragma unroll
+            for (int c = 0; c < NSF_NOALLOC_MAX_RHS; c++)
+            {
+                if (c >= nrhs)
+                    break;
+                const double * xc = x + (size_t)c * rows;
+                double s = 0;
+                for (int j = jb + g.lane; j < je; j += L)
+                    s += ldg(v + j) * ldg(xc + ldg(ci + j));
+                s = g.sum(s);
+                if (g.lane == 0)
+                {
+                    const double bi = b[(size_t)c * rows + row];
+                    const double ri = bi - s;
+                    r[(size_t)c * rows + row] = ri;
+                    red[c] += ri * ri;
+                    red[NSF_NOALLOC_MAX_RHS + c] += bi * bi;
+                }
+            }
+        }
+        Outs<kNoAllocK> o;
+#pragma unroll
+        for (int k = 0; k < kNoAllocK; k++)
+        {
+            const int c = k % NSF_NOALLOC_MAX_RHS;
+            o.p[k] = c < nrhs ? norms2 + (k < NSF_NOALLOC_MAX_RHS ? c : nrhs + c) : nullptr;
+        }
+        gridSum<double, kNoAllocK>(red, sc->part, o, &sc->ticket, nullptr);
+    }
+
+    // Device address of the scratch, looked up once per device.
+    NoAllocScratch * noAllocScratch()
+    {
+        static std::mutex m;
+        static NoAllocScratch * addr[kNoAllocMaxDevices] = {};
+        int dev = 0;
+        NSF_CUDA(cudaGetDevice(&dev));
+        require(dev >= 0 && dev < kNoAllocMaxDevices, "device ordinal out of range");
+        std::lock_guard<std::mutex> lock(m);
+        if (!addr[dev])
+        {
+            NoAllocScratch * ptr = nullptr;
+            NSF_CUDA(cudaGetSymbolAddress((void **)&ptr, g_noallocScratch));
+            addr[dev] = ptr;
+        }
+        return addr[dev];
+    }
+} // namespace
+
+extern "C" int nsf_residual_noalloc(nsf_csr a, int nrhs, const double * x, const double * b, double * r,
+                                    double * norms2, void * stream)
+{
+    return guarded([&] {
+        require(a && x && b && r && norms2, "null argument");
+        require(a->dtype == NSF_F64, "nsf_residual_noalloc needs an FP64 matrix");
+        require(a->rows == a->cols, "nsf_residual_noalloc needs a square matrix");
+        if (nrhs < 1 || nrhs > NSF_NOALLOC_MAX_RHS)
+            throw Error(ST_INVALID, "nsf_residual_noalloc: nrhs = " + std::to_string(nrhs) +
+                                        " is outside 1.." + std::to_string(NSF_NOALLOC_MAX_RHS) +
+                                        " (the static scratch holds the reduction of at most that many channels)");
+        NoAllocScratch * sc = noAllocScratch();
+        const int grid = std::min(cappedBlocks((long long)a->rows * a->L), kNoAllocMaxBlocks);
+        cudaStream_t s = asStream(stream);
+        NSF_LANES(a->L, NSF_LAUNCH((kResidualNoAlloc<LL>), grid, s, a->rows, a->rs.get(), a->ci.get(),
+                                   a->v64.get(), nrhs, x, b, r, norms2, sc));
+    });
+}
