@@ -115,7 +115,54 @@ def run_cpu_reference(mesh_path: str, steps: int, warmup: int):
     for _ in range(steps):
         ch.step()
     dt = time.perf_counter() - t0
-    return steps / dt, dt, ctx
+    u, p = ch.state()
+    return steps / dt, dt, ctx, (u, p, oracle.forces(m, u, p, NU))
+
+
+ACC_STEPS = 100                    # accuracy run: mixed vs FP64 from rest
+ACC_CHECKPOINTS = (4, 25, 50, 100)  # steps at which the fields are compared
+
+
+def accuracy_run(G, ctx, mesh, stepper, torch, stream):
+    """Mixed-precision and FP64 steppers from rest for ACC_STEPS steps: relative L2 field
+    differences at the checkpoints and the drag/lift time series (both on the device, FP64)."""
+    sp = stream.cuda_stream
+    runs = {}
+    for name, prec in (("fp64", G.NSF_PREC_F64), ("mixed", G.NSF_PREC_MIXED)):
+        st = stepper(prec)
+        fn = G.Forces(mesh, st)
+        F = torch.zeros((ACC_STEPS, 2), dtype=torch.float64, device="cuda")
+        states = {}
+        with torch.cuda.stream(stream):
+            for k in range(ACC_STEPS):
+                st.step(1, sp)
+                fn.into(F[k], sp)
+                if k + 1 in ACC_CHECKPOINTS:
+                    states[k + 1] = st.state()
+        torch.cuda.synchronize()
+        runs[name] = (F.cpu().numpy(), states)
+        del fn, st
+
+    def rel(a, b):
+        import numpy as np
+        return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+
+    import numpy as np
+    F64, S64 = runs["fp64"]
+    FMX, SMX = runs["mixed"]
+    # coefficients c = 2 F / (U_mean^2 D) with U_mean = 2/3 U_max = PEAK / 6, D = 0.1
+    cscale = 2.0 / ((PEAK / 6.0) ** 2 * 0.1)
+    out = {
+        "steps": ACC_STEPS,
+        "field_rel_l2_mixed_vs_fp64": {str(k): {"u": rel(SMX[k][0], S64[k][0]), "p": rel(SMX[k][1], S64[k][1])}
+                                       for k in ACC_CHECKPOINTS},
+        "drag_max_rel_err_mixed_vs_fp64": float(np.abs(FMX[:, 0] - F64[:, 0]).max() / np.abs(F64[:, 0]).max()),
+        "lift_max_err_mixed_vs_fp64_rel_to_max_drag": float(np.abs(FMX[:, 1] - F64[:, 1]).max() /
+                                                            np.abs(F64[:, 0]).max()),
+        "c_drag_fp64_last": float(cscale * F64[-1, 0]),
+        "c_lift_fp64_last": float(cscale * F64[-1, 1]),
+    }
+    return out, (S64[4][0], S64[4][1], F64[3])
 
 
 def bench_ours(args, rank, world, local_rank):
@@ -240,6 +287,10 @@ def bench_ours(args, rank, world, local_rank):
         sweep_b = (nnz_p - n_p) * 8 + (n_p + 1) * 4 + 3 * n_p * 4 + n_p * 4
         pcg_bytes = spmv_b + 2 * sweep_b + 7 * n_p * 4
 
+        # ---- accuracy (untimed): mixed vs FP64 fields and drag/lift series from rest
+        accuracy, f64_step4 = (accuracy_run(G, ctx, mesh, stepper, torch, stream) if args.accuracy
+                               else (None, None))
+
         times = [t_mixed]
         if world > 1:
             tt = torch.tensor([t_mixed, t_f64, t_e2e], dtype=torch.float64, device="cuda")
@@ -290,6 +341,9 @@ def bench_ours(args, rank, world, local_rank):
                                   "stats": st_f64},
                          "mixed_stats": st_mixed},
         }
+        if accuracy is not None:
+            line["accuracy"] = accuracy
+            line["_f64_step4"] = f64_step4  # compared with the oracle in main(), then dropped
         if clk:
             line["clocks"] = clk
         return line
@@ -304,6 +358,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cpu-sample-steps", type=int, default=3)
+    ap.add_argument("--no-accuracy", dest="accuracy", action="store_false",
+                    help="skip the untimed mixed-vs-FP64 field and drag/lift comparison")
     args = ap.parse_args()
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -317,7 +373,7 @@ def main():
         try:
             path = make_mesh(tmp, H, 0)
             k = max(1, min(args.steps, 10))
-            sps, dt, ctx = run_cpu_reference(path, k, min(args.warmup, 2))
+            sps, dt, ctx, _ = run_cpu_reference(path, k, min(args.warmup, 2))
         finally:
             shutil.rmtree(tmp, ignore_errors=True)
         line = {"impl": "reference", "metric": METRIC, "value": round(sps, 4), "unit": "steps/s", "n_gpus": 0,
@@ -337,15 +393,25 @@ def main():
         torch.distributed.init_process_group("nccl")
     line = bench_ours(args, rank, world, local_rank)
     if rank == 0 and line is not None:
+        f64_step4 = line.pop("_f64_step4", None)
         # CPU baseline on a bounded sample of the same workload (rank 0, N = 1 only)
         if world == 1 and args.cpu_sample_steps > 0:
             tmp = tempfile.mkdtemp()
             try:
                 path = make_mesh(tmp, H, 0)
-                sps, dt, _ = run_cpu_reference(path, args.cpu_sample_steps, 1)
+                sps, dt, _, (uo, po, fo) = run_cpu_reference(path, args.cpu_sample_steps, 1)
                 line["cpu_baseline"] = {"value": round(sps, 4), "unit": "steps/s", "cores": 1, "kind": "port",
                                         "sample": f"{args.cpu_sample_steps} time steps (after 1 warm-up) of the same "
                                                   f"workload, FP64 C oracle, single thread"}
+                if f64_step4 is not None and args.cpu_sample_steps == 3:
+                    # the oracle has run 4 steps from rest: the FP64 GPU state after 4 steps vs it
+                    import numpy as np
+                    ug, pg, fg = f64_step4
+                    line["accuracy"]["fp64_vs_oracle_step4"] = {
+                        "u_rel_l2": float(np.linalg.norm(ug - uo) / np.linalg.norm(uo)),
+                        "p_rel_l2": float(np.linalg.norm(pg - po) / np.linalg.norm(po)),
+                        "drag_rel_err": float(abs(fg[0] - fo[0]) / abs(fo[0])),
+                        "lift_err_rel_to_drag": float(abs(fg[1] - fo[1]) / abs(fo[0]))}
             finally:
                 shutil.rmtree(tmp, ignore_errors=True)
         print(json.dumps(line))

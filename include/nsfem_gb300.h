@@ -198,6 +198,23 @@ int nsf_chorin_stats(nsf_chorin s, double *stats);
 long long nsf_kernel_launches(void);
 void nsf_chorin_destroy(nsf_chorin s);
 
+/* ========================================================= force functional (drag/lift) == */
+
+typedef struct nsf_forces_s *nsf_forces;
+
+/* Force of the flow on the border group `group` of mesh ("Circle": the cylinder), evaluated on the
+   state of stepper s (created from a context of the same mesh; s must outlive the handle):
+     F = sum over the group's edges of integral ( -p n + nu du/dn ) ds,
+   n the unit edge normal pointing into the fluid, u the P2 velocity and p the P1 pressure of the
+   adjacent triangle, 2-point Gauss-Legendre per edge, FP64.  forces[0] = F_x (drag),
+   forces[1] = F_y (lift).  No counterpart in the reference: the DFG benchmark's continuum
+   definition in stress form with the velocity gradient, for the drag/lift time series. */
+int nsf_forces_create(nsf_mesh mesh, nsf_chorin s, const char *group, nsf_forces *out);
+/* onDevice == 0: forces is a host array of 2 doubles and the call synchronises the stream;
+   otherwise a device array written asynchronously on stream (NULL: the stepper's stream) */
+int nsf_forces_eval(nsf_forces f, double *forces, int onDevice, void *stream);
+void nsf_forces_destroy(nsf_forces f);
+
 #ifdef __cplusplus
 }
 #endif

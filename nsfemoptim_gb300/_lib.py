@@ -73,6 +73,9 @@ _SIGS = {
     "nsf_chorin_stats": (C.c_int, [vp, f64p]),
     "nsf_kernel_launches": (C.c_longlong, []),
     "nsf_chorin_destroy": (None, [vp]),
+    "nsf_forces_create": (C.c_int, [vp, vp, C.c_char_p, C.POINTER(vp)]),
+    "nsf_forces_eval": (C.c_int, [vp, vp, C.c_int, vp]),
+    "nsf_forces_destroy": (None, [vp]),
 }
 
 _LIB = None

@@ -378,6 +378,34 @@ def kernel_launches() -> int:
     return int(lib().nsf_kernel_launches())
 
 
+class Forces:
+    """Drag/lift functional on a border group ("Circle": the cylinder) of a stepper's state:
+    F = integral (-p n + nu du/dn) ds, n into the fluid, FP64 on the device.  New: the reference
+    has no force functional."""
+
+    def __init__(self, mesh: Mesh, stepper: ChorinStepper, group: str = "Circle"):
+        h = vp()
+        check(lib().nsf_forces_create(mesh._h, stepper._h, group.encode(), C.byref(h)))
+        self._h = h
+        self._stepper = stepper  # the stepper must outlive the functional
+
+    def __call__(self, stream=None) -> np.ndarray:
+        """(F_x, F_y) of the current state (synchronous)."""
+        out = np.zeros(2, np.float64)
+        check(lib().nsf_forces_eval(self._h, _p(out, C.c_double), 0, vp(stream)))
+        return out
+
+    def into(self, out, stream=None):
+        """Write (F_x, F_y) into a device tensor of 2 doubles, asynchronously on stream."""
+        check(lib().nsf_forces_eval(self._h, _dptr(out), 1, vp(stream)))
+        return out
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            lib().nsf_forces_destroy(self._h)
+            self._h = None
+
+
 __all__ = ["Mesh", "load_gmsh", "ChorinContext", "build_chorin_context", "coloring", "CsrF", "Spmv", "Spmm",
            "spmv", "spmm", "fastconv_apply", "AbstractSolver", "create_solver", "ChorinStepper", "kernel_launches",
-           "NSF_F32", "NSF_F64", "NSF_PREC_F64", "NSF_PREC_MIXED", "NsfError"]
+           "Forces", "NSF_F32", "NSF_F64", "NSF_PREC_F64", "NSF_PREC_MIXED", "NsfError"]

@@ -1077,6 +1077,181 @@ extern "C" int nsf_chorin_stats(nsf_chorin S, double * stats)
 
 extern "C" void nsf_chorin_destroy(nsf_chorin S) { delete S; }
 
+// ============================================================ force functional (drag / lift)
+
+namespace
+{
+    // One quadrature point on one border edge: P2 velocity dofs and P1 pressure dofs of the
+    // adjacent triangle (stepper numbering; pressure -1 = Dirichlet node, p = 0), the physical
+    // gradients of the six P2 basis functions and the P1 shape values at the point, the weight
+    // (half the edge length) and the unit normal into the fluid.
+    struct ForcePoint
+    {
+        int v[6], p[3];
+        double gx[6], gy[6], psi[3], w, nx, ny;
+    };
+
+    // F = sum_points w (-p n + nu (grad u) n); one block, fixed summation order
+    __global__ void __launch_bounds__(256) kForces(const ForcePoint * __restrict__ pts, int npts,
+                                                   const double * __restrict__ u, int N,
+                                                   const double * __restrict__ pInt, double nu, double * out)
+    {
+        double fx = 0, fy = 0;
+        for (int i = threadIdx.x; i < npts; i += blockDim.x)
+        {
+            const ForcePoint & q = pts[i];
+            double uxx = 0, uxy = 0, uyx = 0, uyy = 0, pq = 0;
+#pragma unroll
+            for (int k = 0; k < 6; k++)
+            {
+                const double ux = u[q.v[k]], uy = u[N + q.v[k]];
+                uxx += ux * q.gx[k];
+                uxy += ux * q.gy[k];
+                uyx += uy * q.gx[k];
+                uyy += uy * q.gy[k];
+            }
+#pragma unroll
+            for (int k = 0; k < 3; k++)
+                if (q.p[k] >= 0)
+                    pq += pInt[q.p[k]] * q.psi[k];
+            fx += q.w * (-pq * q.nx + nu * (uxx * q.nx + uxy * q.ny));
+            fy += q.w * (-pq * q.ny + nu * (uyx * q.nx + uyy * q.ny));
+        }
+        __shared__ double part[2][8];
+        for (int o = 16; o > 0; o >>= 1)
+        {
+            fx += __shfl_xor_sync(FULL, fx, o);
+            fy += __shfl_xor_sync(FULL, fy, o);
+        }
+        const int warp = threadIdx.x >> 5;
+        if ((threadIdx.x & 31) == 0)
+        {
+            part[0][warp] = fx;
+            part[1][warp] = fy;
+        }
+        __syncthreads();
+        if (threadIdx.x == 0)
+        {
+            double sx = 0, sy = 0;
+            for (int w = 0; w < (int)(blockDim.x >> 5); w++)
+            {
+                sx += part[0][w];
+                sy += part[1][w];
+            }
+            out[0] = sx;
+            out[1] = sy;
+        }
+    }
+} // namespace
+
+struct nsf_forces_s
+{
+    nsf_chorin s = nullptr;
+    int npts = 0;
+    DevBuf<ForcePoint> pts;
+    DevBuf<double> out;
+    PinnedBuf<double> host{2};
+};
+
+extern "C" int nsf_forces_create(nsf_mesh mesh, nsf_chorin S, const char * group, nsf_forces * out)
+{
+    return guarded([&] {
+        require(mesh && S && group && out, "null argument");
+        const Mesh & m = mesh->m;
+        require(m.N == S->N && m.P == S->P, "mesh and stepper sizes differ");
+        const int gid = m.groupId(group);
+        require(gid >= 0, "no such border group");
+        // stepper numbering of velocity nodes and of pressure nodes (-1: Dirichlet, p = 0)
+        const std::vector<int> invV = inverse(S->permV), invP = inverse(S->permP);
+        std::vector<int> pCol(S->P, -1);
+        for (int i = 0; i < S->nIntP; i++)
+            pCol[S->intP[i]] = invP[i];
+        const double gq = 0.5 / std::sqrt(3.0);
+        const double tq[2] = {0.5 - gq, 0.5 + gq};
+        std::vector<ForcePoint> pts;
+        for (int b = 0; b < m.numBorder(); b++)
+        {
+            const int * vb = m.vBorder.data() + 6 * b;
+            if (vb[2] != gid)
+                continue;
+            const int t = vb[0];
+            const int * ve = m.vElem.data() + 6 * t;
+            const int * pe = m.pElem.data() + 3 * t;
+            auto X = [&](int node) { return (double)m.vXY[2 * node]; };
+            auto Y = [&](int node) { return (double)m.vXY[2 * node + 1]; };
+            const double x0 = X(ve[0]), y0 = Y(ve[0]);
+            // reference triangle map J = [[x1-x0, x2-x0], [y1-y0, y2-y0]] (corners c0, c1, c2)
+            const double j00 = X(ve[2]) - x0, j01 = X(ve[4]) - x0, j10 = Y(ve[2]) - y0, j11 = Y(ve[4]) - y0;
+            const double det = j00 * j11 - j01 * j10;
+            const double i00 = j11 / det, i01 = -j01 / det, i10 = -j10 / det, i11 = j00 / det;
+            const double ax = X(vb[3]), ay = Y(vb[3]), bx = X(vb[5]), by = Y(vb[5]);
+            const double dx = bx - ax, dy = by - ay, len = std::sqrt(dx * dx + dy * dy);
+            double nx = dy / len, ny = -dx / len;
+            const double cx = (x0 + X(ve[2]) + X(ve[4])) / 3 - 0.5 * (ax + bx);
+            const double cy = (y0 + Y(ve[2]) + Y(ve[4])) / 3 - 0.5 * (ay + by);
+            if (nx * cx + ny * cy < 0)
+            {
+                nx = -nx;
+                ny = -ny;
+            }
+            for (int q = 0; q < 2; q++)
+            {
+                ForcePoint fp{};
+                const double px = ax + tq[q] * dx - x0, py = ay + tq[q] * dy - y0;
+                const double xi = i00 * px + i01 * py, eta = i10 * px + i11 * py;
+                // P2 basis (node order c0, m01, c1, m12, c2, m20): reference gradients
+                const double rgx[6] = {-3 + 4 * xi + 4 * eta, 4 - 8 * xi - 4 * eta, -1 + 4 * xi, 4 * eta, 0.0,
+                                       -4 * eta};
+                const double rgy[6] = {-3 + 4 * eta + 4 * xi, -4 * xi, 0.0, 4 * xi, -1 + 4 * eta,
+                                       4 - 8 * eta - 4 * xi};
+                for (int k = 0; k < 6; k++)
+                {
+                    fp.v[k] = invV[ve[k]];
+                    fp.gx[k] = i00 * rgx[k] + i10 * rgy[k];
+                    fp.gy[k] = i01 * rgx[k] + i11 * rgy[k];
+                }
+                const double psi[3] = {1 - xi - eta, xi, eta};
+                for (int k = 0; k < 3; k++)
+                {
+                    fp.p[k] = pCol[pe[k]];
+                    fp.psi[k] = psi[k];
+                }
+                fp.w = 0.5 * len;
+                fp.nx = nx;
+                fp.ny = ny;
+                pts.push_back(fp);
+            }
+        }
+        require(!pts.empty(), "the border group has no edges");
+        auto f = std::make_unique<nsf_forces_s>();
+        f->s = S;
+        f->npts = (int)pts.size();
+        f->pts.upload(pts);
+        f->out.alloc(2);
+        *out = f.release();
+    });
+}
+
+extern "C" int nsf_forces_eval(nsf_forces f, double * forces, int onDevice, void * stream)
+{
+    return guarded([&] {
+        require(f && forces, "null argument");
+        cudaStream_t s = stream ? asStream(stream) : f->s->stream;
+        double * dst = onDevice ? forces : f->out.get();
+        NSF_LAUNCH(kForces, 1, s, f->pts.get(), f->npts, f->s->u.get(), f->s->N, f->s->pInt.get(),
+                   f->s->cfg.nu, dst);
+        if (!onDevice)
+        {
+            NSF_CUDA(cudaMemcpyAsync(f->host.get(), dst, 2 * sizeof(double), cudaMemcpyDeviceToHost, s));
+            NSF_CUDA(cudaStreamSynchronize(s));
+            forces[0] = f->host.get()[0];
+            forces[1] = f->host.get()[1];
+        }
+    });
+}
+
+extern "C" void nsf_forces_destroy(nsf_forces f) { delete f; }
+
 // ============================================================ allocation-free FP64 residual
 
 namespace

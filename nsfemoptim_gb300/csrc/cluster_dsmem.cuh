@@ -33,7 +33,7 @@
 #define NSF_DS_TPB 1024
 #endif
 #ifndef NSF_DS_RB
-#define NSF_DS_RB 8
+#define NSF_DS_RB 4 // measured: 4 beats 8 by ~6% per iteration on the pressure system (rows of ~6 entries)
 #endif
 #ifndef NSF_DS_EXACT
 #define NSF_DS_EXACT 0

@@ -93,6 +93,7 @@ def lib():
         L.orc_chorin_set.argtypes = [C.c_void_p, f64p, f64p]
         L.orc_chorin_step.argtypes = [C.c_void_p, f64p]
         L.orc_fastconv.argtypes = [C.POINTER(ContextS), C.c_double, f64p, f64p]
+        L.orc_forces.argtypes = [C.POINTER(MeshS), C.c_int, f64p, f64p, C.c_double, f64p]
         _LIB = L
     return _LIB
 
@@ -291,6 +292,19 @@ def fastconv(ctx: Context, nu: float, u) -> np.ndarray:
     u = np.ascontiguousarray(u, dtype=np.float64)
     out = np.zeros(ctx.K.nnz, dtype=np.float64)
     lib().orc_fastconv(C.byref(ctx._s), nu, _ptr(u, C.c_double), _ptr(out, C.c_double))
+    return out
+
+
+def forces(mesh: Mesh, u, p, nu: float, group: str = "Circle") -> np.ndarray:
+    """(F_x, F_y) = integral over the border group of (-p n + nu du/dn), n into the fluid."""
+    L = lib()
+    gid = L.orc_group_id(mesh._p, group.encode())
+    if gid < 0:
+        raise ValueError(f"no border group {group!r}")
+    u = np.ascontiguousarray(u, dtype=np.float64)
+    p = np.ascontiguousarray(p, dtype=np.float64)
+    out = np.zeros(2, dtype=np.float64)
+    L.orc_forces(mesh._p, gid, _ptr(u, C.c_double), _ptr(p, C.c_double), nu, _ptr(out, C.c_double))
     return out
 
 

@@ -132,6 +132,8 @@ int orc_chorin_step(orc_chorin *s, double *stats);
 
 /* the separate stages, exposed for parity tests */
 void orc_fastconv(const orc_context *ctx, double nu, const double *u, double *Avals);
+/* drag/lift: out[0..1] = integral over border group gid of (-p n + nu du/dn), n into the fluid */
+void orc_forces(const orc_mesh *m, int gid, const double *u, const double *p, double nu, double *out);
 void orc_spmm2(const orc_csr *a, const double *vals, const double *x, double *y);
 
 #ifdef __cplusplus

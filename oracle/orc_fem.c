@@ -453,6 +453,71 @@ void orc_context_free(orc_context *ctx)
     memset(ctx, 0, sizeof *ctx);
 }
 
+/* Force of the flow on the border group `gid` (the cylinder "Circle"):
+     F = sum over the group's border edges of  integral ( -p n + nu du/dn ) ds
+   with n the unit edge normal pointing into the fluid (towards the adjacent triangle), u the P2
+   velocity (planar u[0..N) x, u[N..2N) y) and p the P1 pressure of the adjacent triangle, on each
+   straight edge by 2-point Gauss-Legendre quadrature (exact: the integrand is at most quadratic
+   along the edge).  New: the reference has no force functional; the definition is the continuum
+   one of the DFG benchmark in stress form with the velocity gradient (not symmetrised). */
+void orc_forces(const orc_mesh *m, int gid, const double *u, const double *p, double nu, double *out)
+{
+    const int N = m->numV;
+    const double g = 0.5 / sqrt(3.0);
+    const double tq[2] = {0.5 - g, 0.5 + g};
+    double fx = 0, fy = 0;
+    for (int b = 0; b < m->numBorder; b++)
+    {
+        const int *vb = m->vBorder + 6 * b;
+        if (vb[2] != gid)
+            continue;
+        const int t = vb[0];
+        const int *ve = m->vElem + 6 * t, *pe = m->pElem + 3 * t;
+        const double x0 = m->vXY[2 * ve[0]], y0 = m->vXY[2 * ve[0] + 1];
+        const double x1 = m->vXY[2 * ve[2]], y1 = m->vXY[2 * ve[2] + 1];
+        const double x2 = m->vXY[2 * ve[4]], y2 = m->vXY[2 * ve[4] + 1];
+        /* J = [[x1-x0, x2-x0], [y1-y0, y2-y0]] maps the reference triangle */
+        const double j00 = x1 - x0, j01 = x2 - x0, j10 = y1 - y0, j11 = y2 - y0;
+        const double det = j00 * j11 - j01 * j10;
+        const double i00 = j11 / det, i01 = -j01 / det, i10 = -j10 / det, i11 = j00 / det; /* J^-1 */
+        const double ax = m->vXY[2 * vb[3]], ay = m->vXY[2 * vb[3] + 1];
+        const double bx = m->vXY[2 * vb[5]], by = m->vXY[2 * vb[5] + 1];
+        const double dx = bx - ax, dy = by - ay, len = sqrt(dx * dx + dy * dy);
+        double nx = dy / len, ny = -dx / len;
+        const double cx = (x0 + x1 + x2) / 3 - 0.5 * (ax + bx), cy = (y0 + y1 + y2) / 3 - 0.5 * (ay + by);
+        if (nx * cx + ny * cy < 0)
+        {
+            nx = -nx;
+            ny = -ny;
+        }
+        for (int q = 0; q < 2; q++)
+        {
+            const double px = ax + tq[q] * dx - x0, py = ay + tq[q] * dy - y0;
+            const double xi = i00 * px + i01 * py, eta = i10 * px + i11 * py;
+            double gx[6], gy[6], psi[3];
+            p2_grad(xi, eta, gx, gy);
+            p1_shape(xi, eta, psi);
+            double uxx = 0, uxy = 0, uyx = 0, uyy = 0, pq = 0;
+            for (int k = 0; k < 6; k++)
+            {
+                /* physical gradient = J^-T * reference gradient */
+                const double Gx = i00 * gx[k] + i10 * gy[k], Gy = i01 * gx[k] + i11 * gy[k];
+                uxx += u[ve[k]] * Gx;
+                uxy += u[ve[k]] * Gy;
+                uyx += u[N + ve[k]] * Gx;
+                uyy += u[N + ve[k]] * Gy;
+            }
+            for (int k = 0; k < 3; k++)
+                pq += p[pe[k]] * psi[k];
+            const double w = 0.5 * len;
+            fx += w * (-pq * nx + nu * (uxx * nx + uxy * ny));
+            fy += w * (-pq * ny + nu * (uyx * nx + uyy * ny));
+        }
+    }
+    out[0] = fx;
+    out[1] = fy;
+}
+
 /* A.values = nu * K.values + I * u  (fastConvection.cpp:102-115 with chorinCuda.cu:243-250) */
 void orc_fastconv(const orc_context *ctx, double nu, const double *u, double *Avals)
 {

@@ -280,6 +280,36 @@ def test_chorin_fp64_matches_oracle(setup, torch_cuda, graph):
     assert s["status"] == 0 and s["pres_rel"] <= 1e-10
 
 
+@pytest.mark.parametrize("precision", ["f64", "mixed"])
+def test_forces_match_oracle(setup, torch_cuda, precision):
+    """Drag/lift on the cylinder.  The device functional equals the oracle's functional on the same
+    state (relative 1e-12: only the summation order differs); the time series of the FP64 stepper
+    follows the FP64 oracle's (relative 1e-7), the mixed stepper's within 1e-4, over 5 steps."""
+    G, O, mesh, ctx, om, oc = setup
+    prec = G.NSF_PREC_F64 if precision == "f64" else G.NSF_PREC_MIXED
+    st = G.ChorinStepper(ctx, 1e-3, 1e-3, precision=prec, vel_method=1, vel_max_iters=300, vel_tol=1e-10,
+                         pres_max_iters=3000, pres_tol=1e-10, use_graph=True)
+    f = G.Forces(mesh, st)
+    ch = O.Chorin(oc, 1e-3, 1e-3, vel_method=1, vel_max_iters=300, vel_tol=1e-10, pres_max_iters=3000,
+                  pres_tol=1e-10)
+    dev = torch_cuda.zeros(2, dtype=torch_cuda.float64, device="cuda")
+    for _ in range(5):
+        st.step(1)
+        ch.step()
+        fg = f()
+        u, p = st.state()
+        same = O.forces(om, u, p, 1e-3)
+        scale = np.abs(same).max()
+        assert np.abs(fg - same).max() <= 1e-12 * scale
+        f.into(dev)
+        torch_cuda.cuda.synchronize()
+        assert np.array_equal(dev.cpu().numpy(), fg)
+        uo, po = ch.state()
+        fo = O.forces(om, uo, po, 1e-3)
+        tol = 1e-7 if precision == "f64" else 1e-4
+        assert np.abs(fg - fo).max() <= tol * np.abs(fo).max(), (fg, fo)
+
+
 @pytest.mark.parametrize("path", ["auto", "grid", "cluster", "multikernel"])
 @pytest.mark.parametrize("precision", ["f64", "mixed"])
 def test_chorin_graph_equals_eager_bitwise(setup, torch_cuda, path, precision, monkeypatch):

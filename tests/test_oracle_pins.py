@@ -72,6 +72,48 @@ def test_oracle_matches_reference_golden_square(oracle_lib, square_small):
     _check_against_golden(oracle_lib, square_small, _golden("square_n33_s0"), True)
 
 
+def _hole_area(m, gid):
+    """Area of the polygon formed by the border edges of group gid (star-shaped from (0.2, 0.2))."""
+    vb = m.v_border[m.v_border[:, 2] == gid]
+    a = m.v_xy.astype(np.float64)[vb[:, 3]] - (0.2, 0.2)
+    b = m.v_xy.astype(np.float64)[vb[:, 5]] - (0.2, 0.2)
+    return 0.5 * np.abs(a[:, 0] * b[:, 1] - a[:, 1] * b[:, 0]).sum()
+
+
+def test_force_functional_identities(oracle_lib, channel_coarse):
+    """Drag/lift functional (new, no reference counterpart): exact for fields the elements
+    represent exactly.  With n pointing into the fluid (out of the hole H):
+      u = 0, p = x        ->  F = -integral(x n) = (-|H|, 0)
+      u = (x^2, 0), p = 0 ->  F = nu integral(2 x n_x, 0) = (2 nu |H|, 0)"""
+    O = oracle_lib
+    m = O.Mesh(channel_coarse)
+    gid = m.groups.index("Circle")
+    H = _hole_area(m, gid)
+    n_edges = int((m.v_border[:, 2] == gid).sum())
+    # inscribed regular-ish polygon of the r = 0.05 circle
+    assert abs(H - 0.5 * n_edges * 0.05 ** 2 * np.sin(2 * np.pi / n_edges)) < 0.02 * H
+    # pressure node coordinates: the corners of each triangle (c0, c1, c2 = P2 nodes 0, 2, 4)
+    px = np.zeros(m.P)
+    for t in range(m.num_tri):
+        for k in range(3):
+            px[m.p_elem[t, k]] = m.v_xy[m.v_elem[t, 2 * k], 0]
+    f = O.forces(m, np.zeros(2 * m.N), px, 1e-3)
+    assert abs(f[0] + H) < 1e-12 and abs(f[1]) < 1e-12
+    # x^2 at the corners and at the exact edge midpoints (the stored midpoint coordinates are
+    # float-rounded, which would perturb the interpolant at the 1e-6 level)
+    u = np.zeros(2 * m.N)
+    xv = m.v_xy[:, 0].astype(np.float64)
+    for t in range(m.num_tri):
+        c = m.v_elem[t]
+        for k in (0, 2, 4):
+            u[c[k]] = xv[c[k]] ** 2
+        for mid, a, b in ((1, 0, 2), (3, 2, 4), (5, 4, 0)):
+            u[c[mid]] = (0.5 * (xv[c[a]] + xv[c[b]])) ** 2
+    nu = 2e-3
+    f = O.forces(m, u, np.zeros(m.P), nu)
+    assert abs(f[0] - 2 * nu * H) < 1e-12 and abs(f[1]) < 1e-12
+
+
 def test_fem_identities(oracle_lib, channel_coarse):
     """Values are restated (the reference integrator needs OpenCV): check the physics instead."""
     O = oracle_lib
