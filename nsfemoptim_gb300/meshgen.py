@@ -288,6 +288,33 @@ def _finish(pts, tris, border) -> TriMesh:
     return TriMesh(nodes=pts, triangles=tris, border=border)
 
 
+def p1_stiffness(nodes, triangles):
+    """P1 Laplacian (stiffness) of a triangle mesh as a CSR (rowStart, col, val): FP64, columns
+    sorted, duplicates summed.  K_ij = sum over triangles of area * grad(phi_i) . grad(phi_j), the
+    operator the channel context assembles as the pressure stiffness, built here without the P2
+    operators for pressure-only workloads."""
+    import scipy.sparse as sp
+
+    x = np.asarray(nodes, dtype=np.float64)[np.asarray(triangles)]  # T x 3 x 2
+    det = ((x[:, 1, 0] - x[:, 0, 0]) * (x[:, 2, 1] - x[:, 0, 1]) -
+           (x[:, 2, 0] - x[:, 0, 0]) * (x[:, 1, 1] - x[:, 0, 1]))
+    area = 0.5 * np.abs(det)
+    # gradients of the barycentric coordinates: grad(l_i) = (y_j - y_k, x_k - x_j) / det
+    g = np.empty((len(x), 3, 2))
+    for i, j, k in ((0, 1, 2), (1, 2, 0), (2, 0, 1)):
+        g[:, i, 0] = (x[:, j, 1] - x[:, k, 1]) / det
+        g[:, i, 1] = (x[:, k, 0] - x[:, j, 0]) / det
+    ke = area[:, None, None] * np.einsum("tik,tjk->tij", g, g)
+    t = np.asarray(triangles)
+    rows = np.repeat(t, 3, axis=1).ravel()
+    cols = np.tile(t, (1, 3)).ravel()
+    n = len(nodes)
+    a = sp.coo_matrix((ke.ravel(), (rows, cols)), shape=(n, n)).tocsr()
+    a.sum_duplicates()
+    a.sort_indices()
+    return a.indptr.astype(np.int32), a.indices.astype(np.int32), a.data
+
+
 def jittered_square(n: int, seed: int = 0, jitter: float = 0.2) -> TriMesh:
     """Unit square, n x n nodes, interior nodes moved by U(+-jitter*h), one diagonal per cell.
 

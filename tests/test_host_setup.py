@@ -96,6 +96,24 @@ def test_square_mesh_matches_golden(G, square_small):
     assert digest(kp.column) == g["sha256"]["Kp_col"]
 
 
+def test_p1_stiffness_matches_context(G, square_small):
+    """meshgen.p1_stiffness (the pressure-only Poisson workload's assembly) is the operator the
+    context assembles as Kp: same pattern, values within the float-coordinate rounding."""
+    from nsfemoptim_gb300 import meshgen
+    m = G.load_gmsh(square_small)
+    ve, pe, vxy, vb = m.arrays()
+    # P1 node coordinates from the triangles' corners (P2 nodes 0, 2, 4)
+    xy = np.zeros((m.P, 2))
+    for k in range(3):
+        xy[pe[:, k]] = vxy[ve[:, 2 * k]]
+    rs, ci, val = meshgen.p1_stiffness(xy, pe)
+    kp = G.build_chorin_context(m, 1.0, 2).matrix("Kp")
+    assert np.array_equal(rs, kp.rowStart) and np.array_equal(ci, kp.column)
+    assert np.abs(val - kp.values).max() <= 1e-5 * np.abs(kp.values).max()
+    # a Laplacian: rows sum to zero
+    assert np.abs(np.add.reduceat(val, rs[:-1])).max() < 1e-9
+
+
 def test_bad_inputs_rejected_with_status(G, tmp_path):
     from nsfemoptim_gb300 import _lib
     # missing file
