@@ -165,6 +165,101 @@ def accuracy_run(G, ctx, mesh, stepper, torch, stream):
     return out, (S64[4][0], S64[4][1], F64[3])
 
 
+POISSON_NODES = 1024  # nodes per side of the jittered unit square (1,048,576 nodes)
+
+
+def bench_poisson(args):
+    """Standalone pressure-Poisson solve: P1 Laplacian of a jittered 1024 x 1024-node unit square
+    (interior nodes moved by U(+-0.2 h), one diagonal per cell, seed 0), pure Neumann with one
+    Dirichlet pin (node 0 removed), RHS i.i.d. N(0,1) from seed 0 projected to zero mean.  FP64
+    PCG-SGS against FP32-inner / FP64-refinement, both to 1e-10 relative residual; GB/s of the PCG
+    iteration and of the SpMV."""
+    import numpy as np
+    import scipy.sparse as sp
+    import torch
+
+    import nsfemoptim_gb300 as G
+    from nsfemoptim_gb300 import meshgen
+    from nsfemoptim_gb300.api import HostCsr
+
+    t0 = time.perf_counter()
+    mesh = meshgen.jittered_square(POISSON_NODES, seed=0, jitter=0.2)
+    rs, ci, val = meshgen.p1_stiffness(mesh.nodes, mesh.triangles)
+    a = sp.csr_matrix((val, ci, rs))[1:, 1:].tocsr()
+    a.sort_indices()
+    n = a.shape[0]
+    rng = np.random.default_rng(0)
+    b = rng.standard_normal(n + 1)
+    b = (b - b.mean())[1:]
+    host = HostCsr(n, n, a.indptr.astype(np.int32), a.indices.astype(np.int32), a.data)
+    setup_s = time.perf_counter() - t0
+    bd = torch.tensor(b, device="cuda")
+
+    def ev():
+        return torch.cuda.Event(enable_timing=True)
+
+    out = {}
+    for name, prec in (("fp64", G.NSF_PREC_F64), ("mixed", G.NSF_PREC_MIXED)):
+        s = G.create_solver("pcg", 1, host, 20000, 1e-10, 1, precision=prec)
+        s.getRhs().copy_(bd)
+        best = None
+        for rep in range(1 + max(1, args.poisson_reps)):  # the first solve is a warm-up
+            s.getSol().zero_()
+            torch.cuda.synchronize()
+            e0, e1 = ev(), ev()
+            e0.record()
+            st = s.solve()
+            e1.record()
+            torch.cuda.synchronize()
+            if rep > 0:
+                t = e0.elapsed_time(e1) / 1e3
+                best = t if best is None else min(best, t)
+        x = s.getSol().cpu().numpy()
+        its = s.getLastIterations()
+        sv = 8 if name == "fp64" else 4
+        nnz = a.nnz
+        it_bytes = (nnz * (sv + 4) + (n + 1) * 4 + 2 * n * sv) + \
+            2 * ((nnz - n) * (sv + 4) + (n + 1) * 4 + 4 * n * sv) + 7 * n * sv
+        out[name] = {"solve_s": round(best, 5), "solves_per_s": round(1.0 / best, 3), "iterations": int(its),
+                     "status": int(st), "true_rel_residual": float(np.linalg.norm(b - a @ x) / np.linalg.norm(b)),
+                     "us_per_iteration": round(1e6 * best / max(1, its), 3),
+                     "pcg_iteration_gbs": round(it_bytes * its / best / 1e9, 1)}
+        del s
+    # SpMV alone, L2 flushed (a 256 MB write) before every timed launch
+    flush = torch.empty(64 << 20, dtype=torch.float32, device="cuda")
+    spmv = {}
+    for name, dt, tdt in (("fp64", G.NSF_F64, torch.float64), ("fp32", G.NSF_F32, torch.float32)):
+        A = G.CsrF.from_host(host, dtype=dt)
+        xv = torch.randn(n, dtype=tdt, device="cuda")
+        yv = torch.zeros(n, dtype=tdt, device="cuda")
+        tot, reps = 0.0, 10
+        for rep in range(reps + 2):
+            flush.fill_(float(rep))
+            e0, e1 = ev(), ev()
+            e0.record()
+            G.spmv(A, xv, yv)
+            e1.record()
+            torch.cuda.synchronize()
+            if rep >= 2:
+                tot += e0.elapsed_time(e1) / 1e3
+        sv = 8 if name == "fp64" else 4
+        byts = a.nnz * (sv + 4) + (n + 1) * 4 + 2 * n * sv
+        spmv[name] = {"us": round(1e6 * tot / reps, 2), "gbs": round(byts / (tot / reps) / 1e9, 1),
+                      "algorithmic_bytes": byts}
+    hbm, kind = peaks()
+    for v in spmv.values():
+        v["frac_of_hbm_peak"] = round(v["gbs"] / hbm, 4)
+    return {
+        "metric": "config 3: standalone P1 Poisson PCG-SGS to 1e-10 rel (1024x1024 jittered square), solves/s",
+        "value": out["mixed"]["solves_per_s"], "unit": "solves/s", "n_gpus": 1, "higher_is_better": True,
+        "dtype": "f32-inner/f64-refine", "data": "synthetic (seeded jittered unit square, RHS N(0,1) seed 0)",
+        "config": {"workload": "P1 Laplacian, 1024x1024 nodes, jitter 0.2h, one pin", "rows": n, "nnz": int(a.nnz),
+                   "setup_s": round(setup_s, 2)},
+        "variants": out, "spmv": spmv, "peak": hbm, "peak_kind": kind,
+        "mixed_vs_fp64_speedup": round(out["fp64"]["solve_s"] / out["mixed"]["solve_s"], 3),
+    }
+
+
 def bench_ours(args, rank, world, local_rank):
     import numpy as np
     import torch
@@ -360,11 +455,19 @@ def main():
     ap.add_argument("--cpu-sample-steps", type=int, default=3)
     ap.add_argument("--no-accuracy", dest="accuracy", action="store_false",
                     help="skip the untimed mixed-vs-FP64 field and drag/lift comparison")
+    ap.add_argument("--workload", default="channel", choices=["channel", "poisson"],
+                    help="channel: the time step (default); poisson: the standalone 1M-DOF pressure solve")
+    ap.add_argument("--poisson-reps", type=int, default=2)
     args = ap.parse_args()
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+
+    if args.workload == "poisson":
+        if rank == 0 and args.impl == "ours":
+            print(json.dumps(bench_poisson(args)))
+        return
 
     if args.impl == "reference":
         if rank != 0:
