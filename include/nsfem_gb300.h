@@ -117,8 +117,8 @@ int nsf_fastconv_apply(nsf_csr I, const void *Kvals, double nu, const void *u, v
 
 /* FP64 residual with no device allocation: r[c] = b[c] - A x[c] for nrhs planar channels of
    a->rows doubles (device pointers), and the squared norms written to the device array norms2:
-   norms2[c] = ||r[c]||^2, norms2[nrhs + c] = ||b[c]||^2 (c < nrhs).  r is bit-identical to
-   nsf_spmv(a, x, y = copy of b, -1, 1).
+   norms2[c] = ||r[c]||^2, norms2[nrhs + c] = ||b[c]||^2 (c < nrhs).  r equals
+   nsf_spmv(a, x, y = copy of b, -1, 1) up to the summation order of each row.
    No counterpart in the reference.  It exists for callers that may not allocate device memory
    during the call: code that runs while another component holds the allocator (a caching
    allocator or a memory pool it does not own), real-time loops where an allocation would

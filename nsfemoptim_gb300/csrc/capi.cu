@@ -404,9 +404,19 @@ extern "C" int nsf_spmv(nsf_csr a, const void * x, void * y, double alpha, doubl
 {
     return guarded([&] {
         require(a && x && y, "null argument");
-        const int grid = cappedBlocks((long long)a->rows * a->L);
+        // plain operator (no grid reduction): one row group per row, no grid cap
+        const int grid = blocksFor((long long)a->rows * a->L);
         cudaStream_t s = asStream(stream);
-        if (a->dtype == NSF_F64)
+        if (a->nBlocks > 0) // CSR-stream: every row fits a stream block
+        {
+            if (a->dtype == NSF_F64)
+                NSF_LAUNCH((kSpmvStream<double, double, double, double>), a->nBlocks, s, a->rb.get(), a->rs.get(),
+                           a->ci.get(), a->v64.get(), (const double *)x, (double *)y, alpha, beta);
+            else
+                NSF_LAUNCH((kSpmvStream<float, float, float, float>), a->nBlocks, s, a->rb.get(), a->rs.get(),
+                           a->ci.get(), a->v32.get(), (const float *)x, (float *)y, alpha, beta);
+        }
+        else if (a->dtype == NSF_F64)
         {
             NSF_LANES(a->L, NSF_LAUNCH((kSpmv<double, double, double, double, LL>), grid, s, a->rows, a->rs.get(),
                                        a->ci.get(), a->v64.get(), (const double *)x, (double *)y, alpha, beta));
@@ -424,7 +434,7 @@ extern "C" int nsf_spmm(nsf_csr a, int nrhs, const void * X, int ldx, void * Y, 
     return guarded([&] {
         require(a && X && Y && nrhs >= 1, "bad argument");
         require(ldx >= a->cols && ldy >= a->rows, "leading dimensions too small");
-        const int grid = cappedBlocks((long long)a->rows * a->L);
+        const int grid = blocksFor((long long)a->rows * a->L);
         cudaStream_t s = asStream(stream);
         for (int c0 = 0; c0 < nrhs; c0 += 2)
         {
@@ -459,7 +469,7 @@ extern "C" int nsf_fastconv_apply(nsf_csr I, const void * K, double nu, const vo
 {
     return guarded([&] {
         require(I && K && u && A, "null argument");
-        const int grid = cappedBlocks((long long)I->rows * I->L);
+        const int grid = blocksFor((long long)I->rows * I->L);
         cudaStream_t s = asStream(stream);
         if (I->nBlocks > 0)
         {
@@ -599,7 +609,7 @@ extern "C" int nsf_solver_solve(nsf_solver s, const double * b, double * x, void
     int st = guarded([&] {
         require(s && b && x, "null argument");
         cudaStream_t cs = asStream(stream);
-        const int n = s->n, grid = cappedBlocks(n);
+        const int n = s->n, grid = blocksFor(n);
         NSF_LAUNCH(kGatherPerm<double>, grid, cs, n, s->numCh, s->perm.get(), b, s->bp.get());
         NSF_LAUNCH(kGatherPerm<double>, grid, cs, n, s->numCh, s->perm.get(), x, s->xp.get());
         const bool rel = true;
@@ -742,46 +752,46 @@ struct nsf_chorin_s
         {
             NSF_LAUNCH((kFastConvStream<float, double, float, float>), I32.nBlocks, s, I32.rb.get(), I32.rs.get(),
                        I32.ci.get(), I32.v.get(), u.get(), K32.get(), (float)cfg.nu, A32.get());
-            NSF_LANES(M32.L, NSF_LAUNCH((kSpmm<float, double, double, float, LL, 2>), M32.fullBlocks(), s, N,
+            NSF_LANES(M32.L, NSF_LAUNCH((kSpmm<float, double, double, float, LL, 2>), blocksFor((long long)N * M32.L), s, N,
                                         M32.rsF.get(), M32.ciF.get(), A32.get(), u.get(), N, rhs.get(), N));
         }
         else
         {
             NSF_LAUNCH((kFastConvStream<double, double, double, double>), I64.nBlocks, s, I64.rb.get(), I64.rs.get(),
                        I64.ci.get(), I64.v.get(), u.get(), K64.get(), cfg.nu, A64.get());
-            NSF_LANES(M64.L, NSF_LAUNCH((kSpmm<double, double, double, double, LL, 2>), M64.fullBlocks(), s, N,
+            NSF_LANES(M64.L, NSF_LAUNCH((kSpmm<double, double, double, double, LL, 2>), blocksFor((long long)N * M64.L), s, N,
                                         M64.rsF.get(), M64.ciF.get(), A64.get(), u.get(), N, rhs.get(), N));
         }
         // 2. M acc = rhs ; u = u - tau acc ; Dirichlet
         enqueueMassSolve(s, true);
-        NSF_LAUNCH(kUpdateVelocity<double>, cappedBlocks(N), s, N, u.get(), acc.get(), cfg.tau, isDir.get(),
+        NSF_LAUNCH(kUpdateVelocity<double>, blocksFor(N), s, N, u.get(), acc.get(), cfg.tau, isDir.get(),
                    dirVal.get());
         // 3. rhsP = -(1/tau) D u ; Kpi pInt = rhsP (warm start)
         const double invTau = -1.0 / cfg.tau;
         if (mixed)
         {
-            NSF_LANES(D32.L, NSF_LAUNCH((kSpmv<float, double, double, float, LL>), cappedBlocks((long long)nIntP * D32.L),
+            NSF_LANES(D32.L, NSF_LAUNCH((kSpmv<float, double, double, float, LL>), blocksFor((long long)nIntP * D32.L),
                                         s, nIntP, D32.rs.get(), D32.ci.get(), D32.v.get(), u.get(), rhsP.get(),
                                         invTau, 0.0));
             mpres.enqueue(s, body, rhsP.get(), pInt.get(), cfg.maxOuter, cfg.presTol, cfg.presMaxIters, cfg.innerTol,
                           cfg.checkInterval);
-            NSF_LANES(G32.L, NSF_LAUNCH((kSpmv<float, double, double, float, LL>), cappedBlocks((long long)2 * N * G32.L),
+            NSF_LANES(G32.L, NSF_LAUNCH((kSpmv<float, double, double, float, LL>), blocksFor((long long)2 * N * G32.L),
                                         s, 2 * N, G32.rs.get(), G32.ci.get(), G32.v.get(), pInt.get(), rhs.get(), 1.0,
                                         0.0));
         }
         else
         {
             NSF_LANES(D64.L, NSF_LAUNCH((kSpmv<double, double, double, double, LL>),
-                                        cappedBlocks((long long)nIntP * D64.L), s, nIntP, D64.rs.get(), D64.ci.get(),
+                                        blocksFor((long long)nIntP * D64.L), s, nIntP, D64.rs.get(), D64.ci.get(),
                                         D64.v.get(), u.get(), rhsP.get(), invTau, 0.0));
             pres.enqueue(s, body, rhsP.get(), pInt.get(), cfg.presMaxIters, cfg.presTol, false, cfg.checkInterval);
             NSF_LANES(G64.L, NSF_LAUNCH((kSpmv<double, double, double, double, LL>),
-                                        cappedBlocks((long long)2 * N * G64.L), s, 2 * N, G64.rs.get(), G64.ci.get(),
+                                        blocksFor((long long)2 * N * G64.L), s, 2 * N, G64.rs.get(), G64.ci.get(),
                                         G64.v.get(), pInt.get(), rhs.get(), 1.0, 0.0));
         }
         // 4. M acc = G p ; u = u - tau acc ; Dirichlet
         enqueueMassSolve(s, false);
-        NSF_LAUNCH(kUpdateVelocity<double>, cappedBlocks(N), s, N, u.get(), acc.get(), cfg.tau, isDir.get(),
+        NSF_LAUNCH(kUpdateVelocity<double>, blocksFor(N), s, N, u.get(), acc.get(), cfg.tau, isDir.get(),
                    dirVal.get());
     }
 
@@ -1270,8 +1280,8 @@ namespace
     };
     static __device__ __align__(256) NoAllocScratch g_noallocScratch;
 
-    // r = b - A x per channel and its squared norms (kSpmv's row arithmetic, so r matches
-    // nsf_spmv(alpha = -1, beta = 1) bit for bit), then one deterministic grid reduction.
+    // r = b - A x per channel and its squared norms (row groups of L lanes, as the row-group SpMV),
+    // then one deterministic grid reduction.
     template <int L>
     __global__ void __launch_bounds__(TPB) kResidualNoAlloc(int rows, const int * __restrict__ rs,
                                                             const int * __restrict__ ci,

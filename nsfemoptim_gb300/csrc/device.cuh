@@ -134,8 +134,9 @@ namespace nsf
         return (int)(b < 1 ? 1 : b);
     }
 
-    // Blocks per kernel are capped at 4 per SM (grid-stride loops cover the rest): enough warps to
-    // hide L2 latency while keeping the per-kernel reductions at O(#SM) block sums.
+    // Kernels that end in a grid reduction cap their blocks at 4 per SM (grid-stride loops cover the
+    // rest), which keeps the reduction at O(#SM) block sums; plain operators use blocksFor (one row
+    // group per row: the rows' dependent loads overlap across the whole grid).
     inline int smCount()
     {
         static int n = 0;

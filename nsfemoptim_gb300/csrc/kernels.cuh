@@ -264,6 +264,50 @@ namespace nsf
         }
     }
 
+    // y = alpha A x + beta y (beta == 0: y is not read), CSR-stream: block b covers the rows
+    // [rb[b], rb[b+1]) whose entries fit in STREAM_NNZ.  Stage 1: coalesced loads of values and
+    // columns, STREAM_NNZ / TPB independent loads and gathers per thread, products (rounded) into
+    // shared memory; stage 2: one thread per row sums its products in entry order.
+    template <typename TM, typename TX, typename TY, typename TA>
+    __global__ void __launch_bounds__(TPB) kSpmvStream(const int * __restrict__ rb, const int * __restrict__ rs,
+                                                        const int * __restrict__ ci, const TM * __restrict__ v,
+                                                        const TX * __restrict__ x, TY * __restrict__ y, double alpha,
+                                                        double beta)
+    {
+        __shared__ TA prod[STREAM_NNZ];
+        const int r0 = ldg(rb + blockIdx.x), r1 = ldg(rb + blockIdx.x + 1);
+        const int s = ldg(rs + r0), e = ldg(rs + r1);
+        const int cnt = e - s;
+        TM vals[STREAM_NNZ / TPB];
+        int cols[STREAM_NNZ / TPB];
+#pragma unroll
+        for (int q = 0; q < STREAM_NNZ / TPB; q++)
+        {
+            const int j = threadIdx.x + q * TPB;
+            vals[q] = j < cnt ? ldg(v + s + j) : (TM)0;
+            cols[q] = j < cnt ? ldg(ci + s + j) : 0;
+        }
+#pragma unroll
+        for (int q = 0; q < STREAM_NNZ / TPB; q++)
+        {
+            const int j = threadIdx.x + q * TPB;
+            if (j < cnt)
+                prod[j] = (TA)vals[q] * (TA)ldg(x + cols[q]);
+        }
+        __syncthreads();
+        for (int r = r0 + threadIdx.x; r < r1; r += TPB)
+        {
+            const int b = ldg(rs + r) - s, en = ldg(rs + r + 1) - s;
+            TA acc = 0;
+            for (int j = b; j < en; j++)
+                acc += prod[j];
+            double out = alpha * (double)acc;
+            if (beta != 0.0)
+                out += beta * (double)y[r];
+            y[r] = (TY)out;
+        }
+    }
+
     // u <- Dirichlet value on boundary rows, u - tau * acc elsewhere (2 planar channels)
     template <typename TA>
     __global__ void __launch_bounds__(TPB) kUpdateVelocity(int n, double * __restrict__ u, const TA * __restrict__ acc,

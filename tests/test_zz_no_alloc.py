@@ -1,7 +1,8 @@
 """nsf_residual_noalloc (no device allocation during the call) against nsf_spmv, through the C ABI.
 
-Two calls in a row on one stream: r must equal nsf_spmv(a, x, y = b, -1, 1) bit for bit and the
-squared norms must match numpy (relative 1e-12: only the summation order differs).  The second
+Two calls in a row on one stream: r must match nsf_spmv(a, x, y = b, -1, 1) within 1e-13 of
+max |b| + max |A x| (the SpMV tolerance of the parity tests: the two kernels sum each row in a
+different order) and the squared norms must match numpy on that r (relative 1e-12).  The second
 call checks that the first left the static scratch ready for the next one.  nrhs outside
 1..NSF_NOALLOC_MAX_RHS is rejected before anything runs on the device.
 """
@@ -63,7 +64,8 @@ def test_residual_noalloc_matches_spmv(system, torch_cuda):
                     st = L.nsf_spmv(a._h, _ptr(xc), _ptr(yc), -1.0, 1.0, C.c_void_p(stream.cuda_stream))
                     assert st == 0
             stream.synchronize()
-            assert torch.equal(r, ref), (nrhs, call)
+            scale = float(b.abs().max() + (ref - b).abs().max())
+            assert float((r - ref).abs().max()) <= 1e-13 * scale, (nrhs, call)
             rh, bh = r.cpu().numpy(), b.cpu().numpy()
             want = [float(rh[c * n:(c + 1) * n] @ rh[c * n:(c + 1) * n]) for c in range(nrhs)] + \
                    [float(bh[c * n:(c + 1) * n] @ bh[c * n:(c + 1) * n]) for c in range(nrhs)]
