@@ -165,6 +165,80 @@ def accuracy_run(G, ctx, mesh, stepper, torch, stream):
     return out, (S64[4][0], S64[4][1], F64[3])
 
 
+def bench_small(args):
+    """The small plain-FP64 configuration: synthetic channel at h = 0.02 (the reference does not
+    ship that mesh; the generator makes it), U_max = 0.3 (peak 1.2), nu = 1e-3, tau = 1e-3, 2000
+    steps from rest, pressure PCG-SGS to 1e-10 relative.  GPU FP64 and mixed steppers over all
+    steps; the CPU oracle (FP64, one thread) on a bounded sample of the same run from rest."""
+    import numpy as np
+    import torch
+
+    import nsfemoptim_gb300 as G
+    import oracle
+
+    h, peak, nu, tau, steps = 0.02, 1.2, 1e-3, 1e-3, args.small_steps
+    tmp = tempfile.mkdtemp()
+    try:
+        path = make_mesh(tmp, h, 0)
+        mesh = G.load_gmsh(path)
+        ctx = G.build_chorin_context(mesh, peak)
+        stream = torch.cuda.Stream()
+        sp = stream.cuda_stream
+        res = {}
+        for name, prec in (("fp64", G.NSF_PREC_F64), ("mixed", G.NSF_PREC_MIXED)):
+            st = G.ChorinStepper(ctx, nu, tau, precision=prec, vel_method=1, vel_max_iters=500, vel_tol=1e-10,
+                                 pres_max_iters=5000, pres_tol=1e-10, check_interval=8, use_graph=True,
+                                 max_outer=4, inner_tol=1e-5)
+            with torch.cuda.stream(stream):
+                torch.cuda.synchronize()
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                st.step(steps, sp)
+                e1.record(stream)
+                torch.cuda.synchronize()
+            t = e0.elapsed_time(e1) / 1e3
+            u, p = st.state()
+            res[name] = {"steps_per_s": round(steps / t, 2), "ms_per_step": round(1e3 * t / steps, 4),
+                         "stats": st.stats(), "u": u, "p": p}
+            del st
+        # CPU oracle from rest on a bounded sample; its state is compared with a GPU FP64 run of
+        # the same number of steps
+        k = max(1, args.small_cpu_steps)
+        oracle.build()
+        om = oracle.Mesh(path)
+        oc = oracle.Context(om, peak, True)
+        ch = oracle.Chorin(oc, nu, tau, vel_method=1, vel_max_iters=500, vel_tol=1e-10, pres_max_iters=5000,
+                           pres_tol=1e-10)
+        t0 = time.perf_counter()
+        for _ in range(k):
+            ch.step()
+        cpu_t = time.perf_counter() - t0
+        uo, po = ch.state()
+        st = G.ChorinStepper(ctx, nu, tau, precision=G.NSF_PREC_F64, vel_method=1, vel_max_iters=500, vel_tol=1e-10,
+                             pres_max_iters=5000, pres_tol=1e-10, use_graph=True)
+        st.step(k)
+        ug, pg = st.state()
+    finally:
+        shutil.rmtree(tmp, ignore_errors=True)
+
+    def rel(a, b):
+        return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+
+    return {
+        "metric": "config 1: plain FP64 Chorin projection, h=0.02 channel, steps/s (GPU FP64 drop-in)",
+        "value": res["fp64"]["steps_per_s"], "unit": "steps/s", "n_gpus": 1, "steps": steps,
+        "higher_is_better": True, "dtype": "f64", "data": "synthetic (seeded DFG channel mesh, h=0.02)",
+        "config": {"workload": "DFG channel h=0.02, Umax=0.3, nu=1e-3, tau=1e-3, P2/P1, pressure PCG-SGS to 1e-10 rel",
+                   "triangles": mesh.num_tri, "N": ctx.N, "P": ctx.P},
+        "variants": {n: {kk: v for kk, v in r.items() if kk not in ("u", "p")} for n, r in res.items()},
+        "mixed_vs_fp64_after_all_steps": {"u_rel_l2": rel(res["mixed"]["u"], res["fp64"]["u"]),
+                                          "p_rel_l2": rel(res["mixed"]["p"], res["fp64"]["p"])},
+        "cpu_baseline": {"value": round(k / cpu_t, 3), "unit": "steps/s", "cores": 1, "kind": "port",
+                         "sample": f"the first {k} steps from rest, FP64 C oracle"},
+        "fp64_vs_oracle": {"steps": k, "u_rel_l2": rel(ug, uo), "p_rel_l2": rel(pg, po)},
+    }
+
+
 POISSON_NODES = 1024  # nodes per side of the jittered unit square (1,048,576 nodes)
 
 
@@ -455,8 +529,11 @@ def main():
     ap.add_argument("--cpu-sample-steps", type=int, default=3)
     ap.add_argument("--no-accuracy", dest="accuracy", action="store_false",
                     help="skip the untimed mixed-vs-FP64 field and drag/lift comparison")
-    ap.add_argument("--workload", default="channel", choices=["channel", "poisson"],
-                    help="channel: the time step (default); poisson: the standalone 1M-DOF pressure solve")
+    ap.add_argument("--workload", default="channel", choices=["channel", "poisson", "small"],
+                    help="channel: the h=0.005 time step (default); poisson: the standalone 1M-DOF pressure "
+                         "solve; small: the plain FP64 h=0.02 channel")
+    ap.add_argument("--small-steps", type=int, default=2000)
+    ap.add_argument("--small-cpu-steps", type=int, default=100)
     ap.add_argument("--poisson-reps", type=int, default=2)
     args = ap.parse_args()
 
@@ -464,9 +541,9 @@ def main():
     rank = int(os.environ.get("RANK", "0"))
     local_rank = int(os.environ.get("LOCAL_RANK", "0"))
 
-    if args.workload == "poisson":
+    if args.workload in ("poisson", "small"):
         if rank == 0 and args.impl == "ours":
-            print(json.dumps(bench_poisson(args)))
+            print(json.dumps(bench_poisson(args) if args.workload == "poisson" else bench_small(args)))
         return
 
     if args.impl == "reference":
