@@ -187,6 +187,11 @@ typedef struct nsf_chorin_s *nsf_chorin;
 int nsf_chorin_create(nsf_context ctx, const nsf_chorin_config *cfg, nsf_chorin *out);
 /* advance nSteps time steps on the stepper's stream (stream may be NULL: default stream) */
 int nsf_chorin_step(nsf_chorin s, int nSteps, void *stream);
+/* enqueue nSteps time steps (graph replays; needs useGraph = 1) and return without waiting, so
+   several steppers can advance concurrently on their own streams; nsf_chorin_stats keeps the
+   statistics of the last nsf_chorin_step.  No counterpart in the reference (its loop is
+   synchronous); used to run independent flow instances side by side. */
+int nsf_chorin_launch(nsf_chorin s, int nSteps, void *stream);
 /* copy the state to/from host memory in the original numbering: u[2N] planar, p[P] */
 int nsf_chorin_get_state(nsf_chorin s, double *u, double *p, void *stream);
 int nsf_chorin_set_state(nsf_chorin s, const double *u, const double *p, void *stream);

@@ -68,6 +68,7 @@ _SIGS = {
     "nsf_solver_destroy": (None, [vp]),
     "nsf_chorin_create": (C.c_int, [vp, C.POINTER(ChorinConfig), C.POINTER(vp)]),
     "nsf_chorin_step": (C.c_int, [vp, C.c_int, vp]),
+    "nsf_chorin_launch": (C.c_int, [vp, C.c_int, vp]),
     "nsf_chorin_get_state": (C.c_int, [vp, f64p, f64p, vp]),
     "nsf_chorin_set_state": (C.c_int, [vp, f64p, f64p, vp]),
     "nsf_chorin_stats": (C.c_int, [vp, f64p]),

@@ -347,6 +347,11 @@ class ChorinStepper:
     def step(self, n: int = 1, stream=None):
         check(lib().nsf_chorin_step(self._h, n, vp(stream)))
 
+    def launch(self, n: int = 1, stream=None):
+        """Enqueue n steps (graph replays) without waiting: independent steppers on their own
+        streams advance concurrently.  stats() keeps the last step() call's statistics."""
+        check(lib().nsf_chorin_launch(self._h, n, vp(stream)))
+
     def state(self):
         u = np.zeros(2 * self.N, np.float64)
         p = np.zeros(self.P, np.float64)

@@ -977,11 +977,35 @@ extern "C" int nsf_chorin_create(nsf_context ctx, const nsf_chorin_config * cfg,
     });
 }
 
+// Enqueue nSteps time steps on stream s (graph replays when the stepper uses a graph; the
+// graph is captured on the first call).
+static void enqueueSteps(nsf_chorin S, int nSteps, cudaStream_t s);
+
 extern "C" int nsf_chorin_step(nsf_chorin S, int nSteps, void * stream)
 {
     return guarded([&] {
         require(S && nSteps >= 0, "bad argument");
         cudaStream_t s = stream ? asStream(stream) : S->stream;
+        enqueueSteps(S, nSteps, s);
+        if (nSteps > 0)
+            S->collectStats(s);
+        if (S->stats[7] == ST_NONFINITE)
+            throw Error(ST_NONFINITE, "non-finite solver residual in the time step");
+    });
+}
+
+extern "C" int nsf_chorin_launch(nsf_chorin S, int nSteps, void * stream)
+{
+    return guarded([&] {
+        require(S && nSteps >= 0, "bad argument");
+        require(S->cfg.useGraph, "nsf_chorin_launch needs a graph-captured stepper (useGraph = 1)");
+        enqueueSteps(S, nSteps, stream ? asStream(stream) : S->stream);
+    });
+}
+
+static void enqueueSteps(nsf_chorin S, int nSteps, cudaStream_t s)
+{
+    {
         if (S->cfg.useGraph)
         {
             if (!S->exec)
@@ -1018,11 +1042,7 @@ extern "C" int nsf_chorin_step(nsf_chorin S, int nSteps, void * stream)
             for (int i = 0; i < nSteps; i++)
                 S->enqueueStep(s);
         }
-        if (nSteps > 0)
-            S->collectStats(s);
-        if (S->stats[7] == ST_NONFINITE)
-            throw Error(ST_NONFINITE, "non-finite solver residual in the time step");
-    });
+    }
 }
 
 extern "C" int nsf_chorin_get_state(nsf_chorin S, double * uOut, double * pOut, void * stream)

@@ -256,10 +256,15 @@ namespace nsf
             const std::string want = envStr("NSF_PCG_PATH", "auto");
             if (tryPersistent && want != "multikernel")
             {
-                const bool any = want == "auto";
-                if ((any || want == "dsmem" || want == "dsmem-novals") && setupDsmem(s, want != "dsmem-novals"))
+                // "auto-cluster": never the whole-GPU grid, so that independent solvers (batched
+                // instances on separate streams) can run side by side
+                const bool any = want == "auto", anyCl = want == "auto-cluster";
+                if ((any || anyCl || want == "dsmem" || want == "dsmem-novals") &&
+                    setupDsmem(s, want != "dsmem-novals"))
                     path = DSMEM;
                 else if ((want == "cluster" || want == "cluster-global") && setupCluster(s, want == "cluster"))
+                    path = CLUSTER;
+                else if (anyCl && (setupCluster(s, true) || setupCluster(s, false)))
                     path = CLUSTER;
                 else if ((any || want == "grid" || want == "grid-global") && setupGrid(s, want != "grid-global"))
                     path = GRID;
