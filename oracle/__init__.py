@@ -94,6 +94,10 @@ def lib():
         L.orc_chorin_step.argtypes = [C.c_void_p, f64p]
         L.orc_fastconv.argtypes = [C.POINTER(ContextS), C.c_double, f64p, f64p]
         L.orc_forces.argtypes = [C.POINTER(MeshS), C.c_int, f64p, f64p, C.c_double, f64p]
+        L.orc_chorin_set_dirichlet.argtypes = [C.c_void_p, f64p]
+        L.orc_forces_weights.argtypes = [C.POINTER(MeshS), C.c_int, f64p, f64p, f64p]
+        L.orc_adjoint_run.argtypes = [C.POINTER(ContextS), C.POINTER(MeshS), C.c_int, C.POINTER(ChorinCfgS), f64p,
+                                      f64p, f64p, C.c_int, f64p, f64p, C.c_double, f64p, f64p, f64p]
         _LIB = L
     return _LIB
 
@@ -336,11 +340,80 @@ class Chorin:
         p = np.ascontiguousarray(p, dtype=np.float64)
         lib().orc_chorin_set(self._h, _ptr(u, C.c_double), _ptr(p, C.c_double))
 
+    def set_dirichlet(self, dir_vx):
+        """x values of the Dirichlet velocity nodes (ctx.dir_ids order), imposed on the state too."""
+        d = np.ascontiguousarray(dir_vx, dtype=np.float64)
+        if d.shape != (len(self.ctx.dir_ids),):
+            raise ValueError("one value per Dirichlet node")
+        lib().orc_chorin_set_dirichlet(self._h, _ptr(d, C.c_double))
+
     def __del__(self):
         try:
             lib().orc_chorin_free(self._h)
         except Exception:
             pass
+
+
+def forces_weights(mesh: Mesh, group: str = "Circle"):
+    """(wV, wPx, wPy): F_x = nu wV.u_x + wPx.p and F_y = nu wV.u_y + wPy.p."""
+    L = lib()
+    gid = L.orc_group_id(mesh._p, group.encode())
+    if gid < 0:
+        raise ValueError(f"no border group {group!r}")
+    wV = np.zeros(mesh.N, dtype=np.float64)
+    wPx = np.zeros(mesh.P, dtype=np.float64)
+    wPy = np.zeros(mesh.P, dtype=np.float64)
+    L.orc_forces_weights(mesh._p, gid, _ptr(wV, C.c_double), _ptr(wPx, C.c_double), _ptr(wPy, C.c_double))
+    return wV, wPx, wPy
+
+
+def adjoint_run(ctx: Context, mesh: Mesh, nu, tau, n_steps, w_drag, w_lift=None, dir_vx=None, u0=None, p0=None,
+                vel_method=1, vel_max_iters=100000, vel_tol=1e-14, pres_max_iters=100000, pres_tol=1e-14,
+                solve_tol=1e-14, group: str = "Circle"):
+    """FP64 forward + discrete-adjoint sweep of the oracle (orc_adjoint_run).
+
+    Returns (J, dJ/dnu, dJ/d dirVx [nDir], dJ/du0 [2N])."""
+    L = lib()
+    gid = L.orc_group_id(mesh._p, group.encode())
+    if gid < 0:
+        raise ValueError(f"no border group {group!r}")
+    cfg = ChorinCfgS(nu, tau, vel_method, vel_max_iters, vel_tol, pres_max_iters, pres_tol)
+    d = np.ascontiguousarray(ctx.dir_vx if dir_vx is None else dir_vx, dtype=np.float64)
+    wd = np.ascontiguousarray(np.broadcast_to(np.asarray(w_drag, dtype=np.float64), (n_steps,)))
+    wl = np.zeros(n_steps) if w_lift is None else np.asarray(w_lift, dtype=np.float64)
+    wl = np.ascontiguousarray(np.broadcast_to(wl, (n_steps,)))
+    uu = None if u0 is None else np.ascontiguousarray(u0, dtype=np.float64)
+    pp = None if p0 is None else np.ascontiguousarray(p0, dtype=np.float64)
+    out = np.zeros(2)
+    gdir = np.zeros(len(ctx.dir_ids) + 1)
+    gu = np.zeros(2 * ctx.N)
+    rc = L.orc_adjoint_run(C.byref(ctx._s), mesh._p, gid, C.byref(cfg), _ptr(d, C.c_double),
+                           None if uu is None else _ptr(uu, C.c_double),
+                           None if pp is None else _ptr(pp, C.c_double), int(n_steps), _ptr(wd, C.c_double),
+                           _ptr(wl, C.c_double), solve_tol, _ptr(out, C.c_double), _ptr(gdir, C.c_double),
+                           _ptr(gu, C.c_double))
+    if rc != 0:
+        raise RuntimeError(f"oracle adjoint failed with status {rc}")
+    return float(out[0]), float(out[1]), gdir[:len(ctx.dir_ids)].copy(), gu
+
+
+def forward_functional(ctx: Context, mesh: Mesh, nu, tau, n_steps, w_drag, w_lift=None, dir_vx=None,
+                       vel_tol=1e-14, pres_tol=1e-14, group: str = "Circle"):
+    """J of adjoint_run from a forward run alone (for finite differences)."""
+    s = Chorin(ctx, nu, tau, vel_method=1, vel_max_iters=100000, vel_tol=vel_tol, pres_max_iters=100000,
+               pres_tol=pres_tol)
+    if dir_vx is not None:
+        s.set_dirichlet(dir_vx)
+    wd = np.broadcast_to(np.asarray(w_drag, dtype=np.float64), (n_steps,))
+    wl = np.broadcast_to(np.asarray(0.0 if w_lift is None else w_lift, dtype=np.float64), (n_steps,))
+    J = 0.0
+    for n in range(n_steps):
+        s.step()
+        if wd[n] != 0 or wl[n] != 0:
+            u, p = s.state()
+            f = forces(mesh, u, p, nu, group)
+            J += wd[n] * f[0] + wl[n] * f[1]
+    return J
 
 
 # ---------------------------------------------------------------- reference build (oracle/_ref)

@@ -129,12 +129,31 @@ void orc_chorin_set(orc_chorin *s, const double *u, const double *p);
 /* one time step; stats[0..5] = velocity iters (tentative), pressure iters, velocity iters
    (final), pressure relative residual, tentative residual, final residual */
 int orc_chorin_step(orc_chorin *s, double *stats);
+/* replace the x values of the Dirichlet velocity nodes (nDir, in ctx->dirIds order; y stays 0)
+   and impose them on the current state */
+void orc_chorin_set_dirichlet(orc_chorin *s, const double *dirVx);
 
 /* the separate stages, exposed for parity tests */
 void orc_fastconv(const orc_context *ctx, double nu, const double *u, double *Avals);
 /* drag/lift: out[0..1] = integral over border group gid of (-p n + nu du/dn), n into the fluid */
 void orc_forces(const orc_mesh *m, int gid, const double *u, const double *p, double nu, double *out);
 void orc_spmm2(const orc_csr *a, const double *vals, const double *x, double *y);
+
+/* ---------------- discrete adjoint (no counterpart in the reference) ---------------- */
+/* Gradient of the force functional: F_x = nu * wV . u_x + wPx . p and F_y = nu * wV . u_y + wPy . p
+   (wV: numV entries, wPx/wPy: numP entries), the same quadrature as orc_forces. */
+void orc_forces_weights(const orc_mesh *m, int gid, double *wV, double *wPx, double *wPy);
+
+/* Forward run of nSteps Chorin steps from (u0, p0) with Dirichlet x values dirVx, then the reverse
+   sweep of the discrete adjoint (every linear solve taken as exact: PCG to solveTol), for
+     J = sum_{n=1..nSteps} wDrag[n-1] F_x(u_n, p_n) + wLift[n-1] F_y(u_n, p_n),
+   F the force on border group gid.  u0 (or the rest state if NULL) gets (dirVx, 0) on its
+   Dirichlet rows.  out[0] = J, out[1] = dJ/dnu; dJdDir (nDir) = dJ/d dirVx (through the initial
+   state and every step's impositions); dJdU0 (2N) = dJ/du0 on the free rows (0 on the Dirichlet
+   rows).  Either may be NULL.  Returns 0, or the failing status. */
+int orc_adjoint_run(const orc_context *ctx, const orc_mesh *m, int gid, const orc_chorin_cfg *cfg,
+                    const double *dirVx, const double *u0, const double *p0, int nSteps, const double *wDrag,
+                    const double *wLift, double solveTol, double *out, double *dJdDir, double *dJdU0);
 
 #ifdef __cplusplus
 }

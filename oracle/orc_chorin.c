@@ -27,6 +27,7 @@ struct orc_chorin_s
     orc_chorin_cfg cfg;
     orc_coloring colM, colP;
     double *u, *p, *pInt, *Avals, *rhs, *acc, *div, *rhsP, *g;
+    double *dirVx; /* x values imposed on the Dirichlet nodes (ctx->dirVx unless set) */
 };
 
 orc_chorin *orc_chorin_create(const orc_context *ctx, const orc_chorin_cfg *cfg)
@@ -46,9 +47,11 @@ orc_chorin *orc_chorin_create(const orc_context *ctx, const orc_chorin_cfg *cfg)
     s->div = (double *)calloc(P, sizeof(double));
     s->rhsP = (double *)calloc(ctx->nIntP + 1, sizeof(double));
     s->g = (double *)calloc(2 * N, sizeof(double));
+    s->dirVx = (double *)calloc(ctx->nDir + 1, sizeof(double));
+    memcpy(s->dirVx, ctx->dirVx, sizeof(double) * ctx->nDir);
     for (int i = 0; i < ctx->nDir; i++)
     {
-        s->u[ctx->dirIds[i]] = ctx->dirVx[i];
+        s->u[ctx->dirIds[i]] = s->dirVx[i];
         s->u[ctx->dirIds[i] + N] = 0.0;
     }
     return s;
@@ -69,7 +72,19 @@ void orc_chorin_free(orc_chorin *s)
     free(s->div);
     free(s->rhsP);
     free(s->g);
+    free(s->dirVx);
     free(s);
+}
+
+void orc_chorin_set_dirichlet(orc_chorin *s, const double *dirVx)
+{
+    const orc_context *ctx = s->ctx;
+    memcpy(s->dirVx, dirVx, sizeof(double) * ctx->nDir);
+    for (int i = 0; i < ctx->nDir; i++)
+    {
+        s->u[ctx->dirIds[i]] = s->dirVx[i];
+        s->u[ctx->dirIds[i] + ctx->N] = 0.0;
+    }
 }
 
 void orc_chorin_get(const orc_chorin *s, double *u, double *p)
@@ -98,7 +113,7 @@ static void impose(orc_chorin *s)
     const orc_context *ctx = s->ctx;
     for (int i = 0; i < ctx->nDir; i++)
     {
-        s->u[ctx->dirIds[i]] = ctx->dirVx[i];
+        s->u[ctx->dirIds[i]] = s->dirVx[i];
         s->u[ctx->dirIds[i] + ctx->N] = 0.0;
     }
 }

@@ -518,6 +518,60 @@ void orc_forces(const orc_mesh *m, int gid, const double *u, const double *p, do
     out[1] = fy;
 }
 
+/* The same sums as orc_forces, with each nodal value's coefficient collected instead of its
+   product: F_x = nu wV.u_x + wPx.p, F_y = nu wV.u_y + wPy.p (the functional is linear). */
+void orc_forces_weights(const orc_mesh *m, int gid, double *wV, double *wPx, double *wPy)
+{
+    const double g = 0.5 / sqrt(3.0);
+    const double tq[2] = {0.5 - g, 0.5 + g};
+    memset(wV, 0, sizeof(double) * m->numV);
+    memset(wPx, 0, sizeof(double) * m->numP);
+    memset(wPy, 0, sizeof(double) * m->numP);
+    for (int b = 0; b < m->numBorder; b++)
+    {
+        const int *vb = m->vBorder + 6 * b;
+        if (vb[2] != gid)
+            continue;
+        const int t = vb[0];
+        const int *ve = m->vElem + 6 * t, *pe = m->pElem + 3 * t;
+        const double x0 = m->vXY[2 * ve[0]], y0 = m->vXY[2 * ve[0] + 1];
+        const double x1 = m->vXY[2 * ve[2]], y1 = m->vXY[2 * ve[2] + 1];
+        const double x2 = m->vXY[2 * ve[4]], y2 = m->vXY[2 * ve[4] + 1];
+        const double j00 = x1 - x0, j01 = x2 - x0, j10 = y1 - y0, j11 = y2 - y0;
+        const double det = j00 * j11 - j01 * j10;
+        const double i00 = j11 / det, i01 = -j01 / det, i10 = -j10 / det, i11 = j00 / det;
+        const double ax = m->vXY[2 * vb[3]], ay = m->vXY[2 * vb[3] + 1];
+        const double bx = m->vXY[2 * vb[5]], by = m->vXY[2 * vb[5] + 1];
+        const double dx = bx - ax, dy = by - ay, len = sqrt(dx * dx + dy * dy);
+        double nx = dy / len, ny = -dx / len;
+        const double cx = (x0 + x1 + x2) / 3 - 0.5 * (ax + bx), cy = (y0 + y1 + y2) / 3 - 0.5 * (ay + by);
+        if (nx * cx + ny * cy < 0)
+        {
+            nx = -nx;
+            ny = -ny;
+        }
+        for (int q = 0; q < 2; q++)
+        {
+            const double px = ax + tq[q] * dx - x0, py = ay + tq[q] * dy - y0;
+            const double xi = i00 * px + i01 * py, eta = i10 * px + i11 * py;
+            double gx[6], gy[6], psi[3];
+            p2_grad(xi, eta, gx, gy);
+            p1_shape(xi, eta, psi);
+            const double w = 0.5 * len;
+            for (int k = 0; k < 6; k++)
+            {
+                const double Gx = i00 * gx[k] + i10 * gy[k], Gy = i01 * gx[k] + i11 * gy[k];
+                wV[ve[k]] += w * (Gx * nx + Gy * ny);
+            }
+            for (int k = 0; k < 3; k++)
+            {
+                wPx[pe[k]] -= w * psi[k] * nx;
+                wPy[pe[k]] -= w * psi[k] * ny;
+            }
+        }
+    }
+}
+
 /* A.values = nu * K.values + I * u  (fastConvection.cpp:102-115 with chorinCuda.cu:243-250) */
 void orc_fastconv(const orc_context *ctx, double nu, const double *u, double *Avals)
 {

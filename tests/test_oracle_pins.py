@@ -243,3 +243,58 @@ def test_multicolor_gs_matches_reference_gs2ch(oracle_lib, channel_coarse):
     xr = np.r_[x_ref[0::2], x_ref[1::2]]
     assert np.max(np.abs(xo - xr)) <= 1e-13 * np.max(np.abs(xr))
     assert np.allclose(rms, res, rtol=1e-10)
+
+
+def test_oracle_adjoint_matches_finite_differences(oracle_lib, channel_coarse):
+    """The FP64 discrete adjoint of the oracle (no reference counterpart) against FP64 central
+    differences of its own forward run: d/dnu, two inflow sine-series coefficients and a random
+    direction of the initial velocity.  J = mean drag over the second half of 10 steps."""
+    O = oracle_lib
+    m = O.Mesh(channel_coarse)
+    ctx = O.Context(m, 1.0)
+    nu, tau, n = 1e-3, 5e-4, 10
+    wd = np.zeros(n)
+    wd[n // 2:] = 1.0 / (n - n // 2)
+    rng = np.random.default_rng(5)
+    u0 = np.zeros(2 * ctx.N)
+    u0[:ctx.N] = 0.3 * rng.random(ctx.N)
+    u0[ctx.N:] = 0.05 * rng.standard_normal(ctx.N)
+    J, gnu, gdir, gu = O.adjoint_run(ctx, m, nu, tau, n, wd, u0=u0)
+
+    def fwd(nu_=nu, dv=None, uu=u0):
+        s = O.Chorin(ctx, nu_, tau, vel_method=1, vel_max_iters=100000, vel_tol=1e-14, pres_max_iters=100000,
+                     pres_tol=1e-14)
+        s.set_state(uu, np.zeros(ctx.P))
+        s.set_dirichlet(ctx.dir_vx if dv is None else dv)
+        out = 0.0
+        for k in range(n):
+            s.step()
+            if wd[k]:
+                uk, pk = s.state()
+                out += wd[k] * O.forces(m, uk, pk, nu_)[0]
+        return out
+
+    assert abs(fwd() - J) <= 1e-14 * abs(J)
+    eps = 1e-6
+    fd = (fwd(nu_=nu + eps) - fwd(nu_=nu - eps)) / (2 * eps)
+    assert abs(fd - gnu) <= 1e-6 * abs(gnu)
+    xy = m.v_xy.astype(np.float64)[ctx.dir_ids]
+    inflow = np.abs(xy[:, 0]) < 1e-9
+    # per coefficient for the two largest components; normwise over four (a small component's
+    # relative error is FD noise at the solver-tolerance level divided by eps)
+    fds, gs = [], []
+    for k in (1, 2, 3, 4):
+        b = np.where(inflow, np.sin(k * np.pi * xy[:, 1] / 0.41), 0.0)
+        fds.append((fwd(dv=ctx.dir_vx + eps * b) - fwd(dv=ctx.dir_vx - eps * b)) / (2 * eps))
+        gs.append(float(b @ gdir))
+    fds, gs = np.array(fds), np.array(gs)
+    for i in (0, 2):
+        assert abs(fds[i] - gs[i]) <= 1e-6 * abs(gs[i])
+    assert np.linalg.norm(fds - gs) <= 1e-6 * np.linalg.norm(gs)
+    d = rng.standard_normal(2 * ctx.N)
+    d[ctx.dir_ids] = 0.0
+    d[ctx.N + ctx.dir_ids] = 0.0
+    fd = (fwd(uu=u0 + eps * d) - fwd(uu=u0 - eps * d)) / (2 * eps)
+    g = float(d @ gu)
+    assert abs(fd - g) <= 1e-6 * abs(g)
+    assert np.all(gu[ctx.dir_ids] == 0) and np.all(gu[ctx.N + ctx.dir_ids] == 0)
