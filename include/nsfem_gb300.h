@@ -220,6 +220,47 @@ int nsf_forces_create(nsf_mesh mesh, nsf_chorin s, const char *group, nsf_forces
 int nsf_forces_eval(nsf_forces f, double *forces, int onDevice, void *stream);
 void nsf_forces_destroy(nsf_forces f);
 
+/* ============================================ parameters and discrete adjoint (gradients) == */
+/* None of these has a counterpart in the reference (it has no adjoint and fixes the inflow and
+   the viscosity for a run). */
+
+/* Replace the x values of the Dirichlet velocity nodes (one per node, in the context's dirIds
+   order; the y values stay 0) and impose them on the current state.  Synchronous. */
+int nsf_chorin_set_dirichlet(nsf_chorin s, const double *dirVx, void *stream);
+/* Change the viscosity of the following steps (a captured step is captured again). */
+int nsf_chorin_set_nu(nsf_chorin s, double nu);
+
+typedef struct
+{
+    int checkpointInterval; /* steps between stored states; the reverse sweep recomputes each
+                               segment from its checkpoint.  0: keep every state (no recomputation) */
+    int maxIters;           /* cap of each adjoint CG solve (<= 0: 20000) */
+    double tol;             /* relative residual of each adjoint CG solve (<= 0: 1e-13) */
+} nsf_adjoint_config;
+
+typedef struct nsf_adjoint_s *nsf_adjoint;
+
+/* Discrete adjoint of an FP64 stepper's time step for the force functional of f (created on s):
+     J = sum_{n=1..nSteps} wDrag[n-1] F_x(u_n, p_n) + wLift[n-1] F_y(u_n, p_n),
+   u_n, p_n the state after step n.  Every linear solve of the step is taken as exact; the adjoint
+   mass and pressure solves are CG with the multicolor SGS preconditioner on the stepper's systems
+   (both symmetric).  cfg may be NULL (defaults). */
+int nsf_adjoint_create(nsf_chorin s, nsf_forces f, const nsf_adjoint_config *cfg, nsf_adjoint *out);
+/* Run nSteps steps forward from the stepper's current state (whose Dirichlet rows hold the
+   Dirichlet values), then the reverse sweep.  wDrag / wLift: nSteps host weights (NULL = 0).
+   result[0] = J, result[1] = dJ/dnu; dJdDir (may be NULL): dJ/d(Dirichlet x value), one per
+   Dirichlet node in dirIds order, through the initial state and every step; dJdU0 (may be NULL):
+   dJ/du0 in the original numbering, planar [x(N); y(N)], 0 on the Dirichlet rows.  The stepper
+   ends in the state after the nSteps steps.  Synchronous. */
+int nsf_adjoint_run(nsf_adjoint a, int nSteps, const double *wDrag, const double *wLift, double *result,
+                    double *dJdDir, double *dJdU0, void *stream);
+/* stats[0..9] of the last run: forward steps, recomputed steps, reverse steps, adjoint mass CG
+   iterations (summed over channels and solves), adjoint pressure CG iterations, worst forward solver
+   status, worst adjoint solver status, bytes of stored states, forward ms, reverse-sweep ms
+   (CUDA events on the run's stream; the reverse sweep includes the recomputation) */
+int nsf_adjoint_stats(nsf_adjoint a, double *stats);
+void nsf_adjoint_destroy(nsf_adjoint a);
+
 #ifdef __cplusplus
 }
 #endif

@@ -37,6 +37,11 @@ class ChorinConfig(C.Structure):
                 ("maxOuter", C.c_int), ("innerTol", C.c_double)]
 
 
+class AdjointConfig(C.Structure):
+    """nsf_adjoint_config"""
+    _fields_ = [("checkpointInterval", C.c_int), ("maxIters", C.c_int), ("tol", C.c_double)]
+
+
 _SIGS = {
     "nsf_last_error": (C.c_char_p, []),
     "nsf_status_string": (C.c_char_p, [C.c_int]),
@@ -77,6 +82,12 @@ _SIGS = {
     "nsf_forces_create": (C.c_int, [vp, vp, C.c_char_p, C.POINTER(vp)]),
     "nsf_forces_eval": (C.c_int, [vp, vp, C.c_int, vp]),
     "nsf_forces_destroy": (None, [vp]),
+    "nsf_chorin_set_dirichlet": (C.c_int, [vp, f64p, vp]),
+    "nsf_chorin_set_nu": (C.c_int, [vp, C.c_double]),
+    "nsf_adjoint_create": (C.c_int, [vp, vp, C.POINTER(AdjointConfig), C.POINTER(vp)]),
+    "nsf_adjoint_run": (C.c_int, [vp, C.c_int, f64p, f64p, f64p, f64p, f64p, vp]),
+    "nsf_adjoint_stats": (C.c_int, [vp, f64p]),
+    "nsf_adjoint_destroy": (None, [vp]),
 }
 
 _LIB = None

@@ -366,6 +366,19 @@ class ChorinStepper:
         p = np.ascontiguousarray(p, np.float64)
         check(lib().nsf_chorin_set_state(self._h, _p(u, C.c_double), _p(p, C.c_double), None))
 
+    def set_dirichlet(self, dir_vx, stream=None):
+        """Replace the x values of the Dirichlet velocity nodes (ctx.dir_ids order) and impose them
+        on the current state.  New: the reference fixes the inflow for a run."""
+        d = np.ascontiguousarray(dir_vx, np.float64)
+        if d.shape != (len(self.ctx.dir_ids),):
+            raise NsfError(1, "one Dirichlet value per Dirichlet node")
+        check(lib().nsf_chorin_set_dirichlet(self._h, _p(d, C.c_double), vp(stream)))
+
+    def set_nu(self, nu: float):
+        """Viscosity of the following steps."""
+        check(lib().nsf_chorin_set_nu(self._h, float(nu)))
+        self.cfg.nu = float(nu)
+
     def stats(self):
         s = (C.c_double * 8)()
         check(lib().nsf_chorin_stats(self._h, s))
@@ -411,6 +424,52 @@ class Forces:
             self._h = None
 
 
+class Adjoint:
+    """Discrete adjoint of an FP64 stepper's time step for the force functional of `forces`:
+    J = sum_n w_drag[n] F_x(u_n, p_n) + w_lift[n] F_y(u_n, p_n).  New: the reference has no adjoint.
+
+    checkpoint_interval: steps between stored states (segments recomputed in the reverse sweep);
+    0 keeps every state."""
+
+    STATS = ("forward_steps", "recomputed_steps", "reverse_steps", "mass_iters", "pres_iters",
+             "forward_status", "adjoint_status", "state_bytes", "forward_ms", "reverse_ms")
+
+    def __init__(self, stepper: ChorinStepper, forces: Forces, checkpoint_interval: int = 50,
+                 max_iters: int = 20000, tol: float = 1e-13):
+        from ._lib import AdjointConfig
+        self.cfg = AdjointConfig(int(checkpoint_interval), int(max_iters), float(tol))
+        h = vp()
+        check(lib().nsf_adjoint_create(stepper._h, forces._h, C.byref(self.cfg), C.byref(h)))
+        self._h = h
+        self._keep = (stepper, forces)
+        self.N = stepper.N
+        self.n_dir = len(stepper.ctx.dir_ids)
+
+    def run(self, n_steps: int, w_drag=None, w_lift=None, stream=None):
+        """Forward n_steps from the stepper's state, then the reverse sweep.
+        Returns (J, dJ/dnu, dJ/d dirVx [nDir], dJ/du0 [2N])."""
+        wd = np.ascontiguousarray(np.broadcast_to(np.asarray(0.0 if w_drag is None else w_drag, np.float64),
+                                                  (n_steps,)))
+        wl = np.ascontiguousarray(np.broadcast_to(np.asarray(0.0 if w_lift is None else w_lift, np.float64),
+                                                  (n_steps,)))
+        res = np.zeros(2, np.float64)
+        gd = np.zeros(max(1, self.n_dir), np.float64)
+        gu = np.zeros(2 * self.N, np.float64)
+        check(lib().nsf_adjoint_run(self._h, int(n_steps), _p(wd, C.c_double), _p(wl, C.c_double),
+                                    _p(res, C.c_double), _p(gd, C.c_double), _p(gu, C.c_double), vp(stream)))
+        return float(res[0]), float(res[1]), gd[:self.n_dir].copy(), gu
+
+    def stats(self):
+        s = (C.c_double * 10)()
+        check(lib().nsf_adjoint_stats(self._h, s))
+        return dict(zip(self.STATS, list(s)))
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            lib().nsf_adjoint_destroy(self._h)
+            self._h = None
+
+
 __all__ = ["Mesh", "load_gmsh", "ChorinContext", "build_chorin_context", "coloring", "CsrF", "Spmv", "Spmm",
            "spmv", "spmm", "fastconv_apply", "AbstractSolver", "create_solver", "ChorinStepper", "kernel_launches",
-           "Forces", "NSF_F32", "NSF_F64", "NSF_PREC_F64", "NSF_PREC_MIXED", "NsfError"]
+           "Forces", "Adjoint", "NSF_F32", "NSF_F64", "NSF_PREC_F64", "NSF_PREC_MIXED", "NsfError"]

@@ -683,6 +683,7 @@ struct nsf_chorin_s
     bool mixed = false;
     int N = 0, P = 0, nIntP = 0;
     std::vector<int> permV, permP, intP;
+    std::vector<int> dirRows; // stepper row of each Dirichlet node (context dirIds order)
     // operators in the color-permuted numbering
     SweepSystem<double> M64, Kpi64;
     SweepSystem<float> M32, Kpi32;
@@ -936,6 +937,7 @@ static void buildChorin(nsf_chorin_s & S, const Context & c)
     {
         isDir[invV[c.dirIds[i]]] = 1;
         dval[invV[c.dirIds[i]]] = c.dirVx[i];
+        S.dirRows.push_back(invV[c.dirIds[i]]);
     }
     S.isDir.upload(isDir);
     S.dirVal.upload(dval);
@@ -1121,12 +1123,14 @@ namespace
         double gx[6], gy[6], psi[3], w, nx, ny;
     };
 
-    // F = sum_points w (-p n + nu (grad u) n); one block, fixed summation order
+    // F = sum_points w (-p n + nu (grad u) n); one block, fixed summation order.  visc (may be
+    // null) receives the viscous integrals sum_points w (grad u) n without the factor nu.
     __global__ void __launch_bounds__(256) kForces(const ForcePoint * __restrict__ pts, int npts,
                                                    const double * __restrict__ u, int N,
-                                                   const double * __restrict__ pInt, double nu, double * out)
+                                                   const double * __restrict__ pInt, double nu, double * out,
+                                                   double * visc)
     {
-        double fx = 0, fy = 0;
+        double fx = 0, fy = 0, vx = 0, vy = 0;
         for (int i = threadIdx.x; i < npts; i += blockDim.x)
         {
             const ForcePoint & q = pts[i];
@@ -1146,30 +1150,39 @@ namespace
                     pq += pInt[q.p[k]] * q.psi[k];
             fx += q.w * (-pq * q.nx + nu * (uxx * q.nx + uxy * q.ny));
             fy += q.w * (-pq * q.ny + nu * (uyx * q.nx + uyy * q.ny));
+            vx += q.w * (uxx * q.nx + uxy * q.ny);
+            vy += q.w * (uyx * q.nx + uyy * q.ny);
         }
-        __shared__ double part[2][8];
+        __shared__ double part[4][8];
         for (int o = 16; o > 0; o >>= 1)
         {
             fx += __shfl_xor_sync(FULL, fx, o);
             fy += __shfl_xor_sync(FULL, fy, o);
+            vx += __shfl_xor_sync(FULL, vx, o);
+            vy += __shfl_xor_sync(FULL, vy, o);
         }
         const int warp = threadIdx.x >> 5;
         if ((threadIdx.x & 31) == 0)
         {
             part[0][warp] = fx;
             part[1][warp] = fy;
+            part[2][warp] = vx;
+            part[3][warp] = vy;
         }
         __syncthreads();
         if (threadIdx.x == 0)
         {
-            double sx = 0, sy = 0;
+            double s[4] = {0, 0, 0, 0};
             for (int w = 0; w < (int)(blockDim.x >> 5); w++)
+                for (int k = 0; k < 4; k++)
+                    s[k] += part[k][w];
+            out[0] = s[0];
+            out[1] = s[1];
+            if (visc)
             {
-                sx += part[0][w];
-                sy += part[1][w];
+                visc[0] = s[2];
+                visc[1] = s[3];
             }
-            out[0] = sx;
-            out[1] = sy;
         }
     }
 } // namespace
@@ -1269,7 +1282,7 @@ extern "C" int nsf_forces_eval(nsf_forces f, double * forces, int onDevice, void
         cudaStream_t s = stream ? asStream(stream) : f->s->stream;
         double * dst = onDevice ? forces : f->out.get();
         NSF_LAUNCH(kForces, 1, s, f->pts.get(), f->npts, f->s->u.get(), f->s->N, f->s->pInt.get(),
-                   f->s->cfg.nu, dst);
+                   f->s->cfg.nu, dst, (double *)nullptr);
         if (!onDevice)
         {
             NSF_CUDA(cudaMemcpyAsync(f->host.get(), dst, 2 * sizeof(double), cudaMemcpyDeviceToHost, s));
@@ -1385,3 +1398,6 @@ extern "C" int nsf_residual_noalloc(nsf_csr a, int nrhs, const double * x, const
                                    a->v64.get(), nrhs, x, b, r, norms2, sc));
     });
 }
+
+// ============================================================ discrete adjoint (gradients)
+#include "adjoint.cuh"
