@@ -46,6 +46,9 @@ class DragProblem:
         self.basis = np.where(inflow[:, None], np.sin(np.pi * np.outer(xy[:, 1], k) / H_CHANNEL), 0.0)
         self.g0 = ctx.dir_vx.copy()
         self.N, self.P = ctx.N, ctx.P
+        # a stream of its own: the default stream's handle is 0, which the C ABI reads as "the
+        # stepper's stream", a non-blocking stream the default stream does not wait for
+        self._stream = torch.cuda.Stream()
         self._dev = torch.zeros(max(1, self.n_steps), 2, dtype=torch.float64, device="cuda")
 
     def _reset(self, nu: float, theta: np.ndarray):
@@ -56,15 +59,17 @@ class DragProblem:
     def value(self, nu: float, theta) -> float:
         """J from a forward run alone (graph replays; forces written on the device)."""
         theta = np.asarray(theta, np.float64)
-        self._reset(nu, theta)
-        stream = torch.cuda.current_stream().cuda_stream
-        self._dev.zero_()
-        for n in range(self.n_steps):
-            self.stepper.launch(1, stream)
-            if self.w[n] != 0.0:
-                self.forces.into(self._dev[n], stream)
+        self._reset(nu, theta)  # synchronous
         torch.cuda.current_stream().synchronize()
-        f = self._dev[:self.n_steps, 0].cpu().numpy()
+        with torch.cuda.stream(self._stream):
+            stream = self._stream.cuda_stream
+            self._dev.zero_()
+            for n in range(self.n_steps):
+                self.stepper.launch(1, stream)
+                if self.w[n] != 0.0:
+                    self.forces.into(self._dev[n], stream)
+            f = self._dev[:self.n_steps, 0].cpu().numpy()
+        self._stream.synchronize()
         return float(np.dot(self.w, f))
 
     def gradient(self, nu: float, theta):
