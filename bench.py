@@ -239,6 +239,137 @@ def bench_small(args):
     }
 
 
+ADJ_H, ADJ_PEAK, ADJ_NU, ADJ_TAU, ADJ_TOL = 0.01, 4.0, 1e-3, 5e-4, 1e-13
+ADJ_METRIC = "adjoint drag gradient time (d/dnu + 16 inflow coefficients), h=0.01, 1000 steps"
+
+
+def _adjoint_oracle_sample(path, k, theta, basis, g0, scale):
+    """The FP64 CPU adjoint (C oracle) on the first k steps from rest, every step weighted
+    scale / k.  Returns (seconds, J, dJ/dnu, dJ/dtheta)."""
+    import numpy as np
+    import oracle
+    oracle.build()
+    om = oracle.Mesh(path)
+    oc = oracle.Context(om, ADJ_PEAK, True)
+    w = np.full(k, scale / k)
+    t0 = time.perf_counter()
+    J, gnu, gdir, _ = oracle.adjoint_run(oc, om, ADJ_NU, ADJ_TAU, k, w, dir_vx=g0 + basis @ theta, vel_tol=ADJ_TOL,
+                                         pres_tol=ADJ_TOL, solve_tol=ADJ_TOL)
+    return time.perf_counter() - t0, J, gnu, basis.T @ gdir
+
+
+def bench_adjoint(args):
+    """Config 5, the discrete-adjoint gradient.  Synthetic DFG channel at h = 0.01, U_max = 1.0
+    (context peak 4.0), nu = 1e-3, tau = 5e-4, 1000 steps from rest; J = mean drag coefficient over
+    the last 500 steps; parameters nu and 16 sine-series coefficients of the inflow perturbation,
+    theta ~ N(0, 0.01^2) (seed 0).  Forward and adjoint CG solves to 1e-13 relative residual, FP64.
+    A "step" of this line is one whole gradient evaluation (forward run with checkpoints every 50
+    steps, then the reverse sweep with segment recomputation).  Checked against FP64 central
+    differences (eps = 1e-6) of the GPU forward run and against the FP64 CPU adjoint (C oracle) on
+    a bounded sample at the same mesh."""
+    import numpy as np
+    import torch
+
+    import nsfemoptim_gb300 as G
+    from nsfemoptim_gb300 import gradcheck as GC
+
+    n = args.adjoint_steps
+    tmp = tempfile.mkdtemp()
+    try:
+        path = make_mesh(tmp, ADJ_H, 0)
+        mesh = G.load_gmsh(path)
+        ctx = G.build_chorin_context(mesh, ADJ_PEAK)
+        w = np.zeros(n)
+        w[n // 2:] = 1.0 / (n - n // 2)
+        prob = GC.DragProblem(mesh, ctx, ADJ_PEAK, ADJ_NU, ADJ_TAU, n, w, n_coef=16, tol=ADJ_TOL,
+                              checkpoint_interval=args.adjoint_checkpoint)
+        theta = 0.01 * np.random.default_rng(0).standard_normal(16)
+        launches0 = G.kernel_launches()
+        for _ in range(max(0, args.adjoint_warmup)):
+            prob.gradient(ADJ_NU, theta)
+        clk = Clocks(0)
+        t_grad, t_e2e, t_fwd, t_rev = [], [], [], []
+        launches0 = G.kernel_launches()
+        for _ in range(max(1, args.adjoint_reps)):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            J, gnu, gth, gdir = prob.gradient(ADJ_NU, theta)
+            t_e2e.append(time.perf_counter() - t0)
+            s = prob.adjoint.stats()
+            t_fwd.append(s["forward_ms"] / 1e3)
+            t_rev.append(s["reverse_ms"] / 1e3)
+            t_grad.append(t_fwd[-1] + t_rev[-1])
+        launches = G.kernel_launches() - launches0
+        clocks = clk.stop()
+        reps = max(1, args.adjoint_reps)
+        st = prob.adjoint.stats()
+        variants = {}
+        if args.adjoint_variants:
+            keep = GC.DragProblem(mesh, ctx, ADJ_PEAK, ADJ_NU, ADJ_TAU, n, w, n_coef=16, tol=ADJ_TOL,
+                                  checkpoint_interval=0)
+            Jk, gnuk, gthk, _ = keep.gradient(ADJ_NU, theta)
+            sk = keep.adjoint.stats()
+            variants["keep_all_states"] = {
+                "gradient_s": round((sk["forward_ms"] + sk["reverse_ms"]) / 1e3, 3),
+                "forward_s": round(sk["forward_ms"] / 1e3, 3), "reverse_s": round(sk["reverse_ms"] / 1e3, 3),
+                "state_bytes": int(sk["state_bytes"]),
+                "max_rel_diff_vs_checkpointed": float(max(abs(gnuk - gnu) / abs(gnu),
+                                                          np.abs(gthk - gth).max() / np.abs(gth).max()))}
+            del keep
+        # central differences of the GPU forward run
+        eps = 1e-6
+        fd = {}
+        fnu = (prob.value(ADJ_NU + eps, theta) - prob.value(ADJ_NU - eps, theta)) / (2 * eps)
+        fd["nu"] = {"adjoint": gnu, "fd": fnu, "rel_err": abs(fnu - gnu) / abs(gnu)}
+        for k in args.adjoint_fd_coefs:
+            e = np.zeros(16)
+            e[k - 1] = eps
+            fk = (prob.value(ADJ_NU, theta + e) - prob.value(ADJ_NU, theta - e)) / (2 * eps)
+            fd[f"theta_{k}"] = {"adjoint": float(gth[k - 1]), "fd": fk,
+                                "rel_err": abs(fk - gth[k - 1]) / abs(gth[k - 1])}
+        # the FP64 CPU adjoint on a bounded sample (first k steps, all weighted) vs the GPU adjoint
+        k = max(1, args.adjoint_cpu_steps)
+        cpu_t, Jo, gnuo, gtho = _adjoint_oracle_sample(path, k, theta, prob.basis, prob.g0, prob.scale)
+        small = GC.DragProblem(mesh, ctx, ADJ_PEAK, ADJ_NU, ADJ_TAU, k, np.full(k, 1.0 / k), n_coef=16, tol=ADJ_TOL,
+                               checkpoint_interval=0)
+        Js, gnus, gths, _ = small.gradient(ADJ_NU, theta)
+    finally:
+        shutil.rmtree(tmp, ignore_errors=True)
+    N, P = ctx.N, ctx.P
+    h2d = 8 * (2 * N + P) + 8 * N + 16 * n
+    d2h = 8 * N + 8 * N + 16 * N + 24 + 24
+    grad_s = statistics.median(t_grad)
+    line = {
+        "metric": ADJ_METRIC, "value": round(grad_s, 3), "unit": "s", "n_gpus": 1, "steps": reps,
+        "warmup": max(0, args.adjoint_warmup), "ms_per_step": round(1e3 * grad_s, 1), "higher_is_better": False,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded DFG channel mesh, h=0.01; inflow coefficients seeded N(0, 0.01^2))",
+        "config": {"workload": f"adjoint drag gradient: DFG channel h={ADJ_H}, Umax=1.0, nu={ADJ_NU}, tau={ADJ_TAU}, "
+                               f"{n} steps from rest, J = mean c_D over the last {n - n // 2} steps, "
+                               f"grad wrt nu + 16 inflow sine coefficients",
+                   "N": N, "P": P, "checkpoint_interval": args.adjoint_checkpoint, "solve_tol": ADJ_TOL,
+                   "l2": "no flush: one step is a whole gradient (seconds), its working set re-read thousands of times"},
+        "e2e": {"value": round(statistics.median(t_e2e), 3), "unit": "s", "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h},
+        "gpu_launches": int(launches),
+        "breakdown": {"forward_s": round(statistics.median(t_fwd), 3), "reverse_s": round(statistics.median(t_rev), 3),
+                      "recomputed_steps": int(st["recomputed_steps"]), "reverse_steps": int(st["reverse_steps"]),
+                      "adjoint_mass_cg_iters": int(st["mass_iters"]), "adjoint_pressure_cg_iters": int(st["pres_iters"]),
+                      "state_bytes": int(st["state_bytes"]), "forward_ms_per_step": round(statistics.median(t_fwd) * 1e3 / n, 3)},
+        "gradient": {"J": J, "dJ_dnu": gnu, "dJ_dtheta": [float(x) for x in gth]},
+        "fd_check_eps_1e-6": fd,
+        "variants": variants,
+        "cpu_baseline": {"value": round(cpu_t * n / k, 1), "unit": "s", "cores": 1, "kind": "port",
+                         "sample": f"FP64 C oracle forward + adjoint over the first {k} steps from rest, scaled by "
+                                   f"{n}/{k} to the {n}-step gradient (the oracle keeps every state)"},
+        "gpu_vs_cpu_adjoint_sample": {"steps": k, "J_rel": abs(Js - Jo) / abs(Jo), "dnu_rel": abs(gnus - gnuo) / abs(gnuo),
+                                      "dtheta_rel_l2": float(np.linalg.norm(gths - gtho) / np.linalg.norm(gtho))},
+    }
+    if clocks:
+        line["clocks"] = clocks
+    return line
+
+
 def bench_batch(args):
     """Batched instances: B independent channel flows on one h = 0.01 mesh, U_max ~ U[0.2, 1.5]
     (peak = 4 U_max) and nu ~ logU[5e-4, 2e-3] from seed 0, tau = 2e-4 (the explicit scheme's
@@ -621,9 +752,18 @@ def main():
     ap.add_argument("--cpu-sample-steps", type=int, default=3)
     ap.add_argument("--no-accuracy", dest="accuracy", action="store_false",
                     help="skip the untimed mixed-vs-FP64 field and drag/lift comparison")
-    ap.add_argument("--workload", default="channel", choices=["channel", "poisson", "small", "batch"],
+    ap.add_argument("--workload", default="channel", choices=["channel", "poisson", "small", "batch", "adjoint"],
                     help="channel: the h=0.005 time step (default); poisson: the standalone 1M-DOF pressure "
-                         "solve; small: the plain FP64 h=0.02 channel")
+                         "solve; small: the plain FP64 h=0.02 channel; batch: 64 instances at h=0.01; "
+                         "adjoint: the drag gradient at h=0.01 over 1000 steps")
+    ap.add_argument("--adjoint-steps", type=int, default=1000)
+    ap.add_argument("--adjoint-checkpoint", type=int, default=50)
+    ap.add_argument("--adjoint-reps", type=int, default=1, help="timed gradient evaluations")
+    ap.add_argument("--adjoint-warmup", type=int, default=1, help="untimed gradient evaluations")
+    ap.add_argument("--adjoint-cpu-steps", type=int, default=6)
+    ap.add_argument("--adjoint-fd-coefs", type=int, nargs="*", default=[1],
+                    help="inflow coefficients (1..16) checked by central differences besides nu")
+    ap.add_argument("--no-adjoint-variants", dest="adjoint_variants", action="store_false")
     ap.add_argument("--small-steps", type=int, default=2000)
     ap.add_argument("--small-cpu-steps", type=int, default=100)
     ap.add_argument("--batch", type=int, default=64)
@@ -635,9 +775,40 @@ def main():
     rank = int(os.environ.get("RANK", "0"))
     local_rank = int(os.environ.get("LOCAL_RANK", "0"))
 
-    if args.workload in ("poisson", "small", "batch"):
+    if args.workload == "adjoint" and args.impl == "reference":
+        if rank != 0:
+            return
+        import numpy as np
+        tmp = tempfile.mkdtemp()
+        try:
+            path = make_mesh(tmp, ADJ_H, 0)
+            import oracle
+            oracle.build()
+            om = oracle.Mesh(path)
+            oc = oracle.Context(om, ADJ_PEAK, True)
+            xy = om.v_xy.astype(np.float64)[oc.dir_ids]
+            inflow = np.abs(xy[:, 0]) < 1e-9
+            basis = np.where(inflow[:, None], np.sin(np.pi * np.outer(xy[:, 1], np.arange(1, 17)) / 0.41), 0.0)
+            theta = 0.01 * np.random.default_rng(0).standard_normal(16)
+            k = max(1, args.adjoint_cpu_steps)
+            cpu_t, _, _, _ = _adjoint_oracle_sample(path, k, theta, basis, oc.dir_vx.copy(),
+                                                    2.0 / ((ADJ_PEAK / 6.0) ** 2 * 0.1))
+        finally:
+            shutil.rmtree(tmp, ignore_errors=True)
+        v = round(cpu_t * args.adjoint_steps / k, 1)
+        print(json.dumps({"impl": "reference", "metric": ADJ_METRIC, "value": v, "unit": "s", "n_gpus": 0,
+                          "steps": 1, "warmup": 0, "higher_is_better": False, "dtype": "f64",
+                          "config": {"workload": "adjoint drag gradient, DFG channel h=0.01, 1000 steps"},
+                          "cpu_baseline": {"value": v, "unit": "s", "cores": 1, "kind": "port",
+                                           "sample": f"FP64 C oracle forward + adjoint over {k} steps, scaled to "
+                                                     f"{args.adjoint_steps}"},
+                          "e2e": {"value": v, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}))
+        return
+
+    if args.workload in ("poisson", "small", "batch", "adjoint"):
         if rank == 0 and args.impl == "ours":
-            fn = {"poisson": bench_poisson, "small": bench_small, "batch": bench_batch}[args.workload]
+            fn = {"poisson": bench_poisson, "small": bench_small, "batch": bench_batch,
+                  "adjoint": bench_adjoint}[args.workload]
             print(json.dumps(fn(args)))
         return
 

@@ -7,7 +7,8 @@ same discrete forward map.  The product API is the C ABI (``Adjoint``); this wra
 gradient checks.
 
 The functional: J = sum_n w[n] c_D(u_n, p_n), c_D = 2 F_x / (U_mean^2 D) the drag coefficient of the
-cylinder (D = 0.1, U_mean = 2/3 of the peak inflow velocity), u_n, p_n the state after step n,
+cylinder (D = 0.1; the context's inflow is peak * y (H - y) / H^2, so U_max = peak / 4 and
+U_mean = 2/3 U_max = peak / 6), u_n, p_n the state after step n,
 starting from rest with the perturbed inflow imposed.  The inflow x values are
 g(y) = g0(y) + sum_k theta_k sin(k pi y / H) on the nodes at x = 0 (H = 0.41), g0 the parabolic
 profile of the context (the reference's, cpp/execs/NavierStokes/src/buildContext.cpp:64-93).
@@ -37,7 +38,7 @@ class DragProblem:
         self.forces = Forces(mesh, self.stepper)
         self.adjoint = Adjoint(self.stepper, self.forces, checkpoint_interval=checkpoint_interval,
                                max_iters=max_iters, tol=tol)
-        u_mean = 2.0 * peak / 3.0
+        u_mean = peak / 6.0
         self.scale = 2.0 / (u_mean * u_mean * D_CYLINDER)
         self.w = np.ascontiguousarray(np.broadcast_to(np.asarray(weights, np.float64), (self.n_steps,))) * self.scale
         xy = mesh.arrays()[2].astype(np.float64)[ctx.dir_ids]

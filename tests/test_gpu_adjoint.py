@@ -14,7 +14,7 @@ import pytest
 
 pytestmark = pytest.mark.gpu
 
-NU, TAU, PEAK = 1e-3, 5e-4, 1.0
+NU, TAU, PEAK = 1e-3, 5e-4, 4.0  # U_max = PEAK / 4 = 1.0
 
 
 @pytest.fixture(scope="module")
