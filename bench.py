@@ -319,20 +319,22 @@ def bench_adjoint(args):
         # central differences of the GPU forward run
         eps = 1e-6
         fd = {}
-        fnu = (prob.value(ADJ_NU + eps, theta) - prob.value(ADJ_NU - eps, theta)) / (2 * eps)
-        fd["nu"] = {"adjoint": gnu, "fd": fnu, "rel_err": abs(fnu - gnu) / abs(gnu)}
-        for k in args.adjoint_fd_coefs:
-            e = np.zeros(16)
-            e[k - 1] = eps
-            fk = (prob.value(ADJ_NU, theta + e) - prob.value(ADJ_NU, theta - e)) / (2 * eps)
-            fd[f"theta_{k}"] = {"adjoint": float(gth[k - 1]), "fd": fk,
-                                "rel_err": abs(fk - gth[k - 1]) / abs(gth[k - 1])}
+        if args.adjoint_fd:
+            fnu = (prob.value(ADJ_NU + eps, theta) - prob.value(ADJ_NU - eps, theta)) / (2 * eps)
+            fd["nu"] = {"adjoint": gnu, "fd": fnu, "rel_err": abs(fnu - gnu) / abs(gnu)}
+            for k in args.adjoint_fd_coefs:
+                e = np.zeros(16)
+                e[k - 1] = eps
+                fk = (prob.value(ADJ_NU, theta + e) - prob.value(ADJ_NU, theta - e)) / (2 * eps)
+                fd[f"theta_{k}"] = {"adjoint": float(gth[k - 1]), "fd": fk,
+                                    "rel_err": abs(fk - gth[k - 1]) / abs(gth[k - 1])}
         # the FP64 CPU adjoint on a bounded sample (first k steps, all weighted) vs the GPU adjoint
-        k = max(1, args.adjoint_cpu_steps)
-        cpu_t, Jo, gnuo, gtho = _adjoint_oracle_sample(path, k, theta, prob.basis, prob.g0, prob.scale)
-        small = GC.DragProblem(mesh, ctx, ADJ_PEAK, ADJ_NU, ADJ_TAU, k, np.full(k, 1.0 / k), n_coef=16, tol=ADJ_TOL,
-                               checkpoint_interval=0)
-        Js, gnus, gths, _ = small.gradient(ADJ_NU, theta)
+        k = args.adjoint_cpu_steps
+        if k > 0:
+            cpu_t, Jo, gnuo, gtho = _adjoint_oracle_sample(path, k, theta, prob.basis, prob.g0, prob.scale)
+            small = GC.DragProblem(mesh, ctx, ADJ_PEAK, ADJ_NU, ADJ_TAU, k, np.full(k, 1.0 / k), n_coef=16,
+                                   tol=ADJ_TOL, checkpoint_interval=0)
+            Js, gnus, gths, _ = small.gradient(ADJ_NU, theta)
     finally:
         shutil.rmtree(tmp, ignore_errors=True)
     N, P = ctx.N, ctx.P
@@ -359,12 +361,14 @@ def bench_adjoint(args):
         "gradient": {"J": J, "dJ_dnu": gnu, "dJ_dtheta": [float(x) for x in gth]},
         "fd_check_eps_1e-6": fd,
         "variants": variants,
-        "cpu_baseline": {"value": round(cpu_t * n / k, 1), "unit": "s", "cores": 1, "kind": "port",
-                         "sample": f"FP64 C oracle forward + adjoint over the first {k} steps from rest, scaled by "
-                                   f"{n}/{k} to the {n}-step gradient (the oracle keeps every state)"},
-        "gpu_vs_cpu_adjoint_sample": {"steps": k, "J_rel": abs(Js - Jo) / abs(Jo), "dnu_rel": abs(gnus - gnuo) / abs(gnuo),
-                                      "dtheta_rel_l2": float(np.linalg.norm(gths - gtho) / np.linalg.norm(gtho))},
     }
+    if k > 0:
+        line["cpu_baseline"] = {"value": round(cpu_t * n / k, 1), "unit": "s", "cores": 1, "kind": "port",
+                                "sample": f"FP64 C oracle forward + adjoint over the first {k} steps from rest, scaled "
+                                          f"by {n}/{k} to the {n}-step gradient (the oracle keeps every state)"}
+        line["gpu_vs_cpu_adjoint_sample"] = {"steps": k, "J_rel": abs(Js - Jo) / abs(Jo),
+                                             "dnu_rel": abs(gnus - gnuo) / abs(gnuo),
+                                             "dtheta_rel_l2": float(np.linalg.norm(gths - gtho) / np.linalg.norm(gtho))}
     if clocks:
         line["clocks"] = clocks
     return line
@@ -764,6 +768,8 @@ def main():
     ap.add_argument("--adjoint-fd-coefs", type=int, nargs="*", default=[1],
                     help="inflow coefficients (1..16) checked by central differences besides nu")
     ap.add_argument("--no-adjoint-variants", dest="adjoint_variants", action="store_false")
+    ap.add_argument("--no-adjoint-fd", dest="adjoint_fd", action="store_false",
+                    help="skip the central-difference check")
     ap.add_argument("--small-steps", type=int, default=2000)
     ap.add_argument("--small-cpu-steps", type=int, default=100)
     ap.add_argument("--batch", type=int, default=64)
