@@ -281,8 +281,10 @@ def bench_adjoint(args):
         ctx = G.build_chorin_context(mesh, ADJ_PEAK)
         w = np.zeros(n)
         w[n // 2:] = 1.0 / (n - n // 2)
+        precs = {"f64": G.NSF_PREC_F64, "mixedsolve": G.NSF_PREC_F64_MIXEDSOLVE}
+        prec = precs[args.adjoint_precision]
         prob = GC.DragProblem(mesh, ctx, ADJ_PEAK, ADJ_NU, ADJ_TAU, n, w, n_coef=16, tol=ADJ_TOL,
-                              checkpoint_interval=args.adjoint_checkpoint)
+                              checkpoint_interval=args.adjoint_checkpoint, precision=prec)
         theta = 0.01 * np.random.default_rng(0).standard_normal(16)
         launches0 = G.kernel_launches()
         for _ in range(max(0, args.adjoint_warmup)):
@@ -305,17 +307,21 @@ def bench_adjoint(args):
         st = prob.adjoint.stats()
         variants = {}
         if args.adjoint_variants:
-            keep = GC.DragProblem(mesh, ctx, ADJ_PEAK, ADJ_NU, ADJ_TAU, n, w, n_coef=16, tol=ADJ_TOL,
-                                  checkpoint_interval=0)
-            Jk, gnuk, gthk, _ = keep.gradient(ADJ_NU, theta)
-            sk = keep.adjoint.stats()
-            variants["keep_all_states"] = {
-                "gradient_s": round((sk["forward_ms"] + sk["reverse_ms"]) / 1e3, 3),
-                "forward_s": round(sk["forward_ms"] / 1e3, 3), "reverse_s": round(sk["reverse_ms"] / 1e3, 3),
-                "state_bytes": int(sk["state_bytes"]),
-                "max_rel_diff_vs_checkpointed": float(max(abs(gnuk - gnu) / abs(gnu),
+            other = [p for p in precs if p != args.adjoint_precision][0]
+            for name, ck, pr in (("keep_all_states", 0, prec),
+                                 (f"precision_{other}", args.adjoint_checkpoint, precs[other])):
+                var = GC.DragProblem(mesh, ctx, ADJ_PEAK, ADJ_NU, ADJ_TAU, n, w, n_coef=16, tol=ADJ_TOL,
+                                     checkpoint_interval=ck, precision=pr)
+                Jk, gnuk, gthk, _ = var.gradient(ADJ_NU, theta)
+                sk = var.adjoint.stats()
+                variants[name] = {
+                    "gradient_s": round((sk["forward_ms"] + sk["reverse_ms"]) / 1e3, 3),
+                    "forward_s": round(sk["forward_ms"] / 1e3, 3), "reverse_s": round(sk["reverse_ms"] / 1e3, 3),
+                    "state_bytes": int(sk["state_bytes"]), "checkpoint_interval": ck,
+                    "adjoint_pressure_cg_iters": int(sk["pres_iters"]), "adjoint_mass_cg_iters": int(sk["mass_iters"]),
+                    "max_rel_diff_vs_headline": float(max(abs(gnuk - gnu) / abs(gnu),
                                                           np.abs(gthk - gth).max() / np.abs(gth).max()))}
-            del keep
+                del var
         # central differences of the GPU forward run
         eps = 1e-6
         fd = {}
@@ -333,7 +339,7 @@ def bench_adjoint(args):
         if k > 0:
             cpu_t, Jo, gnuo, gtho = _adjoint_oracle_sample(path, k, theta, prob.basis, prob.g0, prob.scale)
             small = GC.DragProblem(mesh, ctx, ADJ_PEAK, ADJ_NU, ADJ_TAU, k, np.full(k, 1.0 / k), n_coef=16,
-                                   tol=ADJ_TOL, checkpoint_interval=0)
+                                   tol=ADJ_TOL, checkpoint_interval=0, precision=prec)
             Js, gnus, gths, _ = small.gradient(ADJ_NU, theta)
     finally:
         shutil.rmtree(tmp, ignore_errors=True)
@@ -350,6 +356,9 @@ def bench_adjoint(args):
                                f"{n} steps from rest, J = mean c_D over the last {n - n // 2} steps, "
                                f"grad wrt nu + 16 inflow sine coefficients",
                    "N": N, "P": P, "checkpoint_interval": args.adjoint_checkpoint, "solve_tol": ADJ_TOL,
+                   "precision": {"f64": "FP64 operators and solves",
+                                 "mixedsolve": "FP64 operators and state; FP32 CG inside FP64 residual replacement / "
+                                               "refinement to the same FP64 tolerance"}[args.adjoint_precision],
                    "l2": "no flush: one step is a whole gradient (seconds), its working set re-read thousands of times"},
         "e2e": {"value": round(statistics.median(t_e2e), 3), "unit": "s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h},
@@ -762,6 +771,7 @@ def main():
                          "adjoint: the drag gradient at h=0.01 over 1000 steps")
     ap.add_argument("--adjoint-steps", type=int, default=1000)
     ap.add_argument("--adjoint-checkpoint", type=int, default=50)
+    ap.add_argument("--adjoint-precision", default="f64", choices=["f64", "mixedsolve"])
     ap.add_argument("--adjoint-reps", type=int, default=1, help="timed gradient evaluations")
     ap.add_argument("--adjoint-warmup", type=int, default=1, help="untimed gradient evaluations")
     ap.add_argument("--adjoint-cpu-steps", type=int, default=6)

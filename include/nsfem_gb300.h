@@ -37,7 +37,10 @@ typedef enum
 typedef enum
 {
     NSF_PREC_F64 = 0,   /* everything in FP64 */
-    NSF_PREC_MIXED = 1  /* FP32 SpMV/sweeps/inner CG, FP64 residual refinement, dots and state */
+    NSF_PREC_MIXED = 1, /* FP32 SpMV/sweeps/inner CG, FP64 residual refinement, dots and state */
+    NSF_PREC_F64_MIXEDSOLVE = 2 /* stepper only: FP64 operators and state (the FP64 step), every
+                                   solve FP32 CG inside FP64 refinement / residual replacement,
+                                   stopping on the same FP64 residual test as NSF_PREC_F64 */
 } nsf_precision;
 
 const char *nsf_last_error(void);

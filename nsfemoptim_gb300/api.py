@@ -22,7 +22,8 @@ import ctypes as C
 
 import numpy as np
 
-from ._lib import (NSF_F32, NSF_F64, NSF_PREC_F64, NSF_PREC_MIXED, ChorinConfig, NsfError, check, lib, vp)
+from ._lib import (NSF_F32, NSF_F64, NSF_PREC_F64, NSF_PREC_F64_MIXEDSOLVE, NSF_PREC_MIXED, ChorinConfig, NsfError,
+                   check, lib, vp)
 
 
 def _i32(a):
@@ -472,4 +473,5 @@ class Adjoint:
 
 __all__ = ["Mesh", "load_gmsh", "ChorinContext", "build_chorin_context", "coloring", "CsrF", "Spmv", "Spmm",
            "spmv", "spmm", "fastconv_apply", "AbstractSolver", "create_solver", "ChorinStepper", "kernel_launches",
-           "Forces", "Adjoint", "NSF_F32", "NSF_F64", "NSF_PREC_F64", "NSF_PREC_MIXED", "NsfError"]
+           "Forces", "Adjoint", "NSF_F32", "NSF_F64", "NSF_PREC_F64", "NSF_PREC_MIXED", "NSF_PREC_F64_MIXEDSOLVE",
+           "NsfError"]

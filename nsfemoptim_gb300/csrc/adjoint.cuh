@@ -238,7 +238,8 @@ namespace
         }
     }
 
-    // tally[0] = max(tally[0], status of every channel); tally[1] += iterations (if iters != 0)
+    // tally[0] = max(tally[0], status of every channel); tally[1] += CG iterations when iters is 1
+    // (a plain solve's count) or 2 (the inner FP32 iterations of a refinement solve)
     __global__ void kTally(const SolverState * st, int numCh, int * tally, int iters)
     {
         if (blockIdx.x != 0 || threadIdx.x != 0)
@@ -247,8 +248,10 @@ namespace
         {
             if (st->status[c] > tally[0])
                 tally[0] = st->status[c];
-            if (iters)
+            if (iters == 1)
                 tally[1] += st->iters[c];
+            else if (iters == 2)
+                tally[1] += st->innerTotal[c];
         }
     }
 
@@ -284,6 +287,8 @@ struct nsf_adjoint_s
     DevBuf<double> ckU, ckP, segU, finU, finP;
     PcgSolver<double, 2> mass;
     PcgSolver<double, 1> pres;
+    MixedPcg<2> mmass; // the solves of a NSF_PREC_F64_MIXEDSOLVE stepper: FP32 CG, FP64 residuals
+    MixedPcg<1> mpres;
     cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
     std::vector<double> hwD, hwL;
     double stats[10] = {0};
@@ -305,8 +310,44 @@ struct nsf_adjoint_s
     {
         const SolverState * st[3] = {S->cfg.velMethod == 0 ? S->gsT.st.get() : S->velT.st.get(), S->pres.st.get(),
                                      S->cfg.velMethod == 0 ? S->gsF.st.get() : S->velF.st.get()};
+        if (S->mixedSolve)
+        {
+            st[0] = S->mvelT.st.get();
+            st[1] = S->mpres.st.get();
+            st[2] = S->mvelF.st.get();
+        }
         for (int k = 0; k < 3; k++)
             NSF_LAUNCH(kTally, 1, s, st[k], k == 1 ? 1 : 2, tally.get(), 0);
+    }
+
+    // M x = rhs (two channels, x from zero) and Kpi y = lpI (y warm), tallied
+    void massSolve(cudaStream_t s)
+    {
+        NSF_CUDA(cudaMemsetAsync(x.get(), 0, sizeof(double) * 2 * N, s));
+        if (S->mixedSolve)
+        {
+            mmass.enqueue(s, S->body, rhs.get(), x.get(), S->cfg.maxOuter, cfg.tol, cfg.maxIters, S->cfg.innerTol, 1);
+            NSF_LAUNCH(kTally, 1, s, mmass.st.get(), 2, tally.get() + 2, 2);
+        }
+        else
+        {
+            mass.enqueue(s, S->body, rhs.get(), x.get(), cfg.maxIters, cfg.tol, false, 1);
+            NSF_LAUNCH(kTally, 1, s, mass.st.get(), 2, tally.get() + 2, 1);
+        }
+    }
+
+    void presSolve(cudaStream_t s)
+    {
+        if (S->mixedSolve)
+        {
+            mpres.enqueue(s, S->body, lpI.get(), y.get(), S->cfg.maxOuter, cfg.tol, cfg.maxIters, S->cfg.innerTol, 1);
+            NSF_LAUNCH(kTally, 1, s, mpres.st.get(), 1, tally.get() + 4, 2);
+        }
+        else
+        {
+            pres.enqueue(s, S->body, lpI.get(), y.get(), cfg.maxIters, cfg.tol, false, 1);
+            NSF_LAUNCH(kTally, 1, s, pres.st.get(), 1, tally.get() + 4, 1);
+        }
     }
 
     void copyDev(double * dst, const double * src, size_t n, cudaStream_t s)
@@ -320,20 +361,14 @@ struct nsf_adjoint_s
     {
         const double nu = S->cfg.nu, tau = S->cfg.tau;
         const double cx = hwD[n], cy = hwL[n];
-        const int maxIt = cfg.maxIters;
         NSF_LAUNCH(kAdjSeed, blocksFor(std::max(N, nI)), s, N, nI, lam.get(), lw.get(), rhs.get(), S->isDir.get(),
                    lDir.get(), wV.get(), wPx.get(), wPy.get(), lpI.get(), cx * nu, cy * nu, cx, cy, tau);
-        NSF_CUDA(cudaMemsetAsync(x.get(), 0, sizeof(double) * 2 * N, s));
-        mass.enqueue(s, S->body, rhs.get(), x.get(), maxIt, cfg.tol, false, 1);
-        NSF_LAUNCH(kTally, 1, s, mass.st.get(), 2, tally.get() + 2, 1);
+        massSolve(s);
         spmvF64(GT, x.get(), lpI.get(), 1.0, 1.0, s);
-        pres.enqueue(s, S->body, lpI.get(), y.get(), maxIt, cfg.tol, false, 1);
-        NSF_LAUNCH(kTally, 1, s, pres.st.get(), 1, tally.get() + 4, 1);
+        presSolve(s);
         spmvF64(DT, y.get(), lw.get(), -1.0 / tau, 1.0, s);
         NSF_LAUNCH(kAdjDirichlet, blocksFor(N), s, N, lw.get(), rhs.get(), S->isDir.get(), lDir.get(), tau);
-        NSF_CUDA(cudaMemsetAsync(x.get(), 0, sizeof(double) * 2 * N, s));
-        mass.enqueue(s, S->body, rhs.get(), x.get(), maxIt, cfg.tol, false, 1);
-        NSF_LAUNCH(kTally, 1, s, mass.st.get(), 2, tally.get() + 2, 1);
+        massSolve(s);
         NSF_LAUNCH((kFastConvStream<double, double, double, double>), S->I64.nBlocks, s, S->I64.rb.get(),
                    S->I64.rs.get(), S->I64.ci.get(), S->I64.v.get(), u0, S->K64.get(), nu, A.get());
         const SweepSystem<double> & M = S->M64;
@@ -447,7 +482,7 @@ extern "C" int nsf_adjoint_create(nsf_chorin S, nsf_forces f, const nsf_adjoint_
     return guarded([&] {
         require(S && f && out, "null argument");
         require(f->s == S, "the force functional belongs to another stepper");
-        require(!S->mixed, "the adjoint needs an FP64 stepper (precision NSF_PREC_F64)");
+        require(!S->mixed, "the adjoint needs FP64 operators (precision NSF_PREC_F64 or NSF_PREC_F64_MIXEDSOLVE)");
         require(S->I64.nBlocks > 0, "FastConvection rows too long for the stream kernel");
         auto a = std::make_unique<nsf_adjoint_s>();
         if (cfg)
@@ -493,8 +528,16 @@ extern "C" int nsf_adjoint_create(nsf_chorin S, nsf_forces f, const nsf_adjoint_
         a->tally = DevBuf<int>(6);
         a->finU.alloc(twoN);
         a->finP.alloc(nI);
-        a->mass.setup(&S->M64, 2);
-        a->pres.setup(&S->Kpi64, 1);
+        if (S->mixedSolve)
+        {
+            a->mmass.setup(&S->M64, &S->M32, 2);
+            a->mpres.setup(&S->Kpi64, &S->Kpi32, 1);
+        }
+        else
+        {
+            a->mass.setup(&S->M64, 2);
+            a->pres.setup(&S->Kpi64, 1);
+        }
         for (cudaEvent_t & e : a->ev)
             NSF_CUDA(cudaEventCreate(&e));
         NSF_CUDA(cudaStreamSynchronize(S->stream));

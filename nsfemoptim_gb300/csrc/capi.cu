@@ -680,7 +680,8 @@ extern "C" void nsf_solver_destroy(nsf_solver s) { delete s; }
 struct nsf_chorin_s
 {
     nsf_chorin_config cfg{};
-    bool mixed = false;
+    bool mixed = false;      // FP32 operators and FP32-inner solves
+    bool mixedSolve = false; // FP64 operators, FP32-inner solves (NSF_PREC_F64_MIXEDSOLVE)
     int N = 0, P = 0, nIntP = 0;
     std::vector<int> permV, permP, intP;
     std::vector<int> dirRows; // stepper row of each Dirichlet node (context dirIds order)
@@ -737,7 +738,7 @@ struct nsf_chorin_s
         double * b = rhs.get();
         double * x = acc.get();
         NSF_CUDA(cudaMemsetAsync(x, 0, sizeof(double) * 2 * N, s));
-        if (mixed)
+        if (mixed || mixedSolve)
             (tentative ? mvelT : mvelF)
                 .enqueue(s, body, b, x, cfg.maxOuter, cfg.velTol, cfg.velMaxIters, cfg.innerTol, cfg.checkInterval);
         else if (cfg.velMethod == 0)
@@ -785,7 +786,12 @@ struct nsf_chorin_s
             NSF_LANES(D64.L, NSF_LAUNCH((kSpmv<double, double, double, double, LL>),
                                         blocksFor((long long)nIntP * D64.L), s, nIntP, D64.rs.get(), D64.ci.get(),
                                         D64.v.get(), u.get(), rhsP.get(), invTau, 0.0));
-            pres.enqueue(s, body, rhsP.get(), pInt.get(), cfg.presMaxIters, cfg.presTol, false, cfg.checkInterval);
+            if (mixedSolve)
+                mpres.enqueue(s, body, rhsP.get(), pInt.get(), cfg.maxOuter, cfg.presTol, cfg.presMaxIters,
+                              cfg.innerTol, cfg.checkInterval);
+            else
+                pres.enqueue(s, body, rhsP.get(), pInt.get(), cfg.presMaxIters, cfg.presTol, false,
+                             cfg.checkInterval);
             NSF_LANES(G64.L, NSF_LAUNCH((kSpmv<double, double, double, double, LL>),
                                         blocksFor((long long)2 * N * G64.L), s, 2 * N, G64.rs.get(), G64.ci.get(),
                                         G64.v.get(), pInt.get(), rhs.get(), 1.0, 0.0));
@@ -799,7 +805,8 @@ struct nsf_chorin_s
     void collectStats(cudaStream_t s)
     {
         const SolverState * src[3];
-        if (mixed)
+        const bool inner = mixed || mixedSolve;
+        if (inner)
         {
             src[0] = mvelT.st.get();
             src[1] = mpres.st.get();
@@ -823,7 +830,7 @@ struct nsf_chorin_s
             double rel = 0;
             for (int c = 0; c < nch; c++)
             {
-                it = std::max(it, mixed ? L.innerTotal[c] : L.iters[c]);
+                it = std::max(it, inner ? L.innerTotal[c] : L.iters[c]);
                 const double r = L.bb[c] > 0 ? std::sqrt(std::max(0.0, L.lastRR[c]) / L.bb[c]) : 0.0;
                 rel = std::max(rel, r);
                 worst = std::max(worst, L.status[c]);
@@ -833,7 +840,7 @@ struct nsf_chorin_s
             stats[idxIt[i]] = it;
             stats[idxRel[i]] = rel;
             if (i == 1)
-                stats[6] = mixed ? L.iters[0] : 0;
+                stats[6] = inner ? L.iters[0] : 0;
         }
         stats[7] = worst;
     }
@@ -918,17 +925,29 @@ static void buildChorin(nsf_chorin_s & S, const Context & c)
         S.G64.upload(Gp);
         S.K64.upload(knu);
         S.A64.alloc(knu.size());
-        if (S.cfg.velMethod == 0)
+        if (S.mixedSolve)
         {
-            S.gsT.setup(&S.M64, 2, 1);
-            S.gsF.setup(&S.M64, 2, 1);
+            // FP64 operators, FP32-inner solves on FP32 copies of the two systems
+            S.M32.build(Mp, cv.partStart);
+            S.Kpi32.build(Kpip, cp.partStart);
+            S.mvelT.setup(&S.M64, &S.M32, 2);
+            S.mvelF.setup(&S.M64, &S.M32, 2);
+            S.mpres.setup(&S.Kpi64, &S.Kpi32, 1);
         }
         else
         {
-            S.velT.setup(&S.M64, 2);
-            S.velF.setup(&S.M64, 2);
+            if (S.cfg.velMethod == 0)
+            {
+                S.gsT.setup(&S.M64, 2, 1);
+                S.gsF.setup(&S.M64, 2, 1);
+            }
+            else
+            {
+                S.velT.setup(&S.M64, 2);
+                S.velF.setup(&S.M64, 2);
+            }
+            S.pres.setup(&S.Kpi64, 1);
         }
-        S.pres.setup(&S.Kpi64, 1);
     }
     // Dirichlet rows in the colored numbering
     std::vector<unsigned char> isDir(N, 0);
@@ -958,7 +977,11 @@ extern "C" int nsf_chorin_create(nsf_context ctx, const nsf_chorin_config * cfg,
     return guarded([&] {
         require(ctx && cfg && out, "null argument");
         require(cfg->tau > 0 && cfg->nu >= 0, "tau must be > 0 and nu >= 0");
-        require(cfg->precision == NSF_PREC_F64 || cfg->precision == NSF_PREC_MIXED, "unknown precision");
+        require(cfg->precision == NSF_PREC_F64 || cfg->precision == NSF_PREC_MIXED ||
+                    cfg->precision == NSF_PREC_F64_MIXEDSOLVE,
+                "unknown precision");
+        require(!(cfg->precision == NSF_PREC_F64_MIXEDSOLVE && cfg->velMethod == 0),
+                "mixed solves use velMethod 1 (pcg)");
         require(cfg->velMethod == 0 || cfg->velMethod == 1, "velMethod must be 0 (gs) or 1 (pcg)");
         require(!(cfg->precision == NSF_PREC_MIXED && cfg->velMethod == 0), "mixed precision uses velMethod 1 (pcg)");
         require(cfg->velMaxIters >= 1 && cfg->presMaxIters >= 1, "iteration caps must be >= 1");
@@ -971,6 +994,7 @@ extern "C" int nsf_chorin_create(nsf_context ctx, const nsf_chorin_config * cfg,
         if (!(S->cfg.innerTol > 0))
             S->cfg.innerTol = 1e-4;
         S->mixed = cfg->precision == NSF_PREC_MIXED;
+        S->mixedSolve = cfg->precision == NSF_PREC_F64_MIXEDSOLVE;
         buildChorin(*S, ctx->c);
         NSF_CUDA(cudaStreamCreateWithFlags(&S->stream, cudaStreamNonBlocking));
         NSF_CUDA(cudaStreamCreateWithFlags(&S->body, cudaStreamNonBlocking));

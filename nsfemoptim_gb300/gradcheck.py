@@ -19,7 +19,7 @@ from __future__ import annotations
 import numpy as np
 import torch
 
-from .api import Adjoint, ChorinContext, ChorinStepper, Forces, Mesh
+from .api import NSF_PREC_F64, Adjoint, ChorinContext, ChorinStepper, Forces, Mesh
 
 H_CHANNEL = 0.41
 D_CYLINDER = 0.1
@@ -30,11 +30,16 @@ class DragProblem:
 
     def __init__(self, mesh: Mesh, ctx: ChorinContext, peak: float, nu: float, tau: float, n_steps: int,
                  weights, n_coef: int = 16, tol: float = 1e-13, checkpoint_interval: int = 50,
-                 max_iters: int = 20000):
+                 max_iters: int = 20000, precision: int = NSF_PREC_F64, max_outer: int = 6,
+                 inner_tol: float = 1e-5):
+        """precision: NSF_PREC_F64 (FP64 solves) or NSF_PREC_F64_MIXEDSOLVE (FP64 operators, FP32 CG
+        inside FP64 refinement / residual replacement to the same tolerance; max_outer passes with
+        inner tolerance inner_tol)."""
         self.mesh, self.ctx = mesh, ctx
         self.n_steps = int(n_steps)
-        self.stepper = ChorinStepper(ctx, nu, tau, vel_method=1, vel_max_iters=max_iters, vel_tol=tol,
-                                     pres_max_iters=max_iters, pres_tol=tol, use_graph=True)
+        self.stepper = ChorinStepper(ctx, nu, tau, precision=precision, vel_method=1, vel_max_iters=max_iters,
+                                     vel_tol=tol, pres_max_iters=max_iters, pres_tol=tol, use_graph=True,
+                                     max_outer=max_outer, inner_tol=inner_tol)
         self.forces = Forces(mesh, self.stepper)
         self.adjoint = Adjoint(self.stepper, self.forces, checkpoint_interval=checkpoint_interval,
                                max_iters=max_iters, tol=tol)

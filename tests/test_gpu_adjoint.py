@@ -40,9 +40,10 @@ def _rel(a, b):
     return float(np.linalg.norm(np.asarray(a) - np.asarray(b)) / max(np.linalg.norm(b), 1e-300))
 
 
-def _stepper(G, ctx, tol=1e-13):
-    return G.ChorinStepper(ctx, NU, TAU, vel_method=1, vel_max_iters=20000, vel_tol=tol, pres_max_iters=20000,
-                           pres_tol=tol, use_graph=True)
+def _stepper(G, ctx, tol=1e-13, precision=None):
+    prec = G.NSF_PREC_F64 if precision in (None, "f64") else G.NSF_PREC_F64_MIXEDSOLVE
+    return G.ChorinStepper(ctx, NU, TAU, precision=prec, vel_method=1, vel_max_iters=20000, vel_tol=tol,
+                           pres_max_iters=20000, pres_tol=tol, use_graph=True, max_outer=6, inner_tol=1e-5)
 
 
 def _start(rng, n_nodes):
@@ -52,15 +53,18 @@ def _start(rng, n_nodes):
     return u0
 
 
-def test_adjoint_matches_oracle_adjoint(adj_setup):
-    """Drag and lift weights on every step, a random initial velocity and perturbed inflow values."""
+@pytest.mark.parametrize("precision", ["f64", "mixedsolve"])
+def test_adjoint_matches_oracle_adjoint(adj_setup, precision):
+    """Drag and lift weights on every step, a random initial velocity and perturbed inflow values.
+    mixedsolve: FP64 operators with FP32-inner solves refined to the same FP64 tolerance, in the
+    forward step and in the adjoint solves."""
     G, O, mesh, ctx, om, oc = adj_setup
     rng = np.random.default_rng(11)
     n = 12
     wd, wl = rng.random(n), rng.standard_normal(n)
     u0 = _start(rng, ctx.N)
     dv = ctx.dir_vx + 0.01 * rng.standard_normal(len(ctx.dir_vx)) * (ctx.dir_vx != 0)
-    st = _stepper(G, ctx)
+    st = _stepper(G, ctx, precision=precision)
     f = G.Forces(mesh, st)
     adj = G.Adjoint(st, f, checkpoint_interval=0, tol=1e-13)
     st.set_state(u0, np.zeros(ctx.P))
@@ -85,6 +89,27 @@ def test_adjoint_matches_oracle_adjoint(adj_setup):
     for _ in range(n):
         ch.step()
     assert _rel(ue, ch.state()[0]) <= 1e-9
+
+
+def test_mixedsolve_step_matches_fp64_step(adj_setup):
+    """NSF_PREC_F64_MIXEDSOLVE keeps the FP64 step: its states follow the FP64 stepper's to the
+    solver tolerance (1e-12 here) over 6 steps; every solve reports convergence."""
+    G, O, mesh, ctx, om, oc = adj_setup
+    rng = np.random.default_rng(14)
+    u0 = _start(rng, ctx.N)
+    a, b = _stepper(G, ctx, 1e-12), _stepper(G, ctx, 1e-12, "mixedsolve")
+    for st in (a, b):
+        st.set_state(u0, np.zeros(ctx.P))
+        st.set_dirichlet(ctx.dir_vx)
+    for _ in range(6):
+        a.step(1)
+        b.step(1)
+        assert b.stats()["status"] == 0
+        assert max(b.stats()["tent_rel"], b.stats()["pres_rel"], b.stats()["final_rel"]) <= 1e-12
+    ua, pa = a.state()
+    ub, pb = b.state()
+    assert _rel(ub, ua) <= 1e-10
+    assert _rel(pb, pa) <= 1e-8
 
 
 def test_checkpointing_is_exact(adj_setup):
