@@ -247,7 +247,9 @@ typedef struct nsf_adjoint_s *nsf_adjoint;
      J = sum_{n=1..nSteps} wDrag[n-1] F_x(u_n, p_n) + wLift[n-1] F_y(u_n, p_n),
    u_n, p_n the state after step n.  Every linear solve of the step is taken as exact; the adjoint
    mass and pressure solves are CG with the multicolor SGS preconditioner on the stepper's systems
-   (both symmetric).  cfg may be NULL (defaults). */
+   (both symmetric); on an NSF_PREC_F64_MIXEDSOLVE stepper they are FP32 CG inside FP64 refinement,
+   to the same tolerance, and a refinement solve that used up its passes (the FP64 residual floor of
+   a tight tolerance) is reported in the stats, not as an error.  cfg may be NULL (defaults). */
 int nsf_adjoint_create(nsf_chorin s, nsf_forces f, const nsf_adjoint_config *cfg, nsf_adjoint *out);
 /* Run nSteps steps forward from the stepper's current state (whose Dirichlet rows hold the
    Dirichlet values), then the reverse sweep.  wDrag / wLift: nSteps host weights (NULL = 0).

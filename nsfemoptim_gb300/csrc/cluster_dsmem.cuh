@@ -297,6 +297,11 @@ namespace nsf
         double bb[NCH], rr[NCH], rz[NCH], rzPrev[NCH];
         int replace, replacements; // residual replacement due in this iteration; count
         double rrRef[NCH];         // ||r||^2 at the last replacement
+        // ru: the FP32 recurrence runs on gsc * (b - A x), gsc = 2^-e with 2^(e-1) <= ||b|| < 2^e:
+        // an exact power-of-two scale (the same bits as the unscaled recurrence, shifted), so that
+        // the FP32 residual and its dot products stay O(1) instead of underflowing for small ||b||
+        // or tight tolerances; the increment is scaled back (igsc) when it is folded into x64
+        double gsc[NCH], igsc[NCH];
     };
 
     template <typename T, int NCH, bool VALS>
@@ -417,7 +422,7 @@ namespace nsf
                         if (c < numCh)
                         {
                             double * px = A.x64 + (size_t)c * n + i;
-                            *px = __ldcg(px) + (double)xs[c * S + l];
+                            *px = __ldcg(px) + (double)xs[c * S + l] * sc.igsc[c];
                             xs[c * S + l] = (T)0;
                         }
                 }
@@ -456,10 +461,10 @@ namespace nsf
                                 for (int t = 0; t < DRB; t++)
                                     acc += v[t] * g[t];
                             }
-                            const double bi = ldg(A.b64 + (size_t)c * n + i);
-                            rsv[c * S + l] = (T)(bi - acc);
+                            const double bi = ldg(A.b64 + (size_t)c * n + i), g = sc.gsc[c];
+                            rsv[c * S + l] = (T)((bi - acc) * g);
                             if (withBb)
-                                bbAcc[c] += (T)bi * (T)bi;
+                                bbAcc[c] += (T)(bi * g) * (T)(bi * g);
                         }
                 }
         };
@@ -469,8 +474,41 @@ namespace nsf
 #pragma unroll
         for (int c = 0; c < NCH; c++)
             bbP[c] = (T)0;
+        if (threadIdx.x == 0)
+            for (int c = 0; c < NCH; c++)
+                sc.gsc[c] = sc.igsc[c] = 1.0;
         if (A.ru)
+        {
+            // ||b64||^2 in FP64 over the cluster -> the power-of-two scale of the FP32 recurrence
+            __shared__ double dslot[2][8];
+            double bq[NCH];
+#pragma unroll
+            for (int c = 0; c < NCH; c++)
+                bq[c] = 0.0;
+            for (int col = 0; col < C; col++)
+                for (int l = chunkL[col] + threadIdx.x; l < chunkL[col + 1]; l += DTPB)
+                {
+                    const int i = chunkA[col] + (l - chunkL[col]);
+#pragma unroll
+                    for (int c = 0; c < NCH; c++)
+                        if (c < numCh)
+                        {
+                            const double bi = ldg(A.b64 + (size_t)c * n + i);
+                            bq[c] += bi * bi;
+                        }
+                }
+            dsClusterSum<double, NCH>(cl, bq, dslot, buf, [&](const double (&tot)[NCH]) {
+                for (int c = 0; c < NCH; c++)
+                    if (tot[c] > 0.0 && isfinite(tot[c]))
+                    {
+                        int e = 0;
+                        frexp(sqrt(tot[c]), &e);
+                        sc.gsc[c] = ldexp(1.0, -e);
+                        sc.igsc[c] = ldexp(1.0, e);
+                    }
+            });
             trueResidual(bbP, true);
+        }
         else
         for (int col = 0; col < C; col++)
         {
@@ -598,7 +636,7 @@ namespace nsf
                 sc.rz[c] = rz;
                 sc.rzPrev[c] = rz;
                 const bool fin = isfinite(rr) && isfinite(bb);
-                const bool conv = absMode ? (rr < tol2) : (rr <= tol2 * bb);
+                const bool conv = absMode ? (rr * sc.igsc[c] * sc.igsc[c] < tol2) : (rr <= tol2 * bb);
                 sc.status[c] = fin ? 0 : 2;
                 sc.iters[c] = 0;
                 sc.act[c] = (c < numCh) && fin && !conv;
@@ -720,7 +758,8 @@ namespace nsf
                         sc.rr[c] = rr;
                         sc.rz[c] = rz;
                         const bool fin = isfinite(rr) && isfinite(rz);
-                        const bool conv = absMode ? (rr < tol2) : (rr <= tol2 * sc.bb[c]);
+                        const bool conv =
+                            absMode ? (rr * sc.igsc[c] * sc.igsc[c] < tol2) : (rr <= tol2 * sc.bb[c]);
                         // with replacement the solve stops only on an FP64 residual; a converged
                         // or sufficiently reduced iterated residual schedules a replacement
                         const bool stop = !fin || (conv && (!A.ru || replaced));
@@ -774,8 +813,9 @@ namespace nsf
                 st->iters[c] = A.ru ? sc.replacements : sc.iters[c];
                 if (A.ru)
                     st->innerTotal[c] = sc.iters[c];
-                st->bb[c] = sc.bb[c];
-                st->lastRR[c] = sc.rr[c];
+                // in the units of b (the ru recurrence runs scaled by gsc)
+                st->bb[c] = sc.bb[c] * sc.igsc[c] * sc.igsc[c];
+                st->lastRR[c] = sc.rr[c] * sc.igsc[c] * sc.igsc[c];
                 st->active[c] = 0;
             }
             st->iter = k;

@@ -393,6 +393,9 @@ namespace nsf
         // by every thread in the solve precision
         double alphaD[MAXCH], betaD[MAXCH];
         float alphaF[MAXCH], betaF[MAXCH];
+        // refinement: power-of-two scale of the pass's FP32 right-hand side (2^-e, ||r|| ~ 2^e) and
+        // its inverse, so that the inner FP32 solve works on O(1) values whatever ||r|| is
+        double rscale[MAXCH], rinv[MAXCH];
     };
 
     __device__ __forceinline__ void loadScalar(float & v, const double *, const float * f, int c) { v = f[c]; }
@@ -1093,6 +1096,27 @@ namespace nsf
         gridSum<double, 2 * NCH>(red, scratch, o, &st->ticket, nullptr);
     }
 
+    // refinement pass: r32 *= rscale (exact: a power of two), skipped once the loop has stopped
+    template <int NCH>
+    __global__ void __launch_bounds__(TPB) kScalePass(int n, float * __restrict__ r32, const SolverState * st)
+    {
+        if (st->skip)
+            return;
+        for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < NCH * n; i += gridDim.x * blockDim.x)
+            r32[i] = (float)((double)r32[i] * st->rscale[i / n]);
+    }
+
+    // refinement update x64 += d / rscale
+    template <int NCH>
+    __global__ void __launch_bounds__(TPB) kAddScaled(int n, double * __restrict__ x, const float * __restrict__ d,
+                                                       const SolverState * st)
+    {
+        if (st->skip)
+            return;
+        for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < NCH * n; i += gridDim.x * blockDim.x)
+            x[i] += (double)d[i] * st->rinv[i / n];
+    }
+
     // Stop decision of refinement pass `pass` (sticky); stats: iters = refinement updates applied.
     // The next inner solve only has to reach half the remaining distance to the target:
     // inner relative tolerance = max(innerMin, 0.5 * tol * ||b|| / ||r||), written into the inner
@@ -1131,6 +1155,14 @@ namespace nsf
         }
         else
         {
+            for (int c = 0; c < NCH; c++)
+            {
+                int e = 0;
+                if (c < numCh && rr[c] > 0)
+                    frexp(sqrt(rr[c]), &e);
+                st->rscale[c] = ldexp(1.0, -e);
+                st->rinv[c] = ldexp(1.0, e);
+            }
             // loosest inner tolerance over the channels still above the target
             double need = 1.0;
             for (int c = 0; c < NCH && c < numCh; c++)

@@ -483,7 +483,10 @@ namespace nsf
             const SweepSystem<double> & S = *sys64;
             const int n = S.n;
             SolverState * sd = st.get();
-            if (inner.canReplace())
+            // Residual replacement stops only on a replaced FP64 residual.  Below ~1e-11 relative the
+            // FP64 residual b - A x of these systems reaches its own rounding floor, so a tighter
+            // target would keep it iterating up to the cap; restarted passes stop after maxOuter.
+            if (inner.canReplace() && tol >= 1e-11)
             {
                 // one launch: FP32 CG whose residual is replaced by the FP64 one whenever it has
                 // dropped by a factor 10 (and before stopping), so the Krylov recurrence survives
@@ -503,10 +506,12 @@ namespace nsf
                 NSF_LAUNCH((kOuterDecide<NCH>), 1, s, sd, inner.st.get(), numCh, pass, innerTol, innerMaxIters);
                 if (pass == maxOuter)
                     break;
+                NSF_LAUNCH((kScalePass<NCH>), cappedBlocks((long long)NCH * n), s, n, b32.get(), (const SolverState *)sd);
                 NSF_CUDA(cudaMemsetAsync(d32.get(), 0, sizeof(float) * NCH * n, s));
                 inner.enqueue(s, bodyStream, b32.get(), d32.get(), innerMaxIters, innerTol, false, checkInterval,
                               false);
-                NSF_LAUNCH((kAddTo<float>), cappedBlocks((long long)NCH * n), s, NCH * n, x, d32.get(), &sd->skip);
+                NSF_LAUNCH((kAddScaled<NCH>), cappedBlocks((long long)NCH * n), s, n, x, d32.get(),
+                           (const SolverState *)sd);
             }
         }
     };
