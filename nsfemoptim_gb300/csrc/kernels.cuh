@@ -1127,7 +1127,8 @@ namespace nsf
     {
         if (threadIdx.x != 0 || st->skip)
             return;
-        bool all = true, bad = false;
+        bool all = true, bad = false, settled = true;
+        bool convC[NCH];
         double rr[NCH], bb[NCH];
         for (int c = 0; c < NCH && c < numCh; c++)
         {
@@ -1137,20 +1138,25 @@ namespace nsf
                 st->innerTotal[c] += inner->iters[c];
             const bool fin = isfinite(rr[c]) && isfinite(bb[c]);
             const bool conv = rr[c] <= st->tol2 * bb[c];
+            // a pass that no longer halves the FP64 residual has reached its rounding floor: further
+            // passes would refine noise
+            const bool stalled = pass > 0 && rr[c] > 0.25 * st->lastRR[c];
+            convC[c] = conv;
             bad |= !fin;
             all &= conv;
+            settled &= conv || stalled;
             st->bb[c] = bb[c];
             st->lastRR[c] = rr[c];
             st->iters[c] = pass;
         }
-        if (all || bad || pass >= st->maxIters)
+        if (all || bad || settled || pass >= st->maxIters)
         {
             st->skip = 1;
             st->anyActive = 0;
             for (int c = 0; c < NCH; c++)
             {
                 st->active[c] = 0;
-                st->status[c] = bad ? 2 : (all ? 0 : 3);
+                st->status[c] = bad ? 2 : ((c >= numCh || convC[c]) ? 0 : 3);
             }
         }
         else
