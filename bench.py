@@ -284,7 +284,8 @@ def bench_adjoint(args):
         precs = {"f64": G.NSF_PREC_F64, "mixedsolve": G.NSF_PREC_F64_MIXEDSOLVE}
         prec = precs[args.adjoint_precision]
         prob = GC.DragProblem(mesh, ctx, ADJ_PEAK, ADJ_NU, ADJ_TAU, n, w, n_coef=16, tol=ADJ_TOL,
-                              checkpoint_interval=args.adjoint_checkpoint, precision=prec)
+                              checkpoint_interval=args.adjoint_checkpoint, precision=prec,
+                              vel_method=args.adjoint_vel_method)
         theta = 0.01 * np.random.default_rng(0).standard_normal(16)
         launches0 = G.kernel_launches()
         for _ in range(max(0, args.adjoint_warmup)):
@@ -311,7 +312,7 @@ def bench_adjoint(args):
             for name, ck, pr in (("keep_all_states", 0, prec),
                                  (f"precision_{other}", args.adjoint_checkpoint, precs[other])):
                 var = GC.DragProblem(mesh, ctx, ADJ_PEAK, ADJ_NU, ADJ_TAU, n, w, n_coef=16, tol=ADJ_TOL,
-                                     checkpoint_interval=ck, precision=pr)
+                                     checkpoint_interval=ck, precision=pr, vel_method=args.adjoint_vel_method)
                 Jk, gnuk, gthk, _ = var.gradient(ADJ_NU, theta)
                 sk = var.adjoint.stats()
                 variants[name] = {
@@ -339,7 +340,8 @@ def bench_adjoint(args):
         if k > 0:
             cpu_t, Jo, gnuo, gtho = _adjoint_oracle_sample(path, k, theta, prob.basis, prob.g0, prob.scale)
             small = GC.DragProblem(mesh, ctx, ADJ_PEAK, ADJ_NU, ADJ_TAU, k, np.full(k, 1.0 / k), n_coef=16,
-                                   tol=ADJ_TOL, checkpoint_interval=0, precision=prec)
+                                   tol=ADJ_TOL, checkpoint_interval=0, precision=prec,
+                                   vel_method=args.adjoint_vel_method)
             Js, gnus, gths, _ = small.gradient(ADJ_NU, theta)
     finally:
         shutil.rmtree(tmp, ignore_errors=True)
@@ -356,6 +358,7 @@ def bench_adjoint(args):
                                f"{n} steps from rest, J = mean c_D over the last {n - n // 2} steps, "
                                f"grad wrt nu + 16 inflow sine coefficients",
                    "N": N, "P": P, "checkpoint_interval": args.adjoint_checkpoint, "solve_tol": ADJ_TOL,
+                   "mass_preconditioner": {1: "multicolor SGS", 2: "Jacobi"}[args.adjoint_vel_method],
                    "precision": {"f64": "FP64 operators and solves",
                                  "mixedsolve": "FP64 operators and state; FP32 CG inside FP64 residual replacement / "
                                                "refinement to the same FP64 tolerance"}[args.adjoint_precision],
@@ -772,6 +775,8 @@ def main():
     ap.add_argument("--adjoint-steps", type=int, default=1000)
     ap.add_argument("--adjoint-checkpoint", type=int, default=50)
     ap.add_argument("--adjoint-precision", default="f64", choices=["f64", "mixedsolve"])
+    ap.add_argument("--adjoint-vel-method", type=int, default=1, choices=[1, 2],
+                    help="mass-solve preconditioner: 1 multicolor SGS, 2 Jacobi")
     ap.add_argument("--adjoint-reps", type=int, default=1, help="timed gradient evaluations")
     ap.add_argument("--adjoint-warmup", type=int, default=1, help="untimed gradient evaluations")
     ap.add_argument("--adjoint-cpu-steps", type=int, default=6)

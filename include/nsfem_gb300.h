@@ -170,7 +170,11 @@ typedef struct
     double nu;            /* viscosity */
     double tau;           /* time step */
     int precision;        /* nsf_precision */
-    int velMethod;        /* 0: "gs" (RMS target velTol, relative), 1: "pcg" (relative velTol) */
+    int velMethod;        /* mass solves. 0: "gs" (RMS target velTol, relative), 1: "pcg" with the
+                             multicolor SGS preconditioner (relative velTol), 2: "pcg" with the
+                             Jacobi preconditioner (no reference counterpart: the diagonally
+                             scaled P2 mass matrix has condition number ~5.2 whatever h, and each
+                             iteration is one parallel phase) */
     int velMaxIters;
     double velTol;
     int presMaxIters;

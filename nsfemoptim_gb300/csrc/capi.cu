@@ -899,12 +899,16 @@ static void buildChorin(nsf_chorin_s & S, const Context & c)
         pCol[c.intP[i]] = invP[i];
     HostCsr<double> Gp = renumber(c.G, dofRows, pCol, S.nIntP);
 
-    S.M64.build(Mp, cv.partStart);
+    // velMethod 2: the mass systems as one color, which turns the SGS preconditioner of the PCG
+    // kernels into Jacobi (the forward phase of a single color gathers nothing): one parallel phase
+    // per iteration instead of 2C - 1 color phases
+    const std::vector<int> mParts = S.cfg.velMethod == 2 ? std::vector<int>{0, N} : cv.partStart;
+    S.M64.build(Mp, mParts);
     S.Kpi64.build(Kpip, cp.partStart);
     std::vector<double> knu(Kp.val.begin(), Kp.val.end());
     if (S.mixed)
     {
-        S.M32.build(Mp, cv.partStart);
+        S.M32.build(Mp, mParts);
         S.Kpi32.build(Kpip, cp.partStart);
         S.I32.upload(Ip, true);
         require(S.I32.nBlocks > 0, "FastConvection row longer than the stream block");
@@ -928,7 +932,7 @@ static void buildChorin(nsf_chorin_s & S, const Context & c)
         if (S.mixedSolve)
         {
             // FP64 operators, FP32-inner solves on FP32 copies of the two systems
-            S.M32.build(Mp, cv.partStart);
+            S.M32.build(Mp, mParts);
             S.Kpi32.build(Kpip, cp.partStart);
             S.mvelT.setup(&S.M64, &S.M32, 2);
             S.mvelF.setup(&S.M64, &S.M32, 2);
@@ -982,7 +986,8 @@ extern "C" int nsf_chorin_create(nsf_context ctx, const nsf_chorin_config * cfg,
                 "unknown precision");
         require(!(cfg->precision == NSF_PREC_F64_MIXEDSOLVE && cfg->velMethod == 0),
                 "mixed solves use velMethod 1 (pcg)");
-        require(cfg->velMethod == 0 || cfg->velMethod == 1, "velMethod must be 0 (gs) or 1 (pcg)");
+        require(cfg->velMethod >= 0 && cfg->velMethod <= 2,
+                "velMethod must be 0 (gs), 1 (pcg, SGS preconditioner) or 2 (pcg, Jacobi preconditioner)");
         require(!(cfg->precision == NSF_PREC_MIXED && cfg->velMethod == 0), "mixed precision uses velMethod 1 (pcg)");
         require(cfg->velMaxIters >= 1 && cfg->presMaxIters >= 1, "iteration caps must be >= 1");
         auto S = std::make_unique<nsf_chorin_s>();

@@ -31,13 +31,14 @@ class DragProblem:
     def __init__(self, mesh: Mesh, ctx: ChorinContext, peak: float, nu: float, tau: float, n_steps: int,
                  weights, n_coef: int = 16, tol: float = 1e-13, checkpoint_interval: int = 50,
                  max_iters: int = 20000, precision: int = NSF_PREC_F64, max_outer: int = 6,
-                 inner_tol: float = 1e-5):
+                 inner_tol: float = 1e-5, vel_method: int = 1):
         """precision: NSF_PREC_F64 (FP64 solves) or NSF_PREC_F64_MIXEDSOLVE (FP64 operators, FP32 CG
         inside FP64 refinement / residual replacement to the same tolerance; max_outer passes with
-        inner tolerance inner_tol)."""
+        inner tolerance inner_tol).  vel_method: mass-solve preconditioner, 1 SGS, 2 Jacobi."""
         self.mesh, self.ctx = mesh, ctx
         self.n_steps = int(n_steps)
-        self.stepper = ChorinStepper(ctx, nu, tau, precision=precision, vel_method=1, vel_max_iters=max_iters,
+        self.stepper = ChorinStepper(ctx, nu, tau, precision=precision, vel_method=vel_method,
+                                     vel_max_iters=max_iters,
                                      vel_tol=tol, pres_max_iters=max_iters, pres_tol=tol, use_graph=True,
                                      max_outer=max_outer, inner_tol=inner_tol)
         self.forces = Forces(mesh, self.stepper)

@@ -101,7 +101,7 @@ int orc_gs_solve_ex(const orc_csr *a, const orc_coloring *c, int numCh, const do
                     int maxIters, double target, int relative, int checkInterval, double *lastRms, int *lastIter);
 
 /* CG preconditioned by symmetric multicolor Gauss-Seidel (forward colors, then backward).
-   precond: 0 = none, 1 = multicolor SGS. Stops when ||r|| <= relTol * ||b||.
+   precond: 0 = none, 1 = multicolor SGS, 2 = Jacobi. Stops when ||r|| <= relTol * ||b||.
    Returns 0 converged, 3 max iterations, 4 breakdown (p^T A p <= 0), 2 non-finite. */
 int orc_pcg(const orc_csr *a, const orc_coloring *c, int precond, const double *b, double *x,
             int maxIters, double relTol, int *iters, double *relRes);
@@ -113,7 +113,7 @@ void orc_sgs_apply(const orc_csr *a, const orc_coloring *c, const double *r, dou
 typedef struct
 {
     double nu, tau;
-    int velMethod;       /* 0 = multicolor GS (RMS target), 1 = PCG-SGS (relative tol) */
+    int velMethod;       /* 0 = multicolor GS (RMS target), 1 = PCG-SGS, 2 = PCG-Jacobi (relative tol) */
     int velMaxIters;
     double velTol;       /* RMS target for GS, relative tolerance for PCG */
     int presMaxIters;

@@ -138,7 +138,9 @@ static int mass_solve(orc_chorin *s, const double *rhs, double *acc, double *res
     {
         int it = 0;
         double rr = 0;
-        int st = orc_pcg(&ctx->M, &s->colM, 1, rhs + ch * N, acc + ch * N, s->cfg.velMaxIters, s->cfg.velTol, &it, &rr);
+        /* velMethod 1: SGS preconditioner, 2: Jacobi */
+        int st = orc_pcg(&ctx->M, &s->colM, s->cfg.velMethod == 2 ? 2 : 1, rhs + ch * N, acc + ch * N,
+                         s->cfg.velMaxIters, s->cfg.velTol, &it, &rr);
         (void)st;
         if (it > itMax)
             itMax = it;

@@ -485,6 +485,19 @@ void orc_sgs_apply(const orc_csr *a, const orc_coloring *c, const double *r, dou
     gs_ctx_free(&g);
 }
 
+/* z = preconditioner(r): 0 none, 1 multicolor SGS, 2 Jacobi (z = r / diag) */
+static void precond_apply(const gs_ctx *g, const orc_coloring *c, int precond, const double *r, double *z)
+{
+    const int n = g->s.rows;
+    if (precond == 1)
+        sgs_colored(g, c, r, z);
+    else if (precond == 2)
+        for (int i = 0; i < n; i++)
+            z[i] = r[i] * g->invD[i];
+    else
+        memcpy(z, r, sizeof(double) * n);
+}
+
 static double dot(const double *a, const double *b, int n)
 {
     double s = 0;
@@ -526,10 +539,7 @@ int orc_pcg(const orc_csr *a, const orc_coloring *c, int precond, const double *
         status = 0;
     else
     {
-        if (precond)
-            sgs_colored(&g, c, r, z);
-        else
-            memcpy(z, r, sizeof(double) * n);
+        precond_apply(&g, c, precond, r, z);
         memcpy(p, z, sizeof(double) * n);
         double rz = dot(r, z, n);
         for (it = 1; it <= maxIters; it++)
@@ -558,10 +568,7 @@ int orc_pcg(const orc_csr *a, const orc_coloring *c, int precond, const double *
                 status = 0;
                 break;
             }
-            if (precond)
-                sgs_colored(&g, c, r, z);
-            else
-                memcpy(z, r, sizeof(double) * n);
+            precond_apply(&g, c, precond, r, z);
             double rzNew = dot(r, z, n);
             double beta = rzNew / rz;
             rz = rzNew;

@@ -280,6 +280,27 @@ def test_chorin_fp64_matches_oracle(setup, torch_cuda, graph):
     assert s["status"] == 0 and s["pres_rel"] <= 1e-10
 
 
+@pytest.mark.parametrize("path", ["auto", "grid", "multikernel"])
+@pytest.mark.parametrize("precision", ["f64", "mixed"])
+def test_chorin_jacobi_mass_matches_oracle(setup, torch_cuda, path, precision, monkeypatch):
+    """velMethod 2: the mass solves as PCG with the Jacobi preconditioner (the SGS kernels on a
+    one-color system).  FP64 against the oracle's Jacobi-PCG step (1e-7 after 5 steps, as the SGS
+    variant); mixed against the same FP64 oracle within the mixed tolerances."""
+    G, O, mesh, ctx, om, oc = setup
+    monkeypatch.setenv("NSF_PCG_PATH", path)
+    prec = G.NSF_PREC_F64 if precision == "f64" else G.NSF_PREC_MIXED
+    st = G.ChorinStepper(ctx, 1e-3, 1e-3, precision=prec, vel_method=2, vel_max_iters=300, vel_tol=1e-10,
+                         pres_max_iters=3000, pres_tol=1e-10, use_graph=True)
+    st.step(5)
+    u, p = st.state()
+    uo, po = _oracle_steps(O, oc, 1e-3, 1e-3, 5, vel_method=2)
+    tu, tp = (1e-7, 1e-7) if precision == "f64" else (1e-5, 1e-4)
+    assert _rel(u, uo) <= tu
+    assert _rel(p, po) <= tp
+    s = st.stats()
+    assert s["status"] == 0 and s["tent_rel"] <= 1e-10 and s["final_rel"] <= 1e-10
+
+
 def test_concurrent_launch_equals_step(setup, torch_cuda, monkeypatch):
     """Independent steppers (different viscosities) enqueued with launch() on their own streams,
     interleaved step by step, reach bit-identical states to the same steppers advanced with
