@@ -101,13 +101,13 @@ class Clocks:
         return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def run_cpu_reference(mesh_path: str, steps: int, warmup: int):
+def run_cpu_reference(mesh_path: str, steps: int, warmup: int, vel_method: int = 1):
     """Time the oracle's FP64 Chorin step (the CPU restatement of the reference path)."""
     import oracle
     oracle.build()
     m = oracle.Mesh(mesh_path)
     ctx = oracle.Context(m, PEAK, True)
-    ch = oracle.Chorin(ctx, NU, TAU, vel_method=1, vel_max_iters=500, vel_tol=VEL_TOL, pres_max_iters=5000,
+    ch = oracle.Chorin(ctx, NU, TAU, vel_method=vel_method, vel_max_iters=500, vel_tol=VEL_TOL, pres_max_iters=5000,
                        pres_tol=PRES_TOL)
     for _ in range(warmup):
         ch.step()
@@ -590,7 +590,7 @@ def bench_ours(args, rank, world, local_rank):
         N, P, nip = ctx.N, ctx.P, len(ctx.int_p)
 
         def stepper(precision, graph=True):
-            return G.ChorinStepper(ctx, NU, TAU, precision=precision, vel_method=1, vel_max_iters=500,
+            return G.ChorinStepper(ctx, NU, TAU, precision=precision, vel_method=args.vel_method, vel_max_iters=500,
                                    vel_tol=VEL_TOL, pres_max_iters=5000, pres_tol=PRES_TOL, check_interval=8,
                                    use_graph=graph, max_outer=4, inner_tol=1e-5)
 
@@ -728,7 +728,8 @@ def bench_ours(args, rank, world, local_rank):
                                    "pressure PCG-SGS to 1e-8 rel", "triangles": mesh.num_tri, "N": N, "P": P,
                        "internal_pressure": nip, "nnz_I": nnzI, "parallelism": f"replicas x{world}",
                        "l2": "working set > L2 (FastConvection matrix %.0f MB FP32)" % (nnzI * 8 / 1e6),
-                       "graph": True, "setup_s": round(setup_s, 2)},
+                       "graph": True, "setup_s": round(setup_s, 2),
+                       "mass_solve": {1: "PCG, multicolor SGS", 2: "PCG, Jacobi"}[args.vel_method]},
             "e2e": {"value": round(world * e2e_steps / t_e2e, 3), "unit": "steps/s",
                     "h2d_bytes_per_step": (2 * N + P) * 8, "d2h_bytes_per_step": (2 * N + P) * 8},
             "gpu_launches": int(launches),
@@ -772,6 +773,8 @@ def main():
                     help="channel: the h=0.005 time step (default); poisson: the standalone 1M-DOF pressure "
                          "solve; small: the plain FP64 h=0.02 channel; batch: 64 instances at h=0.01; "
                          "adjoint: the drag gradient at h=0.01 over 1000 steps")
+    ap.add_argument("--vel-method", type=int, default=1, choices=[1, 2],
+                    help="channel workload: mass-solve preconditioner, 1 multicolor SGS, 2 Jacobi")
     ap.add_argument("--adjoint-steps", type=int, default=1000)
     ap.add_argument("--adjoint-checkpoint", type=int, default=50)
     ap.add_argument("--adjoint-precision", default="f64", choices=["f64", "mixedsolve"])
@@ -866,7 +869,7 @@ def main():
             tmp = tempfile.mkdtemp()
             try:
                 path = make_mesh(tmp, H, 0)
-                sps, dt, _, (uo, po, fo) = run_cpu_reference(path, args.cpu_sample_steps, 1)
+                sps, dt, _, (uo, po, fo) = run_cpu_reference(path, args.cpu_sample_steps, 1, args.vel_method)
                 line["cpu_baseline"] = {"value": round(sps, 4), "unit": "steps/s", "cores": 1, "kind": "port",
                                         "sample": f"{args.cpu_sample_steps} time steps (after 1 warm-up) of the same "
                                                   f"workload, FP64 C oracle, single thread"}
