@@ -773,7 +773,7 @@ def main():
                     help="channel: the h=0.005 time step (default); poisson: the standalone 1M-DOF pressure "
                          "solve; small: the plain FP64 h=0.02 channel; batch: 64 instances at h=0.01; "
                          "adjoint: the drag gradient at h=0.01 over 1000 steps")
-    ap.add_argument("--vel-method", type=int, default=1, choices=[1, 2],
+    ap.add_argument("--vel-method", type=int, default=2, choices=[1, 2],
                     help="channel workload: mass-solve preconditioner, 1 multicolor SGS, 2 Jacobi")
     ap.add_argument("--adjoint-steps", type=int, default=1000)
     ap.add_argument("--adjoint-checkpoint", type=int, default=50)
