@@ -741,7 +741,7 @@ def bench_ours(args, rank, world, local_rank):
                          "note": "vectors and matrix live in shared memory across the cluster; the kernel is "
                                  "bound by barrier/gather latency, not HBM (ncu DRAM traffic per launch is "
                                  "~1% of the algorithmic bytes)"},
-            "roofline_fastconv": {"bound": "hbm", "kernel": "kFastConvStream<float> (A = nu K + I u)",
+            "roofline_fastconv": {"bound": "hbm", "kernel": "kFastConvSell<float> (A = nu K + I u, SELL-32-256)",
                                   "achieved": round(achieved, 1), "peak": hbm, "unit": "GB/s",
                                   "frac": round(achieved / hbm, 4), "peak_kind": kind,
                                   "algorithmic_bytes": fc_bytes, "launch_us": round(t_fc * 1e6, 2)},

@@ -58,15 +58,10 @@ namespace
         return t;
     }
 
-    // y = alpha A x + beta y with the CSR-stream kernel where the rows fit its blocks
+    // y = alpha A x + beta y through the SELL copy
     void spmvF64(const DevCsr<double> & a, const double * x, double * y, double alpha, double beta, cudaStream_t s)
     {
-        if (a.nBlocks > 0)
-            NSF_LAUNCH((kSpmvStream<double, double, double, double>), a.nBlocks, s, a.rb.get(), a.rs.get(),
-                       a.ci.get(), a.v.get(), x, y, alpha, beta);
-        else
-            NSF_LANES(a.L, NSF_LAUNCH((kSpmv<double, double, double, double, LL>), blocksFor((long long)a.rows * a.L),
-                                      s, a.rows, a.rs.get(), a.ci.get(), a.v.get(), x, y, alpha, beta));
+        sellSpmv<double>(a.sell, x, y, alpha, beta, s);
     }
 
     // gridSum epilogue: *acc += *total (the total has just been written)
@@ -369,8 +364,9 @@ struct nsf_adjoint_s
         spmvF64(DT, y.get(), lw.get(), -1.0 / tau, 1.0, s);
         NSF_LAUNCH(kAdjDirichlet, blocksFor(N), s, N, lw.get(), rhs.get(), S->isDir.get(), lDir.get(), tau);
         massSolve(s);
-        NSF_LAUNCH((kFastConvStream<double, double, double, double>), S->I64.nBlocks, s, S->I64.rb.get(),
-                   S->I64.rs.get(), S->I64.ci.get(), S->I64.v.get(), u0, S->K64.get(), nu, A.get());
+        const DevSell<double> & IS = S->I64.sell;
+        NSF_LAUNCH((kFastConvSell<double, double, double, double>), IS.blocks(), s, IS.rows, IS.nSlices, IS.ss.get(),
+                   IS.perm.get(), IS.ci.get(), IS.v.get(), u0, S->K64.get(), nu, A.get());
         const SweepSystem<double> & M = S->M64;
         NSF_LANES(M.L, NSF_LAUNCH((kAdjConv<LL>), cappedBlocks((long long)N * LL), s, N, M.rsF.get(), M.ciF.get(),
                                   T.get(), A.get(), S->K64.get(), x.get(), u0, lw.get(), lam.get(), lA.get(),
@@ -483,7 +479,6 @@ extern "C" int nsf_adjoint_create(nsf_chorin S, nsf_forces f, const nsf_adjoint_
         require(S && f && out, "null argument");
         require(f->s == S, "the force functional belongs to another stepper");
         require(!S->mixed, "the adjoint needs FP64 operators (precision NSF_PREC_F64 or NSF_PREC_F64_MIXEDSOLVE)");
-        require(S->I64.nBlocks > 0, "FastConvection rows too long for the stream kernel");
         auto a = std::make_unique<nsf_adjoint_s>();
         if (cfg)
             a->cfg = *cfg;

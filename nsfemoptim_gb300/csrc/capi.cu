@@ -5,6 +5,7 @@
 #include "solvers.cuh"
 
 #include <algorithm>
+#include <climits>
 #include <cstring>
 #include <memory>
 #include <mutex>
@@ -111,15 +112,95 @@ namespace nsf
         return rb;
     }
 
+    // SELL-C-sigma copy of a CSR matrix for kSpmvSell / kFastConvSell (layout in kernels.cuh).
+    // Rows are sorted by length (descending, stable) inside windows of sigma = 256 rows, which
+    // keeps the padding of these FEM operators at 1-7% and the scattered result writes inside a
+    // window; a padded entry repeats the row's last column with a zero value, so it never
+    // gathers a value that the row does not already use.
+    template <typename T>
+    struct DevSell
+    {
+        int rows = 0, nSlices = 0;
+        long long stored = 0;
+        DevBuf<int> ss, perm, ci, src; // src (only with keepSrc): CSR entry of each stored entry, -1 = pad
+        DevBuf<T> v;
+
+        void build(int n, const int * rs, const int * col, const double * val, bool keepSrc = false,
+                   int sigma = 256)
+        {
+            rows = n;
+            nSlices = (n + SELL_C - 1) / SELL_C;
+            std::vector<int> order(n);
+            std::iota(order.begin(), order.end(), 0);
+            auto len = [&](int r) { return rs[r + 1] - rs[r]; };
+            for (int w0 = 0; w0 < n; w0 += sigma)
+                std::stable_sort(order.begin() + w0, order.begin() + std::min(n, w0 + sigma),
+                                 [&](int a, int b) { return len(a) > len(b); });
+            std::vector<long long> start(nSlices + 1, 0);
+            for (int s = 0; s < nSlices; s++)
+            {
+                int w = 0;
+                for (int l = 0; l < SELL_C && s * SELL_C + l < n; l++)
+                    w = std::max(w, len(order[s * SELL_C + l]));
+                start[s + 1] = start[s] + (long long)SELL_C * w;
+            }
+            stored = start[nSlices];
+            if (stored >= INT_MAX)
+                throw Error(ST_NOTSUP, "matrix too large for 32-bit SELL offsets");
+            std::vector<int> hs(nSlices + 1), hc((size_t)stored), hsrc(keepSrc ? (size_t)stored : 0);
+            std::vector<T> hv((size_t)stored);
+            for (int s = 0; s <= nSlices; s++)
+                hs[s] = (int)start[s];
+            for (int s = 0; s < nSlices; s++)
+            {
+                const int w = (int)((start[s + 1] - start[s]) / SELL_C);
+                for (int l = 0; l < SELL_C; l++)
+                {
+                    const int sr = s * SELL_C + l;
+                    const int r = sr < n ? order[sr] : -1;
+                    const int m = r >= 0 ? len(r) : 0;
+                    const int last = m > 0 ? col[rs[r] + m - 1] : 0;
+                    for (int k = 0; k < w; k++)
+                    {
+                        const size_t i = (size_t)start[s] + (size_t)k * SELL_C + l;
+                        const bool real = k < m;
+                        hc[i] = real ? col[rs[r] + k] : last;
+                        hv[i] = real ? (T)val[rs[r] + k] : (T)0;
+                        if (keepSrc)
+                            hsrc[i] = real ? rs[r] + k : -1;
+                    }
+                }
+            }
+            ss.upload(hs);
+            perm.upload(order);
+            ci.upload(hc);
+            v.upload(hv);
+            if (keepSrc)
+                src.upload(hsrc);
+        }
+
+        int blocks() const { return blocksFor((long long)nSlices * SELL_C); }
+    };
+
+    // y = alpha A x + beta y through the SELL copy (accumulation in TA)
+    template <typename TA, typename TM, typename TX, typename TY>
+    void sellSpmv(const DevSell<TM> & S, const TX * x, TY * y, double alpha, double beta, cudaStream_t s)
+    {
+        NSF_LAUNCH((kSpmvSell<TM, TX, TY, TA>), S.blocks(), s, S.rows, S.nSlices, S.ss.get(), S.perm.get(),
+                   S.ci.get(), S.v.get(), x, y, alpha, beta);
+    }
+
     template <typename T>
     struct DevCsr
     {
         int rows = 0, cols = 0, nnz = 0, L = 4, nBlocks = 0;
         DevBuf<int> rs, ci, rb;
         DevBuf<T> v;
+        DevSell<T> sell;
 
         void upload(const HostCsr<double> & a, bool stream = false)
         {
+            sell.build(a.rows, a.rowStart.data(), a.col.data(), a.val.data());
             rows = a.rows;
             cols = a.cols;
             nnz = a.nnz();
@@ -157,6 +238,8 @@ struct nsf_csr_s
     DevBuf<int> rs, ci, rb;
     DevBuf<double> v64;
     DevBuf<float> v32;
+    DevSell<double> s64; // SELL copy used by nsf_spmv / nsf_fastconv_apply (values kept in step
+    DevSell<float> s32;  // with nsf_csr_update_values)
 };
 
 extern "C" const char * nsf_last_error(void) { return lastError.c_str(); }
@@ -355,6 +438,7 @@ extern "C" int nsf_csr_create(int rows, int cols, int nnz, const int * rowStart,
             for (int i = 0; i < nnz; i++)
                 require(std::isfinite(v[i]), "non-finite CSR value at " + std::to_string(i));
             h->v64.upload(v, nnz);
+            h->s64.build(rows, rowStart, col, v, true);
         }
         else
         {
@@ -362,6 +446,8 @@ extern "C" int nsf_csr_create(int rows, int cols, int nnz, const int * rowStart,
             for (int i = 0; i < nnz; i++)
                 require(std::isfinite(v[i]), "non-finite CSR value at " + std::to_string(i));
             h->v32.upload(v, nnz);
+            const std::vector<double> vd(v, v + nnz);
+            h->s32.build(rows, rowStart, col, vd.data(), true);
         }
         h->L = lanesFor(nnz, rows);
         std::vector<int> rb = streamRowBlocks(rowStart, rows);
@@ -380,6 +466,12 @@ extern "C" int nsf_csr_update_values(nsf_csr a, const void * values, int onDevic
         void * dst = a->dtype == NSF_F64 ? (void *)a->v64.get() : (void *)a->v32.get();
         NSF_CUDA(cudaMemcpyAsync(dst, values, bytes, onDevice ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice,
                                  asStream(stream)));
+        if (a->dtype == NSF_F64 && a->s64.stored > 0)
+            NSF_LAUNCH((kSellGather<double>), cappedBlocks(a->s64.stored), asStream(stream), a->s64.stored,
+                       a->s64.src.get(), a->v64.get(), a->s64.v.get());
+        else if (a->dtype == NSF_F32 && a->s32.stored > 0)
+            NSF_LAUNCH((kSellGather<float>), cappedBlocks(a->s32.stored), asStream(stream), a->s32.stored,
+                       a->s32.src.get(), a->v32.get(), a->s32.v.get());
         if (!onDevice)
             NSF_CUDA(cudaStreamSynchronize(asStream(stream)));
     });
@@ -404,27 +496,19 @@ extern "C" int nsf_spmv(nsf_csr a, const void * x, void * y, double alpha, doubl
 {
     return guarded([&] {
         require(a && x && y, "null argument");
-        // plain operator (no grid reduction): one row group per row, no grid cap
-        const int grid = blocksFor((long long)a->rows * a->L);
+        // SELL-C-sigma: one thread per row, coalesced slice loads, one FMA per stored entry
         cudaStream_t s = asStream(stream);
-        if (a->nBlocks > 0) // CSR-stream: every row fits a stream block
+        if (a->dtype == NSF_F64)
         {
-            if (a->dtype == NSF_F64)
-                NSF_LAUNCH((kSpmvStream<double, double, double, double>), a->nBlocks, s, a->rb.get(), a->rs.get(),
-                           a->ci.get(), a->v64.get(), (const double *)x, (double *)y, alpha, beta);
-            else
-                NSF_LAUNCH((kSpmvStream<float, float, float, float>), a->nBlocks, s, a->rb.get(), a->rs.get(),
-                           a->ci.get(), a->v32.get(), (const float *)x, (float *)y, alpha, beta);
-        }
-        else if (a->dtype == NSF_F64)
-        {
-            NSF_LANES(a->L, NSF_LAUNCH((kSpmv<double, double, double, double, LL>), grid, s, a->rows, a->rs.get(),
-                                       a->ci.get(), a->v64.get(), (const double *)x, (double *)y, alpha, beta));
+            const DevSell<double> & S = a->s64;
+            NSF_LAUNCH((kSpmvSell<double, double, double, double>), S.blocks(), s, S.rows, S.nSlices, S.ss.get(),
+                       S.perm.get(), S.ci.get(), S.v.get(), (const double *)x, (double *)y, alpha, beta);
         }
         else
         {
-            NSF_LANES(a->L, NSF_LAUNCH((kSpmv<float, float, float, float, LL>), grid, s, a->rows, a->rs.get(),
-                                       a->ci.get(), a->v32.get(), (const float *)x, (float *)y, alpha, beta));
+            const DevSell<float> & S = a->s32;
+            NSF_LAUNCH((kSpmvSell<float, float, float, float>), S.blocks(), s, S.rows, S.nSlices, S.ss.get(),
+                       S.perm.get(), S.ci.get(), S.v.get(), (const float *)x, (float *)y, alpha, beta);
         }
     });
 }
@@ -469,24 +553,20 @@ extern "C" int nsf_fastconv_apply(nsf_csr I, const void * K, double nu, const vo
 {
     return guarded([&] {
         require(I && K && u && A, "null argument");
-        const int grid = blocksFor((long long)I->rows * I->L);
         cudaStream_t s = asStream(stream);
-        if (I->nBlocks > 0)
+        if (I->dtype == NSF_F64)
         {
-            if (I->dtype == NSF_F64)
-                NSF_LAUNCH((kFastConvStream<double, double, double, double>), I->nBlocks, s, I->rb.get(), I->rs.get(),
-                           I->ci.get(), I->v64.get(), (const double *)u, (const double *)K, nu, (double *)A);
-            else
-                NSF_LAUNCH((kFastConvStream<float, float, float, float>), I->nBlocks, s, I->rb.get(), I->rs.get(),
-                           I->ci.get(), I->v32.get(), (const float *)u, (const float *)K, (float)nu, (float *)A);
+            const DevSell<double> & S = I->s64;
+            NSF_LAUNCH((kFastConvSell<double, double, double, double>), S.blocks(), s, S.rows, S.nSlices, S.ss.get(),
+                       S.perm.get(), S.ci.get(), S.v.get(), (const double *)u, (const double *)K, nu, (double *)A);
         }
-        else if (I->dtype == NSF_F64)
-            NSF_LANES(I->L, NSF_LAUNCH((kFastConv<double, double, double, double, LL>), grid, s, I->rows, I->rs.get(),
-                                       I->ci.get(), I->v64.get(), (const double *)u, (const double *)K, nu, (double *)A));
         else
-            NSF_LANES(I->L, NSF_LAUNCH((kFastConv<float, float, float, float, LL>), grid, s, I->rows, I->rs.get(),
-                                       I->ci.get(), I->v32.get(), (const float *)u, (const float *)K, (float)nu,
-                                       (float *)A));
+        {
+            const DevSell<float> & S = I->s32;
+            NSF_LAUNCH((kFastConvSell<float, float, float, float>), S.blocks(), s, S.rows, S.nSlices, S.ss.get(),
+                       S.perm.get(), S.ci.get(), S.v.get(), (const float *)u, (const float *)K, (float)nu,
+                       (float *)A);
+        }
     });
 }
 
@@ -749,18 +829,20 @@ struct nsf_chorin_s
 
     void enqueueStep(cudaStream_t s)
     {
-        // 1. A = nu K + I u (CSR-stream over the FastConvection matrix) ;  rhs = A [ux uy]
+        // 1. A = nu K + I u (SELL copy of the FastConvection matrix) ;  rhs = A [ux uy]
         if (mixed)
         {
-            NSF_LAUNCH((kFastConvStream<float, double, float, float>), I32.nBlocks, s, I32.rb.get(), I32.rs.get(),
-                       I32.ci.get(), I32.v.get(), u.get(), K32.get(), (float)cfg.nu, A32.get());
+            const DevSell<float> & IS = I32.sell;
+            NSF_LAUNCH((kFastConvSell<float, double, float, float>), IS.blocks(), s, IS.rows, IS.nSlices, IS.ss.get(),
+                       IS.perm.get(), IS.ci.get(), IS.v.get(), u.get(), K32.get(), (float)cfg.nu, A32.get());
             NSF_LANES(M32.L, NSF_LAUNCH((kSpmm<float, double, double, float, LL, 2>), blocksFor((long long)N * M32.L), s, N,
                                         M32.rsF.get(), M32.ciF.get(), A32.get(), u.get(), N, rhs.get(), N));
         }
         else
         {
-            NSF_LAUNCH((kFastConvStream<double, double, double, double>), I64.nBlocks, s, I64.rb.get(), I64.rs.get(),
-                       I64.ci.get(), I64.v.get(), u.get(), K64.get(), cfg.nu, A64.get());
+            const DevSell<double> & IS = I64.sell;
+            NSF_LAUNCH((kFastConvSell<double, double, double, double>), IS.blocks(), s, IS.rows, IS.nSlices,
+                       IS.ss.get(), IS.perm.get(), IS.ci.get(), IS.v.get(), u.get(), K64.get(), cfg.nu, A64.get());
             NSF_LANES(M64.L, NSF_LAUNCH((kSpmm<double, double, double, double, LL, 2>), blocksFor((long long)N * M64.L), s, N,
                                         M64.rsF.get(), M64.ciF.get(), A64.get(), u.get(), N, rhs.get(), N));
         }
@@ -772,29 +854,21 @@ struct nsf_chorin_s
         const double invTau = -1.0 / cfg.tau;
         if (mixed)
         {
-            NSF_LANES(D32.L, NSF_LAUNCH((kSpmv<float, double, double, float, LL>), blocksFor((long long)nIntP * D32.L),
-                                        s, nIntP, D32.rs.get(), D32.ci.get(), D32.v.get(), u.get(), rhsP.get(),
-                                        invTau, 0.0));
+            sellSpmv<float>(D32.sell, u.get(), rhsP.get(), invTau, 0.0, s);
             mpres.enqueue(s, body, rhsP.get(), pInt.get(), cfg.maxOuter, cfg.presTol, cfg.presMaxIters, cfg.innerTol,
                           cfg.checkInterval);
-            NSF_LANES(G32.L, NSF_LAUNCH((kSpmv<float, double, double, float, LL>), blocksFor((long long)2 * N * G32.L),
-                                        s, 2 * N, G32.rs.get(), G32.ci.get(), G32.v.get(), pInt.get(), rhs.get(), 1.0,
-                                        0.0));
+            sellSpmv<float>(G32.sell, pInt.get(), rhs.get(), 1.0, 0.0, s);
         }
         else
         {
-            NSF_LANES(D64.L, NSF_LAUNCH((kSpmv<double, double, double, double, LL>),
-                                        blocksFor((long long)nIntP * D64.L), s, nIntP, D64.rs.get(), D64.ci.get(),
-                                        D64.v.get(), u.get(), rhsP.get(), invTau, 0.0));
+            sellSpmv<double>(D64.sell, u.get(), rhsP.get(), invTau, 0.0, s);
             if (mixedSolve)
                 mpres.enqueue(s, body, rhsP.get(), pInt.get(), cfg.maxOuter, cfg.presTol, cfg.presMaxIters,
                               cfg.innerTol, cfg.checkInterval);
             else
                 pres.enqueue(s, body, rhsP.get(), pInt.get(), cfg.presMaxIters, cfg.presTol, false,
                              cfg.checkInterval);
-            NSF_LANES(G64.L, NSF_LAUNCH((kSpmv<double, double, double, double, LL>),
-                                        blocksFor((long long)2 * N * G64.L), s, 2 * N, G64.rs.get(), G64.ci.get(),
-                                        G64.v.get(), pInt.get(), rhs.get(), 1.0, 0.0));
+            sellSpmv<double>(G64.sell, pInt.get(), rhs.get(), 1.0, 0.0, s);
         }
         // 4. M acc = G p ; u = u - tau acc ; Dirichlet
         enqueueMassSolve(s, false);
@@ -911,7 +985,6 @@ static void buildChorin(nsf_chorin_s & S, const Context & c)
         S.M32.build(Mp, mParts);
         S.Kpi32.build(Kpip, cp.partStart);
         S.I32.upload(Ip, true);
-        require(S.I32.nBlocks > 0, "FastConvection row longer than the stream block");
         S.D32.upload(Dp);
         S.G32.upload(Gp);
         std::vector<float> k32(knu.begin(), knu.end());
@@ -924,7 +997,6 @@ static void buildChorin(nsf_chorin_s & S, const Context & c)
     else
     {
         S.I64.upload(Ip, true);
-        require(S.I64.nBlocks > 0, "FastConvection row longer than the stream block");
         S.D64.upload(Dp);
         S.G64.upload(Gp);
         S.K64.upload(knu);

@@ -308,6 +308,101 @@ namespace nsf
         }
     }
 
+    // ------------------------------------------------------------------ SELL-C-sigma operators
+    // SELL-C-sigma with C = 32: the rows, sorted by length inside windows of sigma rows, form slices
+    // of 32; slice s stores its rows column-major (entry k of lane l at ss[s] + 32 k + l), padded to
+    // the slice's longest row with zero values.  One warp per slice, one thread per row: every
+    // value and column load of a warp is one coalesced 32-entry segment, and each stored entry
+    // costs one FMA.  (FP64 runs at 1/64 of the FP32 rate on this GPU: the CSR-stream kernels
+    // spend a multiply and an add per entry and become FP64-issue-bound.)  Results go to the
+    // original row perm[row].  e - b is a multiple of 32, so the unrolled loop is warp-uniform.
+    constexpr int SELL_C = 32;
+
+    template <typename TM, typename TX, typename TA>
+    __device__ __forceinline__ TA sellRow(int b, int e, int lane, const int * __restrict__ ci,
+                                          const TM * __restrict__ v, const TX * __restrict__ x)
+    {
+        TA acc = 0;
+        int j = b + lane;
+        for (; j + 3 * SELL_C < e; j += 4 * SELL_C)
+        {
+            int c[4];
+            TM a[4];
+#pragma unroll
+            for (int t = 0; t < 4; t++)
+            {
+                c[t] = ldg(ci + j + t * SELL_C);
+                a[t] = ldg(v + j + t * SELL_C);
+            }
+            TX g[4];
+#pragma unroll
+            for (int t = 0; t < 4; t++)
+                g[t] = ldg(x + c[t]);
+#pragma unroll
+            for (int t = 0; t < 4; t++)
+                acc += (TA)a[t] * (TA)g[t];
+        }
+        for (; j < e; j += SELL_C)
+            acc += (TA)ldg(v + j) * (TA)ldg(x + ldg(ci + j));
+        return acc;
+    }
+
+    // y[perm[row]] = alpha * (A x)[row] + beta * y[perm[row]]   (beta == 0: y is not read)
+    template <typename TM, typename TX, typename TY, typename TA>
+    __global__ void __launch_bounds__(TPB) kSpmvSell(int rows, int nSlices, const int * __restrict__ ss,
+                                                      const int * __restrict__ perm, const int * __restrict__ ci,
+                                                      const TM * __restrict__ v, const TX * __restrict__ x,
+                                                      TY * __restrict__ y, double alpha, double beta)
+    {
+        const int slice = (int)((blockIdx.x * (unsigned)blockDim.x + threadIdx.x) >> 5);
+        if (slice >= nSlices)
+            return; // whole warps
+        const int lane = threadIdx.x & 31;
+        const TA acc = sellRow<TM, TX, TA>(ldg(ss + slice), ldg(ss + slice + 1), lane, ci, v, x);
+        const int row = slice * SELL_C + lane;
+        if (row < rows)
+        {
+            const int r = ldg(perm + row);
+            double out = alpha * (double)acc;
+            if (beta != 0.0)
+                out += beta * (double)y[r];
+            y[r] = (TY)out;
+        }
+    }
+
+    // A[perm[row]] = nu K[perm[row]] + (I u)[row]   (FastConvection with the nu K add fused)
+    template <typename TI, typename TU, typename TK, typename TA>
+    __global__ void __launch_bounds__(TPB) kFastConvSell(int rows, int nSlices, const int * __restrict__ ss,
+                                                          const int * __restrict__ perm, const int * __restrict__ ci,
+                                                          const TI * __restrict__ iv, const TU * __restrict__ u,
+                                                          const TK * __restrict__ k, TA nu, TK * __restrict__ a)
+    {
+        const int slice = (int)((blockIdx.x * (unsigned)blockDim.x + threadIdx.x) >> 5);
+        if (slice >= nSlices)
+            return;
+        const int lane = threadIdx.x & 31;
+        const TA acc = sellRow<TI, TU, TA>(ldg(ss + slice), ldg(ss + slice + 1), lane, ci, iv, u);
+        const int row = slice * SELL_C + lane;
+        if (row < rows)
+        {
+            const int r = ldg(perm + row);
+            a[r] = (TK)(nu * (TA)ldg(k + r) + acc);
+        }
+    }
+
+    // SELL values from CSR values after an update: sv[i] = src[i] >= 0 ? cv[src[i]] : 0
+    template <typename T>
+    __global__ void __launch_bounds__(TPB) kSellGather(long long stored, const int * __restrict__ src,
+                                                        const T * __restrict__ cv, T * __restrict__ sv)
+    {
+        for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < stored;
+             i += (long long)gridDim.x * blockDim.x)
+        {
+            const int s = src[i];
+            sv[i] = s >= 0 ? cv[s] : (T)0;
+        }
+    }
+
     // u <- Dirichlet value on boundary rows, u - tau * acc elsewhere (2 planar channels)
     template <typename TA>
     __global__ void __launch_bounds__(TPB) kUpdateVelocity(int n, double * __restrict__ u, const TA * __restrict__ acc,
