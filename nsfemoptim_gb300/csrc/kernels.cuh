@@ -318,32 +318,36 @@ namespace nsf
     // original row perm[row].  e - b is a multiple of 32, so the unrolled loop is warp-uniform.
     constexpr int SELL_C = 32;
 
+    // Groups of 8 slice columns with predicated loads: all loads of a short row (a 7-point stencil,
+    // say) are in flight together, then the gathers, then the FMAs.
     template <typename TM, typename TX, typename TA>
     __device__ __forceinline__ TA sellRow(int b, int e, int lane, const int * __restrict__ ci,
                                           const TM * __restrict__ v, const TX * __restrict__ x)
     {
+        constexpr int U = 8;
         TA acc = 0;
-        int j = b + lane;
-        for (; j + 3 * SELL_C < e; j += 4 * SELL_C)
+        const int w = (e - b) / SELL_C;
+        for (int k = 0; k < w; k += U)
         {
-            int c[4];
-            TM a[4];
+            int c[U];
+            TM a[U];
 #pragma unroll
-            for (int t = 0; t < 4; t++)
+            for (int t = 0; t < U; t++)
             {
-                c[t] = ldg(ci + j + t * SELL_C);
-                a[t] = ldg(v + j + t * SELL_C);
+                const int j = b + (k + t) * SELL_C + lane;
+                const bool ok = k + t < w;
+                c[t] = ok ? ldg(ci + j) : 0;
+                a[t] = ok ? ldg(v + j) : (TM)0;
             }
-            TX g[4];
+            TX g[U];
 #pragma unroll
-            for (int t = 0; t < 4; t++)
-                g[t] = ldg(x + c[t]);
+            for (int t = 0; t < U; t++)
+                g[t] = k + t < w ? ldg(x + c[t]) : (TX)0;
 #pragma unroll
-            for (int t = 0; t < 4; t++)
-                acc += (TA)a[t] * (TA)g[t];
+            for (int t = 0; t < U; t++)
+                if (k + t < w)
+                    acc += (TA)a[t] * (TA)g[t];
         }
-        for (; j < e; j += SELL_C)
-            acc += (TA)ldg(v + j) * (TA)ldg(x + ldg(ci + j));
         return acc;
     }
 
@@ -358,11 +362,11 @@ namespace nsf
         if (slice >= nSlices)
             return; // whole warps
         const int lane = threadIdx.x & 31;
-        const TA acc = sellRow<TM, TX, TA>(ldg(ss + slice), ldg(ss + slice + 1), lane, ci, v, x);
         const int row = slice * SELL_C + lane;
+        const int r = row < rows ? ldg(perm + row) : 0; // issued before the row's loads
+        const TA acc = sellRow<TM, TX, TA>(ldg(ss + slice), ldg(ss + slice + 1), lane, ci, v, x);
         if (row < rows)
         {
-            const int r = ldg(perm + row);
             double out = alpha * (double)acc;
             if (beta != 0.0)
                 out += beta * (double)y[r];
@@ -381,13 +385,12 @@ namespace nsf
         if (slice >= nSlices)
             return;
         const int lane = threadIdx.x & 31;
-        const TA acc = sellRow<TI, TU, TA>(ldg(ss + slice), ldg(ss + slice + 1), lane, ci, iv, u);
         const int row = slice * SELL_C + lane;
+        const int r = row < rows ? ldg(perm + row) : 0;
+        const TA kr = row < rows ? (TA)ldg(k + r) : (TA)0;
+        const TA acc = sellRow<TI, TU, TA>(ldg(ss + slice), ldg(ss + slice + 1), lane, ci, iv, u);
         if (row < rows)
-        {
-            const int r = ldg(perm + row);
-            a[r] = (TK)(nu * (TA)ldg(k + r) + acc);
-        }
+            a[r] = (TK)(nu * kr + acc);
     }
 
     // SELL values from CSR values after an update: sv[i] = src[i] >= 0 ? cv[src[i]] : 0
