@@ -179,15 +179,14 @@ namespace nsf
                 src.upload(hsrc);
         }
 
-        int blocks() const { return blocksFor((long long)nSlices * SELL_C); }            // a warp per slice
-        int pairBlocks() const { return blocksFor((long long)((nSlices + 1) / 2) * SELL_C); } // per slice pair
+        int blocks() const { return blocksFor((long long)nSlices * SELL_C); }
     };
 
     // y = alpha A x + beta y through the SELL copy (accumulation in TA)
     template <typename TA, typename TM, typename TX, typename TY>
     void sellSpmv(const DevSell<TM> & S, const TX * x, TY * y, double alpha, double beta, cudaStream_t s)
     {
-        NSF_LAUNCH((kSpmvSell<TM, TX, TY, TA>), S.pairBlocks(), s, S.rows, S.nSlices, S.ss.get(), S.perm.get(),
+        NSF_LAUNCH((kSpmvSell<TM, TX, TY, TA>), S.blocks(), s, S.rows, S.nSlices, S.ss.get(), S.perm.get(),
                    S.ci.get(), S.v.get(), x, y, alpha, beta);
     }
 
@@ -500,9 +499,17 @@ extern "C" int nsf_spmv(nsf_csr a, const void * x, void * y, double alpha, doubl
         // SELL-C-sigma: one thread per row, coalesced slice loads, one FMA per stored entry
         cudaStream_t s = asStream(stream);
         if (a->dtype == NSF_F64)
-            sellSpmv<double>(a->s64, (const double *)x, (double *)y, alpha, beta, s);
+        {
+            const DevSell<double> & S = a->s64;
+            NSF_LAUNCH((kSpmvSell<double, double, double, double>), S.blocks(), s, S.rows, S.nSlices, S.ss.get(),
+                       S.perm.get(), S.ci.get(), S.v.get(), (const double *)x, (double *)y, alpha, beta);
+        }
         else
-            sellSpmv<float>(a->s32, (const float *)x, (float *)y, alpha, beta, s);
+        {
+            const DevSell<float> & S = a->s32;
+            NSF_LAUNCH((kSpmvSell<float, float, float, float>), S.blocks(), s, S.rows, S.nSlices, S.ss.get(),
+                       S.perm.get(), S.ci.get(), S.v.get(), (const float *)x, (float *)y, alpha, beta);
+        }
     });
 }
 

@@ -351,83 +351,26 @@ namespace nsf
         return acc;
     }
 
-    // Two slices (rows r0 of slice s0, r1 of slice s0 + 1) per thread, their loads interleaved in
-    // groups of 4 columns each: for short rows (a P1 stencil has 7 entries) a warp's life is a
-    // single load -> gather -> store chain, and the second slice doubles the bytes it has in flight.
-    template <typename TM, typename TX, typename TA>
-    __device__ __forceinline__ void sellRowPair(int b0, int e0, int b1, int e1, int lane, const int * __restrict__ ci,
-                                                const TM * __restrict__ v, const TX * __restrict__ x, TA & acc0,
-                                                TA & acc1)
-    {
-        constexpr int U = 4;
-        acc0 = 0;
-        acc1 = 0;
-        const int w0 = (e0 - b0) / SELL_C, w1 = (e1 - b1) / SELL_C, w = w0 > w1 ? w0 : w1;
-        for (int k = 0; k < w; k += U)
-        {
-            int c[2 * U];
-            TM a[2 * U];
-#pragma unroll
-            for (int t = 0; t < U; t++)
-            {
-                const bool ok0 = k + t < w0, ok1 = k + t < w1;
-                const int j0 = b0 + (k + t) * SELL_C + lane, j1 = b1 + (k + t) * SELL_C + lane;
-                c[t] = ok0 ? ldg(ci + j0) : 0;
-                a[t] = ok0 ? ldg(v + j0) : (TM)0;
-                c[U + t] = ok1 ? ldg(ci + j1) : 0;
-                a[U + t] = ok1 ? ldg(v + j1) : (TM)0;
-            }
-            TX g[2 * U];
-#pragma unroll
-            for (int t = 0; t < U; t++)
-            {
-                g[t] = k + t < w0 ? ldg(x + c[t]) : (TX)0;
-                g[U + t] = k + t < w1 ? ldg(x + c[U + t]) : (TX)0;
-            }
-#pragma unroll
-            for (int t = 0; t < U; t++)
-            {
-                if (k + t < w0)
-                    acc0 += (TA)a[t] * (TA)g[t];
-                if (k + t < w1)
-                    acc1 += (TA)a[U + t] * (TA)g[U + t];
-            }
-        }
-    }
-
-    // y[perm[row]] = alpha * (A x)[row] + beta * y[perm[row]]   (beta == 0: y is not read);
-    // one warp per pair of slices
+    // y[perm[row]] = alpha * (A x)[row] + beta * y[perm[row]]   (beta == 0: y is not read)
     template <typename TM, typename TX, typename TY, typename TA>
     __global__ void __launch_bounds__(TPB) kSpmvSell(int rows, int nSlices, const int * __restrict__ ss,
                                                       const int * __restrict__ perm, const int * __restrict__ ci,
                                                       const TM * __restrict__ v, const TX * __restrict__ x,
                                                       TY * __restrict__ y, double alpha, double beta)
     {
-        const int s0 = 2 * (int)((blockIdx.x * (unsigned)blockDim.x + threadIdx.x) >> 5);
-        if (s0 >= nSlices)
+        const int slice = (int)((blockIdx.x * (unsigned)blockDim.x + threadIdx.x) >> 5);
+        if (slice >= nSlices)
             return; // whole warps
-        const int s1 = s0 + 1 < nSlices ? s0 + 1 : s0; // an odd last slice pairs with itself
         const int lane = threadIdx.x & 31;
-        const int row0 = s0 * SELL_C + lane, row1 = (s0 + 1) * SELL_C + lane;
-        const bool has1 = s0 + 1 < nSlices && row1 < rows;
-        const int r0 = row0 < rows ? ldg(perm + row0) : 0; // issued before the rows' loads
-        const int r1 = has1 ? ldg(perm + row1) : 0;
-        TA acc0, acc1;
-        sellRowPair<TM, TX, TA>(ldg(ss + s0), ldg(ss + s0 + 1), ldg(ss + s1), ldg(ss + s1 + 1), lane, ci, v, x, acc0,
-                                acc1);
-        if (row0 < rows)
+        const int row = slice * SELL_C + lane;
+        const int r = row < rows ? ldg(perm + row) : 0; // issued before the row's loads
+        const TA acc = sellRow<TM, TX, TA>(ldg(ss + slice), ldg(ss + slice + 1), lane, ci, v, x);
+        if (row < rows)
         {
-            double out = alpha * (double)acc0;
+            double out = alpha * (double)acc;
             if (beta != 0.0)
-                out += beta * (double)y[r0];
-            y[r0] = (TY)out;
-        }
-        if (has1)
-        {
-            double out = alpha * (double)acc1;
-            if (beta != 0.0)
-                out += beta * (double)y[r1];
-            y[r1] = (TY)out;
+                out += beta * (double)y[r];
+            y[r] = (TY)out;
         }
     }
 
