@@ -1,8 +1,10 @@
 // sm_103a kernels of the Chorin path.  All sparse work is memory/latency bound (no tensor-core
 // shape), so the kernels are built around:
-//   * CSR-stream SpMV for the big FastConvection matrix: a block streams a contiguous nnz chunk
-//     (coalesced, several independent loads per thread), multiplies into shared memory and then
-//     reduces its rows - full memory-level parallelism for rows of ~15 entries;
+//   * SELL-C-sigma (C = 32) for the operators applied once per step (FastConvection, D, G, the
+//     library SpMV and the adjoint's transposes): one thread per row, coalesced slice loads and
+//     one FMA per entry, because FP64 issues at 1/64 of the FP32 rate on this GPU and the
+//     product-plus-sum of a CSR-stream kernel made FP64 SpMV issue-bound (the CSR-stream kernels
+//     remain for reference);
 //   * row groups of L lanes (L = 2..32) per CSR row for the sweeps and the solver SpMVs;
 //   * grids capped at a few blocks per SM (grid-stride loops), and one deterministic reduction per
 //     producing kernel: every block writes its block sum, the last block to finish (atomic ticket)
