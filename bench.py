@@ -538,10 +538,13 @@ def bench_poisson(args):
                      "us_per_iteration": round(1e6 * best / max(1, its), 3),
                      "pcg_iteration_gbs": round(it_bytes * its / best / 1e9, 1)}
         del s
-    # SpMV alone from DRAM: the L2 is flushed (a 256 MB write) before every launch.  A 25 us
-    # launch bracketed by its own events carries the event and launch gaps, so the time is
-    # differential: events around reps x (flush, SpMV) minus events around reps x (flush).
+    # SpMV alone from DRAM: the L2 is flushed before every launch by a 256 MB write followed by a
+    # read of the same buffer (the read pass takes the write-backs of the dirty lines, which would
+    # otherwise share DRAM with the SpMV).  A 25 us launch bracketed by its own events carries the
+    # event and launch gaps, so the time is differential: events around reps x (flush, SpMV) minus
+    # events around reps x (flush).
     flush = torch.empty(64 << 20, dtype=torch.float32, device="cuda")
+    flush_sum = torch.zeros((), dtype=torch.float32, device="cuda")
     spmv = {}
     for name, dt, tdt in (("fp64", G.NSF_F64, torch.float64), ("fp32", G.NSF_F32, torch.float32)):
         A = G.CsrF.from_host(host, dtype=dt)
@@ -555,6 +558,7 @@ def bench_poisson(args):
             e0.record()
             for rep in range(reps):
                 flush.fill_(float(rep))
+                flush_sum.copy_(flush.sum())
                 if with_spmv:
                     G.spmv(A, xv, yv)
             e1.record()
