@@ -792,8 +792,8 @@ def main():
                     help="channel workload: mass-solve preconditioner, 1 multicolor SGS, 2 Jacobi")
     ap.add_argument("--adjoint-steps", type=int, default=1000)
     ap.add_argument("--adjoint-checkpoint", type=int, default=50)
-    ap.add_argument("--adjoint-precision", default="f64", choices=["f64", "mixedsolve"])
-    ap.add_argument("--adjoint-vel-method", type=int, default=1, choices=[1, 2],
+    ap.add_argument("--adjoint-precision", default="mixedsolve", choices=["f64", "mixedsolve"])
+    ap.add_argument("--adjoint-vel-method", type=int, default=2, choices=[1, 2],
                     help="mass-solve preconditioner: 1 multicolor SGS, 2 Jacobi")
     ap.add_argument("--adjoint-reps", type=int, default=1, help="timed gradient evaluations")
     ap.add_argument("--adjoint-warmup", type=int, default=1, help="untimed gradient evaluations")
