@@ -102,13 +102,17 @@ class Clocks:
 
 
 def run_cpu_reference(mesh_path: str, steps: int, warmup: int, vel_method: int = 1):
-    """Time the oracle's FP64 Chorin step (the CPU restatement of the reference path)."""
+    """Time the oracle's FP64 Chorin step (the CPU restatement of the reference path) on every host
+    thread (its OpenMP build; the single-thread build if that cannot be compiled).  The thread
+    count is left in CPU_THREADS."""
+    global CPU_THREADS
     import oracle
     oracle.build()
     m = oracle.Mesh(mesh_path)
     ctx = oracle.Context(m, PEAK, True)
     ch = oracle.Chorin(ctx, NU, TAU, vel_method=vel_method, vel_max_iters=500, vel_tol=VEL_TOL, pres_max_iters=5000,
-                       pres_tol=PRES_TOL)
+                       pres_tol=PRES_TOL, mt=True)
+    CPU_THREADS = ch.threads
     for _ in range(warmup):
         ch.step()
     t0 = time.perf_counter()
@@ -119,6 +123,7 @@ def run_cpu_reference(mesh_path: str, steps: int, warmup: int, vel_method: int =
     return steps / dt, dt, ctx, (u, p, oracle.forces(m, u, p, NU))
 
 
+CPU_THREADS = 1                    # host threads of the last CPU-oracle timing
 ACC_STEPS = 100                    # accuracy run: mixed vs FP64 from rest
 ACC_CHECKPOINTS = (4, 25, 50, 100)  # steps at which the fields are compared
 
@@ -208,7 +213,8 @@ def bench_small(args):
         om = oracle.Mesh(path)
         oc = oracle.Context(om, peak, True)
         ch = oracle.Chorin(oc, nu, tau, vel_method=1, vel_max_iters=500, vel_tol=1e-10, pres_max_iters=5000,
-                           pres_tol=1e-10)
+                           pres_tol=1e-10, mt=True)
+        cpu_threads = ch.threads
         t0 = time.perf_counter()
         for _ in range(k):
             ch.step()
@@ -233,8 +239,8 @@ def bench_small(args):
         "variants": {n: {kk: v for kk, v in r.items() if kk not in ("u", "p")} for n, r in res.items()},
         "mixed_vs_fp64_after_all_steps": {"u_rel_l2": rel(res["mixed"]["u"], res["fp64"]["u"]),
                                           "p_rel_l2": rel(res["mixed"]["p"], res["fp64"]["p"])},
-        "cpu_baseline": {"value": round(k / cpu_t, 3), "unit": "steps/s", "cores": 1, "kind": "port",
-                         "sample": f"the first {k} steps from rest, FP64 C oracle"},
+        "cpu_baseline": {"value": round(k / cpu_t, 3), "unit": "steps/s", "cores": cpu_threads, "kind": "port",
+                         "sample": f"the first {k} steps from rest, FP64 C oracle on {cpu_threads} host threads"},
         "fp64_vs_oracle": {"steps": k, "u_rel_l2": rel(ug, uo), "p_rel_l2": rel(pg, po)},
     }
 
@@ -244,17 +250,20 @@ ADJ_METRIC = "adjoint drag gradient time (d/dnu + 16 inflow coefficients), h=0.0
 
 
 def _adjoint_oracle_sample(path, k, theta, basis, g0, scale):
-    """The FP64 CPU adjoint (C oracle) on the first k steps from rest, every step weighted
-    scale / k.  Returns (seconds, J, dJ/dnu, dJ/dtheta)."""
+    """The FP64 CPU adjoint (C oracle, on every host thread) on the first k steps from rest, every
+    step weighted scale / k.  Returns (seconds, J, dJ/dnu, dJ/dtheta); the thread count is left in
+    CPU_THREADS."""
+    global CPU_THREADS
     import numpy as np
     import oracle
     oracle.build()
     om = oracle.Mesh(path)
     oc = oracle.Context(om, ADJ_PEAK, True)
     w = np.full(k, scale / k)
+    CPU_THREADS = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1)) if oracle.lib_mt() else 1
     t0 = time.perf_counter()
     J, gnu, gdir, _ = oracle.adjoint_run(oc, om, ADJ_NU, ADJ_TAU, k, w, dir_vx=g0 + basis @ theta, vel_tol=ADJ_TOL,
-                                         pres_tol=ADJ_TOL, solve_tol=ADJ_TOL)
+                                         pres_tol=ADJ_TOL, solve_tol=ADJ_TOL, mt=True)
     return time.perf_counter() - t0, J, gnu, basis.T @ gdir
 
 
@@ -375,9 +384,10 @@ def bench_adjoint(args):
         "variants": variants,
     }
     if k > 0:
-        line["cpu_baseline"] = {"value": round(cpu_t * n / k, 1), "unit": "s", "cores": 1, "kind": "port",
-                                "sample": f"FP64 C oracle forward + adjoint over the first {k} steps from rest, scaled "
-                                          f"by {n}/{k} to the {n}-step gradient (the oracle keeps every state)"}
+        line["cpu_baseline"] = {"value": round(cpu_t * n / k, 1), "unit": "s", "cores": CPU_THREADS, "kind": "port",
+                                "sample": f"FP64 C oracle forward + adjoint over the first {k} steps from rest on "
+                                          f"{CPU_THREADS} host threads, scaled by {n}/{k} to the {n}-step gradient "
+                                          f"(the oracle keeps every state)"}
         line["gpu_vs_cpu_adjoint_sample"] = {"steps": k, "J_rel": abs(Js - Jo) / abs(Jo),
                                              "dnu_rel": abs(gnus - gnuo) / abs(gnuo),
                                              "dtheta_rel_l2": float(np.linalg.norm(gths - gtho) / np.linalg.norm(gtho))}
@@ -838,9 +848,9 @@ def main():
         print(json.dumps({"impl": "reference", "metric": ADJ_METRIC, "value": v, "unit": "s", "n_gpus": 0,
                           "steps": 1, "warmup": 0, "higher_is_better": False, "dtype": "f64",
                           "config": {"workload": "adjoint drag gradient, DFG channel h=0.01, 1000 steps"},
-                          "cpu_baseline": {"value": v, "unit": "s", "cores": 1, "kind": "port",
-                                           "sample": f"FP64 C oracle forward + adjoint over {k} steps, scaled to "
-                                                     f"{args.adjoint_steps}"},
+                          "cpu_baseline": {"value": v, "unit": "s", "cores": CPU_THREADS, "kind": "port",
+                                           "sample": f"FP64 C oracle forward + adjoint over {k} steps on {CPU_THREADS} "
+                                                     f"host threads, scaled to {args.adjoint_steps}"},
                           "e2e": {"value": v, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}))
         return
 
@@ -867,8 +877,9 @@ def main():
                 "data": "synthetic (seeded DFG channel mesh, h=0.005)",
                 "config": {"workload": "DFG channel h=0.005, Umax=1.5, nu=1e-3, tau=1e-4, P2/P1, "
                                        "pressure PCG-SGS to 1e-8 rel", "N": ctx.N, "P": ctx.P},
-                "cpu_baseline": {"value": round(sps, 4), "unit": "steps/s", "cores": 1, "kind": "port",
-                                 "sample": f"{k} time steps after {min(args.warmup, 2)} warm-up steps, FP64 C oracle"},
+                "cpu_baseline": {"value": round(sps, 4), "unit": "steps/s", "cores": CPU_THREADS, "kind": "port",
+                                 "sample": f"{k} time steps after {min(args.warmup, 2)} warm-up steps, FP64 C oracle "
+                                           f"on {CPU_THREADS} host threads"},
                 "e2e": {"value": round(sps, 4), "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
         print(json.dumps(line))
         return
@@ -885,9 +896,9 @@ def main():
             try:
                 path = make_mesh(tmp, H, 0)
                 sps, dt, _, (uo, po, fo) = run_cpu_reference(path, args.cpu_sample_steps, 1, args.vel_method)
-                line["cpu_baseline"] = {"value": round(sps, 4), "unit": "steps/s", "cores": 1, "kind": "port",
+                line["cpu_baseline"] = {"value": round(sps, 4), "unit": "steps/s", "cores": CPU_THREADS, "kind": "port",
                                         "sample": f"{args.cpu_sample_steps} time steps (after 1 warm-up) of the same "
-                                                  f"workload, FP64 C oracle, single thread"}
+                                                  f"workload, FP64 C oracle on {CPU_THREADS} host threads (OpenMP)"}
                 if f64_step4 is not None and args.cpu_sample_steps == 3:
                     # the oracle has run 4 steps from rest: the FP64 GPU state after 4 steps vs it
                     import numpy as np

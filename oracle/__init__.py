@@ -60,13 +60,38 @@ def build(quiet: bool = True) -> str:
     return os.path.join(HERE, "_build", "liboracle.so")
 
 
+_LIB_MT = None
+
+
+def build_mt() -> bool:
+    """Compile liboracle_mt.so (OpenMP); False if this toolchain cannot."""
+    out = subprocess.run(["make", "-C", HERE, "-s", "mt"], capture_output=True, text=True)
+    return out.returncode == 0
+
+
+def lib_mt():
+    """The OpenMP build of the oracle (the timed CPU baseline on all host cores), or None."""
+    global _LIB_MT
+    if _LIB_MT is None:
+        path = os.path.join(HERE, "_build", "liboracle_mt.so")
+        if not os.path.exists(path) and not build_mt():
+            return None
+        _LIB_MT = _configure(C.CDLL(path))
+    return _LIB_MT
+
+
 def lib():
     global _LIB
     if _LIB is None:
         path = os.path.join(HERE, "_build", "liboracle.so")
         if not os.path.exists(path):
             build()
-        L = C.CDLL(path)
+        _LIB = _configure(C.CDLL(path))
+    return _LIB
+
+
+def _configure(L):
+    if True:
         L.orc_last_error.restype = C.c_char_p
         L.orc_mesh_load.restype = C.POINTER(MeshS)
         L.orc_mesh_load.argtypes = [C.c_char_p]
@@ -98,8 +123,7 @@ def lib():
         L.orc_forces_weights.argtypes = [C.POINTER(MeshS), C.c_int, f64p, f64p, f64p]
         L.orc_adjoint_run.argtypes = [C.POINTER(ContextS), C.POINTER(MeshS), C.c_int, C.POINTER(ChorinCfgS), f64p,
                                       f64p, f64p, C.c_int, f64p, f64p, C.c_double, f64p, f64p, f64p]
-        _LIB = L
-    return _LIB
+    return L
 
 
 def _arr(ptr, n, dtype):
@@ -314,17 +338,22 @@ def forces(mesh: Mesh, u, p, nu: float, group: str = "Circle") -> np.ndarray:
 
 class Chorin:
     """FP64 Chorin stepper of the oracle.  vel_method 0 = multicolor GS (RMS target),
-    1 = CG + multicolor SGS (relative tolerance)."""
+    1 = CG + multicolor SGS, 2 = CG + Jacobi (relative tolerance).  mt: run on the OpenMP build
+    (all host threads, OMP_NUM_THREADS); self.threads says what ran (1 if that build is missing)."""
 
     def __init__(self, ctx: Context, nu, tau, vel_method=1, vel_max_iters=200, vel_tol=1e-10,
-                 pres_max_iters=2000, pres_tol=1e-10):
+                 pres_max_iters=2000, pres_tol=1e-10, mt=False):
         self.ctx = ctx
+        self._L = lib_mt() if mt else None
+        self.threads = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1)) if self._L else 1
+        if self._L is None:
+            self._L = lib()
         cfg = ChorinCfgS(nu, tau, vel_method, vel_max_iters, vel_tol, pres_max_iters, pres_tol)
-        self._h = lib().orc_chorin_create(C.byref(ctx._s), C.byref(cfg))
+        self._h = self._L.orc_chorin_create(C.byref(ctx._s), C.byref(cfg))
 
     def step(self):
         st = np.zeros(6, dtype=np.float64)
-        rc = lib().orc_chorin_step(self._h, _ptr(st, C.c_double))
+        rc = self._L.orc_chorin_step(self._h, _ptr(st, C.c_double))
         if rc != 0:
             raise RuntimeError(f"oracle Chorin step failed with status {rc}")
         return st
@@ -332,24 +361,24 @@ class Chorin:
     def state(self):
         u = np.zeros(2 * self.ctx.N, dtype=np.float64)
         p = np.zeros(self.ctx.P, dtype=np.float64)
-        lib().orc_chorin_get(self._h, _ptr(u, C.c_double), _ptr(p, C.c_double))
+        self._L.orc_chorin_get(self._h, _ptr(u, C.c_double), _ptr(p, C.c_double))
         return u, p
 
     def set_state(self, u, p):
         u = np.ascontiguousarray(u, dtype=np.float64)
         p = np.ascontiguousarray(p, dtype=np.float64)
-        lib().orc_chorin_set(self._h, _ptr(u, C.c_double), _ptr(p, C.c_double))
+        self._L.orc_chorin_set(self._h, _ptr(u, C.c_double), _ptr(p, C.c_double))
 
     def set_dirichlet(self, dir_vx):
         """x values of the Dirichlet velocity nodes (ctx.dir_ids order), imposed on the state too."""
         d = np.ascontiguousarray(dir_vx, dtype=np.float64)
         if d.shape != (len(self.ctx.dir_ids),):
             raise ValueError("one value per Dirichlet node")
-        lib().orc_chorin_set_dirichlet(self._h, _ptr(d, C.c_double))
+        self._L.orc_chorin_set_dirichlet(self._h, _ptr(d, C.c_double))
 
     def __del__(self):
         try:
-            lib().orc_chorin_free(self._h)
+            self._L.orc_chorin_free(self._h)
         except Exception:
             pass
 
@@ -369,11 +398,12 @@ def forces_weights(mesh: Mesh, group: str = "Circle"):
 
 def adjoint_run(ctx: Context, mesh: Mesh, nu, tau, n_steps, w_drag, w_lift=None, dir_vx=None, u0=None, p0=None,
                 vel_method=1, vel_max_iters=100000, vel_tol=1e-14, pres_max_iters=100000, pres_tol=1e-14,
-                solve_tol=1e-14, group: str = "Circle"):
-    """FP64 forward + discrete-adjoint sweep of the oracle (orc_adjoint_run).
+                solve_tol=1e-14, group: str = "Circle", mt=False):
+    """FP64 forward + discrete-adjoint sweep of the oracle (orc_adjoint_run); mt: the OpenMP build
+    (falls back to the single-thread build if it is missing).
 
     Returns (J, dJ/dnu, dJ/d dirVx [nDir], dJ/du0 [2N])."""
-    L = lib()
+    L = (lib_mt() if mt else None) or lib()
     gid = L.orc_group_id(mesh._p, group.encode())
     if gid < 0:
         raise ValueError(f"no border group {group!r}")

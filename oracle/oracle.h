@@ -106,6 +106,14 @@ int orc_gs_solve_ex(const orc_csr *a, const orc_coloring *c, int numCh, const do
 int orc_pcg(const orc_csr *a, const orc_coloring *c, int precond, const double *b, double *x,
             int maxIters, double relTol, int *iters, double *relRes);
 
+/* the same PCG on a system prepared once (color permutation and diagonal split), for repeated
+   solves with one matrix; a reference solver object likewise keeps its permuted matrix */
+typedef struct orc_sys_s orc_sys;
+orc_sys *orc_sys_create(const orc_csr *a, const orc_coloring *c);
+void orc_sys_free(orc_sys *s);
+int orc_sys_pcg(const orc_sys *s, int precond, const double *b, double *x, int maxIters, double relTol, int *iters,
+                double *relRes);
+
 /* y = (D+L) D^-1 (D+U) inverse applied to r in colored order (the preconditioner alone) */
 void orc_sgs_apply(const orc_csr *a, const orc_coloring *c, const double *r, double *z);
 

@@ -38,12 +38,12 @@ static void spmv_t_add(const orc_csr *a, const double *vals, const double *x, do
     }
 }
 
-static int solve(const orc_csr *a, const orc_coloring *c, const double *b, double *x, double tol)
+static int solve(const orc_sys *s, int n, const double *b, double *x, double tol)
 {
     int it = 0;
     double rr = 0;
-    memset(x, 0, sizeof(double) * a->rows);
-    const int st = orc_pcg(a, c, 1, b, x, 100000, tol, &it, &rr);
+    memset(x, 0, sizeof(double) * n);
+    const int st = orc_sys_pcg(s, 1, b, x, 100000, tol, &it, &rr);
     return st == 0 ? 0 : st;
 }
 
@@ -99,6 +99,7 @@ int orc_adjoint_run(const orc_context *ctx, const orc_mesh *m, int gid, const or
     orc_coloring colM, colP;
     orc_coloring_build(&ctx->M, &colM);
     orc_coloring_build(&ctx->Kpi, &colP);
+    orc_sys *sysM = orc_sys_create(&ctx->M, &colM), *sysP = orc_sys_create(&ctx->Kpi, &colP);
     const double invTau = 1.0 / tau;
     for (int n = nSteps - 1; n >= 0 && status == 0; n--)
     {
@@ -123,13 +124,13 @@ int orc_adjoint_run(const orc_context *ctx, const orc_mesh *m, int gid, const or
         /* second mass solve and the gradient */
         for (int i = 0; i < 2 * N; i++)
             rhs[i] = -tau * lam[i];
-        status |= solve(&ctx->M, &colM, rhs, x, solveTol);
-        status |= solve(&ctx->M, &colM, rhs + N, x + N, solveTol);
+        status |= solve(sysM, N, rhs, x, solveTol);
+        status |= solve(sysM, N, rhs + N, x + N, solveTol);
         spmv_t_add(&ctx->G, ctx->G.val, x, lp);
         for (int i = 0; i < nI; i++)
             lpI[i] = lp[ctx->intP[i]];
         /* pressure solve and the divergence */
-        status |= solve(&ctx->Kpi, &colP, lpI, y, solveTol);
+        status |= solve(sysP, nI, lpI, y, solveTol);
         memset(lDiv, 0, sizeof(double) * P);
         for (int i = 0; i < nI; i++)
             lDiv[ctx->intP[i]] = -invTau * y[i];
@@ -146,8 +147,8 @@ int orc_adjoint_run(const orc_context *ctx, const orc_mesh *m, int gid, const or
         /* first mass solve, A^T and the linearisation */
         for (int i = 0; i < 2 * N; i++)
             rhs[i] = -tau * ls[i];
-        status |= solve(&ctx->M, &colM, rhs, x, solveTol);
-        status |= solve(&ctx->M, &colM, rhs + N, x + N, solveTol);
+        status |= solve(sysM, N, rhs, x, solveTol);
+        status |= solve(sysM, N, rhs + N, x + N, solveTol);
         orc_fastconv(ctx, nu, u, A);
         memcpy(lam, ls, sizeof(double) * 2 * N);
         spmv_t_add(&ctx->K, A, x, lam);
@@ -164,6 +165,8 @@ int orc_adjoint_run(const orc_context *ctx, const orc_mesh *m, int gid, const or
     }
     orc_coloring_free(&colM);
     orc_coloring_free(&colP);
+    orc_sys_free(sysM);
+    orc_sys_free(sysP);
     /* the initial state's Dirichlet rows hold (dirVx, 0) as well */
     for (int d = 0; d < ctx->nDir; d++)
     {

@@ -26,6 +26,7 @@ struct orc_chorin_s
     const orc_context *ctx;
     orc_chorin_cfg cfg;
     orc_coloring colM, colP;
+    orc_sys *sysM, *sysP; /* M and Kp_int prepared once for the PCG solves */
     double *u, *p, *pInt, *Avals, *rhs, *acc, *div, *rhsP, *g;
     double *dirVx; /* x values imposed on the Dirichlet nodes (ctx->dirVx unless set) */
 };
@@ -37,6 +38,8 @@ orc_chorin *orc_chorin_create(const orc_context *ctx, const orc_chorin_cfg *cfg)
     s->cfg = *cfg;
     orc_coloring_build(&ctx->M, &s->colM);
     orc_coloring_build(&ctx->Kpi, &s->colP);
+    s->sysM = orc_sys_create(&ctx->M, &s->colM);
+    s->sysP = orc_sys_create(&ctx->Kpi, &s->colP);
     const int N = ctx->N, P = ctx->P;
     s->u = (double *)calloc(2 * N, sizeof(double));
     s->p = (double *)calloc(P, sizeof(double));
@@ -63,6 +66,8 @@ void orc_chorin_free(orc_chorin *s)
         return;
     orc_coloring_free(&s->colM);
     orc_coloring_free(&s->colP);
+    orc_sys_free(s->sysM);
+    orc_sys_free(s->sysP);
     free(s->u);
     free(s->p);
     free(s->pInt);
@@ -139,7 +144,7 @@ static int mass_solve(orc_chorin *s, const double *rhs, double *acc, double *res
         int it = 0;
         double rr = 0;
         /* velMethod 1: SGS preconditioner, 2: Jacobi */
-        int st = orc_pcg(&ctx->M, &s->colM, s->cfg.velMethod == 2 ? 2 : 1, rhs + ch * N, acc + ch * N,
+        int st = orc_sys_pcg(s->sysM, s->cfg.velMethod == 2 ? 2 : 1, rhs + ch * N, acc + ch * N,
                          s->cfg.velMaxIters, s->cfg.velTol, &it, &rr);
         (void)st;
         if (it > itMax)
@@ -171,7 +176,7 @@ int orc_chorin_step(orc_chorin *s, double *stats)
     for (int i = 0; i < ctx->nIntP; i++)
         s->rhsP[i] = s->div[ctx->intP[i]];
     int itP = 0;
-    int st = orc_pcg(&ctx->Kpi, &s->colP, 1, s->rhsP, s->pInt, s->cfg.presMaxIters, s->cfg.presTol, &itP, &resP);
+    int st = orc_sys_pcg(s->sysP, 1, s->rhsP, s->pInt, s->cfg.presMaxIters, s->cfg.presTol, &itP, &resP);
     memset(s->p, 0, sizeof(double) * P);
     for (int i = 0; i < ctx->nIntP; i++)
         s->p[ctx->intP[i]] = s->pInt[i];

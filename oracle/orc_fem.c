@@ -576,6 +576,7 @@ void orc_forces_weights(const orc_mesh *m, int gid, double *wV, double *wPx, dou
 void orc_fastconv(const orc_context *ctx, double nu, const double *u, double *Avals)
 {
     const orc_csr *I = &ctx->I;
+#pragma omp parallel for schedule(static)
     for (int k = 0; k < I->rows; k++)
     {
         double s = 0;

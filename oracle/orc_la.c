@@ -38,6 +38,7 @@ void orc_csr_free(orc_csr *a)
 
 void orc_spmv(const orc_csr *a, const double *x, double *y)
 {
+#pragma omp parallel for schedule(static)
     for (int i = 0; i < a->rows; i++)
     {
         double s = 0;
@@ -51,6 +52,7 @@ void orc_spmv(const orc_csr *a, const double *x, double *y)
 void orc_spmm2(const orc_csr *a, const double *vals, const double *x, double *y)
 {
     const int n = a->rows, m = a->cols;
+#pragma omp parallel for schedule(static)
     for (int i = 0; i < n; i++)
     {
         double s0 = 0, s1 = 0;
@@ -371,6 +373,8 @@ static void gs_ctx_free(gs_ctx *g)
 /* one color phase: rows [r0, r1) of the stripped, permuted system */
 static void gs_phase(const gs_ctx *g, int r0, int r1, double *x, const double *b)
 {
+    /* the rows of one color do not couple: any order, any number of threads */
+#pragma omp parallel for schedule(static)
     for (int r = r0; r < r1; r++)
     {
         double s = 0;
@@ -492,8 +496,11 @@ static void precond_apply(const gs_ctx *g, const orc_coloring *c, int precond, c
     if (precond == 1)
         sgs_colored(g, c, r, z);
     else if (precond == 2)
+    {
+#pragma omp parallel for schedule(static)
         for (int i = 0; i < n; i++)
             z[i] = r[i] * g->invD[i];
+    }
     else
         memcpy(z, r, sizeof(double) * n);
 }
@@ -501,6 +508,7 @@ static void precond_apply(const gs_ctx *g, const orc_coloring *c, int precond, c
 static double dot(const double *a, const double *b, int n)
 {
     double s = 0;
+#pragma omp parallel for schedule(static) reduction(+ : s)
     for (int i = 0; i < n; i++)
         s += a[i] * b[i];
     return s;
@@ -508,20 +516,14 @@ static double dot(const double *a, const double *b, int n)
 
 /* PCG in the colored ordering (the system is permuted once at entry and the solution permuted
    back at exit, as cu::GaussSeidel keeps its vectors permuted during a solve). */
-int orc_pcg(const orc_csr *a, const orc_coloring *c, int precond, const double *b, double *x,
-            int maxIters, double relTol, int *iters, double *relRes)
+static int pcg_core(const gs_ctx *g, const orc_coloring *c, int precond, const double *b, double *x,
+                    int maxIters, double relTol, int *iters, double *relRes)
 {
-    gs_ctx g;
-    memset(&g, 0, sizeof g);
-    if (gs_ctx_build(a, c, &g))
-    {
-        gs_ctx_free(&g);
-        return 1;
-    }
-    const int n = a->rows;
+    const int n = g->full.rows;
     double *xp = (double *)malloc(sizeof(double) * n), *bp = (double *)malloc(sizeof(double) * n);
     double *r = (double *)malloc(sizeof(double) * n), *z = (double *)malloc(sizeof(double) * n);
     double *p = (double *)malloc(sizeof(double) * n), *q = (double *)malloc(sizeof(double) * n);
+#pragma omp parallel for schedule(static)
     for (int i = 0; i < n; i++)
     {
         xp[i] = x[c->perm[i]];
@@ -529,7 +531,8 @@ int orc_pcg(const orc_csr *a, const orc_coloring *c, int precond, const double *
     }
     int status = 3, it = 0;
     double bnorm = sqrt(dot(bp, bp, n));
-    orc_spmv(&g.full, xp, q);
+    orc_spmv(&g->full, xp, q);
+#pragma omp parallel for schedule(static)
     for (int i = 0; i < n; i++)
         r[i] = bp[i] - q[i];
     double rnorm = sqrt(dot(r, r, n));
@@ -539,12 +542,12 @@ int orc_pcg(const orc_csr *a, const orc_coloring *c, int precond, const double *
         status = 0;
     else
     {
-        precond_apply(&g, c, precond, r, z);
+        precond_apply(g, c, precond, r, z);
         memcpy(p, z, sizeof(double) * n);
         double rz = dot(r, z, n);
         for (it = 1; it <= maxIters; it++)
         {
-            orc_spmv(&g.full, p, q);
+            orc_spmv(&g->full, p, q);
             double pq = dot(p, q, n);
             if (!(pq > 0))
             {
@@ -552,6 +555,7 @@ int orc_pcg(const orc_csr *a, const orc_coloring *c, int precond, const double *
                 break;
             }
             double alpha = rz / pq;
+#pragma omp parallel for schedule(static)
             for (int i = 0; i < n; i++)
             {
                 xp[i] += alpha * p[i];
@@ -568,16 +572,18 @@ int orc_pcg(const orc_csr *a, const orc_coloring *c, int precond, const double *
                 status = 0;
                 break;
             }
-            precond_apply(&g, c, precond, r, z);
+            precond_apply(g, c, precond, r, z);
             double rzNew = dot(r, z, n);
             double beta = rzNew / rz;
             rz = rzNew;
+#pragma omp parallel for schedule(static)
             for (int i = 0; i < n; i++)
                 p[i] = z[i] + beta * p[i];
         }
         if (it > maxIters)
             it = maxIters;
     }
+#pragma omp parallel for schedule(static)
     for (int i = 0; i < n; i++)
         x[c->perm[i]] = xp[i];
     *iters = it;
@@ -588,6 +594,53 @@ int orc_pcg(const orc_csr *a, const orc_coloring *c, int precond, const double *
     free(z);
     free(p);
     free(q);
-    gs_ctx_free(&g);
     return status;
+}
+
+int orc_pcg(const orc_csr *a, const orc_coloring *c, int precond, const double *b, double *x,
+            int maxIters, double relTol, int *iters, double *relRes)
+{
+    gs_ctx g;
+    memset(&g, 0, sizeof g);
+    if (gs_ctx_build(a, c, &g))
+    {
+        gs_ctx_free(&g);
+        return 1;
+    }
+    const int st = pcg_core(&g, c, precond, b, x, maxIters, relTol, iters, relRes);
+    gs_ctx_free(&g);
+    return st;
+}
+
+/* a system prepared once (color-permuted, diagonal split off) for repeated PCG solves */
+struct orc_sys_s
+{
+    gs_ctx g;
+    const orc_coloring *c;
+};
+
+orc_sys *orc_sys_create(const orc_csr *a, const orc_coloring *c)
+{
+    orc_sys *s = (orc_sys *)calloc(1, sizeof *s);
+    s->c = c;
+    if (gs_ctx_build(a, c, &s->g))
+    {
+        orc_sys_free(s);
+        return NULL;
+    }
+    return s;
+}
+
+void orc_sys_free(orc_sys *s)
+{
+    if (!s)
+        return;
+    gs_ctx_free(&s->g);
+    free(s);
+}
+
+int orc_sys_pcg(const orc_sys *s, int precond, const double *b, double *x, int maxIters, double relTol, int *iters,
+                double *relRes)
+{
+    return pcg_core(&s->g, s->c, precond, b, x, maxIters, relTol, iters, relRes);
 }
