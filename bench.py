@@ -427,7 +427,7 @@ def bench_batch(args):
         steppers = []
         for b in range(B):
             ctx = G.build_chorin_context(mesh, 4.0 * float(umax[b]))
-            steppers.append(G.ChorinStepper(ctx, float(nus[b]), tau, precision=G.NSF_PREC_MIXED, vel_method=1,
+            steppers.append(G.ChorinStepper(ctx, float(nus[b]), tau, precision=G.NSF_PREC_MIXED, vel_method=2,
                                             vel_max_iters=500, vel_tol=VEL_TOL, pres_max_iters=5000,
                                             pres_tol=PRES_TOL, check_interval=8, use_graph=True, max_outer=4,
                                             inner_tol=1e-5))
@@ -458,6 +458,17 @@ def bench_batch(args):
 
         t_one = run([(steppers[0], streams[0])], K)
         t_all = run(list(zip(steppers, streams)), K)
+        # the same instances as one pack: every instance's step a branch of one graph
+        pack = G.Pack(steppers)
+        pack.step(1, master.cuda_stream)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(master)
+        pack.step(K, master.cuda_stream)
+        e1.record(master)
+        torch.cuda.synchronize()
+        t_pack = e0.elapsed_time(e1) / 1e3
+        del pack
         # one synchronous step per instance: statistics and status
         status, pres_iters = [], []
         for st, s in zip(steppers, streams):
@@ -483,8 +494,105 @@ def bench_batch(args):
                    "execution": "one graph-captured stepper per instance on its own stream, cluster-resident solves"},
         "one_instance_steps_per_s": round(one, 2),
         "speedup_vs_one_at_a_time": round(agg / one, 2),
+        "one_graph_pack": {"instance_steps_per_s": round(B * K / t_pack, 2),
+                           "execution": "all instances' steps as branches of one CUDA graph (nsf_pack), one launch "
+                                        "per step"},
         "status_all_ok": all(s == 0 for s in status),
         "pres_iters_range": [min(pres_iters), max(pres_iters)],
+    }
+
+
+def bench_pack(args):
+    """Uneven pack: 16 instances on each of three channel meshes (h = 0.025, 0.01, 0.005; synthetic,
+    seed 0), U_max ~ U[0.2, 1.5] and nu ~ logU[5e-4, 2e-3] per instance (seed 1), mixed precision,
+    Jacobi mass solves, pressure to 1e-8, tau = 5e-5 (inside the explicit limit
+    2 / (nu lambda_max(M^-1 K)) = 9.9e-5 of the finest mesh at nu = 2e-3).  All 48 time steps are
+    branches of one CUDA graph (nsf_pack): one launch advances every instance, and every solve stays
+    inside a thread-block cluster so the branches run side by side.  Timed: K launches (CUDA events
+    on the launching stream).  Compared with the same 48 steppers stepped one after another."""
+    import math
+
+    import numpy as np
+    import torch
+
+    import nsfemoptim_gb300 as G
+
+    per, K, W, tau = args.pack_per_mesh, args.pack_steps, 3, 5e-5
+    hs = (0.025, 0.01, 0.005)
+    rng = np.random.default_rng(1)
+    tmp = tempfile.mkdtemp()
+    old = os.environ.get("NSF_PCG_PATH")
+    os.environ["NSF_PCG_PATH"] = "auto-cluster"
+    try:
+        t0 = time.perf_counter()
+        steppers, meshes, sizes = [], [], {}
+        for h in hs:
+            mesh = G.load_gmsh(make_mesh(tmp, h, 0))
+            meshes.append(mesh)
+            for _ in range(per):
+                umax = float(rng.uniform(0.2, 1.5))
+                nu = float(math.exp(rng.uniform(math.log(5e-4), math.log(2e-3))))
+                ctx = G.build_chorin_context(mesh, 4.0 * umax)
+                sizes[h] = (ctx.N, ctx.P)
+                steppers.append(G.ChorinStepper(ctx, nu, tau, precision=G.NSF_PREC_MIXED, vel_method=2,
+                                                vel_max_iters=500, vel_tol=VEL_TOL, pres_max_iters=5000,
+                                                pres_tol=PRES_TOL, check_interval=8, use_graph=True, max_outer=4,
+                                                inner_tol=1e-5))
+        setup_s = time.perf_counter() - t0
+        stream = torch.cuda.Stream()
+        pack = G.Pack(steppers)
+        pack.step(W, stream.cuda_stream)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        pack.step(K, stream.cuda_stream)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        t_pack = e0.elapsed_time(e1) / 1e3
+        # the same steppers one after another (each its own graph), and one of each mesh alone
+        e0.record(stream)
+        for _ in range(K):
+            for st in steppers:
+                st.launch(1, stream.cuda_stream)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        t_seq = e0.elapsed_time(e1) / 1e3
+        alone = {}
+        for i, h in enumerate(hs):
+            st = steppers[i * per]
+            e0.record(stream)
+            st.launch(K, stream.cuda_stream)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            alone[str(h)] = round(K / (e0.elapsed_time(e1) / 1e3), 2)
+        status = []
+        for st in steppers:
+            st.step(1, stream.cuda_stream)
+            status.append(int(st.stats()["status"]))
+        launches = G.kernel_launches()
+        del pack
+    finally:
+        if old is None:
+            os.environ.pop("NSF_PCG_PATH", None)
+        else:
+            os.environ["NSF_PCG_PATH"] = old
+        shutil.rmtree(tmp, ignore_errors=True)
+    n = len(steppers)
+    return {
+        "metric": "config 4b: uneven pack of channel instances on three meshes, aggregate instance-steps/s",
+        "value": round(n * K / t_pack, 2), "unit": "instance-steps/s", "n_gpus": 1, "steps": K, "warmup": W,
+        "higher_is_better": True, "dtype": "f32-inner/f64-refine",
+        "data": "synthetic (seeded DFG channel meshes h=0.025/0.01/0.005; U_max, nu per instance from seed 1)",
+        "config": {"workload": f"{per} instances on each of h={hs}, U_max~U[0.2,1.5], nu~logU[5e-4,2e-3], "
+                               f"tau={tau}, pressure to 1e-8 rel", "instances": n,
+                   "mesh_sizes_N_P": {str(h): sizes[h] for h in hs}, "setup_s": round(setup_s, 1),
+                   "execution": "one CUDA graph per step whose branches are the 48 instances' steps (nsf_pack); "
+                                "cluster-resident solves"},
+        "sequential_instance_steps_per_s": round(n * K / t_seq, 2),
+        "speedup_vs_sequential": round(t_seq / t_pack, 2),
+        "one_instance_alone_steps_per_s": alone,
+        "status_all_ok": all(s == 0 for s in status),
+        "kernel_launches_total": int(launches),
     }
 
 
@@ -794,7 +902,7 @@ def main():
     ap.add_argument("--cpu-sample-steps", type=int, default=3)
     ap.add_argument("--no-accuracy", dest="accuracy", action="store_false",
                     help="skip the untimed mixed-vs-FP64 field and drag/lift comparison")
-    ap.add_argument("--workload", default="channel", choices=["channel", "poisson", "small", "batch", "adjoint"],
+    ap.add_argument("--workload", default="channel", choices=["channel", "poisson", "small", "batch", "pack", "adjoint"],
                     help="channel: the h=0.005 time step (default); poisson: the standalone 1M-DOF pressure "
                          "solve; small: the plain FP64 h=0.02 channel; batch: 64 instances at h=0.01; "
                          "adjoint: the drag gradient at h=0.01 over 1000 steps")
@@ -817,6 +925,8 @@ def main():
     ap.add_argument("--small-cpu-steps", type=int, default=100)
     ap.add_argument("--batch", type=int, default=64)
     ap.add_argument("--batch-steps", type=int, default=20)
+    ap.add_argument("--pack-per-mesh", type=int, default=16, help="pack workload: instances per mesh")
+    ap.add_argument("--pack-steps", type=int, default=20)
     ap.add_argument("--poisson-reps", type=int, default=2)
     args = ap.parse_args()
 
@@ -854,10 +964,10 @@ def main():
                           "e2e": {"value": v, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}))
         return
 
-    if args.workload in ("poisson", "small", "batch", "adjoint"):
+    if args.workload in ("poisson", "small", "batch", "pack", "adjoint"):
         if rank == 0 and args.impl == "ours":
             fn = {"poisson": bench_poisson, "small": bench_small, "batch": bench_batch,
-                  "adjoint": bench_adjoint}[args.workload]
+                  "pack": bench_pack, "adjoint": bench_adjoint}[args.workload]
             print(json.dumps(fn(args)))
         return
 

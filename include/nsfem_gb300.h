@@ -210,6 +210,21 @@ int nsf_chorin_stats(nsf_chorin s, double *stats);
 long long nsf_kernel_launches(void);
 void nsf_chorin_destroy(nsf_chorin s);
 
+/* ===================================================================== packs of steppers == */
+
+typedef struct nsf_pack_s *nsf_pack;
+
+/* A pack: one CUDA graph whose branches are the time steps of n steppers (on one mesh or on meshes
+   of different resolution), so that one graph launch advances every instance.  No counterpart in
+   the reference (its loop drives one flow).  With n > 1 every stepper must keep its solves inside
+   thread-block clusters (created with NSF_PCG_PATH=auto-cluster): concurrent branches on the
+   whole-GPU cooperative grid could wait on each other's SMs.  The steppers must outlive the pack
+   and must not be stepped through their own handles while a pack launch is in flight. */
+int nsf_pack_create(const nsf_chorin *steppers, int n, nsf_pack *out);
+/* enqueue nSteps launches of the pack graph on stream (NULL: the pack's own stream); asynchronous */
+int nsf_pack_step(nsf_pack p, int nSteps, void *stream);
+void nsf_pack_destroy(nsf_pack p);
+
 /* ========================================================= force functional (drag/lift) == */
 
 typedef struct nsf_forces_s *nsf_forces;

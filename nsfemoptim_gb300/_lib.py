@@ -88,6 +88,9 @@ _SIGS = {
     "nsf_adjoint_run": (C.c_int, [vp, C.c_int, f64p, f64p, f64p, f64p, f64p, vp]),
     "nsf_adjoint_stats": (C.c_int, [vp, f64p]),
     "nsf_adjoint_destroy": (None, [vp]),
+    "nsf_pack_create": (C.c_int, [C.POINTER(vp), C.c_int, C.POINTER(vp)]),
+    "nsf_pack_step": (C.c_int, [vp, C.c_int, vp]),
+    "nsf_pack_destroy": (None, [vp]),
 }
 
 _LIB = None

@@ -425,6 +425,28 @@ class Forces:
             self._h = None
 
 
+class Pack:
+    """Steppers advanced together by one CUDA graph launch per step (each stepper's time step is a
+    branch of the graph).  New: the reference drives one flow.  With more than one stepper, create
+    them with NSF_PCG_PATH=auto-cluster in the environment (solves inside thread-block clusters)."""
+
+    def __init__(self, steppers):
+        self._steppers = list(steppers)  # they must outlive the pack
+        arr = (vp * len(self._steppers))(*[s._h for s in self._steppers])
+        h = vp()
+        check(lib().nsf_pack_create(arr, len(self._steppers), C.byref(h)))
+        self._h = h
+
+    def step(self, n: int = 1, stream=None):
+        """Enqueue n graph launches (asynchronous)."""
+        check(lib().nsf_pack_step(self._h, int(n), vp(stream)))
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            lib().nsf_pack_destroy(self._h)
+            self._h = None
+
+
 class Adjoint:
     """Discrete adjoint of an FP64 stepper's time step for the force functional of `forces`:
     J = sum_n w_drag[n] F_x(u_n, p_n) + w_lift[n] F_y(u_n, p_n).  New: the reference has no adjoint.
@@ -473,5 +495,5 @@ class Adjoint:
 
 __all__ = ["Mesh", "load_gmsh", "ChorinContext", "build_chorin_context", "coloring", "CsrF", "Spmv", "Spmm",
            "spmv", "spmm", "fastconv_apply", "AbstractSolver", "create_solver", "ChorinStepper", "kernel_launches",
-           "Forces", "Adjoint", "NSF_F32", "NSF_F64", "NSF_PREC_F64", "NSF_PREC_MIXED", "NSF_PREC_F64_MIXEDSOLVE",
+           "Forces", "Adjoint", "Pack", "NSF_F32", "NSF_F64", "NSF_PREC_F64", "NSF_PREC_MIXED", "NSF_PREC_F64_MIXEDSOLVE",
            "NsfError"]

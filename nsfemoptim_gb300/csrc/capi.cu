@@ -801,6 +801,14 @@ struct nsf_chorin_s
     }
     double stats[8] = {0};
 
+    // whether a solve of this stepper runs on the whole-GPU cooperative grid
+    bool usesGrid() const
+    {
+        using P = PcgSolver<double, 1>;
+        return velT.path == P::GRID || velF.path == P::GRID || pres.path == P::GRID ||
+               mvelT.inner.path == P::GRID || mvelF.inner.path == P::GRID || mpres.inner.path == P::GRID;
+    }
+
     ~nsf_chorin_s()
     {
         if (exec)
@@ -1502,3 +1510,6 @@ extern "C" int nsf_residual_noalloc(nsf_csr a, int nrhs, const double * x, const
 
 // ============================================================ discrete adjoint (gradients)
 #include "adjoint.cuh"
+
+// ============================================================ packs of steppers (one graph)
+#include "pack.cuh"

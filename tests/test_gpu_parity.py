@@ -302,6 +302,41 @@ def test_chorin_jacobi_mass_matches_oracle(setup, torch_cuda, path, precision, m
     assert s["status"] == 0 and s["tent_rel"] <= 1e-10 and s["final_rel"] <= 1e-10
 
 
+def test_pack_equals_separate_steps(setup, torch_cuda, monkeypatch, mesh_dir):
+    """A pack (one graph, one branch per stepper) of three steppers on two meshes (h = 0.025 and
+    h = 0.04, different viscosities and precisions) reaches bit-identical states to the same
+    steppers stepped one at a time; a pack refuses steppers that solve on the cooperative grid."""
+    import os
+    G, O, mesh, ctx, om, oc = setup
+    from nsfemoptim_gb300 import meshgen
+    p2 = os.path.join(mesh_dir, "channel_h0.04_s0.msh")
+    if not os.path.exists(p2):
+        meshgen.write_gmsh41(p2, meshgen.dfg_channel(0.04, seed=0))
+    mesh2 = G.load_gmsh(p2)
+    ctx2 = G.build_chorin_context(mesh2, 1.2)
+    monkeypatch.setenv("NSF_PCG_PATH", "auto-cluster")
+
+    def make():
+        return [G.ChorinStepper(ctx, 1e-3, 1e-3, precision=G.NSF_PREC_MIXED, vel_method=2, use_graph=True),
+                G.ChorinStepper(ctx, 2e-3, 1e-3, precision=G.NSF_PREC_F64, vel_method=1, use_graph=True),
+                G.ChorinStepper(ctx2, 1e-3, 1e-3, precision=G.NSF_PREC_MIXED, vel_method=2, use_graph=True)]
+
+    packed, single = make(), make()
+    pack = G.Pack(packed)
+    pack.step(4)
+    torch_cuda.cuda.synchronize()
+    for st in single:
+        st.step(4)
+    for a, b in zip(packed, single):
+        ua, pa = a.state()
+        ub, pb = b.state()
+        assert np.array_equal(ua, ub) and np.array_equal(pa, pb)
+    monkeypatch.setenv("NSF_PCG_PATH", "grid")
+    grid = [G.ChorinStepper(ctx, 1e-3, 1e-3, vel_method=1, use_graph=True) for _ in range(2)]
+    with pytest.raises(G.NsfError):
+        G.Pack(grid)
+
+
 def test_concurrent_launch_equals_step(setup, torch_cuda, monkeypatch):
     """Independent steppers (different viscosities) enqueued with launch() on their own streams,
     interleaved step by step, reach bit-identical states to the same steppers advanced with
