@@ -928,6 +928,9 @@ struct nsf_chorin_s
     }
 };
 
+// typical iteration counts of the step's solves (weights for the path autotuner)
+constexpr int kMassIters = 30, kPresIters = 400;
+
 static void buildChorin(nsf_chorin_s & S, const Context & c)
 {
     const int N = c.N, P = c.P;
@@ -998,9 +1001,9 @@ static void buildChorin(nsf_chorin_s & S, const Context & c)
         std::vector<float> k32(knu.begin(), knu.end());
         S.K32.upload(k32);
         S.A32.alloc(knu.size());
-        S.mvelT.setup(&S.M64, &S.M32, 2);
-        S.mvelF.setup(&S.M64, &S.M32, 2);
-        S.mpres.setup(&S.Kpi64, &S.Kpi32, 1);
+        S.mvelT.setup(&S.M64, &S.M32, 2, kMassIters);
+        S.mvelF.setup(&S.M64, &S.M32, 2, kMassIters);
+        S.mpres.setup(&S.Kpi64, &S.Kpi32, 1, kPresIters);
     }
     else
     {
@@ -1014,9 +1017,9 @@ static void buildChorin(nsf_chorin_s & S, const Context & c)
             // FP64 operators, FP32-inner solves on FP32 copies of the two systems
             S.M32.build(Mp, mParts);
             S.Kpi32.build(Kpip, cp.partStart);
-            S.mvelT.setup(&S.M64, &S.M32, 2);
-            S.mvelF.setup(&S.M64, &S.M32, 2);
-            S.mpres.setup(&S.Kpi64, &S.Kpi32, 1);
+            S.mvelT.setup(&S.M64, &S.M32, 2, kMassIters);
+            S.mvelF.setup(&S.M64, &S.M32, 2, kMassIters);
+            S.mpres.setup(&S.Kpi64, &S.Kpi32, 1, kPresIters);
         }
         else
         {
@@ -1027,10 +1030,10 @@ static void buildChorin(nsf_chorin_s & S, const Context & c)
             }
             else
             {
-                S.velT.setup(&S.M64, 2);
-                S.velF.setup(&S.M64, 2);
+                S.velT.setup(&S.M64, 2, true, kMassIters);
+                S.velF.setup(&S.M64, 2, true, kMassIters);
             }
-            S.pres.setup(&S.Kpi64, 1);
+            S.pres.setup(&S.Kpi64, 1, true, kPresIters);
         }
     }
     // Dirichlet rows in the colored numbering

@@ -242,19 +242,140 @@ namespace nsf
             return true;
         }
 
-        void setup(const SweepSystem<T> * s, int channels, bool tryPersistent = true)
+        // ---- autotuning (NSF_PCG_PATH=tune): every path that fits is timed and the fastest kept.
+        // A candidate is a path and its variant (DSMEM: values in shared memory or not; CLUSTER /
+        // GRID: row structure in shared memory or not).
+        bool applyCandidate(const SweepSystem<T> * s, int cpath, int variant)
+        {
+            path = MULTI;
+            clusterSize = 0;
+            clusterShared = false;
+            clusterSmem = 0;
+            dsVals = -1;
+            bool ok = true;
+            if (cpath == DSMEM)
+                ok = setupDsmem(s, variant != 0) && dsVals == variant;
+            else if (cpath == CLUSTER)
+                ok = setupCluster(s, variant != 0) && clusterShared == (variant != 0);
+            else if (cpath == GRID)
+                ok = setupGrid(s, variant != 0) && clusterShared == (variant != 0);
+            if (ok)
+                path = cpath;
+            else
+            {
+                clusterSize = 0;
+                clusterShared = false;
+                clusterSmem = 0;
+                dsVals = -1;
+            }
+            return ok;
+        }
+
+        // Seconds of one solve of exactly `iters` iterations (tolerance 0) on b, captured as a
+        // graph (as the steppers run it) and replayed; the best of three replays after two warm-ups.
+        double trialSolve(int iters, const T * b, T * x, cudaStream_t st, cudaStream_t body)
+        {
+            const long long before = launchCounter().load();
+            cudaGraph_t g = nullptr;
+            cudaGraphExec_t e = nullptr;
+            NSF_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+            NSF_CUDA(cudaMemsetAsync(x, 0, sizeof(T) * NCH * (size_t)sys->n, st));
+            enqueue(st, body, b, x, iters, 0.0, false, 1);
+            NSF_CUDA(cudaStreamEndCapture(st, &g));
+            launchCounter().fetch_sub(launchCounter().load() - before); // trial kernels are not work
+            NSF_CUDA(cudaGraphInstantiate(&e, g, 0));
+            cudaEvent_t e0, e1;
+            NSF_CUDA(cudaEventCreate(&e0));
+            NSF_CUDA(cudaEventCreate(&e1));
+            double best = 1e30;
+            for (int rep = 0; rep < 5; rep++)
+            {
+                NSF_CUDA(cudaEventRecord(e0, st));
+                NSF_CUDA(cudaGraphLaunch(e, st));
+                NSF_CUDA(cudaEventRecord(e1, st));
+                NSF_CUDA(cudaStreamSynchronize(st));
+                float ms = 0;
+                NSF_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+                if (rep >= 2)
+                    best = std::min(best, 1e-3 * ms);
+            }
+            cudaEventDestroy(e0);
+            cudaEventDestroy(e1);
+            cudaGraphExecDestroy(e);
+            cudaGraphDestroy(g);
+            return best;
+        }
+
+        // Time every candidate on trial solves of 8 and 24 iterations; keep the one with the least
+        // fixed + expectIters x per-iteration time.  The choice can differ between runs when two
+        // paths are within timing noise (the paths differ only in summation order).
+        void tune(const SweepSystem<T> * s, int expectIters)
+        {
+            const int n = s->n;
+            std::vector<T> hb((size_t)NCH * n);
+            for (size_t i = 0; i < hb.size(); i++)
+                hb[i] = (T)(std::sin(0.37 * (double)i + 0.11) + 0.5);
+            DevBuf<T> b, x;
+            b.upload(hb);
+            x.alloc(hb.size());
+            cudaStream_t st = nullptr, body = nullptr;
+            NSF_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+            NSF_CUDA(cudaStreamCreateWithFlags(&body, cudaStreamNonBlocking));
+            const int cands[7][2] = {{DSMEM, 1}, {DSMEM, 0}, {CLUSTER, 1}, {CLUSTER, 0},
+                                     {GRID, 1},  {GRID, 0},  {MULTI, 0}};
+            int bestPath = MULTI, bestVar = 0;
+            double bestCost = 1e30;
+            for (const auto & c : cands)
+            {
+                if (!applyCandidate(s, c[0], c[1]))
+                    continue;
+                const double t8 = trialSolve(8, b.get(), x.get(), st, body);
+                const double t24 = trialSolve(24, b.get(), x.get(), st, body);
+                const double per = std::max(0.0, (t24 - t8) / 16.0), fixed = std::max(0.0, t8 - 8.0 * per);
+                const double cost = fixed + expectIters * per;
+                if (envFlag("NSF_VERBOSE"))
+                    std::fprintf(stderr, "[nsf] tune n=%d path=%d variant=%d: %.2f us/iteration + %.1f us\n", n,
+                                 c[0], c[1], 1e6 * per, 1e6 * fixed);
+                if (cost < bestCost)
+                {
+                    bestCost = cost;
+                    bestPath = c[0];
+                    bestVar = c[1];
+                }
+            }
+            cudaStreamDestroy(st);
+            cudaStreamDestroy(body);
+            applyCandidate(s, bestPath, bestVar);
+        }
+
+        // expectIters: a typical iteration count of this system's solves (weighs the autotuner's
+        // per-iteration against its fixed cost)
+        void setup(const SweepSystem<T> * s, int channels, bool tryPersistent = true, int expectIters = 100)
         {
             sys = s;
             numCh = channels;
             const int n = s->n;
             psDev.upload(s->ps);
+            r.alloc((size_t)NCH * n);
+            z.alloc((size_t)NCH * n);
+            p.alloc((size_t)2 * NCH * n);
+            q.alloc((size_t)NCH * n);
+            scratch.alloc((size_t)2 * MAXCH * cappedBlocks(1ll << 40));
+            st.alloc(1);
+            P.n = n;
+            P.nColors = s->nColors;
+            P.scratch = scratch.get();
+            P.st = st.get();
+            P.cond = 0;
             path = MULTI;
             clusterSize = 0;
             clusterShared = false;
             clusterSmem = 0;
             dsVals = -1;
             const std::string want = envStr("NSF_PCG_PATH", "auto");
-            if (tryPersistent && want != "multikernel")
+            if (tryPersistent && want == "tune")
+                tune(s, expectIters);
+            else if (tryPersistent && want != "multikernel")
             {
                 // "auto-cluster": never the whole-GPU grid, so that independent solvers (batched
                 // instances on separate streams) can run side by side
@@ -278,17 +399,6 @@ namespace nsf
             if (envFlag("NSF_VERBOSE"))
                 std::fprintf(stderr, "[nsf] PCG n=%d nnz=%d colors=%d path=%d ctas=%d shared=%d dsvals=%d smem=%zu\n",
                              n, s->nnzFull, s->nColors, path, clusterSize, (int)clusterShared, dsVals, clusterSmem);
-            r.alloc((size_t)NCH * n);
-            z.alloc((size_t)NCH * n);
-            p.alloc((size_t)2 * NCH * n);
-            q.alloc((size_t)NCH * n);
-            scratch.alloc((size_t)2 * MAXCH * cappedBlocks(1ll << 40));
-            st.alloc(1);
-            P.n = n;
-            P.nColors = s->nColors;
-            P.scratch = scratch.get();
-            P.st = st.get();
-            P.cond = 0;
         }
 
         void sgs(cudaStream_t s, PcgPtrs PP, int init, T * x, bool tickLast)
@@ -462,11 +572,12 @@ namespace nsf
         DevBuf<SolverState> st;
         PinnedBuf<int> flag{1};
 
-        void setup(const SweepSystem<double> * s64, const SweepSystem<float> * s32, int channels)
+        void setup(const SweepSystem<double> * s64, const SweepSystem<float> * s32, int channels,
+                   int expectIters = 100)
         {
             sys64 = s64;
             numCh = channels;
-            inner.setup(s32, channels);
+            inner.setup(s32, channels, true, expectIters);
             b32.alloc((size_t)NCH * s64->n);
             d32.alloc((size_t)NCH * s64->n);
             scratch.alloc((size_t)2 * MAXCH * cappedBlocks(1ll << 40));

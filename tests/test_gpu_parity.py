@@ -163,6 +163,29 @@ def test_pcg_paths_match_oracle(setup, torch_cuda, path, monkeypatch, capfd):
         assert abs(s.getLastIterations() - it) <= 1
 
 
+def test_pcg_autotuned_path_matches_oracle(setup, torch_cuda, monkeypatch, capfd):
+    """NSF_PCG_PATH=tune times every path that fits on trial solves and keeps the fastest; the
+    solve on the chosen path matches the oracle as every path does, and the trial solves do not
+    count as library kernel launches."""
+    G, O, mesh, ctx, om, oc = setup
+    t = torch_cuda
+    _force_path(monkeypatch, "tune")
+    capfd.readouterr()
+    a = ctx.matrix("Kpi")
+    before = G.kernel_launches()
+    s = G.create_solver("pcg", 1, a, 3000, 1e-10, 1)
+    assert G.kernel_launches() == before
+    err = capfd.readouterr().err
+    assert "[nsf] tune" in err and "[nsf] PCG" in err, err
+    b = np.random.default_rng(12).standard_normal(a.rows)
+    s.getRhs().copy_(t.tensor(b))
+    s.getSol().zero_()
+    assert s.solve() == 0
+    xo, st, it, rr = O.pcg(oc.Kpi, O.coloring(oc.Kpi), b, np.zeros(a.rows), 3000, 1e-10)
+    assert _rel(s.getSol().cpu().numpy(), xo) <= 1e-8
+    assert abs(s.getLastIterations() - it) <= 1
+
+
 def test_pcg_mass_two_channels_warm_start(setup, torch_cuda):
     G, O, mesh, ctx, om, oc = setup
     t = torch_cuda
