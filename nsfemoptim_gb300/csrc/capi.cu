@@ -774,6 +774,10 @@ struct nsf_chorin_s
     DevBuf<float> K32, A32;
     // state and work vectors
     DevBuf<double> u, pInt, rhs, acc, rhsP;
+    // pressure initial guess extrapolated from the last two solutions (NSF_EXTRAPOLATE=1 at creation)
+    bool extrapolate = false;
+    DevBuf<double> pPrev;
+    DevBuf<int> pHist;
     DevBuf<unsigned char> isDir;
     DevBuf<double> dirVal;
     // solvers: separate objects for the tentative and the final mass solve keep both stats
@@ -860,6 +864,11 @@ struct nsf_chorin_s
                    dirVal.get());
         // 3. rhsP = -(1/tau) D u ; Kpi pInt = rhsP (warm start)
         const double invTau = -1.0 / cfg.tau;
+        if (extrapolate)
+        {
+            NSF_LAUNCH(kExtrapolate, blocksFor(nIntP), s, nIntP, pInt.get(), pPrev.get(), (const int *)pHist.get());
+            NSF_LAUNCH(kHistBump, 1, s, pHist.get());
+        }
         if (mixed)
         {
             sellSpmv<float>(D32.sell, u.get(), rhsP.get(), invTau, 0.0, s);
@@ -1054,6 +1063,12 @@ static void buildChorin(nsf_chorin_s & S, const Context & c)
             u0[r] = dval[r];
     S.u.upload(u0);
     S.pInt.alloc(S.nIntP);
+    S.extrapolate = envFlag("NSF_EXTRAPOLATE") != 0;
+    if (S.extrapolate)
+    {
+        S.pPrev.alloc(S.nIntP);
+        S.pHist.alloc(1);
+    }
     S.rhs.alloc(2 * (size_t)N);
     S.acc.alloc(2 * (size_t)N);
     S.rhsP.alloc(S.nIntP);
@@ -1207,6 +1222,8 @@ extern "C" int nsf_chorin_set_state(nsf_chorin S, const double * uIn, const doub
                 h[2 * N + r] = pIn[S->intP[S->permP[r]]];
             NSF_CUDA(cudaMemcpyAsync(S->pInt.get(), h + 2 * N, sizeof(double) * S->nIntP, cudaMemcpyHostToDevice, s));
         }
+        if (S->extrapolate) // a new history starts from the state just set
+            NSF_CUDA(cudaMemsetAsync(S->pHist.get(), 0, sizeof(int), s));
         NSF_CUDA(cudaStreamSynchronize(s));
     });
 }

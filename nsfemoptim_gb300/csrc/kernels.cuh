@@ -429,6 +429,29 @@ namespace nsf
         }
     }
 
+    // Initial guess of the pressure solve from the last two solutions: before step k the solve
+    // starts from 2 p_{k-1} - p_{k-2} once two solved pressures exist (hist >= 2), else from p_{k-1};
+    // prev keeps p_{k-1} for the next step.  kHistBump advances the count afterwards (separate
+    // launch: every thread here reads the same count).
+    __global__ void __launch_bounds__(TPB) kExtrapolate(int n, double * __restrict__ p, double * __restrict__ prev,
+                                                         const int * __restrict__ hist)
+    {
+        const bool two = *hist >= 2;
+        for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        {
+            const double cur = p[i];
+            if (two)
+                p[i] = 2.0 * cur - prev[i];
+            prev[i] = cur;
+        }
+    }
+
+    __global__ void kHistBump(int * hist)
+    {
+        if (threadIdx.x == 0 && blockIdx.x == 0 && *hist < 2)
+            *hist += 1;
+    }
+
     // x64 += d (mixed-precision refinement update)
     template <typename TD>
     __global__ void __launch_bounds__(TPB) kAddTo(int n, double * __restrict__ x, const TD * __restrict__ d,
