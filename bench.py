@@ -101,7 +101,7 @@ class Clocks:
         return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def run_cpu_reference(mesh_path: str, steps: int, warmup: int, vel_method: int = 1):
+def run_cpu_reference(mesh_path: str, steps: int, warmup: int, vel_method: int = 1, pres_guess: int = 0):
     """Time the oracle's FP64 Chorin step (the CPU restatement of the reference path) on every host
     thread (its OpenMP build; the single-thread build if that cannot be compiled).  The thread
     count is left in CPU_THREADS."""
@@ -111,7 +111,7 @@ def run_cpu_reference(mesh_path: str, steps: int, warmup: int, vel_method: int =
     m = oracle.Mesh(mesh_path)
     ctx = oracle.Context(m, PEAK, True)
     ch = oracle.Chorin(ctx, NU, TAU, vel_method=vel_method, vel_max_iters=500, vel_tol=VEL_TOL, pres_max_iters=5000,
-                       pres_tol=PRES_TOL, mt=True)
+                       pres_tol=PRES_TOL, mt=True, pres_guess=pres_guess)
     CPU_THREADS = ch.threads
     for _ in range(warmup):
         ch.step()
@@ -725,7 +725,7 @@ def bench_ours(args, rank, world, local_rank):
         def stepper(precision, graph=True):
             return G.ChorinStepper(ctx, NU, TAU, precision=precision, vel_method=args.vel_method, vel_max_iters=500,
                                    vel_tol=VEL_TOL, pres_max_iters=5000, pres_tol=PRES_TOL, check_interval=8,
-                                   use_graph=graph, max_outer=4, inner_tol=1e-5)
+                                   use_graph=graph, max_outer=4, inner_tol=1e-5, pressure_guess=args.pressure_guess)
 
         stream = torch.cuda.Stream()
         sp = stream.cuda_stream
@@ -862,7 +862,8 @@ def bench_ours(args, rank, world, local_rank):
                        "internal_pressure": nip, "nnz_I": nnzI, "parallelism": f"replicas x{world}",
                        "l2": "working set > L2 (FastConvection matrix %.0f MB FP32)" % (nnzI * 8 / 1e6),
                        "graph": True, "setup_s": round(setup_s, 2),
-                       "mass_solve": {1: "PCG, multicolor SGS", 2: "PCG, Jacobi"}[args.vel_method]},
+                       "mass_solve": {1: "PCG, multicolor SGS", 2: "PCG, Jacobi"}[args.vel_method],
+                       "pressure_guess": {0: "previous solution", 1: "2 p(n-1) - p(n-2)"}[args.pressure_guess]},
             "e2e": {"value": round(world * e2e_steps / t_e2e, 3), "unit": "steps/s",
                     "h2d_bytes_per_step": (2 * N + P) * 8, "d2h_bytes_per_step": (2 * N + P) * 8},
             "gpu_launches": int(launches),
@@ -908,6 +909,8 @@ def main():
                          "adjoint: the drag gradient at h=0.01 over 1000 steps")
     ap.add_argument("--vel-method", type=int, default=2, choices=[1, 2],
                     help="channel workload: mass-solve preconditioner, 1 multicolor SGS, 2 Jacobi")
+    ap.add_argument("--pressure-guess", type=int, default=1, choices=[0, 1],
+                    help="channel workload: pressure initial guess, 0 previous solution, 1 extrapolated")
     ap.add_argument("--adjoint-steps", type=int, default=1000)
     ap.add_argument("--adjoint-checkpoint", type=int, default=50)
     ap.add_argument("--adjoint-precision", default="mixedsolve", choices=["f64", "mixedsolve"])
@@ -1005,7 +1008,8 @@ def main():
             tmp = tempfile.mkdtemp()
             try:
                 path = make_mesh(tmp, H, 0)
-                sps, dt, _, (uo, po, fo) = run_cpu_reference(path, args.cpu_sample_steps, 1, args.vel_method)
+                sps, dt, _, (uo, po, fo) = run_cpu_reference(path, args.cpu_sample_steps, 1, args.vel_method,
+                                                             args.pressure_guess)
                 line["cpu_baseline"] = {"value": round(sps, 4), "unit": "steps/s", "cores": CPU_THREADS, "kind": "port",
                                         "sample": f"{args.cpu_sample_steps} time steps (after 1 warm-up) of the same "
                                                   f"workload, FP64 C oracle on {CPU_THREADS} host threads (OpenMP)"}

@@ -184,6 +184,10 @@ typedef struct
                              conditional while nodes (no host synchronisation); 0: eager */
     int maxOuter;         /* mixed precision: FP64 refinement passes per solve */
     double innerTol;      /* mixed precision: relative tolerance of each FP32 inner solve */
+    int pressureGuess;    /* initial guess of the pressure solve: 0 the previous solution (as the
+                             reference's solver keeps it), 1 the linear extrapolation
+                             2 p(n-1) - p(n-2) from the last two solutions (no reference
+                             counterpart; fewer iterations, the same tolerance) */
 } nsf_chorin_config;
 
 typedef struct nsf_chorin_s *nsf_chorin;

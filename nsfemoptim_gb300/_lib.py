@@ -34,7 +34,7 @@ class ChorinConfig(C.Structure):
     _fields_ = [("nu", C.c_double), ("tau", C.c_double), ("precision", C.c_int), ("velMethod", C.c_int),
                 ("velMaxIters", C.c_int), ("velTol", C.c_double), ("presMaxIters", C.c_int),
                 ("presTol", C.c_double), ("checkInterval", C.c_int), ("useGraph", C.c_int),
-                ("maxOuter", C.c_int), ("innerTol", C.c_double)]
+                ("maxOuter", C.c_int), ("innerTol", C.c_double), ("pressureGuess", C.c_int)]
 
 
 class AdjointConfig(C.Structure):

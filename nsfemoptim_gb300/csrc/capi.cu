@@ -774,7 +774,7 @@ struct nsf_chorin_s
     DevBuf<float> K32, A32;
     // state and work vectors
     DevBuf<double> u, pInt, rhs, acc, rhsP;
-    // pressure initial guess extrapolated from the last two solutions (NSF_EXTRAPOLATE=1 at creation)
+    // pressure initial guess extrapolated from the last two solutions (cfg.pressureGuess == 1)
     bool extrapolate = false;
     DevBuf<double> pPrev;
     DevBuf<int> pHist;
@@ -1063,7 +1063,7 @@ static void buildChorin(nsf_chorin_s & S, const Context & c)
             u0[r] = dval[r];
     S.u.upload(u0);
     S.pInt.alloc(S.nIntP);
-    S.extrapolate = envFlag("NSF_EXTRAPOLATE") != 0;
+    S.extrapolate = S.cfg.pressureGuess == 1;
     if (S.extrapolate)
     {
         S.pPrev.alloc(S.nIntP);
@@ -1088,6 +1088,7 @@ extern "C" int nsf_chorin_create(nsf_context ctx, const nsf_chorin_config * cfg,
                 "velMethod must be 0 (gs), 1 (pcg, SGS preconditioner) or 2 (pcg, Jacobi preconditioner)");
         require(!(cfg->precision == NSF_PREC_MIXED && cfg->velMethod == 0), "mixed precision uses velMethod 1 (pcg)");
         require(cfg->velMaxIters >= 1 && cfg->presMaxIters >= 1, "iteration caps must be >= 1");
+        require(cfg->pressureGuess == 0 || cfg->pressureGuess == 1, "pressureGuess must be 0 or 1");
         auto S = std::make_unique<nsf_chorin_s>();
         S->cfg = *cfg;
         if (S->cfg.checkInterval < 1)

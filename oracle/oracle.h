@@ -126,6 +126,8 @@ typedef struct
     double velTol;       /* RMS target for GS, relative tolerance for PCG */
     int presMaxIters;
     double presTol;      /* relative residual */
+    int presGuess;       /* 0: start from the previous pressure; 1: from 2 p(n-1) - p(n-2) once two
+                            solved pressures exist */
 } orc_chorin_cfg;
 
 typedef struct orc_chorin_s orc_chorin;

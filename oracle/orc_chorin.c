@@ -29,6 +29,8 @@ struct orc_chorin_s
     orc_sys *sysM, *sysP; /* M and Kp_int prepared once for the PCG solves */
     double *u, *p, *pInt, *Avals, *rhs, *acc, *div, *rhsP, *g;
     double *dirVx; /* x values imposed on the Dirichlet nodes (ctx->dirVx unless set) */
+    double *pPrev; /* presGuess 1: the pressure solution before the last one */
+    int pHist;     /* solved pressures seen since create / set (capped at 2) */
 };
 
 orc_chorin *orc_chorin_create(const orc_context *ctx, const orc_chorin_cfg *cfg)
@@ -50,6 +52,7 @@ orc_chorin *orc_chorin_create(const orc_context *ctx, const orc_chorin_cfg *cfg)
     s->div = (double *)calloc(P, sizeof(double));
     s->rhsP = (double *)calloc(ctx->nIntP + 1, sizeof(double));
     s->g = (double *)calloc(2 * N, sizeof(double));
+    s->pPrev = (double *)calloc(ctx->nIntP + 1, sizeof(double));
     s->dirVx = (double *)calloc(ctx->nDir + 1, sizeof(double));
     memcpy(s->dirVx, ctx->dirVx, sizeof(double) * ctx->nDir);
     for (int i = 0; i < ctx->nDir; i++)
@@ -78,6 +81,7 @@ void orc_chorin_free(orc_chorin *s)
     free(s->rhsP);
     free(s->g);
     free(s->dirVx);
+    free(s->pPrev);
     free(s);
 }
 
@@ -111,6 +115,7 @@ void orc_chorin_set(orc_chorin *s, const double *u, const double *p)
         for (int i = 0; i < ctx->nIntP; i++)
             s->pInt[i] = p[ctx->intP[i]];
     }
+    s->pHist = 0; /* a new pressure history starts from the state just set */
 }
 
 static void impose(orc_chorin *s)
@@ -175,6 +180,19 @@ int orc_chorin_step(orc_chorin *s, double *stats)
         s->div[i] *= invTau;
     for (int i = 0; i < ctx->nIntP; i++)
         s->rhsP[i] = s->div[ctx->intP[i]];
+    if (s->cfg.presGuess == 1)
+    {
+        /* start from 2 p(n-1) - p(n-2) once two solved pressures exist */
+        for (int i = 0; i < ctx->nIntP; i++)
+        {
+            const double cur = s->pInt[i];
+            if (s->pHist >= 2)
+                s->pInt[i] = 2.0 * cur - s->pPrev[i];
+            s->pPrev[i] = cur;
+        }
+        if (s->pHist < 2)
+            s->pHist++;
+    }
     int itP = 0;
     int st = orc_sys_pcg(s->sysP, 1, s->rhsP, s->pInt, s->cfg.presMaxIters, s->cfg.presTol, &itP, &resP);
     memset(s->p, 0, sizeof(double) * P);

@@ -325,6 +325,33 @@ def test_chorin_jacobi_mass_matches_oracle(setup, torch_cuda, path, precision, m
     assert s["status"] == 0 and s["tent_rel"] <= 1e-10 and s["final_rel"] <= 1e-10
 
 
+@pytest.mark.parametrize("precision", ["f64", "mixed"])
+def test_chorin_extrapolated_pressure_guess_matches_oracle(setup, torch_cuda, precision):
+    """pressure_guess 1 (the pressure solve starts from 2 p(n-1) - p(n-2)): the FP64 stepper follows
+    the oracle with the same option (1e-7 after 6 steps), the mixed one within the mixed bounds;
+    set_state restarts the history on both sides."""
+    G, O, mesh, ctx, om, oc = setup
+    prec = G.NSF_PREC_F64 if precision == "f64" else G.NSF_PREC_MIXED
+    st = G.ChorinStepper(ctx, 1e-3, 1e-3, precision=prec, vel_method=1, vel_max_iters=300, vel_tol=1e-10,
+                         pres_max_iters=3000, pres_tol=1e-10, use_graph=True, pressure_guess=1)
+    ch = O.Chorin(oc, 1e-3, 1e-3, vel_method=1, vel_max_iters=300, vel_tol=1e-10, pres_max_iters=3000, pres_tol=1e-10,
+                  pres_guess=1)
+    st.step(3)
+    for _ in range(3):
+        ch.step()
+    u, p = ch.state()
+    st.set_state(u, p)
+    ch.set_state(u, p)
+    st.step(3)
+    for _ in range(3):
+        ch.step()
+    ug, pg = st.state()
+    uo, po = ch.state()
+    tu, tp = (1e-7, 1e-7) if precision == "f64" else (1e-5, 2e-4)
+    assert _rel(ug, uo) <= tu and _rel(pg, po) <= tp
+    assert st.stats()["status"] == 0
+
+
 def test_pack_equals_separate_steps(setup, torch_cuda, monkeypatch, mesh_dir):
     """A pack (one graph, one branch per stepper) of three steppers on two meshes (h = 0.025 and
     h = 0.04, different viscosities and precisions) reaches bit-identical states to the same
