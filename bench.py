@@ -762,9 +762,10 @@ def bench_ours(args, rank, world, local_rank):
         st_f64 = f64.stats()
         u_m, p_m = mixed.state()
 
-        # ---- e2e through the C ABI with host buffers: H2D state, step, D2H state every step
-        u_h = np.zeros(2 * N)
-        p_h = np.zeros(P)
+        # ---- e2e through the C ABI with host buffers: H2D state, step, D2H state every step, from
+        # and to pinned host memory
+        u_h = torch.zeros(2 * N, dtype=torch.float64, pin_memory=True).numpy()
+        p_h = torch.zeros(P, dtype=torch.float64, pin_memory=True).numpy()
         mixed.get_state_into(u_h, p_h)
         e2e_steps = max(3, args.steps // 4)
         torch.cuda.synchronize()

@@ -778,6 +778,9 @@ struct nsf_chorin_s
     bool extrapolate = false;
     DevBuf<double> pPrev;
     DevBuf<int> pHist;
+    // state copies: device staging (original numbering) and the renumbering maps
+    DevBuf<double> stateStage;
+    DevBuf<int> permVDev, pIdxDev;
     DevBuf<unsigned char> isDir;
     DevBuf<double> dirVal;
     // solvers: separate objects for the tentative and the final mass solve keep both stats
@@ -1175,28 +1178,43 @@ static void enqueueSteps(nsf_chorin S, int nSteps, cudaStream_t s)
     }
 }
 
+// Device-side renumbering for the state copies: the host arrays (original numbering) are copied
+// as they are into a device buffer and permuted there by a kernel, instead of permuting element by
+// element on the host (scattered host accesses over MBs).
+static void stateMaps(nsf_chorin S)
+{
+    if (S->permVDev.size() == (size_t)S->N && S->pIdxDev.size() == (size_t)S->nIntP)
+        return;
+    S->permVDev.upload(S->permV);
+    std::vector<int> idx(S->nIntP);
+    for (int r = 0; r < S->nIntP; r++)
+        idx[r] = S->intP[S->permP[r]];
+    S->pIdxDev.upload(idx);
+    S->stateStage.alloc(2 * (size_t)S->N + S->P);
+}
+
 extern "C" int nsf_chorin_get_state(nsf_chorin S, double * uOut, double * pOut, void * stream)
 {
     return guarded([&] {
         require(S, "null stepper");
         cudaStream_t s = stream ? asStream(stream) : S->stream;
-        double * h = S->staging(2 * (size_t)S->N + S->nIntP);
-        NSF_CUDA(cudaMemcpyAsync(h, S->u.get(), sizeof(double) * 2 * S->N, cudaMemcpyDeviceToHost, s));
-        NSF_CUDA(cudaMemcpyAsync(h + 2 * S->N, S->pInt.get(), sizeof(double) * S->nIntP, cudaMemcpyDeviceToHost, s));
-        NSF_CUDA(cudaStreamSynchronize(s));
+        stateMaps(S);
         const int N = S->N;
+        double * su = S->stateStage.get(), * sp = su + 2 * (size_t)N;
         if (uOut)
-            for (int r = 0; r < N; r++)
-            {
-                uOut[S->permV[r]] = h[r];
-                uOut[S->permV[r] + N] = h[r + N];
-            }
+        {
+            NSF_LAUNCH((kScatterPerm<double>), blocksFor(N), s, N, 2, S->permVDev.get(), (const double *)S->u.get(),
+                       su);
+            NSF_CUDA(cudaMemcpyAsync(uOut, su, sizeof(double) * 2 * N, cudaMemcpyDeviceToHost, s));
+        }
         if (pOut)
         {
-            std::fill(pOut, pOut + S->P, 0.0);
-            for (int r = 0; r < S->nIntP; r++)
-                pOut[S->intP[S->permP[r]]] = h[2 * N + r];
+            NSF_CUDA(cudaMemsetAsync(sp, 0, sizeof(double) * S->P, s)); // Dirichlet pressure: 0
+            NSF_LAUNCH((kScatterPerm<double>), blocksFor(S->nIntP), s, S->nIntP, 1, S->pIdxDev.get(),
+                       (const double *)S->pInt.get(), sp);
+            NSF_CUDA(cudaMemcpyAsync(pOut, sp, sizeof(double) * S->P, cudaMemcpyDeviceToHost, s));
         }
+        NSF_CUDA(cudaStreamSynchronize(s));
     });
 }
 
@@ -1205,23 +1223,20 @@ extern "C" int nsf_chorin_set_state(nsf_chorin S, const double * uIn, const doub
     return guarded([&] {
         require(S, "null stepper");
         cudaStream_t s = stream ? asStream(stream) : S->stream;
-        double * h = S->staging(2 * (size_t)S->N + S->nIntP);
+        stateMaps(S);
         const int N = S->N;
-        NSF_CUDA(cudaStreamSynchronize(s)); // the staging buffer may still feed an earlier copy
+        double * su = S->stateStage.get(), * sp = su + 2 * (size_t)N;
         if (uIn)
         {
-            for (int r = 0; r < N; r++)
-            {
-                h[r] = uIn[S->permV[r]];
-                h[r + N] = uIn[S->permV[r] + N];
-            }
-            NSF_CUDA(cudaMemcpyAsync(S->u.get(), h, sizeof(double) * 2 * N, cudaMemcpyHostToDevice, s));
+            NSF_CUDA(cudaMemcpyAsync(su, uIn, sizeof(double) * 2 * N, cudaMemcpyHostToDevice, s));
+            NSF_LAUNCH((kGatherPerm<double>), blocksFor(N), s, N, 2, S->permVDev.get(), (const double *)su,
+                       S->u.get());
         }
         if (pIn)
         {
-            for (int r = 0; r < S->nIntP; r++)
-                h[2 * N + r] = pIn[S->intP[S->permP[r]]];
-            NSF_CUDA(cudaMemcpyAsync(S->pInt.get(), h + 2 * N, sizeof(double) * S->nIntP, cudaMemcpyHostToDevice, s));
+            NSF_CUDA(cudaMemcpyAsync(sp, pIn, sizeof(double) * S->P, cudaMemcpyHostToDevice, s));
+            NSF_LAUNCH((kGatherPerm<double>), blocksFor(S->nIntP), s, S->nIntP, 1, S->pIdxDev.get(),
+                       (const double *)sp, S->pInt.get());
         }
         if (S->extrapolate) // a new history starts from the state just set
             NSF_CUDA(cudaMemsetAsync(S->pHist.get(), 0, sizeof(int), s));
