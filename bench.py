@@ -596,6 +596,75 @@ def bench_pack(args):
     }
 
 
+def bench_long(args):
+    """Config 2 over a long horizon: the h = 0.005 channel of the default workload (U_max = 1.5,
+    nu = 1e-3, tau = 1e-4, pressure to 1e-8, Jacobi mass solves, extrapolated pressure guess) from
+    rest for --long-steps steps with the mixed stepper and the FP64 stepper side by side: the
+    relative L2 difference of u and p every 1000 steps, and the drag / lift time series (every step,
+    written on the device) compared over the whole run.  Both steppers are timed."""
+    import numpy as np
+    import torch
+
+    import nsfemoptim_gb300 as G
+
+    n, chunk = args.long_steps, 1000
+    tmp = tempfile.mkdtemp()
+    try:
+        mesh = G.load_gmsh(make_mesh(tmp, H, 0))
+        ctx = G.build_chorin_context(mesh, PEAK)
+
+        def stepper(prec):
+            return G.ChorinStepper(ctx, NU, TAU, precision=prec, vel_method=2, vel_max_iters=500, vel_tol=VEL_TOL,
+                                   pres_max_iters=5000, pres_tol=PRES_TOL, check_interval=8, use_graph=True,
+                                   max_outer=4, inner_tol=1e-5, pressure_guess=1)
+
+        steppers = {"mixed": stepper(G.NSF_PREC_MIXED), "fp64": stepper(G.NSF_PREC_F64)}
+        forces = {k: G.Forces(mesh, s) for k, s in steppers.items()}
+        series = {k: torch.zeros(n, 2, dtype=torch.float64, device="cuda") for k in steppers}
+        stream = torch.cuda.Stream()
+        sp = stream.cuda_stream
+        secs = {k: 0.0 for k in steppers}
+        field = []
+        done = 0
+        while done < n:
+            m = min(chunk, n - done)
+            for k, st in steppers.items():
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                for i in range(m):
+                    st.launch(1, sp)
+                    forces[k].into(series[k][done + i], sp)
+                e1.record(stream)
+                torch.cuda.synchronize()
+                secs[k] += e0.elapsed_time(e1) / 1e3
+            done += m
+            (um, pm), (uf, pf) = steppers["mixed"].state(), steppers["fp64"].state()
+            field.append({"step": done, "u_rel_l2": float(np.linalg.norm(um - uf) / np.linalg.norm(uf)),
+                          "p_rel_l2": float(np.linalg.norm(pm - pf) / np.linalg.norm(pf))})
+        sm, sf = series["mixed"].cpu().numpy(), series["fp64"].cpu().numpy()
+        for st in steppers.values():  # one synchronous step each: solver status at the end
+            st.step(1, sp)
+        ok = all(int(st.stats()["status"]) == 0 for st in steppers.values())
+    finally:
+        shutil.rmtree(tmp, ignore_errors=True)
+    fmax = np.abs(sf[:, 0]).max()
+    return {
+        "metric": "config 2 long run: mixed vs FP64 steppers side by side, field and drag/lift differences",
+        "value": round(n / secs["mixed"], 2), "unit": "steps/s", "n_gpus": 1, "steps": n, "higher_is_better": True,
+        "dtype": "f32-inner/f64-refine",
+        "data": "synthetic (seeded DFG channel mesh, h=0.005)",
+        "config": {"workload": f"DFG channel h={H}, Umax=1.5, nu={NU}, tau={TAU}, {n} steps from rest, pressure "
+                               f"to {PRES_TOL} rel", "N": ctx.N, "P": ctx.P},
+        "fp64_steps_per_s": round(n / secs["fp64"], 2),
+        "field_rel_l2_mixed_vs_fp64": field,
+        "drag_max_rel_err": float(np.abs(sm[:, 0] - sf[:, 0]).max() / fmax),
+        "lift_max_err_rel_to_max_drag": float(np.abs(sm[:, 1] - sf[:, 1]).max() / fmax),
+        "drag_fp64_last": float(sf[-1, 0]), "lift_fp64_last": float(sf[-1, 1]),
+        "c_drag_fp64_last": float(sf[-1, 0] * 2.0 / ((PEAK / 6.0) ** 2 * 0.1)),  # U_mean = PEAK / 6, D = 0.1
+        "status_all_ok": ok,
+    }
+
+
 POISSON_NODES = 1024  # nodes per side of the jittered unit square (1,048,576 nodes)
 
 
@@ -904,7 +973,7 @@ def main():
     ap.add_argument("--cpu-sample-steps", type=int, default=3)
     ap.add_argument("--no-accuracy", dest="accuracy", action="store_false",
                     help="skip the untimed mixed-vs-FP64 field and drag/lift comparison")
-    ap.add_argument("--workload", default="channel", choices=["channel", "poisson", "small", "batch", "pack", "adjoint"],
+    ap.add_argument("--workload", default="channel", choices=["channel", "poisson", "small", "batch", "pack", "adjoint", "long"],
                     help="channel: the h=0.005 time step (default); poisson: the standalone 1M-DOF pressure "
                          "solve; small: the plain FP64 h=0.02 channel; batch: 64 instances at h=0.01; "
                          "adjoint: the drag gradient at h=0.01 over 1000 steps")
@@ -931,6 +1000,7 @@ def main():
     ap.add_argument("--batch-steps", type=int, default=20)
     ap.add_argument("--pack-per-mesh", type=int, default=16, help="pack workload: instances per mesh")
     ap.add_argument("--pack-steps", type=int, default=20)
+    ap.add_argument("--long-steps", type=int, default=10000, help="long workload: steps from rest")
     ap.add_argument("--poisson-reps", type=int, default=2)
     args = ap.parse_args()
 
@@ -968,10 +1038,10 @@ def main():
                           "e2e": {"value": v, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}))
         return
 
-    if args.workload in ("poisson", "small", "batch", "pack", "adjoint"):
+    if args.workload in ("poisson", "small", "batch", "pack", "adjoint", "long"):
         if rank == 0 and args.impl == "ours":
             fn = {"poisson": bench_poisson, "small": bench_small, "batch": bench_batch,
-                  "pack": bench_pack, "adjoint": bench_adjoint}[args.workload]
+                  "pack": bench_pack, "adjoint": bench_adjoint, "long": bench_long}[args.workload]
             print(json.dumps(fn(args)))
         return
 

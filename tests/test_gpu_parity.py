@@ -70,6 +70,31 @@ def test_spmv_alpha_beta_and_fp32(setup, torch_cuda):
     assert np.max(np.abs(y32.cpu().numpy() - ref)) <= 1e-5 * np.max(np.abs(ref))
 
 
+@pytest.mark.parametrize("dtype", ["f64", "f32"])
+def test_spmv_after_value_updates(setup, torch_cuda, dtype):
+    """nsf_csr_update_values from host and from device memory: the SpMV (which runs on the SELL
+    copy) uses the new values -- the copy is regathered from the CSR values on every update."""
+    G, O, mesh, ctx, om, oc = setup
+    t = torch_cuda
+    a = ctx.matrix("M")
+    dt, tdt, tol = (G.NSF_F64, t.float64, 1e-13) if dtype == "f64" else (G.NSF_F32, t.float32, 1e-5)
+    A = G.CsrF.from_host(a, dtype=dt)
+    rng = np.random.default_rng(21)
+    x = rng.standard_normal(a.cols)
+    xd = t.tensor(x, dtype=tdt, device="cuda")
+    for k, new in enumerate((2.0 * a.values, rng.standard_normal(a.nnz))):
+        if k == 0:
+            A.update_values(new)                                    # host values
+        else:
+            A.update_values(t.tensor(new, dtype=tdt, device="cuda"))  # device values
+            t.cuda.synchronize()
+        y = t.zeros(a.rows, dtype=tdt, device="cuda")
+        G.spmv(A, xd, y)
+        t.cuda.synchronize()
+        ref = O.spmv(O.Csr(a.rows, a.cols, a.rowStart, a.column, new), x)
+        assert np.max(np.abs(y.cpu().numpy() - ref)) <= tol * np.max(np.abs(ref)), (dtype, k)
+
+
 def test_spmm_two_channels(setup, torch_cuda):
     G, O, mesh, ctx, om, oc = setup
     t = torch_cuda
