@@ -48,6 +48,9 @@ def peaks():
     return 6800.0, "fallback"
 
 
+MASS_SOLVES = {1: "PCG, multicolor SGS", 2: "PCG, Jacobi", 3: "Chebyshev, Jacobi (a priori iteration count)"}
+
+
 def make_mesh(tmpdir: str, h: float, seed: int = 0) -> str:
     from nsfemoptim_gb300 import meshgen
     path = os.path.join(tmpdir, f"channel_h{h}_s{seed}.msh")
@@ -367,7 +370,7 @@ def bench_adjoint(args):
                                f"{n} steps from rest, J = mean c_D over the last {n - n // 2} steps, "
                                f"grad wrt nu + 16 inflow sine coefficients",
                    "N": N, "P": P, "checkpoint_interval": args.adjoint_checkpoint, "solve_tol": ADJ_TOL,
-                   "mass_preconditioner": {1: "multicolor SGS", 2: "Jacobi"}[args.adjoint_vel_method],
+                   "mass_solve": MASS_SOLVES[args.adjoint_vel_method],
                    "precision": {"f64": "FP64 operators and solves",
                                  "mixedsolve": "FP64 operators and state; FP32 CG inside FP64 residual replacement / "
                                                "refinement to the same FP64 tolerance"}[args.adjoint_precision],
@@ -427,7 +430,7 @@ def bench_batch(args):
         steppers = []
         for b in range(B):
             ctx = G.build_chorin_context(mesh, 4.0 * float(umax[b]))
-            steppers.append(G.ChorinStepper(ctx, float(nus[b]), tau, precision=G.NSF_PREC_MIXED, vel_method=2,
+            steppers.append(G.ChorinStepper(ctx, float(nus[b]), tau, precision=G.NSF_PREC_MIXED, vel_method=args.vel_method,
                                             vel_max_iters=500, vel_tol=VEL_TOL, pres_max_iters=5000,
                                             pres_tol=PRES_TOL, check_interval=8, use_graph=True, max_outer=4,
                                             inner_tol=1e-5))
@@ -491,6 +494,7 @@ def bench_batch(args):
         "data": "synthetic (seeded DFG channel mesh h=0.01; U_max, nu per instance from seed 0)",
         "config": {"workload": f"{B} instances, h=0.01, U_max~U[0.2,1.5], nu~logU[5e-4,2e-3], tau=2e-4, "
                                "pressure to 1e-8 rel", "instances": B, "setup_s": round(setup_s, 1),
+                   "mass_solve": MASS_SOLVES[args.vel_method],
                    "execution": "one graph-captured stepper per instance on its own stream, cluster-resident solves"},
         "one_instance_steps_per_s": round(one, 2),
         "speedup_vs_one_at_a_time": round(agg / one, 2),
@@ -505,7 +509,7 @@ def bench_batch(args):
 def bench_pack(args):
     """Uneven pack: 16 instances on each of three channel meshes (h = 0.025, 0.01, 0.005; synthetic,
     seed 0), U_max ~ U[0.2, 1.5] and nu ~ logU[5e-4, 2e-3] per instance (seed 1), mixed precision,
-    Jacobi mass solves, pressure to 1e-8, tau = 5e-5 (inside the explicit limit
+    mass solves of --vel-method, pressure to 1e-8, tau = 5e-5 (inside the explicit limit
     2 / (nu lambda_max(M^-1 K)) = 9.9e-5 of the finest mesh at nu = 2e-3).  All 48 time steps are
     branches of one CUDA graph (nsf_pack): one launch advances every instance, and every solve stays
     inside a thread-block cluster so the branches run side by side.  Timed: K launches (CUDA events
@@ -534,7 +538,7 @@ def bench_pack(args):
                 nu = float(math.exp(rng.uniform(math.log(5e-4), math.log(2e-3))))
                 ctx = G.build_chorin_context(mesh, 4.0 * umax)
                 sizes[h] = (ctx.N, ctx.P)
-                steppers.append(G.ChorinStepper(ctx, nu, tau, precision=G.NSF_PREC_MIXED, vel_method=2,
+                steppers.append(G.ChorinStepper(ctx, nu, tau, precision=G.NSF_PREC_MIXED, vel_method=args.vel_method,
                                                 vel_max_iters=500, vel_tol=VEL_TOL, pres_max_iters=5000,
                                                 pres_tol=PRES_TOL, check_interval=8, use_graph=True, max_outer=4,
                                                 inner_tol=1e-5))
@@ -585,6 +589,7 @@ def bench_pack(args):
         "data": "synthetic (seeded DFG channel meshes h=0.025/0.01/0.005; U_max, nu per instance from seed 1)",
         "config": {"workload": f"{per} instances on each of h={hs}, U_max~U[0.2,1.5], nu~logU[5e-4,2e-3], "
                                f"tau={tau}, pressure to 1e-8 rel", "instances": n,
+                   "mass_solve": MASS_SOLVES[args.vel_method],
                    "mesh_sizes_N_P": {str(h): sizes[h] for h in hs}, "setup_s": round(setup_s, 1),
                    "execution": "one CUDA graph per step whose branches are the 48 instances' steps (nsf_pack); "
                                 "cluster-resident solves"},
@@ -598,7 +603,7 @@ def bench_pack(args):
 
 def bench_long(args):
     """Config 2 over a long horizon: the h = 0.005 channel of the default workload (U_max = 1.5,
-    nu = 1e-3, tau = 1e-4, pressure to 1e-8, Jacobi mass solves, extrapolated pressure guess) from
+    nu = 1e-3, tau = 1e-4, pressure to 1e-8, mass solves of --vel-method, extrapolated pressure guess) from
     rest for --long-steps steps with the mixed stepper and the FP64 stepper side by side: the
     relative L2 difference of u and p every 1000 steps, and the drag / lift time series (every step,
     written on the device) compared over the whole run.  Both steppers are timed."""
@@ -614,7 +619,7 @@ def bench_long(args):
         ctx = G.build_chorin_context(mesh, PEAK)
 
         def stepper(prec):
-            return G.ChorinStepper(ctx, NU, TAU, precision=prec, vel_method=2, vel_max_iters=500, vel_tol=VEL_TOL,
+            return G.ChorinStepper(ctx, NU, TAU, precision=prec, vel_method=args.vel_method, vel_max_iters=500, vel_tol=VEL_TOL,
                                    pres_max_iters=5000, pres_tol=PRES_TOL, check_interval=8, use_graph=True,
                                    max_outer=4, inner_tol=1e-5, pressure_guess=1)
 
@@ -654,7 +659,8 @@ def bench_long(args):
         "dtype": "f32-inner/f64-refine",
         "data": "synthetic (seeded DFG channel mesh, h=0.005)",
         "config": {"workload": f"DFG channel h={H}, Umax=1.5, nu={NU}, tau={TAU}, {n} steps from rest, pressure "
-                               f"to {PRES_TOL} rel", "N": ctx.N, "P": ctx.P},
+                               f"to {PRES_TOL} rel", "N": ctx.N, "P": ctx.P,
+                   "mass_solve": MASS_SOLVES[args.vel_method]},
         "fp64_steps_per_s": round(n / secs["fp64"], 2),
         "field_rel_l2_mixed_vs_fp64": field,
         "drag_max_rel_err": float(np.abs(sm[:, 0] - sf[:, 0]).max() / fmax),
@@ -932,7 +938,7 @@ def bench_ours(args, rank, world, local_rank):
                        "internal_pressure": nip, "nnz_I": nnzI, "parallelism": f"replicas x{world}",
                        "l2": "working set > L2 (FastConvection matrix %.0f MB FP32)" % (nnzI * 8 / 1e6),
                        "graph": True, "setup_s": round(setup_s, 2),
-                       "mass_solve": {1: "PCG, multicolor SGS", 2: "PCG, Jacobi"}[args.vel_method],
+                       "mass_solve": MASS_SOLVES[args.vel_method],
                        "pressure_guess": {0: "previous solution", 1: "2 p(n-1) - p(n-2)"}[args.pressure_guess]},
             "e2e": {"value": round(world * e2e_steps / t_e2e, 3), "unit": "steps/s",
                     "h2d_bytes_per_step": (2 * N + P) * 8, "d2h_bytes_per_step": (2 * N + P) * 8},
@@ -977,15 +983,16 @@ def main():
                     help="channel: the h=0.005 time step (default); poisson: the standalone 1M-DOF pressure "
                          "solve; small: the plain FP64 h=0.02 channel; batch: 64 instances at h=0.01; "
                          "adjoint: the drag gradient at h=0.01 over 1000 steps")
-    ap.add_argument("--vel-method", type=int, default=2, choices=[1, 2],
-                    help="channel workload: mass-solve preconditioner, 1 multicolor SGS, 2 Jacobi")
+    ap.add_argument("--vel-method", type=int, default=3, choices=[1, 2, 3],
+                    help="channel, batch, pack and long workloads: mass solve, 1 PCG multicolor SGS, 2 PCG "
+                         "Jacobi, 3 Chebyshev Jacobi")
     ap.add_argument("--pressure-guess", type=int, default=1, choices=[0, 1],
                     help="channel workload: pressure initial guess, 0 previous solution, 1 extrapolated")
     ap.add_argument("--adjoint-steps", type=int, default=1000)
     ap.add_argument("--adjoint-checkpoint", type=int, default=50)
     ap.add_argument("--adjoint-precision", default="mixedsolve", choices=["f64", "mixedsolve"])
-    ap.add_argument("--adjoint-vel-method", type=int, default=2, choices=[1, 2],
-                    help="mass-solve preconditioner: 1 multicolor SGS, 2 Jacobi")
+    ap.add_argument("--adjoint-vel-method", type=int, default=2, choices=[1, 2, 3],
+                    help="mass solve: 1 PCG multicolor SGS, 2 PCG Jacobi, 3 Chebyshev Jacobi")
     ap.add_argument("--adjoint-reps", type=int, default=1, help="timed gradient evaluations")
     ap.add_argument("--adjoint-warmup", type=int, default=1, help="untimed gradient evaluations")
     ap.add_argument("--adjoint-cpu-steps", type=int, default=6)

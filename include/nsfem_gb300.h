@@ -174,7 +174,11 @@ typedef struct
                              multicolor SGS preconditioner (relative velTol), 2: "pcg" with the
                              Jacobi preconditioner (no reference counterpart: the diagonally
                              scaled P2 mass matrix has condition number ~5.2 whatever h, and each
-                             iteration is one parallel phase) */
+                             iteration is one parallel phase), 3: Chebyshev iteration with the
+                             Jacobi preconditioner over the spectral bounds [0.39237, 2.05982] of
+                             D^-1 M (those of every affine P2 element), the iteration count fixed
+                             in advance from velTol (relative); FP64 in every precision mode, one
+                             kernel per iteration, no reductions but the final residual check */
     int velMaxIters;
     double velTol;
     int presMaxIters;

@@ -337,7 +337,8 @@ class ChorinStepper:
                  vel_method: int = 1, vel_max_iters: int = 200, vel_tol: float = 1e-10,
                  pres_max_iters: int = 2000, pres_tol: float = 1e-10, check_interval: int = 8,
                  use_graph: bool = True, max_outer: int = 4, inner_tol: float = 1e-4, pressure_guess: int = 0):
-        """pressure_guess: 0 the previous pressure (as the reference), 1 extrapolated from the last two."""
+        """vel_method: mass solve, 0 multicolor GS, 1 PCG-SGS, 2 PCG-Jacobi, 3 Chebyshev-Jacobi.
+        pressure_guess: 0 the previous pressure (as the reference), 1 extrapolated from the last two."""
         self.ctx = ctx
         self.cfg = ChorinConfig(nu, tau, precision, vel_method, vel_max_iters, vel_tol, pres_max_iters, pres_tol,
                                 check_interval, int(use_graph), max_outer, inner_tol, int(pressure_guess))

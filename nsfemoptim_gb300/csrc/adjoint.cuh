@@ -283,6 +283,7 @@ struct nsf_adjoint_s
     PcgSolver<double, 2> mass;
     PcgSolver<double, 1> pres;
     MixedPcg<2> mmass; // the solves of a NSF_PREC_F64_MIXEDSOLVE stepper: FP32 CG, FP64 residuals
+    ChebSolver cmass;  // the mass solve of a velMethod 3 stepper
     MixedPcg<1> mpres;
     cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
     std::vector<double> hwD, hwL;
@@ -311,6 +312,11 @@ struct nsf_adjoint_s
             st[1] = S->mpres.st.get();
             st[2] = S->mvelF.st.get();
         }
+        if (S->cfg.velMethod == 3)
+        {
+            st[0] = S->chebT.st.get();
+            st[2] = S->chebF.st.get();
+        }
         for (int k = 0; k < 3; k++)
             NSF_LAUNCH(kTally, 1, s, st[k], k == 1 ? 1 : 2, tally.get(), 0);
     }
@@ -319,7 +325,12 @@ struct nsf_adjoint_s
     void massSolve(cudaStream_t s)
     {
         NSF_CUDA(cudaMemsetAsync(x.get(), 0, sizeof(double) * 2 * N, s));
-        if (S->mixedSolve)
+        if (S->cfg.velMethod == 3)
+        {
+            cmass.enqueue(s, rhs.get(), x.get(), cfg.maxIters, cfg.tol);
+            NSF_LAUNCH(kTally, 1, s, cmass.st.get(), 2, tally.get() + 2, 1);
+        }
+        else if (S->mixedSolve)
         {
             mmass.enqueue(s, S->body, rhs.get(), x.get(), S->cfg.maxOuter, cfg.tol, cfg.maxIters, S->cfg.innerTol, 1);
             NSF_LAUNCH(kTally, 1, s, mmass.st.get(), 2, tally.get() + 2, 2);
@@ -524,16 +535,16 @@ extern "C" int nsf_adjoint_create(nsf_chorin S, nsf_forces f, const nsf_adjoint_
         a->tally = DevBuf<int>(6);
         a->finU.alloc(twoN);
         a->finP.alloc(nI);
-        if (S->mixedSolve)
-        {
+        if (S->cfg.velMethod == 3)
+            a->cmass.setup(&S->M64, &S->Msell, 2);
+        else if (S->mixedSolve)
             a->mmass.setup(&S->M64, &S->M32, 2);
-            a->mpres.setup(&S->Kpi64, &S->Kpi32, 1);
-        }
         else
-        {
             a->mass.setup(&S->M64, 2);
+        if (S->mixedSolve)
+            a->mpres.setup(&S->Kpi64, &S->Kpi32, 1);
+        else
             a->pres.setup(&S->Kpi64, 1);
-        }
         for (cudaEvent_t & e : a->ev)
             NSF_CUDA(cudaEventCreate(&e));
         NSF_CUDA(cudaStreamSynchronize(S->stream));

@@ -182,6 +182,80 @@ namespace nsf
         int blocks() const { return blocksFor((long long)nSlices * SELL_C); }
     };
 
+    // Chebyshev iteration with the Jacobi preconditioner for the P2 mass matrix (velMethod 3).  The
+    // spectrum of D^-1 M lies in [0.392375, 2.059816]: every element matrix is |T| times the same
+    // reference matrix (affine P2 triangles, exact quadrature), and those are the extreme generalized
+    // eigenvalues of the reference pair (M_ref, diag M_ref), so the bound holds on any mesh.  With
+    // kappa = 5.25 the error contracts by rho = (sqrt(kappa) - 1) / (sqrt(kappa) + 1) = 0.392 per
+    // iteration: the count for a relative tolerance is fixed in advance (no dot products, one fused
+    // kernel per iteration, graph-capturable), and a final FP64 residual gives the statistics.
+    constexpr double kMassSpecLo = 0.39237, kMassSpecHi = 2.05982;
+
+    struct ChebSolver
+    {
+        const SweepSystem<double> * sys = nullptr;
+        const DevSell<double> * sell = nullptr;
+        int numCh = 2;
+        double dratio = 1.0; // max / min of diag(M): the 2-norm factor of the D-scaled error bound
+        DevBuf<double> r, d0, d1, scratch;
+        DevBuf<SolverState> st;
+
+        void setup(const SweepSystem<double> * s, const DevSell<double> * sl, int channels)
+        {
+            sys = s;
+            sell = sl;
+            numCh = channels;
+            const size_t n = (size_t)s->n;
+            r.alloc(2 * n);
+            d0.alloc(2 * n);
+            d1.alloc(2 * n);
+            scratch.alloc((size_t)2 * MAXCH * cappedBlocks(1ll << 40));
+            st.alloc(1);
+            const std::vector<double> dg = s->diag.download();
+            double lo = 1e300, hi = 0;
+            for (double v : dg)
+            {
+                lo = std::min(lo, std::fabs(v));
+                hi = std::max(hi, std::fabs(v));
+            }
+            dratio = lo > 0 ? hi / lo : 1.0;
+        }
+
+        // iterations for ||r|| <= tol ||b||: 2 rho^k sqrt(dratio) <= tol
+        int itersFor(double tol) const
+        {
+            const double kappa = kMassSpecHi / kMassSpecLo;
+            const double rho = (std::sqrt(kappa) - 1.0) / (std::sqrt(kappa) + 1.0);
+            const double target = tol / (2.0 * std::sqrt(dratio));
+            return std::max(1, (int)std::ceil(std::log(target) / std::log(rho)));
+        }
+
+        // x must be 0 on entry (the mass solves of the step start from zero)
+        void enqueue(cudaStream_t s, const double * b, double * x, int maxIters, double tol)
+        {
+            const int n = sys->n, k = std::min(maxIters, itersFor(tol));
+            NSF_LAUNCH(kSetConfig, 1, s, st.get(), maxIters, 0, tol * tol);
+            const double theta = 0.5 * (kMassSpecHi + kMassSpecLo), delta = 0.5 * (kMassSpecHi - kMassSpecLo);
+            const double sigma = theta / delta;
+            NSF_LAUNCH((kChebStart<2>), blocksFor(n), s, n, b, sys->invD.get(), 1.0 / theta, r.get(), d0.get());
+            double rho = 1.0 / sigma;
+            double * dc = d0.get();
+            double * dn = d1.get();
+            for (int it = 0; it < k; it++)
+            {
+                const double rhoN = 1.0 / (2.0 * sigma - rho);
+                NSF_LAUNCH((kChebStep<2>), sell->blocks(), s, n, sell->nSlices, sell->ss.get(), sell->perm.get(),
+                           sell->ci.get(), sell->v.get(), sys->invD.get(), (const double *)dc, dn, x, r.get(),
+                           rhoN * rho, 2.0 * rhoN / delta);
+                rho = rhoN;
+                std::swap(dc, dn);
+            }
+            const SweepSystem<double> & S = *sys;
+            NSF_LANES(S.L, NSF_LAUNCH((kChebFinal<LL, 2>), S.fullBlocks(), s, n, S.rsF.get(), S.ciF.get(), S.vF.get(),
+                                      (const double *)x, b, st.get(), scratch.get(), numCh, k));
+        }
+    };
+
     // y = alpha A x + beta y through the SELL copy (accumulation in TA)
     template <typename TA, typename TM, typename TX, typename TY>
     void sellSpmv(const DevSell<TM> & S, const TX * x, TY * y, double alpha, double beta, cudaStream_t s)
@@ -785,6 +859,8 @@ struct nsf_chorin_s
     DevBuf<double> dirVal;
     // solvers: separate objects for the tentative and the final mass solve keep both stats
     PcgSolver<double, 2> velT, velF;
+    ChebSolver chebT, chebF; // velMethod 3 (FP64 Chebyshev-Jacobi on the SELL copy of M)
+    DevSell<double> Msell;
     GsSolver<double, 2> gsT, gsF;
     PcgSolver<double, 1> pres;
     MixedPcg<2> mvelT, mvelF;
@@ -833,7 +909,9 @@ struct nsf_chorin_s
         double * b = rhs.get();
         double * x = acc.get();
         NSF_CUDA(cudaMemsetAsync(x, 0, sizeof(double) * 2 * N, s));
-        if (mixed || mixedSolve)
+        if (cfg.velMethod == 3)
+            (tentative ? chebT : chebF).enqueue(s, b, x, cfg.velMaxIters, cfg.velTol);
+        else if (mixed || mixedSolve)
             (tentative ? mvelT : mvelF)
                 .enqueue(s, body, b, x, cfg.maxOuter, cfg.velTol, cfg.velMaxIters, cfg.innerTol, cfg.checkInterval);
         else if (cfg.velMethod == 0)
@@ -900,6 +978,7 @@ struct nsf_chorin_s
     {
         const SolverState * src[3];
         const bool inner = mixed || mixedSolve;
+        bool srcInner[3] = {inner, inner, inner};
         if (inner)
         {
             src[0] = mvelT.st.get();
@@ -911,6 +990,12 @@ struct nsf_chorin_s
             src[0] = cfg.velMethod == 0 ? gsT.st.get() : velT.st.get();
             src[1] = pres.st.get();
             src[2] = cfg.velMethod == 0 ? gsF.st.get() : velF.st.get();
+        }
+        if (cfg.velMethod == 3)
+        {
+            src[0] = chebT.st.get();
+            src[2] = chebF.st.get();
+            srcInner[0] = srcInner[2] = false;
         }
         for (int i = 0; i < 3; i++)
             NSF_CUDA(cudaMemcpyAsync(stat.get() + i, src[i], sizeof(SolverState), cudaMemcpyDeviceToHost, s));
@@ -924,7 +1009,7 @@ struct nsf_chorin_s
             double rel = 0;
             for (int c = 0; c < nch; c++)
             {
-                it = std::max(it, inner ? L.innerTotal[c] : L.iters[c]);
+                it = std::max(it, srcInner[i] ? L.innerTotal[c] : L.iters[c]);
                 const double r = L.bb[c] > 0 ? std::sqrt(std::max(0.0, L.lastRR[c]) / L.bb[c]) : 0.0;
                 rel = std::max(rel, r);
                 worst = std::max(worst, L.status[c]);
@@ -999,12 +1084,21 @@ static void buildChorin(nsf_chorin_s & S, const Context & c)
     // velMethod 2: the mass systems as one color, which turns the SGS preconditioner of the PCG
     // kernels into Jacobi (the forward phase of a single color gathers nothing): one parallel phase
     // per iteration instead of 2C - 1 color phases
-    const std::vector<int> mParts = S.cfg.velMethod == 2 ? std::vector<int>{0, N} : cv.partStart;
+    const bool cheb = S.cfg.velMethod == 3;
+    const std::vector<int> mParts = S.cfg.velMethod >= 2 ? std::vector<int>{0, N} : cv.partStart;
     S.M64.build(Mp, mParts);
+    if (cheb)
+    {
+        // velMethod 3: the Chebyshev iteration reads M through its SELL copy, with no other solver
+        S.Msell.build(N, Mp.rowStart.data(), Mp.col.data(), Mp.val.data());
+        S.chebT.setup(&S.M64, &S.Msell, 2);
+        S.chebF.setup(&S.M64, &S.Msell, 2);
+    }
     S.Kpi64.build(Kpip, cp.partStart);
     std::vector<double> knu(Kp.val.begin(), Kp.val.end());
     if (S.mixed)
     {
+        // M32 also carries the pattern of the rhs = A u product of the mixed step (M and K share it)
         S.M32.build(Mp, mParts);
         S.Kpi32.build(Kpip, cp.partStart);
         S.I32.upload(Ip, true);
@@ -1013,8 +1107,11 @@ static void buildChorin(nsf_chorin_s & S, const Context & c)
         std::vector<float> k32(knu.begin(), knu.end());
         S.K32.upload(k32);
         S.A32.alloc(knu.size());
-        S.mvelT.setup(&S.M64, &S.M32, 2, kMassIters);
-        S.mvelF.setup(&S.M64, &S.M32, 2, kMassIters);
+        if (!cheb)
+        {
+            S.mvelT.setup(&S.M64, &S.M32, 2, kMassIters);
+            S.mvelF.setup(&S.M64, &S.M32, 2, kMassIters);
+        }
         S.mpres.setup(&S.Kpi64, &S.Kpi32, 1, kPresIters);
     }
     else
@@ -1027,10 +1124,13 @@ static void buildChorin(nsf_chorin_s & S, const Context & c)
         if (S.mixedSolve)
         {
             // FP64 operators, FP32-inner solves on FP32 copies of the two systems
-            S.M32.build(Mp, mParts);
             S.Kpi32.build(Kpip, cp.partStart);
-            S.mvelT.setup(&S.M64, &S.M32, 2, kMassIters);
-            S.mvelF.setup(&S.M64, &S.M32, 2, kMassIters);
+            if (!cheb)
+            {
+                S.M32.build(Mp, mParts);
+                S.mvelT.setup(&S.M64, &S.M32, 2, kMassIters);
+                S.mvelF.setup(&S.M64, &S.M32, 2, kMassIters);
+            }
             S.mpres.setup(&S.Kpi64, &S.Kpi32, 1, kPresIters);
         }
         else
@@ -1040,7 +1140,7 @@ static void buildChorin(nsf_chorin_s & S, const Context & c)
                 S.gsT.setup(&S.M64, 2, 1);
                 S.gsF.setup(&S.M64, 2, 1);
             }
-            else
+            else if (!cheb)
             {
                 S.velT.setup(&S.M64, 2, true, kMassIters);
                 S.velF.setup(&S.M64, 2, true, kMassIters);
@@ -1086,10 +1186,12 @@ extern "C" int nsf_chorin_create(nsf_context ctx, const nsf_chorin_config * cfg,
                     cfg->precision == NSF_PREC_F64_MIXEDSOLVE,
                 "unknown precision");
         require(!(cfg->precision == NSF_PREC_F64_MIXEDSOLVE && cfg->velMethod == 0),
-                "mixed solves use velMethod 1 (pcg)");
-        require(cfg->velMethod >= 0 && cfg->velMethod <= 2,
-                "velMethod must be 0 (gs), 1 (pcg, SGS preconditioner) or 2 (pcg, Jacobi preconditioner)");
-        require(!(cfg->precision == NSF_PREC_MIXED && cfg->velMethod == 0), "mixed precision uses velMethod 1 (pcg)");
+                "mixed solves use velMethod 1, 2 (pcg) or 3 (chebyshev)");
+        require(cfg->velMethod >= 0 && cfg->velMethod <= 3,
+                "velMethod must be 0 (gs), 1 (pcg, SGS preconditioner), 2 (pcg, Jacobi preconditioner) or 3 "
+                "(chebyshev, Jacobi preconditioner)");
+        require(!(cfg->precision == NSF_PREC_MIXED && cfg->velMethod == 0),
+                "mixed precision uses velMethod 1, 2 (pcg) or 3 (chebyshev)");
         require(cfg->velMaxIters >= 1 && cfg->presMaxIters >= 1, "iteration caps must be >= 1");
         require(cfg->pressureGuess == 0 || cfg->pressureGuess == 1, "pressureGuess must be 0 or 1");
         auto S = std::make_unique<nsf_chorin_s>();

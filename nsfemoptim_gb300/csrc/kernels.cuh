@@ -429,6 +429,90 @@ namespace nsf
         }
     }
 
+    // ------------------------------------------------------------------ Chebyshev (mass matrix)
+    // Chebyshev iteration with the Jacobi preconditioner for an SPD matrix whose D^-1 A spectrum
+    // lies in known bounds (Saad, Iterative Methods, Alg. 12.1): no dot products, one fused kernel
+    // per iteration over the SELL copy.  NCH planar channels of n rows each, x starts at 0.
+    //   start:  r = b,  d = D^-1 b / theta
+    //   step k: q = A d;  x += d;  r -= q;  d' = c1 d + c2 D^-1 r   (c1, c2 from the bounds and k)
+    template <int NCH>
+    __global__ void __launch_bounds__(TPB) kChebStart(int n, const double * __restrict__ b, const double * __restrict__ invD,
+                                                       double invTheta, double * __restrict__ r, double * __restrict__ d)
+    {
+        for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        {
+            const double id = invD[i];
+#pragma unroll
+            for (int c = 0; c < NCH; c++)
+            {
+                const double bi = b[(size_t)c * n + i];
+                r[(size_t)c * n + i] = bi;
+                d[(size_t)c * n + i] = bi * id * invTheta;
+            }
+        }
+    }
+
+    template <int NCH>
+    __global__ void __launch_bounds__(TPB) kChebStep(int n, int nSlices, const int * __restrict__ ss,
+                                                      const int * __restrict__ perm, const int * __restrict__ ci,
+                                                      const double * __restrict__ v, const double * __restrict__ invD,
+                                                      const double * __restrict__ d, double * __restrict__ dn,
+                                                      double * __restrict__ x, double * __restrict__ r, double c1,
+                                                      double c2)
+    {
+        const int slice = (int)((blockIdx.x * (unsigned)blockDim.x + threadIdx.x) >> 5);
+        if (slice >= nSlices)
+            return;
+        const int lane = threadIdx.x & 31;
+        const int row = slice * SELL_C + lane;
+        const int b0 = ldg(ss + slice), e0 = ldg(ss + slice + 1);
+        // q = A d for every channel; each column / value load serves all channels
+        double q[NCH];
+#pragma unroll
+        for (int c = 0; c < NCH; c++)
+            q[c] = 0.0;
+        const int w = (e0 - b0) / SELL_C;
+        for (int k = 0; k < w; k += 4)
+        {
+            int cc[4];
+            double a[4];
+#pragma unroll
+            for (int t = 0; t < 4; t++)
+            {
+                const bool ok = k + t < w;
+                const int j = b0 + (k + t) * SELL_C + lane;
+                cc[t] = ok ? ldg(ci + j) : 0;
+                a[t] = ok ? ldg(v + j) : 0.0;
+            }
+#pragma unroll
+            for (int c = 0; c < NCH; c++)
+            {
+                double g[4];
+#pragma unroll
+                for (int t = 0; t < 4; t++)
+                    g[t] = k + t < w ? ldg(d + (size_t)c * n + cc[t]) : 0.0;
+#pragma unroll
+                for (int t = 0; t < 4; t++)
+                    if (k + t < w)
+                        q[c] += a[t] * g[t];
+            }
+        }
+        if (row >= n)
+            return;
+        const int i = ldg(perm + row);
+        const double id = ldg(invD + i);
+#pragma unroll
+        for (int c = 0; c < NCH; c++)
+        {
+            const size_t o = (size_t)c * n + i;
+            const double di = d[o];
+            x[o] += di;
+            const double ri = r[o] - q[c];
+            r[o] = ri;
+            dn[o] = c1 * di + c2 * ri * id;
+        }
+    }
+
     // Initial guess of the pressure solve from the last two solutions: before step k the solve
     // starts from 2 p_{k-1} - p_{k-2} once two solved pressures exist (hist >= 2), else from p_{k-1};
     // prev keeps p_{k-1} for the next step.  kHistBump advances the count afterwards (separate
@@ -1238,6 +1322,76 @@ namespace nsf
             return;
         for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < NCH * n; i += gridDim.x * blockDim.x)
             x[i] += (double)d[i] * st->rinv[i / n];
+    }
+
+    // After a Chebyshev solve: ||b - A x||^2 and ||b||^2 per channel in FP64 (row groups over the
+    // CSR), recorded as the solve's statistics: iters, bb, lastRR, status (0 if within tol2, else 3).
+    struct ChebEpi
+    {
+        SolverState * st;
+        int numCh, iters;
+        __device__ void operator()() const
+        {
+            for (int c = 0; c < numCh; c++)
+            {
+                const double rr = st->rrOut[0][c], bb = st->bbOut[c];
+                st->bb[c] = bb;
+                st->lastRR[c] = rr;
+                st->iters[c] = iters;
+                st->innerTotal[c] = iters;
+                st->active[c] = 0;
+                st->status[c] = !(isfinite(rr) && isfinite(bb)) ? 2 : (rr <= st->tol2 * bb ? 0 : 3);
+            }
+            st->anyActive = 0;
+        }
+    };
+
+    template <int L, int NCH>
+    __global__ void __launch_bounds__(TPB) kChebFinal(int n, const int * __restrict__ rs, const int * __restrict__ ci,
+                                                       const double * __restrict__ v, const double * __restrict__ x,
+                                                       const double * __restrict__ b, SolverState * st, double * scratch,
+                                                       int numCh, int iters)
+    {
+        Group<L> g;
+        double red[2 * NCH];
+#pragma unroll
+        for (int c = 0; c < 2 * NCH; c++)
+            red[c] = 0;
+        for (int i = g.gid; i < n; i += g.ngroups)
+        {
+            const int s0 = ldg(rs + i), e0 = ldg(rs + i + 1);
+            double acc[NCH];
+#pragma unroll
+            for (int c = 0; c < NCH; c++)
+                acc[c] = 0;
+            for (int j = s0 + g.lane; j < e0; j += L)
+            {
+                const double a = ldg(v + j);
+                const int col = ldg(ci + j);
+#pragma unroll
+                for (int c = 0; c < NCH; c++)
+                    acc[c] += a * x[(size_t)c * n + col];
+            }
+#pragma unroll
+            for (int c = 0; c < NCH; c++)
+            {
+                const double t = g.sum(acc[c]);
+                if (g.lane == 0)
+                {
+                    const double bi = b[(size_t)c * n + i], ri = bi - t;
+                    red[c] += ri * ri;
+                    red[NCH + c] += bi * bi;
+                }
+            }
+        }
+        Outs<2 * NCH> o;
+#pragma unroll
+        for (int c = 0; c < NCH; c++)
+        {
+            o.p[c] = &st->rrOut[0][c];
+            o.p[NCH + c] = &st->bbOut[c];
+        }
+        gridSum<double, 2 * NCH>(red, scratch, o, &st->ticket, nullptr, ChebEpi{st, numCh, iters});
     }
 
     // Stop decision of refinement pass `pass` (sticky); stats: iters = refinement updates applied.

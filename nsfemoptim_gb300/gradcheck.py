@@ -34,7 +34,7 @@ class DragProblem:
                  inner_tol: float = 1e-5, vel_method: int = 1):
         """precision: NSF_PREC_F64 (FP64 solves) or NSF_PREC_F64_MIXEDSOLVE (FP64 operators, FP32 CG
         inside FP64 refinement / residual replacement to the same tolerance; max_outer passes with
-        inner tolerance inner_tol).  vel_method: mass-solve preconditioner, 1 SGS, 2 Jacobi."""
+        inner tolerance inner_tol).  vel_method: mass solve, 1 PCG-SGS, 2 PCG-Jacobi, 3 Chebyshev-Jacobi."""
         self.mesh, self.ctx = mesh, ctx
         self.n_steps = int(n_steps)
         self.stepper = ChorinStepper(ctx, nu, tau, precision=precision, vel_method=vel_method,

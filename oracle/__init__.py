@@ -102,6 +102,9 @@ def _configure(L):
         L.orc_context_free.argtypes = [C.POINTER(ContextS)]
         L.orc_csr_free.argtypes = [C.POINTER(CsrS)]
         L.orc_spmv.argtypes = [C.POINTER(CsrS), f64p, f64p]
+        L.orc_cheb_iters.argtypes = [C.POINTER(CsrS), C.c_double, C.c_double, C.c_double, C.c_int]
+        L.orc_cheb_solve.argtypes = [C.POINTER(CsrS), f64p, f64p, C.c_double, C.c_double, C.c_int, C.c_double,
+                                     f64p]
         L.orc_spmm2.argtypes = [C.POINTER(CsrS), f64p, f64p, f64p]
         L.orc_slice.argtypes = [C.POINTER(CsrS), C.c_int, i32p, C.c_int, i32p, C.POINTER(CsrS)]
         L.orc_coloring_build.argtypes = [C.POINTER(CsrS), C.POINTER(ColoringS)]
@@ -269,6 +272,27 @@ def spmv(a: Csr, x) -> np.ndarray:
     return y
 
 
+# spectral bounds of D^-1 M for the P2 mass matrix (oracle.h ORC_MASS_SPEC_LO / _HI)
+MASS_SPEC_LO, MASS_SPEC_HI = 0.39237, 2.05982
+
+
+def cheb_iters(a: Csr, rel_tol, max_iters=100000, lo=MASS_SPEC_LO, hi=MASS_SPEC_HI) -> int:
+    """A priori Chebyshev-Jacobi iteration count for ||r|| <= rel_tol ||b|| (orc_cheb_iters)."""
+    s = a.struct()
+    return int(lib().orc_cheb_iters(C.byref(s), lo, hi, rel_tol, max_iters))
+
+
+def cheb_solve(a: Csr, b, iters, rel_tol, lo=MASS_SPEC_LO, hi=MASS_SPEC_HI):
+    """x from `iters` Chebyshev-Jacobi iterations from 0; returns (x, status, relative residual)."""
+    b = np.ascontiguousarray(b, dtype=np.float64)
+    x = np.zeros(a.rows, dtype=np.float64)
+    rr = np.zeros(1, dtype=np.float64)
+    s = a.struct()
+    st = lib().orc_cheb_solve(C.byref(s), _ptr(b, C.c_double), _ptr(x, C.c_double), lo, hi, iters, rel_tol,
+                              _ptr(rr, C.c_double))
+    return x, int(st), float(rr[0])
+
+
 def spmm2(a: Csr, vals, x) -> np.ndarray:
     x = np.ascontiguousarray(x, dtype=np.float64)
     vals = np.ascontiguousarray(vals, dtype=np.float64)
@@ -338,7 +362,7 @@ def forces(mesh: Mesh, u, p, nu: float, group: str = "Circle") -> np.ndarray:
 
 class Chorin:
     """FP64 Chorin stepper of the oracle.  vel_method 0 = multicolor GS (RMS target),
-    1 = CG + multicolor SGS, 2 = CG + Jacobi (relative tolerance).  mt: run on the OpenMP build
+    1 = CG + multicolor SGS, 2 = CG + Jacobi, 3 = Chebyshev-Jacobi (relative tolerance).  mt: run on the OpenMP build
     (all host threads, OMP_NUM_THREADS); self.threads says what ran (1 if that build is missing)."""
 
     def __init__(self, ctx: Context, nu, tau, vel_method=1, vel_max_iters=200, vel_tol=1e-10,

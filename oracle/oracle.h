@@ -114,6 +114,16 @@ void orc_sys_free(orc_sys *s);
 int orc_sys_pcg(const orc_sys *s, int precond, const double *b, double *x, int maxIters, double relTol, int *iters,
                 double *relRes);
 
+/* Chebyshev iteration with the Jacobi preconditioner from x = 0, for an SPD matrix whose D^-1 A
+   spectrum lies in [lo, hi]; orc_cheb_iters gives the a priori count for ||r|| <= relTol ||b||
+   (capped at maxIters).  Returns 0 if the true residual meets relTol, 3 if not, 2 non-finite. */
+int orc_cheb_iters(const orc_csr *a, double lo, double hi, double relTol, int maxIters);
+int orc_cheb_solve(const orc_csr *a, const double *b, double *x, double lo, double hi, int iters,
+                   double relTol, double *relRes);
+/* spectral bounds of D^-1 M for the P2 mass matrix of affine triangles (any mesh) */
+#define ORC_MASS_SPEC_LO 0.39237
+#define ORC_MASS_SPEC_HI 2.05982
+
 /* y = (D+L) D^-1 (D+U) inverse applied to r in colored order (the preconditioner alone) */
 void orc_sgs_apply(const orc_csr *a, const orc_coloring *c, const double *r, double *z);
 
@@ -121,7 +131,8 @@ void orc_sgs_apply(const orc_csr *a, const orc_coloring *c, const double *r, dou
 typedef struct
 {
     double nu, tau;
-    int velMethod;       /* 0 = multicolor GS (RMS target), 1 = PCG-SGS, 2 = PCG-Jacobi (relative tol) */
+    int velMethod;       /* 0 = multicolor GS (RMS target), 1 = PCG-SGS, 2 = PCG-Jacobi, 3 = Chebyshev-
+                            Jacobi (relative tol) */
     int velMaxIters;
     double velTol;       /* RMS target for GS, relative tolerance for PCG */
     int presMaxIters;

@@ -13,7 +13,9 @@
  *   g = G p;  acc = 0;  solve M acc = g;  u = u - tau acc;  Dirichlet   (:341-356)
  * Velocity solves: method 0 is the multicolor Gauss-Seidel solver with an RMS target (the
  * reference's "gs"), method 1 is CG with the multicolor SGS preconditioner to a relative
- * tolerance.  Pressure: CG with the multicolor SGS preconditioner to a relative tolerance.
+ * tolerance, method 2 the same CG with the Jacobi preconditioner, method 3 Chebyshev-Jacobi
+ * with the a priori iteration count of orc_cheb_iters.  Pressure: CG with the multicolor SGS
+ * preconditioner to a relative tolerance.
  */
 #include "oracle.h"
 
@@ -144,6 +146,19 @@ static int mass_solve(orc_chorin *s, const double *rhs, double *acc, double *res
     }
     int itMax = 0;
     *res = 0;
+    if (s->cfg.velMethod == 3)
+    {
+        const int k = orc_cheb_iters(&ctx->M, ORC_MASS_SPEC_LO, ORC_MASS_SPEC_HI, s->cfg.velTol, s->cfg.velMaxIters);
+        for (int ch = 0; ch < 2; ch++)
+        {
+            double rr = 0;
+            orc_cheb_solve(&ctx->M, rhs + ch * N, acc + ch * N, ORC_MASS_SPEC_LO, ORC_MASS_SPEC_HI, k,
+                           s->cfg.velTol, &rr);
+            if (rr > *res)
+                *res = rr;
+        }
+        return k;
+    }
     for (int ch = 0; ch < 2; ch++)
     {
         int it = 0;

@@ -644,3 +644,82 @@ int orc_sys_pcg(const orc_sys *s, int precond, const double *b, double *x, int m
 {
     return pcg_core(&s->g, s->c, precond, b, x, maxIters, relTol, iters, relRes);
 }
+
+/* ---------------- Chebyshev-Jacobi solve (mass-solve method 3) ----------------
+ * Saad, Iterative Methods for Sparse Linear Systems, Alg. 12.1 with the Jacobi preconditioner and
+ * x0 = 0; [lo, hi] bounds the spectrum of D^-1 A.  The iteration count follows the a priori bound
+ * ||r_k|| <= 2 rho^k sqrt(max D / min D) ||b||, rho = (sqrt(hi/lo) - 1) / (sqrt(hi/lo) + 1),
+ * taken as the smallest k that brings it under relTol (at least 1, at most maxIters). */
+static double diag_ratio(const orc_csr *a)
+{
+    double lo = 1e300, hi = 0;
+    for (int i = 0; i < a->rows; i++)
+        for (int j = a->rowStart[i]; j < a->rowStart[i + 1]; j++)
+            if (a->col[j] == i)
+            {
+                const double d = fabs(a->val[j]);
+                lo = d < lo ? d : lo;
+                hi = d > hi ? d : hi;
+            }
+    return lo > 0 && lo < 1e300 ? hi / lo : 1.0;
+}
+
+int orc_cheb_iters(const orc_csr *a, double lo, double hi, double relTol, int maxIters)
+{
+    const double kappa = hi / lo, rho = (sqrt(kappa) - 1.0) / (sqrt(kappa) + 1.0);
+    int k = (int)ceil(log(relTol / (2.0 * sqrt(diag_ratio(a)))) / log(rho));
+    if (k < 1)
+        k = 1;
+    return k < maxIters ? k : maxIters;
+}
+
+int orc_cheb_solve(const orc_csr *a, const double *b, double *x, double lo, double hi, int iters,
+                   double relTol, double *relRes)
+{
+    const int n = a->rows;
+    double *invD = (double *)malloc(sizeof(double) * n), *r = (double *)malloc(sizeof(double) * n);
+    double *d = (double *)malloc(sizeof(double) * n), *q = (double *)malloc(sizeof(double) * n);
+    for (int i = 0; i < n; i++)
+    {
+        invD[i] = 0;
+        for (int j = a->rowStart[i]; j < a->rowStart[i + 1]; j++)
+            if (a->col[j] == i)
+                invD[i] = 1.0 / a->val[j];
+    }
+    const double theta = 0.5 * (hi + lo), delta = 0.5 * (hi - lo), sigma = theta / delta;
+    double rho = 1.0 / sigma;
+#pragma omp parallel for schedule(static)
+    for (int i = 0; i < n; i++)
+    {
+        x[i] = 0;
+        r[i] = b[i];
+        d[i] = b[i] * invD[i] / theta;
+    }
+    for (int k = 0; k < iters; k++)
+    {
+        const double rhoN = 1.0 / (2.0 * sigma - rho), c1 = rhoN * rho, c2 = 2.0 * rhoN / delta;
+        orc_spmv(a, d, q);
+#pragma omp parallel for schedule(static)
+        for (int i = 0; i < n; i++)
+        {
+            x[i] += d[i];
+            r[i] -= q[i];
+            d[i] = c1 * d[i] + c2 * r[i] * invD[i];
+        }
+        rho = rhoN;
+    }
+    /* true residual of the result */
+    orc_spmv(a, x, q);
+    const double bb = dot(b, b, n);
+    double rr = 0;
+    for (int i = 0; i < n; i++)
+        rr += (b[i] - q[i]) * (b[i] - q[i]);
+    *relRes = bb > 0 ? sqrt(rr / bb) : sqrt(rr);
+    free(invD);
+    free(r);
+    free(d);
+    free(q);
+    if (!isfinite(rr))
+        return 2;
+    return rr <= relTol * relTol * bb ? 0 : 3;
+}

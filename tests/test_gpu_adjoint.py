@@ -53,12 +53,14 @@ def _start(rng, n_nodes):
     return u0
 
 
-@pytest.mark.parametrize("precision,vel_method", [("f64", 1), ("mixedsolve", 1), ("f64", 2), ("mixedsolve", 2)])
+@pytest.mark.parametrize("precision,vel_method", [("f64", 1), ("mixedsolve", 1), ("f64", 2), ("mixedsolve", 2),
+                                                  ("f64", 3), ("mixedsolve", 3)])
 def test_adjoint_matches_oracle_adjoint(adj_setup, precision, vel_method):
     """Drag and lift weights on every step, a random initial velocity and perturbed inflow values.
     mixedsolve: FP64 operators with FP32-inner solves refined to the same FP64 tolerance, in the
-    forward step and in the adjoint solves.  vel_method 2: Jacobi-preconditioned mass solves (the
-    discrete step is the same; only the solver differs, within the tolerance)."""
+    forward step and in the adjoint solves.  vel_method 2: Jacobi-preconditioned mass solves, 3:
+    Chebyshev-Jacobi mass solves (the discrete step is the same; only the solver differs, within
+    the tolerance)."""
     G, O, mesh, ctx, om, oc = adj_setup
     rng = np.random.default_rng(11)
     n = 12

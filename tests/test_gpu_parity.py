@@ -350,6 +350,29 @@ def test_chorin_jacobi_mass_matches_oracle(setup, torch_cuda, path, precision, m
     assert s["status"] == 0 and s["tent_rel"] <= 1e-10 and s["final_rel"] <= 1e-10
 
 
+@pytest.mark.parametrize("graph", [True, False])
+@pytest.mark.parametrize("precision", ["f64", "mixed", "mixedsolve"])
+def test_chorin_chebyshev_mass_matches_oracle(setup, torch_cuda, precision, graph):
+    """velMethod 3: the mass solves as Chebyshev-Jacobi with the a priori iteration count.  The
+    count equals the oracle's (orc_cheb_iters), and both solves meet the tolerance on the true
+    residual; FP64 and mixed-solve fields within 1e-7 of the oracle's Chebyshev step after 5 steps,
+    mixed within the mixed bounds (u 1e-5, p 2e-4)."""
+    G, O, mesh, ctx, om, oc = setup
+    prec = {"f64": G.NSF_PREC_F64, "mixed": G.NSF_PREC_MIXED, "mixedsolve": G.NSF_PREC_F64_MIXEDSOLVE}[precision]
+    st = G.ChorinStepper(ctx, 1e-3, 1e-3, precision=prec, vel_method=3, vel_max_iters=300, vel_tol=1e-10,
+                         pres_max_iters=3000, pres_tol=1e-10, use_graph=graph)
+    st.step(5)
+    u, p = st.state()
+    uo, po = _oracle_steps(O, oc, 1e-3, 1e-3, 5, vel_method=3)
+    tu, tp = (1e-5, 2e-4) if precision == "mixed" else (1e-7, 1e-7)
+    assert _rel(u, uo) <= tu
+    assert _rel(p, po) <= tp
+    s = st.stats()
+    k = O.cheb_iters(oc.M, 1e-10)
+    assert s["tent_iters"] == k and s["final_iters"] == k
+    assert s["status"] == 0 and s["tent_rel"] <= 1e-10 and s["final_rel"] <= 1e-10
+
+
 @pytest.mark.parametrize("precision", ["f64", "mixed"])
 def test_chorin_extrapolated_pressure_guess_matches_oracle(setup, torch_cuda, precision):
     """pressure_guess 1 (the pressure solve starts from 2 p(n-1) - p(n-2)): the FP64 stepper follows

@@ -298,3 +298,88 @@ def test_oracle_adjoint_matches_finite_differences(oracle_lib, channel_coarse):
     g = float(d @ gu)
     assert abs(fd - g) <= 1e-6 * abs(g)
     assert np.all(gu[ctx.dir_ids] == 0) and np.all(gu[ctx.N + ctx.dir_ids] == 0)
+
+
+def _p2_element_mass():
+    """P2 element mass matrix on one triangle (unit area): basis lambda_i (2 lambda_i - 1) at the
+    vertices and 4 lambda_i lambda_j at the edge midpoints, integrated exactly with
+    int lambda1^a lambda2^b lambda3^c dA = 2 |T| a! b! c! / (a + b + c + 2)!."""
+    from math import factorial
+
+    def mul(p, q):
+        out = {}
+        for ka, va in p.items():
+            for kb, vb in q.items():
+                k = tuple(x + y for x, y in zip(ka, kb))
+                out[k] = out.get(k, 0.0) + va * vb
+        return out
+
+    def integrate(p):
+        return sum(v * 2.0 * factorial(a) * factorial(b) * factorial(c) / factorial(a + b + c + 2)
+                   for (a, b, c), v in p.items())
+
+    e = [(1, 0, 0), (0, 1, 0), (0, 0, 1)]
+    basis = []
+    for i in range(3):
+        basis.append({tuple(2 * x for x in e[i]): 2.0, e[i]: -1.0})
+    for i, j in ((0, 1), (1, 2), (2, 0)):
+        basis.append({tuple(x + y for x, y in zip(e[i], e[j])): 4.0})
+    return np.array([[integrate(mul(p, q)) for q in basis] for p in basis])
+
+
+def test_chebyshev_mass_bounds(oracle_lib, channel_coarse):
+    """The Chebyshev mass solve (velocity method 3) relies on spec(D^-1 M) lying in
+    [MASS_SPEC_LO, MASS_SPEC_HI] on every mesh: the element pair (M_e, diag M_e) has those extreme
+    generalized eigenvalues (the same for every affine triangle), and the assembled spectrum
+    lies inside them."""
+    import scipy.linalg as sla
+    O = oracle_lib
+    Me = _p2_element_mass()
+    assert abs(Me.sum() - 1.0) < 1e-14
+    ev = sla.eigh(Me, np.diag(np.diag(Me)), eigvals_only=True)
+    assert O.MASS_SPEC_LO <= ev.min() < O.MASS_SPEC_LO + 1e-5
+    assert O.MASS_SPEC_HI - 1e-5 < ev.max() <= O.MASS_SPEC_HI
+    m = O.Mesh(channel_coarse)
+    ctx = O.Context(m, 1.2, True)
+    Md = ctx.M.to_scipy().toarray()
+    d = np.diag(Md)
+    g = sla.eigh(Md, np.diag(d), eigvals_only=True)
+    assert O.MASS_SPEC_LO <= g.min() and g.max() <= O.MASS_SPEC_HI
+
+
+def test_chebyshev_mass_solve(oracle_lib, channel_coarse):
+    """The a priori count reaches the tolerance (true residual), and the solution matches a
+    direct solve."""
+    import scipy.sparse.linalg as spla
+    O = oracle_lib
+    m = O.Mesh(channel_coarse)
+    ctx = O.Context(m, 1.2, True)
+    rng = np.random.default_rng(3)
+    b = rng.standard_normal(ctx.N)
+    ref = spla.spsolve(ctx.M.to_scipy().tocsc(), b)
+    for tol in (1e-6, 1e-10, 1e-13):
+        k = O.cheb_iters(ctx.M, tol)
+        x, st, rel = O.cheb_solve(ctx.M, b, k, tol)
+        assert st == 0 and rel <= tol, (tol, k, rel)
+        assert np.max(np.abs(x - ref)) <= 50 * tol * np.max(np.abs(ref))
+    # fewer iterations than the count miss tight tolerances
+    k = O.cheb_iters(ctx.M, 1e-10)
+    _, st, rel = O.cheb_solve(ctx.M, b, k // 2, 1e-10)
+    assert st == 3 and rel > 1e-10
+
+
+def test_chebyshev_chorin_matches_pcg(oracle_lib, channel_coarse):
+    """Chorin steps with the Chebyshev mass solve agree with the PCG ones at tight tolerances."""
+    O = oracle_lib
+    m = O.Mesh(channel_coarse)
+    ctx = O.Context(m, 1.2, True)
+    a = O.Chorin(ctx, 1e-3, 1e-3, vel_method=1, vel_tol=1e-12, pres_tol=1e-12)
+    b = O.Chorin(ctx, 1e-3, 1e-3, vel_method=3, vel_tol=1e-12, pres_tol=1e-12)
+    for _ in range(5):
+        a.step()
+        st = b.step()
+        assert st[0] == O.cheb_iters(ctx.M, 1e-12)
+    ua, pa = a.state()
+    ub, pb = b.state()
+    assert np.max(np.abs(ua - ub)) <= 1e-9 * np.max(np.abs(ua))
+    assert np.max(np.abs(pa - pb)) <= 1e-8 * np.max(np.abs(pa))
