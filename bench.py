@@ -48,6 +48,8 @@ def peaks():
     return 6800.0, "fallback"
 
 
+PRESSURE_GUESSES = {0: "previous solution", 1: "2 p(n-1) - p(n-2)",
+                    2: "projection onto <= {} earlier solutions, Kp_int-orthonormal (Fischer 1998)"}
 MASS_SOLVES = {1: "PCG, multicolor SGS", 2: "PCG, Jacobi", 3: "Chebyshev, Jacobi (a priori iteration count)"}
 
 
@@ -104,26 +106,39 @@ class Clocks:
         return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def run_cpu_reference(mesh_path: str, steps: int, warmup: int, vel_method: int = 1, pres_guess: int = 0):
+def run_cpu_reference(mesh_path: str, steps: int, warmup: int, vel_method: int = 1, pres_guess: int = 0,
+                      pres_basis: int = 0, snapshot_step: int = 0):
     """Time the oracle's FP64 Chorin step (the CPU restatement of the reference path) on every host
-    thread (its OpenMP build; the single-thread build if that cannot be compiled).  The thread
-    count is left in CPU_THREADS."""
+    thread (its OpenMP build; the single-thread build if that cannot be compiled): `warmup` steps
+    from rest, then `steps` timed ones.  The thread count is left in CPU_THREADS.  Returns steps/s,
+    the timed seconds, the context and (u, p, forces) after `snapshot_step` steps in all (taken
+    outside the timing; the final state if 0)."""
     global CPU_THREADS
     import oracle
     oracle.build()
     m = oracle.Mesh(mesh_path)
     ctx = oracle.Context(m, PEAK, True)
     ch = oracle.Chorin(ctx, NU, TAU, vel_method=vel_method, vel_max_iters=500, vel_tol=VEL_TOL, pres_max_iters=5000,
-                       pres_tol=PRES_TOL, mt=True, pres_guess=pres_guess)
+                       pres_tol=PRES_TOL, mt=True, pres_guess=pres_guess, pres_basis=pres_basis)
     CPU_THREADS = ch.threads
-    for _ in range(warmup):
+    snap = None
+
+    def take():
+        u, p = ch.state()
+        return u, p, oracle.forces(m, u, p, NU)
+
+    for k in range(warmup):
         ch.step()
-    t0 = time.perf_counter()
-    for _ in range(steps):
+        if k + 1 == snapshot_step:
+            snap = take()
+    dt = 0.0
+    for k in range(steps):
+        t0 = time.perf_counter()
         ch.step()
-    dt = time.perf_counter() - t0
-    u, p = ch.state()
-    return steps / dt, dt, ctx, (u, p, oracle.forces(m, u, p, NU))
+        dt += time.perf_counter() - t0
+        if warmup + k + 1 == snapshot_step:
+            snap = take()
+    return steps / dt, dt, ctx, snap if snap is not None else take()
 
 
 CPU_THREADS = 1                    # host threads of the last CPU-oracle timing
@@ -133,22 +148,27 @@ ACC_CHECKPOINTS = (4, 25, 50, 100)  # steps at which the fields are compared
 
 def accuracy_run(G, ctx, mesh, stepper, torch, stream):
     """Mixed-precision and FP64 steppers from rest for ACC_STEPS steps: relative L2 field
-    differences at the checkpoints and the drag/lift time series (both on the device, FP64)."""
+    differences at the checkpoints, the drag/lift time series (both on the device, FP64) and the
+    pressure-solve iterations of every step."""
     sp = stream.cuda_stream
     runs = {}
+    iters = {}
     for name, prec in (("fp64", G.NSF_PREC_F64), ("mixed", G.NSF_PREC_MIXED)):
         st = stepper(prec)
         fn = G.Forces(mesh, st)
         F = torch.zeros((ACC_STEPS, 2), dtype=torch.float64, device="cuda")
         states = {}
+        its = []
         with torch.cuda.stream(stream):
             for k in range(ACC_STEPS):
                 st.step(1, sp)
                 fn.into(F[k], sp)
+                its.append(int(st.stats()["pres_iters"]))
                 if k + 1 in ACC_CHECKPOINTS:
                     states[k + 1] = st.state()
         torch.cuda.synchronize()
         runs[name] = (F.cpu().numpy(), states)
+        iters[name] = its
         del fn, st
 
     def rel(a, b):
@@ -169,6 +189,9 @@ def accuracy_run(G, ctx, mesh, stepper, torch, stream):
                                                             np.abs(F64[:, 0]).max()),
         "c_drag_fp64_last": float(cscale * F64[-1, 0]),
         "c_lift_fp64_last": float(cscale * F64[-1, 1]),
+        "pressure_iterations": {k: {"mean": round(float(np.mean(v)), 1), "max": int(np.max(v)),
+                                    "mean_last_50": round(float(np.mean(v[-50:])), 1), "last_10": v[-10:]}
+                                for k, v in iters.items()},
     }
     return out, (S64[4][0], S64[4][1], F64[3])
 
@@ -433,7 +456,8 @@ def bench_batch(args):
             steppers.append(G.ChorinStepper(ctx, float(nus[b]), tau, precision=G.NSF_PREC_MIXED, vel_method=args.vel_method,
                                             vel_max_iters=500, vel_tol=VEL_TOL, pres_max_iters=5000,
                                             pres_tol=PRES_TOL, check_interval=8, use_graph=True, max_outer=4,
-                                            inner_tol=1e-5))
+                                            inner_tol=1e-5, pressure_guess=args.pressure_guess,
+                                            pressure_basis=args.pressure_basis))
         setup_s = time.perf_counter() - t0
         streams = [torch.cuda.Stream() for _ in range(B)]
         for st, s in zip(steppers, streams):
@@ -495,6 +519,7 @@ def bench_batch(args):
         "config": {"workload": f"{B} instances, h=0.01, U_max~U[0.2,1.5], nu~logU[5e-4,2e-3], tau=2e-4, "
                                "pressure to 1e-8 rel", "instances": B, "setup_s": round(setup_s, 1),
                    "mass_solve": MASS_SOLVES[args.vel_method],
+                   "pressure_guess": PRESSURE_GUESSES[args.pressure_guess].format(args.pressure_basis or 60),
                    "execution": "one graph-captured stepper per instance on its own stream, cluster-resident solves"},
         "one_instance_steps_per_s": round(one, 2),
         "speedup_vs_one_at_a_time": round(agg / one, 2),
@@ -541,7 +566,8 @@ def bench_pack(args):
                 steppers.append(G.ChorinStepper(ctx, nu, tau, precision=G.NSF_PREC_MIXED, vel_method=args.vel_method,
                                                 vel_max_iters=500, vel_tol=VEL_TOL, pres_max_iters=5000,
                                                 pres_tol=PRES_TOL, check_interval=8, use_graph=True, max_outer=4,
-                                                inner_tol=1e-5))
+                                                inner_tol=1e-5, pressure_guess=args.pressure_guess,
+                                                pressure_basis=args.pressure_basis))
         setup_s = time.perf_counter() - t0
         stream = torch.cuda.Stream()
         pack = G.Pack(steppers)
@@ -590,6 +616,7 @@ def bench_pack(args):
         "config": {"workload": f"{per} instances on each of h={hs}, U_max~U[0.2,1.5], nu~logU[5e-4,2e-3], "
                                f"tau={tau}, pressure to 1e-8 rel", "instances": n,
                    "mass_solve": MASS_SOLVES[args.vel_method],
+                   "pressure_guess": PRESSURE_GUESSES[args.pressure_guess].format(args.pressure_basis or 60),
                    "mesh_sizes_N_P": {str(h): sizes[h] for h in hs}, "setup_s": round(setup_s, 1),
                    "execution": "one CUDA graph per step whose branches are the 48 instances' steps (nsf_pack); "
                                 "cluster-resident solves"},
@@ -621,7 +648,8 @@ def bench_long(args):
         def stepper(prec):
             return G.ChorinStepper(ctx, NU, TAU, precision=prec, vel_method=args.vel_method, vel_max_iters=500, vel_tol=VEL_TOL,
                                    pres_max_iters=5000, pres_tol=PRES_TOL, check_interval=8, use_graph=True,
-                                   max_outer=4, inner_tol=1e-5, pressure_guess=1)
+                                   max_outer=4, inner_tol=1e-5, pressure_guess=args.pressure_guess,
+                                   pressure_basis=args.pressure_basis)
 
         steppers = {"mixed": stepper(G.NSF_PREC_MIXED), "fp64": stepper(G.NSF_PREC_F64)}
         forces = {k: G.Forces(mesh, s) for k, s in steppers.items()}
@@ -660,7 +688,8 @@ def bench_long(args):
         "data": "synthetic (seeded DFG channel mesh, h=0.005)",
         "config": {"workload": f"DFG channel h={H}, Umax=1.5, nu={NU}, tau={TAU}, {n} steps from rest, pressure "
                                f"to {PRES_TOL} rel", "N": ctx.N, "P": ctx.P,
-                   "mass_solve": MASS_SOLVES[args.vel_method]},
+                   "mass_solve": MASS_SOLVES[args.vel_method],
+                   "pressure_guess": PRESSURE_GUESSES[args.pressure_guess].format(args.pressure_basis or 60)},
         "fp64_steps_per_s": round(n / secs["fp64"], 2),
         "field_rel_l2_mixed_vs_fp64": field,
         "drag_max_rel_err": float(np.abs(sm[:, 0] - sf[:, 0]).max() / fmax),
@@ -800,7 +829,8 @@ def bench_ours(args, rank, world, local_rank):
         def stepper(precision, graph=True):
             return G.ChorinStepper(ctx, NU, TAU, precision=precision, vel_method=args.vel_method, vel_max_iters=500,
                                    vel_tol=VEL_TOL, pres_max_iters=5000, pres_tol=PRES_TOL, check_interval=8,
-                                   use_graph=graph, max_outer=4, inner_tol=1e-5, pressure_guess=args.pressure_guess)
+                                   use_graph=graph, max_outer=4, inner_tol=1e-5, pressure_guess=args.pressure_guess,
+                                   pressure_basis=args.pressure_basis)
 
         stream = torch.cuda.Stream()
         sp = stream.cuda_stream
@@ -846,7 +876,7 @@ def bench_ours(args, rank, world, local_rank):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         for _ in range(e2e_steps):
-            mixed.set_state(u_h, p_h)
+            mixed.set_state(u_h, p_h, keep_history=True)  # the state continues the run
             mixed.step(1, sp)
             mixed.get_state_into(u_h, p_h)
         t_e2e = time.perf_counter() - t0
@@ -939,9 +969,12 @@ def bench_ours(args, rank, world, local_rank):
                        "l2": "working set > L2 (FastConvection matrix %.0f MB FP32)" % (nnzI * 8 / 1e6),
                        "graph": True, "setup_s": round(setup_s, 2),
                        "mass_solve": MASS_SOLVES[args.vel_method],
-                       "pressure_guess": {0: "previous solution", 1: "2 p(n-1) - p(n-2)"}[args.pressure_guess]},
+                       "pressure_guess": PRESSURE_GUESSES[args.pressure_guess].format(args.pressure_basis or 60)},
             "e2e": {"value": round(world * e2e_steps / t_e2e, 3), "unit": "steps/s",
-                    "h2d_bytes_per_step": (2 * N + P) * 8, "d2h_bytes_per_step": (2 * N + P) * 8},
+                    "h2d_bytes_per_step": (2 * N + P) * 8, "d2h_bytes_per_step": (2 * N + P) * 8,
+                    "path": "per step: set_state (u, p from pinned host memory, renumbered on the device; "
+                            "the run's pressure-guess history kept), one graph-launched step, get_state "
+                            "(u, p to pinned host memory)"},
             "gpu_launches": int(launches),
             "roofline": {"bound": "hbm", "kernel": "kPcgClusterDs<float,1> (pressure PCG, FP32 inner solve)",
                          "achieved": round(achieved_pcg, 1), "peak": hbm, "unit": "GB/s",
@@ -976,7 +1009,9 @@ def main():
     ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--cpu-sample-steps", type=int, default=3)
+    ap.add_argument("--cpu-sample-steps", type=int, default=-1,
+                    help="CPU baseline of the channel workload: -1 the timed GPU window (--warmup steps from "
+                         "rest, then --steps timed), k > 0 the first k steps after one warm-up, 0 none")
     ap.add_argument("--no-accuracy", dest="accuracy", action="store_false",
                     help="skip the untimed mixed-vs-FP64 field and drag/lift comparison")
     ap.add_argument("--workload", default="channel", choices=["channel", "poisson", "small", "batch", "pack", "adjoint", "long"],
@@ -986,8 +1021,11 @@ def main():
     ap.add_argument("--vel-method", type=int, default=3, choices=[1, 2, 3],
                     help="channel, batch, pack and long workloads: mass solve, 1 PCG multicolor SGS, 2 PCG "
                          "Jacobi, 3 Chebyshev Jacobi")
-    ap.add_argument("--pressure-guess", type=int, default=1, choices=[0, 1],
-                    help="channel workload: pressure initial guess, 0 previous solution, 1 extrapolated")
+    ap.add_argument("--pressure-basis", type=int, default=0,
+                    help="pressure guess 2: basis vectors (3..64; 0: 60)")
+    ap.add_argument("--pressure-guess", type=int, default=2, choices=[0, 1, 2],
+                    help="channel, batch, pack and long workloads: pressure initial guess, 0 previous "
+                         "solution, 1 extrapolated, 2 projected onto earlier solutions")
     ap.add_argument("--adjoint-steps", type=int, default=1000)
     ap.add_argument("--adjoint-checkpoint", type=int, default=50)
     ap.add_argument("--adjoint-precision", default="mixedsolve", choices=["f64", "mixedsolve"])
@@ -1058,19 +1096,21 @@ def main():
         tmp = tempfile.mkdtemp()
         try:
             path = make_mesh(tmp, H, 0)
-            k = max(1, min(args.steps, 10))
-            sps, dt, ctx, _ = run_cpu_reference(path, k, min(args.warmup, 2))
+            k, w = max(1, min(args.steps, 400)), args.warmup
+            sps, dt, ctx, _ = run_cpu_reference(path, k, w)
         finally:
             shutil.rmtree(tmp, ignore_errors=True)
         line = {"impl": "reference", "metric": METRIC, "value": round(sps, 4), "unit": "steps/s", "n_gpus": 0,
-                "steps": k, "warmup": min(args.warmup, 2), "ms_per_step": round(1e3 * dt / k, 2),
+                "steps": k, "warmup": w, "ms_per_step": round(1e3 * dt / k, 2),
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
                 "data": "synthetic (seeded DFG channel mesh, h=0.005)",
                 "config": {"workload": "DFG channel h=0.005, Umax=1.5, nu=1e-3, tau=1e-4, P2/P1, "
                                        "pressure PCG-SGS to 1e-8 rel", "N": ctx.N, "P": ctx.P},
                 "cpu_baseline": {"value": round(sps, 4), "unit": "steps/s", "cores": CPU_THREADS, "kind": "port",
-                                 "sample": f"{k} time steps after {min(args.warmup, 2)} warm-up steps, FP64 C oracle "
-                                           f"on {CPU_THREADS} host threads"},
+                                 "sample": f"time steps {w + 1}..{w + k} from rest (after {w} warm-up steps), the "
+                                           f"reference's algorithm (mass and pressure PCG with the multicolor SGS "
+                                           f"preconditioner, previous-solution pressure guess), FP64 C oracle on "
+                                           f"{CPU_THREADS} host threads"},
                 "e2e": {"value": round(sps, 4), "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
         print(json.dumps(line))
         return
@@ -1082,16 +1122,19 @@ def main():
     if rank == 0 and line is not None:
         f64_step4 = line.pop("_f64_step4", None)
         # CPU baseline on a bounded sample of the same workload (rank 0, N = 1 only)
-        if world == 1 and args.cpu_sample_steps > 0:
+        if world == 1 and args.cpu_sample_steps != 0:
+            cw, ck = (args.warmup, args.steps) if args.cpu_sample_steps < 0 else (1, args.cpu_sample_steps)
             tmp = tempfile.mkdtemp()
             try:
                 path = make_mesh(tmp, H, 0)
-                sps, dt, _, (uo, po, fo) = run_cpu_reference(path, args.cpu_sample_steps, 1, args.vel_method,
-                                                             args.pressure_guess)
+                sps, dt, _, snap = run_cpu_reference(path, ck, cw, args.vel_method, args.pressure_guess,
+                                                     args.pressure_basis, snapshot_step=4)
+                uo, po, fo = snap
                 line["cpu_baseline"] = {"value": round(sps, 4), "unit": "steps/s", "cores": CPU_THREADS, "kind": "port",
-                                        "sample": f"{args.cpu_sample_steps} time steps (after 1 warm-up) of the same "
-                                                  f"workload, FP64 C oracle on {CPU_THREADS} host threads (OpenMP)"}
-                if f64_step4 is not None and args.cpu_sample_steps == 3:
+                                        "sample": f"time steps {cw + 1}..{cw + ck} from rest (after {cw} warm-up "
+                                                  f"steps) of the same workload and algorithm, FP64 C oracle on "
+                                                  f"{CPU_THREADS} host threads (OpenMP)"}
+                if f64_step4 is not None and cw + ck >= 4:
                     # the oracle has run 4 steps from rest: the FP64 GPU state after 4 steps vs it
                     import numpy as np
                     ug, pg, fg = f64_step4

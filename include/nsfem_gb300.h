@@ -190,8 +190,13 @@ typedef struct
     double innerTol;      /* mixed precision: relative tolerance of each FP32 inner solve */
     int pressureGuess;    /* initial guess of the pressure solve: 0 the previous solution (as the
                              reference's solver keeps it), 1 the linear extrapolation
-                             2 p(n-1) - p(n-2) from the last two solutions (no reference
-                             counterpart; fewer iterations, the same tolerance) */
+                             2 p(n-1) - p(n-2) from the last two solutions, 2 the projection of
+                             the new solution onto up to pressureBasis earlier solutions,
+                             orthonormal in the Kp_int inner product (Fischer 1998: x0 = sum_k
+                             (x_k . b) x_k; each solve's correction joins the basis; a full basis
+                             restarts from the solution and its last two differences).  1 and 2
+                             have no reference counterpart: fewer iterations, the same tolerance */
+    int pressureBasis;    /* pressureGuess 2: basis vectors, 3..64 (0: 60) */
 } nsf_chorin_config;
 
 typedef struct nsf_chorin_s *nsf_chorin;
@@ -210,6 +215,12 @@ int nsf_chorin_launch(nsf_chorin s, int nSteps, void *stream);
 /* copy the state to/from host memory in the original numbering: u[2N] planar, p[P] */
 int nsf_chorin_get_state(nsf_chorin s, double *u, double *p, void *stream);
 int nsf_chorin_set_state(nsf_chorin s, const double *u, const double *p, void *stream);
+/* nsf_chorin_set_state with flags.  NSF_STATE_KEEP_HISTORY: the state continues the stepper's run
+   (a host that reads the state, and writes it back, every step), so the pressure-guess history
+   (pressureGuess 1 and 2: the earlier solutions) is kept; nsf_chorin_set_state starts a new one.
+   The history only shapes the initial guess: the solves reach the same tolerance either way. */
+#define NSF_STATE_KEEP_HISTORY 1
+int nsf_chorin_set_state_ex(nsf_chorin s, const double *u, const double *p, int flags, void *stream);
 /* stats[0..7] of the last step: tentative iterations, pressure iterations, final iterations,
    pressure relative residual, tentative relative residual, final relative residual,
    pressure refinement sweeps (mixed), status */

@@ -34,7 +34,8 @@ class ChorinConfig(C.Structure):
     _fields_ = [("nu", C.c_double), ("tau", C.c_double), ("precision", C.c_int), ("velMethod", C.c_int),
                 ("velMaxIters", C.c_int), ("velTol", C.c_double), ("presMaxIters", C.c_int),
                 ("presTol", C.c_double), ("checkInterval", C.c_int), ("useGraph", C.c_int),
-                ("maxOuter", C.c_int), ("innerTol", C.c_double), ("pressureGuess", C.c_int)]
+                ("maxOuter", C.c_int), ("innerTol", C.c_double), ("pressureGuess", C.c_int),
+                ("pressureBasis", C.c_int)]
 
 
 class AdjointConfig(C.Structure):
@@ -76,6 +77,7 @@ _SIGS = {
     "nsf_chorin_launch": (C.c_int, [vp, C.c_int, vp]),
     "nsf_chorin_get_state": (C.c_int, [vp, f64p, f64p, vp]),
     "nsf_chorin_set_state": (C.c_int, [vp, f64p, f64p, vp]),
+    "nsf_chorin_set_state_ex": (C.c_int, [vp, f64p, f64p, C.c_int, vp]),
     "nsf_chorin_stats": (C.c_int, [vp, f64p]),
     "nsf_kernel_launches": (C.c_longlong, []),
     "nsf_chorin_destroy": (None, [vp]),

@@ -336,12 +336,15 @@ class ChorinStepper:
     def __init__(self, ctx: ChorinContext, nu: float, tau: float, precision: int = NSF_PREC_F64,
                  vel_method: int = 1, vel_max_iters: int = 200, vel_tol: float = 1e-10,
                  pres_max_iters: int = 2000, pres_tol: float = 1e-10, check_interval: int = 8,
-                 use_graph: bool = True, max_outer: int = 4, inner_tol: float = 1e-4, pressure_guess: int = 0):
+                 use_graph: bool = True, max_outer: int = 4, inner_tol: float = 1e-4, pressure_guess: int = 0,
+                 pressure_basis: int = 0):
         """vel_method: mass solve, 0 multicolor GS, 1 PCG-SGS, 2 PCG-Jacobi, 3 Chebyshev-Jacobi.
-        pressure_guess: 0 the previous pressure (as the reference), 1 extrapolated from the last two."""
+        pressure_guess: 0 the previous pressure (as the reference), 1 extrapolated from the last two,
+        2 projected onto up to pressure_basis earlier solutions (0: 60)."""
         self.ctx = ctx
         self.cfg = ChorinConfig(nu, tau, precision, vel_method, vel_max_iters, vel_tol, pres_max_iters, pres_tol,
-                                check_interval, int(use_graph), max_outer, inner_tol, int(pressure_guess))
+                                check_interval, int(use_graph), max_outer, inner_tol, int(pressure_guess),
+                                int(pressure_basis))
         h = vp()
         check(lib().nsf_chorin_create(ctx._h, C.byref(self.cfg), C.byref(h)))
         self._h = h
@@ -364,10 +367,13 @@ class ChorinStepper:
     def get_state_into(self, u: np.ndarray, p: np.ndarray):
         check(lib().nsf_chorin_get_state(self._h, _p(u, C.c_double), _p(p, C.c_double), None))
 
-    def set_state(self, u, p):
+    def set_state(self, u, p, keep_history: bool = False):
+        """keep_history: the state continues this stepper's run, so the pressure-guess history is
+        kept (otherwise a new one starts); only the initial guesses differ."""
         u = np.ascontiguousarray(u, np.float64)
         p = np.ascontiguousarray(p, np.float64)
-        check(lib().nsf_chorin_set_state(self._h, _p(u, C.c_double), _p(p, C.c_double), None))
+        check(lib().nsf_chorin_set_state_ex(self._h, _p(u, C.c_double), _p(p, C.c_double),
+                                            1 if keep_history else 0, None))
 
     def set_dirichlet(self, dir_vx, stream=None):
         """Replace the x values of the Dirichlet velocity nodes (ctx.dir_ids order) and impose them

@@ -490,7 +490,8 @@ extern "C" int nsf_adjoint_create(nsf_chorin S, nsf_forces f, const nsf_adjoint_
         require(S && f && out, "null argument");
         require(f->s == S, "the force functional belongs to another stepper");
         require(!S->mixed, "the adjoint needs FP64 operators (precision NSF_PREC_F64 or NSF_PREC_F64_MIXEDSOLVE)");
-        require(!S->extrapolate, "the adjoint's checkpoints hold (u, p) only: create the stepper with pressureGuess 0");
+        require(!S->extrapolate && !S->project,
+                "the adjoint's checkpoints hold (u, p) only: create the stepper with pressureGuess 0");
         auto a = std::make_unique<nsf_adjoint_s>();
         if (cfg)
             a->cfg = *cfg;

@@ -2,6 +2,7 @@
 // device-resident Chorin stepper.  See include/nsfem_gb300.h for the contract of each call.
 #include "../../include/nsfem_gb300.h"
 
+#include "projection.cuh"
 #include "solvers.cuh"
 
 #include <algorithm>
@@ -852,6 +853,9 @@ struct nsf_chorin_s
     bool extrapolate = false;
     DevBuf<double> pPrev;
     DevBuf<int> pHist;
+    // pressure initial guess projected onto earlier solutions (cfg.pressureGuess == 2)
+    bool project = false;
+    PressureProjection proj;
     // state copies: device staging (original numbering) and the renumbering maps
     DevBuf<double> stateStage;
     DevBuf<int> permVDev, pIdxDev;
@@ -928,7 +932,9 @@ struct nsf_chorin_s
             const DevSell<float> & IS = I32.sell;
             NSF_LAUNCH((kFastConvSell<float, double, float, float>), IS.blocks(), s, IS.rows, IS.nSlices, IS.ss.get(),
                        IS.perm.get(), IS.ci.get(), IS.v.get(), u.get(), K32.get(), (float)cfg.nu, A32.get());
-            NSF_LANES(M32.L, NSF_LAUNCH((kSpmm<float, double, double, float, LL, 2>), blocksFor((long long)N * M32.L), s, N,
+            // FP32 values, FP64 sums (4.6M FMAs): FP32 sums would put step-to-step rounding noise into
+            // u, which the divergence amplifies in the pressure right-hand side
+            NSF_LANES(M32.L, NSF_LAUNCH((kSpmm<float, double, double, double, LL, 2>), blocksFor((long long)N * M32.L), s, N,
                                         M32.rsF.get(), M32.ciF.get(), A32.get(), u.get(), N, rhs.get(), N));
         }
         else
@@ -952,14 +958,21 @@ struct nsf_chorin_s
         }
         if (mixed)
         {
-            sellSpmv<float>(D32.sell, u.get(), rhsP.get(), invTau, 0.0, s);
+            // FP32 values, FP64 sums: D u cancels heavily, and FP32 sums would leave rounding noise of
+            // ~1e-5 of the result in rhsP that changes from step to step, which the pressure solve
+            // then has to remove to its tolerance (no initial guess can predict it)
+            sellSpmv<double>(D32.sell, u.get(), rhsP.get(), invTau, 0.0, s);
+            if (project)
+                proj.guess(s, rhsP.get(), pInt.get());
             mpres.enqueue(s, body, rhsP.get(), pInt.get(), cfg.maxOuter, cfg.presTol, cfg.presMaxIters, cfg.innerTol,
                           cfg.checkInterval);
-            sellSpmv<float>(G32.sell, pInt.get(), rhs.get(), 1.0, 0.0, s);
+            sellSpmv<double>(G32.sell, pInt.get(), rhs.get(), 1.0, 0.0, s);
         }
         else
         {
             sellSpmv<double>(D64.sell, u.get(), rhsP.get(), invTau, 0.0, s);
+            if (project)
+                proj.guess(s, rhsP.get(), pInt.get());
             if (mixedSolve)
                 mpres.enqueue(s, body, rhsP.get(), pInt.get(), cfg.maxOuter, cfg.presTol, cfg.presMaxIters,
                               cfg.innerTol, cfg.checkInterval);
@@ -968,6 +981,8 @@ struct nsf_chorin_s
                              cfg.checkInterval);
             sellSpmv<double>(G64.sell, pInt.get(), rhs.get(), 1.0, 0.0, s);
         }
+        if (project)
+            proj.update(s, pInt.get());
         // 4. M acc = G p ; u = u - tau acc ; Dirichlet
         enqueueMassSolve(s, false);
         NSF_LAUNCH(kUpdateVelocity<double>, blocksFor(N), s, N, u.get(), acc.get(), cfg.tau, isDir.get(),
@@ -1166,6 +1181,9 @@ static void buildChorin(nsf_chorin_s & S, const Context & c)
             u0[r] = dval[r];
     S.u.upload(u0);
     S.pInt.alloc(S.nIntP);
+    S.project = S.cfg.pressureGuess == 2;
+    if (S.project)
+        S.proj.setup(&S.Kpi64, S.cfg.pressureBasis > 0 ? S.cfg.pressureBasis : 60);
     S.extrapolate = S.cfg.pressureGuess == 1;
     if (S.extrapolate)
     {
@@ -1193,7 +1211,9 @@ extern "C" int nsf_chorin_create(nsf_context ctx, const nsf_chorin_config * cfg,
         require(!(cfg->precision == NSF_PREC_MIXED && cfg->velMethod == 0),
                 "mixed precision uses velMethod 1, 2 (pcg) or 3 (chebyshev)");
         require(cfg->velMaxIters >= 1 && cfg->presMaxIters >= 1, "iteration caps must be >= 1");
-        require(cfg->pressureGuess == 0 || cfg->pressureGuess == 1, "pressureGuess must be 0 or 1");
+        require(cfg->pressureGuess >= 0 && cfg->pressureGuess <= 2, "pressureGuess must be 0, 1 or 2");
+        require(cfg->pressureBasis == 0 || (cfg->pressureBasis >= 3 && cfg->pressureBasis <= PROJ_MAXL),
+                "pressureBasis must be 0 (60) or 3..64");
         auto S = std::make_unique<nsf_chorin_s>();
         S->cfg = *cfg;
         if (S->cfg.checkInterval < 1)
@@ -1322,7 +1342,14 @@ extern "C" int nsf_chorin_get_state(nsf_chorin S, double * uOut, double * pOut, 
 
 extern "C" int nsf_chorin_set_state(nsf_chorin S, const double * uIn, const double * pIn, void * stream)
 {
+    return nsf_chorin_set_state_ex(S, uIn, pIn, 0, stream);
+}
+
+extern "C" int nsf_chorin_set_state_ex(nsf_chorin S, const double * uIn, const double * pIn, int flags,
+                                       void * stream)
+{
     return guarded([&] {
+        require((flags & ~NSF_STATE_KEEP_HISTORY) == 0, "unknown set_state flags");
         require(S, "null stepper");
         cudaStream_t s = stream ? asStream(stream) : S->stream;
         stateMaps(S);
@@ -1340,8 +1367,11 @@ extern "C" int nsf_chorin_set_state(nsf_chorin S, const double * uIn, const doub
             NSF_LAUNCH((kGatherPerm<double>), blocksFor(S->nIntP), s, S->nIntP, 1, S->pIdxDev.get(),
                        (const double *)sp, S->pInt.get());
         }
-        if (S->extrapolate) // a new history starts from the state just set
+        const bool keep = (flags & NSF_STATE_KEEP_HISTORY) != 0;
+        if (S->extrapolate && !keep) // a new history starts from the state just set
             NSF_CUDA(cudaMemsetAsync(S->pHist.get(), 0, sizeof(int), s));
+        if (S->project && !keep)
+            S->proj.reset(s);
         NSF_CUDA(cudaStreamSynchronize(s));
     });
 }

@@ -186,6 +186,14 @@ namespace nsf
         afterLaunch(name);
     }
 
+    // the same with a 2-D / 3-D grid
+    template <typename... KArgs, typename... Args>
+    inline void launchKernel(const char * name, void (*k)(KArgs...), dim3 grid, cudaStream_t s, Args &&... a)
+    {
+        k<<<grid, TPB, 0, s>>>(std::forward<Args>(a)...);
+        afterLaunch(name);
+    }
+
 #define NSF_LAUNCH(kernel, grid, stream, ...) ::nsf::launchKernel(#kernel, kernel, (grid), (stream), __VA_ARGS__)
 
     // launch a one-cluster kernel: cs CTAs of `threads` threads forming one thread-block cluster

@@ -49,7 +49,8 @@ class ColoringS(C.Structure):
 
 class ChorinCfgS(C.Structure):
     _fields_ = [("nu", C.c_double), ("tau", C.c_double), ("velMethod", C.c_int), ("velMaxIters", C.c_int),
-                ("velTol", C.c_double), ("presMaxIters", C.c_int), ("presTol", C.c_double), ("presGuess", C.c_int)]
+                ("velTol", C.c_double), ("presMaxIters", C.c_int), ("presTol", C.c_double), ("presGuess", C.c_int),
+                ("presBasis", C.c_int)]
 
 
 def build(quiet: bool = True) -> str:
@@ -366,13 +367,14 @@ class Chorin:
     (all host threads, OMP_NUM_THREADS); self.threads says what ran (1 if that build is missing)."""
 
     def __init__(self, ctx: Context, nu, tau, vel_method=1, vel_max_iters=200, vel_tol=1e-10,
-                 pres_max_iters=2000, pres_tol=1e-10, mt=False, pres_guess=0):
+                 pres_max_iters=2000, pres_tol=1e-10, mt=False, pres_guess=0, pres_basis=0):
         self.ctx = ctx
         self._L = lib_mt() if mt else None
         self.threads = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1)) if self._L else 1
         if self._L is None:
             self._L = lib()
-        cfg = ChorinCfgS(nu, tau, vel_method, vel_max_iters, vel_tol, pres_max_iters, pres_tol, pres_guess)
+        cfg = ChorinCfgS(nu, tau, vel_method, vel_max_iters, vel_tol, pres_max_iters, pres_tol, pres_guess,
+                         pres_basis)
         self._h = self._L.orc_chorin_create(C.byref(ctx._s), C.byref(cfg))
 
     def step(self):

@@ -33,6 +33,13 @@ struct orc_chorin_s
     double *dirVx; /* x values imposed on the Dirichlet nodes (ctx->dirVx unless set) */
     double *pPrev; /* presGuess 1: the pressure solution before the last one */
     int pHist;     /* solved pressures seen since create / set (capped at 2) */
+    /* presGuess 2 (Fischer, "Projection techniques for iterative solution of Ax = b with
+       successive right-hand sides", CMAME 163, 1998): pX holds pL vectors, the first pM of them
+       orthonormal in the Kp_int inner product; the solve starts from their projection of the new
+       solution, sum_i (x_i . b) x_i, and its correction is orthogonalised into the basis (a full
+       basis restarts from the solution and its last differences) */
+    double *pX, *pX0, *pW, *pQ, *pPrev2; /* pPrev2 (with pPrev, pHist): the last two solutions */
+    int pM, pL;
 };
 
 orc_chorin *orc_chorin_create(const orc_context *ctx, const orc_chorin_cfg *cfg)
@@ -55,6 +62,15 @@ orc_chorin *orc_chorin_create(const orc_context *ctx, const orc_chorin_cfg *cfg)
     s->rhsP = (double *)calloc(ctx->nIntP + 1, sizeof(double));
     s->g = (double *)calloc(2 * N, sizeof(double));
     s->pPrev = (double *)calloc(ctx->nIntP + 1, sizeof(double));
+    s->pL = cfg->presBasis > 0 ? (cfg->presBasis < 64 ? cfg->presBasis : 64) : 60;
+    if (cfg->presGuess == 2)
+    {
+        s->pX = (double *)calloc((size_t)s->pL * ctx->nIntP + 1, sizeof(double));
+        s->pX0 = (double *)calloc(ctx->nIntP + 1, sizeof(double));
+        s->pW = (double *)calloc(ctx->nIntP + 1, sizeof(double));
+        s->pQ = (double *)calloc(ctx->nIntP + 1, sizeof(double));
+        s->pPrev2 = (double *)calloc(ctx->nIntP + 1, sizeof(double));
+    }
     s->dirVx = (double *)calloc(ctx->nDir + 1, sizeof(double));
     memcpy(s->dirVx, ctx->dirVx, sizeof(double) * ctx->nDir);
     for (int i = 0; i < ctx->nDir; i++)
@@ -84,6 +100,11 @@ void orc_chorin_free(orc_chorin *s)
     free(s->g);
     free(s->dirVx);
     free(s->pPrev);
+    free(s->pX);
+    free(s->pX0);
+    free(s->pW);
+    free(s->pQ);
+    free(s->pPrev2);
     free(s);
 }
 
@@ -118,6 +139,7 @@ void orc_chorin_set(orc_chorin *s, const double *u, const double *p)
             s->pInt[i] = p[ctx->intP[i]];
     }
     s->pHist = 0; /* a new pressure history starts from the state just set */
+    s->pM = 0;
 }
 
 static void impose(orc_chorin *s)
@@ -175,6 +197,101 @@ static int mass_solve(orc_chorin *s, const double *rhs, double *acc, double *res
     return itMax;
 }
 
+static double dotn(const double *a, const double *b, int n)
+{
+    double t = 0;
+    for (int i = 0; i < n; i++)
+        t += a[i] * b[i];
+    return t;
+}
+
+/* pressure initial guess x0 = sum_i a_i x_i, a_i = x_i . b, over the basis (the previous solution
+   while the basis is empty); x0 is kept for the update */
+static void proj_guess(orc_chorin *s)
+{
+    const int n = s->ctx->nIntP;
+    if (s->pM > 0)
+    {
+        double a[64];
+        for (int k = 0; k < s->pM; k++)
+            a[k] = dotn(s->pX + (size_t)k * n, s->rhsP, n);
+        for (int i = 0; i < n; i++)
+        {
+            double v = 0;
+            for (int k = 0; k < s->pM; k++)
+                v += a[k] * s->pX[(size_t)k * n + i];
+            s->pInt[i] = v;
+        }
+    }
+    memcpy(s->pX0, s->pInt, sizeof(double) * n);
+}
+
+/* w (in pW) joins the basis: q = A w, beta_k = x_k . q, w' = w - sum_k beta_k x_k, and w' / |w'|_A
+   with |w'|_A^2 = w' . A w' (a second product: no cancellation when w is close to the span) unless
+   w' is (numerically) inside the span */
+static void proj_add(orc_chorin *s)
+{
+    const int n = s->ctx->nIntP;
+    orc_spmv(&s->ctx->Kpi, s->pW, s->pQ);
+    const double g = dotn(s->pW, s->pQ, n);
+    double beta[64];
+    for (int k = 0; k < s->pM; k++)
+        beta[k] = dotn(s->pX + (size_t)k * n, s->pQ, n);
+    double *x = s->pX + (size_t)s->pM * n;
+    for (int i = 0; i < n; i++)
+    {
+        double v = s->pW[i];
+        for (int k = 0; k < s->pM; k++)
+            v -= beta[k] * s->pX[(size_t)k * n + i];
+        x[i] = v;
+    }
+    orc_spmv(&s->ctx->Kpi, x, s->pQ);
+    const double nn = dotn(x, s->pQ, n);
+    if (!(g > 0) || !(nn > 1e-20 * g))
+        return;
+    const double inv = 1.0 / sqrt(nn);
+    for (int i = 0; i < n; i++)
+        x[i] *= inv;
+    s->pM++;
+}
+
+/* After a solve: the correction x - x0 joins the basis.  An empty or full basis restarts from the
+   solution and its first and second differences over the last two steps (the span then holds the
+   linear and quadratic extrapolations; the pressure of the projection step carries a two-step
+   oscillation that a single vector misses). */
+static void proj_update(orc_chorin *s)
+{
+    const int n = s->ctx->nIntP;
+    if (s->pM == 0 || s->pM == s->pL)
+    {
+        s->pM = 0;
+        memcpy(s->pW, s->pInt, sizeof(double) * n);
+        proj_add(s);
+        if (s->pHist >= 1)
+        {
+            for (int i = 0; i < n; i++)
+                s->pW[i] = s->pInt[i] - s->pPrev[i];
+            proj_add(s);
+        }
+        if (s->pHist >= 2)
+        {
+            for (int i = 0; i < n; i++)
+                s->pW[i] = s->pInt[i] - 2.0 * s->pPrev[i] + s->pPrev2[i];
+            proj_add(s);
+        }
+    }
+    else
+    {
+        for (int i = 0; i < n; i++)
+            s->pW[i] = s->pInt[i] - s->pX0[i];
+        proj_add(s);
+    }
+    memcpy(s->pPrev2, s->pPrev, sizeof(double) * n);
+    memcpy(s->pPrev, s->pInt, sizeof(double) * n);
+    if (s->pHist < 2)
+        s->pHist++;
+}
+
 int orc_chorin_step(orc_chorin *s, double *stats)
 {
     const orc_context *ctx = s->ctx;
@@ -208,8 +325,12 @@ int orc_chorin_step(orc_chorin *s, double *stats)
         if (s->pHist < 2)
             s->pHist++;
     }
+    if (s->cfg.presGuess == 2)
+        proj_guess(s);
     int itP = 0;
     int st = orc_sys_pcg(s->sysP, 1, s->rhsP, s->pInt, s->cfg.presMaxIters, s->cfg.presTol, &itP, &resP);
+    if (s->cfg.presGuess == 2)
+        proj_update(s);
     memset(s->p, 0, sizeof(double) * P);
     for (int i = 0; i < ctx->nIntP; i++)
         s->p[ctx->intP[i]] = s->pInt[i];

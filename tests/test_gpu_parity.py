@@ -400,6 +400,49 @@ def test_chorin_extrapolated_pressure_guess_matches_oracle(setup, torch_cuda, pr
     assert st.stats()["status"] == 0
 
 
+@pytest.mark.parametrize("graph", [True, False])
+@pytest.mark.parametrize("precision", ["f64", "mixed", "mixedsolve"])
+def test_chorin_projected_pressure_guess_matches_oracle(setup, torch_cuda, precision, graph):
+    """pressure_guess 2 (the pressure solve starts from the projection of the new solution onto a
+    Kp_int-orthonormal basis of earlier solutions): with a 4-vector basis, 12 steps pass through
+    three restarts; the FP64 stepper follows the oracle with the same option (1e-7), the mixed one
+    within the mixed bounds; set_state empties the basis on both sides; the solves meet their
+    tolerance and the basis takes fewer pressure iterations than the previous-solution guess."""
+    G, O, mesh, ctx, om, oc = setup
+    prec = {"f64": G.NSF_PREC_F64, "mixed": G.NSF_PREC_MIXED, "mixedsolve": G.NSF_PREC_F64_MIXEDSOLVE}[precision]
+
+    def gpu(guess):
+        return G.ChorinStepper(ctx, 1e-3, 1e-3, precision=prec, vel_method=1, vel_max_iters=300, vel_tol=1e-10,
+                               pres_max_iters=3000, pres_tol=1e-10, use_graph=graph, pressure_guess=guess,
+                               pressure_basis=4)
+
+    st = gpu(2)
+    ch = O.Chorin(oc, 1e-3, 1e-3, vel_method=1, vel_max_iters=300, vel_tol=1e-10, pres_max_iters=3000, pres_tol=1e-10,
+                  pres_guess=2, pres_basis=4)
+    st.step(3)
+    for _ in range(3):
+        ch.step()
+    u, p = ch.state()
+    st.set_state(u, p)
+    ch.set_state(u, p)
+    ref = gpu(0)
+    ref.set_state(u, p)
+    its, its0 = [], []
+    for _ in range(12):
+        st.step(1)
+        ch.step()
+        ref.step(1)
+        s = st.stats()
+        assert s["status"] == 0 and s["pres_rel"] <= 1e-10
+        its.append(s["pres_iters"])
+        its0.append(ref.stats()["pres_iters"])
+    ug, pg = st.state()
+    uo, po = ch.state()
+    tu, tp = (1e-5, 2e-4) if precision == "mixed" else (1e-7, 1e-7)
+    assert _rel(ug, uo) <= tu and _rel(pg, po) <= tp
+    assert sum(its[6:]) < sum(its0[6:]), (its, its0)
+
+
 def test_pack_equals_separate_steps(setup, torch_cuda, monkeypatch, mesh_dir):
     """A pack (one graph, one branch per stepper) of three steppers on two meshes (h = 0.025 and
     h = 0.04, different viscosities and precisions) reaches bit-identical states to the same

@@ -383,3 +383,25 @@ def test_chebyshev_chorin_matches_pcg(oracle_lib, channel_coarse):
     ub, pb = b.state()
     assert np.max(np.abs(ua - ub)) <= 1e-9 * np.max(np.abs(ua))
     assert np.max(np.abs(pa - pb)) <= 1e-8 * np.max(np.abs(pa))
+
+
+def test_projected_pressure_guess(oracle_lib, channel_coarse):
+    """Pressure guess 2 (projection onto a Kp_int-orthonormal basis of earlier solutions, restarts
+    from the solution and its last differences): the fields follow the previous-solution guess to
+    the solver tolerance, and the solves get shorter once the basis holds a few vectors, across
+    restarts of a small basis."""
+    O = oracle_lib
+    m = O.Mesh(channel_coarse)
+    ctx = O.Context(m, 1.2, True)
+    runs = {}
+    for guess, basis in ((0, 0), (2, 5), (2, 0)):
+        ch = O.Chorin(ctx, 1e-3, 1e-3, vel_method=1, vel_tol=1e-12, pres_tol=1e-12, pres_guess=guess,
+                      pres_basis=basis)
+        its = [ch.step()[1] for _ in range(30)]
+        runs[(guess, basis)] = (its, ch.state())
+    its0, (u0, p0) = runs[(0, 0)]
+    for key in ((2, 5), (2, 0)):
+        its, (u, p) = runs[key]
+        assert np.linalg.norm(u - u0) <= 1e-9 * np.linalg.norm(u0), key
+        assert np.linalg.norm(p - p0) <= 1e-7 * np.linalg.norm(p0), key
+        assert sum(its[10:]) < 0.9 * sum(its0[10:]), (key, its, its0)
