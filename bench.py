@@ -519,7 +519,7 @@ def bench_batch(args):
         "config": {"workload": f"{B} instances, h=0.01, U_max~U[0.2,1.5], nu~logU[5e-4,2e-3], tau=2e-4, "
                                "pressure to 1e-8 rel", "instances": B, "setup_s": round(setup_s, 1),
                    "mass_solve": MASS_SOLVES[args.vel_method],
-                   "pressure_guess": PRESSURE_GUESSES[args.pressure_guess].format(args.pressure_basis or 60),
+                   "pressure_guess": PRESSURE_GUESSES[args.pressure_guess].format(args.pressure_basis or 250),
                    "execution": "one graph-captured stepper per instance on its own stream, cluster-resident solves"},
         "one_instance_steps_per_s": round(one, 2),
         "speedup_vs_one_at_a_time": round(agg / one, 2),
@@ -616,7 +616,7 @@ def bench_pack(args):
         "config": {"workload": f"{per} instances on each of h={hs}, U_max~U[0.2,1.5], nu~logU[5e-4,2e-3], "
                                f"tau={tau}, pressure to 1e-8 rel", "instances": n,
                    "mass_solve": MASS_SOLVES[args.vel_method],
-                   "pressure_guess": PRESSURE_GUESSES[args.pressure_guess].format(args.pressure_basis or 60),
+                   "pressure_guess": PRESSURE_GUESSES[args.pressure_guess].format(args.pressure_basis or 250),
                    "mesh_sizes_N_P": {str(h): sizes[h] for h in hs}, "setup_s": round(setup_s, 1),
                    "execution": "one CUDA graph per step whose branches are the 48 instances' steps (nsf_pack); "
                                 "cluster-resident solves"},
@@ -689,7 +689,7 @@ def bench_long(args):
         "config": {"workload": f"DFG channel h={H}, Umax=1.5, nu={NU}, tau={TAU}, {n} steps from rest, pressure "
                                f"to {PRES_TOL} rel", "N": ctx.N, "P": ctx.P,
                    "mass_solve": MASS_SOLVES[args.vel_method],
-                   "pressure_guess": PRESSURE_GUESSES[args.pressure_guess].format(args.pressure_basis or 60)},
+                   "pressure_guess": PRESSURE_GUESSES[args.pressure_guess].format(args.pressure_basis or 250)},
         "fp64_steps_per_s": round(n / secs["fp64"], 2),
         "field_rel_l2_mixed_vs_fp64": field,
         "drag_max_rel_err": float(np.abs(sm[:, 0] - sf[:, 0]).max() / fmax),
@@ -863,44 +863,56 @@ def bench_ours(args, rank, world, local_rank):
 
         # ---- FP64 drop-in on the same workload
         f64 = stepper(G.NSF_PREC_F64)
-        t_f64, _ = timed(f64, max(1, args.steps // 2), args.warmup)
+        t_f64, _ = timed(f64, args.steps, args.warmup)  # the same steps from rest as the main line
         st_f64 = f64.stats()
         u_m, p_m = mixed.state()
+        del f64
 
-        # ---- e2e through the C ABI with host buffers: H2D state, step, D2H state every step, from
-        # and to pinned host memory
+        # ---- e2e through the C ABI with host buffers, on a fresh mixed stepper over the same steps
+        # from rest as the main line (W untimed, K timed): every step H2D of the state from pinned
+        # host memory, one step, D2H of the state to pinned host memory
+        e2e = stepper(G.NSF_PREC_MIXED)
         u_h = torch.zeros(2 * N, dtype=torch.float64, pin_memory=True).numpy()
         p_h = torch.zeros(P, dtype=torch.float64, pin_memory=True).numpy()
-        mixed.get_state_into(u_h, p_h)
-        e2e_steps = max(3, args.steps // 4)
+        e2e.get_state_into(u_h, p_h)
+
+        def e2e_step():
+            e2e.set_state(u_h, p_h, keep_history=True)  # the state continues the run
+            e2e.step(1, sp)
+            e2e.get_state_into(u_h, p_h)
+
+        for _ in range(args.warmup):
+            e2e_step()
+        e2e_steps = args.steps
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         for _ in range(e2e_steps):
-            mixed.set_state(u_h, p_h, keep_history=True)  # the state continues the run
-            mixed.step(1, sp)
-            mixed.get_state_into(u_h, p_h)
+            e2e_step()
         t_e2e = time.perf_counter() - t0
+        del e2e
 
         # ---- dominant kernel alone: FastConvection SpMV (I: nnz(K) x 2N) fused with the nu K add
+        # (the mixed stepper's instantiation: FP32 values of I, FP64 u, K, A and sums)
         Ih = ctx.matrix("I")
         Kh = ctx.matrix("K")
         I32 = G.CsrF.from_host(Ih, dtype=G.NSF_F32)
-        u32 = torch.tensor(u_m, dtype=torch.float32, device="cuda")
-        K32 = torch.tensor(Kh.values, dtype=torch.float32, device="cuda")
-        A32 = torch.zeros_like(K32)
+        u64 = torch.tensor(u_m, dtype=torch.float64, device="cuda")
+        K64 = torch.tensor(Kh.values, dtype=torch.float64, device="cuda")
+        A64 = torch.zeros_like(K64)
         reps = 20
         with torch.cuda.stream(stream):
             for _ in range(3):
-                G.fastconv_apply(I32, K32, NU, u32, A32, sp)
+                G.fastconv_apply_mixed(I32, K64, NU, u64, A64, sp)
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             e0.record(stream)
             for _ in range(reps):
-                G.fastconv_apply(I32, K32, NU, u32, A32, sp)
+                G.fastconv_apply_mixed(I32, K64, NU, u64, A64, sp)
             e1.record(stream)
             torch.cuda.synchronize()
         t_fc = e0.elapsed_time(e1) / 1e3 / reps
         nnzI, rowsI = Ih.nnz, Ih.rows
-        fc_bytes = nnzI * (4 + 4) + (rowsI + 1) * 4 + 2 * N * 4 + 2 * rowsI * 4
+        # values + column indices of I, row starts, u once (FP64), K read and A written (FP64)
+        fc_bytes = nnzI * (4 + 4) + (rowsI + 1) * 4 + 2 * N * 8 + 2 * rowsI * 8
 
         # ---- dominant kernel: the cluster-resident pressure PCG (FP32 inner solve of the
         # refinement).  Per-iteration time from two solves that differ only in the iteration cap
@@ -969,7 +981,7 @@ def bench_ours(args, rank, world, local_rank):
                        "l2": "working set > L2 (FastConvection matrix %.0f MB FP32)" % (nnzI * 8 / 1e6),
                        "graph": True, "setup_s": round(setup_s, 2),
                        "mass_solve": MASS_SOLVES[args.vel_method],
-                       "pressure_guess": PRESSURE_GUESSES[args.pressure_guess].format(args.pressure_basis or 60)},
+                       "pressure_guess": PRESSURE_GUESSES[args.pressure_guess].format(args.pressure_basis or 250)},
             "e2e": {"value": round(world * e2e_steps / t_e2e, 3), "unit": "steps/s",
                     "h2d_bytes_per_step": (2 * N + P) * 8, "d2h_bytes_per_step": (2 * N + P) * 8,
                     "path": "per step: set_state (u, p from pinned host memory, renumbered on the device; "
@@ -984,7 +996,8 @@ def bench_ours(args, rank, world, local_rank):
                          "note": "vectors and matrix live in shared memory across the cluster; the kernel is "
                                  "bound by barrier/gather latency, not HBM (ncu DRAM traffic per launch is "
                                  "~1% of the algorithmic bytes)"},
-            "roofline_fastconv": {"bound": "hbm", "kernel": "kFastConvSell<float> (A = nu K + I u, SELL-32-256)",
+            "roofline_fastconv": {"bound": "hbm", "kernel": "kFastConvSell<float, double, double, double> (A = nu K + I u, FP32 I values, FP64 "
+                                                "u, K, A and sums, SELL-32-256)",
                                   "achieved": round(achieved, 1), "peak": hbm, "unit": "GB/s",
                                   "frac": round(achieved / hbm, 4), "peak_kind": kind,
                                   "algorithmic_bytes": fc_bytes, "launch_us": round(t_fc * 1e6, 2)},
@@ -1022,7 +1035,7 @@ def main():
                     help="channel, batch, pack and long workloads: mass solve, 1 PCG multicolor SGS, 2 PCG "
                          "Jacobi, 3 Chebyshev Jacobi")
     ap.add_argument("--pressure-basis", type=int, default=0,
-                    help="pressure guess 2: basis vectors (3..64; 0: 60)")
+                    help="pressure guess 2: basis vectors (3..256; 0: 250)")
     ap.add_argument("--pressure-guess", type=int, default=2, choices=[0, 1, 2],
                     help="channel, batch, pack and long workloads: pressure initial guess, 0 previous "
                          "solution, 1 extrapolated, 2 projected onto earlier solutions")

@@ -114,6 +114,12 @@ int nsf_spmm(nsf_csr a, int nrhs, const void *X, int ldx, void *Y, int ldy, void
 /* Avals = nu * Kvals + I u, the linearised advection update fused with the diffusion add.
    Replaces fcSpmv.compute + cublasSgeam (cpp/execs/NavierStokes/src/chorinCuda.cu:243-250). */
 int nsf_fastconv_apply(nsf_csr I, const void *Kvals, double nu, const void *u, void *Avals, void *stream);
+/* The same with FP32 operator values and FP64 vectors and sums (I of dtype NSF_F32; Kvals, u and
+   Avals FP64): the FastConvection product of the mixed-precision stepper.  The matrix traffic is
+   FP32; the sums and A stay FP64 because A u feeds the divergence, which would amplify rounding
+   noise that changes from step to step.  Replaces the same reference calls as nsf_fastconv_apply. */
+int nsf_fastconv_apply_mixed(nsf_csr I, const double *Kvals, double nu, const double *u, double *Avals,
+                             void *stream);
 
 /* Largest nrhs nsf_residual_noalloc accepts (its scratch is sized for it). */
 #define NSF_NOALLOC_MAX_RHS 4
@@ -196,7 +202,7 @@ typedef struct
                              (x_k . b) x_k; each solve's correction joins the basis; a full basis
                              restarts from the solution and its last two differences).  1 and 2
                              have no reference counterpart: fewer iterations, the same tolerance */
-    int pressureBasis;    /* pressureGuess 2: basis vectors, 3..64 (0: 60) */
+    int pressureBasis;    /* pressureGuess 2: basis vectors, 3..256 (0: 250) */
 } nsf_chorin_config;
 
 typedef struct nsf_chorin_s *nsf_chorin;

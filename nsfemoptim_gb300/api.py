@@ -210,6 +210,13 @@ def fastconv_apply(I: CsrF, K_values, nu: float, u, A_values, stream=None):
     return A_values
 
 
+def fastconv_apply_mixed(I: CsrF, K_values, nu: float, u, A_values, stream=None):
+    """A = nu * K + I u with I in FP32 and K, u, A (and the sums) in FP64: the mixed stepper's
+    FastConvection product."""
+    check(lib().nsf_fastconv_apply_mixed(I._h, _dptr(K_values), nu, _dptr(u), _dptr(A_values), vp(stream)))
+    return A_values
+
+
 class Spmv:
     """cu::spmv: b = M x with default operand vectors."""
 
@@ -340,7 +347,7 @@ class ChorinStepper:
                  pressure_basis: int = 0):
         """vel_method: mass solve, 0 multicolor GS, 1 PCG-SGS, 2 PCG-Jacobi, 3 Chebyshev-Jacobi.
         pressure_guess: 0 the previous pressure (as the reference), 1 extrapolated from the last two,
-        2 projected onto up to pressure_basis earlier solutions (0: 60)."""
+        2 projected onto up to pressure_basis earlier solutions (0: 250)."""
         self.ctx = ctx
         self.cfg = ChorinConfig(nu, tau, precision, vel_method, vel_max_iters, vel_tol, pres_max_iters, pres_tol,
                                 check_interval, int(use_graph), max_outer, inner_tol, int(pressure_guess),
@@ -502,6 +509,6 @@ class Adjoint:
 
 
 __all__ = ["Mesh", "load_gmsh", "ChorinContext", "build_chorin_context", "coloring", "CsrF", "Spmv", "Spmm",
-           "spmv", "spmm", "fastconv_apply", "AbstractSolver", "create_solver", "ChorinStepper", "kernel_launches",
+           "spmv", "spmm", "fastconv_apply", "fastconv_apply_mixed", "AbstractSolver", "create_solver", "ChorinStepper", "kernel_launches",
            "Forces", "Adjoint", "Pack", "NSF_F32", "NSF_F64", "NSF_PREC_F64", "NSF_PREC_MIXED", "NSF_PREC_F64_MIXEDSOLVE",
            "NsfError"]

@@ -624,6 +624,18 @@ extern "C" int nsf_spmm(nsf_csr a, int nrhs, const void * X, int ldx, void * Y, 
     });
 }
 
+extern "C" int nsf_fastconv_apply_mixed(nsf_csr I, const double * K, double nu, const double * u, double * A,
+                                        void * stream)
+{
+    return guarded([&] {
+        require(I && K && u && A, "null argument");
+        require(I->dtype == NSF_F32, "nsf_fastconv_apply_mixed takes an FP32 FastConvection matrix");
+        const DevSell<float> & S = I->s32;
+        NSF_LAUNCH((kFastConvSell<float, double, double, double>), S.blocks(), asStream(stream), S.rows, S.nSlices,
+                   S.ss.get(), S.perm.get(), S.ci.get(), S.v.get(), u, K, nu, A);
+    });
+}
+
 extern "C" int nsf_fastconv_apply(nsf_csr I, const void * K, double nu, const void * u, void * A, void * stream)
 {
     return guarded([&] {
@@ -846,7 +858,6 @@ struct nsf_chorin_s
     DevCsr<double> I64, D64, G64;
     DevCsr<float> I32, D32, G32;
     DevBuf<double> K64, A64;
-    DevBuf<float> K32, A32;
     // state and work vectors
     DevBuf<double> u, pInt, rhs, acc, rhsP;
     // pressure initial guess extrapolated from the last two solutions (cfg.pressureGuess == 1)
@@ -930,12 +941,12 @@ struct nsf_chorin_s
         if (mixed)
         {
             const DevSell<float> & IS = I32.sell;
-            NSF_LAUNCH((kFastConvSell<float, double, float, float>), IS.blocks(), s, IS.rows, IS.nSlices, IS.ss.get(),
-                       IS.perm.get(), IS.ci.get(), IS.v.get(), u.get(), K32.get(), (float)cfg.nu, A32.get());
+            NSF_LAUNCH((kFastConvSell<float, double, double, double>), IS.blocks(), s, IS.rows, IS.nSlices,
+                       IS.ss.get(), IS.perm.get(), IS.ci.get(), IS.v.get(), u.get(), K64.get(), cfg.nu, A64.get());
             // FP32 values, FP64 sums (4.6M FMAs): FP32 sums would put step-to-step rounding noise into
             // u, which the divergence amplifies in the pressure right-hand side
-            NSF_LANES(M32.L, NSF_LAUNCH((kSpmm<float, double, double, double, LL, 2>), blocksFor((long long)N * M32.L), s, N,
-                                        M32.rsF.get(), M32.ciF.get(), A32.get(), u.get(), N, rhs.get(), N));
+            NSF_LANES(M32.L, NSF_LAUNCH((kSpmm<double, double, double, double, LL, 2>), blocksFor((long long)N * M32.L), s, N,
+                                        M32.rsF.get(), M32.ciF.get(), A64.get(), u.get(), N, rhs.get(), N));
         }
         else
         {
@@ -1119,9 +1130,8 @@ static void buildChorin(nsf_chorin_s & S, const Context & c)
         S.I32.upload(Ip, true);
         S.D32.upload(Dp);
         S.G32.upload(Gp);
-        std::vector<float> k32(knu.begin(), knu.end());
-        S.K32.upload(k32);
-        S.A32.alloc(knu.size());
+        S.K64.upload(knu);
+        S.A64.alloc(knu.size());
         if (!cheb)
         {
             S.mvelT.setup(&S.M64, &S.M32, 2, kMassIters);
@@ -1183,7 +1193,7 @@ static void buildChorin(nsf_chorin_s & S, const Context & c)
     S.pInt.alloc(S.nIntP);
     S.project = S.cfg.pressureGuess == 2;
     if (S.project)
-        S.proj.setup(&S.Kpi64, S.cfg.pressureBasis > 0 ? S.cfg.pressureBasis : 60);
+        S.proj.setup(&S.Kpi64, S.cfg.pressureBasis > 0 ? S.cfg.pressureBasis : 250);
     S.extrapolate = S.cfg.pressureGuess == 1;
     if (S.extrapolate)
     {
@@ -1213,7 +1223,7 @@ extern "C" int nsf_chorin_create(nsf_context ctx, const nsf_chorin_config * cfg,
         require(cfg->velMaxIters >= 1 && cfg->presMaxIters >= 1, "iteration caps must be >= 1");
         require(cfg->pressureGuess >= 0 && cfg->pressureGuess <= 2, "pressureGuess must be 0, 1 or 2");
         require(cfg->pressureBasis == 0 || (cfg->pressureBasis >= 3 && cfg->pressureBasis <= PROJ_MAXL),
-                "pressureBasis must be 0 (60) or 3..64");
+                "pressureBasis must be 0 (250) or 3..256");
         auto S = std::make_unique<nsf_chorin_s>();
         S->cfg = *cfg;
         if (S->cfg.checkInterval < 1)

@@ -6,8 +6,10 @@
 // Kp_int-orthogonal projection of the new solution onto their span,
 //     x0 = sum_k a_k x_k,   a_k = x_k . b          (b: the pressure right-hand side),
 // which needs no product with the matrix.  After the solve the correction w = x - x0 joins the
-// basis: q = A w, beta_k = x_k . q, w' = w - sum_k beta_k x_k, x_new = w' / sqrt(w' . A w') (the
-// norm from a second product, so no cancellation when w lies close to the span).  An empty or
+// basis: q = A w, beta_k = x_k . q, w' = w - sum_k beta_k x_k, done twice (classical Gram-Schmidt
+// with one re-orthogonalisation keeps a basis of hundreds of vectors orthonormal), and
+// x_new = w' / sqrt(w' . A w') (the norm from its own product: no cancellation when w lies close to
+// the span).  An empty or
 // full basis restarts from the solution x and its first and second differences over the last two
 // steps, x - x(n-1) and x - 2 x(n-1) + x(n-2): the span then holds the linear and quadratic
 // extrapolations (the projection step's pressure carries a two-step oscillation that the
@@ -25,7 +27,7 @@
 
 namespace nsf
 {
-    constexpr int PROJ_MAXL = 64;  // basis vectors at most
+    constexpr int PROJ_MAXL = 256; // basis vectors at most
     constexpr int PROJ_CHUNKS = 8; // blocks per dot product in kProjDots
 
     struct ProjState
@@ -147,7 +149,8 @@ namespace nsf
     }
 
     // once per grid after kProjSpmvDot: stage 0 keeps g = w . A w; stage 1 accepts the new vector
-    // if its A-norm is not lost in rounding, and advances the basis
+    // if its A-norm is not lost in rounding, and advances the basis; stage 2 (the product of the
+    // re-orthogonalisation) keeps nothing
     struct ProjEpi
     {
         ProjState * st;
@@ -155,10 +158,9 @@ namespace nsf
         __device__ void operator()() const
         {
             if (stage == 0)
-            {
                 st->g = st->dot;
+            if (stage != 1)
                 return;
-            }
             const double g = st->g, nn = st->dot;
             const bool ok = g > 0 && nn > 1e-20 * g && isfinite(nn);
             st->nn = nn;
@@ -172,8 +174,8 @@ namespace nsf
         }
     };
 
-    // q = A src and src . q (row groups of L lanes over the CSR); stage 0: src = w, stage 1: src =
-    // the slot being filled.  Skipped unless add `which` is active.
+    // q = A src and src . q (row groups of L lanes over the CSR); stage 0: src = w, stages 1 and 2:
+    // src = the slot being filled.  Skipped unless add `which` is active.
     template <int L>
     __global__ void __launch_bounds__(TPB) kProjSpmvDot(int n, const int * __restrict__ rs, const int * __restrict__ ci,
                                                          const double * __restrict__ v, ProjState * st, int which,
@@ -200,9 +202,9 @@ namespace nsf
         gridSum<double, 1>(red, scratch, Outs<1>{{&st->dot}}, &st->ticket, nullptr, ProjEpi{st, stage});
     }
 
-    // X[slot] = w - sum_k beta_k X_k over the basis
+    // X[slot] = w - sum_k beta_k X_k over the basis (w == nullptr: in place, X[slot] -= ...)
     __global__ void __launch_bounds__(TPB) kProjOrth(int n, double * X, const double * beta, const ProjState * st,
-                                                      int which, const double * __restrict__ w)
+                                                      int which, const double * w)
     {
         if (!st->active[which])
             return;
@@ -212,9 +214,10 @@ namespace nsf
             c[k] = beta[k];
         __syncthreads();
         double * dst = X + (size_t)slot * n;
+        const double * src = w ? w : dst;
         for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
         {
-            double v = w[i];
+            double v = src[i];
             for (int k = 0; k < m; k++)
                 v -= c[k] * X[(size_t)k * n + i];
             dst[i] = v;
@@ -292,17 +295,19 @@ namespace nsf
                 NSF_LAUNCH(kProjPrep, blocksFor(n), s, n, which, (const ProjState *)st.get(), p,
                            (const double *)x0.get(), (const double *)prev1.get(), (const double *)prev2.get(),
                            w.get());
-                for (int stage = 0; stage < 2; stage++)
+                // products of w, of the orthogonalised vector (re-orthogonalisation), of the result
+                for (int stage : {0, 2, 1})
                 {
                     NSF_LANES(S.L, NSF_LAUNCH((kProjSpmvDot<LL>), S.fullBlocks(), s, n, S.rsF.get(), S.ciF.get(),
                                               S.vF.get(), st.get(), which, stage, (const double *)w.get(),
                                               (const double *)X.get(), q.get(), scratch.get()));
-                    if (stage == 0)
+                    if (stage != 1)
                     {
                         NSF_LAUNCH(kProjDots, dim3(PROJ_CHUNKS, L), s, n, (const double *)X.get(),
                                    (const double *)q.get(), st.get(), partial.get(), coef.get(), which);
                         NSF_LAUNCH(kProjOrth, blocksFor(n), s, n, X.get(), (const double *)coef.get(),
-                                   (const ProjState *)st.get(), which, (const double *)w.get());
+                                   (const ProjState *)st.get(), which,
+                                   stage == 0 ? (const double *)w.get() : (const double *)nullptr);
                     }
                 }
                 NSF_LAUNCH(kProjScale, blocksFor(n), s, n, X.get(), (const ProjState *)st.get(), which);
@@ -310,6 +315,6 @@ namespace nsf
             NSF_LAUNCH(kProjShift, blocksFor(n), s, n, st.get(), p, prev1.get(), prev2.get());
         }
 
-        int basisKernelsPerStep() const { return 2 + 1 + 3 * 6 + 1; }
+        int basisKernelsPerStep() const { return 2 + 1 + 3 * 9 + 1; }
     };
 } // namespace nsf

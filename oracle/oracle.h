@@ -140,7 +140,7 @@ typedef struct
     int presGuess;       /* 0: start from the previous pressure; 1: from 2 p(n-1) - p(n-2) once two
                             solved pressures exist; 2: the Kp_int-orthogonal projection of the new
                             solution onto the last solutions (Fischer's method, presBasis vectors) */
-    int presBasis;       /* presGuess 2: basis size, 3..64 (0 = 60) */
+    int presBasis;       /* presGuess 2: basis size, 3..256 (0 = 250) */
 } orc_chorin_cfg;
 
 typedef struct orc_chorin_s orc_chorin;

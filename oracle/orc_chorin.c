@@ -22,6 +22,9 @@
 #include <math.h>
 #include <stdlib.h>
 #include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
 
 struct orc_chorin_s
 {
@@ -37,7 +40,7 @@ struct orc_chorin_s
        successive right-hand sides", CMAME 163, 1998): pX holds pL vectors, the first pM of them
        orthonormal in the Kp_int inner product; the solve starts from their projection of the new
        solution, sum_i (x_i . b) x_i, and its correction is orthogonalised into the basis (a full
-       basis restarts from the solution and its last differences) */
+       basis restarts from the solution and its last two differences) */
     double *pX, *pX0, *pW, *pQ, *pPrev2; /* pPrev2 (with pPrev, pHist): the last two solutions */
     int pM, pL;
 };
@@ -62,7 +65,7 @@ orc_chorin *orc_chorin_create(const orc_context *ctx, const orc_chorin_cfg *cfg)
     s->rhsP = (double *)calloc(ctx->nIntP + 1, sizeof(double));
     s->g = (double *)calloc(2 * N, sizeof(double));
     s->pPrev = (double *)calloc(ctx->nIntP + 1, sizeof(double));
-    s->pL = cfg->presBasis > 0 ? (cfg->presBasis < 64 ? cfg->presBasis : 64) : 60;
+    s->pL = cfg->presBasis > 0 ? (cfg->presBasis < 256 ? cfg->presBasis : 256) : 250;
     if (cfg->presGuess == 2)
     {
         s->pX = (double *)calloc((size_t)s->pL * ctx->nIntP + 1, sizeof(double));
@@ -205,6 +208,55 @@ static double dotn(const double *a, const double *b, int n)
     return t;
 }
 
+/* out[k] = X_k . v for k < m: the rows split into one chunk per thread, the chunks' partial sums
+   added in thread order */
+static void multi_dot(const double *X, int m, int n, const double *v, double *out)
+{
+    int nt = 1;
+#ifdef _OPENMP
+    nt = omp_get_max_threads();
+#endif
+    double *part = (double *)calloc((size_t)nt * m + 1, sizeof(double));
+#pragma omp parallel num_threads(nt)
+    {
+        int t = 0, T = 1;
+#ifdef _OPENMP
+        t = omp_get_thread_num();
+        T = omp_get_num_threads();
+#endif
+        const int i0 = (int)((long long)n * t / T), i1 = (int)((long long)n * (t + 1) / T);
+        for (int k = 0; k < m; k++)
+        {
+            const double *x = X + (size_t)k * n;
+            double acc = 0;
+            for (int i = i0; i < i1; i++)
+                acc += x[i] * v[i];
+            part[(size_t)t * m + k] = acc;
+        }
+    }
+    for (int k = 0; k < m; k++)
+    {
+        double acc = 0;
+        for (int t = 0; t < nt; t++)
+            acc += part[(size_t)t * m + k];
+        out[k] = acc;
+    }
+    free(part);
+}
+
+/* y = base + sign * sum_k c_k X_k for k < m (base may be y) */
+static void combine(const double *X, int m, int n, const double *c, const double *base, double sign, double *y)
+{
+#pragma omp parallel for schedule(static)
+    for (int i = 0; i < n; i++)
+    {
+        double v = 0;
+        for (int k = 0; k < m; k++)
+            v += c[k] * X[(size_t)k * n + i];
+        y[i] = (base ? base[i] : 0.0) + sign * v;
+    }
+}
+
 /* pressure initial guess x0 = sum_i a_i x_i, a_i = x_i . b, over the basis (the previous solution
    while the basis is empty); x0 is kept for the update */
 static void proj_guess(orc_chorin *s)
@@ -212,38 +264,31 @@ static void proj_guess(orc_chorin *s)
     const int n = s->ctx->nIntP;
     if (s->pM > 0)
     {
-        double a[64];
-        for (int k = 0; k < s->pM; k++)
-            a[k] = dotn(s->pX + (size_t)k * n, s->rhsP, n);
-        for (int i = 0; i < n; i++)
-        {
-            double v = 0;
-            for (int k = 0; k < s->pM; k++)
-                v += a[k] * s->pX[(size_t)k * n + i];
-            s->pInt[i] = v;
-        }
+        double a[256];
+        multi_dot(s->pX, s->pM, n, s->rhsP, a);
+        combine(s->pX, s->pM, n, a, NULL, 1.0, s->pInt);
     }
     memcpy(s->pX0, s->pInt, sizeof(double) * n);
 }
 
-/* w (in pW) joins the basis: q = A w, beta_k = x_k . q, w' = w - sum_k beta_k x_k, and w' / |w'|_A
-   with |w'|_A^2 = w' . A w' (a second product: no cancellation when w is close to the span) unless
-   w' is (numerically) inside the span */
+/* w (in pW) joins the basis: q = A w, beta_k = x_k . q, w' = w - sum_k beta_k x_k, twice
+   (classical Gram-Schmidt with one re-orthogonalisation), and w' / |w'|_A with
+   |w'|_A^2 = w' . A w' (its own product: no cancellation when w is close to the span) unless w' is
+   (numerically) inside the span */
 static void proj_add(orc_chorin *s)
 {
     const int n = s->ctx->nIntP;
     orc_spmv(&s->ctx->Kpi, s->pW, s->pQ);
     const double g = dotn(s->pW, s->pQ, n);
-    double beta[64];
-    for (int k = 0; k < s->pM; k++)
-        beta[k] = dotn(s->pX + (size_t)k * n, s->pQ, n);
+    double beta[256];
     double *x = s->pX + (size_t)s->pM * n;
-    for (int i = 0; i < n; i++)
+    memcpy(x, s->pW, sizeof(double) * n);
+    for (int pass = 0; pass < 2; pass++)
     {
-        double v = s->pW[i];
-        for (int k = 0; k < s->pM; k++)
-            v -= beta[k] * s->pX[(size_t)k * n + i];
-        x[i] = v;
+        if (pass == 1)
+            orc_spmv(&s->ctx->Kpi, x, s->pQ);
+        multi_dot(s->pX, s->pM, n, s->pQ, beta);
+        combine(s->pX, s->pM, n, beta, x, -1.0, x);
     }
     orc_spmv(&s->ctx->Kpi, x, s->pQ);
     const double nn = dotn(x, s->pQ, n);

@@ -121,6 +121,30 @@ def test_fastconv(setup, torch_cuda):
     assert np.max(np.abs(A.cpu().numpy() - ref)) <= 1e-13 * np.max(np.abs(ref))
 
 
+def test_fastconv_mixed(setup, torch_cuda):
+    """FP32 FastConvection values, FP64 vectors and sums: within the FP32 rounding of I's values
+    (2^-24 relative per entry) of the FP64 oracle, and equal to the FP64 product of the
+    FP32-rounded matrix up to FP64 summation order."""
+    G, O, mesh, ctx, om, oc = setup
+    t = torch_cuda
+    rng = np.random.default_rng(4)
+    u = rng.uniform(-1, 1.5, 2 * ctx.N)
+    Ih = ctx.matrix("I")
+    I32 = G.CsrF.from_host(Ih, dtype=G.NSF_F32)
+    K = t.tensor(ctx.matrix("K").values, device="cuda")
+    A = t.zeros_like(K)
+    G.fastconv_apply_mixed(I32, K, 1e-3, t.tensor(u, device="cuda"), A)
+    got = A.cpu().numpy()
+    ref = O.fastconv(oc, 1e-3, u)
+    # |sum_j (I_kj rounded) u_j - sum_j I_kj u_j| <= 2^-24 sum_j |I_kj u_j|
+    rs, ci, iv = np.asarray(Ih.rowStart), np.asarray(Ih.column), np.asarray(Ih.values)
+    bound = np.add.reduceat(np.abs(iv * u[ci]), rs[:-1]) * 2.0 ** -24
+    assert np.all(np.abs(got - ref) <= bound + 1e-14 * np.max(np.abs(ref)))
+    iv32 = iv.astype(np.float32).astype(np.float64)
+    exact32 = 1e-3 * ctx.matrix("K").values + np.add.reduceat(iv32 * u[ci], rs[:-1])
+    assert np.max(np.abs(got - exact32)) <= 1e-13 * np.max(np.abs(ref))
+
+
 def test_pcg_pressure_matches_oracle(setup, torch_cuda):
     G, O, mesh, ctx, om, oc = setup
     t = torch_cuda
