@@ -892,26 +892,26 @@ def bench_ours(args, rank, world, local_rank):
         del e2e
 
         # ---- dominant kernel alone: FastConvection SpMV (I: nnz(K) x 2N) fused with the nu K add
-        # (the mixed stepper's instantiation: FP32 values of I, FP64 u, K, A and sums)
+        # (the mixed stepper's kernel: FP32 values of I; u, K, A and the sums as double-floats)
         Ih = ctx.matrix("I")
         Kh = ctx.matrix("K")
         I32 = G.CsrF.from_host(Ih, dtype=G.NSF_F32)
-        u64 = torch.tensor(u_m, dtype=torch.float64, device="cuda")
-        K64 = torch.tensor(Kh.values, dtype=torch.float64, device="cuda")
-        A64 = torch.zeros_like(K64)
+        u2 = G.split_df(torch.tensor(u_m, dtype=torch.float64, device="cuda"))
+        K2 = G.split_df(torch.tensor(Kh.values, dtype=torch.float64, device="cuda"))
+        A2 = torch.zeros_like(K2)
         reps = 20
         with torch.cuda.stream(stream):
             for _ in range(3):
-                G.fastconv_apply_mixed(I32, K64, NU, u64, A64, sp)
+                G.fastconv_apply_df(I32, K2, NU, u2, A2, sp)
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             e0.record(stream)
             for _ in range(reps):
-                G.fastconv_apply_mixed(I32, K64, NU, u64, A64, sp)
+                G.fastconv_apply_df(I32, K2, NU, u2, A2, sp)
             e1.record(stream)
             torch.cuda.synchronize()
         t_fc = e0.elapsed_time(e1) / 1e3 / reps
         nnzI, rowsI = Ih.nnz, Ih.rows
-        # values + column indices of I, row starts, u once (FP64), K read and A written (FP64)
+        # values + column indices of I, row starts, u once, K read and A written (8-byte pairs)
         fc_bytes = nnzI * (4 + 4) + (rowsI + 1) * 4 + 2 * N * 8 + 2 * rowsI * 8
 
         # ---- dominant kernel: the cluster-resident pressure PCG (FP32 inner solve of the
@@ -996,8 +996,8 @@ def bench_ours(args, rank, world, local_rank):
                          "note": "vectors and matrix live in shared memory across the cluster; the kernel is "
                                  "bound by barrier/gather latency, not HBM (ncu DRAM traffic per launch is "
                                  "~1% of the algorithmic bytes)"},
-            "roofline_fastconv": {"bound": "hbm", "kernel": "kFastConvSell<float, double, double, double> (A = nu K + I u, FP32 I values, FP64 "
-                                                "u, K, A and sums, SELL-32-256)",
+            "roofline_fastconv": {"bound": "hbm", "kernel": "kFastConvSellDf (A = nu K + I u, FP32 I values; u, K, A and sums as "
+                                                "double-floats, SELL-32-256)",
                                   "achieved": round(achieved, 1), "peak": hbm, "unit": "GB/s",
                                   "frac": round(achieved / hbm, 4), "peak_kind": kind,
                                   "algorithmic_bytes": fc_bytes, "launch_us": round(t_fc * 1e6, 2)},

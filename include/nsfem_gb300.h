@@ -114,12 +114,13 @@ int nsf_spmm(nsf_csr a, int nrhs, const void *X, int ldx, void *Y, int ldy, void
 /* Avals = nu * Kvals + I u, the linearised advection update fused with the diffusion add.
    Replaces fcSpmv.compute + cublasSgeam (cpp/execs/NavierStokes/src/chorinCuda.cu:243-250). */
 int nsf_fastconv_apply(nsf_csr I, const void *Kvals, double nu, const void *u, void *Avals, void *stream);
-/* The same with FP32 operator values and FP64 vectors and sums (I of dtype NSF_F32; Kvals, u and
-   Avals FP64): the FastConvection product of the mixed-precision stepper.  The matrix traffic is
-   FP32; the sums and A stay FP64 because A u feeds the divergence, which would amplify rounding
-   noise that changes from step to step.  Replaces the same reference calls as nsf_fastconv_apply. */
-int nsf_fastconv_apply_mixed(nsf_csr I, const double *Kvals, double nu, const double *u, double *Avals,
-                             void *stream);
+/* The same with FP32 operator values and double-float vectors and sums: Kvals, u and Avals hold
+   (hi, lo) float pairs (value = hi + lo, about 48 significant bits), 2 floats per entry; I has
+   dtype NSF_F32.  The FastConvection product of the mixed-precision stepper: the matrix traffic is
+   FP32 and the arithmetic runs on the FP32 pipes, while A keeps the precision that the divergence
+   needs (it amplifies rounding noise that changes from step to step).  Replaces the same
+   reference calls as nsf_fastconv_apply. */
+int nsf_fastconv_apply_df(nsf_csr I, const float *Kvals, double nu, const float *u, float *Avals, void *stream);
 
 /* Largest nrhs nsf_residual_noalloc accepts (its scratch is sized for it). */
 #define NSF_NOALLOC_MAX_RHS 4

@@ -65,7 +65,7 @@ _SIGS = {
     "nsf_spmv": (C.c_int, [vp, vp, vp, C.c_double, C.c_double, vp]),
     "nsf_spmm": (C.c_int, [vp, C.c_int, vp, C.c_int, vp, C.c_int, vp]),
     "nsf_fastconv_apply": (C.c_int, [vp, vp, C.c_double, vp, vp, vp]),
-    "nsf_fastconv_apply_mixed": (C.c_int, [vp, vp, C.c_double, vp, vp, vp]),
+    "nsf_fastconv_apply_df": (C.c_int, [vp, vp, C.c_double, vp, vp, vp]),
     "nsf_residual_noalloc": (C.c_int, [vp, C.c_int, vp, vp, vp, vp, vp]),
     "nsf_solver_create": (C.c_int, [C.c_char_p, C.c_int, C.c_int, i32p, i32p, f64p, C.c_int, C.c_int, C.c_double,
                                     C.c_int, C.POINTER(vp)]),

@@ -210,11 +210,24 @@ def fastconv_apply(I: CsrF, K_values, nu: float, u, A_values, stream=None):
     return A_values
 
 
-def fastconv_apply_mixed(I: CsrF, K_values, nu: float, u, A_values, stream=None):
-    """A = nu * K + I u with I in FP32 and K, u, A (and the sums) in FP64: the mixed stepper's
-    FastConvection product."""
-    check(lib().nsf_fastconv_apply_mixed(I._h, _dptr(K_values), nu, _dptr(u), _dptr(A_values), vp(stream)))
+def fastconv_apply_df(I: CsrF, K_values, nu: float, u, A_values, stream=None):
+    """A = nu * K + I u with I in FP32 and K, u, A (and the sums) as double-floats: float32 device
+    tensors of shape (n, 2) holding (hi, lo), value = hi + lo.  The mixed stepper's FastConvection
+    product."""
+    check(lib().nsf_fastconv_apply_df(I._h, _dptr(K_values), nu, _dptr(u), _dptr(A_values), vp(stream)))
     return A_values
+
+
+def split_df(x):
+    """(n, 2) float32 (hi, lo) pairs of an FP64 array (numpy or torch), value = hi + lo."""
+    if isinstance(x, np.ndarray):
+        hi = x.astype(np.float32)
+        lo = (x - hi.astype(np.float64)).astype(np.float32)
+        return np.stack([hi, lo], axis=1)
+    import torch
+    hi = x.float()
+    lo = (x - hi.double()).float()
+    return torch.stack([hi, lo], dim=1).contiguous()
 
 
 class Spmv:
@@ -509,6 +522,6 @@ class Adjoint:
 
 
 __all__ = ["Mesh", "load_gmsh", "ChorinContext", "build_chorin_context", "coloring", "CsrF", "Spmv", "Spmm",
-           "spmv", "spmm", "fastconv_apply", "fastconv_apply_mixed", "AbstractSolver", "create_solver", "ChorinStepper", "kernel_launches",
+           "spmv", "spmm", "fastconv_apply", "fastconv_apply_df", "split_df", "AbstractSolver", "create_solver", "ChorinStepper", "kernel_launches",
            "Forces", "Adjoint", "Pack", "NSF_F32", "NSF_F64", "NSF_PREC_F64", "NSF_PREC_MIXED", "NSF_PREC_F64_MIXEDSOLVE",
            "NsfError"]

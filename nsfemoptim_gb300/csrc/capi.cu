@@ -200,6 +200,34 @@ namespace nsf
         double dratio = 1.0; // max / min of diag(M): the 2-norm factor of the D-scaled error bound
         DevBuf<double> r, d0, d1, scratch;
         DevBuf<SolverState> st;
+        // double-float iterations (enableDoubleFloat): the SELL values, D^-1 and the vectors as
+        // (hi, lo) float pairs, so the iterations run on the FP32 pipes at about 48-bit precision
+        bool df = false;
+        DevBuf<float2> vDf, invDDf, xDf, rDf, dDf0, dDf1;
+
+        static float2 split(double v)
+        {
+            const float hi = (float)v;
+            return make_float2(hi, (float)(v - (double)hi));
+        }
+
+        void enableDoubleFloat()
+        {
+            df = true;
+            const std::vector<double> hv = sell->v.download(), hd = sys->invD.download();
+            std::vector<float2> sv(hv.size()), sd(hd.size());
+            for (size_t i = 0; i < hv.size(); i++)
+                sv[i] = split(hv[i]);
+            for (size_t i = 0; i < hd.size(); i++)
+                sd[i] = split(hd[i]);
+            vDf.upload(sv);
+            invDDf.upload(sd);
+            const size_t n2 = 2 * (size_t)sys->n;
+            xDf.alloc(n2);
+            rDf.alloc(n2);
+            dDf0.alloc(n2);
+            dDf1.alloc(n2);
+        }
 
         void setup(const SweepSystem<double> * s, const DevSell<double> * sl, int channels)
         {
@@ -238,18 +266,39 @@ namespace nsf
             NSF_LAUNCH(kSetConfig, 1, s, st.get(), maxIters, 0, tol * tol);
             const double theta = 0.5 * (kMassSpecHi + kMassSpecLo), delta = 0.5 * (kMassSpecHi - kMassSpecLo);
             const double sigma = theta / delta;
-            NSF_LAUNCH((kChebStart<2>), blocksFor(n), s, n, b, sys->invD.get(), 1.0 / theta, r.get(), d0.get());
             double rho = 1.0 / sigma;
-            double * dc = d0.get();
-            double * dn = d1.get();
-            for (int it = 0; it < k; it++)
+            if (df)
             {
-                const double rhoN = 1.0 / (2.0 * sigma - rho);
-                NSF_LAUNCH((kChebStep<2>), sell->blocks(), s, n, sell->nSlices, sell->ss.get(), sell->perm.get(),
-                           sell->ci.get(), sell->v.get(), sys->invD.get(), (const double *)dc, dn, x, r.get(),
-                           rhoN * rho, 2.0 * rhoN / delta);
-                rho = rhoN;
-                std::swap(dc, dn);
+                NSF_LAUNCH((kChebStartDf<2>), blocksFor(n), s, n, b, (const float2 *)invDDf.get(), split(1.0 / theta),
+                           rDf.get(), dDf0.get(), xDf.get());
+                float2 * dc = dDf0.get();
+                float2 * dn = dDf1.get();
+                for (int it = 0; it < k; it++)
+                {
+                    const double rhoN = 1.0 / (2.0 * sigma - rho);
+                    NSF_LAUNCH((kChebStepDf<2>), sell->blocks(), s, n, sell->nSlices, sell->ss.get(),
+                               sell->perm.get(), sell->ci.get(), (const float2 *)vDf.get(),
+                               (const float2 *)invDDf.get(), (const float2 *)dc, dn, xDf.get(), rDf.get(),
+                               split(rhoN * rho), split(2.0 * rhoN / delta));
+                    rho = rhoN;
+                    std::swap(dc, dn);
+                }
+                NSF_LAUNCH(kDfToDouble, blocksFor(2ll * n), s, 2ll * n, (const float2 *)xDf.get(), x);
+            }
+            else
+            {
+                NSF_LAUNCH((kChebStart<2>), blocksFor(n), s, n, b, sys->invD.get(), 1.0 / theta, r.get(), d0.get());
+                double * dc = d0.get();
+                double * dn = d1.get();
+                for (int it = 0; it < k; it++)
+                {
+                    const double rhoN = 1.0 / (2.0 * sigma - rho);
+                    NSF_LAUNCH((kChebStep<2>), sell->blocks(), s, n, sell->nSlices, sell->ss.get(),
+                               sell->perm.get(), sell->ci.get(), sell->v.get(), sys->invD.get(), (const double *)dc,
+                               dn, x, r.get(), rhoN * rho, 2.0 * rhoN / delta);
+                    rho = rhoN;
+                    std::swap(dc, dn);
+                }
             }
             const SweepSystem<double> & S = *sys;
             NSF_LANES(S.L, NSF_LAUNCH((kChebFinal<LL, 2>), S.fullBlocks(), s, n, S.rsF.get(), S.ciF.get(), S.vF.get(),
@@ -624,15 +673,15 @@ extern "C" int nsf_spmm(nsf_csr a, int nrhs, const void * X, int ldx, void * Y, 
     });
 }
 
-extern "C" int nsf_fastconv_apply_mixed(nsf_csr I, const double * K, double nu, const double * u, double * A,
-                                        void * stream)
+extern "C" int nsf_fastconv_apply_df(nsf_csr I, const float * K, double nu, const float * u, float * A,
+                                     void * stream)
 {
     return guarded([&] {
         require(I && K && u && A, "null argument");
-        require(I->dtype == NSF_F32, "nsf_fastconv_apply_mixed takes an FP32 FastConvection matrix");
+        require(I->dtype == NSF_F32, "nsf_fastconv_apply_df takes an FP32 FastConvection matrix");
         const DevSell<float> & S = I->s32;
-        NSF_LAUNCH((kFastConvSell<float, double, double, double>), S.blocks(), asStream(stream), S.rows, S.nSlices,
-                   S.ss.get(), S.perm.get(), S.ci.get(), S.v.get(), u, K, nu, A);
+        NSF_LAUNCH(kFastConvSellDf, S.blocks(), asStream(stream), S.rows, S.nSlices, S.ss.get(), S.perm.get(),
+                   S.ci.get(), S.v.get(), (const float2 *)u, (const float2 *)K, ChebSolver::split(nu), (float2 *)A);
     });
 }
 
@@ -875,6 +924,7 @@ struct nsf_chorin_s
     // solvers: separate objects for the tentative and the final mass solve keep both stats
     PcgSolver<double, 2> velT, velF;
     ChebSolver chebT, chebF; // velMethod 3 (FP64 Chebyshev-Jacobi on the SELL copy of M)
+    DevBuf<float2> uDf, KDf, ADf; // mixed: u, K and A as double-floats
     DevSell<double> Msell;
     GsSolver<double, 2> gsT, gsF;
     PcgSolver<double, 1> pres;
@@ -941,12 +991,16 @@ struct nsf_chorin_s
         if (mixed)
         {
             const DevSell<float> & IS = I32.sell;
-            NSF_LAUNCH((kFastConvSell<float, double, double, double>), IS.blocks(), s, IS.rows, IS.nSlices,
-                       IS.ss.get(), IS.perm.get(), IS.ci.get(), IS.v.get(), u.get(), K64.get(), cfg.nu, A64.get());
-            // FP32 values, FP64 sums (4.6M FMAs): FP32 sums would put step-to-step rounding noise into
-            // u, which the divergence amplifies in the pressure right-hand side
-            NSF_LANES(M32.L, NSF_LAUNCH((kSpmm<double, double, double, double, LL, 2>), blocksFor((long long)N * M32.L), s, N,
-                                        M32.rsF.get(), M32.ciF.get(), A64.get(), u.get(), N, rhs.get(), N));
+            // double-float (FP32 pipes, 48 bits) for the products that feed the divergence
+            NSF_LAUNCH(kSplitDf, blocksFor(2ll * N), s, 2ll * N, (const double *)u.get(), uDf.get());
+            NSF_LAUNCH(kFastConvSellDf, IS.blocks(), s, IS.rows, IS.nSlices, IS.ss.get(), IS.perm.get(), IS.ci.get(),
+                       IS.v.get(), (const float2 *)uDf.get(), (const float2 *)KDf.get(), ChebSolver::split(cfg.nu),
+                       ADf.get());
+            // double-float sums: FP32 sums would put step-to-step rounding noise into u, which the
+            // divergence amplifies in the pressure right-hand side
+            NSF_LANES(M32.L, NSF_LAUNCH((kSpmmDf<LL, 2>), blocksFor((long long)N * M32.L), s, N, M32.rsF.get(),
+                                        M32.ciF.get(), (const float2 *)ADf.get(), (const float2 *)uDf.get(), N,
+                                        rhs.get(), N));
         }
         else
         {
@@ -1119,6 +1173,13 @@ static void buildChorin(nsf_chorin_s & S, const Context & c)
         S.Msell.build(N, Mp.rowStart.data(), Mp.col.data(), Mp.val.data());
         S.chebT.setup(&S.M64, &S.Msell, 2);
         S.chebF.setup(&S.M64, &S.Msell, 2);
+        if (S.mixed)
+        {
+            // the mixed stepper iterates in double-float on the FP32 pipes (48 bits: the rounding
+            // of the mass solves stays far below their tolerance)
+            S.chebT.enableDoubleFloat();
+            S.chebF.enableDoubleFloat();
+        }
     }
     S.Kpi64.build(Kpip, cp.partStart);
     std::vector<double> knu(Kp.val.begin(), Kp.val.end());
@@ -1130,8 +1191,12 @@ static void buildChorin(nsf_chorin_s & S, const Context & c)
         S.I32.upload(Ip, true);
         S.D32.upload(Dp);
         S.G32.upload(Gp);
-        S.K64.upload(knu);
-        S.A64.alloc(knu.size());
+        std::vector<float2> kdf(knu.size());
+        for (size_t i = 0; i < knu.size(); i++)
+            kdf[i] = ChebSolver::split(knu[i]);
+        S.KDf.upload(kdf);
+        S.ADf.alloc(knu.size());
+        S.uDf.alloc(2 * (size_t)N);
         if (!cheb)
         {
             S.mvelT.setup(&S.M64, &S.M32, 2, kMassIters);

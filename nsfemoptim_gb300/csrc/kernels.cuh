@@ -513,6 +513,233 @@ namespace nsf
         }
     }
 
+    // ------------------------------------------------------------------ double-float Chebyshev
+    // A double-float is an unevaluated sum hi + lo of two floats (|lo| <= ulp(hi) / 2): about 48
+    // significant bits computed on the FP32 pipes, which run at 64x the FP64 rate on this GPU.  The
+    // operations are the error-free transformations of Dekker ("A floating-point technique for
+    // extending the available precision", 1971) and Knuth (TAOCP vol. 2, TwoSum); fmaf gives the
+    // exact product error.  Vectors and matrix values are float2 = (hi, lo).
+    __device__ __forceinline__ float2 dfTwoSum(float a, float b)
+    {
+        const float s = a + b, bb = s - a;
+        return make_float2(s, (a - (s - bb)) + (b - bb));
+    }
+
+    __device__ __forceinline__ float2 dfFastTwoSum(float a, float b) // needs |a| >= |b| or a == 0
+    {
+        const float s = a + b;
+        return make_float2(s, b - (s - a));
+    }
+
+    __device__ __forceinline__ float2 dfAdd(float2 a, float2 b)
+    {
+        const float2 s = dfTwoSum(a.x, b.x);
+        return dfFastTwoSum(s.x, s.y + (a.y + b.y));
+    }
+
+    __device__ __forceinline__ float2 dfMul(float2 a, float2 b)
+    {
+        const float p = a.x * b.x;
+        float e = fmaf(a.x, b.x, -p);
+        e = fmaf(a.x, b.y, fmaf(a.y, b.x, e));
+        return dfFastTwoSum(p, e);
+    }
+
+    __device__ __forceinline__ float2 dfNeg(float2 a) { return make_float2(-a.x, -a.y); }
+
+    __device__ __forceinline__ float2 dfFromDouble(double v)
+    {
+        const float hi = (float)v;
+        return make_float2(hi, (float)(v - (double)hi));
+    }
+
+    __device__ __forceinline__ double dfToDouble(float2 a) { return (double)a.x + (double)a.y; }
+
+    // the double-float Chebyshev start: r = b, d = D^-1 b / theta, x = 0 (b and D^-1 from FP64)
+    template <int NCH>
+    __global__ void __launch_bounds__(TPB) kChebStartDf(int n, const double * __restrict__ b,
+                                                         const float2 * __restrict__ invD, float2 invTheta,
+                                                         float2 * __restrict__ r, float2 * __restrict__ d,
+                                                         float2 * __restrict__ x)
+    {
+        for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        {
+            const float2 id = invD[i];
+#pragma unroll
+            for (int c = 0; c < NCH; c++)
+            {
+                const size_t o = (size_t)c * n + i;
+                const float2 bi = dfFromDouble(b[o]);
+                r[o] = bi;
+                d[o] = dfMul(dfMul(bi, id), invTheta);
+                x[o] = make_float2(0.f, 0.f);
+            }
+        }
+    }
+
+    // kChebStep in double-float arithmetic: q = A d; x += d; r -= q; d' = c1 d + c2 D^-1 r
+    template <int NCH>
+    __global__ void __launch_bounds__(TPB) kChebStepDf(int n, int nSlices, const int * __restrict__ ss,
+                                                        const int * __restrict__ perm, const int * __restrict__ ci,
+                                                        const float2 * __restrict__ v, const float2 * __restrict__ invD,
+                                                        const float2 * __restrict__ d, float2 * __restrict__ dn,
+                                                        float2 * __restrict__ x, float2 * __restrict__ r, float2 c1,
+                                                        float2 c2)
+    {
+        const int slice = (int)((blockIdx.x * (unsigned)blockDim.x + threadIdx.x) >> 5);
+        if (slice >= nSlices)
+            return;
+        const int lane = threadIdx.x & 31;
+        const int row = slice * SELL_C + lane;
+        const int b0 = ldg(ss + slice), e0 = ldg(ss + slice + 1);
+        float2 q[NCH];
+#pragma unroll
+        for (int c = 0; c < NCH; c++)
+            q[c] = make_float2(0.f, 0.f);
+        const int w = (e0 - b0) / SELL_C;
+        for (int k = 0; k < w; k += 4)
+        {
+            int cc[4];
+            float2 a[4];
+#pragma unroll
+            for (int t = 0; t < 4; t++)
+            {
+                const bool ok = k + t < w;
+                const int j = b0 + (k + t) * SELL_C + lane;
+                cc[t] = ok ? ldg(ci + j) : 0;
+                a[t] = ok ? ldg(v + j) : make_float2(0.f, 0.f);
+            }
+#pragma unroll
+            for (int c = 0; c < NCH; c++)
+            {
+                float2 g[4];
+#pragma unroll
+                for (int t = 0; t < 4; t++)
+                    g[t] = k + t < w ? ldg(d + (size_t)c * n + cc[t]) : make_float2(0.f, 0.f);
+#pragma unroll
+                for (int t = 0; t < 4; t++)
+                    if (k + t < w)
+                        q[c] = dfAdd(q[c], dfMul(a[t], g[t]));
+            }
+        }
+        if (row >= n)
+            return;
+        const int i = ldg(perm + row);
+        const float2 id = ldg(invD + i);
+#pragma unroll
+        for (int c = 0; c < NCH; c++)
+        {
+            const size_t o = (size_t)c * n + i;
+            const float2 di = d[o];
+            x[o] = dfAdd(x[o], di);
+            const float2 ri = dfAdd(r[o], dfNeg(q[c]));
+            r[o] = ri;
+            dn[o] = dfAdd(dfMul(c1, di), dfMul(c2, dfMul(ri, id)));
+        }
+    }
+
+    // y = (hi, lo) split of an FP64 vector
+    __global__ void __launch_bounds__(TPB) kSplitDf(long long n, const double * __restrict__ x, float2 * __restrict__ y)
+    {
+        for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+            y[i] = dfFromDouble(x[i]);
+    }
+
+    // FastConvection in double-float: A[k] = nu K[k] + sum_j I[k, j] u[j] with FP32 values of I (the
+    // product I_kj u_j of a float and a double-float is formed exactly up to the last bits), u, K, A
+    // and the sums as double-floats.  Same SELL layout and predicated 8-wide load groups as
+    // kFastConvSell.
+    __global__ void __launch_bounds__(TPB) kFastConvSellDf(int rows, int nSlices, const int * __restrict__ ss,
+                                                            const int * __restrict__ perm, const int * __restrict__ ci,
+                                                            const float * __restrict__ iv, const float2 * __restrict__ u,
+                                                            const float2 * __restrict__ k, float2 nu,
+                                                            float2 * __restrict__ a)
+    {
+        const int slice = (int)((blockIdx.x * (unsigned)blockDim.x + threadIdx.x) >> 5);
+        if (slice >= nSlices)
+            return;
+        const int lane = threadIdx.x & 31;
+        const int row = slice * SELL_C + lane;
+        const int b0 = ldg(ss + slice), e0 = ldg(ss + slice + 1);
+        const int w = (e0 - b0) / SELL_C;
+        float2 acc = make_float2(0.f, 0.f);
+        constexpr int U = 8;
+        for (int kk = 0; kk < w; kk += U)
+        {
+            int cc[U];
+            float av[U];
+#pragma unroll
+            for (int t = 0; t < U; t++)
+            {
+                const bool ok = kk + t < w;
+                const int j = b0 + (kk + t) * SELL_C + lane;
+                cc[t] = ok ? ldg(ci + j) : 0;
+                av[t] = ok ? ldg(iv + j) : 0.f;
+            }
+            float2 g[U];
+#pragma unroll
+            for (int t = 0; t < U; t++)
+                g[t] = kk + t < w ? ldg(u + cc[t]) : make_float2(0.f, 0.f);
+#pragma unroll
+            for (int t = 0; t < U; t++)
+            {
+                const float p = av[t] * g[t].x;
+                const float e = fmaf(av[t], g[t].y, fmaf(av[t], g[t].x, -p));
+                acc = dfAdd(acc, dfFastTwoSum(p, e));
+            }
+        }
+        if (row >= rows)
+            return;
+        const int r = ldg(perm + row);
+        a[r] = dfAdd(dfMul(nu, ldg(k + r)), acc);
+    }
+
+    // planar multi-RHS in double-float, FP64 result: Y[c ldy + r] = sum_j A[r, j] X[c ldx + j]
+    template <int L, int NCH>
+    __global__ void __launch_bounds__(TPB) kSpmmDf(int rows, const int * __restrict__ rs, const int * __restrict__ ci,
+                                                    const float2 * __restrict__ v, const float2 * __restrict__ X, int ldx,
+                                                    double * __restrict__ Y, int ldy)
+    {
+        Group<L> g;
+        for (int r = g.gid; r < rows; r += g.ngroups)
+        {
+            const int b = ldg(rs + r), e = ldg(rs + r + 1);
+            float2 s[NCH];
+#pragma unroll
+            for (int c = 0; c < NCH; c++)
+                s[c] = make_float2(0.f, 0.f);
+            for (int j = b + g.lane; j < e; j += L)
+            {
+                const float2 a = ldg(v + j);
+                const int col = ldg(ci + j);
+#pragma unroll
+                for (int c = 0; c < NCH; c++)
+                    s[c] = dfAdd(s[c], dfMul(a, ldg(X + (size_t)c * ldx + col)));
+            }
+#pragma unroll
+            for (int c = 0; c < NCH; c++)
+            {
+                float2 t = s[c];
+#pragma unroll
+                for (int o = L / 2; o > 0; o >>= 1)
+                {
+                    const float2 other = make_float2(__shfl_down_sync(g.mask, t.x, o, L),
+                                                     __shfl_down_sync(g.mask, t.y, o, L));
+                    t = dfAdd(t, other);
+                }
+                if (g.lane == 0)
+                    Y[(size_t)c * ldy + r] = dfToDouble(t);
+            }
+        }
+    }
+
+    // x64 = hi + lo of the double-float result
+    __global__ void __launch_bounds__(TPB) kDfToDouble(long long n, const float2 * __restrict__ x, double * __restrict__ y)
+    {
+        for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+            y[i] = dfToDouble(x[i]);
+    }
+
     // Initial guess of the pressure solve from the last two solutions: before step k the solve
     // starts from 2 p_{k-1} - p_{k-2} once two solved pressures exist (hist >= 2), else from p_{k-1};
     // prev keeps p_{k-1} for the next step.  kHistBump advances the count afterwards (separate

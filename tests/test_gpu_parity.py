@@ -121,28 +121,31 @@ def test_fastconv(setup, torch_cuda):
     assert np.max(np.abs(A.cpu().numpy() - ref)) <= 1e-13 * np.max(np.abs(ref))
 
 
-def test_fastconv_mixed(setup, torch_cuda):
-    """FP32 FastConvection values, FP64 vectors and sums: within the FP32 rounding of I's values
-    (2^-24 relative per entry) of the FP64 oracle, and equal to the FP64 product of the
-    FP32-rounded matrix up to FP64 summation order."""
+def test_fastconv_df(setup, torch_cuda):
+    """FP32 FastConvection values with double-float vectors and sums (the mixed stepper's product):
+    within the FP32 rounding of I's values (2^-24 relative per entry) of the FP64 oracle, and equal to
+    the FP64 product of the FP32-rounded matrix to double-float precision (1e-12 relative)."""
     G, O, mesh, ctx, om, oc = setup
     t = torch_cuda
     rng = np.random.default_rng(4)
     u = rng.uniform(-1, 1.5, 2 * ctx.N)
     Ih = ctx.matrix("I")
+    Kv = np.asarray(ctx.matrix("K").values)
     I32 = G.CsrF.from_host(Ih, dtype=G.NSF_F32)
-    K = t.tensor(ctx.matrix("K").values, device="cuda")
-    A = t.zeros_like(K)
-    G.fastconv_apply_mixed(I32, K, 1e-3, t.tensor(u, device="cuda"), A)
-    got = A.cpu().numpy()
+    K2 = t.tensor(G.split_df(Kv), device="cuda")
+    u2 = t.tensor(G.split_df(u), device="cuda")
+    A2 = t.zeros_like(K2)
+    G.fastconv_apply_df(I32, K2, 1e-3, u2, A2)
+    a = A2.cpu().numpy().astype(np.float64)
+    got = a[:, 0] + a[:, 1]
     ref = O.fastconv(oc, 1e-3, u)
     # |sum_j (I_kj rounded) u_j - sum_j I_kj u_j| <= 2^-24 sum_j |I_kj u_j|
     rs, ci, iv = np.asarray(Ih.rowStart), np.asarray(Ih.column), np.asarray(Ih.values)
     bound = np.add.reduceat(np.abs(iv * u[ci]), rs[:-1]) * 2.0 ** -24
     assert np.all(np.abs(got - ref) <= bound + 1e-14 * np.max(np.abs(ref)))
     iv32 = iv.astype(np.float32).astype(np.float64)
-    exact32 = 1e-3 * ctx.matrix("K").values + np.add.reduceat(iv32 * u[ci], rs[:-1])
-    assert np.max(np.abs(got - exact32)) <= 1e-13 * np.max(np.abs(ref))
+    exact32 = 1e-3 * Kv + np.add.reduceat(iv32 * u[ci], rs[:-1])
+    assert np.max(np.abs(got - exact32)) <= 1e-12 * np.max(np.abs(ref))
 
 
 def test_pcg_pressure_matches_oracle(setup, torch_cuda):
