@@ -50,7 +50,8 @@ def peaks():
 
 PRESSURE_GUESSES = {0: "previous solution", 1: "2 p(n-1) - p(n-2)",
                     2: "projection onto <= {} earlier solutions, Kp_int-orthonormal (Fischer 1998)"}
-MASS_SOLVES = {1: "PCG, multicolor SGS", 2: "PCG, Jacobi", 3: "Chebyshev, Jacobi (a priori iteration count)"}
+MASS_SOLVES = {1: "PCG, multicolor SGS", 2: "PCG, Jacobi", 3: "Chebyshev, Jacobi (a priori iteration count)",
+               4: "Chebyshev, Jacobi, from the previous step's solution (a priori count from the initial residual)"}
 
 
 def make_mesh(tmpdir: str, h: float, seed: int = 0) -> str:
@@ -1031,9 +1032,9 @@ def main():
                     help="channel: the h=0.005 time step (default); poisson: the standalone 1M-DOF pressure "
                          "solve; small: the plain FP64 h=0.02 channel; batch: 64 instances at h=0.01; "
                          "adjoint: the drag gradient at h=0.01 over 1000 steps")
-    ap.add_argument("--vel-method", type=int, default=3, choices=[1, 2, 3],
+    ap.add_argument("--vel-method", type=int, default=3, choices=[1, 2, 3, 4],
                     help="channel, batch, pack and long workloads: mass solve, 1 PCG multicolor SGS, 2 PCG "
-                         "Jacobi, 3 Chebyshev Jacobi")
+                         "Jacobi, 3 Chebyshev Jacobi, 4 the same warm-started from the previous step")
     ap.add_argument("--pressure-basis", type=int, default=0,
                     help="pressure guess 2: basis vectors (3..256; 0: 250)")
     ap.add_argument("--pressure-guess", type=int, default=2, choices=[0, 1, 2],

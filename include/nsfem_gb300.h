@@ -184,8 +184,12 @@ typedef struct
                              iteration is one parallel phase), 3: Chebyshev iteration with the
                              Jacobi preconditioner over the spectral bounds [0.39237, 2.05982] of
                              D^-1 M (those of every affine P2 element), the iteration count fixed
-                             in advance from velTol (relative); FP64 in every precision mode, one
-                             kernel per iteration, no reductions but the final residual check */
+                             in advance from velTol (relative); one kernel per iteration, no
+                             reductions but the final residual check; FP64, or double-float (float
+                             pairs on the FP32 pipes) in NSF_PREC_MIXED; 4: the same started from
+                             the previous step's solution of that solve, the count set on the
+                             device from the initial residual (at most the count of 3); a channel
+                             whose previous solution is no better a start than 0 starts cold */
     int velMaxIters;
     double velTol;
     int presMaxIters;

@@ -358,7 +358,8 @@ class ChorinStepper:
                  pres_max_iters: int = 2000, pres_tol: float = 1e-10, check_interval: int = 8,
                  use_graph: bool = True, max_outer: int = 4, inner_tol: float = 1e-4, pressure_guess: int = 0,
                  pressure_basis: int = 0):
-        """vel_method: mass solve, 0 multicolor GS, 1 PCG-SGS, 2 PCG-Jacobi, 3 Chebyshev-Jacobi.
+        """vel_method: mass solve, 0 multicolor GS, 1 PCG-SGS, 2 PCG-Jacobi, 3 Chebyshev-Jacobi,
+        4 Chebyshev-Jacobi warm-started from the previous step's solution.
         pressure_guess: 0 the previous pressure (as the reference), 1 extrapolated from the last two,
         2 projected onto up to pressure_basis earlier solutions (0: 250)."""
         self.ctx = ctx

@@ -312,7 +312,7 @@ struct nsf_adjoint_s
             st[1] = S->mpres.st.get();
             st[2] = S->mvelF.st.get();
         }
-        if (S->cfg.velMethod == 3)
+        if (S->cfg.velMethod >= 3)
         {
             st[0] = S->chebT.st.get();
             st[2] = S->chebF.st.get();
@@ -492,6 +492,8 @@ extern "C" int nsf_adjoint_create(nsf_chorin S, nsf_forces f, const nsf_adjoint_
         require(!S->mixed, "the adjoint needs FP64 operators (precision NSF_PREC_F64 or NSF_PREC_F64_MIXEDSOLVE)");
         require(!S->extrapolate && !S->project,
                 "the adjoint's checkpoints hold (u, p) only: create the stepper with pressureGuess 0");
+        require(S->cfg.velMethod != 4,
+                "the adjoint's checkpoints hold (u, p) only: warm-started mass solves (velMethod 4) are not supported");
         auto a = std::make_unique<nsf_adjoint_s>();
         if (cfg)
             a->cfg = *cfg;
@@ -536,7 +538,7 @@ extern "C" int nsf_adjoint_create(nsf_chorin S, nsf_forces f, const nsf_adjoint_
         a->tally = DevBuf<int>(6);
         a->finU.alloc(twoN);
         a->finP.alloc(nI);
-        if (S->cfg.velMethod == 3)
+        if (S->cfg.velMethod >= 3)
             a->cmass.setup(&S->M64, &S->Msell, 2);
         else if (S->mixedSolve)
             a->mmass.setup(&S->M64, &S->M32, 2);

@@ -204,6 +204,7 @@ namespace nsf
         // (hi, lo) float pairs, so the iterations run on the FP32 pipes at about 48-bit precision
         bool df = false;
         DevBuf<float2> vDf, invDDf, xDf, rDf, dDf0, dDf1;
+        DevBuf<int> kw; // warm solves: the device count and the per-channel warm flags
 
         static float2 split(double v)
         {
@@ -240,6 +241,7 @@ namespace nsf
             d1.alloc(2 * n);
             scratch.alloc((size_t)2 * MAXCH * cappedBlocks(1ll << 40));
             st.alloc(1);
+            kw.alloc(1 + MAXCH);
             const std::vector<double> dg = s->diag.download();
             double lo = 1e300, hi = 0;
             for (double v : dg)
@@ -259,18 +261,37 @@ namespace nsf
             return std::max(1, (int)std::ceil(std::log(target) / std::log(rho)));
         }
 
-        // x must be 0 on entry (the mass solves of the step start from zero)
-        void enqueue(cudaStream_t s, const double * b, double * x, int maxIters, double tol)
+        // warm == false: x must be 0 on entry, and the count is the a priori one for x0 = 0.
+        // warm == true (mass-solve method 4): x holds the previous step's solution of this solve;
+        // a device kernel decides per channel whether it is a better start than 0 and sets the
+        // count from the initial residual (at most the cold count); the iterations past it exit
+        // at once.
+        void enqueue(cudaStream_t s, const double * b, double * x, int maxIters, double tol, bool warm = false)
         {
             const int n = sys->n, k = std::min(maxIters, itersFor(tol));
+            const SweepSystem<double> & S = *sys;
             NSF_LAUNCH(kSetConfig, 1, s, st.get(), maxIters, 0, tol * tol);
             const double theta = 0.5 * (kMassSpecHi + kMassSpecLo), delta = 0.5 * (kMassSpecHi - kMassSpecLo);
             const double sigma = theta / delta;
             double rho = 1.0 / sigma;
+            const int * kdev = nullptr;
+            if (warm)
+            {
+                const double kappa = kMassSpecHi / kMassSpecLo;
+                const double lnRho = std::log((std::sqrt(kappa) - 1.0) / (std::sqrt(kappa) + 1.0));
+                const ChebWarmEpi epi{st.get(), kw.get(), numCh, k, std::log(tol / (2.0 * std::sqrt(dratio))), lnRho};
+                NSF_LANES(S.L, NSF_LAUNCH((kChebWarmResidual<LL, 2>), S.fullBlocks(), s, n, S.rsF.get(), S.ciF.get(),
+                                          S.vF.get(), (const double *)x, b, r.get(), st.get(), scratch.get(), epi));
+                kdev = kw.get();
+            }
             if (df)
             {
-                NSF_LAUNCH((kChebStartDf<2>), blocksFor(n), s, n, b, (const float2 *)invDDf.get(), split(1.0 / theta),
-                           rDf.get(), dDf0.get(), xDf.get());
+                if (warm)
+                    NSF_LAUNCH((kChebWarmInitDf<2>), blocksFor(n), s, n, b, (const double *)x, (const double *)r.get(),
+                               (const float2 *)invDDf.get(), split(1.0 / theta), kdev, xDf.get(), rDf.get(), dDf0.get());
+                else
+                    NSF_LAUNCH((kChebStartDf<2>), blocksFor(n), s, n, b, (const float2 *)invDDf.get(),
+                               split(1.0 / theta), rDf.get(), dDf0.get(), xDf.get());
                 float2 * dc = dDf0.get();
                 float2 * dn = dDf1.get();
                 for (int it = 0; it < k; it++)
@@ -279,7 +300,7 @@ namespace nsf
                     NSF_LAUNCH((kChebStepDf<2>), sell->blocks(), s, n, sell->nSlices, sell->ss.get(),
                                sell->perm.get(), sell->ci.get(), (const float2 *)vDf.get(),
                                (const float2 *)invDDf.get(), (const float2 *)dc, dn, xDf.get(), rDf.get(),
-                               split(rhoN * rho), split(2.0 * rhoN / delta));
+                               split(rhoN * rho), split(2.0 * rhoN / delta), kdev, it);
                     rho = rhoN;
                     std::swap(dc, dn);
                 }
@@ -287,7 +308,12 @@ namespace nsf
             }
             else
             {
-                NSF_LAUNCH((kChebStart<2>), blocksFor(n), s, n, b, sys->invD.get(), 1.0 / theta, r.get(), d0.get());
+                if (warm)
+                    NSF_LAUNCH((kChebWarmInit<2>), blocksFor(n), s, n, b, sys->invD.get(), 1.0 / theta, kdev, x, r.get(),
+                               d0.get());
+                else
+                    NSF_LAUNCH((kChebStart<2>), blocksFor(n), s, n, b, sys->invD.get(), 1.0 / theta, r.get(),
+                               d0.get());
                 double * dc = d0.get();
                 double * dn = d1.get();
                 for (int it = 0; it < k; it++)
@@ -295,14 +321,13 @@ namespace nsf
                     const double rhoN = 1.0 / (2.0 * sigma - rho);
                     NSF_LAUNCH((kChebStep<2>), sell->blocks(), s, n, sell->nSlices, sell->ss.get(),
                                sell->perm.get(), sell->ci.get(), sell->v.get(), sys->invD.get(), (const double *)dc,
-                               dn, x, r.get(), rhoN * rho, 2.0 * rhoN / delta);
+                               dn, x, r.get(), rhoN * rho, 2.0 * rhoN / delta, kdev, it);
                     rho = rhoN;
                     std::swap(dc, dn);
                 }
             }
-            const SweepSystem<double> & S = *sys;
             NSF_LANES(S.L, NSF_LAUNCH((kChebFinal<LL, 2>), S.fullBlocks(), s, n, S.rsF.get(), S.ciF.get(), S.vF.get(),
-                                      (const double *)x, b, st.get(), scratch.get(), numCh, k));
+                                      (const double *)x, b, st.get(), scratch.get(), numCh, k, kdev));
         }
     };
 
@@ -925,6 +950,7 @@ struct nsf_chorin_s
     PcgSolver<double, 2> velT, velF;
     ChebSolver chebT, chebF; // velMethod 3 (FP64 Chebyshev-Jacobi on the SELL copy of M)
     DevBuf<float2> uDf, KDf, ADf; // mixed: u, K and A as double-floats
+    DevBuf<double> accT, accF;    // velMethod 4: the last tentative and final mass-solve solutions
     DevSell<double> Msell;
     GsSolver<double, 2> gsT, gsF;
     PcgSolver<double, 1> pres;
@@ -969,9 +995,17 @@ struct nsf_chorin_s
             cudaStreamDestroy(stream);
     }
 
-    void enqueueMassSolve(cudaStream_t s, bool tentative)
+    // returns the buffer that holds the solution
+    double * enqueueMassSolve(cudaStream_t s, bool tentative)
     {
         double * b = rhs.get();
+        if (cfg.velMethod == 4)
+        {
+            // warm start from this solve's solution of the previous step (kept in accT / accF)
+            double * x = tentative ? accT.get() : accF.get();
+            (tentative ? chebT : chebF).enqueue(s, b, x, cfg.velMaxIters, cfg.velTol, true);
+            return x;
+        }
         double * x = acc.get();
         NSF_CUDA(cudaMemsetAsync(x, 0, sizeof(double) * 2 * N, s));
         if (cfg.velMethod == 3)
@@ -983,6 +1017,7 @@ struct nsf_chorin_s
             (tentative ? gsT : gsF).enqueue(s, body, b, x, cfg.velMaxIters, cfg.velTol, false, cfg.checkInterval);
         else
             (tentative ? velT : velF).enqueue(s, body, b, x, cfg.velMaxIters, cfg.velTol, false, cfg.checkInterval);
+        return x;
     }
 
     void enqueueStep(cudaStream_t s)
@@ -1011,9 +1046,8 @@ struct nsf_chorin_s
                                         M64.rsF.get(), M64.ciF.get(), A64.get(), u.get(), N, rhs.get(), N));
         }
         // 2. M acc = rhs ; u = u - tau acc ; Dirichlet
-        enqueueMassSolve(s, true);
-        NSF_LAUNCH(kUpdateVelocity<double>, blocksFor(N), s, N, u.get(), acc.get(), cfg.tau, isDir.get(),
-                   dirVal.get());
+        const double * accT1 = enqueueMassSolve(s, true);
+        NSF_LAUNCH(kUpdateVelocity<double>, blocksFor(N), s, N, u.get(), accT1, cfg.tau, isDir.get(), dirVal.get());
         // 3. rhsP = -(1/tau) D u ; Kpi pInt = rhsP (warm start)
         const double invTau = -1.0 / cfg.tau;
         if (extrapolate)
@@ -1049,9 +1083,8 @@ struct nsf_chorin_s
         if (project)
             proj.update(s, pInt.get());
         // 4. M acc = G p ; u = u - tau acc ; Dirichlet
-        enqueueMassSolve(s, false);
-        NSF_LAUNCH(kUpdateVelocity<double>, blocksFor(N), s, N, u.get(), acc.get(), cfg.tau, isDir.get(),
-                   dirVal.get());
+        const double * accF1 = enqueueMassSolve(s, false);
+        NSF_LAUNCH(kUpdateVelocity<double>, blocksFor(N), s, N, u.get(), accF1, cfg.tau, isDir.get(), dirVal.get());
     }
 
     void collectStats(cudaStream_t s)
@@ -1071,7 +1104,7 @@ struct nsf_chorin_s
             src[1] = pres.st.get();
             src[2] = cfg.velMethod == 0 ? gsF.st.get() : velF.st.get();
         }
-        if (cfg.velMethod == 3)
+        if (cfg.velMethod >= 3)
         {
             src[0] = chebT.st.get();
             src[2] = chebF.st.get();
@@ -1164,7 +1197,7 @@ static void buildChorin(nsf_chorin_s & S, const Context & c)
     // velMethod 2: the mass systems as one color, which turns the SGS preconditioner of the PCG
     // kernels into Jacobi (the forward phase of a single color gathers nothing): one parallel phase
     // per iteration instead of 2C - 1 color phases
-    const bool cheb = S.cfg.velMethod == 3;
+    const bool cheb = S.cfg.velMethod >= 3;
     const std::vector<int> mParts = S.cfg.velMethod >= 2 ? std::vector<int>{0, N} : cv.partStart;
     S.M64.build(Mp, mParts);
     if (cheb)
@@ -1173,6 +1206,13 @@ static void buildChorin(nsf_chorin_s & S, const Context & c)
         S.Msell.build(N, Mp.rowStart.data(), Mp.col.data(), Mp.val.data());
         S.chebT.setup(&S.M64, &S.Msell, 2);
         S.chebF.setup(&S.M64, &S.Msell, 2);
+        if (S.cfg.velMethod == 4)
+        {
+            S.accT = DevBuf<double>(2 * (size_t)N);
+            S.accF = DevBuf<double>(2 * (size_t)N);
+            NSF_CUDA(cudaMemset(S.accT.get(), 0, sizeof(double) * 2 * N));
+            NSF_CUDA(cudaMemset(S.accF.get(), 0, sizeof(double) * 2 * N));
+        }
         if (S.mixed)
         {
             // the mixed stepper iterates in double-float on the FP32 pipes (48 bits: the rounding
@@ -1280,9 +1320,9 @@ extern "C" int nsf_chorin_create(nsf_context ctx, const nsf_chorin_config * cfg,
                 "unknown precision");
         require(!(cfg->precision == NSF_PREC_F64_MIXEDSOLVE && cfg->velMethod == 0),
                 "mixed solves use velMethod 1, 2 (pcg) or 3 (chebyshev)");
-        require(cfg->velMethod >= 0 && cfg->velMethod <= 3,
-                "velMethod must be 0 (gs), 1 (pcg, SGS preconditioner), 2 (pcg, Jacobi preconditioner) or 3 "
-                "(chebyshev, Jacobi preconditioner)");
+        require(cfg->velMethod >= 0 && cfg->velMethod <= 4,
+                "velMethod must be 0 (gs), 1 (pcg, SGS preconditioner), 2 (pcg, Jacobi preconditioner), 3 "
+                "(chebyshev, Jacobi preconditioner) or 4 (the same warm-started from the last step)");
         require(!(cfg->precision == NSF_PREC_MIXED && cfg->velMethod == 0),
                 "mixed precision uses velMethod 1, 2 (pcg) or 3 (chebyshev)");
         require(cfg->velMaxIters >= 1 && cfg->presMaxIters >= 1, "iteration caps must be >= 1");
@@ -1447,6 +1487,11 @@ extern "C" int nsf_chorin_set_state_ex(nsf_chorin S, const double * uIn, const d
             NSF_CUDA(cudaMemsetAsync(S->pHist.get(), 0, sizeof(int), s));
         if (S->project && !keep)
             S->proj.reset(s);
+        if (S->cfg.velMethod == 4 && !keep) // the mass solves start cold again
+        {
+            NSF_CUDA(cudaMemsetAsync(S->accT.get(), 0, sizeof(double) * 2 * N, s));
+            NSF_CUDA(cudaMemsetAsync(S->accF.get(), 0, sizeof(double) * 2 * N, s));
+        }
         NSF_CUDA(cudaStreamSynchronize(s));
     });
 }

@@ -458,10 +458,10 @@ namespace nsf
                                                       const double * __restrict__ v, const double * __restrict__ invD,
                                                       const double * __restrict__ d, double * __restrict__ dn,
                                                       double * __restrict__ x, double * __restrict__ r, double c1,
-                                                      double c2)
+                                                      double c2, const int * kdev, int it)
     {
         const int slice = (int)((blockIdx.x * (unsigned)blockDim.x + threadIdx.x) >> 5);
-        if (slice >= nSlices)
+        if (slice >= nSlices || (kdev && it >= *kdev))
             return;
         const int lane = threadIdx.x & 31;
         const int row = slice * SELL_C + lane;
@@ -584,10 +584,10 @@ namespace nsf
                                                         const float2 * __restrict__ v, const float2 * __restrict__ invD,
                                                         const float2 * __restrict__ d, float2 * __restrict__ dn,
                                                         float2 * __restrict__ x, float2 * __restrict__ r, float2 c1,
-                                                        float2 c2)
+                                                        float2 c2, const int * kdev, int it)
     {
         const int slice = (int)((blockIdx.x * (unsigned)blockDim.x + threadIdx.x) >> 5);
-        if (slice >= nSlices)
+        if (slice >= nSlices || (kdev && it >= *kdev))
             return;
         const int lane = threadIdx.x & 31;
         const int row = slice * SELL_C + lane;
@@ -1557,8 +1557,10 @@ namespace nsf
     {
         SolverState * st;
         int numCh, iters;
+        const int * kdev; // the warm solve's device count (else iters)
         __device__ void operator()() const
         {
+            const int iters = kdev ? *kdev : this->iters;
             for (int c = 0; c < numCh; c++)
             {
                 const double rr = st->rrOut[0][c], bb = st->bbOut[c];
@@ -1577,7 +1579,7 @@ namespace nsf
     __global__ void __launch_bounds__(TPB) kChebFinal(int n, const int * __restrict__ rs, const int * __restrict__ ci,
                                                        const double * __restrict__ v, const double * __restrict__ x,
                                                        const double * __restrict__ b, SolverState * st, double * scratch,
-                                                       int numCh, int iters)
+                                                       int numCh, int iters, const int * kdev)
     {
         Group<L> g;
         double red[2 * NCH];
@@ -1618,8 +1620,149 @@ namespace nsf
             o.p[c] = &st->rrOut[0][c];
             o.p[NCH + c] = &st->bbOut[c];
         }
-        gridSum<double, 2 * NCH>(red, scratch, o, &st->ticket, nullptr, ChebEpi{st, numCh, iters});
+        gridSum<double, 2 * NCH>(red, scratch, o, &st->ticket, nullptr, ChebEpi{st, numCh, iters, kdev});
     }
+
+    // Warm-started Chebyshev (mass-solve method 4): x0 is the previous step's solution of the same
+    // solve.  Part 1: r0 = b - A x0 (FP64, row groups over the CSR), ||r0||^2 and ||b||^2 per
+    // channel; the last block decides per channel whether x0 is a better start than 0 (else that
+    // channel starts cold) and the iteration count from the a priori bound
+    //   ||r_k|| <= 2 rho^k sqrt(max D / min D) ||r0|| <= tol ||b||,  k <= kmax (the cold count).
+    struct ChebWarmEpi
+    {
+        SolverState * st;
+        int * kw; // kw[0]: the iteration count, kw[1 + c]: channel c starts from x0
+        int numCh, kmax;
+        double lnTarget, lnRho; // log(tol / (2 sqrt(max D / min D))), log(rho)
+        __device__ void operator()() const
+        {
+            int k = 0;
+            for (int c = 0; c < numCh; c++)
+            {
+                const double rr = st->rrOut[0][c], bb = st->bbOut[c];
+                int kc;
+                if (!(rr < bb))
+                {
+                    kw[1 + c] = 0;
+                    kc = kmax;
+                }
+                else
+                {
+                    kw[1 + c] = 1;
+                    if (!(rr > st->tol2 * bb))
+                        kc = 0;
+                    else
+                    {
+                        kc = (int)ceil((lnTarget + 0.5 * log(bb / rr)) / lnRho);
+                        kc = kc < 1 ? 1 : (kc > kmax ? kmax : kc);
+                    }
+                }
+                k = kc > k ? kc : k;
+            }
+            kw[0] = k;
+        }
+    };
+
+    template <int L, int NCH>
+    __global__ void __launch_bounds__(TPB) kChebWarmResidual(int n, const int * __restrict__ rs, const int * __restrict__ ci,
+                                                              const double * __restrict__ v, const double * __restrict__ x0,
+                                                              const double * __restrict__ b, double * __restrict__ r0,
+                                                              SolverState * st, double * scratch, ChebWarmEpi epi)
+    {
+        Group<L> g;
+        double red[2 * NCH];
+#pragma unroll
+        for (int c = 0; c < 2 * NCH; c++)
+            red[c] = 0;
+        for (int i = g.gid; i < n; i += g.ngroups)
+        {
+            const int s0 = ldg(rs + i), e0 = ldg(rs + i + 1);
+            double acc[NCH];
+#pragma unroll
+            for (int c = 0; c < NCH; c++)
+                acc[c] = 0;
+            for (int j = s0 + g.lane; j < e0; j += L)
+            {
+                const double a = ldg(v + j);
+                const int col = ldg(ci + j);
+#pragma unroll
+                for (int c = 0; c < NCH; c++)
+                    acc[c] += a * x0[(size_t)c * n + col];
+            }
+#pragma unroll
+            for (int c = 0; c < NCH; c++)
+            {
+                const double t = g.sum(acc[c]);
+                if (g.lane == 0)
+                {
+                    const double bi = b[(size_t)c * n + i], ri = bi - t;
+                    r0[(size_t)c * n + i] = ri;
+                    red[c] += ri * ri;
+                    red[NCH + c] += bi * bi;
+                }
+            }
+        }
+        Outs<2 * NCH> o;
+#pragma unroll
+        for (int c = 0; c < NCH; c++)
+        {
+            o.p[c] = &st->rrOut[0][c];
+            o.p[NCH + c] = &st->bbOut[c];
+        }
+        gridSum<double, 2 * NCH>(red, scratch, o, &st->ticket, nullptr, epi);
+    }
+
+    // Part 2 (FP64 iterations): a warm channel keeps x = x0 and r = r0, a cold one gets x = 0 and
+    // r = b; d = D^-1 r / theta
+    template <int NCH>
+    __global__ void __launch_bounds__(TPB) kChebWarmInit(int n, const double * __restrict__ b, const double * __restrict__ invD,
+                                                          double invTheta, const int * __restrict__ kw,
+                                                          double * __restrict__ x, double * __restrict__ r,
+                                                          double * __restrict__ d)
+    {
+        for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        {
+            const double id = invD[i];
+#pragma unroll
+            for (int c = 0; c < NCH; c++)
+            {
+                const size_t o = (size_t)c * n + i;
+                double ri = r[o];
+                if (!kw[1 + c])
+                {
+                    ri = b[o];
+                    r[o] = ri;
+                    x[o] = 0.0;
+                }
+                d[o] = ri * id * invTheta;
+            }
+        }
+    }
+
+    // Part 2 (double-float iterations): the same into the double-float vectors
+    template <int NCH>
+    __global__ void __launch_bounds__(TPB) kChebWarmInitDf(int n, const double * __restrict__ b, const double * __restrict__ x0,
+                                                            const double * __restrict__ r0, const float2 * __restrict__ invD,
+                                                            float2 invTheta, const int * __restrict__ kw,
+                                                            float2 * __restrict__ x, float2 * __restrict__ r,
+                                                            float2 * __restrict__ d)
+    {
+        for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        {
+            const float2 id = invD[i];
+#pragma unroll
+            for (int c = 0; c < NCH; c++)
+            {
+                const size_t o = (size_t)c * n + i;
+                const bool warm = kw[1 + c] != 0;
+                const float2 ri = dfFromDouble(warm ? r0[o] : b[o]);
+                r[o] = ri;
+                x[o] = warm ? dfFromDouble(x0[o]) : make_float2(0.f, 0.f);
+                d[o] = dfMul(dfMul(ri, id), invTheta);
+            }
+        }
+    }
+
 
     // Stop decision of refinement pass `pass` (sticky); stats: iters = refinement updates applied.
     // The next inner solve only has to reach half the remaining distance to the target:

@@ -363,7 +363,8 @@ def forces(mesh: Mesh, u, p, nu: float, group: str = "Circle") -> np.ndarray:
 
 class Chorin:
     """FP64 Chorin stepper of the oracle.  vel_method 0 = multicolor GS (RMS target),
-    1 = CG + multicolor SGS, 2 = CG + Jacobi, 3 = Chebyshev-Jacobi (relative tolerance).  mt: run on the OpenMP build
+    1 = CG + multicolor SGS, 2 = CG + Jacobi, 3 = Chebyshev-Jacobi, 4 = Chebyshev-Jacobi warm-started from
+    the previous step (relative tolerance).  mt: run on the OpenMP build
     (all host threads, OMP_NUM_THREADS); self.threads says what ran (1 if that build is missing)."""
 
     def __init__(self, ctx: Context, nu, tau, vel_method=1, vel_max_iters=200, vel_tol=1e-10,

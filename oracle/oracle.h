@@ -120,6 +120,13 @@ int orc_sys_pcg(const orc_sys *s, int precond, const double *b, double *x, int m
 int orc_cheb_iters(const orc_csr *a, double lo, double hi, double relTol, int maxIters);
 int orc_cheb_solve(const orc_csr *a, const double *b, double *x, double lo, double hi, int iters,
                    double relTol, double *relRes);
+/* the same from x0 (x0 == NULL: from 0); orc_cheb_warm_iters: the a priori count from the initial
+   residual, ||r_k|| <= 2 rho^k sqrt(max D / min D) ||b - A x0|| <= relTol ||b|| (0 if x0 already
+   meets it; capped at maxIters; -1 if ||b - A x0|| >= ||b||: then start from 0) */
+int orc_cheb_solve_from(const orc_csr *a, const double *b, const double *x0, double *x, double lo, double hi,
+                        int iters, double relTol, double *relRes);
+int orc_cheb_warm_iters(const orc_csr *a, double lo, double hi, const double *b, const double *x0, double relTol,
+                        int maxIters);
 /* spectral bounds of D^-1 M for the P2 mass matrix of affine triangles (any mesh) */
 #define ORC_MASS_SPEC_LO 0.39237
 #define ORC_MASS_SPEC_HI 2.05982
@@ -132,7 +139,8 @@ typedef struct
 {
     double nu, tau;
     int velMethod;       /* 0 = multicolor GS (RMS target), 1 = PCG-SGS, 2 = PCG-Jacobi, 3 = Chebyshev-
-                            Jacobi (relative tol) */
+                            Jacobi, 4 = Chebyshev-Jacobi from the previous step's solution of the
+                            same solve (relative tol) */
     int velMaxIters;
     double velTol;       /* RMS target for GS, relative tolerance for PCG */
     int presMaxIters;

@@ -14,7 +14,8 @@
  * Velocity solves: method 0 is the multicolor Gauss-Seidel solver with an RMS target (the
  * reference's "gs"), method 1 is CG with the multicolor SGS preconditioner to a relative
  * tolerance, method 2 the same CG with the Jacobi preconditioner, method 3 Chebyshev-Jacobi
- * with the a priori iteration count of orc_cheb_iters.  Pressure: CG with the multicolor SGS
+ * with the a priori iteration count of orc_cheb_iters, method 4 the same started from the
+ * previous step's solution of that solve (count from the initial residual, orc_cheb_warm_iters).  Pressure: CG with the multicolor SGS
  * preconditioner to a relative tolerance.
  */
 #include "oracle.h"
@@ -42,6 +43,7 @@ struct orc_chorin_s
        solution, sum_i (x_i . b) x_i, and its correction is orthogonalised into the basis (a full
        basis restarts from the solution and its last two differences) */
     double *pX, *pX0, *pW, *pQ, *pPrev2; /* pPrev2 (with pPrev, pHist): the last two solutions */
+    double *accPrevT, *accPrevF;         /* velMethod 4: the last tentative and final mass solutions */
     int pM, pL;
 };
 
@@ -65,6 +67,8 @@ orc_chorin *orc_chorin_create(const orc_context *ctx, const orc_chorin_cfg *cfg)
     s->rhsP = (double *)calloc(ctx->nIntP + 1, sizeof(double));
     s->g = (double *)calloc(2 * N, sizeof(double));
     s->pPrev = (double *)calloc(ctx->nIntP + 1, sizeof(double));
+    s->accPrevT = (double *)calloc(2 * (size_t)N + 1, sizeof(double));
+    s->accPrevF = (double *)calloc(2 * (size_t)N + 1, sizeof(double));
     s->pL = cfg->presBasis > 0 ? (cfg->presBasis < 256 ? cfg->presBasis : 256) : 250;
     if (cfg->presGuess == 2)
     {
@@ -108,6 +112,8 @@ void orc_chorin_free(orc_chorin *s)
     free(s->pW);
     free(s->pQ);
     free(s->pPrev2);
+    free(s->accPrevT);
+    free(s->accPrevF);
     free(s);
 }
 
@@ -143,6 +149,8 @@ void orc_chorin_set(orc_chorin *s, const double *u, const double *p)
     }
     s->pHist = 0; /* a new pressure history starts from the state just set */
     s->pM = 0;
+    memset(s->accPrevT, 0, sizeof(double) * 2 * ctx->N); /* the mass solves start cold again */
+    memset(s->accPrevF, 0, sizeof(double) * 2 * ctx->N);
 }
 
 static void impose(orc_chorin *s)
@@ -156,7 +164,7 @@ static void impose(orc_chorin *s)
 }
 
 /* mass solve for both channels; returns iterations (max over channels) and the residual */
-static int mass_solve(orc_chorin *s, const double *rhs, double *acc, double *res)
+static int mass_solve(orc_chorin *s, const double *rhs, double *acc, double *res, int final)
 {
     const orc_context *ctx = s->ctx;
     const int N = ctx->N;
@@ -171,6 +179,33 @@ static int mass_solve(orc_chorin *s, const double *rhs, double *acc, double *res
     }
     int itMax = 0;
     *res = 0;
+    if (s->cfg.velMethod == 4)
+    {
+        /* warm start from this solve's result of the previous step: the a priori count from the
+           initial residual, ||r_k|| <= 2 rho^k sqrt(max D / min D) ||r_0|| <= tol ||b|| */
+        double *prev = final ? s->accPrevF : s->accPrevT;
+        const int kmax = orc_cheb_iters(&ctx->M, ORC_MASS_SPEC_LO, ORC_MASS_SPEC_HI, s->cfg.velTol, s->cfg.velMaxIters);
+        int kUsed = 0, warm[2];
+        for (int ch = 0; ch < 2; ch++)
+        {
+            int k = orc_cheb_warm_iters(&ctx->M, ORC_MASS_SPEC_LO, ORC_MASS_SPEC_HI, rhs + ch * N, prev + ch * N,
+                                        s->cfg.velTol, kmax);
+            warm[ch] = k >= 0; /* a channel whose previous solution is no better than 0 starts cold */
+            if (k < 0)
+                k = kmax;
+            kUsed = k > kUsed ? k : kUsed;
+        }
+        for (int ch = 0; ch < 2; ch++)
+        {
+            double rr = 0;
+            orc_cheb_solve_from(&ctx->M, rhs + ch * N, warm[ch] ? prev + ch * N : NULL, acc + ch * N,
+                                ORC_MASS_SPEC_LO, ORC_MASS_SPEC_HI, kUsed, s->cfg.velTol, &rr);
+            if (rr > *res)
+                *res = rr;
+        }
+        memcpy(prev, acc, sizeof(double) * 2 * N);
+        return kUsed;
+    }
     if (s->cfg.velMethod == 3)
     {
         const int k = orc_cheb_iters(&ctx->M, ORC_MASS_SPEC_LO, ORC_MASS_SPEC_HI, s->cfg.velTol, s->cfg.velMaxIters);
@@ -346,7 +381,7 @@ int orc_chorin_step(orc_chorin *s, double *stats)
 
     orc_fastconv(ctx, s->cfg.nu, s->u, s->Avals);
     orc_spmm2(&ctx->K, s->Avals, s->u, s->rhs);
-    int itT = mass_solve(s, s->rhs, s->acc, &resT);
+    int itT = mass_solve(s, s->rhs, s->acc, &resT, 0);
     for (int i = 0; i < 2 * N; i++)
         s->u[i] -= tau * s->acc[i];
     impose(s);
@@ -381,7 +416,7 @@ int orc_chorin_step(orc_chorin *s, double *stats)
         s->p[ctx->intP[i]] = s->pInt[i];
 
     orc_spmv(&ctx->G, s->p, s->g);
-    int itF = mass_solve(s, s->g, s->acc, &resF);
+    int itF = mass_solve(s, s->g, s->acc, &resF, 1);
     for (int i = 0; i < 2 * N; i++)
         s->u[i] -= tau * s->acc[i];
     impose(s);

@@ -673,8 +673,38 @@ int orc_cheb_iters(const orc_csr *a, double lo, double hi, double relTol, int ma
     return k < maxIters ? k : maxIters;
 }
 
+int orc_cheb_warm_iters(const orc_csr *a, double lo, double hi, const double *b, const double *x0, double relTol,
+                        int maxIters)
+{
+    const int n = a->rows;
+    double *q = (double *)malloc(sizeof(double) * n);
+    orc_spmv(a, x0, q);
+    double rr = 0, bb = 0;
+    for (int i = 0; i < n; i++)
+    {
+        rr += (b[i] - q[i]) * (b[i] - q[i]);
+        bb += b[i] * b[i];
+    }
+    free(q);
+    if (!(rr < bb))
+        return -1; /* x0 is no better a start than 0 */
+    if (!(rr > relTol * relTol * bb))
+        return 0;
+    const double kappa = hi / lo, rho = (sqrt(kappa) - 1.0) / (sqrt(kappa) + 1.0);
+    int k = (int)ceil(log(relTol * sqrt(bb) / (2.0 * sqrt(diag_ratio(a)) * sqrt(rr))) / log(rho));
+    if (k < 1)
+        k = 1;
+    return k < maxIters ? k : maxIters;
+}
+
 int orc_cheb_solve(const orc_csr *a, const double *b, double *x, double lo, double hi, int iters,
                    double relTol, double *relRes)
+{
+    return orc_cheb_solve_from(a, b, NULL, x, lo, hi, iters, relTol, relRes);
+}
+
+int orc_cheb_solve_from(const orc_csr *a, const double *b, const double *x0, double *x, double lo, double hi,
+                        int iters, double relTol, double *relRes)
 {
     const int n = a->rows;
     double *invD = (double *)malloc(sizeof(double) * n), *r = (double *)malloc(sizeof(double) * n);
@@ -688,12 +718,14 @@ int orc_cheb_solve(const orc_csr *a, const double *b, double *x, double lo, doub
     }
     const double theta = 0.5 * (hi + lo), delta = 0.5 * (hi - lo), sigma = theta / delta;
     double rho = 1.0 / sigma;
+    if (x0)
+        orc_spmv(a, x0, q);
 #pragma omp parallel for schedule(static)
     for (int i = 0; i < n; i++)
     {
-        x[i] = 0;
-        r[i] = b[i];
-        d[i] = b[i] * invD[i] / theta;
+        x[i] = x0 ? x0[i] : 0.0;
+        r[i] = x0 ? b[i] - q[i] : b[i];
+        d[i] = r[i] * invD[i] / theta;
     }
     for (int k = 0; k < iters; k++)
     {

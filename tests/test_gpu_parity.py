@@ -400,6 +400,42 @@ def test_chorin_chebyshev_mass_matches_oracle(setup, torch_cuda, precision, grap
     assert s["status"] == 0 and s["tent_rel"] <= 1e-10 and s["final_rel"] <= 1e-10
 
 
+@pytest.mark.parametrize("graph", [True, False])
+@pytest.mark.parametrize("precision", ["f64", "mixed", "mixedsolve"])
+def test_chorin_warm_chebyshev_mass_matches_oracle(setup, torch_cuda, precision, graph):
+    """velMethod 4: Chebyshev mass solves from the previous step's solution, the count set on the
+    device from the initial residual.  Every solve meets the tolerance, the counts stay at or below
+    the cold one and drop below it, the fields follow the oracle's method 4 (FP64 and mixed-solve
+    1e-7, mixed within the mixed bounds), and set_state restarts the mass solves cold on both
+    sides."""
+    G, O, mesh, ctx, om, oc = setup
+    prec = {"f64": G.NSF_PREC_F64, "mixed": G.NSF_PREC_MIXED, "mixedsolve": G.NSF_PREC_F64_MIXEDSOLVE}[precision]
+    st = G.ChorinStepper(ctx, 1e-3, 1e-3, precision=prec, vel_method=4, vel_max_iters=300, vel_tol=1e-10,
+                         pres_max_iters=3000, pres_tol=1e-10, use_graph=graph)
+    ch = O.Chorin(oc, 1e-3, 1e-3, vel_method=4, vel_max_iters=300, vel_tol=1e-10, pres_max_iters=3000, pres_tol=1e-10)
+    cold = O.cheb_iters(oc.M, 1e-10)
+    st.step(2)
+    for _ in range(2):
+        ch.step()
+    u, p = ch.state()
+    st.set_state(u, p)
+    ch.set_state(u, p)
+    counts = []
+    for _ in range(8):
+        st.step(1)
+        ch.step()
+        s = st.stats()
+        assert s["status"] == 0 and s["tent_rel"] <= 1e-10 and s["final_rel"] <= 1e-10, s
+        assert s["tent_iters"] <= cold and s["final_iters"] <= cold
+        counts.append(s["tent_iters"] + s["final_iters"])
+    assert counts[0] == 2 * cold  # after set_state both solves start cold
+    assert min(counts[1:]) < 2 * cold, counts
+    ug, pg = st.state()
+    uo, po = ch.state()
+    tu, tp = (1e-5, 2e-4) if precision == "mixed" else (1e-7, 1e-7)
+    assert _rel(ug, uo) <= tu and _rel(pg, po) <= tp
+
+
 @pytest.mark.parametrize("precision", ["f64", "mixed"])
 def test_chorin_extrapolated_pressure_guess_matches_oracle(setup, torch_cuda, precision):
     """pressure_guess 1 (the pressure solve starts from 2 p(n-1) - p(n-2)): the FP64 stepper follows

@@ -405,3 +405,27 @@ def test_projected_pressure_guess(oracle_lib, channel_coarse):
         assert np.linalg.norm(u - u0) <= 1e-9 * np.linalg.norm(u0), key
         assert np.linalg.norm(p - p0) <= 1e-7 * np.linalg.norm(p0), key
         assert sum(its[10:]) < 0.9 * sum(its0[10:]), (key, its, its0)
+
+
+def test_warm_chebyshev_mass_solves(oracle_lib, channel_coarse):
+    """Mass-solve method 4 (Chebyshev from the previous step's solution, the count from the initial
+    residual): the solves meet the tolerance, the fields follow the cold method 3, and the counts
+    drop below the cold one once the flow settles."""
+    O = oracle_lib
+    m = O.Mesh(channel_coarse)
+    ctx = O.Context(m, 1.2, True)
+    cold = O.cheb_iters(ctx.M, 1e-10)
+    a = O.Chorin(ctx, 1e-3, 1e-3, vel_method=3, vel_tol=1e-10, pres_tol=1e-12)
+    b = O.Chorin(ctx, 1e-3, 1e-3, vel_method=4, vel_tol=1e-10, pres_tol=1e-12)
+    its = []
+    for _ in range(20):
+        a.step()
+        st = b.step()
+        assert st[4] <= 1e-10 and st[5] <= 1e-10, st
+        assert st[0] <= cold and st[2] <= cold
+        its.append((st[0], st[2]))
+    ua, pa = a.state()
+    ub, pb = b.state()
+    assert np.linalg.norm(ub - ua) <= 1e-8 * np.linalg.norm(ua)
+    assert np.linalg.norm(pb - pa) <= 1e-7 * np.linalg.norm(pa)
+    assert sum(t + f for t, f in its[10:]) < 0.9 * 2 * 10 * cold, its
