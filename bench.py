@@ -867,6 +867,23 @@ def bench_ours(args, rank, world, local_rank):
         t_f64, _ = timed(f64, args.steps, args.warmup)  # the same steps from rest as the main line
         st_f64 = f64.stats()
         u_m, p_m = mixed.state()
+
+        # ---- steady-state window: both steppers continue to step --steady-from, then --steady-steps
+        # more steps are timed each (the early steps from rest need hundreds of pressure iterations,
+        # the developed flow tens)
+        steady = None
+        if args.steady_steps > 0:
+            done = args.warmup + args.steps
+            lead = max(0, args.steady_from - done)
+            t_sm, _ = timed(mixed, args.steady_steps, lead)
+            st_sm = mixed.stats()
+            t_sf, _ = timed(f64, args.steady_steps, lead)
+            st_sf = f64.stats()
+            steady = {"from_step": done + lead, "steps": args.steady_steps,
+                      "mixed_steps_per_s": round(args.steady_steps / t_sm, 3),
+                      "fp64_steps_per_s": round(args.steady_steps / t_sf, 3),
+                      "mixed_over_fp64": round(t_sf / t_sm, 3),
+                      "mixed_pres_iters_last": st_sm["pres_iters"], "fp64_pres_iters_last": st_sf["pres_iters"]}
         del f64
 
         # ---- e2e through the C ABI with host buffers, on a fresh mixed stepper over the same steps
@@ -1002,10 +1019,12 @@ def bench_ours(args, rank, world, local_rank):
                                   "achieved": round(achieved, 1), "peak": hbm, "unit": "GB/s",
                                   "frac": round(achieved / hbm, 4), "peak_kind": kind,
                                   "algorithmic_bytes": fc_bytes, "launch_us": round(t_fc * 1e6, 2)},
-            "variants": {"fp64": {"steps_per_s": round(world * max(1, args.steps // 2) / t_f64, 3),
-                                  "ms_per_step": round(1e3 * t_f64 / max(1, args.steps // 2), 4),
+            "variants": {"fp64": {"steps_per_s": round(world * args.steps / t_f64, 3),
+                                  "ms_per_step": round(1e3 * t_f64 / args.steps, 4),
                                   "stats": st_f64},
-                         "mixed_stats": st_mixed},
+                         "mixed_over_fp64": round(t_f64 / t_mixed, 3),
+                         "mixed_stats": st_mixed,
+                         "steady": steady},
         }
         if accuracy is not None:
             line["accuracy"] = accuracy
@@ -1026,6 +1045,10 @@ def main():
     ap.add_argument("--cpu-sample-steps", type=int, default=-1,
                     help="CPU baseline of the channel workload: -1 the timed GPU window (--warmup steps from "
                          "rest, then --steps timed), k > 0 the first k steps after one warm-up, 0 none")
+    ap.add_argument("--steady-from", type=int, default=500,
+                    help="channel workload: step from rest at which the steady-state window starts")
+    ap.add_argument("--steady-steps", type=int, default=100,
+                    help="channel workload: steps timed in the steady-state window (0: none)")
     ap.add_argument("--no-accuracy", dest="accuracy", action="store_false",
                     help="skip the untimed mixed-vs-FP64 field and drag/lift comparison")
     ap.add_argument("--workload", default="channel", choices=["channel", "poisson", "small", "batch", "pack", "adjoint", "long"],

@@ -137,8 +137,8 @@ int nsf_fastconv_apply_df(nsf_csr I, const float *Kvals, double nu, const float 
    array (64 KiB + the counter) inside the library instead of buffers made per handle.
    Limits and rules:
      - a must be FP64 and square; 1 <= nrhs <= NSF_NOALLOC_MAX_RHS, else NSF_ERR_INVALID_ARG;
-     - the first call on a device looks the array up (cudaGetSymbolAddress); make that first
-       call before any stream capture on that device;
+     - the first call in a CUDA context (on each device, and again after cudaDeviceReset) looks
+       the array up (cudaGetSymbolAddress); make that first call before any stream capture;
      - the counter starts at zero when the library is loaded and every completed call leaves it
        at zero; nothing else needs clearing between calls;
      - all calls on one device share the array: calls that overlap in time (other streams or

@@ -10,6 +10,8 @@
 #include <cstring>
 #include <memory>
 #include <mutex>
+#include <utility>
+#include <vector>
 #include <numeric>
 #include <string>
 
@@ -1698,7 +1700,6 @@ namespace
 {
     constexpr int kNoAllocMaxBlocks = 1024;                 // grid cap of nsf_residual_noalloc
     constexpr int kNoAllocK = 2 * NSF_NOALLOC_MAX_RHS;      // reduced values per block
-    constexpr int kNoAllocMaxDevices = 64;
 
     // Scratch of nsf_residual_noalloc: the per-block partial sums of the grid reduction
     // (kNoAllocK x kNoAllocMaxBlocks doubles = 64 KiB) and the last-block counter.  Static device
@@ -1758,22 +1759,55 @@ namespace
         gridSum<double, kNoAllocK>(red, sc->part, o, &sc->ticket, nullptr);
     }
 
-    // Device address of the scratch, looked up once per device.
+    // Device address of the scratch, looked up once per CUDA context and cached under the
+    // context's unique id (cuCtxGetId, reached through the runtime's driver entry points so that the
+    // library does not link the driver).  A device reset ends the context; the module is loaded
+    // again in the next one, possibly at another address, and the new context's id misses the
+    // cache, so the address is looked up again.  If the driver entry points are unavailable the
+    // address is looked up on every call (cudaGetSymbolAddress allocates nothing).
     NoAllocScratch * noAllocScratch()
     {
+        using GetCurrent = int (*)(void **);                 // CUresult cuCtxGetCurrent(CUcontext *)
+        using GetId = int (*)(void *, unsigned long long *); // CUresult cuCtxGetId(CUcontext, u64 *)
         static std::mutex m;
-        static NoAllocScratch * addr[kNoAllocMaxDevices] = {};
-        int dev = 0;
-        NSF_CUDA(cudaGetDevice(&dev));
-        require(dev >= 0 && dev < kNoAllocMaxDevices, "device ordinal out of range");
+        static GetCurrent getCurrent = nullptr;
+        static GetId getId = nullptr;
+        static bool looked = false;
+        static std::vector<std::pair<unsigned long long, NoAllocScratch *>> cache;
         std::lock_guard<std::mutex> lock(m);
-        if (!addr[dev])
+        if (!looked)
         {
-            NoAllocScratch * ptr = nullptr;
-            NSF_CUDA(cudaGetSymbolAddress((void **)&ptr, g_noallocScratch));
-            addr[dev] = ptr;
+            cudaDriverEntryPointQueryResult q1{}, q2{};
+            void * f1 = nullptr;
+            void * f2 = nullptr;
+            if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f1, 12000, cudaEnableDefault, &q1) == cudaSuccess &&
+                cudaGetDriverEntryPointByVersion("cuCtxGetId", &f2, 12000, cudaEnableDefault, &q2) == cudaSuccess &&
+                q1 == cudaDriverEntryPointSuccess && q2 == cudaDriverEntryPointSuccess)
+            {
+                getCurrent = reinterpret_cast<GetCurrent>(f1);
+                getId = reinterpret_cast<GetId>(f2);
+            }
+            cudaGetLastError();
+            looked = true;
         }
-        return addr[dev];
+        auto contextId = [&]() -> unsigned long long {
+            void * c = nullptr;
+            unsigned long long id = 0;
+            if (getCurrent && getId && getCurrent(&c) == 0 && c && getId(c, &id) == 0)
+                return id;
+            return 0;
+        };
+        unsigned long long id = contextId();
+        if (id)
+            for (const auto & e : cache)
+                if (e.first == id)
+                    return e.second;
+        NoAllocScratch * ptr = nullptr;
+        NSF_CUDA(cudaGetSymbolAddress((void **)&ptr, g_noallocScratch)); // makes the primary context current
+        id = contextId();
+        if (id)
+            cache.emplace_back(id, ptr);
+        return ptr;
     }
 } // namespace
 

@@ -1641,7 +1641,12 @@ namespace nsf
             {
                 const double rr = st->rrOut[0][c], bb = st->bbOut[c];
                 int kc;
-                if (!(rr < bb))
+                if (bb == 0.0)
+                {
+                    kw[1 + c] = 0; // b = 0: x = 0 is exact, a cold start needs no iteration
+                    kc = 0;
+                }
+                else if (!(rr < bb))
                 {
                     kw[1 + c] = 0;
                     kc = kmax;

@@ -100,6 +100,7 @@ def _configure(L):
         L.orc_group_id.argtypes = [C.POINTER(MeshS), C.c_char_p]
         L.orc_channel_bcs.argtypes = [C.POINTER(MeshS), C.c_float, C.POINTER(ContextS)]
         L.orc_assemble.argtypes = [C.POINTER(MeshS), C.POINTER(ContextS), C.c_int]
+        L.orc_local_matrices.argtypes = [C.POINTER(MeshS), C.c_int, f64p]
         L.orc_context_free.argtypes = [C.POINTER(ContextS)]
         L.orc_csr_free.argtypes = [C.POINTER(CsrS)]
         L.orc_spmv.argtypes = [C.POINTER(CsrS), f64p, f64p]
@@ -195,6 +196,20 @@ class Mesh:
         self.p_elem = _arr(m.pElem, 3 * m.numTri, np.int32).reshape(-1, 3)
         self.p_border = _arr(m.pBorder, 5 * m.numBorder, np.int32).reshape(-1, 5)
         self.affine = _arr(m.affine, 6 * m.numTri, np.float32).reshape(-1, 6)
+
+    LOCAL_SHAPES = (("mass", (6, 6)), ("stiff", (6, 6)), ("stiffP", (3, 3)), ("divX", (3, 6)), ("divY", (3, 6)),
+                    ("gradX", (6, 3)), ("gradY", (6, 3)), ("conv", (12, 6, 6)))
+
+    def local_matrices(self, e: int) -> dict:
+        """FP64 local matrices of element e (orc_local_matrices), keyed as the reference harness's."""
+        out = np.zeros(585)
+        lib().orc_local_matrices(self._p, int(e), _ptr(out, C.c_double))
+        res, o = {}, 0
+        for k, shp in self.LOCAL_SHAPES:
+            n = int(np.prod(shp))
+            res[k] = out[o:o + n].reshape(shp)
+            o += n
+        return res
 
     def __del__(self):
         try:
@@ -479,9 +494,23 @@ def reference_path() -> str:
     return os.path.join(HERE, "_ref", "libnsfref.so")
 
 
-def build_reference(ref_root: str = "/root/reference/cpp") -> bool:
+def reference_root() -> str:
+    """The reference's ``cpp`` tree: ``$NSFEM_REFERENCE_CPP`` if set, else the default ``REF`` of the
+    build recipe ``oracle/Makefile.ref`` (the one place that names where the tree lies)."""
+    env = os.environ.get("NSFEM_REFERENCE_CPP")
+    if env:
+        return env
+    with open(os.path.join(HERE, "Makefile.ref")) as f:
+        for line in f:
+            if line.startswith("REF ?="):
+                return line.split("?=", 1)[1].strip()
+    return ""
+
+
+def build_reference(ref_root: str | None = None) -> bool:
     """Build oracle/_ref/libnsfref.so from the reference sources if they are present."""
-    if not os.path.isdir(ref_root):
+    ref_root = ref_root or reference_root()
+    if not ref_root or not os.path.isdir(ref_root):
         return False
     out = subprocess.run(["make", "-C", HERE, "-f", "Makefile.ref", "-s", "-j8", f"REF={ref_root}"],
                          capture_output=True, text=True)
@@ -525,5 +554,50 @@ def reference():
         R.ref_coloring.argtypes = [C.c_void_p, i32p, i32p, i32p]
         R.ref_gs2ch_double.argtypes = [C.c_int, i32p, i32p, f64p, f64p, f64p, C.c_int, C.c_double, f64p]
         R.ref_rmult_double.argtypes = [C.c_int, C.c_int, i32p, i32p, f64p, f64p, f64p]
+        R.ref_assembled.restype = C.c_int
+        R.ref_assembled.argtypes = [C.c_void_p, C.c_int, i32p, i32p, i32p, f32p]
+        R.ref_local_matrices.restype = C.c_int
+        R.ref_local_matrices.argtypes = [C.c_void_p, C.c_int] + [f32p] * 8
+        R.ref_fastconv_values.restype = C.c_int
+        R.ref_fastconv_values.argtypes = [C.c_void_p, f32p]
         _REF = R
     return _REF
+
+
+REF_ASSEMBLED = ("M", "K", "Kp", "D", "G")  # ref_assembled's `which` order
+
+
+def reference_assembled(R, h, name: str) -> Csr:
+    """The reference's assembled FP32 operator `name` (M, K, Kp, D, G) for the harness mesh h, or
+    "I" for the FastConvection integration matrix (values from the reference's integrator)."""
+    if name == "I":
+        ph = R.ref_prototype(h, 4)
+        dims = (C.c_int * 3)()
+        R.ref_csr_dims(ph, dims)
+        rs = np.zeros(dims[0] + 1, np.int32)
+        cl = np.zeros(dims[2], np.int32)
+        R.ref_csr_arrays(ph, _ptr(rs, C.c_int), _ptr(cl, C.c_int), None)
+        R.ref_csr_free(ph)
+        val = np.zeros(dims[2], np.float32)
+        if R.ref_fastconv_values(h, _ptr(val, C.c_float)) != 0:
+            raise RuntimeError(R.ref_last_error().decode())
+        return Csr(dims[0], dims[1], rs, cl, val)
+    w = REF_ASSEMBLED.index(name)
+    dims = (C.c_int * 3)()
+    if R.ref_assembled(h, w, dims, None, None, None) != 0:
+        raise RuntimeError(R.ref_last_error().decode())
+    rs = np.zeros(dims[0] + 1, np.int32)
+    cl = np.zeros(dims[2], np.int32)
+    val = np.zeros(dims[2], np.float32)
+    R.ref_assembled(h, w, dims, _ptr(rs, C.c_int), _ptr(cl, C.c_int), _ptr(val, C.c_float))
+    return Csr(dims[0], dims[1], rs, cl, val)
+
+
+def reference_local_matrices(R, h, e: int) -> dict:
+    """The reference integrator's FP32 local matrices of element e (see ref_local_matrices)."""
+    shapes = {"mass": (6, 6), "stiff": (6, 6), "stiffP": (3, 3), "divX": (3, 6), "divY": (3, 6),
+              "gradX": (6, 3), "gradY": (6, 3), "conv": (12, 6, 6)}
+    out = {k: np.zeros(v, np.float32) for k, v in shapes.items()}
+    if R.ref_local_matrices(h, int(e), *[_ptr(out[k], C.c_float) for k in shapes]) != 0:
+        raise RuntimeError(R.ref_last_error().decode())
+    return out

@@ -79,6 +79,12 @@ int orc_channel_bcs(const orc_mesh *m, float peakVelocity, orc_context *ctx);
 /* ---------------- FEM ---------------- */
 /* assembles M, K, Kp, D, G, Kpi and (if withConvection) I; returns 0 on success */
 int orc_assemble(const orc_mesh *m, orc_context *ctx, int withConvection);
+/* Local matrices of element e, FP64, in the layout of the reference harness's ref_local_matrices:
+   mass[36], stiffness[36] (P2), P1 stiffness[9], divergence x/y [3x6] each (rows P1), gradient
+   x/y [6x3] each (rows P2), self-convection [12][6][6] (unit velocity of local DOF k: x of node k
+   for k < 6, y of node k - 6) -- 585 doubles. */
+#define ORC_LOCAL_SIZE 585
+void orc_local_matrices(const orc_mesh *m, int e, double *out);
 void orc_context_free(orc_context *ctx);
 
 /* ---------------- linear algebra ---------------- */
@@ -122,7 +128,8 @@ int orc_cheb_solve(const orc_csr *a, const double *b, double *x, double lo, doub
                    double relTol, double *relRes);
 /* the same from x0 (x0 == NULL: from 0); orc_cheb_warm_iters: the a priori count from the initial
    residual, ||r_k|| <= 2 rho^k sqrt(max D / min D) ||b - A x0|| <= relTol ||b|| (0 if x0 already
-   meets it; capped at maxIters; -1 if ||b - A x0|| >= ||b||: then start from 0) */
+   meets it; capped at maxIters; -1 if ||b - A x0|| >= ||b||: then start from 0; -2 if b = 0: then
+   x = 0 with no iteration) */
 int orc_cheb_solve_from(const orc_csr *a, const double *b, const double *x0, double *x, double lo, double hi,
                         int iters, double relTol, double *relRes);
 int orc_cheb_warm_iters(const orc_csr *a, double lo, double hi, const double *b, const double *x0, double relTol,

@@ -191,7 +191,9 @@ static int mass_solve(orc_chorin *s, const double *rhs, double *acc, double *res
             int k = orc_cheb_warm_iters(&ctx->M, ORC_MASS_SPEC_LO, ORC_MASS_SPEC_HI, rhs + ch * N, prev + ch * N,
                                         s->cfg.velTol, kmax);
             warm[ch] = k >= 0; /* a channel whose previous solution is no better than 0 starts cold */
-            if (k < 0)
+            if (k == -2)
+                k = 0; /* zero right-hand side: cold, x = 0 */
+            else if (k < 0)
                 k = kmax;
             kUsed = k > kUsed ? k : kUsed;
         }

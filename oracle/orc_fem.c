@@ -328,6 +328,69 @@ static int patterns(const orc_mesh *m, orc_context *ctx)
        C[r][c] = sum_q w sgn(det) phi_r (B^T e phi_j) . grad^ phi_c
    so I[(r,c), j_x] = sum_q w sgn phi_r phi_j (b00 gx_c + b01 gy_c) and
       I[(r,c), j_y] = sum_q w sgn phi_r phi_j (b10 gx_c + b11 gy_c). */
+/* Self-convection of one element, linear in the local velocity: Ix[r][c][k] (Iy) is the (r, c) entry
+   of the local convection matrix for a unit x (y) velocity at local DOF k, as FastConvection's
+   constructor evaluates it (fastConvection.cpp:64-97 over triangleIntegrator.cpp:192-231). */
+static void local_convection(const geom *g, double Ix[6][6][6], double Iy[6][6][6])
+{
+    memset(Ix, 0, sizeof(double) * 216);
+    memset(Iy, 0, sizeof(double) * 216);
+    for (int q = 0; q < 6; q++)
+    {
+        double phi[6], gx[6], gy[6];
+        p2_shape(QX[q], QY[q], phi);
+        p2_grad(QX[q], QY[q], gx, gy);
+        double ws = QW[q] * g->sgn;
+        for (int c = 0; c < 6; c++)
+        {
+            double ax = g->b00 * gx[c] + g->b01 * gy[c];
+            double ay = g->b10 * gx[c] + g->b11 * gy[c];
+            for (int r = 0; r < 6; r++)
+                for (int k = 0; k < 6; k++)
+                {
+                    double f = ws * phi[r] * phi[k];
+                    Ix[r][c][k] += f * ax;
+                    Iy[r][c][k] += f * ay;
+                }
+        }
+    }
+}
+
+void orc_local_matrices(const orc_mesh *m, int e, double *out)
+{
+    geom g = element_geom(m->affine + 6 * e);
+    local_mats L;
+    local_matrices(&g, &L);
+    double Ix[6][6][6], Iy[6][6][6];
+    local_convection(&g, Ix, Iy);
+    double *o = out;
+    for (int r = 0; r < 6; r++)
+        for (int c = 0; c < 6; c++)
+            *o++ = L.M[r][c];
+    for (int r = 0; r < 6; r++)
+        for (int c = 0; c < 6; c++)
+            *o++ = L.K[r][c];
+    for (int r = 0; r < 3; r++)
+        for (int c = 0; c < 3; c++)
+            *o++ = L.Kp[r][c];
+    for (int r = 0; r < 3; r++)
+        for (int c = 0; c < 6; c++)
+            *o++ = L.Dx[r][c];
+    for (int r = 0; r < 3; r++)
+        for (int c = 0; c < 6; c++)
+            *o++ = L.Dy[r][c];
+    for (int r = 0; r < 6; r++)
+        for (int c = 0; c < 3; c++)
+            *o++ = L.Gx[r][c];
+    for (int r = 0; r < 6; r++)
+        for (int c = 0; c < 3; c++)
+            *o++ = L.Gy[r][c];
+    for (int k = 0; k < 12; k++)
+        for (int r = 0; r < 6; r++)
+            for (int c = 0; c < 6; c++)
+                *o++ = k < 6 ? Ix[r][c][k] : Iy[r][c][k - 6];
+}
+
 static int fast_convection(const orc_mesh *m, orc_context *ctx)
 {
     const int N = m->numV, T = m->numTri;
@@ -365,27 +428,7 @@ static int fast_convection(const orc_mesh *m, orc_context *ctx)
         const int *iv = m->vElem + 6 * e;
         geom g = element_geom(m->affine + 6 * e);
         double Ix[6][6][6], Iy[6][6][6];
-        memset(Ix, 0, sizeof Ix);
-        memset(Iy, 0, sizeof Iy);
-        for (int q = 0; q < 6; q++)
-        {
-            double phi[6], gx[6], gy[6];
-            p2_shape(QX[q], QY[q], phi);
-            p2_grad(QX[q], QY[q], gx, gy);
-            double ws = QW[q] * g.sgn;
-            for (int c = 0; c < 6; c++)
-            {
-                double ax = g.b00 * gx[c] + g.b01 * gy[c];
-                double ay = g.b10 * gx[c] + g.b11 * gy[c];
-                for (int r = 0; r < 6; r++)
-                    for (int k = 0; k < 6; k++)
-                    {
-                        double f = ws * phi[r] * phi[k];
-                        Ix[r][c][k] += f * ax;
-                        Iy[r][c][k] += f * ay;
-                    }
-            }
-        }
+        local_convection(&g, Ix, Iy);
         for (int r = 0; r < 6; r++)
             for (int c = 0; c < 6; c++)
             {

@@ -686,6 +686,8 @@ int orc_cheb_warm_iters(const orc_csr *a, double lo, double hi, const double *b,
         bb += b[i] * b[i];
     }
     free(q);
+    if (bb == 0)
+        return -2; /* b = 0: x = 0 is exact, a cold start needs no iteration */
     if (!(rr < bb))
         return -1; /* x0 is no better a start than 0 */
     if (!(rr > relTol * relTol * bb))

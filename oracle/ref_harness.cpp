@@ -13,9 +13,13 @@
 //   buildCsrGraph / buildSmallestLastOrdering / partitionGraphGreedy  cpp/libs/LinAlg/src/graphs.cpp
 //   CsrMatrix<float>::slice        cpp/libs/LinAlg/src/csrMatrix.cpp:12-91
 //   gaussSeidel2ch<double>         cpp/libs/LinAlg/src/gaussSeidel.cpp:215-230
-// The element-pattern loops below restate buildPrototypes (cpp/libs/Fem/src/chorinCsr.cpp:61-140)
-// and the FastConvection pattern construction (cpp/libs/Fem/src/fastConvection.cpp:17-80), whose
-// own files need OpenCV/Eigen, on top of the reference's prototype builder.
+//   buildChorinCsrMatrices<float>  cpp/libs/Fem/src/chorinCsr.cpp:436-502 (assembled FP32 values)
+//   TriangleIntegrator             cpp/libs/Element/src/triangleIntegrator.cpp:113-293 (local matrices)
+// Those two files include OpenCV for cv::Mat; they compile here against the test-only stand-in in
+// oracle/cvstub.  The element-pattern loops below restate buildPrototypes
+// (cpp/libs/Fem/src/chorinCsr.cpp:61-140) and the FastConvection construction
+// (cpp/libs/Fem/src/fastConvection.cpp:17-100), whose file needs Eigen, on top of the reference's
+// prototype builder and integrator.
 #include <algorithm>
 #include <cstring>
 #include <exception>
@@ -25,6 +29,8 @@
 
 #include <element/p1.h>
 #include <element/p2.h>
+#include <element/triangleIntegrator.h>
+#include <fem/chorinCsr.h>
 #include <linalg/csrMatrix.h>
 #include <linalg/gaussSeidel.h>
 #include <linalg/graphs.h>
@@ -43,7 +49,10 @@ namespace
         mesh::TriangleMesh tri;
         mesh::ConcreteMesh vmesh;
         mesh::ConcreteMesh pmesh;
+        std::unique_ptr<fem::ChorinCsrMatrices<float>> mats; // assembled on first use
     };
+
+    constexpr int kIntegrationDegree = 4; // cpp/execs/NavierStokes/src/buildContext.cpp:102
 
     struct RefCsr
     {
@@ -352,5 +361,163 @@ extern "C"
         m.column.assign(column, column + nnz);
         m.values.assign(values, values + nnz);
         m.rMultD(x, y);
+    }
+
+    // The reference's assembled FP32 operators (buildChorinCsrMatrices, one thread): which = 0 mass
+    // M, 1 stiffness K (both N x N), 2 pressure stiffness Kp (P x P), 3 D = velocityPressureDiv
+    // (P x 2N), 4 G = pressureVelocityDiv (2N x P).  dims[0..2] = rows, cols, nnz; the arrays are
+    // written when rowStart is non-null.  Returns 0, or -1 with ref_last_error().
+    int ref_assembled(void * hv, int which, int * dims, int * rowStart, int * column, float * values)
+    {
+        try
+        {
+            auto * h = static_cast<RefMesh *>(hv);
+            if (!h->mats)
+                h->mats = std::make_unique<fem::ChorinCsrMatrices<float>>(
+                    fem::buildChorinCsrMatrices<float>(h->vmesh, h->pmesh, kIntegrationDegree, 1));
+            const linalg::CsrMatrix<float> * m = nullptr;
+            switch (which)
+            {
+            case 0: m = &h->mats->velocityMass; break;
+            case 1: m = &h->mats->velocityStiffness; break;
+            case 2: m = &h->mats->pressureStiffness; break;
+            case 3: m = &h->mats->velocityPressureDiv; break;
+            case 4: m = &h->mats->pressureVelocityDiv; break;
+            default: lastError = "ref_assembled: which must be 0..4"; return -1;
+            }
+            dims[0] = m->rows;
+            dims[1] = m->cols;
+            dims[2] = (int)m->column.size();
+            if (rowStart)
+            {
+                std::copy(m->rowStart.begin(), m->rowStart.end(), rowStart);
+                std::copy(m->column.begin(), m->column.end(), column);
+                std::copy(m->values.begin(), m->values.end(), values);
+            }
+            return 0;
+        }
+        catch (const std::exception & e)
+        {
+            lastError = e.what();
+            return -1;
+        }
+    }
+
+    // Local matrices of element e from the reference's integrator (degree 4), float, row-major:
+    // mass[36], stiff[36] (P2), stiffP[9] (P1), divX/divY[18] (swap = false: rows P1, cols P2),
+    // gradX/gradY[18] (swap = true: rows P2, cols P1), conv[12 * 36]: the self-convection matrix for
+    // the unit velocity of local DOF k (k < 6: x component of node k, else y of node k - 6), as
+    // FastConvection's constructor evaluates it.  Any pointer may be null.
+    int ref_local_matrices(void * hv, int e, float * mass, float * stiff, float * stiffP, float * divX, float * divY,
+                           float * gradX, float * gradY, float * conv)
+    {
+        try
+        {
+            auto * h = static_cast<RefMesh *>(hv);
+            const auto & vm = h->vmesh;
+            const auto & pm = h->pmesh;
+            el::TriangleIntegrator vi(vm.baseElement, kIntegrationDegree, pm.baseElement);
+            el::TriangleIntegrator pi(pm.baseElement, kIntegrationDegree);
+            const auto & t = vm.elementTransforms[e];
+            auto put = [](const cv::Mat & m, float * out) {
+                if (!out)
+                    return;
+                for (int r = 0; r < m.rows; r++)
+                    for (int c = 0; c < m.cols; c++)
+                        out[r * m.cols + c] = m.at<float>(r, c);
+            };
+            cv::Mat a, b;
+            vi.integrateLocalMassMatrix(t, a);
+            put(a, mass);
+            vi.integrateLocalStiffnessMatrix(t, a);
+            put(a, stiff);
+            pi.integrateLocalStiffnessMatrix(t, a);
+            put(a, stiffP);
+            vi.integrateLocalDivergenceMatrix(t, false, a, b);
+            put(a, divX);
+            put(b, divY);
+            vi.integrateLocalDivergenceMatrix(t, true, a, b);
+            put(a, gradX);
+            put(b, gradY);
+            if (conv)
+            {
+                std::vector<float> lx(6, 0.0f), ly(6, 0.0f);
+                for (int k = 0; k < 12; k++)
+                {
+                    std::vector<float> & lv = k >= 6 ? ly : lx;
+                    lv[k % 6] = 1.0f;
+                    vi.integrateLocalSelfConvectionMatrix(t, lx.data(), ly.data(), a);
+                    lv[k % 6] = 0.0f;
+                    put(a, conv + 36 * k);
+                }
+            }
+            return 0;
+        }
+        catch (const std::exception & e)
+        {
+            lastError = e.what();
+            return -1;
+        }
+    }
+
+    // Values of the FastConvection integration matrix in the layout of ref_prototype(hv, 4):
+    // fastConvection.cpp:52-97 with the reference's integrator, contributions summed in FP32 in
+    // element order (the order of its triplets).  values[nnz(I)].  Returns 0 or -1.
+    int ref_fastconv_values(void * hv, float * values)
+    {
+        try
+        {
+            auto * h = static_cast<RefMesh *>(hv);
+            const auto & vm = h->vmesh;
+            const int N = (int)vm.nodes.size();
+            std::unique_ptr<RefCsr> vproto(static_cast<RefCsr *>(ref_prototype(hv, 0)));
+            std::unique_ptr<RefCsr> iproto(static_cast<RefCsr *>(ref_prototype(hv, 4)));
+            const auto & P = vproto->m;
+            const auto & I = iproto->m;
+            std::fill(values, values + I.column.size(), 0.0f);
+            el::TriangleIntegrator vi(vm.baseElement, kIntegrationDegree, h->pmesh.baseElement);
+            std::vector<int> iv(6), offs(6);
+            std::vector<float> lx(6, 0.0f), ly(6, 0.0f);
+            cv::Mat conv;
+            for (int e = 0; e < vm.numElements; e++)
+            {
+                vm.getElement(e, iv.data(), nullptr);
+                int rowIdx[6][6];
+                for (int r = 0; r < 6; r++)
+                {
+                    P.findOffsetsUnsorted(iv[r], iv, offs);
+                    for (int c = 0; c < 6; c++)
+                        rowIdx[r][c] = offs[c];
+                }
+                for (int k = 0; k < 12; k++)
+                {
+                    std::vector<float> & lv = k >= 6 ? ly : lx;
+                    lv[k % 6] = 1.0f;
+                    vi.integrateLocalSelfConvectionMatrix(vm.elementTransforms[e], lx.data(), ly.data(), conv);
+                    lv[k % 6] = 0.0f;
+                    const int col = k >= 6 ? iv[k - 6] + N : iv[k];
+                    for (int r = 0; r < 6; r++)
+                        for (int c = 0; c < 6; c++)
+                        {
+                            const int row = rowIdx[r][c];
+                            const int * b0 = I.column.data() + I.rowStart[row];
+                            const int * b1 = I.column.data() + I.rowStart[row + 1];
+                            const int * it = std::lower_bound(b0, b1, col);
+                            if (it == b1 || *it != col)
+                            {
+                                lastError = "ref_fastconv_values: entry outside the prototype";
+                                return -1;
+                            }
+                            values[it - I.column.data()] += conv.at<float>(r, c);
+                        }
+                }
+            }
+            return 0;
+        }
+        catch (const std::exception & e)
+        {
+            lastError = e.what();
+            return -1;
+        }
     }
 }

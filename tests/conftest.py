@@ -10,7 +10,15 @@ if ROOT not in sys.path:
     sys.path.insert(0, ROOT)
 
 GOLDEN = os.path.join(ROOT, "tests", "golden")
-REFERENCE_ASSETS = "/root/reference/cpp/assets"
+
+def _reference_assets():
+    """The reference's shipped meshes (``cpp/assets``), where its tree is present."""
+    import oracle
+    root = oracle.reference_root()
+    return os.path.join(root, "assets") if root else ""
+
+
+REFERENCE_ASSETS = _reference_assets()
 
 
 def pytest_configure(config):
