@@ -19,6 +19,19 @@ def _reference_assets():
 
 
 REFERENCE_ASSETS = _reference_assets()
+# copies of the shipped meshes made by the reference harness build (oracle/Makefile.ref)
+HARNESS_ASSETS = os.path.join(ROOT, "oracle", "_ref", "assets")
+
+
+def shipped_mesh_path(name):
+    """Path of the reference's shipped mesh `name` (e.g. "h_0.01.msh"), from its tree or from the
+    harness build's copy, or None."""
+    for d in (REFERENCE_ASSETS, HARNESS_ASSETS):
+        if d:
+            p = os.path.join(d, name)
+            if os.path.exists(p):
+                return p
+    return None
 
 
 def pytest_configure(config):

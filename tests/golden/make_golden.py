@@ -8,6 +8,9 @@
    M/K, Kp, D, G and the FastConvection integration matrix, and the smallest-last + greedy coloring
    of M and of the internal pressure stiffness.  Their SHA-256 digests (little-endian int32/float32
    bytes) and a few small arrays are written to ref_<mesh>.json.
+3. The reference's element integrator (triangleIntegrator.cpp, compiled into the same harness
+   against a test-only cv::Mat stand-in) gives the FP32 local matrices of 48 seeded elements of the
+   channel mesh: ref_local_<mesh>.npz.
 
 Run from the repository root where the reference tree is present:
     python tests/golden/make_golden.py
@@ -119,6 +122,20 @@ def ref_structures(R, path: str, peak: float) -> dict:
     return out
 
 
+def ref_local_sample(R, path: str, count: int = 48, seed: int = 0) -> dict:
+    """The reference integrator's local matrices (float32) for `count` seeded elements of the mesh."""
+    h = R.ref_mesh_load(path.encode())
+    c = (C.c_int * 6)()
+    R.ref_mesh_counts(h, c)
+    elems = np.sort(np.random.default_rng(seed).choice(c[1], size=count, replace=False)).astype(np.int32)
+    mats = [oracle.reference_local_matrices(R, h, int(e)) for e in elems]
+    R.ref_mesh_free(h)
+    out = {"elements": elems}
+    for k in mats[0]:
+        out[k] = np.stack([m[k] for m in mats]).astype(np.float32)
+    return out
+
+
 def main():
     oracle.build()
     if not oracle.build_reference():
@@ -132,6 +149,8 @@ def main():
         with open(raw, "rb") as f, gzip.GzipFile(raw + ".gz", "wb", mtime=0) as g:
             g.write(f.read())
         res = ref_structures(R, raw, peak)
+        if name.startswith("channel"):
+            np.savez_compressed(os.path.join(HERE, f"ref_local_{name}.npz"), **ref_local_sample(R, raw))
         os.remove(raw)
         with open(os.path.join(HERE, f"ref_{name}.json"), "w") as f:
             json.dump(res, f, indent=1, sort_keys=True)

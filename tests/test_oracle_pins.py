@@ -14,7 +14,7 @@ import os
 import numpy as np
 import pytest
 
-from conftest import GOLDEN, REFERENCE_ASSETS
+from conftest import GOLDEN, shipped_mesh_path
 
 
 def digest(a):
@@ -166,9 +166,9 @@ def _reference():
 
 def _ref_meshes():
     out = []
-    for name in ("h_0.025.msh", "h_0.01.msh"):
-        p = os.path.join(REFERENCE_ASSETS, name)
-        if os.path.exists(p):
+    for name in ("h_0.025.msh", "h_0.01.msh", "h_0.005.msh"):
+        p = shipped_mesh_path(name)
+        if p:
             out.append(p)
     return out
 
@@ -429,3 +429,89 @@ def test_warm_chebyshev_mass_solves(oracle_lib, channel_coarse):
     assert np.linalg.norm(ub - ua) <= 1e-8 * np.linalg.norm(ua)
     assert np.linalg.norm(pb - pa) <= 1e-7 * np.linalg.norm(pa)
     assert sum(t + f for t, f in its[10:]) < 0.9 * 2 * 10 * cold, its
+
+
+# ------------------------------------------------------------ FP values: the reference's integrator
+# The reference's element integrator (triangleIntegrator.cpp) and its CSR assembly (chorinCsr.cpp) run
+# in FP32; the oracle and the product assemble in FP64 from the same float geometry.  Their values
+# therefore agree to the FP32 rounding of the reference's own arithmetic: measured at most 4e-7 of the
+# largest entry of each matrix on every mesh (1.0e-6 of the row's largest entry for the
+# FastConvection matrix, whose rows mix entries of very different size).  The bounds below leave a
+# factor 2.5 on that; a sign, transpose, node-order or quadrature error moves entries by O(1).
+FP32_REL_GLOBAL = 1e-6   # |ours - ref| <= this * max |ref| over the matrix
+FP32_REL_ROW = 2.5e-6    # |ours - ref| <= this * max |ref| over the row (+ 1e-7 max |ref| for empty rows)
+ASSEMBLED = ("M", "K", "Kp", "D", "G", "I")
+
+
+def _check_values(name, rs, cl, val, ref):
+    assert np.array_equal(rs, ref.rowStart) and np.array_equal(cl, ref.col), name
+    rv = ref.val.astype(np.float64)
+    scale = np.abs(rv).max()
+    d = np.abs(np.asarray(val, np.float64) - rv)
+    assert d.max() <= FP32_REL_GLOBAL * scale, (name, d.max() / scale)
+    rows = np.repeat(np.arange(ref.rows), np.diff(ref.rowStart))
+    rmax = np.zeros(ref.rows)
+    np.maximum.at(rmax, rows, np.abs(rv))
+    assert np.all(d <= FP32_REL_ROW * rmax[rows] + 1e-7 * scale), name
+
+
+@pytest.mark.parametrize("which", ["committed", "reference"])
+def test_assembled_values_match_reference(oracle_lib, channel_coarse, which):
+    """M, K, Kp, D, G from the reference's buildChorinCsrMatrices<float> and the FastConvection
+    integration matrix I from its integrator, against the oracle's and the product's FP64 assembly."""
+    import nsfemoptim_gb300 as G
+    R = _reference()
+    O = oracle_lib
+    paths = [channel_coarse] if which == "committed" else _ref_meshes()
+    if not paths:
+        pytest.skip("reference meshes not present")
+    for path in paths:
+        h = R.ref_mesh_load(path.encode())
+        assert h, R.ref_last_error()
+        m = O.Mesh(path)
+        ctx = O.Context(m, 1.2, True)
+        pctx = G.build_chorin_context(G.load_gmsh(path), 1.2)
+        for name in ASSEMBLED:
+            ref = O.reference_assembled(R, h, name)
+            a = getattr(ctx, name)
+            _check_values(name, a.rowStart, a.col, a.val, ref)
+            b = pctx.matrix(name)
+            _check_values(name, b.rowStart, b.column, b.values, ref)
+        R.ref_mesh_free(h)
+
+
+def _local_fixture():
+    return np.load(os.path.join(GOLDEN, "ref_local_channel_h0.025_s0.npz"))
+
+
+def _check_local(ours, ref):
+    for k, r in ref.items():
+        o = ours[k]
+        scale = np.abs(r).max()
+        assert np.abs(o - r.astype(np.float64)).max() <= FP32_REL_GLOBAL * scale, k
+
+
+def test_local_matrices_match_golden_reference(oracle_lib, channel_coarse):
+    """The oracle's local element matrices (mass, stiffness, P1 stiffness, divergence, gradient and
+    the twelve unit-velocity self-convection matrices) against the reference integrator's, stored
+    for a seeded sample of elements of the committed mesh (tests/golden/make_golden.py).  Runs
+    without the reference tree."""
+    O = oracle_lib
+    fx = _local_fixture()
+    m = O.Mesh(channel_coarse)
+    for i, e in enumerate(fx["elements"]):
+        _check_local(m.local_matrices(int(e)), {k: fx[k][i] for k, _ in O.Mesh.LOCAL_SHAPES})
+
+
+def test_local_matrices_match_live_reference(oracle_lib, channel_coarse):
+    """The same on every element of the committed mesh and of the shipped h = 0.025 mesh, against
+    the reference integrator compiled here."""
+    R = _reference()
+    O = oracle_lib
+    paths = [channel_coarse] + [p for p in _ref_meshes() if p.endswith("h_0.025.msh")]
+    for path in paths:
+        h = R.ref_mesh_load(path.encode())
+        m = O.Mesh(path)
+        for e in range(m.num_tri):
+            _check_local(m.local_matrices(e), O.reference_local_matrices(R, h, e))
+        R.ref_mesh_free(h)
