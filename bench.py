@@ -932,6 +932,7 @@ def bench_ours(args, rank, world, local_rank):
         # values + column indices of I, row starts, u once, K read and A written (8-byte pairs)
         fc_bytes = nnzI * (4 + 4) + (rowsI + 1) * 4 + 2 * N * 8 + 2 * rowsI * 8
 
+        pcg_form = "classic" if os.environ.get("NSF_PCG_FORM") == "classic" else "eisenstat"
         # ---- dominant kernel: the cluster-resident pressure PCG (FP32 inner solve of the
         # refinement).  Per-iteration time from two solves that differ only in the iteration cap
         # (same launches, same setup), each solve bracketed by CUDA events on its stream.
@@ -957,12 +958,20 @@ def bench_ours(args, rank, world, local_rank):
             pcg_t[cap] = (best, s.getLastIterations())
             del s
         t_it = (pcg_t[80][0] - pcg_t[20][0]) / max(1, pcg_t[80][1] - pcg_t[20][1])
-        # algorithmic bytes of one PCG iteration in FP32 (sv = si = 4): SpMV + two SGS sweeps + 7
-        # vector passes, rows/nnz of the internal pressure system
         n_p, nnz_p = Kpi.rows, Kpi.nnz
-        spmv_b = nnz_p * 8 + (n_p + 1) * 4 + 2 * n_p * 4
-        sweep_b = (nnz_p - n_p) * 8 + (n_p + 1) * 4 + 3 * n_p * 4 + n_p * 4
-        pcg_bytes = spmv_b + 2 * sweep_b + 7 * n_p * 4
+        if pcg_form == "classic":
+            # algorithmic bytes of one classical PCG iteration in FP32 (sv = si = 4): SpMV + two SGS
+            # sweeps + 7 vector passes, rows/nnz of the internal pressure system
+            spmv_b = nnz_p * 8 + (n_p + 1) * 4 + 2 * n_p * 4
+            sweep_b = (nnz_p - n_p) * 8 + (n_p + 1) * 4 + 3 * n_p * 4 + n_p * 4
+            pcg_bytes = spmv_b + 2 * sweep_b + 7 * n_p * 4
+        else:
+            # Eisenstat's form: every off-diagonal entry once (backward sweep over the later-colour
+            # entries, forward sweep over the earlier-colour ones), the row structure twice, 22
+            # vector passes (update: p, s, x~, r~, w, d read and p, s, x~, r~ written; backward: r~,
+            # 1/d read, t written, t gathered; forward: r~, t, 1/d, d read, f, w written, f and r~
+            # gathered)
+            pcg_bytes = (nnz_p - n_p) * 8 + 2 * (n_p + 1) * 4 + 22 * n_p * 4
 
         # ---- accuracy (untimed): mixed vs FP64 fields and drag/lift series from rest
         accuracy, f64_step4 = (accuracy_run(G, ctx, mesh, stepper, torch, stream) if args.accuracy
@@ -1006,7 +1015,10 @@ def bench_ours(args, rank, world, local_rank):
                             "the run's pressure-guess history kept), one graph-launched step, get_state "
                             "(u, p to pinned host memory)"},
             "gpu_launches": int(launches),
-            "roofline": {"bound": "hbm", "kernel": "kPcgClusterDs<float,1> (pressure PCG, FP32 inner solve)",
+            "roofline": {"bound": "hbm", "kernel": ("kPcgClusterDs<float,1> (pressure PCG-SGS, FP32, classical form)"
+                                                    if pcg_form == "classic" else
+                                                    "kPcgClusterEis<float,1> (pressure PCG-SGS, FP32, Eisenstat's form, "
+                                                    "one reduction per iteration)"),
                          "achieved": round(achieved_pcg, 1), "peak": hbm, "unit": "GB/s",
                          "frac": round(achieved_pcg / hbm, 4), "peak_kind": kind,
                          "algorithmic_bytes_per_iteration": pcg_bytes, "iteration_us": round(t_it * 1e6, 3),

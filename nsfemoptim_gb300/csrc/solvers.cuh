@@ -11,6 +11,7 @@
 
 #include "cluster.cuh"
 #include "cluster_dsmem.cuh"
+#include "cluster_eis.cuh"
 #include "device.cuh"
 #include "host/setup.hpp"
 #include "kernels.cuh"
@@ -163,13 +164,19 @@ namespace nsf
         // DSMEM: 0 matrix values read from global memory, 1 values in shared memory
         int dsVals = -1;
         DsLayout dsLay{};
+        // DSMEM: 1 Eisenstat's form with one reduction per iteration (kPcgClusterEis, systems of at
+        // least two colours), 0 the classical form (kPcgClusterDs; NSF_PCG_FORM=classic forces it)
+        int dsForm = 0;
+        EisLayout eisLay{};
         DevBuf<int> cmapDev;
         // GRID: barrier control words and the per-CTA reduction slots
         DevBuf<unsigned> gridCtl;
         DevBuf<T> gridSlots;
 
-        bool setupDsmem(const SweepSystem<T> * s, bool allowVals)
+        bool setupDsmem(const SweepSystem<T> * s, bool allowVals, int form = -1)
         {
+            if (form < 0)
+                form = (s->nColors >= 2 && envStr("NSF_PCG_FORM", "eisenstat") != "classic") ? 1 : 0;
             for (int cs : {16, 8})
             {
                 DsShares D = dsShares(s->ps, s->hostRsO, s->hostCiO, cs);
@@ -177,6 +184,23 @@ namespace nsf
                     return false;
                 for (int vals = allowVals ? 1 : 0; vals >= 0; vals--)
                 {
+                    if (form == 1)
+                    {
+                        const EisLayout lay = eisLayout(D.rowsMax, D.nzMax, NCH, (int)sizeof(T), vals != 0);
+                        const bool fits = vals ? clusterFits(kPcgClusterEis<T, NCH, true>, cs, lay.bytes)
+                                               : clusterFits(kPcgClusterEis<T, NCH, false>, cs, lay.bytes);
+                        if (fits)
+                        {
+                            clusterSize = cs;
+                            dsVals = vals;
+                            dsForm = 1;
+                            eisLay = lay;
+                            clusterSmem = lay.bytes;
+                            cmapDev.upload(D.cmap);
+                            return true;
+                        }
+                        continue;
+                    }
                     const DsLayout lay = dsLayout(D.rowsMax, D.nzMax, NCH, (int)sizeof(T), vals != 0);
                     const bool fits = vals ? clusterFits(kPcgClusterDs<T, NCH, true>, cs, lay.bytes)
                                            : clusterFits(kPcgClusterDs<T, NCH, false>, cs, lay.bytes);
@@ -184,6 +208,7 @@ namespace nsf
                     {
                         clusterSize = cs;
                         dsVals = vals;
+                        dsForm = 0;
                         dsLay = lay;
                         clusterSmem = lay.bytes;
                         cmapDev.upload(D.cmap);
@@ -252,6 +277,7 @@ namespace nsf
             clusterShared = false;
             clusterSmem = 0;
             dsVals = -1;
+            dsForm = 0;
             bool ok = true;
             if (cpath == DSMEM)
                 ok = setupDsmem(s, variant != 0) && dsVals == variant;
@@ -397,8 +423,9 @@ namespace nsf
                 }
             }
             if (envFlag("NSF_VERBOSE"))
-                std::fprintf(stderr, "[nsf] PCG n=%d nnz=%d colors=%d path=%d ctas=%d shared=%d dsvals=%d smem=%zu\n",
-                             n, s->nnzFull, s->nColors, path, clusterSize, (int)clusterShared, dsVals, clusterSmem);
+                std::fprintf(stderr,
+                             "[nsf] PCG n=%d nnz=%d colors=%d path=%d ctas=%d shared=%d dsvals=%d form=%d smem=%zu\n", n,
+                             s->nnzFull, s->nColors, path, clusterSize, (int)clusterShared, dsVals, dsForm, clusterSmem);
         }
 
         void sgs(cudaStream_t s, PcgPtrs PP, int init, T * x, bool tickLast)
@@ -428,6 +455,18 @@ namespace nsf
             if (setConfig)
                 NSF_LAUNCH(kSetConfig, 1, s, st.get(), maxIters, absolute ? 1 : 0,
                            absolute ? tol * tol * (double)S.n : tol * tol);
+            if (path == DSMEM && dsForm == 1)
+            {
+                EisPcgArgs<T> A{S.n,         S.nColors,     numCh,        psDev.get(),  S.rsO.get(), S.ciO.get(),
+                                S.vO.get(),  cmapDev.get(), S.diag.get(), S.invD.get(), b,           x,
+                                st.get(),    P.skip,        eisLay,       0,            0.0,         nullptr,
+                                nullptr,     nullptr,       nullptr};
+                if (dsVals)
+                    launchCluster(kPcgClusterEis<T, NCH, true>, clusterSize, DTPB, eisLay.bytes, s, A);
+                else
+                    launchCluster(kPcgClusterEis<T, NCH, false>, clusterSize, DTPB, eisLay.bytes, s, A);
+                return;
+            }
             if (path == DSMEM)
             {
                 DsPcgArgs<T> A{S.n,         S.nColors,    numCh,   psDev.get(), S.rsO.get(), S.ciO.get(),
@@ -496,6 +535,18 @@ namespace nsf
                            SolverState * stOut, double delta2)
         {
             const SweepSystem<T> & S = *sys;
+            if (dsForm == 1)
+            {
+                EisPcgArgs<T> A{S.n,          S.nColors,     numCh,          psDev.get(),    S.rsO.get(), S.ciO.get(),
+                                S.vO.get(),   cmapDev.get(), S.diag.get(),   S.invD.get(),   nullptr,     nullptr,
+                                stOut,        nullptr,       eisLay,         1,              delta2,      b64,
+                                s64.vO.get(), s64.diag.get(), x64};
+                if (dsVals)
+                    launchCluster(kPcgClusterEis<T, NCH, true>, clusterSize, DTPB, eisLay.bytes, s, A);
+                else
+                    launchCluster(kPcgClusterEis<T, NCH, false>, clusterSize, DTPB, eisLay.bytes, s, A);
+                return;
+            }
             DsPcgArgs<T> A{S.n,          S.nColors,     numCh,          psDev.get(),    S.rsO.get(), S.ciO.get(),
                            S.vO.get(),   cmapDev.get(), S.diag.get(),   S.invD.get(),   nullptr,     nullptr,
                            stOut,        nullptr,       dsLay,          1,              delta2,      b64,

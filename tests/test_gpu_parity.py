@@ -180,21 +180,29 @@ def test_pcg_pressure_matches_oracle(setup, torch_cuda):
     assert np.linalg.norm(r) <= 1.01e-10 * np.linalg.norm(b)
 
 
-PATH_CODES = {"dsmem": 1, "dsmem-novals": 1, "grid": 2, "grid-global": 2, "cluster": 3, "cluster-global": 3,
-              "multikernel": 0}
+# "-classic": the cluster solve in the classical form (kPcgClusterDs) instead of Eisenstat's
+PATH_CODES = {"dsmem": 1, "dsmem-novals": 1, "dsmem-classic": 1, "dsmem-novals-classic": 1, "grid": 2,
+              "grid-global": 2, "cluster": 3, "cluster-global": 3, "multikernel": 0}
 
 
 def _force_path(monkeypatch, path):
+    if path.endswith("-classic"):
+        monkeypatch.setenv("NSF_PCG_FORM", "classic")
+        path = path[:-len("-classic")]
+    else:
+        monkeypatch.delenv("NSF_PCG_FORM", raising=False)
     monkeypatch.setenv("NSF_PCG_PATH", path)
     monkeypatch.setenv("NSF_VERBOSE", "1")
 
 
 def _check_path(capfd, path):
-    """The first solver created since the last check ran on the forced path."""
+    """The first solver created since the last check ran on the forced path (and form)."""
     err = capfd.readouterr().err
     lines = [ln for ln in err.splitlines() if ln.startswith("[nsf] PCG")]
     assert lines, err
     assert f"path={PATH_CODES[path]} " in lines[0], lines
+    if path.startswith("dsmem"):
+        assert ("form=0" if path.endswith("-classic") else "form=1") in lines[0], lines
 
 
 @pytest.mark.parametrize("path", list(PATH_CODES))
@@ -288,7 +296,7 @@ def test_gs_solver_matches_oracle(setup, torch_cuda):
     assert max(s.getLastMse(0), s.getLastMse(1)) < target
 
 
-@pytest.mark.parametrize("path", ["dsmem", "dsmem-restart", "grid", "cluster", "multikernel"])
+@pytest.mark.parametrize("path", ["dsmem", "dsmem-classic", "dsmem-restart", "grid", "cluster", "multikernel"])
 def test_mixed_pcg_reaches_fp64_tolerance(setup, torch_cuda, path, monkeypatch, capfd):
     """FP32 inner CG + FP64 correction reaches the FP64 tolerance on the true residual: with FP64
     residual replacement inside the cluster solve (dsmem) and with restarted refinement passes."""
