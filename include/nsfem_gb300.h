@@ -170,6 +170,28 @@ int nsf_solver_stats(nsf_solver s, int *iters, double *rms, double *rel);
 int nsf_solver_set(nsf_solver s, int maxIters, double target, int checkInterval);
 void nsf_solver_destroy(nsf_solver s);
 
+/* ============================================== pure-Neumann Poisson: pin and zero mean ======= */
+
+typedef struct nsf_neumann_s *nsf_neumann;
+
+/* A symmetric positive semi-definite system whose null space is the constants (the P1 Laplacian of
+   a domain with Neumann conditions everywhere, e.g. the standalone pressure-Poisson benchmark),
+   made regular by one Dirichlet pin: row and column `pin` are removed and the rest is solved with
+   the "pcg" solver of nsf_solver_create (multicolor SGS preconditioner; precision NSF_PREC_F64 or
+   NSF_PREC_MIXED), to ||b' - A' x'|| <= target ||b'|| on the pinned system.  No counterpart in the
+   reference (its pressure always has Dirichlet nodes on the outflow, buildContext.cpp:64-93): it
+   is the pressure zero-mean / pin correction of the standalone solve, done on the device in FP64. */
+int nsf_neumann_create(int n, const int *rowStart, const int *col, const double *values, int pin, int precision,
+                       int maxIters, double target, nsf_neumann *out);
+/* b, x: device FP64 vectors of n entries; x holds the initial guess.  On the device, in FP64: b is
+   projected to zero mean (b - sum(b)/n), the pinned row dropped, the pinned system solved from x
+   shifted to x[pin] = 0, the solution expanded with x[pin] = 0 and shifted to zero mean.
+   Synchronous: returns the solver status. */
+int nsf_neumann_solve(nsf_neumann h, const double *b, double *x, void *stream);
+/* iterations and relative residual (of the pinned system) of the last solve; either may be NULL */
+int nsf_neumann_stats(nsf_neumann h, int *iters, double *rel);
+void nsf_neumann_destroy(nsf_neumann h);
+
 /* ================================================================= Chorin stepper ======= */
 
 typedef struct

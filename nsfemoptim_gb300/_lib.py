@@ -73,6 +73,11 @@ _SIGS = {
     "nsf_solver_stats": (C.c_int, [vp, i32p, f64p, f64p]),
     "nsf_solver_set": (C.c_int, [vp, C.c_int, C.c_double, C.c_int]),
     "nsf_solver_destroy": (None, [vp]),
+    "nsf_neumann_create": (C.c_int, [C.c_int, i32p, i32p, f64p, C.c_int, C.c_int, C.c_int, C.c_double,
+                                     C.POINTER(vp)]),
+    "nsf_neumann_solve": (C.c_int, [vp, vp, vp, vp]),
+    "nsf_neumann_stats": (C.c_int, [vp, i32p, f64p]),
+    "nsf_neumann_destroy": (None, [vp]),
     "nsf_chorin_create": (C.c_int, [vp, C.POINTER(ChorinConfig), C.POINTER(vp)]),
     "nsf_chorin_step": (C.c_int, [vp, C.c_int, vp]),
     "nsf_chorin_launch": (C.c_int, [vp, C.c_int, vp]),

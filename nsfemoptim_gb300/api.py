@@ -335,6 +335,38 @@ class AbstractSolver:
             self._h = None
 
 
+class NeumannSolver:
+    """Pure-Neumann Poisson solve made regular by one Dirichlet pin (nsf_neumann_*): on the device, the
+    right-hand side is projected to zero mean, the system without row/column `pin` is solved with
+    the "pcg" solver, and the solution is expanded (x[pin] = 0) and shifted to zero mean, in FP64.
+    solve(b, x): device FP64 tensors of n entries, x the initial guess."""
+
+    def __init__(self, m: HostCsr, pin: int = 0, precision: int = NSF_PREC_F64, max_iters: int = 20000,
+                 target: float = 1e-10):
+        if m.rows != m.cols:
+            raise NsfError(1, "matrix must be square")
+        h = vp()
+        rs, ci = _i32(m.rowStart), _i32(m.column)
+        va = np.ascontiguousarray(m.values, dtype=np.float64)
+        check(lib().nsf_neumann_create(m.rows, _p(rs, C.c_int), _p(ci, C.c_int), _p(va, C.c_double), int(pin),
+                                       precision, max_iters, target, C.byref(h)))
+        self._h, self.n, self.pin = h, m.rows, pin
+
+    def solve(self, b, x, stream=None):
+        return check(lib().nsf_neumann_solve(self._h, _dptr(b), _dptr(x), stream))
+
+    def stats(self):
+        it = C.c_int(0)
+        rel = C.c_double(0.0)
+        check(lib().nsf_neumann_stats(self._h, C.byref(it), C.byref(rel)))
+        return {"iters": it.value, "rel": rel.value}
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            lib().nsf_neumann_destroy(self._h)
+            self._h = None
+
+
 def create_solver(name: str, numCh: int, m: HostCsr, maxIters: int, targetMse: float, mseCheckInterval: int,
                   precision: int = NSF_PREC_F64) -> AbstractSolver:
     """cu::createSolver: "gs" (multicolor Gauss-Seidel, absolute RMS target) or "pcg" (CG with the
@@ -523,6 +555,7 @@ class Adjoint:
 
 
 __all__ = ["Mesh", "load_gmsh", "ChorinContext", "build_chorin_context", "coloring", "CsrF", "Spmv", "Spmm",
+           "NeumannSolver",
            "spmv", "spmm", "fastconv_apply", "fastconv_apply_df", "split_df", "AbstractSolver", "create_solver", "ChorinStepper", "kernel_launches",
            "Forces", "Adjoint", "Pack", "NSF_F32", "NSF_F64", "NSF_PREC_F64", "NSF_PREC_MIXED", "NSF_PREC_F64_MIXEDSOLVE",
            "NsfError"]

@@ -918,6 +918,146 @@ extern "C" int nsf_solver_stats(nsf_solver s, int * iters, double * rms, double 
 
 extern "C" void nsf_solver_destroy(nsf_solver s) { delete s; }
 
+// ============================================================ pure-Neumann Poisson (pin + zero mean)
+
+namespace nsf
+{
+    // FP64 sum of x[0..n) into out[0]: fixed-order block sums, the last block adds them up.
+    __global__ void __launch_bounds__(TPB) kSumVec(int n, const double * __restrict__ x, double * scratch,
+                                                    unsigned * ticket, double * out)
+    {
+        double v[1] = {0.0};
+        for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+            v[0] += x[i];
+        Outs<1> o;
+        o.p[0] = out;
+        gridSum<double, 1>(v, scratch, o, ticket, nullptr);
+    }
+
+    // Reduced right-hand side: b projected to zero mean (mean = sum / n), the pinned row dropped.
+    __global__ void __launch_bounds__(TPB) kNeumannRhs(int n, int pin, const double * __restrict__ b,
+                                                        const double * __restrict__ sum, double * __restrict__ bRed)
+    {
+        const double mean = sum[0] / (double)n;
+        for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+            if (i != pin)
+                bRed[i - (i > pin)] = b[i] - mean;
+    }
+
+    // Reduced initial guess: x shifted so that the pinned entry is zero, the pinned entry dropped.
+    __global__ void __launch_bounds__(TPB) kNeumannGuess(int n, int pin, const double * __restrict__ x,
+                                                          double * __restrict__ xRed)
+    {
+        const double x0 = x[pin];
+        for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+            if (i != pin)
+                xRed[i - (i > pin)] = x[i] - x0;
+    }
+
+    // x = the reduced solution with the pinned entry 0
+    __global__ void __launch_bounds__(TPB) kNeumannExpand(int n, int pin, const double * __restrict__ xRed,
+                                                           double * __restrict__ x)
+    {
+        for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+            x[i] = i == pin ? 0.0 : xRed[i - (i > pin)];
+    }
+
+    // x -= sum / n (the zero-mean representative of the solution)
+    __global__ void __launch_bounds__(TPB) kShiftMean(int n, double * __restrict__ x, const double * __restrict__ sum)
+    {
+        const double mean = sum[0] / (double)n;
+        for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+            x[i] -= mean;
+    }
+} // namespace nsf
+
+struct nsf_neumann_s
+{
+    int n = 0, pin = 0;
+    nsf_solver inner = nullptr;
+    DevBuf<double> bRed, xRed, scratch, sums;
+    DevBuf<unsigned> ticket;
+    ~nsf_neumann_s()
+    {
+        if (inner)
+            nsf_solver_destroy(inner);
+    }
+};
+
+extern "C" int nsf_neumann_create(int n, const int * rowStart, const int * col, const double * values, int pin,
+                                  int precision, int maxIters, double target, nsf_neumann * out)
+{
+    return guarded([&] {
+        require(out && rowStart && col && values, "null argument");
+        require(n >= 2, "n must be >= 2");
+        require(pin >= 0 && pin < n, "pin outside 0..n-1");
+        std::string why;
+        require(validCsr(n, n, rowStart[n], rowStart, col, why), "invalid CSR: " + why);
+        // the system without row and column `pin`
+        std::vector<int> rs(1, 0), ci;
+        std::vector<double> va;
+        ci.reserve(rowStart[n]);
+        va.reserve(rowStart[n]);
+        for (int i = 0; i < n; i++)
+        {
+            if (i == pin)
+                continue;
+            for (int j = rowStart[i]; j < rowStart[i + 1]; j++)
+                if (col[j] != pin)
+                {
+                    ci.push_back(col[j] - (col[j] > pin));
+                    va.push_back(values[j]);
+                }
+            rs.push_back((int)ci.size());
+        }
+        auto h = std::make_unique<nsf_neumann_s>();
+        h->n = n;
+        h->pin = pin;
+        const int st = nsf_solver_create("pcg", 1, n - 1, rs.data(), ci.data(), va.data(), precision, maxIters, target,
+                                         1, &h->inner);
+        if (st != NSF_OK)
+            throw Error(st, lastError);
+        h->bRed.alloc((size_t)n - 1);
+        h->xRed.alloc((size_t)n - 1);
+        const int g = cappedBlocks(n);
+        h->scratch.alloc((size_t)g);
+        h->sums.alloc(2);
+        h->ticket.alloc(1);
+        NSF_CUDA(cudaMemset(h->ticket.get(), 0, sizeof(unsigned)));
+        *out = h.release();
+    });
+}
+
+extern "C" int nsf_neumann_solve(nsf_neumann h, const double * b, double * x, void * stream)
+{
+    return guarded([&] {
+        require(h && b && x, "null argument");
+        cudaStream_t s = asStream(stream);
+        const int n = h->n, g = cappedBlocks(n), gb = blocksFor(n);
+        NSF_LAUNCH(kSumVec, g, s, n, b, h->scratch.get(), h->ticket.get(), h->sums.get());
+        NSF_LAUNCH(kNeumannRhs, gb, s, n, h->pin, b, (const double *)h->sums.get(), h->bRed.get());
+        NSF_LAUNCH(kNeumannGuess, gb, s, n, h->pin, (const double *)x, h->xRed.get());
+        const int st = nsf_solver_solve(h->inner, h->bRed.get(), h->xRed.get(), s);
+        NSF_LAUNCH(kNeumannExpand, gb, s, n, h->pin, (const double *)h->xRed.get(), x);
+        NSF_LAUNCH(kSumVec, g, s, n, (const double *)x, h->scratch.get(), h->ticket.get(), h->sums.get() + 1);
+        NSF_LAUNCH(kShiftMean, gb, s, n, x, (const double *)h->sums.get() + 1);
+        if (st != NSF_OK)
+            throw Error(st, lastError);
+    });
+}
+
+extern "C" int nsf_neumann_stats(nsf_neumann h, int * iters, double * rel)
+{
+    return guarded([&] {
+        require(h, "null handle");
+        const int st = nsf_solver_stats(h->inner, iters, nullptr, rel);
+        if (st != NSF_OK)
+            throw Error(st, lastError);
+    });
+}
+
+extern "C" void nsf_neumann_destroy(nsf_neumann h) { delete h; }
+
 // ============================================================================ Chorin stepper
 
 struct nsf_chorin_s
