@@ -91,6 +91,25 @@ void nsf_context_destroy(nsf_context ctx);
    linalg::partitionGraphGreedy (cpp/libs/LinAlg/src/graphs.cpp:64-176). */
 int nsf_coloring(int n, const int *rowStart, const int *col, int *perm, int *partStart, int *nColors);
 
+/* ====================================================== binary CSR / vector interchange files == */
+
+/* The reference's binary format (cpp/libs/LinAlg/src/io.cpp:49-148: linalg::write, linalg::readCsr,
+   linalg::readVec): native byte order, CSR = int dtype (0 float, 1 double), int rows, int cols,
+   int nnz, values[nnz], column[nnz], rowStart[rows + 1]; vector = int dtype, int n, values[n].
+   Values are passed as doubles; dtype says how they are stored in the file.  Reading fails with
+   NSF_ERR_IO on what the reference's reader rejects (bad dtype, non-positive sizes, short data,
+   rowStart[rows] != nnz) and on unsorted or out-of-range columns. */
+/* info[0..3] = rows, cols, nnz, dtype of a CSR file */
+int nsf_io_csr_info(const char *path, int *info);
+/* rowStart[rows + 1], col[nnz], values[nnz] (sizes from nsf_io_csr_info) */
+int nsf_io_read_csr(const char *path, int *rowStart, int *col, double *values);
+int nsf_io_write_csr(const char *path, int rows, int cols, int nnz, const int *rowStart, const int *col,
+                     const double *values, int dtype);
+/* info[0..1] = n, dtype of a vector file */
+int nsf_io_vec_info(const char *path, int *info);
+int nsf_io_read_vec(const char *path, double *values);
+int nsf_io_write_vec(const char *path, int n, const double *values, int dtype);
+
 /* ===================================================================== device CSR ======= */
 
 typedef struct nsf_csr_s *nsf_csr;
@@ -164,6 +183,11 @@ int nsf_solver_create(const char *method, int numCh, int n, const int *rowStart,
 /* Solve A x = b for numCh planar channels; b and x are device FP64 vectors of numCh * n
    entries; x holds the initial guess on entry.  Synchronous: returns the solver status. */
 int nsf_solver_solve(nsf_solver s, const double *b, double *x, void *stream);
+/* The same with host vectors (numCh * n doubles each; x holds the initial guess and receives the
+   solution, also when the solve ends with a non-OK status).  Replaces the host wrappers
+   cu::GaussSeidelHost::solve and cu::ConjGradHost::solve (cpp/libs/CudaUtils/src/gaussSeidelHost.cu,
+   conjGradHost.cu) that the reference's solver test uses. */
+int nsf_solver_solve_host(nsf_solver s, const double *b, double *x);
 /* iters: iterations of the last solve; rms[numCh]: RMS residual per channel (getLastMse);
    rel[numCh]: relative residual per channel; any pointer may be NULL */
 int nsf_solver_stats(nsf_solver s, int *iters, double *rms, double *rel);
@@ -248,6 +272,12 @@ int nsf_chorin_launch(nsf_chorin s, int nSteps, void *stream);
 /* copy the state to/from host memory in the original numbering: u[2N] planar, p[P] */
 int nsf_chorin_get_state(nsf_chorin s, double *u, double *p, void *stream);
 int nsf_chorin_set_state(nsf_chorin s, const double *u, const double *p, void *stream);
+/* Headless frame output: the state in the original numbering written as two vector files of the
+   binary interchange format (nsf_io_*), u (2N planar) to uPath and p (P) to pPath (either may be
+   NULL), values as dtype (NSF_F32 or NSF_F64).  Synchronous.  Replaces the solution frames that
+   the reference's solver loop renders to images every few steps
+   (cpp/execs/NavierStokes/src/navierStokes.cpp:85-119), keeping the fields instead of a picture. */
+int nsf_chorin_dump(nsf_chorin s, const char *uPath, const char *pPath, int dtype, void *stream);
 /* nsf_chorin_set_state with flags.  NSF_STATE_KEEP_HISTORY: the state continues the stepper's run
    (a host that reads the state, and writes it back, every step), so the pressure-guess history
    (pressureGuess 1 and 2: the earlier solutions) is kept; nsf_chorin_set_state starts a new one.

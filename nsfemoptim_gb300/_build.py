@@ -14,9 +14,10 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libnsfem_gb300.so")
+CLI = os.path.join(HERE, "nsf_solver_test")
 NVCC = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-HOST_SOURCES = ["host/mesh.cpp", "host/context.cpp"]
+HOST_SOURCES = ["host/mesh.cpp", "host/context.cpp", "host/io.cpp"]
 CUDA_SOURCES = ["capi.cu"]
 
 
@@ -60,6 +61,11 @@ def build(verbose: bool = False, force: bool = False) -> str:
                 print(out, file=sys.stderr)
     if force or jobs or not os.path.exists(LIB):
         _run([NVCC, *ARCH, "-shared", "-cudart", "static", "-o", LIB, *objs])
+    # the SolverTest-compatible command-line tool, over the C ABI of the library
+    cli_src = os.path.join(HERE, "cli", "solver_test.cpp")
+    if force or _newer(CLI, [cli_src, LIB, os.path.join(HERE, "..", "include", "nsfem_gb300.h")]):
+        _run(["g++", "-std=c++17", "-O2", "-Wall", cli_src, "-o", CLI, "-L" + HERE, "-lnsfem_gb300",
+              "-Wl,-rpath,$ORIGIN"])
     return LIB
 
 

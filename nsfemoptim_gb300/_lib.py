@@ -70,9 +70,17 @@ _SIGS = {
     "nsf_solver_create": (C.c_int, [C.c_char_p, C.c_int, C.c_int, i32p, i32p, f64p, C.c_int, C.c_int, C.c_double,
                                     C.c_int, C.POINTER(vp)]),
     "nsf_solver_solve": (C.c_int, [vp, vp, vp, vp]),
+    "nsf_solver_solve_host": (C.c_int, [vp, f64p, f64p]),
     "nsf_solver_stats": (C.c_int, [vp, i32p, f64p, f64p]),
     "nsf_solver_set": (C.c_int, [vp, C.c_int, C.c_double, C.c_int]),
     "nsf_solver_destroy": (None, [vp]),
+    "nsf_io_csr_info": (C.c_int, [C.c_char_p, i32p]),
+    "nsf_io_read_csr": (C.c_int, [C.c_char_p, i32p, i32p, f64p]),
+    "nsf_io_write_csr": (C.c_int, [C.c_char_p, C.c_int, C.c_int, C.c_int, i32p, i32p, f64p, C.c_int]),
+    "nsf_io_vec_info": (C.c_int, [C.c_char_p, i32p]),
+    "nsf_io_read_vec": (C.c_int, [C.c_char_p, f64p]),
+    "nsf_io_write_vec": (C.c_int, [C.c_char_p, C.c_int, f64p, C.c_int]),
+    "nsf_chorin_dump": (C.c_int, [vp, C.c_char_p, C.c_char_p, C.c_int, vp]),
     "nsf_neumann_create": (C.c_int, [C.c_int, i32p, i32p, f64p, C.c_int, C.c_int, C.c_int, C.c_double,
                                      C.POINTER(vp)]),
     "nsf_neumann_solve": (C.c_int, [vp, vp, vp, vp]),

@@ -428,6 +428,12 @@ class ChorinStepper:
         check(lib().nsf_chorin_set_state_ex(self._h, _p(u, C.c_double), _p(p, C.c_double),
                                             1 if keep_history else 0, None))
 
+    def dump(self, u_path=None, p_path=None, dtype=NSF_F64):
+        """Headless frame output (nsf_chorin_dump): u (2N, planar) and p (P) in the original numbering
+        to vector files of the reference's binary format, as float (NSF_F32) or double (NSF_F64)."""
+        check(lib().nsf_chorin_dump(self._h, u_path.encode() if u_path else None,
+                                    p_path.encode() if p_path else None, dtype, None))
+
     def set_dirichlet(self, dir_vx, stream=None):
         """Replace the x values of the Dirichlet velocity nodes (ctx.dir_ids order) and impose them
         on the current state.  New: the reference fixes the inflow for a run."""

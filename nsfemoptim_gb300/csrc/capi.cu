@@ -566,6 +566,113 @@ extern "C" int nsf_coloring(int n, const int * rowStart, const int * col, int * 
     });
 }
 
+// ============================================================ binary CSR / vector files
+
+extern "C" int nsf_io_csr_info(const char * path, int * info)
+{
+    return guarded([&] {
+        require(path && info, "null argument");
+        try
+        {
+            const BinCsr m = readBinCsr(path);
+            info[0] = m.a.rows;
+            info[1] = m.a.cols;
+            info[2] = m.a.nnz();
+            info[3] = m.dtype;
+        }
+        catch (const std::runtime_error & e)
+        {
+            throw Error(ST_IO, e.what());
+        }
+    });
+}
+
+extern "C" int nsf_io_read_csr(const char * path, int * rowStart, int * col, double * values)
+{
+    return guarded([&] {
+        require(path && rowStart && col && values, "null argument");
+        try
+        {
+            const BinCsr m = readBinCsr(path);
+            std::copy(m.a.rowStart.begin(), m.a.rowStart.end(), rowStart);
+            std::copy(m.a.col.begin(), m.a.col.end(), col);
+            std::copy(m.a.val.begin(), m.a.val.end(), values);
+        }
+        catch (const std::runtime_error & e)
+        {
+            throw Error(ST_IO, e.what());
+        }
+    });
+}
+
+extern "C" int nsf_io_write_csr(const char * path, int rows, int cols, int nnz, const int * rowStart, const int * col,
+                                const double * values, int dtype)
+{
+    return guarded([&] {
+        require(path && rowStart && col && values, "null argument");
+        require(rows >= 1 && cols >= 1 && nnz >= 1, "rows, cols and nnz must be >= 1");
+        std::string why;
+        require(validCsr(rows, cols, nnz, rowStart, col, why), "invalid CSR: " + why);
+        try
+        {
+            writeBinCsr(path, rows, cols, nnz, rowStart, col, values, dtype);
+        }
+        catch (const std::runtime_error & e)
+        {
+            throw Error(ST_IO, e.what());
+        }
+    });
+}
+
+extern "C" int nsf_io_vec_info(const char * path, int * info)
+{
+    return guarded([&] {
+        require(path && info, "null argument");
+        try
+        {
+            const BinVec v = readBinVec(path);
+            info[0] = (int)v.v.size();
+            info[1] = v.dtype;
+        }
+        catch (const std::runtime_error & e)
+        {
+            throw Error(ST_IO, e.what());
+        }
+    });
+}
+
+extern "C" int nsf_io_read_vec(const char * path, double * values)
+{
+    return guarded([&] {
+        require(path && values, "null argument");
+        try
+        {
+            const BinVec v = readBinVec(path);
+            std::copy(v.v.begin(), v.v.end(), values);
+        }
+        catch (const std::runtime_error & e)
+        {
+            throw Error(ST_IO, e.what());
+        }
+    });
+}
+
+extern "C" int nsf_io_write_vec(const char * path, int n, const double * values, int dtype)
+{
+    return guarded([&] {
+        require(path && values, "null argument");
+        require(n >= 1, "n must be >= 1");
+        try
+        {
+            writeBinVec(path, n, values, dtype);
+        }
+        catch (const std::runtime_error & e)
+        {
+            throw Error(ST_IO, e.what());
+        }
+    });
+}
+
 // ============================================================================ device CSR
 
 extern "C" int nsf_csr_create(int rows, int cols, int nnz, const int * rowStart, const int * col, const void * values,
@@ -751,6 +858,7 @@ struct nsf_solver_s
     MixedPcg<1> mix1;
     MixedPcg<2> mix2;
     DevBuf<double> bp, xp;
+    DevBuf<double> hostB, hostX; // device copies for nsf_solver_solve_host (allocated on first use)
     cudaStream_t body = nullptr;
     PinnedBuf<SolverState> stat{1};
     SolverState last{};
@@ -894,6 +1002,33 @@ extern "C" int nsf_solver_solve(nsf_solver s, const double * b, double * x, void
             throw Error(worst, std::string("solver finished with status ") + nsf_status_string(worst));
     });
     return st;
+}
+
+extern "C" int nsf_solver_solve_host(nsf_solver s, const double * b, double * x)
+{
+    int st = guarded([&] {
+        require(s && b && x, "null argument");
+        const size_t len = (size_t)s->numCh * s->n;
+        if (!s->hostB.get())
+        {
+            s->hostB.alloc(len);
+            s->hostX.alloc(len);
+        }
+        NSF_CUDA(cudaMemcpy(s->hostB.get(), b, sizeof(double) * len, cudaMemcpyHostToDevice));
+        NSF_CUDA(cudaMemcpy(s->hostX.get(), x, sizeof(double) * len, cudaMemcpyHostToDevice));
+    });
+    if (st != NSF_OK)
+        return st;
+    const int solved = nsf_solver_solve(s, s->hostB.get(), s->hostX.get(), nullptr);
+    const std::string err = solved != NSF_OK ? lastError : std::string();
+    st = guarded([&] {
+        NSF_CUDA(cudaMemcpy(x, s->hostX.get(), sizeof(double) * (size_t)s->numCh * s->n, cudaMemcpyDeviceToHost));
+    });
+    if (st != NSF_OK)
+        return st;
+    if (solved != NSF_OK)
+        lastError = err;
+    return solved;
 }
 
 extern "C" int nsf_solver_stats(nsf_solver s, int * iters, double * rms, double * rel)
@@ -1594,6 +1729,29 @@ extern "C" int nsf_chorin_get_state(nsf_chorin S, double * uOut, double * pOut, 
             NSF_CUDA(cudaMemcpyAsync(pOut, sp, sizeof(double) * S->P, cudaMemcpyDeviceToHost, s));
         }
         NSF_CUDA(cudaStreamSynchronize(s));
+    });
+}
+
+extern "C" int nsf_chorin_dump(nsf_chorin S, const char * uPath, const char * pPath, int dtype, void * stream)
+{
+    return guarded([&] {
+        require(S, "null stepper");
+        require(dtype == NSF_F32 || dtype == NSF_F64, "dtype must be NSF_F32 or NSF_F64");
+        std::vector<double> u(uPath ? 2 * (size_t)S->N : 0), p(pPath ? (size_t)S->P : 0);
+        const int st = nsf_chorin_get_state(S, uPath ? u.data() : nullptr, pPath ? p.data() : nullptr, stream);
+        if (st != NSF_OK)
+            throw Error(st, lastError);
+        try
+        {
+            if (uPath)
+                writeBinVec(uPath, 2 * S->N, u.data(), dtype);
+            if (pPath)
+                writeBinVec(pPath, S->P, p.data(), dtype);
+        }
+        catch (const std::runtime_error & e)
+        {
+            throw Error(ST_IO, e.what());
+        }
     });
 }
 

@@ -73,4 +73,23 @@ namespace nsf
 
     // validates a CSR: sizes, rowStart monotone, columns sorted/unique/in range
     bool validCsr(int rows, int cols, int nnz, const int * rowStart, const int * col, std::string & why);
+
+    // Binary CSR / vector files in the reference's interchange format (host/io.cpp); values are
+    // widened to double on reading, dtype says what the file held (0 float, 1 double).  Errors throw
+    // std::runtime_error (I/O, format) or std::invalid_argument (arguments).
+    struct BinCsr
+    {
+        int dtype = 1;
+        HostCsr<double> a;
+    };
+    struct BinVec
+    {
+        int dtype = 1;
+        std::vector<double> v;
+    };
+    BinCsr readBinCsr(const std::string & path);
+    void writeBinCsr(const std::string & path, int rows, int cols, int nnz, const int * rowStart, const int * col,
+                     const double * values, int dtype);
+    BinVec readBinVec(const std::string & path);
+    void writeBinVec(const std::string & path, int n, const double * values, int dtype);
 } // namespace nsf

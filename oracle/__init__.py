@@ -560,6 +560,14 @@ def reference():
         R.ref_local_matrices.argtypes = [C.c_void_p, C.c_int] + [f32p] * 8
         R.ref_fastconv_values.restype = C.c_int
         R.ref_fastconv_values.argtypes = [C.c_void_p, f32p]
+        R.ref_io_write_csr.restype = C.c_int
+        R.ref_io_write_csr.argtypes = [C.c_char_p, C.c_int, C.c_int, C.c_int, C.c_int, i32p, i32p, f64p]
+        R.ref_io_read_csr.restype = C.c_int
+        R.ref_io_read_csr.argtypes = [C.c_char_p, C.c_int, i32p, i32p, i32p, f64p]
+        R.ref_io_write_vec.restype = C.c_int
+        R.ref_io_write_vec.argtypes = [C.c_char_p, C.c_int, C.c_int, f64p]
+        R.ref_io_read_vec.restype = C.c_int
+        R.ref_io_read_vec.argtypes = [C.c_char_p, C.c_int, i32p, f64p]
         _REF = R
     return _REF
 

@@ -13,6 +13,7 @@
 //   buildCsrGraph / buildSmallestLastOrdering / partitionGraphGreedy  cpp/libs/LinAlg/src/graphs.cpp
 //   CsrMatrix<float>::slice        cpp/libs/LinAlg/src/csrMatrix.cpp:12-91
 //   gaussSeidel2ch<double>         cpp/libs/LinAlg/src/gaussSeidel.cpp:215-230
+//   linalg::write / readCsr / readVec   cpp/libs/LinAlg/src/io.cpp:49-192 (binary interchange files)
 //   buildChorinCsrMatrices<float>  cpp/libs/Fem/src/chorinCsr.cpp:436-502 (assembled FP32 values)
 //   TriangleIntegrator             cpp/libs/Element/src/triangleIntegrator.cpp:113-293 (local matrices)
 // Those two files include OpenCV for cv::Mat; they compile here against the test-only stand-in in
@@ -33,6 +34,7 @@
 #include <fem/chorinCsr.h>
 #include <linalg/csrMatrix.h>
 #include <linalg/gaussSeidel.h>
+#include <linalg/io.h>
 #include <linalg/graphs.h>
 #include <linalg/sparseDokBuilder.h>
 #include <mesh/concreteMesh.h>
@@ -60,6 +62,40 @@ namespace
     };
 
     thread_local std::string lastError;
+
+    template <typename F>
+    int refWriteCsr(const char * path, int rows, int cols, int nnz, const int * rs, const int * ci,
+                           const double * v)
+    {
+        linalg::CsrMatrix<F> m;
+        m.rows = rows;
+        m.cols = cols;
+        m.rowStart.assign(rs, rs + rows + 1);
+        m.column.assign(ci, ci + nnz);
+        m.values.resize(nnz);
+        for (int i = 0; i < nnz; i++)
+            m.values[i] = (F)v[i];
+        linalg::write(std::string(path), m);
+        return 0;
+    }
+
+    template <typename F>
+    int refReadCsr(const char * path, int * dims, int * rs, int * ci, double * v)
+    {
+        const auto m = linalg::readCsr<F>(std::string(path));
+        dims[0] = m.rows;
+        dims[1] = m.cols;
+        dims[2] = (int)m.column.size();
+        if (rs)
+        {
+            std::copy(m.rowStart.begin(), m.rowStart.end(), rs);
+            std::copy(m.column.begin(), m.column.end(), ci);
+            for (size_t i = 0; i < m.values.size(); i++)
+                v[i] = m.values[i];
+        }
+        return 0;
+    }
+
 }
 
 extern "C"
@@ -511,6 +547,81 @@ extern "C"
                             values[it - I.column.data()] += conv.at<float>(r, c);
                         }
                 }
+            }
+            return 0;
+        }
+        catch (const std::exception & e)
+        {
+            lastError = e.what();
+            return -1;
+        }
+    }
+
+    // Binary interchange files through the reference's linalg::write / readCsr / readVec.  dtype 0
+    // float, 1 double; values passed as doubles.  Reading with rowStart == null returns the sizes in
+    // dims (rows, cols, nnz) only.  0 on success, -1 with ref_last_error().
+    int ref_io_write_csr(const char * path, int dtype, int rows, int cols, int nnz, const int * rs, const int * ci,
+                         const double * v)
+    {
+        try
+        {
+            return dtype == 0 ? refWriteCsr<float>(path, rows, cols, nnz, rs, ci, v)
+                              : refWriteCsr<double>(path, rows, cols, nnz, rs, ci, v);
+        }
+        catch (const std::exception & e)
+        {
+            lastError = e.what();
+            return -1;
+        }
+    }
+
+    int ref_io_read_csr(const char * path, int dtype, int * dims, int * rs, int * ci, double * v)
+    {
+        try
+        {
+            return dtype == 0 ? refReadCsr<float>(path, dims, rs, ci, v) : refReadCsr<double>(path, dims, rs, ci, v);
+        }
+        catch (const std::exception & e)
+        {
+            lastError = e.what();
+            return -1;
+        }
+    }
+
+    int ref_io_write_vec(const char * path, int dtype, int n, const double * v)
+    {
+        try
+        {
+            if (dtype == 0)
+                linalg::write(std::string(path), std::vector<float>(v, v + n));
+            else
+                linalg::write(std::string(path), std::vector<double>(v, v + n));
+            return 0;
+        }
+        catch (const std::exception & e)
+        {
+            lastError = e.what();
+            return -1;
+        }
+    }
+
+    int ref_io_read_vec(const char * path, int dtype, int * n, double * v)
+    {
+        try
+        {
+            if (dtype == 0)
+            {
+                const auto x = linalg::readVec<float>(std::string(path));
+                *n = (int)x.size();
+                if (v)
+                    std::copy(x.begin(), x.end(), v);
+            }
+            else
+            {
+                const auto x = linalg::readVec<double>(std::string(path));
+                *n = (int)x.size();
+                if (v)
+                    std::copy(x.begin(), x.end(), v);
             }
             return 0;
         }

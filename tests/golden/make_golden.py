@@ -11,6 +11,8 @@
 3. The reference's element integrator (triangleIntegrator.cpp, compiled into the same harness
    against a test-only cv::Mat stand-in) gives the FP32 local matrices of 48 seeded elements of the
    channel mesh: ref_local_<mesh>.npz.
+4. The reference's binary writer (linalg::write, io.cpp) writes the square's P1 Laplacian and a seeded
+   vector as float and double files: their SHA-256 digests go to ref_io_square_n33.json.
 
 Run from the repository root where the reference tree is present:
     python tests/golden/make_golden.py
@@ -136,6 +138,35 @@ def ref_local_sample(R, path: str, count: int = 48, seed: int = 0) -> dict:
     return out
 
 
+def ref_io_digests(R, square_path: str, seed: int = 11) -> dict:
+    """SHA-256 of the files the reference's linalg::write produces for the square's P1 Laplacian and
+    a seeded N(0, 1) vector, as float (dtype 0) and double (dtype 1)."""
+    import tempfile
+
+    import scipy.sparse as sp
+
+    m = oracle.Mesh(square_path)
+    rs, ci, val = meshgen.p1_stiffness(m.corner_xy.astype(np.float64), m.tri)
+    K = sp.csr_matrix((val, ci, rs))
+    K.sort_indices()
+    rs, ci, v = K.indptr.astype(np.int32), K.indices.astype(np.int32), K.data.astype(np.float64)
+    n = K.shape[0]
+    x = np.random.default_rng(seed).standard_normal(n)
+    out = {"vector_seed": seed, "n": n, "nnz": int(len(ci)), "csr_sha256": {}, "vec_sha256": {}}
+    with tempfile.TemporaryDirectory() as d:
+        for dtype in (0, 1):
+            p = os.path.join(d, "a.csr")
+            assert R.ref_io_write_csr(p.encode(), dtype, n, n, len(ci), oracle._ptr(rs, C.c_int),
+                                      oracle._ptr(ci, C.c_int), oracle._ptr(v, C.c_double)) == 0
+            with open(p, "rb") as f:
+                out["csr_sha256"][str(dtype)] = hashlib.sha256(f.read()).hexdigest()
+            p = os.path.join(d, "x.vec")
+            assert R.ref_io_write_vec(p.encode(), dtype, n, oracle._ptr(x, C.c_double)) == 0
+            with open(p, "rb") as f:
+                out["vec_sha256"][str(dtype)] = hashlib.sha256(f.read()).hexdigest()
+    return out
+
+
 def main():
     oracle.build()
     if not oracle.build_reference():
@@ -151,6 +182,9 @@ def main():
         res = ref_structures(R, raw, peak)
         if name.startswith("channel"):
             np.savez_compressed(os.path.join(HERE, f"ref_local_{name}.npz"), **ref_local_sample(R, raw))
+        else:
+            with open(os.path.join(HERE, "ref_io_square_n33.json"), "w") as f:
+                json.dump(ref_io_digests(R, raw), f, indent=1, sort_keys=True)
         os.remove(raw)
         with open(os.path.join(HERE, f"ref_{name}.json"), "w") as f:
             json.dump(res, f, indent=1, sort_keys=True)
