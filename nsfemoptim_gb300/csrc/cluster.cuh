@@ -38,7 +38,7 @@ namespace nsf
     constexpr int CTPB = 1024;                    // threads per CTA of the persistent solvers
     constexpr size_t kClusterSmemCap = 200 * 1024; // dynamic shared memory ceiling per CTA
     constexpr int RB = 8;                          // entries per predicated batch of a row
-    constexpr unsigned kGridSpinLimit = 1u << 22;  // polls of a grid barrier before it gives up (seconds)
+    constexpr unsigned kGridSpinLimit = 1u << 22;  // default polls of a grid barrier before it gives up (seconds)
 
     template <typename T>
     struct ClusterPcgArgs
@@ -327,6 +327,13 @@ namespace nsf
         unsigned * ctl = nullptr;
         T * slots = nullptr; // 2 buffers x 8 values x gridDim.x
         int buf = 0;
+        unsigned spinLimit = kGridSpinLimit; // polls of one wait before the barrier gives up
+        // Test hook (negative: off): CTA `quietRank` stops arriving at barriers from its
+        // `quietAfter`-th barrier on, so that the other CTAs' waits run out.  It waits for nobody
+        // either; its loop is bounded like every other CTA's.
+        int quietRank = -1;
+        unsigned quietAfter = 0;
+        unsigned count = 0; // barriers passed by this CTA (per-thread copy, identical in the CTA)
         __device__ __forceinline__ int rank() const { return (int)blockIdx.x; }
         __device__ __forceinline__ int size() const { return (int)gridDim.x; }
         __device__ __forceinline__ bool failed() const { return *(volatile unsigned *)(ctl + 2) != 0u; }
@@ -337,7 +344,9 @@ namespace nsf
         __device__ __forceinline__ void sync()
         {
             __syncthreads();
-            if (threadIdx.x == 0 && !failed())
+            const bool quiet = quietRank == (int)blockIdx.x && count >= quietAfter;
+            count++;
+            if (threadIdx.x == 0 && !quiet && !failed())
             {
                 const unsigned gen = ldAcquireGpu(ctl + 1); // read before arriving
                 const unsigned prev = atomAddAcqRelGpu(ctl, 1u);
@@ -351,7 +360,7 @@ namespace nsf
                     unsigned polls = 0;
                     while (ldAcquireGpu(ctl + 1) == gen)
                     {
-                        if (++polls > kGridSpinLimit || failed())
+                        if (++polls > spinLimit || failed())
                         {
                             atomicExch(ctl + 2, 1u);
                             break;

@@ -500,6 +500,25 @@ namespace nsf
                 GridSync<T> gs{};
                 gs.ctl = gridCtl.get();
                 gs.slots = gridSlots.get();
+                // NSF_GRID_SPIN_LIMIT: polls of one barrier wait before the solve gives up (default
+                // kGridSpinLimit, seconds).  NSF_GRID_TEST_QUIET_CTA="rank:after": test hook, CTA `rank`
+                // stops arriving at barriers after `after` of them, so the other CTAs' waits run out and
+                // the solve ends with status 5 (both read at each solve; an enqueue under stream
+                // capture fixes them for the graph).
+                const long long lim = std::atoll(envStr("NSF_GRID_SPIN_LIMIT", "0").c_str());
+                if (lim > 0)
+                    gs.spinLimit = (unsigned)std::min<long long>(lim, 0xFFFFFFFFll);
+                const std::string quiet = envStr("NSF_GRID_TEST_QUIET_CTA", "");
+                if (!quiet.empty())
+                {
+                    const size_t colon = quiet.find(':');
+                    gs.quietRank = std::atoi(quiet.substr(0, colon).c_str());
+                    gs.quietAfter =
+                        colon == std::string::npos ? 0u : (unsigned)std::atoi(quiet.substr(colon + 1).c_str());
+                    if (gs.quietRank < 1 || gs.quietRank >= clusterSize)
+                        throw Error(ST_INVALID, "NSF_GRID_TEST_QUIET_CTA: rank must be in 1.." +
+                                                    std::to_string(clusterSize - 1));
+                }
                 if (clusterShared)
                     launchCooperative(kPcgSweep<T, NCH, true, GridSync<T>>, clusterSize, clusterSmem, s, A, gs);
                 else

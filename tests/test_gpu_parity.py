@@ -324,6 +324,39 @@ def test_mixed_pcg_reaches_fp64_tolerance(setup, torch_cuda, path, monkeypatch, 
     assert _rel(x, xo) <= 1e-7
 
 
+def test_grid_barrier_wait_gives_up_and_next_solve_succeeds(setup, torch_cuda, monkeypatch):
+    """The software grid barrier of the cooperative-grid path gives up after a bounded number of
+    polls.  With the test hook NSF_GRID_TEST_QUIET_CTA one CTA stops arriving after a few barriers,
+    so every other CTA's wait runs out (NSF_GRID_SPIN_LIMIT = 2000 polls): the kernel ends in every
+    CTA, the solve reports NSF_ERR_CUDA (status 5: results not valid) within seconds, and the next
+    solve on the same solver, without the hook, matches the oracle."""
+    import time
+    G, O, mesh, ctx, om, oc = setup
+    t = torch_cuda
+    monkeypatch.setenv("NSF_PCG_PATH", "grid")
+    monkeypatch.setenv("NSF_GRID_SPIN_LIMIT", "2000")
+    kpi = ctx.matrix("Kpi")
+    b = np.random.default_rng(12).standard_normal(kpi.rows)
+    s = G.create_solver("pcg", 1, kpi, 3000, 1e-10, 1)
+    s.getRhs().copy_(t.tensor(b))
+    monkeypatch.setenv("NSF_GRID_TEST_QUIET_CTA", "3:5")
+    s.getSol().zero_()
+    t0 = time.perf_counter()
+    with pytest.raises(G.NsfError) as e:
+        s.solve()
+    elapsed = time.perf_counter() - t0
+    assert e.value.status == 5, e.value
+    assert elapsed < 10.0, elapsed
+    monkeypatch.delenv("NSF_GRID_TEST_QUIET_CTA")
+    s.getSol().zero_()
+    assert s.solve() == 0
+    xo, st, it, rr = O.pcg(oc.Kpi, O.coloring(oc.Kpi), b, np.zeros_like(b), 3000, 1e-10)
+    assert _rel(s.getSol().cpu().numpy(), xo) <= 1e-8
+    with pytest.raises(G.NsfError):  # rank 0 reports the status: the hook refuses to quiet it
+        monkeypatch.setenv("NSF_GRID_TEST_QUIET_CTA", "0:1")
+        s.solve()
+
+
 def test_solver_errors(setup, torch_cuda):
     G, O, mesh, ctx, om, oc = setup
     import nsfemoptim_gb300 as G2
