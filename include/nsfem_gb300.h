@@ -165,6 +165,21 @@ int nsf_fastconv_apply_df(nsf_csr I, const float *Kvals, double nu, const float 
 int nsf_residual_noalloc(nsf_csr a, int nrhs, const double *x, const double *b, double *r, double *norms2,
                          void *stream);
 
+/* =============================================== vector helpers (the cu:: call sites) ====== */
+/* Device vectors of dtype (NSF_F32 / NSF_F64), asynchronous on stream.  They replace the cuBLAS
+   calls and the small kernels around the reference's time step: cu::saxpy and cu::scale
+   (cpp/libs/CudaUtils/include/cu/blas.h:24-26, used at chorinCuda.cu:275,298,354), the Dirichlet
+   value scatter of DirichletVelocity::impose (chorinCuda.cu:59-74) and the internal-node gather /
+   scatter of PressureSolver (chorinCuda.cu:109-150). */
+/* y += alpha x (n entries) */
+int nsf_axpy(long long n, double alpha, const void *x, void *y, int dtype, void *stream);
+/* x *= alpha */
+int nsf_scale(long long n, double alpha, void *x, int dtype, void *stream);
+/* dst[i] = src[idx[i]], i < n (idx on the device) */
+int nsf_gather(int n, const int *idx, const void *src, void *dst, int dtype, void *stream);
+/* dst[idx[i]] = src[i], i < n (idx on the device) */
+int nsf_scatter(int n, const int *idx, const void *src, void *dst, int dtype, void *stream);
+
 /* ======================================================================== solvers ======= */
 
 typedef struct nsf_solver_s *nsf_solver;
@@ -183,6 +198,10 @@ int nsf_solver_create(const char *method, int numCh, int n, const int *rowStart,
 /* Solve A x = b for numCh planar channels; b and x are device FP64 vectors of numCh * n
    entries; x holds the initial guess on entry.  Synchronous: returns the solver status. */
 int nsf_solver_solve(nsf_solver s, const double *b, double *x, void *stream);
+/* The same with FP32 device vectors (widened to FP64 around the FP64 solve inside the library):
+   the IO vectors of the reference's cu::AbstractSolver are FP32 cu::vec (getRhs / getSol,
+   cpp/libs/CudaUtils/include/cu/solvers/abstractSolver.h:8-32).  Synchronous. */
+int nsf_solver_solve_f32(nsf_solver s, const float *b, float *x, void *stream);
 /* The same with host vectors (numCh * n doubles each; x holds the initial guess and receives the
    solution, also when the solve ends with a non-OK status).  Replaces the host wrappers
    cu::GaussSeidelHost::solve and cu::ConjGradHost::solve (cpp/libs/CudaUtils/src/gaussSeidelHost.cu,

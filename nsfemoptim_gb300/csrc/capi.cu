@@ -840,6 +840,92 @@ extern "C" int nsf_fastconv_apply(nsf_csr I, const void * K, double nu, const vo
     });
 }
 
+// ============================================================ vector helpers (the cu:: call sites)
+
+namespace nsf
+{
+    template <typename T>
+    __global__ void __launch_bounds__(TPB) kAxpy(long long n, T alpha, const T * __restrict__ x, T * __restrict__ y)
+    {
+        for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+            y[i] += alpha * x[i];
+    }
+
+    template <typename T>
+    __global__ void __launch_bounds__(TPB) kScale(long long n, T alpha, T * __restrict__ x)
+    {
+        for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+            x[i] *= alpha;
+    }
+
+    template <typename A, typename B>
+    __global__ void __launch_bounds__(TPB) kConvert(long long n, const A * __restrict__ a, B * __restrict__ b)
+    {
+        for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+            b[i] = (B)a[i];
+    }
+} // namespace nsf
+
+extern "C" int nsf_axpy(long long n, double alpha, const void * x, void * y, int dtype, void * stream)
+{
+    return guarded([&] {
+        require(n >= 0 && (n == 0 || (x && y)), "bad argument");
+        require(dtype == NSF_F32 || dtype == NSF_F64, "unknown dtype");
+        if (n == 0)
+            return;
+        cudaStream_t s = asStream(stream);
+        if (dtype == NSF_F32)
+            NSF_LAUNCH(kAxpy<float>, blocksFor(n), s, n, (float)alpha, (const float *)x, (float *)y);
+        else
+            NSF_LAUNCH(kAxpy<double>, blocksFor(n), s, n, alpha, (const double *)x, (double *)y);
+    });
+}
+
+extern "C" int nsf_scale(long long n, double alpha, void * x, int dtype, void * stream)
+{
+    return guarded([&] {
+        require(n >= 0 && (n == 0 || x), "bad argument");
+        require(dtype == NSF_F32 || dtype == NSF_F64, "unknown dtype");
+        if (n == 0)
+            return;
+        cudaStream_t s = asStream(stream);
+        if (dtype == NSF_F32)
+            NSF_LAUNCH(kScale<float>, blocksFor(n), s, n, (float)alpha, (float *)x);
+        else
+            NSF_LAUNCH(kScale<double>, blocksFor(n), s, n, alpha, (double *)x);
+    });
+}
+
+extern "C" int nsf_gather(int n, const int * idx, const void * src, void * dst, int dtype, void * stream)
+{
+    return guarded([&] {
+        require(n >= 0 && (n == 0 || (idx && src && dst)), "bad argument");
+        require(dtype == NSF_F32 || dtype == NSF_F64, "unknown dtype");
+        if (n == 0)
+            return;
+        cudaStream_t s = asStream(stream);
+        if (dtype == NSF_F32)
+            NSF_LAUNCH(kGatherPerm<float>, blocksFor(n), s, n, 1, idx, (const float *)src, (float *)dst);
+        else
+            NSF_LAUNCH(kGatherPerm<double>, blocksFor(n), s, n, 1, idx, (const double *)src, (double *)dst);
+    });
+}
+
+extern "C" int nsf_scatter(int n, const int * idx, const void * src, void * dst, int dtype, void * stream)
+{
+    return guarded([&] {
+        require(n >= 0 && (n == 0 || (idx && src && dst)), "bad argument");
+        require(dtype == NSF_F32 || dtype == NSF_F64, "unknown dtype");
+        if (n == 0)
+            return;
+        cudaStream_t s = asStream(stream);
+        if (dtype == NSF_F32)
+            NSF_LAUNCH(kScatterPerm<float>, blocksFor(n), s, n, 1, idx, (const float *)src, (float *)dst);
+        else
+            NSF_LAUNCH(kScatterPerm<double>, blocksFor(n), s, n, 1, idx, (const double *)src, (double *)dst);
+    });
+}
+
 // ============================================================================ solvers
 
 struct nsf_solver_s
@@ -1002,6 +1088,37 @@ extern "C" int nsf_solver_solve(nsf_solver s, const double * b, double * x, void
             throw Error(worst, std::string("solver finished with status ") + nsf_status_string(worst));
     });
     return st;
+}
+
+extern "C" int nsf_solver_solve_f32(nsf_solver s, const float * b, float * x, void * stream)
+{
+    int st = guarded([&] {
+        require(s && b && x, "null argument");
+        const long long len = (long long)s->numCh * s->n;
+        if (!s->hostB.get())
+        {
+            s->hostB.alloc((size_t)len);
+            s->hostX.alloc((size_t)len);
+        }
+        cudaStream_t cs = asStream(stream);
+        NSF_LAUNCH((kConvert<float, double>), blocksFor(len), cs, len, b, s->hostB.get());
+        NSF_LAUNCH((kConvert<float, double>), blocksFor(len), cs, len, (const float *)x, s->hostX.get());
+    });
+    if (st != NSF_OK)
+        return st;
+    const int solved = nsf_solver_solve(s, s->hostB.get(), s->hostX.get(), stream);
+    const std::string err = solved != NSF_OK ? lastError : std::string();
+    st = guarded([&] {
+        const long long len = (long long)s->numCh * s->n;
+        NSF_LAUNCH((kConvert<double, float>), blocksFor(len), asStream(stream), len, (const double *)s->hostX.get(),
+                   x);
+        NSF_CUDA(cudaStreamSynchronize(asStream(stream)));
+    });
+    if (st != NSF_OK)
+        return st;
+    if (solved != NSF_OK)
+        lastError = err;
+    return solved;
 }
 
 extern "C" int nsf_solver_solve_host(nsf_solver s, const double * b, double * x)
