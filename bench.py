@@ -450,6 +450,46 @@ def bench_batch(args):
     try:
         path = make_mesh(tmp, h, 0)
         mesh = G.load_gmsh(path)
+        # ---- batched: one context (peak 4.0 = 4 x U_max 1), each instance's inflow the context's
+        # scaled by its U_max; every operation of the step one launch for all instances (nsf_batch)
+        bctx = G.build_chorin_context(mesh, 4.0)
+        bdir = np.stack([bctx.dir_vx * float(umax[b]) for b in range(B)])
+        batch = G.Batch(bctx, nus, tau, dir_vx=bdir, vel_max_iters=500, vel_tol=VEL_TOL, pres_max_iters=5000,
+                        pres_tol=PRES_TOL, use_graph=True, max_outer=4, inner_tol=1e-5,
+                        pressure_guess=args.pressure_guess, pressure_basis=args.pressure_basis)
+        bstream = torch.cuda.Stream()
+        batch.step(W, bstream.cuda_stream)
+        torch.cuda.synchronize()
+
+        def tbatch(steps):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(bstream)
+            batch.launch(steps, bstream.cuda_stream)
+            e1.record(bstream)
+            torch.cuda.synchronize()
+            return e0.elapsed_time(e1) / 1e3
+
+        k0 = G.kernel_launches()
+        t_batch = tbatch(K)  # steps W+1 .. W+K: the window of the per-stream steppers
+        batch_launches = G.kernel_launches() - k0
+        batch.step(1, bstream.cuda_stream)
+        t_batch2 = tbatch(K)  # steps W+K+2 .. W+2K+1: the window of the one-graph pack
+        batch.step(1, bstream.cuda_stream)
+        bstats = [batch.stats(b) for b in range(B)]
+        del batch
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        # the FP64 drop-in on the same mesh (one instance, the reference's pressure guess)
+        f64 = G.ChorinStepper(bctx, float(np.median(nus)), tau, precision=G.NSF_PREC_F64, vel_method=args.vel_method,
+                              vel_max_iters=500, vel_tol=VEL_TOL, pres_max_iters=5000, pres_tol=PRES_TOL,
+                              check_interval=8, use_graph=True, pressure_guess=0)
+        f64.step(W, bstream.cuda_stream)
+        torch.cuda.synchronize()
+        e0.record(bstream)
+        f64.launch(K, bstream.cuda_stream)
+        e1.record(bstream)
+        torch.cuda.synchronize()
+        t_f64 = e0.elapsed_time(e1) / 1e3
+        del f64
         t0 = time.perf_counter()
         steppers = []
         for b in range(B):
@@ -512,19 +552,38 @@ def bench_batch(args):
         shutil.rmtree(tmp, ignore_errors=True)
     agg = B * K / t_all
     one = K / t_one
+    agg_batch = B * K / t_batch
+    f64_one = K / t_f64
     return {
         "metric": "config 4: batched channel instances (h=0.01), aggregate instance-steps/s",
-        "value": round(agg, 2), "unit": "instance-steps/s", "n_gpus": 1, "steps": K, "warmup": W,
+        "value": round(agg_batch, 2), "unit": "instance-steps/s", "n_gpus": 1, "steps": K, "warmup": W,
+        "batched": {"instance_steps_per_s": round(agg_batch, 2), "ms_per_step": round(1e3 * t_batch / K, 3),
+                    "window": f"steps {W + 1}..{W + K} from rest (the per-stream steppers' window)",
+                    "instance_steps_per_s_later_window": round(B * K / t_batch2, 2),
+                    "later_window": f"steps {W + K + 2}..{W + 2 * K + 1} (the one-graph pack's window)",
+                    "kernel_launches_per_step": round(batch_launches / K, 1),
+                    "execution": "nsf_batch: one context, every operation of the step one launch for all "
+                                 "instances (operator kernels instance-fastest, pressure solves one launch of "
+                                 f"{B} clusters), graph-captured; the pressure guess of the other variants",
+                    "pres_iters_range": [int(min(x["pres_iters"] for x in bstats)),
+                                         int(max(x["pres_iters"] for x in bstats))],
+                    "status_all_ok": all(int(x["status"]) == 0 for x in bstats)},
+        "fp64_drop_in_one_instance_steps_per_s": round(f64_one, 2),
+        "batched_mixed_over_fp64_drop_in": round(agg_batch / f64_one, 2),
         "higher_is_better": True, "dtype": "f32-inner/f64-refine",
         "data": "synthetic (seeded DFG channel mesh h=0.01; U_max, nu per instance from seed 0)",
         "config": {"workload": f"{B} instances, h=0.01, U_max~U[0.2,1.5], nu~logU[5e-4,2e-3], tau=2e-4, "
                                "pressure to 1e-8 rel", "instances": B, "setup_s": round(setup_s, 1),
                    "mass_solve": MASS_SOLVES[args.vel_method],
                    "pressure_guess": PRESSURE_GUESSES[args.pressure_guess].format(args.pressure_basis or 250),
-                   "execution": "one graph-captured stepper per instance on its own stream, cluster-resident solves"},
+                   "execution": "nsf_batch (batched kernels); per-stream steppers and the one-graph pack beside it"},
+        "per_stream_steppers": {"instance_steps_per_s": round(agg, 2),
+                                "execution": "one graph-captured stepper per instance on its own stream, "
+                                             "cluster-resident solves"},
         "one_instance_steps_per_s": round(one, 2),
-        "speedup_vs_one_at_a_time": round(agg / one, 2),
+        "batched_over_one_instance": round(agg_batch / one, 2),
         "one_graph_pack": {"instance_steps_per_s": round(B * K / t_pack, 2),
+                           "window": f"steps {W + K + 2}..{W + 2 * K + 1} from rest",
                            "execution": "all instances' steps as branches of one CUDA graph (nsf_pack), one launch "
                                         "per step"},
         "status_all_ok": all(s == 0 for s in status),

@@ -326,6 +326,37 @@ int nsf_pack_create(const nsf_chorin *steppers, int n, nsf_pack *out);
 int nsf_pack_step(nsf_pack p, int nSteps, void *stream);
 void nsf_pack_destroy(nsf_pack p);
 
+/* ================================================================== batched instances == */
+
+typedef struct nsf_batch_s *nsf_batch;
+
+/* nInst flows on the mesh of ctx, each with its own viscosity nu[q] and Dirichlet x values
+   dirVx[q * nDir + i] (context dirIds order; NULL: the context's values for every instance),
+   advanced together: every operation of the time step is one launch for all instances (the
+   operators are read by the instances together, the pressure solves are one launch of nInst
+   thread-block clusters).  Each instance computes exactly what an nsf_chorin stepper with the same
+   configuration computes.  cfg: NSF_PREC_MIXED, velMethod 3, any pressureGuess (2: one basis per
+   instance), presTol >= 1e-11;
+   cfg->nu is ignored.  No counterpart in the reference (its loop, chorinCuda.cu:236-376, advances one
+   flow): the many-instance workload of the parameter studies. */
+int nsf_batch_create(nsf_context ctx, const nsf_chorin_config *cfg, int nInst, const double *nu, const double *dirVx,
+                     nsf_batch *out);
+/* advance every instance nSteps steps (graph replays when cfg->useGraph), then wait and keep the
+   per-instance statistics; NSF_ERR_NONFINITE if a pressure residual became non-finite */
+int nsf_batch_step(nsf_batch b, int nSteps, void *stream);
+/* the same without waiting (statistics not updated) */
+int nsf_batch_launch(nsf_batch b, int nSteps, void *stream);
+/* state of instance inst in the original numbering: u[2N] planar, p[P]; synchronous */
+int nsf_batch_get_state(nsf_batch b, int inst, double *u, double *p, void *stream);
+/* set it (a new pressure history for that instance); synchronous */
+int nsf_batch_set_state(nsf_batch b, int inst, const double *u, const double *p, void *stream);
+/* stats[0..3] of instance inst after the last nsf_batch_step: pressure CG iterations, pressure
+   relative residual, residual replacements, status */
+int nsf_batch_stats(nsf_batch b, int inst, double *stats);
+/* kernel launches of one captured batch step (0 before the first graph step) */
+long long nsf_batch_kernels_per_step(nsf_batch b);
+void nsf_batch_destroy(nsf_batch b);
+
 /* ========================================================= force functional (drag/lift) == */
 
 typedef struct nsf_forces_s *nsf_forces;

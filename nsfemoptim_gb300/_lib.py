@@ -86,6 +86,14 @@ _SIGS = {
     "nsf_io_read_vec": (C.c_int, [C.c_char_p, f64p]),
     "nsf_io_write_vec": (C.c_int, [C.c_char_p, C.c_int, f64p, C.c_int]),
     "nsf_chorin_dump": (C.c_int, [vp, C.c_char_p, C.c_char_p, C.c_int, vp]),
+    "nsf_batch_create": (C.c_int, [vp, C.POINTER(ChorinConfig), C.c_int, f64p, f64p, C.POINTER(vp)]),
+    "nsf_batch_step": (C.c_int, [vp, C.c_int, vp]),
+    "nsf_batch_launch": (C.c_int, [vp, C.c_int, vp]),
+    "nsf_batch_get_state": (C.c_int, [vp, C.c_int, f64p, f64p, vp]),
+    "nsf_batch_set_state": (C.c_int, [vp, C.c_int, f64p, f64p, vp]),
+    "nsf_batch_stats": (C.c_int, [vp, C.c_int, f64p]),
+    "nsf_batch_kernels_per_step": (C.c_longlong, [vp]),
+    "nsf_batch_destroy": (None, [vp]),
     "nsf_neumann_create": (C.c_int, [C.c_int, i32p, i32p, f64p, C.c_int, C.c_int, C.c_int, C.c_double,
                                      C.POINTER(vp)]),
     "nsf_neumann_solve": (C.c_int, [vp, vp, vp, vp]),

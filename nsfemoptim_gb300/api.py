@@ -335,6 +335,62 @@ class AbstractSolver:
             self._h = None
 
 
+class Batch:
+    """Batched instances on one mesh (nsf_batch_*): instance q has viscosity nus[q] and Dirichlet x
+    values dir_vx[q] (context dirIds order; None: the context's inflow for all), every operation of
+    the time step one launch for all instances.  Mixed precision, Chebyshev mass solves, any pressure
+    guess (2: one projection basis per instance); each instance computes what a ChorinStepper with
+    the same options computes."""
+
+    def __init__(self, ctx: ChorinContext, nus, tau: float, dir_vx=None, vel_max_iters: int = 500,
+                 vel_tol: float = 1e-8, pres_max_iters: int = 5000, pres_tol: float = 1e-8, use_graph: bool = True,
+                 max_outer: int = 4, inner_tol: float = 1e-5, pressure_guess: int = 2, pressure_basis: int = 0):
+        self.ctx = ctx
+        nus = np.ascontiguousarray(nus, dtype=np.float64)
+        self.B = len(nus)
+        self.cfg = ChorinConfig(float(nus[0]), tau, NSF_PREC_MIXED, 3, vel_max_iters, vel_tol, pres_max_iters,
+                                pres_tol, 8, int(use_graph), max_outer, inner_tol, int(pressure_guess),
+                                int(pressure_basis))
+        dv = None
+        if dir_vx is not None:
+            dv = np.ascontiguousarray(dir_vx, dtype=np.float64).reshape(self.B, -1)
+        h = vp()
+        check(lib().nsf_batch_create(ctx._h, C.byref(self.cfg), self.B, _p(nus, C.c_double),
+                                     _p(dv, C.c_double) if dv is not None else None, C.byref(h)))
+        self._h = h
+        self.N, self.P = ctx.N, ctx.P
+
+    def step(self, n: int = 1, stream=None):
+        check(lib().nsf_batch_step(self._h, n, vp(stream)))
+
+    def launch(self, n: int = 1, stream=None):
+        check(lib().nsf_batch_launch(self._h, n, vp(stream)))
+
+    def state(self, q: int):
+        u = np.zeros(2 * self.N, np.float64)
+        p = np.zeros(self.P, np.float64)
+        check(lib().nsf_batch_get_state(self._h, q, _p(u, C.c_double), _p(p, C.c_double), None))
+        return u, p
+
+    def set_state(self, q: int, u, p):
+        u = np.ascontiguousarray(u, dtype=np.float64)
+        p = np.ascontiguousarray(p, dtype=np.float64)
+        check(lib().nsf_batch_set_state(self._h, q, _p(u, C.c_double), _p(p, C.c_double), None))
+
+    def stats(self, q: int):
+        s = (C.c_double * 4)()
+        check(lib().nsf_batch_stats(self._h, q, s))
+        return {"pres_iters": s[0], "pres_rel": s[1], "replacements": s[2], "status": s[3]}
+
+    def kernels_per_step(self) -> int:
+        return int(lib().nsf_batch_kernels_per_step(self._h))
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            lib().nsf_batch_destroy(self._h)
+            self._h = None
+
+
 class NeumannSolver:
     """Pure-Neumann Poisson solve made regular by one Dirichlet pin (nsf_neumann_*): on the device, the
     right-hand side is projected to zero mean, the system without row/column `pin` is solved with
@@ -561,7 +617,7 @@ class Adjoint:
 
 
 __all__ = ["Mesh", "load_gmsh", "ChorinContext", "build_chorin_context", "coloring", "CsrF", "Spmv", "Spmm",
-           "NeumannSolver",
+           "NeumannSolver", "Batch",
            "spmv", "spmm", "fastconv_apply", "fastconv_apply_df", "split_df", "AbstractSolver", "create_solver", "ChorinStepper", "kernel_launches",
            "Forces", "Adjoint", "Pack", "NSF_F32", "NSF_F64", "NSF_PREC_F64", "NSF_PREC_MIXED", "NSF_PREC_F64_MIXEDSOLVE",
            "NsfError"]

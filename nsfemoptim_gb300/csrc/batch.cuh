@@ -1,0 +1,516 @@
+// Batched instances: B flows on one mesh (each with its own viscosity, inflow values and state)
+// advanced together, every operation of the time step one launch for all instances.
+//
+// The operators (I, K, M, D, G, Kp_int and their SELL / double-float copies) are read by the
+// instances together: in the operator kernels consecutive blocks are the same rows of consecutive
+// instances (instance = blockIdx.x % B), so a block of the FastConvection matrix I -- the only
+// operator larger than L2 -- is fetched from HBM once and reused from L2 by the other instances'
+// blocks of that row range.  Instance vectors are contiguous per instance ([B][len]).  The pressure
+// solves are one launch of B thread-block clusters (kPcgClusterEis with instStride), cluster q
+// solving instance q.  Each instance runs exactly the kernels' arithmetic of a single stepper with
+// the same configuration (mixed precision, Chebyshev mass solves, any pressure guess), so its
+// fields equal that stepper's.
+//
+// No counterpart in the reference: its loop (chorinCuda.cu:236-376) advances one flow.
+#pragma once
+
+namespace nsf
+{
+    // ---- element-wise kernels: grid (blocks, B), blockIdx.y = instance
+    __global__ void __launch_bounds__(TPB) kBSplitDf(long long n, const double * __restrict__ x, float2 * __restrict__ y,
+                                                      long long stride)
+    {
+        const long long off = (long long)blockIdx.y * stride;
+        for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+            y[off + i] = dfFromDouble(x[off + i]);
+    }
+
+    __global__ void __launch_bounds__(TPB) kBDfToDouble(long long n, const float2 * __restrict__ x, double * __restrict__ y,
+                                                         long long stride)
+    {
+        const long long off = (long long)blockIdx.y * stride;
+        for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+            y[off + i] = dfToDouble(x[off + i]);
+    }
+
+    __global__ void __launch_bounds__(TPB) kBChebStartDf(int n, const double * __restrict__ b,
+                                                          const float2 * __restrict__ invD, float2 invTheta,
+                                                          float2 * __restrict__ r, float2 * __restrict__ d,
+                                                          float2 * __restrict__ x, long long stride)
+    {
+        const long long off = (long long)blockIdx.y * stride;
+        for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+            chebStartDfRow<2>(i, n, b + off, invD, invTheta, r + off, d + off, x + off);
+    }
+
+    // u <- Dirichlet value / u - tau acc (vectors stride 2n, Dirichlet values stride n)
+    __global__ void __launch_bounds__(TPB) kBUpdateVelocity(int n, double * __restrict__ u, const double * __restrict__ acc,
+                                                             double tau, const unsigned char * __restrict__ isDir,
+                                                             const double * __restrict__ dirVal)
+    {
+        const long long off = (long long)blockIdx.y * 2 * n;
+        const double * dv = dirVal + (long long)blockIdx.y * n;
+        for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+            updateVelocityRow<double>(i, n, u + off, acc + off, tau, isDir, dv);
+    }
+
+    // pressure guess 2 p(n-1) - p(n-2) per instance (kExtrapolate's rule), hist[instance]
+    __global__ void __launch_bounds__(TPB) kBExtrapolate(int n, double * __restrict__ p, double * __restrict__ prev,
+                                                          const int * __restrict__ hist)
+    {
+        const long long off = (long long)blockIdx.y * n;
+        const bool two = hist[blockIdx.y] >= 2;
+        for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        {
+            const double cur = p[off + i];
+            if (two)
+                p[off + i] = 2.0 * cur - prev[off + i];
+            prev[off + i] = cur;
+        }
+    }
+
+    __global__ void kBHistBump(int B, int * hist)
+    {
+        const int q = blockIdx.x * blockDim.x + threadIdx.x;
+        if (q < B && hist[q] < 2)
+            hist[q] += 1;
+    }
+
+    __global__ void kBSetConfig(int B, SolverState * st, int maxIters, int absMode, double tol2)
+    {
+        const int q = blockIdx.x * blockDim.x + threadIdx.x;
+        if (q < B)
+        {
+            st[q].maxIters = maxIters;
+            st[q].absMode = absMode;
+            st[q].tol2 = tol2;
+        }
+    }
+
+    // ---- operator kernels: 1-D grid of B x blocks, instance = blockIdx.x % B (instance fastest)
+    __global__ void __launch_bounds__(TPB) kBFastConvSellDf(int B, int rows, int nSlices, const int * __restrict__ ss,
+                                                             const int * __restrict__ perm, const int * __restrict__ ci,
+                                                             const float * __restrict__ iv, const float2 * __restrict__ u,
+                                                             long long su, const float2 * __restrict__ k,
+                                                             const float2 * __restrict__ nu, float2 * __restrict__ a,
+                                                             long long sa)
+    {
+        const int q = (int)(blockIdx.x % (unsigned)B), blk = (int)(blockIdx.x / (unsigned)B);
+        const int slice = (int)((blk * (unsigned)blockDim.x + threadIdx.x) >> 5);
+        fastConvSellDfSlice(slice, rows, nSlices, ss, perm, ci, iv, u + q * su, k, nu[q], a + q * sa);
+    }
+
+    template <int L>
+    __global__ void __launch_bounds__(TPB) kBSpmmDf(int B, int rows, const int * __restrict__ rs, const int * __restrict__ ci,
+                                                     const float2 * __restrict__ v, long long sv,
+                                                     const float2 * __restrict__ X, long long sx,
+                                                     double * __restrict__ Y, long long sy)
+    {
+        const int q = (int)(blockIdx.x % (unsigned)B), blk = (int)(blockIdx.x / (unsigned)B);
+        const Group<L> g(blk, (int)(gridDim.x / (unsigned)B));
+        spmmDfRows<L, 2>(g, rows, rs, ci, v + q * sv, X + q * sx, rows, Y + q * sy, rows);
+    }
+
+    __global__ void __launch_bounds__(TPB) kBChebStepDf(int B, int n, int nSlices, const int * __restrict__ ss,
+                                                         const int * __restrict__ perm, const int * __restrict__ ci,
+                                                         const float2 * __restrict__ v, const float2 * __restrict__ invD,
+                                                         const float2 * __restrict__ d, float2 * __restrict__ dn,
+                                                         float2 * __restrict__ x, float2 * __restrict__ r, long long stride,
+                                                         float2 c1, float2 c2)
+    {
+        const int q = (int)(blockIdx.x % (unsigned)B), blk = (int)(blockIdx.x / (unsigned)B);
+        const int slice = (int)((blk * (unsigned)blockDim.x + threadIdx.x) >> 5);
+        const long long off = q * stride;
+        chebStepDfSlice<2>(slice, n, nSlices, ss, perm, ci, v, invD, d + off, dn + off, x + off, r + off, c1, c2);
+    }
+
+    template <typename TM, typename TX, typename TY, typename TA>
+    __global__ void __launch_bounds__(TPB) kBSpmvSell(int B, int rows, int nSlices, const int * __restrict__ ss,
+                                                       const int * __restrict__ perm, const int * __restrict__ ci,
+                                                       const TM * __restrict__ v, const TX * __restrict__ x, long long sx,
+                                                       TY * __restrict__ y, long long sy, double alpha, double beta)
+    {
+        const int q = (int)(blockIdx.x % (unsigned)B), blk = (int)(blockIdx.x / (unsigned)B);
+        const int slice = (int)((blk * (unsigned)blockDim.x + threadIdx.x) >> 5);
+        spmvSellSlice<TM, TX, TY, TA>(slice, rows, nSlices, ss, perm, ci, v, x + q * sx, y + q * sy, alpha, beta);
+    }
+
+    inline dim3 batchGrid(long long threads, int B)
+    {
+        return dim3((unsigned)blocksFor(threads), (unsigned)B);
+    }
+} // namespace nsf
+
+struct nsf_batch_s
+{
+    nsf_chorin tpl = nullptr; // the shared operators, the solver set-up and the state maps
+    int B = 0, N = 0, P = 0, nIntP = 0, chebK = 0;
+    nsf_chorin_config cfg{};
+    DevBuf<float2> nuDf;
+    DevBuf<double> u, rhs, acc, rhsP, pInt, pPrev, dirVal, stage;
+    DevBuf<int> hist;
+    DevBuf<float2> uDf, ADf, xDf, rDf, d0, d1;
+    DevBuf<SolverState> pst;
+    PressureProjection proj; // pressureGuess 2: one basis per instance
+    // the batch's cluster set-up of the pressure solves (smaller clusters than a single solve uses,
+    // so that more instances' clusters are co-resident)
+    int pcs = 0, pvals = 0;
+    EisLayout play{};
+    DevBuf<int> pcmap, pps;
+
+    // Cluster size of the batched pressure solves: NSF_BATCH_CLUSTER if set, else the smallest of
+    // 4, 8, 16 CTAs whose per-CTA share stays within about 2,700 rows (one row per thread and
+    // colour at 4 colours, the size at which a single 16-CTA solve of the finest mesh runs) and fits
+    // in shared memory.
+    void setupPressureClusters()
+    {
+        const SweepSystem<float> & S = tpl->Kpi32;
+        const int want = std::atoi(envStr("NSF_BATCH_CLUSTER", "0").c_str());
+        std::vector<int> sizes = want > 0 ? std::vector<int>{want} : std::vector<int>{4, 8, 16};
+        for (int cs : sizes)
+        {
+            if (want <= 0 && cs < 16 && (S.n + cs - 1) / cs > 2700)
+                continue;
+            DsShares D = dsShares(S.ps, S.hostRsO, S.hostCiO, cs);
+            if (!dsEncodable(D, S.hostRsO))
+                continue;
+            for (int vals = 1; vals >= 0; vals--)
+            {
+                const EisLayout lay = eisLayout(D.rowsMax, D.nzMax, 1, (int)sizeof(float), vals != 0);
+                const bool fits = vals ? clusterFits(kPcgClusterEis<float, 1, true>, cs, lay.bytes)
+                                       : clusterFits(kPcgClusterEis<float, 1, false>, cs, lay.bytes);
+                if (fits)
+                {
+                    pcs = cs;
+                    pvals = vals;
+                    play = lay;
+                    pcmap.upload(D.cmap);
+                    pps.upload(S.ps);
+                    return;
+                }
+            }
+        }
+        throw Error(ST_NOTSUP, "no cluster size fits the batched pressure solves");
+    }
+    std::unique_ptr<PinnedBuf<SolverState>> stat;
+    cudaStream_t stream = nullptr;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    long long kernelsPerCapture = 0;
+    std::vector<SolverState> last;
+
+    ~nsf_batch_s()
+    {
+        if (exec)
+            cudaGraphExecDestroy(exec);
+        if (graph)
+            cudaGraphDestroy(graph);
+        if (stream)
+            cudaStreamDestroy(stream);
+        if (tpl)
+            nsf_chorin_destroy(tpl);
+    }
+
+    // M acc = b for every instance: double-float Chebyshev with the a priori count (the single
+    // stepper's velMethod 3 iterations, without its per-solve residual check)
+    void massSolve(cudaStream_t s, const double * b, double * x)
+    {
+        const ChebSolver & ch = tpl->chebT;
+        const DevSell<double> & sell = *ch.sell;
+        const long long stride = 2ll * N;
+        const double theta = 0.5 * (kMassSpecHi + kMassSpecLo), delta = 0.5 * (kMassSpecHi - kMassSpecLo);
+        const double sigma = theta / delta;
+        double rho = 1.0 / sigma;
+        NSF_LAUNCH(kBChebStartDf, batchGrid(N, B), s, N, b, (const float2 *)ch.invDDf.get(),
+                   ChebSolver::split(1.0 / theta), rDf.get(), d0.get(), xDf.get(), stride);
+        float2 * dc = d0.get();
+        float2 * dn = d1.get();
+        const int blocks = B * blocksFor((long long)sell.nSlices * SELL_C);
+        for (int it = 0; it < chebK; it++)
+        {
+            const double rhoN = 1.0 / (2.0 * sigma - rho);
+            NSF_LAUNCH(kBChebStepDf, blocks, s, B, N, sell.nSlices, sell.ss.get(), sell.perm.get(), sell.ci.get(),
+                       (const float2 *)ch.vDf.get(), (const float2 *)ch.invDDf.get(), (const float2 *)dc, dn, xDf.get(),
+                       rDf.get(), stride, ChebSolver::split(rhoN * rho), ChebSolver::split(2.0 * rhoN / delta));
+            rho = rhoN;
+            std::swap(dc, dn);
+        }
+        NSF_LAUNCH(kBDfToDouble, batchGrid(stride, B), s, stride, (const float2 *)xDf.get(), x, stride);
+    }
+
+    template <bool VALS>
+    void pressureSolve(cudaStream_t s)
+    {
+        const SweepSystem<float> & S = tpl->Kpi32;
+        const SweepSystem<double> & S64 = tpl->Kpi64;
+        const double delta = std::atof(envStr("NSF_RU_DELTA", "0.1").c_str());
+        NSF_LAUNCH(kBSetConfig, (B + 127) / 128, s, B, pst.get(),
+                   cfg.presMaxIters * (cfg.maxOuter > 0 ? cfg.maxOuter : 1), 0, cfg.presTol * cfg.presTol);
+        EisPcgArgs<float> A{S.n,          S.nColors,     1,              pps.get(),   S.rsO.get(),   S.ciO.get(),
+                            S.vO.get(),   pcmap.get(),   S.diag.get(),   S.invD.get(), nullptr,       nullptr,
+                            pst.get(),    nullptr,       play,           1,           delta * delta, rhsP.get(),
+                            S64.vO.get(), S64.diag.get(), pInt.get(),    (long long)nIntP};
+        launchClusters(kPcgClusterEis<float, 1, VALS>, pcs, B, DTPB, play.bytes, s, A);
+    }
+
+    void enqueueStep(cudaStream_t s)
+    {
+        nsf_chorin_s & T = *tpl;
+        const long long s2 = 2ll * N;
+        // 1. A = nu K + I u (double-float), rhs = A [u_x u_y]
+        NSF_LAUNCH(kBSplitDf, batchGrid(s2, B), s, s2, (const double *)u.get(), uDf.get(), s2);
+        const DevSell<float> & IS = T.I32.sell;
+        const long long nnzK = (long long)T.KDf.size();
+        NSF_LAUNCH(kBFastConvSellDf, B * blocksFor((long long)IS.nSlices * SELL_C), s, B, IS.rows, IS.nSlices,
+                   IS.ss.get(), IS.perm.get(), IS.ci.get(), IS.v.get(), (const float2 *)uDf.get(), s2,
+                   (const float2 *)T.KDf.get(), (const float2 *)nuDf.get(), ADf.get(), nnzK);
+        NSF_LANES(T.M32.L, NSF_LAUNCH((kBSpmmDf<LL>), B * blocksFor((long long)N * T.M32.L), s, B, N, T.M32.rsF.get(),
+                                      T.M32.ciF.get(), (const float2 *)ADf.get(), nnzK, (const float2 *)uDf.get(), s2,
+                                      rhs.get(), s2));
+        // 2. M acc = rhs ; u = u - tau acc ; Dirichlet
+        massSolve(s, rhs.get(), acc.get());
+        NSF_LAUNCH(kBUpdateVelocity, batchGrid(N, B), s, N, u.get(), (const double *)acc.get(), cfg.tau, T.isDir.get(),
+                   (const double *)dirVal.get());
+        // 3. rhsP = -(1/tau) D u ; Kpi pInt = rhsP
+        const DevSell<float> & DS = T.D32.sell;
+        NSF_LAUNCH((kBSpmvSell<float, double, double, double>), B * blocksFor((long long)DS.nSlices * SELL_C), s, B,
+                   DS.rows, DS.nSlices, DS.ss.get(), DS.perm.get(), DS.ci.get(), DS.v.get(), (const double *)u.get(), s2,
+                   rhsP.get(), (long long)nIntP, -1.0 / cfg.tau, 0.0);
+        if (cfg.pressureGuess == 1)
+        {
+            NSF_LAUNCH(kBExtrapolate, batchGrid(nIntP, B), s, nIntP, pInt.get(), pPrev.get(), (const int *)hist.get());
+            NSF_LAUNCH(kBHistBump, (B + 127) / 128, s, B, hist.get());
+        }
+        if (cfg.pressureGuess == 2)
+            proj.guess(s, rhsP.get(), pInt.get());
+        if (pvals)
+            pressureSolve<true>(s);
+        else
+            pressureSolve<false>(s);
+        if (cfg.pressureGuess == 2)
+            proj.update(s, pInt.get());
+        // 4. M acc = G p ; u = u - tau acc ; Dirichlet
+        const DevSell<float> & GS = T.G32.sell;
+        NSF_LAUNCH((kBSpmvSell<float, double, double, double>), B * blocksFor((long long)GS.nSlices * SELL_C), s, B,
+                   GS.rows, GS.nSlices, GS.ss.get(), GS.perm.get(), GS.ci.get(), GS.v.get(), (const double *)pInt.get(),
+                   (long long)nIntP, rhs.get(), s2, 1.0, 0.0);
+        massSolve(s, rhs.get(), acc.get());
+        NSF_LAUNCH(kBUpdateVelocity, batchGrid(N, B), s, N, u.get(), (const double *)acc.get(), cfg.tau, T.isDir.get(),
+                   (const double *)dirVal.get());
+    }
+
+    void enqueueSteps(int nSteps, cudaStream_t s)
+    {
+        if (!cfg.useGraph)
+        {
+            for (int i = 0; i < nSteps; i++)
+                enqueueStep(s);
+            return;
+        }
+        if (!exec)
+        {
+            const long long before = launchCounter().load();
+            NSF_CUDA(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
+            try
+            {
+                enqueueStep(stream);
+            }
+            catch (...)
+            {
+                cudaGraph_t g = nullptr;
+                cudaStreamEndCapture(stream, &g);
+                if (g)
+                    cudaGraphDestroy(g);
+                throw;
+            }
+            NSF_CUDA(cudaStreamEndCapture(stream, &graph));
+            NSF_CUDA(cudaGraphInstantiate(&exec, graph, 0));
+            kernelsPerCapture = launchCounter().load() - before;
+            launchCounter().fetch_sub(kernelsPerCapture);
+        }
+        for (int i = 0; i < nSteps; i++)
+        {
+            NSF_CUDA(cudaGraphLaunch(exec, s));
+            launchCounter().fetch_add(kernelsPerCapture, std::memory_order_relaxed);
+        }
+    }
+};
+
+extern "C" int nsf_batch_create(nsf_context ctx, const nsf_chorin_config * cfg, int nInst, const double * nu,
+                                const double * dirVx, nsf_batch * out)
+{
+    return guarded([&] {
+        require(ctx && cfg && out && nu, "null argument");
+        require(nInst >= 1 && nInst <= 65535, "nInst must be in 1..65535");
+        require(cfg->precision == NSF_PREC_MIXED, "batched instances run in NSF_PREC_MIXED");
+        require(cfg->velMethod == 3, "batched instances use velMethod 3 (Chebyshev mass solves)");
+        require(cfg->pressureGuess >= 0 && cfg->pressureGuess <= 2, "pressureGuess must be 0, 1 or 2");
+        require(cfg->pressureBasis == 0 || (cfg->pressureBasis >= 3 && cfg->pressureBasis <= PROJ_MAXL),
+                "pressureBasis must be 0 (250) or 3..256");
+        require(cfg->presTol >= 1e-11, "batched pressure solves need presTol >= 1e-11 (FP64 residual replacement)");
+        for (int q = 0; q < nInst; q++)
+            require(nu[q] >= 0 && std::isfinite(nu[q]), "viscosities must be finite and >= 0");
+        auto b = std::make_unique<nsf_batch_s>();
+        nsf_chorin_config c0 = *cfg;
+        c0.nu = nu[0];
+        const int st = nsf_chorin_create(ctx, &c0, &b->tpl);
+        if (st != NSF_OK)
+            throw Error(st, lastError);
+        nsf_chorin_s & T = *b->tpl;
+        b->cfg = T.cfg;
+        {
+            PcgSolver<float, 1> & in = T.mpres.inner;
+            require(in.path == PcgSolver<float, 1>::DSMEM && in.dsForm == 1 && in.canReplace(),
+                    "batched pressure solves need the cluster-resident Eisenstat path (NSF_PCG_PATH auto or dsmem)");
+        }
+        const int B = nInst, N = T.N;
+        b->B = B;
+        b->N = N;
+        b->P = T.P;
+        b->nIntP = T.nIntP;
+        b->chebK = std::min(b->cfg.velMaxIters, T.chebT.itersFor(b->cfg.velTol));
+        std::vector<float2> nd(B);
+        for (int q = 0; q < B; q++)
+            nd[q] = ChebSolver::split(nu[q]);
+        b->nuDf.upload(nd);
+        // per-instance Dirichlet values (rows of the colored numbering) and initial states
+        const std::vector<double> dv0 = T.dirVal.download();
+        const size_t nDir = T.dirRows.size();
+        std::vector<double> dv((size_t)B * N, 0.0), u0((size_t)B * 2 * N, 0.0);
+        for (int q = 0; q < B; q++)
+        {
+            double * d = dv.data() + (size_t)q * N;
+            if (dirVx)
+                for (size_t i = 0; i < nDir; i++)
+                    d[T.dirRows[i]] = dirVx[(size_t)q * nDir + i];
+            else
+                std::copy(dv0.begin(), dv0.end(), d);
+            for (size_t i = 0; i < nDir; i++)
+                u0[(size_t)q * 2 * N + T.dirRows[i]] = d[T.dirRows[i]];
+        }
+        b->dirVal.upload(dv);
+        b->u.upload(u0);
+        const size_t s2 = (size_t)B * 2 * N, sp = (size_t)B * T.nIntP;
+        b->rhs.alloc(s2);
+        b->acc.alloc(s2);
+        b->uDf.alloc(s2);
+        b->xDf.alloc(s2);
+        b->rDf.alloc(s2);
+        b->d0.alloc(s2);
+        b->d1.alloc(s2);
+        b->ADf.alloc((size_t)B * T.KDf.size());
+        b->rhsP.alloc(sp);
+        b->pInt.alloc(sp);
+        if (b->cfg.pressureGuess == 1)
+        {
+            b->pPrev.alloc(sp);
+            b->hist.alloc(B);
+        }
+        b->pst.alloc(B);
+        b->setupPressureClusters();
+        if (b->cfg.pressureGuess == 2)
+            b->proj.setup(&T.Kpi64, b->cfg.pressureBasis > 0 ? b->cfg.pressureBasis : 250, B);
+        b->stage.alloc(2 * (size_t)N + T.P);
+        b->stat = std::make_unique<PinnedBuf<SolverState>>(B);
+        b->last.resize(B);
+        NSF_CUDA(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking));
+        NSF_CUDA(cudaDeviceSynchronize());
+        *out = b.release();
+    });
+}
+
+extern "C" int nsf_batch_step(nsf_batch b, int nSteps, void * stream)
+{
+    return guarded([&] {
+        require(b && nSteps >= 0, "bad argument");
+        cudaStream_t s = stream ? asStream(stream) : b->stream;
+        b->enqueueSteps(nSteps, s);
+        if (nSteps == 0)
+            return;
+        NSF_CUDA(cudaMemcpyAsync(b->stat->get(), b->pst.get(), sizeof(SolverState) * b->B, cudaMemcpyDeviceToHost, s));
+        NSF_CUDA(cudaStreamSynchronize(s));
+        std::copy(b->stat->get(), b->stat->get() + b->B, b->last.begin());
+        for (int q = 0; q < b->B; q++)
+            if (b->last[q].status[0] == ST_NONFINITE)
+                throw Error(ST_NONFINITE, "non-finite pressure residual in instance " + std::to_string(q));
+    });
+}
+
+extern "C" int nsf_batch_launch(nsf_batch b, int nSteps, void * stream)
+{
+    return guarded([&] {
+        require(b && nSteps >= 0, "bad argument");
+        b->enqueueSteps(nSteps, stream ? asStream(stream) : b->stream);
+    });
+}
+
+extern "C" int nsf_batch_get_state(nsf_batch b, int inst, double * uOut, double * pOut, void * stream)
+{
+    return guarded([&] {
+        require(b && inst >= 0 && inst < b->B, "bad argument");
+        nsf_chorin S = b->tpl;
+        cudaStream_t s = stream ? asStream(stream) : b->stream;
+        stateMaps(S);
+        const int N = b->N;
+        double * su = b->stage.get(), * sp = su + 2 * (size_t)N;
+        if (uOut)
+        {
+            NSF_LAUNCH((kScatterPerm<double>), blocksFor(N), s, N, 2, S->permVDev.get(),
+                       (const double *)b->u.get() + (size_t)inst * 2 * N, su);
+            NSF_CUDA(cudaMemcpyAsync(uOut, su, sizeof(double) * 2 * N, cudaMemcpyDeviceToHost, s));
+        }
+        if (pOut)
+        {
+            NSF_CUDA(cudaMemsetAsync(sp, 0, sizeof(double) * b->P, s));
+            NSF_LAUNCH((kScatterPerm<double>), blocksFor(b->nIntP), s, b->nIntP, 1, S->pIdxDev.get(),
+                       (const double *)b->pInt.get() + (size_t)inst * b->nIntP, sp);
+            NSF_CUDA(cudaMemcpyAsync(pOut, sp, sizeof(double) * b->P, cudaMemcpyDeviceToHost, s));
+        }
+        NSF_CUDA(cudaStreamSynchronize(s));
+    });
+}
+
+extern "C" int nsf_batch_set_state(nsf_batch b, int inst, const double * uIn, const double * pIn, void * stream)
+{
+    return guarded([&] {
+        require(b && inst >= 0 && inst < b->B, "bad argument");
+        nsf_chorin S = b->tpl;
+        cudaStream_t s = stream ? asStream(stream) : b->stream;
+        stateMaps(S);
+        const int N = b->N;
+        double * su = b->stage.get(), * sp = su + 2 * (size_t)N;
+        if (uIn)
+        {
+            NSF_CUDA(cudaMemcpyAsync(su, uIn, sizeof(double) * 2 * N, cudaMemcpyHostToDevice, s));
+            NSF_LAUNCH((kGatherPerm<double>), blocksFor(N), s, N, 2, S->permVDev.get(), (const double *)su,
+                       b->u.get() + (size_t)inst * 2 * N);
+        }
+        if (pIn)
+        {
+            NSF_CUDA(cudaMemcpyAsync(sp, pIn, sizeof(double) * b->P, cudaMemcpyHostToDevice, s));
+            NSF_LAUNCH((kGatherPerm<double>), blocksFor(b->nIntP), s, b->nIntP, 1, S->pIdxDev.get(), (const double *)sp,
+                       b->pInt.get() + (size_t)inst * b->nIntP);
+        }
+        if (b->hist.get()) // a new pressure history for this instance
+            NSF_CUDA(cudaMemsetAsync(b->hist.get() + inst, 0, sizeof(int), s));
+        if (b->cfg.pressureGuess == 2)
+            b->proj.reset(s, inst);
+        NSF_CUDA(cudaStreamSynchronize(s));
+    });
+}
+
+extern "C" int nsf_batch_stats(nsf_batch b, int inst, double * stats)
+{
+    return guarded([&] {
+        require(b && stats && inst >= 0 && inst < b->B, "bad argument");
+        const SolverState & L = b->last[inst];
+        stats[0] = L.innerTotal[0];
+        stats[1] = L.bb[0] > 0 ? std::sqrt(std::max(0.0, L.lastRR[0]) / L.bb[0]) : 0.0;
+        stats[2] = L.iters[0];
+        stats[3] = L.status[0];
+    });
+}
+
+extern "C" long long nsf_batch_kernels_per_step(nsf_batch b) { return b ? b->kernelsPerCapture : 0; }
+
+extern "C" void nsf_batch_destroy(nsf_batch b) { delete b; }

@@ -2250,3 +2250,6 @@ extern "C" int nsf_residual_noalloc(nsf_csr a, int nrhs, const double * x, const
 
 // ============================================================ packs of steppers (one graph)
 #include "pack.cuh"
+
+// ============================================================ batched instances (one launch per operation)
+#include "batch.cuh"

@@ -92,6 +92,9 @@ namespace nsf
         const double * vO64;
         const double * diag64;
         double * x64;
+        // several clusters in one launch (batched instances of one system): cluster q solves the
+        // system of instance q, its vectors (b, x, b64, x64) at q * instStride and its state at st + q
+        long long instStride;
     };
 
     // The s and r~ updates of one CG step.  The owner of a row and its neighbours (which evaluate the
@@ -240,11 +243,20 @@ namespace nsf
     };
 
     template <typename T, int NCH, bool VALS>
-    __global__ void __launch_bounds__(DTPB, 1) kPcgClusterEis(EisPcgArgs<T> A)
+    __global__ void __launch_bounds__(DTPB, 1) kPcgClusterEis(EisPcgArgs<T> Ain)
     {
         extern __shared__ __align__(16) unsigned char dsm[];
         cg::cluster_group cl = cg::this_cluster();
         const int rank = (int)cl.block_rank(), cs = (int)cl.num_blocks();
+        EisPcgArgs<T> A = Ain;
+        {
+            const long long inst = (long long)(blockIdx.x / (unsigned)cs), off = inst * A.instStride;
+            A.b = A.b ? A.b + off : nullptr;
+            A.x = A.x ? A.x + off : nullptr;
+            A.b64 = A.b64 ? A.b64 + off : nullptr;
+            A.x64 = A.x64 ? A.x64 + off : nullptr;
+            A.st += inst;
+        }
         __shared__ T slot[2][8];
         __shared__ double dslot[2][8];
         __shared__ int chunkA[MAXCOLORS], chunkL[MAXCOLORS + 1], chunkG[MAXCOLORS], nzBase[MAXCOLORS + 1];

@@ -196,6 +196,27 @@ namespace nsf
 
 #define NSF_LAUNCH(kernel, grid, stream, ...) ::nsf::launchKernel(#kernel, kernel, (grid), (stream), __VA_ARGS__)
 
+    // launch `clusters` thread-block clusters of cs CTAs of `threads` threads each
+    template <typename... KArgs, typename... Args>
+    inline void launchClusters(void (*k)(KArgs...), int cs, int clusters, int threads, size_t smem, cudaStream_t s,
+                               const Args &... a)
+    {
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3(cs * clusters);
+        cfg.blockDim = dim3(threads);
+        cfg.dynamicSmemBytes = smem;
+        cfg.stream = s;
+        cudaLaunchAttribute at[1];
+        at[0].id = cudaLaunchAttributeClusterDimension;
+        at[0].val.clusterDim.x = cs;
+        at[0].val.clusterDim.y = 1;
+        at[0].val.clusterDim.z = 1;
+        cfg.attrs = at;
+        cfg.numAttrs = 1;
+        cudaCheck(cudaLaunchKernelEx(&cfg, k, a...), "cluster launch");
+        launchCounter().fetch_add(1, std::memory_order_relaxed);
+    }
+
     // launch a one-cluster kernel: cs CTAs of `threads` threads forming one thread-block cluster
     template <typename... KArgs, typename... Args>
     inline void launchCluster(void (*k)(KArgs...), int cs, int threads, size_t smem, cudaStream_t s,

@@ -32,12 +32,15 @@ namespace nsf
         int lane, gid, ngroups;
         unsigned mask;
 
-        __device__ __forceinline__ Group()
+        __device__ __forceinline__ Group() : Group((int)blockIdx.x, (int)gridDim.x) {}
+
+        // block `blk` of `nblk` (batched launches decode their own block index)
+        __device__ __forceinline__ Group(int blk, int nblk)
         {
-            const int t = blockIdx.x * blockDim.x + threadIdx.x;
+            const int t = blk * blockDim.x + threadIdx.x;
             lane = threadIdx.x & (L - 1);
             gid = t / L;
-            ngroups = (gridDim.x * blockDim.x) / L;
+            ngroups = (nblk * blockDim.x) / L;
             const int w = (threadIdx.x & 31) / L;
             mask = (L == 32) ? FULL : (((1u << L) - 1u) << (w * L));
         }
@@ -355,12 +358,11 @@ namespace nsf
 
     // y[perm[row]] = alpha * (A x)[row] + beta * y[perm[row]]   (beta == 0: y is not read)
     template <typename TM, typename TX, typename TY, typename TA>
-    __global__ void __launch_bounds__(TPB) kSpmvSell(int rows, int nSlices, const int * __restrict__ ss,
-                                                      const int * __restrict__ perm, const int * __restrict__ ci,
-                                                      const TM * __restrict__ v, const TX * __restrict__ x,
-                                                      TY * __restrict__ y, double alpha, double beta)
+    __device__ __forceinline__ void spmvSellSlice(int slice, int rows, int nSlices, const int * __restrict__ ss,
+                                                  const int * __restrict__ perm, const int * __restrict__ ci,
+                                                  const TM * __restrict__ v, const TX * __restrict__ x,
+                                                  TY * __restrict__ y, double alpha, double beta)
     {
-        const int slice = (int)((blockIdx.x * (unsigned)blockDim.x + threadIdx.x) >> 5);
         if (slice >= nSlices)
             return; // whole warps
         const int lane = threadIdx.x & 31;
@@ -374,6 +376,16 @@ namespace nsf
                 out += beta * (double)y[r];
             y[r] = (TY)out;
         }
+    }
+
+    template <typename TM, typename TX, typename TY, typename TA>
+    __global__ void __launch_bounds__(TPB) kSpmvSell(int rows, int nSlices, const int * __restrict__ ss,
+                                                      const int * __restrict__ perm, const int * __restrict__ ci,
+                                                      const TM * __restrict__ v, const TX * __restrict__ x,
+                                                      TY * __restrict__ y, double alpha, double beta)
+    {
+        const int slice = (int)((blockIdx.x * (unsigned)blockDim.x + threadIdx.x) >> 5);
+        spmvSellSlice<TM, TX, TY, TA>(slice, rows, nSlices, ss, perm, ci, v, x, y, alpha, beta);
     }
 
     // A[perm[row]] = nu K[perm[row]] + (I u)[row]   (FastConvection with the nu K add fused)
@@ -410,23 +422,29 @@ namespace nsf
 
     // u <- Dirichlet value on boundary rows, u - tau * acc elsewhere (2 planar channels)
     template <typename TA>
+    __device__ __forceinline__ void updateVelocityRow(int i, int n, double * __restrict__ u, const TA * __restrict__ acc,
+                                                      double tau, const unsigned char * __restrict__ isDir,
+                                                      const double * __restrict__ dirVal)
+    {
+        if (isDir[i])
+        {
+            u[i] = dirVal[i];
+            u[i + n] = 0.0;
+        }
+        else
+        {
+            u[i] -= tau * (double)acc[i];
+            u[i + n] -= tau * (double)acc[i + n];
+        }
+    }
+
+    template <typename TA>
     __global__ void __launch_bounds__(TPB) kUpdateVelocity(int n, double * __restrict__ u, const TA * __restrict__ acc,
                                                             double tau, const unsigned char * __restrict__ isDir,
                                                             const double * __restrict__ dirVal)
     {
         for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
-        {
-            if (isDir[i])
-            {
-                u[i] = dirVal[i];
-                u[i + n] = 0.0;
-            }
-            else
-            {
-                u[i] -= tau * (double)acc[i];
-                u[i + n] -= tau * (double)acc[i + n];
-            }
-        }
+            updateVelocityRow<TA>(i, n, u, acc, tau, isDir, dirVal);
     }
 
     // ------------------------------------------------------------------ Chebyshev (mass matrix)
@@ -557,37 +575,43 @@ namespace nsf
 
     // the double-float Chebyshev start: r = b, d = D^-1 b / theta, x = 0 (b and D^-1 from FP64)
     template <int NCH>
+    __device__ __forceinline__ void chebStartDfRow(int i, int n, const double * __restrict__ b,
+                                                   const float2 * __restrict__ invD, float2 invTheta,
+                                                   float2 * __restrict__ r, float2 * __restrict__ d,
+                                                   float2 * __restrict__ x)
+    {
+        const float2 id = invD[i];
+#pragma unroll
+        for (int c = 0; c < NCH; c++)
+        {
+            const size_t o = (size_t)c * n + i;
+            const float2 bi = dfFromDouble(b[o]);
+            r[o] = bi;
+            d[o] = dfMul(dfMul(bi, id), invTheta);
+            x[o] = make_float2(0.f, 0.f);
+        }
+    }
+
+    template <int NCH>
     __global__ void __launch_bounds__(TPB) kChebStartDf(int n, const double * __restrict__ b,
                                                          const float2 * __restrict__ invD, float2 invTheta,
                                                          float2 * __restrict__ r, float2 * __restrict__ d,
                                                          float2 * __restrict__ x)
     {
         for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
-        {
-            const float2 id = invD[i];
-#pragma unroll
-            for (int c = 0; c < NCH; c++)
-            {
-                const size_t o = (size_t)c * n + i;
-                const float2 bi = dfFromDouble(b[o]);
-                r[o] = bi;
-                d[o] = dfMul(dfMul(bi, id), invTheta);
-                x[o] = make_float2(0.f, 0.f);
-            }
-        }
+            chebStartDfRow<NCH>(i, n, b, invD, invTheta, r, d, x);
     }
 
     // kChebStep in double-float arithmetic: q = A d; x += d; r -= q; d' = c1 d + c2 D^-1 r
     template <int NCH>
-    __global__ void __launch_bounds__(TPB) kChebStepDf(int n, int nSlices, const int * __restrict__ ss,
-                                                        const int * __restrict__ perm, const int * __restrict__ ci,
-                                                        const float2 * __restrict__ v, const float2 * __restrict__ invD,
-                                                        const float2 * __restrict__ d, float2 * __restrict__ dn,
-                                                        float2 * __restrict__ x, float2 * __restrict__ r, float2 c1,
-                                                        float2 c2, const int * kdev, int it)
+    __device__ __forceinline__ void chebStepDfSlice(int slice, int n, int nSlices, const int * __restrict__ ss,
+                                                    const int * __restrict__ perm, const int * __restrict__ ci,
+                                                    const float2 * __restrict__ v, const float2 * __restrict__ invD,
+                                                    const float2 * __restrict__ d, float2 * __restrict__ dn,
+                                                    float2 * __restrict__ x, float2 * __restrict__ r, float2 c1,
+                                                    float2 c2)
     {
-        const int slice = (int)((blockIdx.x * (unsigned)blockDim.x + threadIdx.x) >> 5);
-        if (slice >= nSlices || (kdev && it >= *kdev))
+        if (slice >= nSlices)
             return;
         const int lane = threadIdx.x & 31;
         const int row = slice * SELL_C + lane;
@@ -638,6 +662,20 @@ namespace nsf
         }
     }
 
+    template <int NCH>
+    __global__ void __launch_bounds__(TPB) kChebStepDf(int n, int nSlices, const int * __restrict__ ss,
+                                                        const int * __restrict__ perm, const int * __restrict__ ci,
+                                                        const float2 * __restrict__ v, const float2 * __restrict__ invD,
+                                                        const float2 * __restrict__ d, float2 * __restrict__ dn,
+                                                        float2 * __restrict__ x, float2 * __restrict__ r, float2 c1,
+                                                        float2 c2, const int * kdev, int it)
+    {
+        const int slice = (int)((blockIdx.x * (unsigned)blockDim.x + threadIdx.x) >> 5);
+        if (kdev && it >= *kdev)
+            return;
+        chebStepDfSlice<NCH>(slice, n, nSlices, ss, perm, ci, v, invD, d, dn, x, r, c1, c2);
+    }
+
     // y = (hi, lo) split of an FP64 vector
     __global__ void __launch_bounds__(TPB) kSplitDf(long long n, const double * __restrict__ x, float2 * __restrict__ y)
     {
@@ -649,13 +687,12 @@ namespace nsf
     // product I_kj u_j of a float and a double-float is formed exactly up to the last bits), u, K, A
     // and the sums as double-floats.  Same SELL layout and predicated 8-wide load groups as
     // kFastConvSell.
-    __global__ void __launch_bounds__(TPB) kFastConvSellDf(int rows, int nSlices, const int * __restrict__ ss,
-                                                            const int * __restrict__ perm, const int * __restrict__ ci,
-                                                            const float * __restrict__ iv, const float2 * __restrict__ u,
-                                                            const float2 * __restrict__ k, float2 nu,
-                                                            float2 * __restrict__ a)
+    __device__ __forceinline__ void fastConvSellDfSlice(int slice, int rows, int nSlices, const int * __restrict__ ss,
+                                                        const int * __restrict__ perm, const int * __restrict__ ci,
+                                                        const float * __restrict__ iv, const float2 * __restrict__ u,
+                                                        const float2 * __restrict__ k, float2 nu,
+                                                        float2 * __restrict__ a)
     {
-        const int slice = (int)((blockIdx.x * (unsigned)blockDim.x + threadIdx.x) >> 5);
         if (slice >= nSlices)
             return;
         const int lane = threadIdx.x & 31;
@@ -694,13 +731,22 @@ namespace nsf
         a[r] = dfAdd(dfMul(nu, ldg(k + r)), acc);
     }
 
+    __global__ void __launch_bounds__(TPB) kFastConvSellDf(int rows, int nSlices, const int * __restrict__ ss,
+                                                            const int * __restrict__ perm, const int * __restrict__ ci,
+                                                            const float * __restrict__ iv, const float2 * __restrict__ u,
+                                                            const float2 * __restrict__ k, float2 nu,
+                                                            float2 * __restrict__ a)
+    {
+        const int slice = (int)((blockIdx.x * (unsigned)blockDim.x + threadIdx.x) >> 5);
+        fastConvSellDfSlice(slice, rows, nSlices, ss, perm, ci, iv, u, k, nu, a);
+    }
+
     // planar multi-RHS in double-float, FP64 result: Y[c ldy + r] = sum_j A[r, j] X[c ldx + j]
     template <int L, int NCH>
-    __global__ void __launch_bounds__(TPB) kSpmmDf(int rows, const int * __restrict__ rs, const int * __restrict__ ci,
-                                                    const float2 * __restrict__ v, const float2 * __restrict__ X, int ldx,
-                                                    double * __restrict__ Y, int ldy)
+    __device__ __forceinline__ void spmmDfRows(const Group<L> & g, int rows, const int * __restrict__ rs,
+                                               const int * __restrict__ ci, const float2 * __restrict__ v,
+                                               const float2 * __restrict__ X, int ldx, double * __restrict__ Y, int ldy)
     {
-        Group<L> g;
         for (int r = g.gid; r < rows; r += g.ngroups)
         {
             const int b = ldg(rs + r), e = ldg(rs + r + 1);
@@ -731,6 +777,15 @@ namespace nsf
                     Y[(size_t)c * ldy + r] = dfToDouble(t);
             }
         }
+    }
+
+    template <int L, int NCH>
+    __global__ void __launch_bounds__(TPB) kSpmmDf(int rows, const int * __restrict__ rs, const int * __restrict__ ci,
+                                                    const float2 * __restrict__ v, const float2 * __restrict__ X, int ldx,
+                                                    double * __restrict__ Y, int ldy)
+    {
+        const Group<L> g;
+        spmmDfRows<L, NCH>(g, rows, rs, ci, v, X, ldx, Y, ldy);
     }
 
     // x64 = hi + lo of the double-float result

@@ -49,6 +49,14 @@ namespace nsf
     __global__ void __launch_bounds__(TPB) kProjDots(int n, const double * __restrict__ X, const double * __restrict__ v,
                                                       ProjState * st, double * partial, double * coef, int which)
     {
+        {
+            const long long q = blockIdx.z; // instance of a batched projection (grid z)
+            X += q * gridDim.y * (long long)n;
+            v += q * n;
+            st += q;
+            partial += q * PROJ_MAXL * PROJ_CHUNKS;
+            coef += q * PROJ_MAXL;
+        }
         if (which >= 0 && !st->active[which])
             return;
         const int k = blockIdx.y;
@@ -89,10 +97,18 @@ namespace nsf
     }
 
     // p = sum_k coef[k] X_k over the basis (p unchanged while it is empty); x0 = p
-    __global__ void __launch_bounds__(TPB) kProjGuess(int n, const double * __restrict__ X, const double * coef,
+    __global__ void __launch_bounds__(TPB) kProjGuess(int n, int L, const double * __restrict__ X, const double * coef,
                                                        const ProjState * st, double * __restrict__ p,
                                                        double * __restrict__ x0)
     {
+        {
+            const long long q = blockIdx.y; // instance (grid y)
+            X += q * L * (long long)n;
+            coef += q * PROJ_MAXL;
+            st += q;
+            p += q * n;
+            x0 += q * n;
+        }
         __shared__ double c[PROJ_MAXL];
         const int m = st->m;
         for (int k = threadIdx.x; k < m; k += TPB)
@@ -113,10 +129,12 @@ namespace nsf
     }
 
     // the adds of this update: an empty or full basis restarts (then the differences join too)
-    __global__ void kProjDecide(ProjState * st, int L)
+    __global__ void kProjDecide(ProjState * st, int L, int B)
     {
-        if (blockIdx.x != 0 || threadIdx.x != 0)
+        const int q = blockIdx.x * blockDim.x + threadIdx.x; // one thread per instance
+        if (q >= B)
             return;
+        st += q;
         const int restart = st->m == 0 || st->m >= L;
         if (restart)
             st->m = 0;
@@ -132,6 +150,15 @@ namespace nsf
                                                       const double * __restrict__ x0, const double * __restrict__ prev1,
                                                       const double * __restrict__ prev2, double * __restrict__ w)
     {
+        {
+            const long long q = blockIdx.y; // instance (grid y)
+            st += q;
+            x += q * n;
+            x0 += q * n;
+            prev1 += q * n;
+            prev2 += q * n;
+            w += q * n;
+        }
         if (!st->active[which])
             return;
         const bool restart = st->restart != 0;
@@ -177,11 +204,19 @@ namespace nsf
     // q = A src and src . q (row groups of L lanes over the CSR); stage 0: src = w, stages 1 and 2:
     // src = the slot being filled.  Skipped unless add `which` is active.
     template <int L>
-    __global__ void __launch_bounds__(TPB) kProjSpmvDot(int n, const int * __restrict__ rs, const int * __restrict__ ci,
-                                                         const double * __restrict__ v, ProjState * st, int which,
-                                                         int stage, const double * w, const double * X,
-                                                         double * __restrict__ q, double * scratch)
+    __global__ void __launch_bounds__(TPB) kProjSpmvDot(int n, int basis, const int * __restrict__ rs,
+                                                         const int * __restrict__ ci, const double * __restrict__ v,
+                                                         ProjState * st, int which, int stage, const double * w,
+                                                         const double * X, double * __restrict__ q, double * scratch)
     {
+        {
+            const long long b = blockIdx.y; // instance (grid y); its blocks reduce among themselves
+            st += b;
+            w += b * n;
+            X += b * basis * (long long)n;
+            q += b * n;
+            scratch += b * gridDim.x;
+        }
         if (!st->active[which])
             return;
         const double * src = stage == 0 ? w : X + (size_t)st->slot * n;
@@ -203,9 +238,17 @@ namespace nsf
     }
 
     // X[slot] = w - sum_k beta_k X_k over the basis (w == nullptr: in place, X[slot] -= ...)
-    __global__ void __launch_bounds__(TPB) kProjOrth(int n, double * X, const double * beta, const ProjState * st,
+    __global__ void __launch_bounds__(TPB) kProjOrth(int n, int L, double * X, const double * beta, const ProjState * st,
                                                       int which, const double * w)
     {
+        {
+            const long long q = blockIdx.y; // instance (grid y)
+            X += q * L * (long long)n;
+            beta += q * PROJ_MAXL;
+            st += q;
+            if (w)
+                w += q * n;
+        }
         if (!st->active[which])
             return;
         __shared__ double c[PROJ_MAXL];
@@ -225,8 +268,13 @@ namespace nsf
     }
 
     // normalise the vector that the add accepted
-    __global__ void __launch_bounds__(TPB) kProjScale(int n, double * X, const ProjState * st, int which)
+    __global__ void __launch_bounds__(TPB) kProjScale(int n, int L, double * X, const ProjState * st, int which)
     {
+        {
+            const long long q = blockIdx.y; // instance (grid y)
+            X += q * L * (long long)n;
+            st += q;
+        }
         if (!st->active[which] || st->newSlot < 0)
             return;
         const double s = st->scale;
@@ -239,6 +287,13 @@ namespace nsf
     __global__ void __launch_bounds__(TPB) kProjShift(int n, ProjState * st, const double * __restrict__ x,
                                                        double * __restrict__ prev1, double * __restrict__ prev2)
     {
+        {
+            const long long q = blockIdx.y; // instance (grid y)
+            st += q;
+            x += q * n;
+            prev1 += q * n;
+            prev2 += q * n;
+        }
         for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
         {
             prev2[i] = prev1[i];
@@ -248,40 +303,51 @@ namespace nsf
             st->hist += 1;
     }
 
+    // B instances of the same system (batched steppers): every array holds B instance blocks
+    // ([B][L][n] basis, [B][n] vectors, B states), each kernel one launch for all instances (the
+    // instance in grid y, or z for the dot products whose grid y is the basis vector).
     struct PressureProjection
     {
-        int n = 0, L = 60;
+        int n = 0, L = 60, B = 1;
         const SweepSystem<double> * A = nullptr;
         DevBuf<double> X, x0, w, q, prev1, prev2, coef, partial, scratch;
         DevBuf<ProjState> st;
 
-        void setup(const SweepSystem<double> * a, int basis)
+        void setup(const SweepSystem<double> * a, int basis, int instances = 1)
         {
             A = a;
             n = a->n;
             L = basis;
-            X.alloc((size_t)L * n);
-            x0.alloc(n);
-            w.alloc(n);
-            q.alloc(n);
-            prev1.alloc(n);
-            prev2.alloc(n);
-            coef.alloc(PROJ_MAXL);
-            partial.alloc((size_t)PROJ_MAXL * PROJ_CHUNKS);
-            scratch.alloc((size_t)cappedBlocks(1ll << 40));
-            st.alloc(1);
-            NSF_CUDA(cudaMemset(st.get(), 0, sizeof(ProjState)));
+            B = instances;
+            const size_t nb = (size_t)n * B;
+            X.alloc((size_t)L * nb);
+            x0.alloc(nb);
+            w.alloc(nb);
+            q.alloc(nb);
+            prev1.alloc(nb);
+            prev2.alloc(nb);
+            coef.alloc((size_t)PROJ_MAXL * B);
+            partial.alloc((size_t)PROJ_MAXL * PROJ_CHUNKS * B);
+            scratch.alloc((size_t)cappedBlocks(1ll << 40) * B);
+            st.alloc(B);
+            NSF_CUDA(cudaMemset(st.get(), 0, sizeof(ProjState) * B));
         }
 
         // a new history (set_state): the basis and the solution history start empty
-        void reset(cudaStream_t s) { NSF_CUDA(cudaMemsetAsync(st.get(), 0, sizeof(ProjState), s)); }
+        void reset(cudaStream_t s, int inst = -1)
+        {
+            if (inst < 0)
+                NSF_CUDA(cudaMemsetAsync(st.get(), 0, sizeof(ProjState) * B, s));
+            else
+                NSF_CUDA(cudaMemsetAsync(st.get() + inst, 0, sizeof(ProjState), s));
+        }
 
         // p <- the projection of the solution of A p = b onto the basis (p kept while it is empty)
         void guess(cudaStream_t s, const double * b, double * p)
         {
-            NSF_LAUNCH(kProjDots, dim3(PROJ_CHUNKS, L), s, n, (const double *)X.get(), b, st.get(), partial.get(),
+            NSF_LAUNCH(kProjDots, dim3(PROJ_CHUNKS, L, B), s, n, (const double *)X.get(), b, st.get(), partial.get(),
                        coef.get(), -1);
-            NSF_LAUNCH(kProjGuess, blocksFor(n), s, n, (const double *)X.get(), (const double *)coef.get(),
+            NSF_LAUNCH(kProjGuess, dim3(blocksFor(n), B), s, n, L, (const double *)X.get(), (const double *)coef.get(),
                        (const ProjState *)st.get(), p, x0.get());
         }
 
@@ -289,30 +355,30 @@ namespace nsf
         void update(cudaStream_t s, const double * p)
         {
             const SweepSystem<double> & S = *A;
-            NSF_LAUNCH(kProjDecide, 1, s, st.get(), L);
+            const dim3 grid(blocksFor(n), B);
+            NSF_LAUNCH(kProjDecide, (B + 127) / 128, s, st.get(), L, B);
             for (int which = 0; which < 3; which++)
             {
-                NSF_LAUNCH(kProjPrep, blocksFor(n), s, n, which, (const ProjState *)st.get(), p,
-                           (const double *)x0.get(), (const double *)prev1.get(), (const double *)prev2.get(),
-                           w.get());
+                NSF_LAUNCH(kProjPrep, grid, s, n, which, (const ProjState *)st.get(), p, (const double *)x0.get(),
+                           (const double *)prev1.get(), (const double *)prev2.get(), w.get());
                 // products of w, of the orthogonalised vector (re-orthogonalisation), of the result
                 for (int stage : {0, 2, 1})
                 {
-                    NSF_LANES(S.L, NSF_LAUNCH((kProjSpmvDot<LL>), S.fullBlocks(), s, n, S.rsF.get(), S.ciF.get(),
-                                              S.vF.get(), st.get(), which, stage, (const double *)w.get(),
+                    NSF_LANES(S.L, NSF_LAUNCH((kProjSpmvDot<LL>), dim3(S.fullBlocks(), B), s, n, L, S.rsF.get(),
+                                              S.ciF.get(), S.vF.get(), st.get(), which, stage, (const double *)w.get(),
                                               (const double *)X.get(), q.get(), scratch.get()));
                     if (stage != 1)
                     {
-                        NSF_LAUNCH(kProjDots, dim3(PROJ_CHUNKS, L), s, n, (const double *)X.get(),
+                        NSF_LAUNCH(kProjDots, dim3(PROJ_CHUNKS, L, B), s, n, (const double *)X.get(),
                                    (const double *)q.get(), st.get(), partial.get(), coef.get(), which);
-                        NSF_LAUNCH(kProjOrth, blocksFor(n), s, n, X.get(), (const double *)coef.get(),
+                        NSF_LAUNCH(kProjOrth, grid, s, n, L, X.get(), (const double *)coef.get(),
                                    (const ProjState *)st.get(), which,
                                    stage == 0 ? (const double *)w.get() : (const double *)nullptr);
                     }
                 }
-                NSF_LAUNCH(kProjScale, blocksFor(n), s, n, X.get(), (const ProjState *)st.get(), which);
+                NSF_LAUNCH(kProjScale, grid, s, n, L, X.get(), (const ProjState *)st.get(), which);
             }
-            NSF_LAUNCH(kProjShift, blocksFor(n), s, n, st.get(), p, prev1.get(), prev2.get());
+            NSF_LAUNCH(kProjShift, grid, s, n, st.get(), p, prev1.get(), prev2.get());
         }
 
         int basisKernelsPerStep() const { return 2 + 1 + 3 * 9 + 1; }

@@ -1,0 +1,91 @@
+"""Batched instances (nsf_batch_*) against separate steppers, through the C ABI.
+
+Three instances on the committed h = 0.025 channel mesh with their own viscosities (1e-3, 2e-3,
+5e-4) and inflow values (the context's scaled by 1.0, 0.7, 1.3), tau = 1e-3, mixed precision,
+Chebyshev mass solves to 1e-10, pressure to 1e-10, pressure guess 0, 1 and 2 (a 4-vector projection
+basis, so 5 steps pass through a restart): after 5 steps every
+instance's state equals, bit for bit, the state of a ChorinStepper with the same options (the batched
+kernels run the single stepper's arithmetic, instance by instance).  set_state / state round trip
+and the per-instance statistics are checked too.
+"""
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+NUS = [1e-3, 2e-3, 5e-4]
+SCALES = [1.0, 0.7, 1.3]
+
+
+@pytest.fixture(scope="module")
+def torch_cuda():
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    return torch
+
+
+@pytest.fixture(scope="module")
+def ctx(torch_cuda, channel_coarse):
+    import nsfemoptim_gb300 as G
+    return G, G.build_chorin_context(G.load_gmsh(channel_coarse), 1.2)
+
+
+@pytest.mark.parametrize("guess", [0, 1, 2])
+def test_batch_equals_separate_steppers(ctx, guess, monkeypatch):
+    G, c = ctx
+    monkeypatch.setenv("NSF_BATCH_CLUSTER", "16")  # the cluster size of a single solve: the same reduction order
+    dir_vx = np.stack([c.dir_vx * s for s in SCALES])
+    b = G.Batch(c, NUS, 1e-3, dir_vx=dir_vx, vel_tol=1e-10, pres_tol=1e-10, pressure_guess=guess, pressure_basis=4)
+    b.step(5)
+    assert b.kernels_per_step() > 0
+    for q, (nu, sc) in enumerate(zip(NUS, SCALES)):
+        st = G.ChorinStepper(c, nu, 1e-3, precision=G.NSF_PREC_MIXED, vel_method=3, vel_max_iters=500, vel_tol=1e-10,
+                             pres_max_iters=5000, pres_tol=1e-10, use_graph=True, max_outer=4, inner_tol=1e-5,
+                             pressure_guess=guess, pressure_basis=4)
+        st.set_dirichlet(dir_vx[q])
+        st.step(5)
+        u, p = st.state()
+        ub, pb = b.state(q)
+        assert np.array_equal(u, ub) and np.array_equal(p, pb), (q, np.abs(u - ub).max(), np.abs(p - pb).max())
+        s = b.stats(q)
+        assert s["status"] == 0 and s["pres_rel"] <= 1e-10
+        assert s["pres_iters"] == st.stats()["pres_iters"]
+
+
+def test_batch_state_roundtrip(ctx):
+    G, c = ctx
+    b = G.Batch(c, NUS, 1e-3, vel_tol=1e-10, pres_tol=1e-10)
+    rng = np.random.default_rng(3)
+    u = rng.standard_normal(2 * c.N)
+    p = np.zeros(c.P)
+    p[c.int_p] = rng.standard_normal(len(c.int_p))
+    b.set_state(1, u, p)
+    u2, p2 = b.state(1)
+    assert np.array_equal(u, u2) and np.array_equal(p, p2)
+    with pytest.raises(G.NsfError):
+        b.state(3)
+
+
+def test_batch_small_clusters_follow_steppers(ctx):
+    """With the batch's own cluster size (smaller clusters, so that more instances' pressure solves
+    run at once) only the summation order of the pressure CG's dot products changes: the states
+    follow the separate steppers to the solver tolerance: 10x the measured relative differences
+    (u 2.6e-12, p 2.1e-9 with pressure solves to 1e-10)."""
+    G, c = ctx
+    dir_vx = np.stack([c.dir_vx * s for s in SCALES])
+    b = G.Batch(c, NUS, 1e-3, dir_vx=dir_vx, vel_tol=1e-10, pres_tol=1e-10, pressure_guess=2, pressure_basis=4)
+    b.step(5)
+    for q, nu in enumerate(NUS):
+        st = G.ChorinStepper(c, nu, 1e-3, precision=G.NSF_PREC_MIXED, vel_method=3, vel_max_iters=500, vel_tol=1e-10,
+                             pres_max_iters=5000, pres_tol=1e-10, use_graph=True, max_outer=4, inner_tol=1e-5,
+                             pressure_guess=2, pressure_basis=4)
+        st.set_dirichlet(dir_vx[q])
+        st.step(5)
+        u, p = st.state()
+        ub, pb = b.state(q)
+        eu = np.linalg.norm(u - ub) / np.linalg.norm(u)
+        ep = np.linalg.norm(p - pb) / np.linalg.norm(p)
+        print(f"instance {q}: u {eu:.3e} p {ep:.3e}")
+        assert eu <= 3e-11 and ep <= 2e-8
