@@ -345,16 +345,19 @@ def bench_adjoint(args):
         variants = {}
         if args.adjoint_variants:
             other = [p for p in precs if p != args.adjoint_precision][0]
-            for name, ck, pr in (("keep_all_states", 0, prec),
-                                 (f"precision_{other}", args.adjoint_checkpoint, precs[other])):
+            for name, ck, pr, sn in (("keep_all_states", 0, prec, 0),
+                                     (f"binomial_{args.adjoint_snapshots}_states", 0, prec, args.adjoint_snapshots),
+                                     (f"precision_{other}", args.adjoint_checkpoint, precs[other], 0)):
                 var = GC.DragProblem(mesh, ctx, ADJ_PEAK, ADJ_NU, ADJ_TAU, n, w, n_coef=16, tol=ADJ_TOL,
-                                     checkpoint_interval=ck, precision=pr, vel_method=args.adjoint_vel_method)
+                                     checkpoint_interval=ck, precision=pr, vel_method=args.adjoint_vel_method,
+                                     snapshots=sn)
                 Jk, gnuk, gthk, _ = var.gradient(ADJ_NU, theta)
                 sk = var.adjoint.stats()
                 variants[name] = {
                     "gradient_s": round((sk["forward_ms"] + sk["reverse_ms"]) / 1e3, 3),
                     "forward_s": round(sk["forward_ms"] / 1e3, 3), "reverse_s": round(sk["reverse_ms"] / 1e3, 3),
-                    "state_bytes": int(sk["state_bytes"]), "checkpoint_interval": ck,
+                    "state_bytes": int(sk["state_bytes"]), "checkpoint_interval": ck, "snapshots": sn,
+                    "recomputed_steps": int(sk["recomputed_steps"]),
                     "adjoint_pressure_cg_iters": int(sk["pres_iters"]), "adjoint_mass_cg_iters": int(sk["mass_iters"]),
                     "max_rel_diff_vs_headline": float(max(abs(gnuk - gnu) / abs(gnu),
                                                           np.abs(gthk - gth).max() / np.abs(gth).max()))}
@@ -1144,6 +1147,8 @@ def main():
                          "solution, 1 extrapolated, 2 projected onto earlier solutions")
     ap.add_argument("--adjoint-steps", type=int, default=1000)
     ap.add_argument("--adjoint-checkpoint", type=int, default=50)
+    ap.add_argument("--adjoint-snapshots", type=int, default=20,
+                    help="adjoint workload: stored states of the binomial-checkpointing variant")
     ap.add_argument("--adjoint-precision", default="mixedsolve", choices=["f64", "mixedsolve"])
     ap.add_argument("--adjoint-vel-method", type=int, default=2, choices=[1, 2, 3],
                     help="mass solve: 1 PCG multicolor SGS, 2 PCG Jacobi, 3 Chebyshev Jacobi")

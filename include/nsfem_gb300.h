@@ -390,6 +390,10 @@ typedef struct
                                segment from its checkpoint.  0: keep every state (no recomputation) */
     int maxIters;           /* cap of each adjoint CG solve (<= 0: 20000) */
     double tol;             /* relative residual of each adjoint CG solve (<= 0: 1e-13) */
+    int snapshots;          /* > 0: binomial checkpointing instead (checkpointInterval ignored):
+                               at most this many stored states besides the initial one, placed by
+                               the schedule that minimises the recomputed steps for that memory
+                               (Griewank's binomial checkpointing, as in revolve); 0: off */
 } nsf_adjoint_config;
 
 typedef struct nsf_adjoint_s *nsf_adjoint;

@@ -40,7 +40,8 @@ class ChorinConfig(C.Structure):
 
 class AdjointConfig(C.Structure):
     """nsf_adjoint_config"""
-    _fields_ = [("checkpointInterval", C.c_int), ("maxIters", C.c_int), ("tol", C.c_double)]
+    _fields_ = [("checkpointInterval", C.c_int), ("maxIters", C.c_int), ("tol", C.c_double),
+                ("snapshots", C.c_int)]
 
 
 _SIGS = {

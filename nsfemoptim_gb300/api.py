@@ -575,15 +575,16 @@ class Adjoint:
     J = sum_n w_drag[n] F_x(u_n, p_n) + w_lift[n] F_y(u_n, p_n).  New: the reference has no adjoint.
 
     checkpoint_interval: steps between stored states (segments recomputed in the reverse sweep);
-    0 keeps every state."""
+    0 keeps every state.  snapshots > 0: binomial checkpointing with at most that many stored
+    states besides the initial one (checkpoint_interval ignored)."""
 
     STATS = ("forward_steps", "recomputed_steps", "reverse_steps", "mass_iters", "pres_iters",
              "forward_status", "adjoint_status", "state_bytes", "forward_ms", "reverse_ms")
 
     def __init__(self, stepper: ChorinStepper, forces: Forces, checkpoint_interval: int = 50,
-                 max_iters: int = 20000, tol: float = 1e-13):
+                 max_iters: int = 20000, tol: float = 1e-13, snapshots: int = 0):
         from ._lib import AdjointConfig
-        self.cfg = AdjointConfig(int(checkpoint_interval), int(max_iters), float(tol))
+        self.cfg = AdjointConfig(int(checkpoint_interval), int(max_iters), float(tol), int(snapshots))
         h = vp()
         check(lib().nsf_adjoint_create(stepper._h, forces._h, C.byref(self.cfg), C.byref(h)))
         self._h = h

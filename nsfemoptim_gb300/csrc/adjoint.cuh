@@ -385,8 +385,97 @@ struct nsf_adjoint_s
         spmvF64(IT, lA.get(), lam.get(), 1.0, 1.0, s);
     }
 
+    // ---- binomial checkpointing: the schedule with the fewest recomputed steps for a given number
+    // of stored states (the recursion behind Griewank's revolve, solved exactly by dynamic
+    // programming): to reverse k steps whose first input state is stored, with s more states
+    // available, advance m steps, store that state, reverse the last k - m steps with s - 1 states,
+    // restore the first state and reverse the first m steps with s states;
+    //   R(1, s) = 0,  R(k, 0) = k (k - 1) / 2,  R(k, s) = min_m  m + R(k - m, s - 1) + R(m, s).
+    std::vector<int> binoSplit; // best m for (k, s), row-major over s
+    int binoK = 0, binoS = 0;
+
+    void planBinomial(int K, int Smax)
+    {
+        binoK = K;
+        binoS = Smax;
+        std::vector<long long> R((size_t)(K + 1) * (Smax + 1), 0);
+        binoSplit.assign((size_t)(K + 1) * (Smax + 1), 1);
+        auto at = [&](int k, int s) -> long long & { return R[(size_t)s * (K + 1) + k]; };
+        for (int k = 1; k <= K; k++)
+            at(k, 0) = (long long)k * (k - 1) / 2;
+        for (int s = 1; s <= Smax; s++)
+            for (int k = 2; k <= K; k++)
+            {
+                long long best = -1;
+                int bm = 1;
+                for (int m = 1; m < k; m++)
+                {
+                    const long long c = m + at(k - m, s - 1) + at(m, s);
+                    if (best < 0 || c < best)
+                    {
+                        best = c;
+                        bm = m;
+                    }
+                }
+                at(k, s) = best;
+                binoSplit[(size_t)s * (K + 1) + k] = bm;
+            }
+    }
+
+    void saveState(int slot, cudaStream_t s)
+    {
+        const size_t twoN = 2 * (size_t)N;
+        copyDev(ckU.get() + (size_t)slot * twoN, S->u.get(), twoN, s);
+        copyDev(ckP.get() + (size_t)slot * nI, S->pInt.get(), nI, s);
+    }
+
+    void restoreState(int slot, cudaStream_t s)
+    {
+        const size_t twoN = 2 * (size_t)N;
+        copyDev(S->u.get(), ckU.get() + (size_t)slot * twoN, twoN, s);
+        copyDev(S->pInt.get(), ckP.get() + (size_t)slot * nI, nI, s);
+    }
+
+    // reverse steps [l, l + k) with the input state of step l in slot `slot` and in the stepper,
+    // s more slots above it free
+    void reverseBinomial(int l, int k, int slot, int sFree, cudaStream_t s, long long & recomputed, long long & reversed)
+    {
+        if (k == 1)
+        {
+            copyDev(segU.get(), S->u.get(), 2 * (size_t)N, s);
+            reverseStep(l, segU.get(), s);
+            reversed++;
+            return;
+        }
+        if (sFree == 0)
+        {
+            for (int n = l + k - 1; n >= l; n--)
+            {
+                restoreState(slot, s);
+                enqueueSteps(S, n - l, s);
+                recomputed += n - l;
+                copyDev(segU.get(), S->u.get(), 2 * (size_t)N, s);
+                reverseStep(n, segU.get(), s);
+                reversed++;
+            }
+            return;
+        }
+        const int m = binoSplit[(size_t)sFree * (binoK + 1) + k];
+        enqueueSteps(S, m, s);
+        recomputed += m;
+        saveState(slot + 1, s);
+        reverseBinomial(l + m, k - m, slot + 1, sFree - 1, s, recomputed, reversed);
+        restoreState(slot, s);
+        reverseBinomial(l, m, slot, sFree, s, recomputed, reversed);
+    }
+
     void run(int nSteps, cudaStream_t s)
     {
+        if (cfg.snapshots > 0)
+        {
+            runBinomial(nSteps, s);
+            return;
+        }
         const int C = cfg.checkpointInterval;
         const size_t twoN = 2 * (size_t)N;
         const int nCk = C > 0 ? (nSteps + C - 1) / C : 0;
@@ -482,6 +571,72 @@ struct nsf_adjoint_s
         stats[8] = msF;
         stats[9] = msB;
     }
+
+    // the run with binomial checkpointing: the forward pass stores the initial state only; the
+    // reverse sweep recomputes by the binomial schedule with cfg.snapshots further states
+    void runBinomial(int nSteps, cudaStream_t s)
+    {
+        const size_t twoN = 2 * (size_t)N;
+        int last = -1;
+        for (int n = 0; n < nSteps; n++)
+            if (hwD[n] != 0.0 || hwL[n] != 0.0)
+                last = n;
+        const int K = last + 1, Sfree = cfg.snapshots;
+        if (K > 1 && (binoK != K || binoS != Sfree))
+            planBinomial(K, Sfree);
+        ensure(ckU, (size_t)(Sfree + 1) * twoN);
+        ensure(ckP, (size_t)(Sfree + 1) * nI);
+        ensure(segU, twoN);
+        ensure(forcesLog, 4 * (size_t)std::max(1, nSteps));
+        wD.upload(hwD);
+        wL.upload(hwL);
+        NSF_CUDA(cudaMemsetAsync(tally.get(), 0, 6 * sizeof(int), s));
+        NSF_CUDA(cudaMemsetAsync(scal.get(), 0, 3 * sizeof(double), s));
+        NSF_CUDA(cudaMemsetAsync(forcesLog.get(), 0, 4 * sizeof(double) * std::max(1, nSteps), s));
+        NSF_CUDA(cudaMemsetAsync(lam.get(), 0, twoN * sizeof(double), s));
+        NSF_CUDA(cudaMemsetAsync(lDir.get(), 0, N * sizeof(double), s));
+        NSF_CUDA(cudaMemsetAsync(y.get(), 0, nI * sizeof(double), s));
+        NSF_CUDA(cudaEventRecord(ev[0], s));
+        saveState(0, s);
+        for (int n = 0; n < nSteps; n++)
+        {
+            enqueueSteps(S, 1, s);
+            forwardTallies(s);
+            if (hwD[n] != 0.0 || hwL[n] != 0.0)
+                NSF_LAUNCH(kForces, 1, s, F->pts.get(), F->npts, S->u.get(), N, S->pInt.get(), S->cfg.nu,
+                           forcesLog.get() + 4 * (size_t)n, forcesLog.get() + 4 * (size_t)n + 2);
+        }
+        copyDev(finU.get(), S->u.get(), twoN, s);
+        copyDev(finP.get(), S->pInt.get(), nI, s);
+        NSF_LAUNCH(kFunctional, 1, s, nSteps, forcesLog.get(), wD.get(), wL.get(), scal.get());
+        NSF_CUDA(cudaEventRecord(ev[1], s));
+        long long recomputed = 0, reversed = 0;
+        if (K > 0)
+        {
+            restoreState(0, s);
+            reverseBinomial(0, K, 0, Sfree, s, recomputed, reversed);
+        }
+        NSF_LAUNCH(kAdjFinish, blocksFor(N), s, N, lam.get(), S->isDir.get(), lDir.get());
+        NSF_CUDA(cudaEventRecord(ev[2], s));
+        copyDev(S->u.get(), finU.get(), twoN, s);
+        copyDev(S->pInt.get(), finP.get(), nI, s);
+        int t[6];
+        NSF_CUDA(cudaMemcpyAsync(t, tally.get(), sizeof t, cudaMemcpyDeviceToHost, s));
+        NSF_CUDA(cudaStreamSynchronize(s));
+        float msF = 0, msB = 0;
+        NSF_CUDA(cudaEventElapsedTime(&msF, ev[0], ev[1]));
+        NSF_CUDA(cudaEventElapsedTime(&msB, ev[1], ev[2]));
+        stats[0] = nSteps;
+        stats[1] = (double)recomputed;
+        stats[2] = (double)reversed;
+        stats[3] = t[3];
+        stats[4] = t[5];
+        stats[5] = t[0];
+        stats[6] = std::max(t[2], t[4]);
+        stats[7] = (double)sizeof(double) * ((double)ckU.size() + ckP.size() + segU.size());
+        stats[8] = msF;
+        stats[9] = msB;
+    }
 };
 
 extern "C" int nsf_adjoint_create(nsf_chorin S, nsf_forces f, const nsf_adjoint_config * cfg, nsf_adjoint * out)
@@ -498,6 +653,7 @@ extern "C" int nsf_adjoint_create(nsf_chorin S, nsf_forces f, const nsf_adjoint_
         if (cfg)
             a->cfg = *cfg;
         require(a->cfg.checkpointInterval >= 0, "checkpointInterval must be >= 0");
+        require(a->cfg.snapshots >= 0 && a->cfg.snapshots <= 4096, "snapshots must be in 0..4096");
         if (a->cfg.maxIters <= 0)
             a->cfg.maxIters = 20000;
         if (!(a->cfg.tol > 0))

@@ -31,10 +31,11 @@ class DragProblem:
     def __init__(self, mesh: Mesh, ctx: ChorinContext, peak: float, nu: float, tau: float, n_steps: int,
                  weights, n_coef: int = 16, tol: float = 1e-13, checkpoint_interval: int = 50,
                  max_iters: int = 20000, precision: int = NSF_PREC_F64, max_outer: int = 6,
-                 inner_tol: float = 1e-5, vel_method: int = 1):
+                 inner_tol: float = 1e-5, vel_method: int = 1, snapshots: int = 0):
         """precision: NSF_PREC_F64 (FP64 solves) or NSF_PREC_F64_MIXEDSOLVE (FP64 operators, FP32 CG
         inside FP64 refinement / residual replacement to the same tolerance; max_outer passes with
-        inner tolerance inner_tol).  vel_method: mass solve, 1 PCG-SGS, 2 PCG-Jacobi, 3 Chebyshev-Jacobi."""
+        inner tolerance inner_tol).  vel_method: mass solve, 1 PCG-SGS, 2 PCG-Jacobi, 3 Chebyshev-Jacobi.
+        snapshots > 0: binomial checkpointing with that many stored states (checkpoint_interval ignored)."""
         self.mesh, self.ctx = mesh, ctx
         self.n_steps = int(n_steps)
         self.stepper = ChorinStepper(ctx, nu, tau, precision=precision, vel_method=vel_method,
@@ -43,7 +44,7 @@ class DragProblem:
                                      max_outer=max_outer, inner_tol=inner_tol)
         self.forces = Forces(mesh, self.stepper)
         self.adjoint = Adjoint(self.stepper, self.forces, checkpoint_interval=checkpoint_interval,
-                               max_iters=max_iters, tol=tol)
+                               max_iters=max_iters, tol=tol, snapshots=snapshots)
         u_mean = peak / 6.0
         self.scale = 2.0 / (u_mean * u_mean * D_CYLINDER)
         self.w = np.ascontiguousarray(np.broadcast_to(np.asarray(weights, np.float64), (self.n_steps,))) * self.scale

@@ -5,7 +5,8 @@ nsfemoptim_gb300.gradcheck).  No reference counterpart exists; these are the pin
 Tolerances:
   GPU vs oracle adjoint (same discrete step, solves to 1e-13 / 1e-14):  J rel 1e-11,
       dJ/dnu rel 1e-8, dJ/d dirVx and dJ/du0 normwise rel 1e-8
-  checkpoint interval 0 / 3 / 5:  bit-identical results (the recomputation replays the same kernels)
+  checkpoint interval 0 / 3 / 5 and binomial checkpointing with 1 / 2 / 3 / 8 stored states:
+      bit-identical results (the recomputation replays the same kernels)
   adjoint vs central FD (eps = 1e-6):  rel 1e-6 per component (gradcheck rtol), atol 1e-6 x max|g|
 """
 
@@ -141,6 +142,46 @@ def test_checkpointing_is_exact(adj_setup):
     for c in (3, 5):
         assert out[c][0] == out[0][0] and out[c][1] == out[0][1]
         assert np.array_equal(out[c][2], out[0][2]) and np.array_equal(out[c][3], out[0][3])
+
+
+def _binomial_recomputations(k, s):
+    """Fewest recomputed steps to reverse k steps with s stored states besides the first:
+    R(1, s) = 0, R(k, 0) = k (k - 1) / 2, R(k, s) = min_m m + R(k - m, s - 1) + R(m, s)."""
+    R = [[0] * (s + 1) for _ in range(k + 1)]
+    for kk in range(1, k + 1):
+        R[kk][0] = kk * (kk - 1) // 2
+    for ss in range(1, s + 1):
+        for kk in range(2, k + 1):
+            R[kk][ss] = min(m + R[kk - m][ss - 1] + R[m][ss] for m in range(1, kk))
+    return R[k][s]
+
+
+def test_binomial_checkpointing_is_exact(adj_setup):
+    """Binomial checkpointing (snapshots > 0) gives the same bits as keeping every state, with the
+    fewest recomputed steps for its memory (the binomial recursion's optimum) and (s + 1) stored
+    states."""
+    G, O, mesh, ctx, om, oc = adj_setup
+    rng = np.random.default_rng(13)
+    n = 11
+    wd = np.zeros(n)
+    wd[4:9] = rng.random(5)  # the reverse sweep covers steps 0..8
+    u0 = _start(rng, ctx.N)
+    st = _stepper(G, ctx)
+    f = G.Forces(mesh, st)
+
+    def run(**kw):
+        adj = G.Adjoint(st, f, **kw)
+        st.set_state(u0, np.zeros(ctx.P))
+        st.set_dirichlet(ctx.dir_vx)
+        return adj.run(n, wd), adj.stats()
+
+    ref, _ = run(checkpoint_interval=0)
+    for snaps in (1, 2, 3, 8):
+        out, s = run(snapshots=snaps)
+        assert s["reverse_steps"] == 9
+        assert s["recomputed_steps"] == _binomial_recomputations(9, snaps), (snaps, s["recomputed_steps"])
+        assert out[0] == ref[0] and out[1] == ref[1]
+        assert np.array_equal(out[2], ref[2]) and np.array_equal(out[3], ref[3])
 
 
 def test_set_nu_changes_the_forward_run(adj_setup):
