@@ -74,6 +74,14 @@ typedef struct nsf_context_s *nsf_context;
    fem::buildChorinCsrMatrices (cpp/libs/Fem/src/chorinCsr.cpp:437-502) and fem::FastConvection
    (cpp/libs/Fem/src/fastConvection.cpp:9-100).  nThreads <= 0 picks the hardware count. */
 int nsf_context_build(nsf_mesh mesh, float peakVelocity, int nThreads, nsf_context *out);
+/* nsf_context_build with the operator values assembled on the GPU: the patterns, boundary lists
+   and the internal-pressure slice on the host, every value of M, K, Kp, D, G and I by one device
+   thread per output row gathering its incident elements in ascending order (the element-parallel
+   local matrices of cpp/libs/Element/src/triangleIntegrator.cpp:132-293 and the accumulation of
+   cpp/libs/Fem/src/chorinCsr.cpp:296-419 and cpp/libs/Fem/src/fastConvection.cpp:52-97); the values
+   equal nsf_context_build's bit for bit.  assemblyMs (may be NULL): device time of the assembly
+   kernels. */
+int nsf_context_build_device(nsf_mesh mesh, float peakVelocity, int nThreads, nsf_context *out, double *assemblyMs);
 /* sizes[0..12] = N, P, nDir, nDirP, nIntV, nIntP, nnz(M), nnz(K), nnz(Kp), nnz(Kpi), nnz(D),
    nnz(G), nnz(I) */
 int nsf_context_sizes(nsf_context ctx, int *sizes);

@@ -54,6 +54,7 @@ _SIGS = {
     "nsf_mesh_group": (C.c_char_p, [vp, C.c_int]),
     "nsf_mesh_destroy": (None, [vp]),
     "nsf_context_build": (C.c_int, [vp, C.c_float, C.c_int, C.POINTER(vp)]),
+    "nsf_context_build_device": (C.c_int, [vp, C.c_float, C.c_int, C.POINTER(vp), f64p]),
     "nsf_context_sizes": (C.c_int, [vp, i32p]),
     "nsf_context_matrix": (C.c_int, [vp, C.c_int, i32p, i32p, f64p]),
     "nsf_context_lists": (C.c_int, [vp, i32p, f64p, i32p, i32p, i32p]),

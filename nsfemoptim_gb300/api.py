@@ -92,9 +92,17 @@ class ChorinContext:
 
     MATRICES = ("M", "K", "Kp", "Kpi", "D", "G", "I")
 
-    def __init__(self, mesh: Mesh, peak_velocity: float, n_threads: int = 0):
+    def __init__(self, mesh: Mesh, peak_velocity: float, n_threads: int = 0, device: bool = False):
+        """device: assemble the operator values on the GPU (nsf_context_build_device; the same bits)."""
         h = vp()
-        check(lib().nsf_context_build(mesh._h, C.c_float(peak_velocity), n_threads, C.byref(h)))
+        self.assembly_ms = None
+        if device:
+            ms = C.c_double(0.0)
+            check(lib().nsf_context_build_device(mesh._h, C.c_float(peak_velocity), n_threads, C.byref(h),
+                                                 C.byref(ms)))
+            self.assembly_ms = ms.value
+        else:
+            check(lib().nsf_context_build(mesh._h, C.c_float(peak_velocity), n_threads, C.byref(h)))
         self._h = h
         s = (C.c_int * 13)()
         check(lib().nsf_context_sizes(h, s))
@@ -139,8 +147,8 @@ class ChorinContext:
             self._h = None
 
 
-def build_chorin_context(mesh: Mesh, peak_velocity: float, n_threads: int = 0) -> ChorinContext:
-    return ChorinContext(mesh, peak_velocity, n_threads)
+def build_chorin_context(mesh: Mesh, peak_velocity: float, n_threads: int = 0, device: bool = False) -> ChorinContext:
+    return ChorinContext(mesh, peak_velocity, n_threads, device)
 
 
 def coloring(rowStart, column):

@@ -483,6 +483,22 @@ extern "C" int nsf_context_build(nsf_mesh mesh, float peak, int nThreads, nsf_co
     });
 }
 
+// ============================================================ on-device assembly
+#include "assembly.cuh"
+
+extern "C" int nsf_context_build_device(nsf_mesh mesh, float peak, int nThreads, nsf_context * out, double * assemblyMs)
+{
+    return guarded([&] {
+        require(mesh && out, "null argument");
+        auto h = std::make_unique<nsf_context_s>();
+        h->c = buildChannelContextEx(mesh->m, peak, nThreads, false);
+        const double ms = assembleOnDevice(mesh->m, h->c);
+        if (assemblyMs)
+            *assemblyMs = ms;
+        *out = h.release();
+    });
+}
+
 extern "C" int nsf_context_sizes(nsf_context h, int * s)
 {
     return guarded([&] {

@@ -424,7 +424,35 @@ namespace nsf
         return true;
     }
 
+    AssemblyTables assemblyTables()
+    {
+        static const RefTensors TT = makeTensors();
+        AssemblyTables out;
+        std::copy(&TT.mass[0][0], &TT.mass[0][0] + 36, out.mass);
+        std::copy(&TT.sxx[0][0], &TT.sxx[0][0] + 36, out.sxx);
+        std::copy(&TT.sxy[0][0], &TT.sxy[0][0] + 36, out.sxy);
+        std::copy(&TT.syy[0][0], &TT.syy[0][0] + 36, out.syy);
+        std::copy(&TT.divX[0][0], &TT.divX[0][0] + 18, out.divX);
+        std::copy(&TT.divY[0][0], &TT.divY[0][0] + 18, out.divY);
+        std::copy(&TT.grdX[0][0], &TT.grdX[0][0] + 18, out.grdX);
+        std::copy(&TT.grdY[0][0], &TT.grdY[0][0] + 18, out.grdY);
+        std::copy(&TT.advX[0][0][0], &TT.advX[0][0][0] + 216, out.advX);
+        std::copy(&TT.advY[0][0][0], &TT.advY[0][0][0] + 216, out.advY);
+        std::copy(&TT.p1stiff[0][0][0], &TT.p1stiff[0][0][0] + 27, out.p1stiff);
+        return out;
+    }
+
+    void incidenceOf(int nNodes, const std::vector<int> & elem, int per, std::vector<int> & start, std::vector<int> & list)
+    {
+        incidence(nNodes, elem, per, start, list);
+    }
+
     Context buildChannelContext(const Mesh & m, float peakVelocity, int nThreads)
+    {
+        return buildChannelContextEx(m, peakVelocity, nThreads, true);
+    }
+
+    Context buildChannelContextEx(const Mesh & m, float peakVelocity, int nThreads, bool values)
     {
         if (nThreads <= 0)
             nThreads = (int)std::max(1u, std::thread::hardware_concurrency());
@@ -484,6 +512,35 @@ namespace nsf
 
         // ---- values: gather per row over incident elements in ascending element order
         static const RefTensors TT = makeTensors();
+        if (!values)
+        {
+            // patterns only (the values are assembled elsewhere, e.g. on the device)
+            c.Kpi = sliceCsr(c.Kp, c.intP, c.intP);
+            const int nnzK = c.K.nnz();
+            std::vector<int> entryRow(nnzK);
+            for (int r = 0; r < N; r++)
+                for (int e = c.K.rowStart[r]; e < c.K.rowStart[r + 1]; e++)
+                    entryRow[e] = r;
+            c.I = buildPattern(nnzK, 2 * N, nThreads, [&](int e, std::vector<int> & out)
+            {
+                const int r = entryRow[e], cc = c.K.col[e];
+                for (int k = vStart[r]; k < vStart[r + 1]; k++)
+                {
+                    const int * ids = &m.vElem[6 * (size_t)vList[k]];
+                    bool has = false;
+                    for (int q = 0; q < 6; q++)
+                        has |= ids[q] == cc;
+                    if (!has)
+                        continue;
+                    for (int q = 0; q < 6; q++)
+                    {
+                        out.push_back(ids[q]);
+                        out.push_back(ids[q] + N);
+                    }
+                }
+            });
+            return c;
+        }
         std::vector<Geo> geo(T);
         parallelFor(T, nThreads, [&](int a, int b)
         {

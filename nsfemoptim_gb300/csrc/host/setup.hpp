@@ -56,6 +56,25 @@ namespace nsf
     };
 
     Context buildChannelContext(const Mesh & mesh, float peakVelocity, int nThreads);
+    // the same; values == false: patterns and lists only, every operator value 0 (Kpi and I
+    // patterns included)
+    Context buildChannelContextEx(const Mesh & mesh, float peakVelocity, int nThreads, bool values);
+
+    // Element-independent reference tensors of the P2/P1 operators on straight triangles (degree-4
+    // Cowper rule) that the assembly contracts with each element's adjugate and determinant:
+    // mass, the stiffness parts sum w g_i g_j (xx, xy, yy), divergence sum w psi_r g_c (x, y),
+    // gradient sum w phi_r dpsi_c (x, y), advection [r][c][k] sum w phi_r phi_k g_c (x, y), and the
+    // area-weighted P1 stiffness [i][j][t00 | t01 | t11], all row-major.
+    struct AssemblyTables
+    {
+        double mass[36], sxx[36], sxy[36], syy[36];
+        double divX[18], divY[18], grdX[18], grdY[18];
+        double advX[216], advY[216];
+        double p1stiff[27];
+    };
+    AssemblyTables assemblyTables();
+    // node -> incident elements (ascending); elem holds `per` node ids per element
+    void incidenceOf(int nNodes, const std::vector<int> & elem, int per, std::vector<int> & start, std::vector<int> & list);
 
     HostCsr<double> sliceCsr(const HostCsr<double> & a, const std::vector<int> & rows, const std::vector<int> & cols);
 
