@@ -617,13 +617,14 @@ def bench_pack(args):
     os.environ["NSF_PCG_PATH"] = "auto-cluster"
     try:
         t0 = time.perf_counter()
-        steppers, meshes, sizes = [], [], {}
+        steppers, meshes, sizes, draws = [], [], {}, []
         for h in hs:
             mesh = G.load_gmsh(make_mesh(tmp, h, 0))
             meshes.append(mesh)
             for _ in range(per):
                 umax = float(rng.uniform(0.2, 1.5))
                 nu = float(math.exp(rng.uniform(math.log(5e-4), math.log(2e-3))))
+                draws.append((umax, nu))
                 ctx = G.build_chorin_context(mesh, 4.0 * umax)
                 sizes[h] = (ctx.N, ctx.P)
                 steppers.append(G.ChorinStepper(ctx, nu, tau, precision=G.NSF_PREC_MIXED, vel_method=args.vel_method,
@@ -663,7 +664,32 @@ def bench_pack(args):
             st.step(1, stream.cuda_stream)
             status.append(int(st.stats()["status"]))
         launches = G.kernel_launches()
+        pack_kernels = pack.kernels_per_step()
         del pack
+        # the same instances as three batches (one per mesh, nsf_batch) in one pack graph: every
+        # operation one launch per mesh; the same step window as the pack of steppers
+        batches = []
+        for i, mesh in enumerate(meshes):
+            um = np.array([d[0] for d in draws[i * per:(i + 1) * per]])
+            nus = np.array([d[1] for d in draws[i * per:(i + 1) * per]])
+            bctx = G.build_chorin_context(mesh, 4.0)
+            batches.append(G.Batch(bctx, nus, tau, dir_vx=np.stack([bctx.dir_vx * u for u in um]), vel_max_iters=500,
+                                   vel_tol=VEL_TOL, pres_max_iters=5000, pres_tol=PRES_TOL, use_graph=True,
+                                   max_outer=4, inner_tol=1e-5, pressure_guess=args.pressure_guess,
+                                   pressure_basis=args.pressure_basis))
+        bpack = G.Pack(batches)
+        bpack.step(W, stream.cuda_stream)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        bpack.step(K, stream.cuda_stream)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        t_bpack = e0.elapsed_time(e1) / 1e3
+        bpack_kernels = bpack.kernels_per_step()
+        for b in batches:
+            b.step(1, stream.cuda_stream)
+        bstatus = [int(b.stats(q)["status"]) for b in batches for q in range(per)]
+        del bpack, batches
     finally:
         if old is None:
             os.environ.pop("NSF_PCG_PATH", None)
@@ -688,6 +714,13 @@ def bench_pack(args):
         "one_instance_alone_steps_per_s": alone,
         "status_all_ok": all(s == 0 for s in status),
         "kernel_launches_total": int(launches),
+        "kernels_per_pack_step": int(pack_kernels),
+        "batched_pack": {"instance_steps_per_s": round(n * K / t_bpack, 2),
+                         "over_pack_of_steppers": round(t_pack / t_bpack, 2),
+                         "kernels_per_pack_step": int(bpack_kernels),
+                         "status_all_ok": all(s == 0 for s in bstatus),
+                         "execution": "the same instances as three nsf_batch objects (one per mesh, same U_max and "
+                                      "nu draws) as the branches of one pack graph (nsf_pack_create_batches)"},
     }
 
 

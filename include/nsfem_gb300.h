@@ -330,6 +330,14 @@ typedef struct nsf_pack_s *nsf_pack;
    whole-GPU cooperative grid could wait on each other's SMs.  The steppers must outlive the pack
    and must not be stepped through their own handles while a pack launch is in flight. */
 int nsf_pack_create(const nsf_chorin *steppers, int n, nsf_pack *out);
+/* A pack of batches (nsf_batch_create): one graph whose branches are the batched time steps, one
+   branch per batch (e.g. one batch per mesh resolution), so one graph launch advances every
+   instance of every batch with one kernel per operation and batch.  The batches must outlive the
+   pack and must not be stepped through their own handles while a pack launch is in flight.
+   Declared here, after nsf_batch. */
+int nsf_pack_create_batches(struct nsf_batch_s *const *batches, int n, nsf_pack *out);
+/* kernel launches of one pack step */
+long long nsf_pack_kernels_per_step(nsf_pack p);
 /* enqueue nSteps launches of the pack graph on stream (NULL: the pack's own stream); asynchronous */
 int nsf_pack_step(nsf_pack p, int nSteps, void *stream);
 void nsf_pack_destroy(nsf_pack p);

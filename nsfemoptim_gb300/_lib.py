@@ -120,6 +120,8 @@ _SIGS = {
     "nsf_adjoint_stats": (C.c_int, [vp, f64p]),
     "nsf_adjoint_destroy": (None, [vp]),
     "nsf_pack_create": (C.c_int, [C.POINTER(vp), C.c_int, C.POINTER(vp)]),
+    "nsf_pack_create_batches": (C.c_int, [C.POINTER(vp), C.c_int, C.POINTER(vp)]),
+    "nsf_pack_kernels_per_step": (C.c_longlong, [vp]),
     "nsf_pack_step": (C.c_int, [vp, C.c_int, vp]),
     "nsf_pack_destroy": (None, [vp]),
 }

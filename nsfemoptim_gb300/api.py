@@ -562,11 +562,18 @@ class Pack:
     them with NSF_PCG_PATH=auto-cluster in the environment (solves inside thread-block clusters)."""
 
     def __init__(self, steppers):
+        """steppers: ChorinStepper objects, or Batch objects (one graph branch per batch)."""
         self._steppers = list(steppers)  # they must outlive the pack
         arr = (vp * len(self._steppers))(*[s._h for s in self._steppers])
         h = vp()
-        check(lib().nsf_pack_create(arr, len(self._steppers), C.byref(h)))
+        if all(isinstance(s, Batch) for s in self._steppers):
+            check(lib().nsf_pack_create_batches(arr, len(self._steppers), C.byref(h)))
+        else:
+            check(lib().nsf_pack_create(arr, len(self._steppers), C.byref(h)))
         self._h = h
+
+    def kernels_per_step(self) -> int:
+        return int(lib().nsf_pack_kernels_per_step(self._h))
 
     def step(self, n: int = 1, stream=None):
         """Enqueue n graph launches (asynchronous)."""

@@ -2264,8 +2264,8 @@ extern "C" int nsf_residual_noalloc(nsf_csr a, int nrhs, const double * x, const
 // ============================================================ discrete adjoint (gradients)
 #include "adjoint.cuh"
 
-// ============================================================ packs of steppers (one graph)
-#include "pack.cuh"
-
 // ============================================================ batched instances (one launch per operation)
 #include "batch.cuh"
+
+// ============================================================ packs of steppers (one graph)
+#include "pack.cuh"

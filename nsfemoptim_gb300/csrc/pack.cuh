@@ -13,6 +13,7 @@
 struct nsf_pack_s
 {
     std::vector<nsf_chorin> S;
+    std::vector<nsf_batch> Bt; // batches (nsf_pack_create_batches): one branch per batch
     cudaStream_t stream = nullptr;
     std::vector<cudaStream_t> branch;
     std::vector<cudaEvent_t> joined;
@@ -46,10 +47,14 @@ struct nsf_pack_s
         try
         {
             NSF_CUDA(cudaEventRecord(fork, stream));
-            for (size_t i = 0; i < S.size(); i++)
+            const size_t n = S.size() + Bt.size();
+            for (size_t i = 0; i < n; i++)
             {
                 NSF_CUDA(cudaStreamWaitEvent(branch[i], fork, 0));
-                S[i]->enqueueStep(branch[i]);
+                if (i < S.size())
+                    S[i]->enqueueStep(branch[i]);
+                else
+                    Bt[i - S.size()]->enqueueStep(branch[i]);
                 NSF_CUDA(cudaEventRecord(joined[i], branch[i]));
                 NSF_CUDA(cudaStreamWaitEvent(stream, joined[i], 0));
             }
@@ -98,6 +103,34 @@ extern "C" int nsf_pack_create(const nsf_chorin * steppers, int n, nsf_pack * ou
         *out = p.release();
     });
 }
+
+extern "C" int nsf_pack_create_batches(const nsf_batch * batches, int n, nsf_pack * out)
+{
+    return guarded([&] {
+        require(batches && out && n >= 1, "bad argument");
+        auto p = std::make_unique<nsf_pack_s>();
+        for (int i = 0; i < n; i++)
+        {
+            require(batches[i] != nullptr, "null batch in the pack");
+            for (int j = 0; j < i; j++)
+                require(batches[j] != batches[i], "a batch appears twice in the pack");
+            p->Bt.push_back(batches[i]);
+        }
+        NSF_CUDA(cudaStreamCreateWithFlags(&p->stream, cudaStreamNonBlocking));
+        NSF_CUDA(cudaEventCreateWithFlags(&p->fork, cudaEventDisableTiming));
+        p->branch.resize(n, nullptr);
+        p->joined.resize(n, nullptr);
+        for (int i = 0; i < n; i++)
+        {
+            NSF_CUDA(cudaStreamCreateWithFlags(&p->branch[i], cudaStreamNonBlocking));
+            NSF_CUDA(cudaEventCreateWithFlags(&p->joined[i], cudaEventDisableTiming));
+        }
+        p->capture();
+        *out = p.release();
+    });
+}
+
+extern "C" long long nsf_pack_kernels_per_step(nsf_pack p) { return p ? p->kernelsPerCapture : 0; }
 
 extern "C" int nsf_pack_step(nsf_pack p, int nSteps, void * stream)
 {

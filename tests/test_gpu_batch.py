@@ -89,3 +89,33 @@ def test_batch_small_clusters_follow_steppers(ctx):
         ep = np.linalg.norm(p - pb) / np.linalg.norm(p)
         print(f"instance {q}: u {eu:.3e} p {ep:.3e}")
         assert eu <= 3e-11 and ep <= 2e-8
+
+
+def test_pack_of_batches_equals_batches_alone(ctx, channel_h01):
+    """A pack of batches (nsf_pack_create_batches: one graph whose branches are the batched steps,
+    here a batch on the h = 0.025 mesh and one on the h = 0.01 mesh) leaves every instance's state bit
+    for bit where the same batches stepped on their own leave it: the branches share nothing."""
+    G, c = ctx
+    fine = G.build_chorin_context(G.load_gmsh(channel_h01), 1.2)
+    dir_vx = np.stack([c.dir_vx * s for s in SCALES])
+
+    def make():
+        return [G.Batch(c, NUS, 1e-3, dir_vx=dir_vx, vel_tol=1e-10, pres_tol=1e-10, pressure_guess=2,
+                        pressure_basis=4),
+                G.Batch(fine, NUS[:2], 5e-4, vel_tol=1e-10, pres_tol=1e-10, pressure_guess=1)]
+
+    alone = make()
+    for b in alone:
+        b.step(4)
+    packed = make()
+    pack = G.Pack(packed)
+    assert pack.kernels_per_step() == sum(b.kernels_per_step() for b in alone)
+    pack.step(4)
+    import torch
+    torch.cuda.synchronize()
+    for a, b in zip(alone, packed):
+        for q in range(a.B):
+            ua, pa = a.state(q)
+            ub, pb = b.state(q)
+            assert np.array_equal(ua, ub) and np.array_equal(pa, pb), q
+            assert b.stats(q)["status"] == 0
