@@ -835,8 +835,11 @@ def bench_poisson(args):
         return torch.cuda.Event(enable_timing=True)
 
     out = {}
+    want = args.poisson_precisions.split(",")
     for name, prec in (("fp64", G.NSF_PREC_F64), ("mixed", G.NSF_PREC_MIXED)):
-        s = G.NeumannSolver(fhost, pin=0, precision=prec, max_iters=20000, target=1e-10)
+        if name not in want:
+            continue
+        s = G.NeumannSolver(fhost, pin=0, precision=prec, max_iters=args.poisson_max_iters, target=1e-10)
         xd = torch.zeros(nfull, dtype=torch.float64, device="cuda")
         best = None
         for rep in range(1 + max(1, args.poisson_reps)):  # the first solve is a warm-up
@@ -844,7 +847,11 @@ def bench_poisson(args):
             torch.cuda.synchronize()
             e0, e1 = ev(), ev()
             e0.record()
-            s.solve(bd, xd)
+            try:
+                s.solve(bd, xd)
+            except G.NsfError as e:
+                if e.status != 3 or args.poisson_max_iters >= 20000:
+                    raise  # status 3 (iteration cap) is expected only under a profiling cap
             e1.record()
             torch.cuda.synchronize()
             if rep > 0:
@@ -853,10 +860,13 @@ def bench_poisson(args):
         xf = xd.cpu().numpy()
         stt = s.stats()
         its, st = stt["iters"], 0
-        sv = 8 if name == "fp64" else 4
+        # sv: bytes of a value of A p and of the CG vectors, sp: of the SGS sweeps.  The mixed solve
+        # of a system this size (cooperative-grid path) is one CG with the FP64 recurrence and A p
+        # under the FP32 SGS preconditioner.
+        sv, sp = 8, (8 if name == "fp64" else 4)
         nnz = a.nnz
         it_bytes = (nnz * (sv + 4) + (n + 1) * 4 + 2 * n * sv) + \
-            2 * ((nnz - n) * (sv + 4) + (n + 1) * 4 + 4 * n * sv) + 7 * n * sv
+            2 * ((nnz - n) * (sp + 4) + (n + 1) * 4 + 4 * n * sp) + 7 * n * sv
         out[name] = {"solve_s": round(best, 5), "solves_per_s": round(1.0 / best, 3), "iterations": int(its),
                      "status": int(st),
                      "true_rel_residual": float(np.linalg.norm(bproj - full @ xf) / np.linalg.norm(bproj)),
@@ -873,6 +883,8 @@ def bench_poisson(args):
     flush_sum = torch.zeros((), dtype=torch.float32, device="cuda")
     spmv = {}
     for name, dt, tdt in (("fp64", G.NSF_F64, torch.float64), ("fp32", G.NSF_F32, torch.float32)):
+        if not args.poisson_spmv:
+            break
         A = G.CsrF.from_host(host, dtype=dt)
         xv = torch.randn(n, dtype=tdt, device="cuda")
         yv = torch.zeros(n, dtype=tdt, device="cuda")
@@ -905,12 +917,17 @@ def bench_poisson(args):
         v["frac_of_hbm_peak"] = round(v["gbs"] / hbm, 4)
     return {
         "metric": "config 3: standalone P1 Poisson PCG-SGS to 1e-10 rel (1024x1024 jittered square), solves/s",
-        "value": out["mixed"]["solves_per_s"], "unit": "solves/s", "n_gpus": 1, "higher_is_better": True,
-        "dtype": "f32-inner/f64-refine", "data": "synthetic (seeded jittered unit square, RHS N(0,1) seed 0)",
+        "value": out.get("mixed", out.get("fp64", {})).get("solves_per_s"), "unit": "solves/s", "n_gpus": 1,
+        "higher_is_better": True,
+        "dtype": "f64 CG recurrence and A p, f32 SGS preconditioner",
+        "data": "synthetic (seeded jittered unit square, RHS N(0,1) seed 0)",
         "config": {"workload": "P1 Laplacian, 1024x1024 nodes, jitter 0.2h, one pin", "rows": n, "nnz": int(a.nnz),
                    "setup_s": round(setup_s, 2)},
         "variants": out, "spmv": spmv, "peak": hbm, "peak_kind": kind,
-        "mixed_vs_fp64_speedup": round(out["fp64"]["solve_s"] / out["mixed"]["solve_s"], 3),
+        "mixed_vs_fp64_speedup": (round(out["fp64"]["solve_s"] / out["mixed"]["solve_s"], 3)
+                                  if "fp64" in out and "mixed" in out else None),
+        "mixed_form": "one CG with the FP64 recurrence, FP64 A p and dot products under the FP32 multicolor SGS "
+                      "preconditioner (cooperative grid, one launch), then the FP64 residual test",
     }
 
 
@@ -1201,6 +1218,10 @@ def main():
     ap.add_argument("--pack-steps", type=int, default=20)
     ap.add_argument("--long-steps", type=int, default=10000, help="long workload: steps from rest")
     ap.add_argument("--poisson-reps", type=int, default=2)
+    ap.add_argument("--poisson-max-iters", type=int, default=20000,
+                    help="poisson workload: iteration cap of each solve (a small cap gives short launches to profile)")
+    ap.add_argument("--poisson-precisions", default="fp64,mixed", help="poisson workload: solves to run")
+    ap.add_argument("--poisson-spmv", type=int, default=1, help="poisson workload: 0 skips the SpMV timing")
     args = ap.parse_args()
 
     world = int(os.environ.get("WORLD_SIZE", "1"))

@@ -1390,7 +1390,8 @@ struct nsf_chorin_s
     {
         using P = PcgSolver<double, 1>;
         return velT.path == P::GRID || velF.path == P::GRID || pres.path == P::GRID ||
-               mvelT.inner.path == P::GRID || mvelF.inner.path == P::GRID || mpres.inner.path == P::GRID;
+               mvelT.inner.path == P::GRID || mvelF.inner.path == P::GRID || mpres.inner.path == P::GRID ||
+               (mpres.pre32Form && mpres.pre32Solve.path == P::GRID);
     }
 
     ~nsf_chorin_s()

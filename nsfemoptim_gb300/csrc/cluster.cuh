@@ -40,7 +40,10 @@ namespace nsf
     constexpr int RB = 8;                          // entries per predicated batch of a row
     constexpr unsigned kGridSpinLimit = 1u << 22;  // default polls of a grid barrier before it gives up (seconds)
 
-    template <typename T>
+    // T: the CG recurrence (x, r, p, q, the dot products) and the operator A p; TP: the
+    // preconditioner (its values, 1/diag and z).  TP = float under T = double keeps the FP64
+    // recurrence, and with it the FP64 iteration count, while the sweeps run on the FP32 pipes.
+    template <typename T, typename TP = T>
     struct ClusterPcgArgs
     {
         int n, nColors, numCh;
@@ -48,9 +51,12 @@ namespace nsf
         const int *rsO, *ciO;            // off-diagonal part
         const T * vO;
         const T * diag;                  // diagonal values
-        const T * invD;                  // their inverses
+        const TP * vOP;                  // off-diagonal values of the preconditioner sweeps (vO when TP = T)
+        const float2 * vODf;             // T = double, TP = float: vO as double-float pairs (A z)
+        const TP * invD;                 // inverses of the diagonal, in the preconditioner's type
         const T * b;
-        T *x, *r, *z, *p, *q;            // p holds two planes (ping-pong) of NCH * n
+        T *x, *r, *p, *q;
+        TP * z;
         SolverState * st;
         const int * skip;                // refinement: stop immediately when *skip != 0
     };
@@ -105,14 +111,16 @@ namespace nsf
 
     // acc[c] += sum over entries j of the row with col < limit:  a_j * (v0[c][col] + w * v1[c][col])
     // (v1 may be null).  Arithmetic in T; fixed-width predicated batches keep RB loads in flight.
-    template <typename T, int NCH, bool SMEM>
+    // The gathers are predicated on the column alone, so they issue together with the value loads.
+    template <typename T, typename V0, int NCH, bool SMEM>
     __device__ __forceinline__ void rowGather(const RowView<SMEM> & rv, int color, int jb, int je, int limit,
-                                              const T * vO, int n, const T * v0, const T * v1, const T * w,
+                                              const T * vO, int n, const V0 * v0, const T * v1, const T * w,
                                               const bool (&act)[NCH], T (&acc)[NCH])
     {
         for (int j0 = jb; j0 < je; j0 += RB)
         {
             int cols[RB];
+            bool use[RB];
             T vals[RB];
 #pragma unroll
             for (int t = 0; t < RB; t++)
@@ -120,7 +128,8 @@ namespace nsf
                 const int j = j0 + t;
                 const bool ok = j < je;
                 cols[t] = ok ? rv.col(j) : 0;
-                vals[t] = (ok && cols[t] < limit) ? ldg(vO + rv.gnz(color, j)) : (T)0;
+                use[t] = ok && cols[t] < limit;
+                vals[t] = use[t] ? ldg(vO + rv.gnz(color, j)) : (T)0;
             }
 #pragma unroll
             for (int c = 0; c < NCH; c++)
@@ -131,8 +140,8 @@ namespace nsf
                     for (int t = 0; t < RB; t++)
                     {
                         const size_t o = (size_t)c * n + cols[t];
-                        g[t] = vals[t] != (T)0 ? __ldcg(v0 + o) : (T)0;
-                        if (v1 && vals[t] != (T)0)
+                        g[t] = use[t] ? (T)__ldcg(v0 + o) : (T)0;
+                        if (v1 && use[t])
                             g[t] += w[c] * __ldcg(v1 + o);
                     }
 #pragma unroll
@@ -170,19 +179,20 @@ namespace nsf
     // rowGather for a row shared by LG lanes: lane k takes the entries jb + k, jb + k + LG, ... in
     // predicated batches of 4 (so a row of up to 4 * LG entries has all its loads in flight at
     // once); the caller sums acc over the group.
-    template <typename T, int NCH, bool SMEM, int LG>
+    template <typename T, typename V0, int NCH, bool SMEM, int LG>
     __device__ __forceinline__ void rowGatherLanes(const RowView<SMEM> & rv, int color, int jb, int je, int limit,
-                                                   const T * vO, int n, const T * v0, const T * v1, const T * w,
+                                                   const T * vO, int n, const V0 * v0, const T * v1, const T * w,
                                                    const bool (&act)[NCH], T (&acc)[NCH], int lane)
     {
         if constexpr (LG == 1)
-            rowGather<T, NCH, SMEM>(rv, color, jb, je, limit, vO, n, v0, v1, w, act, acc);
+            rowGather<T, V0, NCH, SMEM>(rv, color, jb, je, limit, vO, n, v0, v1, w, act, acc);
         else
         {
             constexpr int RBL = 4;
             for (int j0 = jb + lane; j0 < je; j0 += RBL * LG)
             {
                 int cols[RBL];
+                bool use[RBL];
                 T vals[RBL];
 #pragma unroll
                 for (int t = 0; t < RBL; t++)
@@ -190,7 +200,8 @@ namespace nsf
                     const int j = j0 + t * LG;
                     const bool ok = j < je;
                     cols[t] = ok ? rv.col(j) : 0;
-                    vals[t] = (ok && cols[t] < limit) ? ldg(vO + rv.gnz(color, j)) : (T)0;
+                    use[t] = ok && cols[t] < limit;
+                    vals[t] = use[t] ? ldg(vO + rv.gnz(color, j)) : (T)0;
                 }
 #pragma unroll
                 for (int c = 0; c < NCH; c++)
@@ -201,8 +212,8 @@ namespace nsf
                         for (int t = 0; t < RBL; t++)
                         {
                             const size_t o = (size_t)c * n + cols[t];
-                            g[t] = vals[t] != (T)0 ? __ldcg(v0 + o) : (T)0;
-                            if (v1 && vals[t] != (T)0)
+                            g[t] = use[t] ? (T)__ldcg(v0 + o) : (T)0;
+                            if (v1 && use[t])
                                 g[t] += w[c] * __ldcg(v1 + o);
                         }
 #pragma unroll
@@ -210,6 +221,48 @@ namespace nsf
                             acc[c] += vals[t] * g[t];
                     }
             }
+        }
+    }
+
+    // acc[c] += sum over the row's entries of a_j * v[c][col_j], a_j a double-float (hi, lo) and v
+    // FP32: each product is exact to ~2^-48 through two FMAs, the sums are TwoSum additions, so the
+    // result carries ~48 significant bits computed on the FP32 pipes.  LG lanes share a row as in
+    // rowGatherLanes.
+    template <int NCH, bool SMEM, int LG>
+    __device__ __forceinline__ void rowGatherDf(const RowView<SMEM> & rv, int color, int jb, int je,
+                                                const float2 * vDf, int n, const float * v, const bool (&act)[NCH],
+                                                float2 (&acc)[NCH], int lane)
+    {
+        constexpr int RBL = LG == 1 ? RB : 4;
+        for (int j0 = jb + (LG == 1 ? 0 : lane); j0 < je; j0 += RBL * LG)
+        {
+            int cols[RBL];
+            bool use[RBL];
+            float2 a[RBL];
+#pragma unroll
+            for (int t = 0; t < RBL; t++)
+            {
+                const int j = j0 + t * LG;
+                use[t] = j < je;
+                cols[t] = use[t] ? rv.col(j) : 0;
+                a[t] = use[t] ? __ldg(vDf + rv.gnz(color, j)) : make_float2(0.f, 0.f);
+            }
+#pragma unroll
+            for (int c = 0; c < NCH; c++)
+                if (act[c])
+                {
+                    float g[RBL];
+#pragma unroll
+                    for (int t = 0; t < RBL; t++)
+                        g[t] = use[t] ? __ldcg(v + (size_t)c * n + cols[t]) : 0.f;
+#pragma unroll
+                    for (int t = 0; t < RBL; t++)
+                    {
+                        const float pr = a[t].x * g[t];
+                        const float e = fmaf(a[t].y, g[t], fmaf(a[t].x, g[t], -pr));
+                        acc[c] = dfAdd(acc[c], make_float2(pr, e));
+                    }
+                }
         }
     }
 
@@ -418,8 +471,9 @@ namespace nsf
         double bb[NCH], rr[NCH], rz[NCH], rzPrev[NCH];
     };
 
-    template <typename T, int NCH, bool SMEM, typename Sync>
-    __global__ void __launch_bounds__(CTPB, 1) kPcgSweep(ClusterPcgArgs<T> A, Sync S)
+    // LG: lanes per row (0: 4 on the grid, 1 in a cluster); TP: the preconditioner's type.
+    template <typename T, int NCH, bool SMEM, typename Sync, int LG0 = 0, typename TP = T>
+    __global__ void __launch_bounds__(CTPB, 1) kPcgSweep(ClusterPcgArgs<T, TP> A, Sync S)
     {
         extern __shared__ int smemI[];
         __shared__ T slotS[2][8];
@@ -503,8 +557,11 @@ namespace nsf
         }
 
         // rows shared by LG lanes on the grid path (many short phases spread over every SM: one
-        // round of gathers per row); one thread per row in a cluster
-        constexpr int LG = std::is_same<Sync, GridSync<T>>::value ? 4 : 1;
+        // round of gathers per row); one thread per row in a cluster, and on the grid for systems
+        // whose colour phases give every thread several rows (more rows, so more loads, in flight)
+        constexpr int LG = LG0 > 0 ? LG0 : (std::is_same<Sync, GridSync<T>>::value ? 4 : 1);
+        // FP64 recurrence under an FP32 preconditioner: A z from the double-float values vODf
+        constexpr bool DFA = std::is_same<T, double>::value && std::is_same<TP, float>::value;
         const RowLanes<LG> RL;
 
         // ---- r = b - A x over own rows; ||b||^2
@@ -520,8 +577,8 @@ namespace nsf
 #pragma unroll
                 for (int c = 0; c < NCH; c++)
                     acc[c] = 0;
-                rowGatherLanes<T, NCH, SMEM, LG>(rv, col, rv.begin(col, l), rv.end(col, l), INT_MAX, A.vO, n, A.x,
-                                                 (const T *)nullptr, nullptr, act, acc, RL.lane);
+                rowGatherLanes<T, T, NCH, SMEM, LG>(rv, col, rv.begin(col, l), rv.end(col, l), INT_MAX, A.vO, n,
+                                                    (const T *)A.x, (const T *)nullptr, nullptr, act, acc, RL.lane);
 #pragma unroll
                 for (int c = 0; c < NCH; c++)
                     acc[c] = RL.sum(acc[c]);
@@ -569,27 +626,27 @@ namespace nsf
                             ri[c] = rvv;
                         }
                     }
-                    T acc[NCH];
+                    TP acc[NCH];
 #pragma unroll
                     for (int c = 0; c < NCH; c++)
                         acc[c] = 0;
-                    rowGatherLanes<T, NCH, SMEM, LG>(rv, col, jb, je, r0, A.vO, n, A.z, (const T *)nullptr, nullptr,
-                                                     act, acc, RL.lane);
+                    rowGatherLanes<TP, TP, NCH, SMEM, LG>(rv, col, jb, je, r0, A.vOP, n, (const TP *)A.z,
+                                                          (const TP *)nullptr, nullptr, act, acc, RL.lane);
 #pragma unroll
                     for (int c = 0; c < NCH; c++)
                         acc[c] = RL.sum(acc[c]);
                     if (RL.lane == 0)
                     {
-                        const T id = ldg(A.invD + i);
+                        const TP id = ldg(A.invD + i);
 #pragma unroll
                         for (int c = 0; c < NCH; c++)
                             if (act[c])
                             {
-                                const T zi = (ri[c] - acc[c]) * id;
+                                const TP zi = ((TP)ri[c] - acc[c]) * id;
                                 A.z[(size_t)c * n + i] = zi;
                                 rr[c] += ri[c] * ri[c];
                                 if (col == C - 1)
-                                    rz[c] += ri[c] * zi;
+                                    rz[c] += ri[c] * (T)zi;
                             }
                     }
                 }
@@ -601,27 +658,28 @@ namespace nsf
                 for (int l = chunkL[col] + RL.group; l < chunkL[col + 1]; l += RL.groups)
                 {
                     const int i = chunkA[col] + (l - chunkL[col]);
-                    T acc[NCH];
+                    TP acc[NCH];
 #pragma unroll
                     for (int c = 0; c < NCH; c++)
                         acc[c] = 0;
-                    rowGatherLanes<T, NCH, SMEM, LG>(rv, col, rv.begin(col, l), rv.end(col, l), INT_MAX, A.vO, n,
-                                                     A.z, (const T *)nullptr, nullptr, act, acc, RL.lane);
+                    rowGatherLanes<TP, TP, NCH, SMEM, LG>(rv, col, rv.begin(col, l), rv.end(col, l), INT_MAX, A.vOP,
+                                                          n, (const TP *)A.z, (const TP *)nullptr, nullptr, act, acc,
+                                                          RL.lane);
 #pragma unroll
                     for (int c = 0; c < NCH; c++)
                         acc[c] = RL.sum(acc[c]);
                     if (RL.lane != 0)
                         continue;
-                    const T id = ldg(A.invD + i);
+                    const TP id = ldg(A.invD + i);
 #pragma unroll
                     for (int c = 0; c < NCH; c++)
                         if (act[c])
                         {
                             const size_t o = (size_t)c * n + i;
                             const T rvv = A.r[o];
-                            const T zi = (rvv - acc[c]) * id;
+                            const TP zi = ((TP)rvv - acc[c]) * id;
                             A.z[o] = zi;
-                            rz[c] += rvv * zi;
+                            rz[c] += rvv * (T)zi;
                         }
                 }
                 if (col > 0)
@@ -671,9 +729,8 @@ namespace nsf
         {
             if (!sc.any)
                 break; // same value in every CTA
-            // direction: p_new = z + beta p_old ; q = A p_new ; p.q   (own rows of every color)
-            const T * pold = A.p + (size_t)((k - 1) & 1) * NCH * n;
-            T * pnew = A.p + (size_t)(k & 1) * NCH * n;
+            // direction: p = z + beta p ; q = A z + beta q (= A p, the previous q being A p_old) ; p.q
+            // over own rows of every color.  Only z is gathered, one product per entry.
             T beta[NCH], pq[NCH];
 #pragma unroll
             for (int c = 0; c < NCH; c++)
@@ -685,21 +742,26 @@ namespace nsf
                 for (int l = chunkL[col] + RL.group; l < chunkL[col + 1]; l += RL.groups)
                 {
                     const int i = chunkA[col] + (l - chunkL[col]);
-                    T pn[NCH], acc[NCH];
+                    T acc[NCH];
 #pragma unroll
                     for (int c = 0; c < NCH; c++)
-                    {
-                        pn[c] = (T)0;
                         acc[c] = (T)0;
-                        if (act[c] && RL.lane == 0)
-                        {
-                            const size_t o = (size_t)c * n + i;
-                            pn[c] = k == 1 ? A.z[o] : A.z[o] + beta[c] * pold[o];
-                        }
+                    if constexpr (DFA)
+                    {
+                        float2 accDf[NCH];
+#pragma unroll
+                        for (int c = 0; c < NCH; c++)
+                            accDf[c] = make_float2(0.f, 0.f);
+                        rowGatherDf<NCH, SMEM, LG>(rv, col, rv.begin(col, l), rv.end(col, l), A.vODf, n,
+                                                   (const float *)A.z, act, accDf, RL.lane);
+#pragma unroll
+                        for (int c = 0; c < NCH; c++)
+                            acc[c] = (T)accDf[c].x + (T)accDf[c].y;
                     }
-                    rowGatherLanes<T, NCH, SMEM, LG>(rv, col, rv.begin(col, l), rv.end(col, l), INT_MAX, A.vO, n,
-                                                     A.z, k == 1 ? (const T *)nullptr : pold, beta, act, acc,
-                                                     RL.lane);
+                    else
+                        rowGatherLanes<T, TP, NCH, SMEM, LG>(rv, col, rv.begin(col, l), rv.end(col, l), INT_MAX,
+                                                             A.vO, n, (const TP *)A.z, (const T *)nullptr, nullptr,
+                                                             act, acc, RL.lane);
 #pragma unroll
                     for (int c = 0; c < NCH; c++)
                         acc[c] = RL.sum(acc[c]);
@@ -711,10 +773,16 @@ namespace nsf
                             if (act[c])
                             {
                                 const size_t o = (size_t)c * n + i;
-                                const T qi = d * pn[c] + acc[c];
-                                pnew[o] = pn[c];
+                                const T zi = (T)A.z[o];
+                                T pn = zi, qi = d * zi + acc[c];
+                                if (k > 1)
+                                {
+                                    pn += beta[c] * A.p[o];
+                                    qi += beta[c] * A.q[o];
+                                }
+                                A.p[o] = pn;
                                 A.q[o] = qi;
-                                pq[c] += pn[c] * qi;
+                                pq[c] += pn * qi;
                             }
                     }
                 }
@@ -739,7 +807,7 @@ namespace nsf
                 act[c] = sc.act[c] != 0;
             }
             T rrN[NCH], rzN[NCH];
-            sgs(false, pnew, rrN, rzN);
+            sgs(false, A.p, rrN, rzN);
             T red2[2 * NCH];
 #pragma unroll
             for (int c = 0; c < NCH; c++)

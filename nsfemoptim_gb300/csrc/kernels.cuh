@@ -917,6 +917,15 @@ namespace nsf
         }
     }
 
+    // refinement: count the iterations of a preceding FP64 solve (the FP32-preconditioned form) as
+    // inner iterations of the solve
+    __global__ void kAddInnerIters(SolverState * st, const SolverState * solve, int numCh)
+    {
+        if (threadIdx.x == 0)
+            for (int c = 0; c < numCh && c < MAXCH; c++)
+                st->innerTotal[c] += solve->iters[c];
+    }
+
     template <int NCH>
     __device__ __forceinline__ bool anyAct(const bool (&a)[NCH])
     {

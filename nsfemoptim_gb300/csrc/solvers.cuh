@@ -172,6 +172,14 @@ namespace nsf
         // GRID: barrier control words and the per-CTA reduction slots
         DevBuf<unsigned> gridCtl;
         DevBuf<T> gridSlots;
+        // GRID: lanes per row, 4 for short colour phases (spread over every SM) or 1 when a phase
+        // gives every thread several rows (NSF_GRID_LANES=1|4 forces one)
+        int gridLanes = 4;
+        // FP32 preconditioner of an FP64 solve on the GRID / CLUSTER path (usePrecondF32): the
+        // sweeps run on the FP32 values of the same structure, z in FP32
+        const SweepSystem<float> * pre32 = nullptr;
+        DevBuf<float> z32;
+        DevBuf<float2> vODf; // the FP64 off-diagonal values as double-float pairs (A z on the FP32 pipes)
 
         bool setupDsmem(const SweepSystem<T> * s, bool allowVals, int form = -1)
         {
@@ -264,6 +272,72 @@ namespace nsf
             clusterSize = G;
             gridCtl.alloc(4);
             gridSlots.alloc((size_t)2 * 8 * G);
+            const int lanes = std::atoi(envStr("NSF_GRID_LANES", "0").c_str());
+            gridLanes = (lanes == 1 || lanes == 4) ? lanes
+                        : ((long long)s->n >= (long long)CTPB * G * std::max(1, s->nColors) ? 1 : 4);
+            if (!sweepKernelFits<T>(GRID))
+                gridLanes = 4;
+            return true;
+        }
+
+        // Calls f with the kPcgSweep instantiation that a solve with barrier policy Sync (CLUSTER:
+        // ClusterSync, GRID: GridSync) and the current setup launches, for a preconditioner of type TP.
+        template <typename TP, typename Sync, typename F>
+        void withSweepKernel(F && f) const
+        {
+            if constexpr (std::is_same<Sync, GridSync<T>>::value)
+                if (gridLanes == 1)
+                {
+                    if (clusterShared)
+                        f(kPcgSweep<T, NCH, true, Sync, 1, TP>);
+                    else
+                        f(kPcgSweep<T, NCH, false, Sync, 1, TP>);
+                    return;
+                }
+            if (clusterShared)
+                f(kPcgSweep<T, NCH, true, Sync, 0, TP>);
+            else
+                f(kPcgSweep<T, NCH, false, Sync, 0, TP>);
+        }
+
+        // Whether the kernel withSweepKernel<TP> picks can run as the current setup launches it;
+        // sets its shared-memory ceiling (and non-portable cluster size), which every instantiation
+        // needs before its first launch.
+        template <typename TP>
+        bool sweepKernelFits(int pth) const
+        {
+            bool ok = false;
+            const size_t smem = clusterShared ? clusterSmem : 0;
+            if (pth == GRID)
+                withSweepKernel<TP, GridSync<T>>([&](auto k) { ok = gridFits(k, smem); });
+            else
+                withSweepKernel<TP, ClusterSync<T>>([&](auto k) {
+                    ok = pickClusterSize(k, clusterSize == 16 ? smem : kClusterSmemCap + 1,
+                                         clusterSize == 8 ? smem : kClusterSmemCap + 1) == clusterSize;
+                });
+            return ok;
+        }
+
+        // Precondition this FP64 solve with the FP32 copy s32 of the system (same structure and
+        // numbering): the CG recurrence, A p and the dot products stay FP64, the SGS sweeps run in
+        // FP32.  Only on the GRID and CLUSTER paths; returns whether it took effect.
+        bool usePrecondF32(const SweepSystem<float> * s32)
+        {
+            if constexpr (!std::is_same<T, double>::value)
+                return false;
+            if ((path != GRID && path != CLUSTER) || s32->n != sys->n || s32->nColors != sys->nColors ||
+                !sweepKernelFits<float>(path))
+                return false;
+            pre32 = s32;
+            z32.alloc((size_t)NCH * sys->n);
+            const std::vector<T> v = sys->vO.download();
+            std::vector<float2> vd(v.size());
+            for (size_t k = 0; k < v.size(); k++)
+            {
+                const float hi = (float)v[k];
+                vd[k] = make_float2(hi, (float)((double)v[k] - (double)hi));
+            }
+            vODf.upload(vd);
             return true;
         }
 
@@ -424,8 +498,10 @@ namespace nsf
             }
             if (envFlag("NSF_VERBOSE"))
                 std::fprintf(stderr,
-                             "[nsf] PCG n=%d nnz=%d colors=%d path=%d ctas=%d shared=%d dsvals=%d form=%d smem=%zu\n", n,
-                             s->nnzFull, s->nColors, path, clusterSize, (int)clusterShared, dsVals, dsForm, clusterSmem);
+                             "[nsf] PCG n=%d nnz=%d colors=%d path=%d ctas=%d shared=%d dsvals=%d form=%d smem=%zu "
+                             "lanes=%d\n",
+                             n, s->nnzFull, s->nColors, path, clusterSize, (int)clusterShared, dsVals, dsForm,
+                             clusterSmem, path == GRID ? gridLanes : 1);
         }
 
         void sgs(cudaStream_t s, PcgPtrs PP, int init, T * x, bool tickLast)
@@ -481,48 +557,22 @@ namespace nsf
             }
             if (path == CLUSTER || path == GRID)
             {
-                ClusterPcgArgs<T> A{S.n, S.nColors, numCh, psDev.get(), S.rsO.get(), S.ciO.get(), S.vO.get(),
-                                    S.diag.get(), S.invD.get(), b, x, r.get(), z.get(), p.get(), q.get(), st.get(),
+                if constexpr (std::is_same<T, double>::value)
+                    if (pre32)
+                    {
+                        ClusterPcgArgs<T, float> A{S.n,         S.nColors,       numCh,       psDev.get(),
+                                                   S.rsO.get(), S.ciO.get(),     S.vO.get(),  S.diag.get(),
+                                                   pre32->vO.get(), vODf.get(),  pre32->invD.get(), b,
+                                                   x,           r.get(),         p.get(),     q.get(),
+                                                   z32.get(),   st.get(),        P.skip};
+                        launchSweep(s, A);
+                        return;
+                    }
+                ClusterPcgArgs<T> A{S.n,        S.nColors,    numCh,       psDev.get(), S.rsO.get(), S.ciO.get(),
+                                    S.vO.get(), S.diag.get(), S.vO.get(), nullptr,     S.invD.get(), b,
+                                    x,          r.get(),      p.get(),     q.get(),     z.get(),     st.get(),
                                     P.skip};
-                if (path == CLUSTER)
-                {
-                    const ClusterSync<T> cs{};
-                    if (clusterShared)
-                        launchCluster(kPcgSweep<T, NCH, true, ClusterSync<T>>, clusterSize, CTPB, clusterSmem, s, A,
-                                      cs);
-                    else
-                        launchCluster(kPcgSweep<T, NCH, false, ClusterSync<T>>, clusterSize, CTPB, 0, s, A, cs);
-                    return;
-                }
-                // barrier words start at zero for every solve (a solve that gave up waiting leaves
-                // them in an unknown state)
-                NSF_CUDA(cudaMemsetAsync(gridCtl.get(), 0, 4 * sizeof(unsigned), s));
-                GridSync<T> gs{};
-                gs.ctl = gridCtl.get();
-                gs.slots = gridSlots.get();
-                // NSF_GRID_SPIN_LIMIT: polls of one barrier wait before the solve gives up (default
-                // kGridSpinLimit, seconds).  NSF_GRID_TEST_QUIET_CTA="rank:after": test hook, CTA `rank`
-                // stops arriving at barriers after `after` of them, so the other CTAs' waits run out and
-                // the solve ends with status 5 (both read at each solve; an enqueue under stream
-                // capture fixes them for the graph).
-                const long long lim = std::atoll(envStr("NSF_GRID_SPIN_LIMIT", "0").c_str());
-                if (lim > 0)
-                    gs.spinLimit = (unsigned)std::min<long long>(lim, 0xFFFFFFFFll);
-                const std::string quiet = envStr("NSF_GRID_TEST_QUIET_CTA", "");
-                if (!quiet.empty())
-                {
-                    const size_t colon = quiet.find(':');
-                    gs.quietRank = std::atoi(quiet.substr(0, colon).c_str());
-                    gs.quietAfter =
-                        colon == std::string::npos ? 0u : (unsigned)std::atoi(quiet.substr(colon + 1).c_str());
-                    if (gs.quietRank < 1 || gs.quietRank >= clusterSize)
-                        throw Error(ST_INVALID, "NSF_GRID_TEST_QUIET_CTA: rank must be in 1.." +
-                                                    std::to_string(clusterSize - 1));
-                }
-                if (clusterShared)
-                    launchCooperative(kPcgSweep<T, NCH, true, GridSync<T>>, clusterSize, clusterSmem, s, A, gs);
-                else
-                    launchCooperative(kPcgSweep<T, NCH, false, GridSync<T>>, clusterSize, 0, s, A, gs);
+                launchSweep(s, A);
                 return;
             }
             NSF_LANES(S.L, NSF_LAUNCH((kPcgInit<T, LL, NCH>), S.fullBlocks(), s, P, S.rsF.get(), S.ciF.get(),
@@ -539,6 +589,46 @@ namespace nsf
                                                      q.get()));
                            sgs(bs, PP, 0, x, true);
                        });
+        }
+
+        // One persistent solve on the CLUSTER or GRID path (the preconditioner's type from A).
+        template <typename TP>
+        void launchSweep(cudaStream_t s, const ClusterPcgArgs<T, TP> & A)
+        {
+            const size_t smem = clusterShared ? clusterSmem : 0;
+            if (path == CLUSTER)
+            {
+                const ClusterSync<T> cs{};
+                withSweepKernel<TP, ClusterSync<T>>(
+                    [&](auto k) { launchCluster(k, clusterSize, CTPB, smem, s, A, cs); });
+                return;
+            }
+            // barrier words start at zero for every solve (a solve that gave up waiting leaves
+            // them in an unknown state)
+            NSF_CUDA(cudaMemsetAsync(gridCtl.get(), 0, 4 * sizeof(unsigned), s));
+            GridSync<T> gs{};
+            gs.ctl = gridCtl.get();
+            gs.slots = gridSlots.get();
+            // NSF_GRID_SPIN_LIMIT: polls of one barrier wait before the solve gives up (default
+            // kGridSpinLimit, seconds).  NSF_GRID_TEST_QUIET_CTA="rank:after": test hook, CTA `rank`
+            // stops arriving at barriers after `after` of them, so the other CTAs' waits run out and
+            // the solve ends with status 5 (both read at each solve; an enqueue under stream
+            // capture fixes them for the graph).
+            const long long lim = std::atoll(envStr("NSF_GRID_SPIN_LIMIT", "0").c_str());
+            if (lim > 0)
+                gs.spinLimit = (unsigned)std::min<long long>(lim, 0xFFFFFFFFll);
+            const std::string quiet = envStr("NSF_GRID_TEST_QUIET_CTA", "");
+            if (!quiet.empty())
+            {
+                const size_t colon = quiet.find(':');
+                gs.quietRank = std::atoi(quiet.substr(0, colon).c_str());
+                gs.quietAfter =
+                    colon == std::string::npos ? 0u : (unsigned)std::atoi(quiet.substr(colon + 1).c_str());
+                if (gs.quietRank < 1 || gs.quietRank >= clusterSize)
+                    throw Error(ST_INVALID, "NSF_GRID_TEST_QUIET_CTA: rank must be in 1.." +
+                                                std::to_string(clusterSize - 1));
+            }
+            withSweepKernel<TP, GridSync<T>>([&](auto k) { launchCooperative(k, clusterSize, smem, s, A, gs); });
         }
 
         int kernelsPerIteration() const { return 2 * sys->nColors; }
@@ -641,6 +731,14 @@ namespace nsf
         DevBuf<double> scratch;
         DevBuf<SolverState> st;
         PinnedBuf<int> flag{1};
+        // Systems too large for the cluster-resident residual replacement (one channel on the GRID
+        // or CLUSTER path): one CG with the FP64 recurrence and A p and the FP32 SGS preconditioner,
+        // followed by the FP64 residual test (and FP32 refinement passes if it stopped short).  FP32
+        // values in A p or FP32 vectors delay CG on ill-conditioned systems (1.5-2.9x the FP64
+        // iterations on the 1M-row P1 Laplacian family with residual replacement, 2x with restarted
+        // passes); an FP32 preconditioner alone does not.  NSF_MIXED_FORM=refine turns it off.
+        PcgSolver<double, NCH> pre32Solve;
+        bool pre32Form = false;
 
         void setup(const SweepSystem<double> * s64, const SweepSystem<float> * s32, int channels,
                    int expectIters = 100)
@@ -652,6 +750,14 @@ namespace nsf
             d32.alloc((size_t)NCH * s64->n);
             scratch.alloc((size_t)2 * MAXCH * cappedBlocks(1ll << 40));
             st.alloc(1);
+            pre32Form = false;
+            if constexpr (NCH == 1)
+                if (!inner.canReplace() && (inner.path == inner.GRID || inner.path == inner.CLUSTER) &&
+                    envStr("NSF_MIXED_FORM", "auto") != "refine")
+                {
+                    pre32Solve.setup(s64, channels, true, expectIters);
+                    pre32Form = pre32Solve.usePrecondF32(s32);
+                }
         }
 
         // Passes of: r = b - A x in FP64 (also the FP32 inner right-hand side) -> stop decision ->
@@ -679,6 +785,12 @@ namespace nsf
             }
             NSF_LAUNCH(kSetConfig, 1, s, sd, maxOuter, 0, tol * tol);
             NSF_LAUNCH(kOuterReset, 1, s, sd);
+            if constexpr (NCH == 1)
+                if (pre32Form)
+                {
+                    pre32Solve.enqueue(s, bodyStream, b, x, innerMaxIters, tol, false, checkInterval);
+                    NSF_LAUNCH(kAddInnerIters, 1, s, sd, (const SolverState *)pre32Solve.st.get(), numCh);
+                }
             inner.P.skip = &sd->skip;
             for (int pass = 0; pass <= maxOuter; pass++)
             {

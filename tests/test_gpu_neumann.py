@@ -78,3 +78,54 @@ def test_neumann_rejects_bad_pin(torch_cuda, laplacian):
     K, host, b, bp, xo = laplacian
     with pytest.raises(G.NsfError):
         G.NeumannSolver(host, pin=host.rows)
+
+
+@pytest.fixture(scope="module")
+def laplacian_256():
+    """P1 Laplacian of a jittered 256 x 256-node unit square (seed 0), the config-3 family at 1/16 of
+    its size: condition number ~1e5 after pinning."""
+    import scipy.sparse as sp
+
+    from nsfemoptim_gb300 import meshgen
+    from nsfemoptim_gb300.api import HostCsr
+    mesh = meshgen.jittered_square(256, seed=0, jitter=0.2)
+    rs, ci, val = meshgen.p1_stiffness(mesh.nodes, mesh.triangles)
+    K = sp.csr_matrix((val, ci, rs))
+    K.sort_indices()
+    n = K.shape[0]
+    host = HostCsr(n, n, K.indptr.astype(np.int32), K.indices.astype(np.int32), K.data.copy())
+    b = np.random.default_rng(0).standard_normal(n)
+    return K, host, b, b - b.mean()
+
+
+def test_mixed_grid_solve_keeps_fp64_iterations(torch_cuda, laplacian_256, monkeypatch):
+    """On the cooperative-grid path a mixed solve is one CG with the FP64 recurrence and A p under
+    the FP32 SGS preconditioner: it needs the FP64 solve's iterations (within 2% + 2) to the same
+    1e-10 on the FP64 residual, where restarted FP32 refinement passes (NSF_MIXED_FORM=refine) need
+    far more.  Both grid row layouts (4 lanes per row, one thread per row) give the same counts."""
+    import nsfemoptim_gb300 as G
+    t = torch_cuda
+    K, host, b, bp = laplacian_256
+    monkeypatch.setenv("NSF_PCG_PATH", "grid")
+    bd = t.tensor(b, device="cuda")
+    its = {}
+    for lanes in ("4", "1"):
+        monkeypatch.setenv("NSF_GRID_LANES", lanes)
+        for form in ("auto", "refine"):
+            monkeypatch.setenv("NSF_MIXED_FORM", form)
+            for name, prec in (("f64", G.NSF_PREC_F64), ("mixed", G.NSF_PREC_MIXED)):
+                if name == "f64" and form == "refine":
+                    continue
+                s = G.NeumannSolver(host, pin=0, precision=prec, max_iters=20000, target=1e-10)
+                xd = t.zeros(len(b), dtype=t.float64, device="cuda")
+                s.solve(bd, xd)
+                x = xd.cpu().numpy()
+                st = s.stats()
+                assert st["rel"] <= 1e-10, (lanes, form, name, st)
+                assert np.linalg.norm(K @ x - bp) <= 1e-9 * np.linalg.norm(bp)
+                its[(lanes, form, name)] = st["iters"]
+        f64, mixed = its[(lanes, "auto", "f64")], its[(lanes, "auto", "mixed")]
+        print(f"lanes {lanes}: FP64 {f64}, mixed {mixed}, refine {its[(lanes, 'refine', 'mixed')]}")
+        assert mixed <= 1.02 * f64 + 2, its
+        assert its[(lanes, "refine", "mixed")] >= 1.2 * f64, its
+    assert abs(its[("4", "auto", "f64")] - its[("1", "auto", "f64")]) <= 2

@@ -180,12 +180,19 @@ def test_pcg_pressure_matches_oracle(setup, torch_cuda):
     assert np.linalg.norm(r) <= 1.01e-10 * np.linalg.norm(b)
 
 
-# "-classic": the cluster solve in the classical form (kPcgClusterDs) instead of Eisenstat's
+# "-classic": the cluster solve in the classical form (kPcgClusterDs) instead of Eisenstat's;
+# "-lanes1": the grid solve with one thread per row instead of 4 lanes
 PATH_CODES = {"dsmem": 1, "dsmem-novals": 1, "dsmem-classic": 1, "dsmem-novals-classic": 1, "grid": 2,
-              "grid-global": 2, "cluster": 3, "cluster-global": 3, "multikernel": 0}
+              "grid-global": 2, "grid-lanes1": 2, "grid-global-lanes1": 2, "cluster": 3, "cluster-global": 3,
+              "multikernel": 0}
 
 
 def _force_path(monkeypatch, path):
+    if path.endswith("-lanes1"):
+        monkeypatch.setenv("NSF_GRID_LANES", "1")
+        path = path[:-len("-lanes1")]
+    else:
+        monkeypatch.delenv("NSF_GRID_LANES", raising=False)
     if path.endswith("-classic"):
         monkeypatch.setenv("NSF_PCG_FORM", "classic")
         path = path[:-len("-classic")]
@@ -201,6 +208,8 @@ def _check_path(capfd, path):
     lines = [ln for ln in err.splitlines() if ln.startswith("[nsf] PCG")]
     assert lines, err
     assert f"path={PATH_CODES[path]} " in lines[0], lines
+    if path.startswith("grid"):
+        assert ("lanes=1" if path.endswith("-lanes1") else "lanes=4") in lines[0], lines
     if path.startswith("dsmem"):
         assert ("form=0" if path.endswith("-classic") else "form=1") in lines[0], lines
 
@@ -296,17 +305,24 @@ def test_gs_solver_matches_oracle(setup, torch_cuda):
     assert max(s.getLastMse(0), s.getLastMse(1)) < target
 
 
-@pytest.mark.parametrize("path", ["dsmem", "dsmem-classic", "dsmem-restart", "grid", "cluster", "multikernel"])
+@pytest.mark.parametrize("path", ["dsmem", "dsmem-classic", "dsmem-restart", "grid", "grid-refine", "grid-lanes1",
+                                  "cluster", "cluster-refine", "multikernel"])
 def test_mixed_pcg_reaches_fp64_tolerance(setup, torch_cuda, path, monkeypatch, capfd):
     """FP32 inner CG + FP64 correction reaches the FP64 tolerance on the true residual: with FP64
-    residual replacement inside the cluster solve (dsmem) and with restarted refinement passes."""
+    residual replacement inside the cluster solve (dsmem), with one FP64-recurrence CG under the
+    FP32 preconditioner (grid, cluster) and with restarted refinement passes (dsmem-restart,
+    *-refine, multikernel)."""
     G, O, mesh, ctx, om, oc = setup
     t = torch_cuda
+    monkeypatch.delenv("NSF_MIXED_FORM", raising=False)
     if path == "dsmem-restart":
         monkeypatch.setenv("NSF_NO_RU", "1")
         path = "dsmem"
     else:
         monkeypatch.delenv("NSF_NO_RU", raising=False)
+    if path.endswith("-refine"):
+        monkeypatch.setenv("NSF_MIXED_FORM", "refine")
+        path = path[:-len("-refine")]
     _force_path(monkeypatch, path)
     capfd.readouterr()
     kpi = ctx.matrix("Kpi")
