@@ -52,7 +52,8 @@ namespace nsf
         const T * vO;
         const T * diag;                  // diagonal values
         const TP * vOP;                  // off-diagonal values of the preconditioner sweeps (vO when TP = T)
-        const float2 * vODf;             // T = double, TP = float: vO as double-float pairs (A z)
+        const float * vOLo;              // T = double, TP = float: vO - vOP, so that (vOP, vOLo) is vO as a
+                                         // double-float pair (A z on the FP32 pipes)
         const TP * invD;                 // inverses of the diagonal, in the preconditioner's type
         const T * b;
         T *x, *r, *p, *q;
@@ -224,14 +225,14 @@ namespace nsf
         }
     }
 
-    // acc[c] += sum over the row's entries of a_j * v[c][col_j], a_j a double-float (hi, lo) and v
-    // FP32: each product is exact to ~2^-48 through two FMAs, the sums are TwoSum additions, so the
+    // acc[c] += sum over the row's entries of a_j * v[c][col_j], a_j the double-float (vHi, vLo) and
+    // v FP32: each product is exact to ~2^-48 through two FMAs, the sums are TwoSum additions, so the
     // result carries ~48 significant bits computed on the FP32 pipes.  LG lanes share a row as in
     // rowGatherLanes.
     template <int NCH, bool SMEM, int LG>
     __device__ __forceinline__ void rowGatherDf(const RowView<SMEM> & rv, int color, int jb, int je,
-                                                const float2 * vDf, int n, const float * v, const bool (&act)[NCH],
-                                                float2 (&acc)[NCH], int lane)
+                                                const float * vHi, const float * vLo, int n, const float * v,
+                                                const bool (&act)[NCH], float2 (&acc)[NCH], int lane)
     {
         constexpr int RBL = LG == 1 ? RB : 4;
         for (int j0 = jb + (LG == 1 ? 0 : lane); j0 < je; j0 += RBL * LG)
@@ -245,7 +246,8 @@ namespace nsf
                 const int j = j0 + t * LG;
                 use[t] = j < je;
                 cols[t] = use[t] ? rv.col(j) : 0;
-                a[t] = use[t] ? __ldg(vDf + rv.gnz(color, j)) : make_float2(0.f, 0.f);
+                const int gj = rv.gnz(color, j);
+                a[t] = use[t] ? make_float2(__ldg(vHi + gj), __ldg(vLo + gj)) : make_float2(0.f, 0.f);
             }
 #pragma unroll
             for (int c = 0; c < NCH; c++)
@@ -560,7 +562,7 @@ namespace nsf
         // round of gathers per row); one thread per row in a cluster, and on the grid for systems
         // whose colour phases give every thread several rows (more rows, so more loads, in flight)
         constexpr int LG = LG0 > 0 ? LG0 : (std::is_same<Sync, GridSync<T>>::value ? 4 : 1);
-        // FP64 recurrence under an FP32 preconditioner: A z from the double-float values vODf
+        // FP64 recurrence under an FP32 preconditioner: A z from the double-float values (vOP, vOLo)
         constexpr bool DFA = std::is_same<T, double>::value && std::is_same<TP, float>::value;
         const RowLanes<LG> RL;
 
@@ -752,8 +754,9 @@ namespace nsf
 #pragma unroll
                         for (int c = 0; c < NCH; c++)
                             accDf[c] = make_float2(0.f, 0.f);
-                        rowGatherDf<NCH, SMEM, LG>(rv, col, rv.begin(col, l), rv.end(col, l), A.vODf, n,
-                                                   (const float *)A.z, act, accDf, RL.lane);
+                        rowGatherDf<NCH, SMEM, LG>(rv, col, rv.begin(col, l), rv.end(col, l),
+                                                   (const float *)A.vOP, A.vOLo, n, (const float *)A.z, act, accDf,
+                                                   RL.lane);
 #pragma unroll
                         for (int c = 0; c < NCH; c++)
                             acc[c] = (T)accDf[c].x + (T)accDf[c].y;

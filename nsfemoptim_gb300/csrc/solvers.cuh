@@ -179,7 +179,7 @@ namespace nsf
         // sweeps run on the FP32 values of the same structure, z in FP32
         const SweepSystem<float> * pre32 = nullptr;
         DevBuf<float> z32;
-        DevBuf<float2> vODf; // the FP64 off-diagonal values as double-float pairs (A z on the FP32 pipes)
+        DevBuf<float> vOLo; // FP64 off-diagonal values minus their FP32 copy: (FP32 copy, vOLo) is a double-float
 
         bool setupDsmem(const SweepSystem<T> * s, bool allowVals, int form = -1)
         {
@@ -328,16 +328,18 @@ namespace nsf
             if ((path != GRID && path != CLUSTER) || s32->n != sys->n || s32->nColors != sys->nColors ||
                 !sweepKernelFits<float>(path))
                 return false;
-            pre32 = s32;
-            z32.alloc((size_t)NCH * sys->n);
+            // the low parts against the FP32 values the sweeps read, so that the pair is the FP64
+            // value to ~48 bits and A z reads the high parts the preconditioner shares
             const std::vector<T> v = sys->vO.download();
-            std::vector<float2> vd(v.size());
+            const std::vector<float> hi = s32->vO.download();
+            if (hi.size() != v.size())
+                return false;
+            std::vector<float> lo(v.size());
             for (size_t k = 0; k < v.size(); k++)
-            {
-                const float hi = (float)v[k];
-                vd[k] = make_float2(hi, (float)((double)v[k] - (double)hi));
-            }
-            vODf.upload(vd);
+                lo[k] = (float)((double)v[k] - (double)hi[k]);
+            vOLo.upload(lo);
+            z32.alloc((size_t)NCH * sys->n);
+            pre32 = s32;
             return true;
         }
 
@@ -562,7 +564,7 @@ namespace nsf
                     {
                         ClusterPcgArgs<T, float> A{S.n,         S.nColors,       numCh,       psDev.get(),
                                                    S.rsO.get(), S.ciO.get(),     S.vO.get(),  S.diag.get(),
-                                                   pre32->vO.get(), vODf.get(),  pre32->invD.get(), b,
+                                                   pre32->vO.get(), vOLo.get(),  pre32->invD.get(), b,
                                                    x,           r.get(),         p.get(),     q.get(),
                                                    z32.get(),   st.get(),        P.skip};
                         launchSweep(s, A);
