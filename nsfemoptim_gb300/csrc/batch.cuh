@@ -25,24 +25,6 @@ namespace nsf
             y[off + i] = dfFromDouble(x[off + i]);
     }
 
-    __global__ void __launch_bounds__(TPB) kBDfToDouble(long long n, const float2 * __restrict__ x, double * __restrict__ y,
-                                                         long long stride)
-    {
-        const long long off = (long long)blockIdx.y * stride;
-        for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
-            y[off + i] = dfToDouble(x[off + i]);
-    }
-
-    __global__ void __launch_bounds__(TPB) kBChebStartDf(int n, const double * __restrict__ b,
-                                                          const float2 * __restrict__ invD, float2 invTheta,
-                                                          float2 * __restrict__ r, float2 * __restrict__ d,
-                                                          float2 * __restrict__ x, long long stride)
-    {
-        const long long off = (long long)blockIdx.y * stride;
-        for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
-            chebStartDfRow<2>(i, n, b + off, invD, invTheta, r + off, d + off, x + off);
-    }
-
     // u <- Dirichlet value / u - tau acc (vectors stride 2n, Dirichlet values stride n)
     __global__ void __launch_bounds__(TPB) kBUpdateVelocity(int n, double * __restrict__ u, const double * __restrict__ acc,
                                                              double tau, const unsigned char * __restrict__ isDir,
@@ -88,6 +70,17 @@ namespace nsf
     }
 
     // ---- operator kernels: 1-D grid of B x blocks, instance = blockIdx.x % B (instance fastest)
+    template <int L>
+    __global__ void __launch_bounds__(TPB) kBSpmmDf(int B, int rows, const int * __restrict__ rs, const int * __restrict__ ci,
+                                                     const float2 * __restrict__ v, long long sv,
+                                                     const float2 * __restrict__ X, long long sx,
+                                                     double * __restrict__ Y, long long sy)
+    {
+        const int q = (int)(blockIdx.x % (unsigned)B), blk = (int)(blockIdx.x / (unsigned)B);
+        const Group<L> g(blk, (int)(gridDim.x / (unsigned)B));
+        spmmDfRows<L, 2>(g, rows, rs, ci, v + q * sv, X + q * sx, rows, Y + q * sy, rows);
+    }
+
     __global__ void __launch_bounds__(TPB) kBFastConvSellDf(int B, int rows, int nSlices, const int * __restrict__ ss,
                                                              const int * __restrict__ perm, const int * __restrict__ ci,
                                                              const float * __restrict__ iv, const float2 * __restrict__ u,
@@ -100,28 +93,124 @@ namespace nsf
         fastConvSellDfSlice(slice, rows, nSlices, ss, perm, ci, iv, u + q * su, k, nu[q], a + q * sa);
     }
 
-    template <int L>
-    __global__ void __launch_bounds__(TPB) kBSpmmDf(int B, int rows, const int * __restrict__ rs, const int * __restrict__ ci,
-                                                     const float2 * __restrict__ v, long long sv,
-                                                     const float2 * __restrict__ X, long long sx,
-                                                     double * __restrict__ Y, long long sy)
+    // ---- the mass solves on instance-interleaved vectors: entry (c, i) of instance q at
+    // ((c n + i) B + q), so that the instances' values of one row are contiguous.  The right-hand
+    // sides and solutions stay instance-major ([B][2n]); 32 x 32 shared-memory tiles transpose them
+    // on the way in and out.
+
+    // r = b, d = D^-1 b / theta, x = 0 (chebStartDfRow per instance) from instance-major b
+    __global__ void __launch_bounds__(TPB) kBChebStartIl(int n, int B, const double * __restrict__ b,
+                                                         const float2 * __restrict__ invD, float2 invTheta,
+                                                         float2 * __restrict__ r, float2 * __restrict__ d,
+                                                         float2 * __restrict__ x)
     {
-        const int q = (int)(blockIdx.x % (unsigned)B), blk = (int)(blockIdx.x / (unsigned)B);
-        const Group<L> g(blk, (int)(gridDim.x / (unsigned)B));
-        spmmDfRows<L, 2>(g, rows, rs, ci, v + q * sv, X + q * sx, rows, Y + q * sy, rows);
+        __shared__ double tile[32][33];
+        const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5, ny = TPB / 32;
+        const long long len = 2ll * n, e0 = (long long)blockIdx.x * 32;
+        const int q0 = blockIdx.y * 32;
+        for (int qq = ty; qq < 32; qq += ny)
+        {
+            const int q = q0 + qq;
+            const long long e = e0 + tx;
+            tile[qq][tx] = (q < B && e < len) ? b[(long long)q * len + e] : 0.0;
+        }
+        __syncthreads();
+        for (int ee = ty; ee < 32; ee += ny)
+        {
+            const long long e = e0 + ee;
+            const int q = q0 + tx;
+            if (e < len && q < B)
+            {
+                const float2 id = invD[(int)(e % n)];
+                const float2 bi = dfFromDouble(tile[tx][ee]);
+                const long long o = e * B + q;
+                r[o] = bi;
+                d[o] = dfMul(dfMul(bi, id), invTheta);
+                x[o] = make_float2(0.f, 0.f);
+            }
+        }
     }
 
-    __global__ void __launch_bounds__(TPB) kBChebStepDf(int B, int n, int nSlices, const int * __restrict__ ss,
-                                                         const int * __restrict__ perm, const int * __restrict__ ci,
-                                                         const float2 * __restrict__ v, const float2 * __restrict__ invD,
-                                                         const float2 * __restrict__ d, float2 * __restrict__ dn,
-                                                         float2 * __restrict__ x, float2 * __restrict__ r, long long stride,
-                                                         float2 c1, float2 c2)
+    // y (instance-major FP64) = x (interleaved double-float)
+    __global__ void __launch_bounds__(TPB) kBDfToDoubleIl(int n, int B, const float2 * __restrict__ x,
+                                                          double * __restrict__ y)
     {
-        const int q = (int)(blockIdx.x % (unsigned)B), blk = (int)(blockIdx.x / (unsigned)B);
-        const int slice = (int)((blk * (unsigned)blockDim.x + threadIdx.x) >> 5);
-        const long long off = q * stride;
-        chebStepDfSlice<2>(slice, n, nSlices, ss, perm, ci, v, invD, d + off, dn + off, x + off, r + off, c1, c2);
+        __shared__ double tile[32][33];
+        const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5, ny = TPB / 32;
+        const long long len = 2ll * n, e0 = (long long)blockIdx.x * 32;
+        const int q0 = blockIdx.y * 32;
+        for (int ee = ty; ee < 32; ee += ny)
+        {
+            const long long e = e0 + ee;
+            const int q = q0 + tx;
+            tile[ee][tx] = (e < len && q < B) ? dfToDouble(x[e * B + q]) : 0.0;
+        }
+        __syncthreads();
+        for (int qq = ty; qq < 32; qq += ny)
+        {
+            const int q = q0 + qq;
+            const long long e = e0 + tx;
+            if (q < B && e < len)
+                y[(long long)q * len + e] = tile[tx][qq];
+        }
+    }
+
+    // One double-float Chebyshev step of instances q0 .. q0 + Bg - 1 (of B).  A warp takes
+    // R = 32 / Q consecutive rows of one SELL slice for Q instances (Q = 2^qLog, min(Bg, 32) rounded
+    // up to a power of two): the matrix entries are loaded once per row for Q instances and the
+    // gathers of neighbouring lanes read contiguous instance values.  Per instance the arithmetic and
+    // its order are chebStepDfSlice's, so the results are bitwise those of the single stepper's
+    // kernel.
+    __global__ void __launch_bounds__(TPB) kBChebStepIl(int B, int q0, int Bg, int qLog, int n, int nSlices,
+                                                        const int * __restrict__ ss, const int * __restrict__ perm,
+                                                        const int * __restrict__ ci, const float2 * __restrict__ v,
+                                                        const float2 * __restrict__ invD,
+                                                        const float2 * __restrict__ d, float2 * __restrict__ dn,
+                                                        float2 * __restrict__ x, float2 * __restrict__ r, float2 c1,
+                                                        float2 c2)
+    {
+        const int Q = 1 << qLog, R = SELL_C >> qLog;
+        const int groups = (Bg + Q - 1) >> qLog;
+        const long long warp = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
+        const int lane = threadIdx.x & 31;
+        const long long row = (warp / groups) * R + (lane >> qLog);
+        const int qg = (int)(warp % groups) * Q + (lane & (Q - 1)), q = q0 + qg;
+        if (row >= (long long)nSlices * SELL_C)
+            return; // whole warps: R divides the slice height
+        const int slice = (int)(row / SELL_C), l = (int)(row % SELL_C);
+        const int b0 = ldg(ss + slice), w = (ldg(ss + slice + 1) - b0) / SELL_C;
+        const bool act = qg < Bg && row < n;
+        // channel planes of the instance: entry j of channel c at dq[c][j B]
+        const float2 * dq0 = d + q;
+        const float2 * dq1 = d + (long long)n * B + q;
+        float2 acc[2] = {make_float2(0.f, 0.f), make_float2(0.f, 0.f)};
+#pragma unroll 4
+        for (int k = 0; k < w; k++)
+        {
+            const int e = b0 + k * SELL_C + l;
+            const int j = ldg(ci + e);
+            const float2 a = ldg(v + e);
+            if (act)
+            {
+                const long long o = (long long)j * B;
+                acc[0] = dfDotAdd(acc[0], a, ldg(dq0 + o));
+                acc[1] = dfDotAdd(acc[1], a, ldg(dq1 + o));
+            }
+        }
+        if (!act)
+            return;
+        const int i = ldg(perm + row);
+        const float2 id = ldg(invD + i);
+#pragma unroll
+        for (int c = 0; c < 2; c++)
+        {
+            const long long o = ((long long)c * n + i) * B + q;
+            const float2 di = d[o];
+            x[o] = dfAdd(x[o], di);
+            const float2 ri = dfAdd(r[o], dfNeg(dfDotEnd(acc[c])));
+            r[o] = ri;
+            dn[o] = dfAdd(dfMul(c1, di), dfMul(c2, dfMul(ri, id)));
+        }
     }
 
     template <typename TM, typename TX, typename TY, typename TA>
@@ -145,6 +234,9 @@ struct nsf_batch_s
 {
     nsf_chorin tpl = nullptr; // the shared operators, the solver set-up and the state maps
     int B = 0, N = 0, P = 0, nIntP = 0, chebK = 0;
+    // instances per group of the mass solves (NSF_BATCH_CHEB_GROUP; default: a power of two whose
+    // four Chebyshev vectors fill at most half of L2)
+    int chebGroup = 1;
     nsf_chorin_config cfg{};
     DevBuf<float2> nuDf;
     DevBuf<double> u, rhs, acc, rhsP, pInt, pPrev, dirVal, stage;
@@ -220,22 +312,36 @@ struct nsf_batch_s
         const long long stride = 2ll * N;
         const double theta = 0.5 * (kMassSpecHi + kMassSpecLo), delta = 0.5 * (kMassSpecHi - kMassSpecLo);
         const double sigma = theta / delta;
-        double rho = 1.0 / sigma;
-        NSF_LAUNCH(kBChebStartDf, batchGrid(N, B), s, N, b, (const float2 *)ch.invDDf.get(),
-                   ChebSolver::split(1.0 / theta), rDf.get(), d0.get(), xDf.get(), stride);
-        float2 * dc = d0.get();
-        float2 * dn = d1.get();
-        const int blocks = B * blocksFor((long long)sell.nSlices * SELL_C);
-        for (int it = 0; it < chebK; it++)
+        const dim3 tiles((unsigned)((stride + 31) / 32), (unsigned)((B + 31) / 32));
+        NSF_LAUNCH(kBChebStartIl, tiles, s, N, B, b, (const float2 *)ch.invDDf.get(),
+                   ChebSolver::split(1.0 / theta), rDf.get(), d0.get(), xDf.get());
+        // the instances in groups of chebGroup, each group's iterations run back to back so that its
+        // vectors stay in L2 between iterations
+        const int G = std::min(chebGroup, B);
+        int qLog = 0;
+        while ((1 << qLog) < std::min(G, 32))
+            qLog++;
+        for (int q0 = 0; q0 < B; q0 += G)
         {
-            const double rhoN = 1.0 / (2.0 * sigma - rho);
-            NSF_LAUNCH(kBChebStepDf, blocks, s, B, N, sell.nSlices, sell.ss.get(), sell.perm.get(), sell.ci.get(),
-                       (const float2 *)ch.vDf.get(), (const float2 *)ch.invDDf.get(), (const float2 *)dc, dn, xDf.get(),
-                       rDf.get(), stride, ChebSolver::split(rhoN * rho), ChebSolver::split(2.0 * rhoN / delta));
-            rho = rhoN;
-            std::swap(dc, dn);
+            const int Bg = std::min(G, B - q0);
+            const long long warps =
+                ((long long)sell.nSlices * SELL_C >> (5 - qLog)) * ((Bg + (1 << qLog) - 1) >> qLog);
+            const int blocks = (int)((warps * 32 + TPB - 1) / TPB);
+            float2 * dc = d0.get();
+            float2 * dn = d1.get();
+            double rh = 1.0 / sigma;
+            for (int it = 0; it < chebK; it++)
+            {
+                const double rhoN = 1.0 / (2.0 * sigma - rh);
+                NSF_LAUNCH(kBChebStepIl, blocks, s, B, q0, Bg, qLog, N, sell.nSlices, sell.ss.get(), sell.perm.get(),
+                           sell.ci.get(), (const float2 *)ch.vDf.get(), (const float2 *)ch.invDDf.get(),
+                           (const float2 *)dc, dn, xDf.get(), rDf.get(), ChebSolver::split(rhoN * rh),
+                           ChebSolver::split(2.0 * rhoN / delta));
+                rh = rhoN;
+                std::swap(dc, dn);
+            }
         }
-        NSF_LAUNCH(kBDfToDouble, batchGrid(stride, B), s, stride, (const float2 *)xDf.get(), x, stride);
+        NSF_LAUNCH(kBDfToDoubleIl, tiles, s, N, B, (const float2 *)xDf.get(), x);
     }
 
     template <bool VALS>
@@ -369,6 +475,18 @@ extern "C" int nsf_batch_create(nsf_context ctx, const nsf_chorin_config * cfg, 
         b->P = T.P;
         b->nIntP = T.nIntP;
         b->chebK = std::min(b->cfg.velMaxIters, T.chebT.itersFor(b->cfg.velTol));
+        {
+            int l2 = 0, dev = 0;
+            NSF_CUDA(cudaGetDevice(&dev));
+            NSF_CUDA(cudaDeviceGetAttribute(&l2, cudaDevAttrL2CacheSize, dev));
+            const long long perInst = 4ll * 2 * b->N * (long long)sizeof(float2);
+            long long g = std::max(1ll, (l2 / 2) / perInst);
+            int p2 = 1;
+            while (2ll * p2 <= g && p2 < 1024)
+                p2 *= 2;
+            const int want = std::atoi(envStr("NSF_BATCH_CHEB_GROUP", "0").c_str());
+            b->chebGroup = want > 0 ? want : p2;
+        }
         std::vector<float2> nd(B);
         for (int q = 0; q < B; q++)
             nd[q] = ChebSolver::split(nu[q]);

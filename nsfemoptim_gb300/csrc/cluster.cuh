@@ -226,9 +226,9 @@ namespace nsf
     }
 
     // acc[c] += sum over the row's entries of a_j * v[c][col_j], a_j the double-float (vHi, vLo) and
-    // v FP32: each product is exact to ~2^-48 through two FMAs, the sums are TwoSum additions, so the
-    // result carries ~48 significant bits computed on the FP32 pipes.  LG lanes share a row as in
-    // rowGatherLanes.
+    // v FP32, accumulated as Dot2 (dfDotAdd: exact FMA product residuals, TwoSum of the high parts,
+    // errors gathered in acc.y), so the result carries ~48 significant bits computed on the FP32
+    // pipes; the caller sums acc.x + acc.y in FP64.  LG lanes share a row as in rowGatherLanes.
     template <int NCH, bool SMEM, int LG>
     __device__ __forceinline__ void rowGatherDf(const RowView<SMEM> & rv, int color, int jb, int je,
                                                 const float * vHi, const float * vLo, int n, const float * v,
@@ -259,11 +259,7 @@ namespace nsf
                         g[t] = use[t] ? __ldcg(v + (size_t)c * n + cols[t]) : 0.f;
 #pragma unroll
                     for (int t = 0; t < RBL; t++)
-                    {
-                        const float pr = a[t].x * g[t];
-                        const float e = fmaf(a[t].y, g[t], fmaf(a[t].x, g[t], -pr));
-                        acc[c] = dfAdd(acc[c], make_float2(pr, e));
-                    }
+                        acc[c] = dfDotAdd(acc[c], a[t], make_float2(g[t], 0.f));
                 }
         }
     }
