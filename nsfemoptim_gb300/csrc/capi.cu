@@ -205,6 +205,8 @@ namespace nsf
         // double-float iterations (enableDoubleFloat): the SELL values, D^-1 and the vectors as
         // (hi, lo) float pairs, so the iterations run on the FP32 pipes at about 48-bit precision
         bool df = false;
+        // one warp per slice and channel (NSF_CHEB_SPLIT=0: one warp per slice for both channels)
+        bool splitChannels = true;
         DevBuf<float2> vDf, invDDf, xDf, rDf, dDf0, dDf1;
         DevBuf<int> kw; // warm solves: the device count and the per-channel warm flags
 
@@ -217,6 +219,7 @@ namespace nsf
         void enableDoubleFloat()
         {
             df = true;
+            splitChannels = numCh == 2 && envStr("NSF_CHEB_SPLIT", "1") != "0";
             const std::vector<double> hv = sell->v.download(), hd = sys->invD.download();
             std::vector<float2> sv(hv.size()), sd(hd.size());
             for (size_t i = 0; i < hv.size(); i++)
@@ -299,10 +302,16 @@ namespace nsf
                 for (int it = 0; it < k; it++)
                 {
                     const double rhoN = 1.0 / (2.0 * sigma - rho);
-                    NSF_LAUNCH((kChebStepDf<2>), sell->blocks(), s, n, sell->nSlices, sell->ss.get(),
-                               sell->perm.get(), sell->ci.get(), (const float2 *)vDf.get(),
-                               (const float2 *)invDDf.get(), (const float2 *)dc, dn, xDf.get(), rDf.get(),
-                               split(rhoN * rho), split(2.0 * rhoN / delta), kdev, it);
+                    if (splitChannels)
+                        NSF_LAUNCH(kChebStepDfSplit, 2 * sell->blocks(), s, n, sell->nSlices, sell->ss.get(),
+                                   sell->perm.get(), sell->ci.get(), (const float2 *)vDf.get(),
+                                   (const float2 *)invDDf.get(), (const float2 *)dc, dn, xDf.get(), rDf.get(),
+                                   split(rhoN * rho), split(2.0 * rhoN / delta), kdev, it);
+                    else
+                        NSF_LAUNCH((kChebStepDf<2>), sell->blocks(), s, n, sell->nSlices, sell->ss.get(),
+                                   sell->perm.get(), sell->ci.get(), (const float2 *)vDf.get(),
+                                   (const float2 *)invDDf.get(), (const float2 *)dc, dn, xDf.get(), rDf.get(),
+                                   split(rhoN * rho), split(2.0 * rhoN / delta), kdev, it);
                     rho = rhoN;
                     std::swap(dc, dn);
                 }

@@ -701,6 +701,23 @@ namespace nsf
         chebStepDfSlice<NCH>(slice, n, nSlices, ss, perm, ci, v, invD, d, dn, x, r, c1, c2);
     }
 
+    // The same step with one warp per slice and channel (warps 2s and 2s + 1 take the two channels of
+    // slice s, so they read the slice's entries through the same L1): twice the warps in flight for
+    // a latency-bound step; per channel the arithmetic and its order are kChebStepDf's.
+    __global__ void __launch_bounds__(TPB) kChebStepDfSplit(int n, int nSlices, const int * __restrict__ ss,
+                                                             const int * __restrict__ perm, const int * __restrict__ ci,
+                                                             const float2 * __restrict__ v, const float2 * __restrict__ invD,
+                                                             const float2 * __restrict__ d, float2 * __restrict__ dn,
+                                                             float2 * __restrict__ x, float2 * __restrict__ r, float2 c1,
+                                                             float2 c2, const int * kdev, int it)
+    {
+        const int w = (int)((blockIdx.x * (unsigned)blockDim.x + threadIdx.x) >> 5);
+        if (kdev && it >= *kdev)
+            return;
+        const size_t o = (size_t)(w & 1) * n;
+        chebStepDfSlice<1>(w >> 1, n, nSlices, ss, perm, ci, v, invD, d + o, dn + o, x + o, r + o, c1, c2);
+    }
+
     // y = (hi, lo) split of an FP64 vector
     __global__ void __launch_bounds__(TPB) kSplitDf(long long n, const double * __restrict__ x, float2 * __restrict__ y)
     {
