@@ -359,6 +359,58 @@ struct nsf_batch_s
         launchClusters(kPcgClusterEis<float, 1, VALS>, pcs, B, DTPB, play.bytes, s, A);
     }
 
+    // The instance group of the mass solves chosen by measurement (NSF_BATCH_CHEB_GROUP=tune, or
+    // NSF_PCG_PATH=tune): every power of two up to B is timed on a mass solve of the (zero)
+    // right-hand-side buffer, captured as a graph and replayed (two warm-ups, best of three), and the
+    // fastest kept.  The solve reads rhs and writes acc, which hold no state before the first step.
+    void tuneChebGroup()
+    {
+        const long long before = launchCounter().load();
+        int best = chebGroup;
+        double bestT = 1e30;
+        for (int g = 1;; g *= 2)
+        {
+            const int gg = std::min(g, B);
+            chebGroup = gg;
+            cudaGraph_t gr = nullptr;
+            cudaGraphExec_t ex = nullptr;
+            NSF_CUDA(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
+            massSolve(stream, rhs.get(), acc.get());
+            NSF_CUDA(cudaStreamEndCapture(stream, &gr));
+            NSF_CUDA(cudaGraphInstantiate(&ex, gr, 0));
+            cudaEvent_t e0, e1;
+            NSF_CUDA(cudaEventCreate(&e0));
+            NSF_CUDA(cudaEventCreate(&e1));
+            double t = 1e30;
+            for (int rep = 0; rep < 5; rep++)
+            {
+                NSF_CUDA(cudaEventRecord(e0, stream));
+                NSF_CUDA(cudaGraphLaunch(ex, stream));
+                NSF_CUDA(cudaEventRecord(e1, stream));
+                NSF_CUDA(cudaStreamSynchronize(stream));
+                float ms = 0;
+                NSF_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+                if (rep >= 2)
+                    t = std::min(t, (double)ms);
+            }
+            cudaEventDestroy(e0);
+            cudaEventDestroy(e1);
+            cudaGraphExecDestroy(ex);
+            cudaGraphDestroy(gr);
+            if (envFlag("NSF_VERBOSE"))
+                std::fprintf(stderr, "[nsf] batch tune: %d instances per mass-solve group: %.1f us\n", gg, 1e3 * t);
+            if (t < bestT)
+            {
+                bestT = t;
+                best = gg;
+            }
+            if (gg == B)
+                break;
+        }
+        chebGroup = best;
+        launchCounter().fetch_sub(launchCounter().load() - before); // trial kernels are not work
+    }
+
     void enqueueStep(cudaStream_t s)
     {
         nsf_chorin_s & T = *tpl;
@@ -532,6 +584,8 @@ extern "C" int nsf_batch_create(nsf_context ctx, const nsf_chorin_config * cfg, 
         b->stat = std::make_unique<PinnedBuf<SolverState>>(B);
         b->last.resize(B);
         NSF_CUDA(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking));
+        if (envStr("NSF_BATCH_CHEB_GROUP", "0") == "tune" || envStr("NSF_PCG_PATH", "auto") == "tune")
+            b->tuneChebGroup();
         NSF_CUDA(cudaDeviceSynchronize());
         *out = b.release();
     });

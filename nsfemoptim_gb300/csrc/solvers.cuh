@@ -346,7 +346,9 @@ namespace nsf
         // ---- autotuning (NSF_PCG_PATH=tune): every path that fits is timed and the fastest kept.
         // A candidate is a path and its variant (DSMEM: values in shared memory or not; CLUSTER /
         // GRID: row structure in shared memory or not).
-        bool applyCandidate(const SweepSystem<T> * s, int cpath, int variant)
+        // opt: DSMEM -- the form (1 Eisenstat's, 0 classical; -1 the default); GRID -- lanes per row
+        // (1 or 4; 0 the default rule).
+        bool applyCandidate(const SweepSystem<T> * s, int cpath, int variant, int opt = -1)
         {
             path = MULTI;
             clusterSize = 0;
@@ -356,11 +358,18 @@ namespace nsf
             dsForm = 0;
             bool ok = true;
             if (cpath == DSMEM)
-                ok = setupDsmem(s, variant != 0) && dsVals == variant;
+                ok = setupDsmem(s, variant != 0, opt) && dsVals == variant && (opt < 0 || dsForm == opt);
             else if (cpath == CLUSTER)
                 ok = setupCluster(s, variant != 0) && clusterShared == (variant != 0);
             else if (cpath == GRID)
+            {
                 ok = setupGrid(s, variant != 0) && clusterShared == (variant != 0);
+                if (ok && opt > 0)
+                {
+                    gridLanes = opt;
+                    ok = sweepKernelFits<T>(GRID);
+                }
+            }
             if (ok)
                 path = cpath;
             else
@@ -423,31 +432,39 @@ namespace nsf
             cudaStream_t st = nullptr, body = nullptr;
             NSF_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
             NSF_CUDA(cudaStreamCreateWithFlags(&body, cudaStreamNonBlocking));
-            const int cands[7][2] = {{DSMEM, 1}, {DSMEM, 0}, {CLUSTER, 1}, {CLUSTER, 0},
-                                     {GRID, 1},  {GRID, 0},  {MULTI, 0}};
-            int bestPath = MULTI, bestVar = 0;
+            // (path, variant, opt): the DSMEM cluster in both forms with or without cached values,
+            // the cluster and the grid with or without cached structure, the grid with 4 lanes or one
+            // thread per row, the multi-kernel path
+            const bool eisOk = s->nColors >= 2;
+            const int cands[11][3] = {{DSMEM, 1, 1},   {DSMEM, 0, 1}, {DSMEM, 1, 0}, {DSMEM, 0, 0},
+                                      {CLUSTER, 1, -1}, {CLUSTER, 0, -1}, {GRID, 1, 4}, {GRID, 1, 1},
+                                      {GRID, 0, 4},    {GRID, 0, 1},    {MULTI, 0, -1}};
+            int bestPath = MULTI, bestVar = 0, bestOpt = -1;
             double bestCost = 1e30;
             for (const auto & c : cands)
             {
-                if (!applyCandidate(s, c[0], c[1]))
+                if (c[0] == DSMEM && c[2] == 1 && !eisOk)
+                    continue;
+                if (!applyCandidate(s, c[0], c[1], c[2]))
                     continue;
                 const double t8 = trialSolve(8, b.get(), x.get(), st, body);
                 const double t24 = trialSolve(24, b.get(), x.get(), st, body);
                 const double per = std::max(0.0, (t24 - t8) / 16.0), fixed = std::max(0.0, t8 - 8.0 * per);
                 const double cost = fixed + expectIters * per;
                 if (envFlag("NSF_VERBOSE"))
-                    std::fprintf(stderr, "[nsf] tune n=%d path=%d variant=%d: %.2f us/iteration + %.1f us\n", n,
-                                 c[0], c[1], 1e6 * per, 1e6 * fixed);
+                    std::fprintf(stderr, "[nsf] tune n=%d path=%d variant=%d opt=%d: %.2f us/iteration + %.1f us\n",
+                                 n, c[0], c[1], c[2], 1e6 * per, 1e6 * fixed);
                 if (cost < bestCost)
                 {
                     bestCost = cost;
                     bestPath = c[0];
                     bestVar = c[1];
+                    bestOpt = c[2];
                 }
             }
             cudaStreamDestroy(st);
             cudaStreamDestroy(body);
-            applyCandidate(s, bestPath, bestVar);
+            applyCandidate(s, bestPath, bestVar, bestOpt);
         }
 
         // expectIters: a typical iteration count of this system's solves (weighs the autotuner's

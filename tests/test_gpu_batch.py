@@ -119,3 +119,21 @@ def test_pack_of_batches_equals_batches_alone(ctx, channel_h01):
             ub, pb = b.state(q)
             assert np.array_equal(ua, ub) and np.array_equal(pa, pb), q
             assert b.stats(q)["status"] == 0
+
+
+def test_batch_mass_solve_groups_do_not_change_results(ctx, monkeypatch):
+    """The instances of the batched mass solves run in L2-sized groups (NSF_BATCH_CHEB_GROUP: a
+    size, or `tune` to time every power of two and keep the fastest); per instance the arithmetic
+    is the same whatever the grouping, so the states are bitwise those of the ungrouped batch."""
+    G, c = ctx
+    dir_vx = np.stack([c.dir_vx * s for s in SCALES])
+    out = {}
+    for group in ("3", "1", "2", "tune"):
+        monkeypatch.setenv("NSF_BATCH_CHEB_GROUP", group)
+        b = G.Batch(c, NUS, 1e-3, dir_vx=dir_vx, vel_tol=1e-10, pres_tol=1e-10, pressure_guess=2, pressure_basis=4)
+        b.step(3)
+        out[group] = [b.state(q) for q in range(3)]
+    for group in ("1", "2", "tune"):
+        for q in range(3):
+            assert np.array_equal(out[group][q][0], out["3"][q][0]), (group, q)
+            assert np.array_equal(out[group][q][1], out["3"][q][1]), (group, q)

@@ -244,7 +244,8 @@ def test_pcg_paths_match_oracle(setup, torch_cuda, path, monkeypatch, capfd):
 
 
 def test_pcg_autotuned_path_matches_oracle(setup, torch_cuda, monkeypatch, capfd):
-    """NSF_PCG_PATH=tune times every path that fits on trial solves and keeps the fastest; the
+    """NSF_PCG_PATH=tune times every path that fits on trial solves and keeps the fastest -- the
+    cluster solve in both forms, the grid with 4 lanes and with one thread per row among them; the
     solve on the chosen path matches the oracle as every path does, and the trial solves do not
     count as library kernel launches."""
     G, O, mesh, ctx, om, oc = setup
@@ -257,6 +258,9 @@ def test_pcg_autotuned_path_matches_oracle(setup, torch_cuda, monkeypatch, capfd
     assert G.kernel_launches() == before
     err = capfd.readouterr().err
     assert "[nsf] tune" in err and "[nsf] PCG" in err, err
+    for cand in ("path=1 variant=1 opt=1", "path=1 variant=1 opt=0", "path=2 variant=1 opt=4",
+                 "path=2 variant=1 opt=1"):
+        assert cand in err, (cand, err)
     b = np.random.default_rng(12).standard_normal(a.rows)
     s.getRhs().copy_(t.tensor(b))
     s.getSol().zero_()
