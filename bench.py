@@ -988,6 +988,31 @@ def bench_ours(args, rank, world, local_rank):
         st_f64 = f64.stats()
         u_m, p_m = mixed.state()
 
+        # ---- the literal FP32-inner split (NSF_PREC_MIXED_F32: FastConvection, A u, D u and G p with
+        # FP32 values, vectors and sums; FP32 PCG mass (Jacobi) and pressure solves inside FP64
+        # refinement / residual replacement) over the same steps from rest, compared with the FP64
+        # drop-in after them, beside the main line's split
+        f32v = None
+        if args.f32_variant:
+            u_f, p_f = f64.state()
+            v32 = G.ChorinStepper(ctx, NU, TAU, precision=G.NSF_PREC_MIXED_F32, vel_method=2, vel_max_iters=500,
+                                  vel_tol=VEL_TOL, pres_max_iters=5000, pres_tol=PRES_TOL, check_interval=8,
+                                  use_graph=True, max_outer=4, inner_tol=1e-5, pressure_guess=args.pressure_guess,
+                                  pressure_basis=args.pressure_basis)
+            t_v, _ = timed(v32, args.steps, args.warmup)
+            st_v = v32.stats()
+            u_v, p_v = v32.state()
+            del v32
+
+            def rel(a, b):
+                return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+
+            f32v = {"steps_per_s": round(world * args.steps / t_v, 3), "ms_per_step": round(1e3 * t_v / args.steps, 4),
+                    "stats": st_v, "mass_solve": MASS_SOLVES[2],
+                    "after_steps": args.warmup + args.steps,
+                    "u_rel_l2_vs_fp64": rel(u_v, u_f), "p_rel_l2_vs_fp64": rel(p_v, p_f),
+                    "main_line_u_rel_l2_vs_fp64": rel(u_m, u_f), "main_line_p_rel_l2_vs_fp64": rel(p_m, p_f)}
+
         # ---- steady-state window: both steppers continue to step --steady-from, then --steady-steps
         # more steps are timed each (the early steps from rest need hundreds of pressure iterations,
         # the developed flow tens)
@@ -1120,7 +1145,7 @@ def bench_ours(args, rank, world, local_rank):
             "higher_is_better": True,
             "scaling": "weak",
             "vs_baseline": None,
-            "dtype": "f32-inner/f64-refine",
+            "dtype": "f32/df32-inner, f64-refine",
             "data": "synthetic (seeded DFG channel mesh, h=0.005)",
             "config": {"workload": "DFG channel h=0.005, Umax=1.5, nu=1e-3, tau=1e-4, P2/P1, "
                                    "pressure PCG-SGS to 1e-8 rel", "triangles": mesh.num_tri, "N": N, "P": P,
@@ -1156,7 +1181,12 @@ def bench_ours(args, rank, world, local_rank):
                                   "stats": st_f64},
                          "mixed_over_fp64": round(t_f64 / t_mixed, 3),
                          "mixed_stats": st_mixed,
-                         "steady": steady},
+                         "steady": steady,
+                         "mixed_f32_inner": f32v},
+            "precision_split": ("FP32 operator values and FP32 inner CG (pressure: FP64 residual replacement); "
+                                "FastConvection, A u and the Chebyshev mass solves in double-float (float pairs on "
+                                "the FP32 pipes, ~48 bits); D u and G p with FP64 sums; state, residuals and step "
+                                "lengths FP64. variants.mixed_f32_inner is the literal FP32-inner split"),
         }
         if accuracy is not None:
             line["accuracy"] = accuracy
@@ -1218,6 +1248,8 @@ def main():
     ap.add_argument("--pack-steps", type=int, default=20)
     ap.add_argument("--long-steps", type=int, default=10000, help="long workload: steps from rest")
     ap.add_argument("--poisson-reps", type=int, default=2)
+    ap.add_argument("--f32-variant", type=int, default=1,
+                    help="channel workload: also time the literal FP32-inner split (NSF_PREC_MIXED_F32)")
     ap.add_argument("--poisson-max-iters", type=int, default=20000,
                     help="poisson workload: iteration cap of each solve (a small cap gives short launches to profile)")
     ap.add_argument("--poisson-precisions", default="fp64,mixed", help="poisson workload: solves to run")

@@ -38,9 +38,15 @@ typedef enum
 {
     NSF_PREC_F64 = 0,   /* everything in FP64 */
     NSF_PREC_MIXED = 1, /* FP32 SpMV/sweeps/inner CG, FP64 residual refinement, dots and state */
-    NSF_PREC_F64_MIXEDSOLVE = 2 /* stepper only: FP64 operators and state (the FP64 step), every
-                                   solve FP32 CG inside FP64 refinement / residual replacement,
-                                   stopping on the same FP64 residual test as NSF_PREC_F64 */
+    NSF_PREC_F64_MIXEDSOLVE = 2, /* stepper only: FP64 operators and state (the FP64 step), every
+                                    solve FP32 CG inside FP64 refinement / residual replacement,
+                                    stopping on the same FP64 residual test as NSF_PREC_F64 */
+    NSF_PREC_MIXED_F32 = 3 /* stepper only: the literal FP32-inner split -- FastConvection, A u,
+                              D u and G p with FP32 values, vectors and sums; the mass and pressure
+                              solves FP32 PCG inside FP64 refinement / residual replacement
+                              (velMethod 1 or 2); state, residuals and dot-product accumulation of
+                              the step lengths in FP64.  NSF_PREC_MIXED keeps FP64-level sums
+                              (double-float, FP64) in the products that feed the divergence. */
 } nsf_precision;
 
 const char *nsf_last_error(void);

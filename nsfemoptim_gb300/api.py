@@ -22,8 +22,8 @@ import ctypes as C
 
 import numpy as np
 
-from ._lib import (NSF_F32, NSF_F64, NSF_PREC_F64, NSF_PREC_F64_MIXEDSOLVE, NSF_PREC_MIXED, ChorinConfig, NsfError,
-                   check, lib, vp)
+from ._lib import (NSF_F32, NSF_F64, NSF_PREC_F64, NSF_PREC_F64_MIXEDSOLVE, NSF_PREC_MIXED, NSF_PREC_MIXED_F32,
+                   ChorinConfig, NsfError, check, lib, vp)
 
 
 def _i32(a):
@@ -635,5 +635,5 @@ class Adjoint:
 __all__ = ["Mesh", "load_gmsh", "ChorinContext", "build_chorin_context", "coloring", "CsrF", "Spmv", "Spmm",
            "NeumannSolver", "Batch",
            "spmv", "spmm", "fastconv_apply", "fastconv_apply_df", "split_df", "AbstractSolver", "create_solver", "ChorinStepper", "kernel_launches",
-           "Forces", "Adjoint", "Pack", "NSF_F32", "NSF_F64", "NSF_PREC_F64", "NSF_PREC_MIXED", "NSF_PREC_F64_MIXEDSOLVE",
+           "Forces", "Adjoint", "Pack", "NSF_F32", "NSF_F64", "NSF_PREC_F64", "NSF_PREC_MIXED", "NSF_PREC_F64_MIXEDSOLVE", "NSF_PREC_MIXED_F32",
            "NsfError"]

@@ -1341,6 +1341,7 @@ struct nsf_chorin_s
 {
     nsf_chorin_config cfg{};
     bool mixed = false;      // FP32 operators and FP32-inner solves
+    bool f32ops = false;     // NSF_PREC_MIXED_F32: the step's products in plain FP32 (mixed is set too)
     bool mixedSolve = false; // FP64 operators, FP32-inner solves (NSF_PREC_F64_MIXEDSOLVE)
     int N = 0, P = 0, nIntP = 0;
     std::vector<int> permV, permP, intP;
@@ -1369,6 +1370,7 @@ struct nsf_chorin_s
     PcgSolver<double, 2> velT, velF;
     ChebSolver chebT, chebF; // velMethod 3 (FP64 Chebyshev-Jacobi on the SELL copy of M)
     DevBuf<float2> uDf, KDf, ADf; // mixed: u, K and A as double-floats
+    DevBuf<float> u32, K32, A32;  // f32ops: u, K and A in FP32
     DevBuf<double> accT, accF;    // velMethod 4: the last tentative and final mass-solve solutions
     DevSell<double> Msell;
     GsSolver<double, 2> gsT, gsF;
@@ -1443,7 +1445,19 @@ struct nsf_chorin_s
     void enqueueStep(cudaStream_t s)
     {
         // 1. A = nu K + I u (SELL copy of the FastConvection matrix) ;  rhs = A [ux uy]
-        if (mixed)
+        if (f32ops)
+        {
+            // the literal FP32 split: FP32 values, vectors and sums, the product rhs widened to FP64
+            const DevSell<float> & IS = I32.sell;
+            NSF_LAUNCH((kConvert<double, float>), blocksFor(2ll * N), s, 2ll * N, (const double *)u.get(), u32.get());
+            NSF_LAUNCH((kFastConvSell<float, float, float, float>), IS.blocks(), s, IS.rows, IS.nSlices, IS.ss.get(),
+                       IS.perm.get(), IS.ci.get(), IS.v.get(), (const float *)u32.get(), (const float *)K32.get(),
+                       cfg.nu, A32.get());
+            NSF_LANES(M32.L, NSF_LAUNCH((kSpmm<float, float, double, float, LL, 2>), blocksFor((long long)N * M32.L), s,
+                                        N, M32.rsF.get(), M32.ciF.get(), (const float *)A32.get(),
+                                        (const float *)u32.get(), N, rhs.get(), N));
+        }
+        else if (mixed)
         {
             const DevSell<float> & IS = I32.sell;
             // double-float (FP32 pipes, 48 bits) for the products that feed the divergence
@@ -1480,12 +1494,18 @@ struct nsf_chorin_s
             // FP32 values, FP64 sums: D u cancels heavily, and FP32 sums would leave rounding noise of
             // ~1e-5 of the result in rhsP that changes from step to step, which the pressure solve
             // then has to remove to its tolerance (no initial guess can predict it)
-            sellSpmv<double>(D32.sell, u.get(), rhsP.get(), invTau, 0.0, s);
+            if (f32ops)
+                sellSpmv<float>(D32.sell, u.get(), rhsP.get(), invTau, 0.0, s);
+            else
+                sellSpmv<double>(D32.sell, u.get(), rhsP.get(), invTau, 0.0, s);
             if (project)
                 proj.guess(s, rhsP.get(), pInt.get());
             mpres.enqueue(s, body, rhsP.get(), pInt.get(), cfg.maxOuter, cfg.presTol, cfg.presMaxIters, cfg.innerTol,
                           cfg.checkInterval);
-            sellSpmv<double>(G32.sell, pInt.get(), rhs.get(), 1.0, 0.0, s);
+            if (f32ops)
+                sellSpmv<float>(G32.sell, pInt.get(), rhs.get(), 1.0, 0.0, s);
+            else
+                sellSpmv<double>(G32.sell, pInt.get(), rhs.get(), 1.0, 0.0, s);
         }
         else
         {
@@ -1657,6 +1677,13 @@ static void buildChorin(nsf_chorin_s & S, const Context & c)
         S.KDf.upload(kdf);
         S.ADf.alloc(knu.size());
         S.uDf.alloc(2 * (size_t)N);
+        if (S.f32ops)
+        {
+            std::vector<float> k32(knu.begin(), knu.end());
+            S.K32.upload(k32);
+            S.A32.alloc(knu.size());
+            S.u32.alloc(2 * (size_t)N);
+        }
         if (!cheb)
         {
             S.mvelT.setup(&S.M64, &S.M32, 2, kMassIters);
@@ -1736,8 +1763,10 @@ extern "C" int nsf_chorin_create(nsf_context ctx, const nsf_chorin_config * cfg,
         require(ctx && cfg && out, "null argument");
         require(cfg->tau > 0 && cfg->nu >= 0, "tau must be > 0 and nu >= 0");
         require(cfg->precision == NSF_PREC_F64 || cfg->precision == NSF_PREC_MIXED ||
-                    cfg->precision == NSF_PREC_F64_MIXEDSOLVE,
+                    cfg->precision == NSF_PREC_F64_MIXEDSOLVE || cfg->precision == NSF_PREC_MIXED_F32,
                 "unknown precision");
+        require(!(cfg->precision == NSF_PREC_MIXED_F32 && cfg->velMethod != 1 && cfg->velMethod != 2),
+                "NSF_PREC_MIXED_F32 runs the mass solves as FP32 PCG: velMethod 1 or 2");
         require(!(cfg->precision == NSF_PREC_F64_MIXEDSOLVE && cfg->velMethod == 0),
                 "mixed solves use velMethod 1, 2 (pcg) or 3 (chebyshev)");
         require(cfg->velMethod >= 0 && cfg->velMethod <= 4,
@@ -1757,7 +1786,8 @@ extern "C" int nsf_chorin_create(nsf_context ctx, const nsf_chorin_config * cfg,
             S->cfg.maxOuter = 4;
         if (!(S->cfg.innerTol > 0))
             S->cfg.innerTol = 1e-4;
-        S->mixed = cfg->precision == NSF_PREC_MIXED;
+        S->mixed = cfg->precision == NSF_PREC_MIXED || cfg->precision == NSF_PREC_MIXED_F32;
+        S->f32ops = cfg->precision == NSF_PREC_MIXED_F32;
         S->mixedSolve = cfg->precision == NSF_PREC_F64_MIXEDSOLVE;
         buildChorin(*S, ctx->c);
         NSF_CUDA(cudaStreamCreateWithFlags(&S->stream, cudaStreamNonBlocking));
