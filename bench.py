@@ -1077,7 +1077,10 @@ def bench_ours(args, rank, world, local_rank):
         # values + column indices of I, row starts, u once, K read and A written (8-byte pairs)
         fc_bytes = nnzI * (4 + 4) + (rowsI + 1) * 4 + 2 * N * 8 + 2 * rowsI * 8
 
-        pcg_form = "classic" if os.environ.get("NSF_PCG_FORM") == "classic" else "eisenstat"
+        coarse = os.environ.get("NSF_PRES_COARSE", "1") != "0"
+        pcg_form = ("coarse" if coarse else
+                    "classic" if os.environ.get("NSF_PCG_FORM") == "classic" else "eisenstat")
+        xy_int = mesh.pressure_xy()[ctx.int_p]
         # ---- dominant kernel: the cluster-resident pressure PCG (FP32 inner solve of the
         # refinement).  Per-iteration time from two solves that differ only in the iteration cap
         # (same launches, same setup), each solve bracketed by CUDA events on its stream.
@@ -1087,6 +1090,8 @@ def bench_ours(args, rank, world, local_rank):
         pcg_t = {}
         for cap in (20, 80):
             s = G.create_solver("pcg", 1, Kpi, cap, 1e-30, 1000, precision=G.NSF_PREC_MIXED)
+            if coarse:  # the stepper's pressure solve: the two-level preconditioner on mesh cells
+                s.setCoarse(xy_int, int(os.environ.get("NSF_PRES_COARSE_ROWS", "240")))
             s.getRhs().copy_(bP)
             best = None
             for rep in range(4):
@@ -1104,12 +1109,14 @@ def bench_ours(args, rank, world, local_rank):
             del s
         t_it = (pcg_t[80][0] - pcg_t[20][0]) / max(1, pcg_t[80][1] - pcg_t[20][1])
         n_p, nnz_p = Kpi.rows, Kpi.nnz
-        if pcg_form == "classic":
+        if pcg_form in ("classic", "coarse"):
             # algorithmic bytes of one classical PCG iteration in FP32 (sv = si = 4): SpMV + two SGS
-            # sweeps + 7 vector passes, rows/nnz of the internal pressure system
+            # sweeps + 7 vector passes, rows/nnz of the internal pressure system; the coarse
+            # correction adds the restriction (r read), the corrected z (z read, z' written) and its
+            # gather in the SpMV (the coarse inverse lives in shared memory)
             spmv_b = nnz_p * 8 + (n_p + 1) * 4 + 2 * n_p * 4
             sweep_b = (nnz_p - n_p) * 8 + (n_p + 1) * 4 + 3 * n_p * 4 + n_p * 4
-            pcg_bytes = spmv_b + 2 * sweep_b + 7 * n_p * 4
+            pcg_bytes = spmv_b + 2 * sweep_b + 7 * n_p * 4 + (3 * n_p * 4 if pcg_form == "coarse" else 0)
         else:
             # Eisenstat's form: every off-diagonal entry once (backward sweep over the later-colour
             # entries, forward sweep over the earlier-colour ones), the row structure twice, 22
@@ -1160,10 +1167,11 @@ def bench_ours(args, rank, world, local_rank):
                             "the run's pressure-guess history kept), one graph-launched step, get_state "
                             "(u, p to pinned host memory)"},
             "gpu_launches": int(launches),
-            "roofline": {"bound": "hbm", "kernel": ("kPcgClusterDs<float,1> (pressure PCG-SGS, FP32, classical form)"
-                                                    if pcg_form == "classic" else
-                                                    "kPcgClusterEis<float,1> (pressure PCG-SGS, FP32, Eisenstat's form, "
-                                                    "one reduction per iteration)"),
+            "roofline": {"bound": "hbm", "kernel": {"classic": "kPcgClusterDs<float,1> (pressure PCG-SGS, FP32, classical form)",
+                                                    "coarse": "kPcgClusterDs<float,1,CO> (pressure PCG, FP32, multicolor SGS "
+                                                              "plus the coarse correction on mesh cells, classical form)",
+                                                    "eisenstat": "kPcgClusterEis<float,1> (pressure PCG-SGS, FP32, Eisenstat's "
+                                                                 "form, one reduction per iteration)"}[pcg_form],
                          "achieved": round(achieved_pcg, 1), "peak": hbm, "unit": "GB/s",
                          "frac": round(achieved_pcg / hbm, 4), "peak_kind": kind,
                          "algorithmic_bytes_per_iteration": pcg_bytes, "iteration_us": round(t_it * 1e6, 3),

@@ -212,6 +212,15 @@ int nsf_solver_create(const char *method, int numCh, int n, const int *rowStart,
 /* Solve A x = b for numCh planar channels; b and x are device FP64 vectors of numCh * n
    entries; x holds the initial guess on entry.  Synchronous: returns the solver status. */
 int nsf_solver_solve(nsf_solver s, const double *b, double *x, void *stream);
+/* Two-level preconditioner for a single-channel NSF_PREC_MIXED "pcg" solver: z = SGS(r) + P Ac^-1 P^T r
+   with P the piecewise-constant prolongation of aggregates of rows -- square cells of about
+   rowsPerAggregate rows of the coordinates xy (2 floats per row, the solver's row numbering), split by
+   the thread-block-cluster CTA that owns the rows -- and Ac = P^T A P inverted densely.  The solve
+   runs in the classical form of the cluster kernel; CG needs several times fewer iterations on
+   Poisson-type systems.  NSF_ERR_NOT_SUPPORTED when the cluster-resident path, at least 3 colours
+   or the shared memory are missing.  No counterpart in the reference (its pressure solve is GS or a
+   direct factorisation, cpp/libs/CudaUtils/src/solvers/solverFactory.cu:221-234). */
+int nsf_solver_set_coarse(nsf_solver s, const float *xy, int rowsPerAggregate);
 /* The same with FP32 device vectors (widened to FP64 around the FP64 solve inside the library):
    the IO vectors of the reference's cu::AbstractSolver are FP32 cu::vec (getRhs / getSol,
    cpp/libs/CudaUtils/include/cu/solvers/abstractSolver.h:8-32).  Synchronous. */

@@ -57,6 +57,13 @@ class Mesh:
         self.num_corner, self.num_tri, self.num_border, self.N, self.P, n_groups = list(c)
         self.groups = [lib().nsf_mesh_group(h, i).decode() for i in range(n_groups)]
 
+    def pressure_xy(self):
+        """(P, 2) coordinates of the P1 (pressure) nodes: the element corners, P2 nodes 0, 2, 4."""
+        v_elem, p_elem, v_xy, _ = self.arrays()
+        xy = np.zeros((self.P, 2), np.float32)
+        xy[p_elem.ravel()] = v_xy[v_elem[:, 0::2].ravel()]
+        return xy
+
     def arrays(self):
         T, B = self.num_tri, self.num_border
         v_elem = np.zeros(6 * T, np.int32)
@@ -290,6 +297,12 @@ class AbstractSolver:
 
     def getNumCh(self):
         return self.numCh
+
+    def setCoarse(self, xy, rows_per_aggregate: int = 240):
+        """Two-level preconditioner (nsf_solver_set_coarse): xy are the coordinates of the rows
+        ((rows, 2) array), the aggregates mesh cells of about rows_per_aggregate rows."""
+        xy = np.ascontiguousarray(xy, dtype=np.float32).reshape(-1)
+        check(lib().nsf_solver_set_coarse(self._h, _p(xy, C.c_float), int(rows_per_aggregate)))
 
     def getRhs(self):
         return self._rhs

@@ -511,7 +511,9 @@ extern "C" int nsf_batch_create(nsf_context ctx, const nsf_chorin_config * cfg, 
         auto b = std::make_unique<nsf_batch_s>();
         nsf_chorin_config c0 = *cfg;
         c0.nu = nu[0];
+        tlTemplateStepper = true;
         const int st = nsf_chorin_create(ctx, &c0, &b->tpl);
+        tlTemplateStepper = false;
         if (st != NSF_OK)
             throw Error(st, lastError);
         nsf_chorin_s & T = *b->tpl;

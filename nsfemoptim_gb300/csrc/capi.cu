@@ -1261,6 +1261,26 @@ struct nsf_neumann_s
     }
 };
 
+extern "C" int nsf_solver_set_coarse(nsf_solver s, const float * xy, int rowsPerAggregate)
+{
+    return guarded([&] {
+        require(s && xy, "null argument");
+        require(rowsPerAggregate >= 8, "rowsPerAggregate must be >= 8");
+        require(s->method == "pcg" && s->precision == NSF_PREC_MIXED && s->numCh == 1,
+                "the coarse correction is provided for single-channel mixed-precision \"pcg\" solvers");
+        // the solver's colour-permuted numbering: row r is input row col.perm[r]
+        std::vector<float> p(2 * (size_t)s->n);
+        for (int r = 0; r < s->n; r++)
+        {
+            p[2 * (size_t)r] = xy[2 * (size_t)s->col.perm[r]];
+            p[2 * (size_t)r + 1] = xy[2 * (size_t)s->col.perm[r] + 1];
+        }
+        if (!s->mix1.inner.enableCoarse(p, rowsPerAggregate))
+            throw Error(ST_NOTSUP, "the coarse correction needs the cluster-resident path, at least 3 colours and "
+                                   "room in the cluster's shared memory");
+    });
+}
+
 extern "C" int nsf_neumann_create(int n, const int * rowStart, const int * col, const double * values, int pin,
                                   int precision, int maxIters, double target, nsf_neumann * out)
 {
@@ -1336,6 +1356,10 @@ extern "C" int nsf_neumann_stats(nsf_neumann h, int * iters, double * rel)
 extern "C" void nsf_neumann_destroy(nsf_neumann h) { delete h; }
 
 // ============================================================================ Chorin stepper
+
+// set while a batch creates its template stepper (the batched pressure solves run their own
+// cluster kernel, with the template's single-level preconditioner layout)
+thread_local bool tlTemplateStepper = false;
 
 struct nsf_chorin_s
 {
@@ -1690,6 +1714,20 @@ static void buildChorin(nsf_chorin_s & S, const Context & c)
             S.mvelF.setup(&S.M64, &S.M32, 2, kMassIters);
         }
         S.mpres.setup(&S.Kpi64, &S.Kpi32, 1, kPresIters);
+        if (envStr("NSF_PRES_COARSE", "1") != "0" && !c.pXY.empty() && !tlTemplateStepper)
+        {
+            // two-level pressure preconditioner: aggregates are mesh cells of about
+            // NSF_PRES_COARSE_ROWS (240) internal pressure nodes, split by the CTA that owns the rows
+            const int per = std::max(8, std::atoi(envStr("NSF_PRES_COARSE_ROWS", "240").c_str()));
+            std::vector<float> xy(2 * (size_t)S.nIntP);
+            for (int r = 0; r < S.nIntP; r++)
+            {
+                const int node = c.intP[cp.perm[r]];
+                xy[2 * (size_t)r] = c.pXY[2 * (size_t)node];
+                xy[2 * (size_t)r + 1] = c.pXY[2 * (size_t)node + 1];
+            }
+            S.mpres.inner.enableCoarse(xy, per);
+        }
     }
     else
     {

@@ -49,12 +49,17 @@ namespace nsf
     {
         int stride;                     // elements per vector plane (largest CTA share, rounded up)
         unsigned offZ, offP, offX, offR, offQ, offInvD, offDiag, offRs, offAd, offV, bytes;
+        // coarse correction (nAgg > 0): the corrected z (ZF), the CTA's aggregate sums (COwn), every
+        // aggregate's sum (CAll), the CTA's coarse values (YOwn), its rows of the coarse inverse
+        // (Ainv, aggMax x nAgg) and each local row's aggregate within the CTA (AggL)
+        int nAgg, aggMax;
+        unsigned offZF, offCOwn, offCAll, offYOwn, offAinv, offAggL;
     };
 
     inline size_t dsAlign(size_t b) { return (b + 15) & ~(size_t)15; }
 
     // rows / off-diagonal entries of the largest CTA share; tsize = sizeof(T); vals: values cached too
-    inline DsLayout dsLayout(int rowsMax, int nzMax, int nch, int tsize, bool vals)
+    inline DsLayout dsLayout(int rowsMax, int nzMax, int nch, int tsize, bool vals, int nAgg = 0, int aggMax = 0)
     {
         DsLayout L{};
         L.stride = (rowsMax + 3) & ~3;
@@ -81,6 +86,23 @@ namespace nsf
         L.offV = (unsigned)o;
         if (vals)
             o += dsAlign((size_t)tsize * nzMax);
+        L.nAgg = nAgg;
+        L.aggMax = aggMax;
+        if (nAgg > 0)
+        {
+            L.offZF = (unsigned)o;
+            o += dsAlign(plane * nch);
+            L.offCOwn = (unsigned)o;
+            o += dsAlign((size_t)tsize * aggMax);
+            L.offCAll = (unsigned)o;
+            o += dsAlign((size_t)tsize * nAgg);
+            L.offYOwn = (unsigned)o;
+            o += dsAlign((size_t)tsize * aggMax);
+            L.offAinv = (unsigned)o;
+            o += dsAlign((size_t)tsize * aggMax * nAgg);
+            L.offAggL = (unsigned)o;
+            o += dsAlign((size_t)4 * rowsMax);
+        }
         L.bytes = (unsigned)o;
         return L;
     }
@@ -113,6 +135,15 @@ namespace nsf
         const double * vO64;
         const double * diag64;
         double * x64;
+        // coarse correction (kernel template CO): z = SGS(r) + P Ac^-1 P^T r over aggregates of
+        // rows owned by one CTA each; aggStart[rank] .. aggStart[rank + 1] are the CTA's aggregates,
+        // aggOfRow the aggregate of each row (permuted numbering), aggRowStart / aggRows each
+        // aggregate's local rows in its CTA, ainv the coarse inverse (nAgg x nAgg, row-major)
+        const int * aggStart;
+        const int * aggOfRow;
+        const int * aggRowStart;
+        const int * aggRows;
+        const T * ainv;
     };
 
     __device__ __forceinline__ unsigned dsMapa(unsigned localAddr, int rank)
@@ -304,7 +335,8 @@ namespace nsf
         double gsc[NCH], igsc[NCH];
     };
 
-    template <typename T, int NCH, bool VALS>
+    // CO: with the coarse correction of DsPcgArgs (NCH == 1, at least three colours)
+    template <typename T, int NCH, bool VALS, bool CO = false>
     __global__ void __launch_bounds__(DTPB, 1) kPcgClusterDs(DsPcgArgs<T> A)
     {
         extern __shared__ __align__(16) unsigned char dsm[];
@@ -369,6 +401,8 @@ namespace nsf
         const T * lv = reinterpret_cast<const T *>(dsm + L.offV);
         const unsigned zBase = (unsigned)__cvta_generic_to_shared(zs);
         const unsigned offX = L.offX - L.offZ, offP0 = L.offP - L.offZ;
+        // the direction phase gathers the corrected z when the coarse correction is on
+        const unsigned offZF = CO ? L.offZF - L.offZ : 0u;
         const int R = chunkL[C];
         for (int c = 0; c < C; c++)
         {
@@ -384,6 +418,8 @@ namespace nsf
                 lrs[l] = (unsigned)(jb - g0 + nb) | ((unsigned)(sp - jb) << 24);
                 invDs[l] = ldg(A.invD + i);
                 diags[l] = ldg(A.diag + i);
+                if (CO)
+                    reinterpret_cast<int *>(dsm + L.offAggL)[l] = ldg(A.aggOfRow + i) - ldg(A.aggStart + rank);
 #pragma unroll
                 for (int ch = 0; ch < NCH; ch++)
                     xs[ch * S + l] = (ch < numCh && !A.ru) ? A.x[(size_t)ch * n + i] : (T)0; // ru: increment
@@ -399,6 +435,19 @@ namespace nsf
         }
         if (threadIdx.x == 0)
             lrs[R] = (unsigned)nzBase[C];
+        // coarse correction: the CTA's rows of the coarse inverse into shared memory
+        const int nAgg = L.nAgg;
+        const int aggA0 = CO ? ldg(A.aggStart + rank) : 0;
+        const int nAggOwn = CO ? ldg(A.aggStart + rank + 1) - aggA0 : 0;
+        T * zfs = reinterpret_cast<T *>(dsm + L.offZF);
+        T * cOwn = reinterpret_cast<T *>(dsm + L.offCOwn);
+        T * cAll = reinterpret_cast<T *>(dsm + L.offCAll);
+        T * yOwn = reinterpret_cast<T *>(dsm + L.offYOwn);
+        T * ainvS = reinterpret_cast<T *>(dsm + L.offAinv);
+        const int * aggL = reinterpret_cast<const int *>(dsm + L.offAggL);
+        if (CO)
+            for (int t = threadIdx.x; t < nAggOwn * nAgg; t += DTPB)
+                ainvS[t] = ldg(A.ainv + (size_t)aggA0 * nAgg + t);
         cl.sync(); // every CTA's x and row structure in place
 
         bool act[NCH];
@@ -578,7 +627,7 @@ namespace nsf
                             const T zi = (ri[c] - acc[c]) * id;
                             zs[c * S + l] = zi;
                             rr[c] += ri[c] * ri[c];
-                            if (col == C - 1)
+                            if (!CO && col == C - 1)
                                 rz[c] += ri[c] * zi;
                         }
                 }
@@ -587,6 +636,58 @@ namespace nsf
             }
             for (int col = C - 2; col >= 0; col--)
             {
+                // plain ifs on CO here: the lambda's discarded if-constexpr branches were not reliably
+                // removed from the CO = false kernel
+                if (CO)
+                {
+                    if (col == C - 2)
+                    {
+                        // r is final on every own row: the CTA's aggregate sums P^T r, a warp per
+                        // aggregate in a fixed order, published by this phase's cluster barrier
+                        const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+                        for (int a = warp; a < nAggOwn; a += DTPB / 32)
+                        {
+                            const int r0 = ldg(A.aggRowStart + aggA0 + a), r1 = ldg(A.aggRowStart + aggA0 + a + 1);
+                            T sum = (T)0;
+                            for (int t = r0 + lane; t < r1; t += 32)
+                                sum += rsv[ldg(A.aggRows + t)];
+#pragma unroll
+                            for (int o = 16; o > 0; o >>= 1)
+                                sum += __shfl_xor_sync(FULL, sum, o);
+                            if (lane == 0)
+                                cOwn[a] = sum;
+                        }
+                    }
+                    if (col == 0)
+                    {
+                        // every aggregate's sum from its CTA, then the CTA's coarse values
+                        // y = Ac^-1 (P^T r) for its own aggregates
+                        const unsigned cBase = (unsigned)__cvta_generic_to_shared(cOwn);
+                        for (int g = threadIdx.x; g < nAgg; g += DTPB)
+                        {
+                            int rk = 0;
+                            while (rk + 1 < cs && ldg(A.aggStart + rk + 1) <= g)
+                                rk++;
+                            cAll[g] = dsLoad(dsMapa(cBase + (unsigned)(g - ldg(A.aggStart + rk)) * (unsigned)sizeof(T), rk),
+                                             (T)0);
+                        }
+                        __syncthreads();
+                        const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+                        for (int a = warp; a < nAggOwn; a += DTPB / 32)
+                        {
+                            const T * row = ainvS + (size_t)a * nAgg;
+                            T sum = (T)0;
+                            for (int g = lane; g < nAgg; g += 32)
+                                sum += row[g] * cAll[g];
+#pragma unroll
+                            for (int o = 16; o > 0; o >>= 1)
+                                sum += __shfl_xor_sync(FULL, sum, o);
+                            if (lane == 0)
+                                yOwn[a] = sum;
+                        }
+                        __syncthreads();
+                    }
+                }
                 const T * vOg = A.vO + (chunkG[col] - nzBase[col]);
                 for (int l = chunkL[col] + threadIdx.x; l < chunkL[col + 1]; l += DTPB)
                 {
@@ -605,9 +706,31 @@ namespace nsf
                             const T rv = rsv[o];
                             const T zi = (rv - acc[c]) * id;
                             zs[o] = zi;
-                            rz[c] += rv * zi;
+                            if (CO)
+                            {
+                                if (col == 0)
+                                {
+                                    const T zf = zi + yOwn[aggL[l]];
+                                    zfs[o] = zf;
+                                    rz[c] += rv * zf;
+                                }
+                            }
+                            else
+                                rz[c] += rv * zi;
                         }
                 }
+                if (CO && col == 0)
+                    // the corrected z of the rows of the later colours (their SGS z is final)
+                    for (int l = chunkL[1] + threadIdx.x; l < chunkL[C]; l += DTPB)
+#pragma unroll
+                        for (int c = 0; c < NCH; c++)
+                            if (act[c])
+                            {
+                                const int o = c * S + l;
+                                const T zf = zs[o] + yOwn[aggL[l]];
+                                zfs[o] = zf;
+                                rz[c] += rsv[o] * zf;
+                            }
                 if (col > 0)
                     cl.sync(); // the last phase's barrier is the reduction's
             }
@@ -682,13 +805,14 @@ namespace nsf
                     for (int c = 0; c < NCH; c++)
                     {
                         const int o = c * S + l;
-                        pn[c] = act[c] ? (k == 1 ? zs[o] : zs[o] + beta[c] * pold[o]) : (T)0;
+                        const T zo = CO ? zfs[o] : zs[o];
+                        pn[c] = act[c] ? (k == 1 ? zo : zo + beta[c] * pold[o]) : (T)0;
                         acc[c] = d * pn[c];
                     }
                     if (k == 1)
-                        dsGather<T, NCH, VALS, false>(lad, lv, vOg, jb, je, 0u, 0u, chBytes, beta, act, acc);
+                        dsGather<T, NCH, VALS, false>(lad, lv, vOg, jb, je, offZF, 0u, chBytes, beta, act, acc);
                     else
-                        dsGather<T, NCH, VALS, true>(lad, lv, vOg, jb, je, 0u, offPold, chBytes, beta, act, acc);
+                        dsGather<T, NCH, VALS, true>(lad, lv, vOg, jb, je, offZF, offPold, chBytes, beta, act, acc);
 #pragma unroll
                     for (int c = 0; c < NCH; c++)
                         if (act[c])

@@ -23,6 +23,7 @@
 #include <algorithm>
 #include <cmath>
 #include <functional>
+#include <limits>
 #include <numeric>
 #include <queue>
 #include <stdexcept>
@@ -475,6 +476,9 @@ namespace nsf
             c.dirPIds.push_back(d.id);
         c.intV = complementOf(N, c.dirIds);
         c.intP = complementOf(P, c.dirPIds);
+        // pressure node coordinates: the P1 nodes are the mesh corners (pElem holds corner ids)
+        if (m.cornerXY.size() == 2 * (size_t)P)
+            c.pXY = m.cornerXY;
 
         // incidence lists
         std::vector<int> vStart, vList, pStart, pList;

@@ -52,6 +52,7 @@ namespace nsf
         std::vector<double> dirVx;     // inflow values (float-rounded as the reference computes them)
         std::vector<int> dirPIds;      // Dirichlet pressure nodes (Right border)
         std::vector<int> intV, intP;   // complements
+        std::vector<float> pXY;        // 2 * P: pressure node coordinates (the mesh corners)
         HostCsr<double> M, K, Kp, Kpi, D, G, I;
     };
 

@@ -18,6 +18,7 @@
 
 #include <cmath>
 #include <functional>
+#include <unordered_map>
 
 namespace nsf
 {
@@ -568,10 +569,7 @@ namespace nsf
                                S.vO.get(),  cmapDev.get(), S.diag.get(), S.invD.get(), b,    x,
                                st.get(),    P.skip,       dsLay,   0,     0.0,         nullptr,     nullptr,
                                nullptr,     nullptr};
-                if (dsVals)
-                    launchCluster(kPcgClusterDs<T, NCH, true>, clusterSize, DTPB, dsLay.bytes, s, A);
-                else
-                    launchCluster(kPcgClusterDs<T, NCH, false>, clusterSize, DTPB, dsLay.bytes, s, A);
+                launchDs(s, A);
                 return;
             }
             if (path == CLUSTER || path == GRID)
@@ -679,10 +677,215 @@ namespace nsf
                            S.vO.get(),   cmapDev.get(), S.diag.get(),   S.invD.get(),   nullptr,     nullptr,
                            stOut,        nullptr,       dsLay,          1,              delta2,      b64,
                            s64.vO.get(), s64.diag.get(), x64};
+            launchDs(s, A);
+        }
+
+        // the classical DSMEM kernel, with the coarse correction when it is on
+        void launchDs(cudaStream_t s, DsPcgArgs<T> A)
+        {
+            if (coarse)
+            {
+                if constexpr (NCH == 1)
+                {
+                    A.aggStart = aggStartDev.get();
+                    A.aggOfRow = aggOfRowDev.get();
+                    A.aggRowStart = aggRowStartDev.get();
+                    A.aggRows = aggRowsDev.get();
+                    A.ainv = ainvDev.get();
+                    if (dsVals)
+                        launchCluster(kPcgClusterDs<T, NCH, true, true>, clusterSize, DTPB, dsLay.bytes, s, A);
+                    else
+                        launchCluster(kPcgClusterDs<T, NCH, false, true>, clusterSize, DTPB, dsLay.bytes, s, A);
+                }
+                return;
+            }
             if (dsVals)
                 launchCluster(kPcgClusterDs<T, NCH, true>, clusterSize, DTPB, dsLay.bytes, s, A);
             else
                 launchCluster(kPcgClusterDs<T, NCH, false>, clusterSize, DTPB, dsLay.bytes, s, A);
+        }
+
+        // ---- two-level preconditioner of the DSMEM solve (enableCoarse)
+        bool coarse = false;
+        DevBuf<int> aggStartDev, aggOfRowDev, aggRowStartDev, aggRowsDev;
+        DevBuf<T> ainvDev;
+
+        // z = SGS(r) + P Ac^-1 P^T r: P is the piecewise-constant prolongation of aggregates of rows
+        // -- rows with equal key owned by the same CTA (keys group rows that lie close together,
+        // e.g. cells of the mesh) -- and Ac = P^T A P, inverted densely in FP64 on the host.  On the
+        // DSMEM path in the classical form, for single-channel systems of at least 3 colours (the
+        // aggregate sums are formed in the first backward phase and read in the last, so no barrier
+        // is added); returns whether it took effect.  With the aggregates of a Poisson-type system at
+        // about 80 rows, CG needs several times fewer iterations (the smooth error components that
+        // SGS damps slowly are removed by the coarse solve).
+        // xy: coordinates of every row (2 per row, the solver's numbering); the aggregates are
+        // square cells of about `per` rows, split by CTA, doubled in size until the cluster's shared
+        // memory holds the layout
+        bool enableCoarse(const std::vector<float> & xy, int per)
+        {
+            if constexpr (NCH != 1)
+                return false;
+            const SweepSystem<T> & S = *sys;
+            const int n = S.n;
+            if (path != DSMEM || S.nColors < 3 || (int)xy.size() != 2 * n || n < 1)
+                return false;
+            float x0 = 1e30f, x1 = -1e30f, y0 = 1e30f, y1 = -1e30f;
+            for (int i = 0; i < n; i++)
+            {
+                x0 = std::min(x0, xy[2 * (size_t)i]);
+                x1 = std::max(x1, xy[2 * (size_t)i]);
+                y0 = std::min(y0, xy[2 * (size_t)i + 1]);
+                y1 = std::max(y1, xy[2 * (size_t)i + 1]);
+            }
+            for (int tries = 0; tries < 4; tries++, per *= 2)
+            {
+                const double cell = std::sqrt((double)(x1 - x0) * (double)(y1 - y0) * per / n);
+                if (!(cell > 0))
+                    return false;
+                std::vector<int> key(n);
+                for (int i = 0; i < n; i++)
+                    key[i] = (int)((xy[2 * (size_t)i] - x0) / cell) * 65536 + (int)((xy[2 * (size_t)i + 1] - y0) / cell);
+                if (enableCoarseKeys(key))
+                    return true;
+            }
+            return false;
+        }
+
+        bool enableCoarseKeys(const std::vector<int> & key)
+        {
+            const SweepSystem<T> & S = *sys;
+            const int n = S.n, C = S.nColors;
+            const std::vector<T> vO = S.vO.download(), dg = S.diag.download();
+            for (int cs : {16, 8})
+            {
+                DsShares D = dsShares(S.ps, S.hostRsO, S.hostCiO, cs);
+                if (!dsEncodable(D, S.hostRsO))
+                    continue;
+                // owner CTA, local row and aggregate of every row; aggregates numbered CTA by CTA
+                std::vector<int> aggOfRow(n), aggStart(cs + 1, 0), localOf(n);
+                std::vector<std::vector<int>> rowsOf;
+                int nAgg = 0, aggMax = 0;
+                for (int rk = 0; rk < cs; rk++)
+                {
+                    aggStart[rk] = nAgg;
+                    std::unordered_map<int, int> id;
+                    int l = 0;
+                    for (int c = 0; c < C; c++)
+                    {
+                        const int len = S.ps[c + 1] - S.ps[c];
+                        const int a0 = S.ps[c] + (int)(((long long)len * rk) / cs);
+                        const int a1 = S.ps[c] + (int)(((long long)len * (rk + 1)) / cs);
+                        for (int i = a0; i < a1; i++, l++)
+                        {
+                            auto it = id.find(key[i]);
+                            if (it == id.end())
+                            {
+                                it = id.emplace(key[i], nAgg++).first;
+                                rowsOf.emplace_back();
+                            }
+                            aggOfRow[i] = it->second;
+                            localOf[i] = l;
+                            rowsOf[it->second].push_back(l);
+                        }
+                    }
+                    aggMax = std::max(aggMax, nAgg - aggStart[rk]);
+                }
+                aggStart[cs] = nAgg;
+                DsLayout lay{};
+                int vals = -1;
+                for (int v = 1; v >= 0 && vals < 0; v--)
+                {
+                    lay = dsLayout(D.rowsMax, D.nzMax, NCH, (int)sizeof(T), v != 0, nAgg, aggMax);
+                    const bool fits = v ? clusterFits(kPcgClusterDs<T, NCH, true, true>, cs, lay.bytes)
+                                        : clusterFits(kPcgClusterDs<T, NCH, false, true>, cs, lay.bytes);
+                    if (fits)
+                        vals = v;
+                }
+                if (vals < 0)
+                    continue;
+                // Ac = P^T A P and its inverse (Cholesky, FP64)
+                std::vector<double> ac((size_t)nAgg * nAgg, 0.0);
+                for (int i = 0; i < n; i++)
+                {
+                    const int a = aggOfRow[i];
+                    ac[(size_t)a * nAgg + a] += (double)dg[i];
+                    for (int e = S.hostRsO[i]; e < S.hostRsO[i + 1]; e++)
+                        ac[(size_t)a * nAgg + aggOfRow[S.hostCiO[e]]] += (double)vO[e];
+                }
+                std::vector<double> inv;
+                if (!choleskyInverse(ac, nAgg, inv))
+                    return false;
+                std::vector<int> rowStart(nAgg + 1, 0), rows;
+                rows.reserve(n);
+                for (int a = 0; a < nAgg; a++)
+                {
+                    rowStart[a] = (int)rows.size();
+                    rows.insert(rows.end(), rowsOf[a].begin(), rowsOf[a].end());
+                }
+                rowStart[nAgg] = (int)rows.size();
+                std::vector<T> invT(inv.begin(), inv.end());
+                aggStartDev.upload(aggStart);
+                aggOfRowDev.upload(aggOfRow);
+                aggRowStartDev.upload(rowStart);
+                aggRowsDev.upload(rows);
+                ainvDev.upload(invT);
+                clusterSize = cs;
+                dsVals = vals;
+                dsForm = 0;
+                dsLay = lay;
+                clusterSmem = lay.bytes;
+                cmapDev.upload(D.cmap);
+                coarse = true;
+                if (envFlag("NSF_VERBOSE"))
+                    std::fprintf(stderr, "[nsf] PCG coarse correction: %d aggregates (at most %d per CTA), ctas=%d "
+                                 "dsvals=%d smem=%u\n", nAgg, aggMax, cs, vals, lay.bytes);
+                return true;
+            }
+            return false;
+        }
+
+        // inverse of the SPD matrix a (n x n, row-major) by Cholesky; false if not positive definite
+        static bool choleskyInverse(const std::vector<double> & a, int n, std::vector<double> & inv)
+        {
+            std::vector<double> L(a);
+            for (int j = 0; j < n; j++)
+            {
+                double d = L[(size_t)j * n + j];
+                for (int k = 0; k < j; k++)
+                    d -= L[(size_t)j * n + k] * L[(size_t)j * n + k];
+                if (!(d > 0))
+                    return false;
+                d = std::sqrt(d);
+                L[(size_t)j * n + j] = d;
+                for (int i = j + 1; i < n; i++)
+                {
+                    double v = L[(size_t)i * n + j];
+                    for (int k = 0; k < j; k++)
+                        v -= L[(size_t)i * n + k] * L[(size_t)j * n + k];
+                    L[(size_t)i * n + j] = v / d;
+                }
+            }
+            // inv = L^-T L^-1, column by column of the identity
+            inv.assign((size_t)n * n, 0.0);
+            std::vector<double> y(n);
+            for (int c = 0; c < n; c++)
+            {
+                for (int i = 0; i < n; i++)
+                {
+                    double v = i == c ? 1.0 : 0.0;
+                    for (int k = 0; k < i; k++)
+                        v -= L[(size_t)i * n + k] * y[k];
+                    y[i] = v / L[(size_t)i * n + i];
+                }
+                for (int i = n - 1; i >= 0; i--)
+                {
+                    double v = y[i];
+                    for (int k = i + 1; k < n; k++)
+                        v -= L[(size_t)k * n + i] * inv[(size_t)k * n + c];
+                    inv[(size_t)i * n + c] = v / L[(size_t)i * n + i];
+                }
+            }
+            return true;
         }
     };
 

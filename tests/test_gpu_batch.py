@@ -36,6 +36,7 @@ def ctx(torch_cuda, channel_coarse):
 def test_batch_equals_separate_steppers(ctx, guess, monkeypatch):
     G, c = ctx
     monkeypatch.setenv("NSF_BATCH_CLUSTER", "16")  # the cluster size of a single solve: the same reduction order
+    monkeypatch.setenv("NSF_PRES_COARSE", "0")  # the batch's pressure preconditioner: single-level SGS
     dir_vx = np.stack([c.dir_vx * s for s in SCALES])
     b = G.Batch(c, NUS, 1e-3, dir_vx=dir_vx, vel_tol=1e-10, pres_tol=1e-10, pressure_guess=guess, pressure_basis=4)
     b.step(5)
@@ -68,12 +69,14 @@ def test_batch_state_roundtrip(ctx):
         b.state(3)
 
 
-def test_batch_small_clusters_follow_steppers(ctx):
+def test_batch_small_clusters_follow_steppers(ctx, monkeypatch):
     """With the batch's own cluster size (smaller clusters, so that more instances' pressure solves
     run at once) only the summation order of the pressure CG's dot products changes: the states
     follow the separate steppers to the solver tolerance: 10x the measured relative differences
-    (u 2.6e-12, p 2.1e-9 with pressure solves to 1e-10)."""
+    (u 2.6e-12, p 2.1e-9 with pressure solves to 1e-10).  The steppers use the batch's single-level
+    pressure preconditioner."""
     G, c = ctx
+    monkeypatch.setenv("NSF_PRES_COARSE", "0")
     dir_vx = np.stack([c.dir_vx * s for s in SCALES])
     b = G.Batch(c, NUS, 1e-3, dir_vx=dir_vx, vel_tol=1e-10, pres_tol=1e-10, pressure_guess=2, pressure_basis=4)
     b.step(5)
