@@ -249,6 +249,10 @@ struct nsf_batch_s
     int pcs = 0, pvals = 0;
     EisLayout play{};
     DevBuf<int> pcmap, pps;
+    // two-level pressure preconditioner (as the single stepper's): the classical cluster kernel with
+    // the coarse correction, its layout and aggregates held by bpres (NSF_PRES_COARSE=0: off)
+    PcgSolver<float, 1> bpres;
+    bool bcoarse = false;
 
     // Cluster size of the batched pressure solves: NSF_BATCH_CLUSTER if set, else the smallest of
     // 4, 8, 16 CTAs whose per-CTA share stays within about 2,700 rows (one row per thread and
@@ -352,6 +356,23 @@ struct nsf_batch_s
         const double delta = std::atof(envStr("NSF_RU_DELTA", "0.1").c_str());
         NSF_LAUNCH(kBSetConfig, (B + 127) / 128, s, B, pst.get(),
                    cfg.presMaxIters * (cfg.maxOuter > 0 ? cfg.maxOuter : 1), 0, cfg.presTol * cfg.presTol);
+        if (bcoarse)
+        {
+            DsPcgArgs<float> A{S.n,          S.nColors,      1,          bpres.psDev.get(), S.rsO.get(),
+                               S.ciO.get(),  S.vO.get(),     bpres.cmapDev.get(), S.diag.get(), S.invD.get(),
+                               nullptr,      nullptr,        pst.get(),  nullptr,     bpres.dsLay,
+                               1,            delta * delta,  rhsP.get(), S64.vO.get(), S64.diag.get(),
+                               pInt.get(),   bpres.aggStartDev.get(), bpres.aggOfRowDev.get(),
+                               bpres.aggRowStartDev.get(), bpres.aggRowsDev.get(), bpres.ainvDev.get(),
+                               (long long)nIntP};
+            if (bpres.dsVals)
+                launchClusters(kPcgClusterDs<float, 1, true, true>, bpres.clusterSize, B, DTPB, bpres.dsLay.bytes, s,
+                               A);
+            else
+                launchClusters(kPcgClusterDs<float, 1, false, true>, bpres.clusterSize, B, DTPB, bpres.dsLay.bytes,
+                               s, A);
+            return;
+        }
         EisPcgArgs<float> A{S.n,          S.nColors,     1,              pps.get(),   S.rsO.get(),   S.ciO.get(),
                             S.vO.get(),   pcmap.get(),   S.diag.get(),   S.invD.get(), nullptr,       nullptr,
                             pst.get(),    nullptr,       play,           1,           delta * delta, rhsP.get(),
@@ -580,6 +601,23 @@ extern "C" int nsf_batch_create(nsf_context ctx, const nsf_chorin_config * cfg, 
         }
         b->pst.alloc(B);
         b->setupPressureClusters();
+        if (envStr("NSF_PRES_COARSE", "1") != "0" && !ctx->c.pXY.empty() && T.Kpi32.nColors >= 3)
+        {
+            // the coarse correction on mesh cells, with the batch's cluster size (the smallest of
+            // 4, 8, 16 that holds the layout, or NSF_BATCH_CLUSTER)
+            const int per = std::max(8, std::atoi(envStr("NSF_PRES_COARSE_ROWS", "240").c_str()));
+            std::vector<float> xy(2 * (size_t)T.nIntP);
+            for (int r = 0; r < T.nIntP; r++)
+            {
+                const int node = ctx->c.intP[T.permP[r]];
+                xy[2 * (size_t)r] = ctx->c.pXY[2 * (size_t)node];
+                xy[2 * (size_t)r + 1] = ctx->c.pXY[2 * (size_t)node + 1];
+            }
+            const int want = std::atoi(envStr("NSF_BATCH_CLUSTER", "0").c_str());
+            b->bpres.setup(&T.Kpi32, 1, true, 100);
+            b->bcoarse = b->bpres.path == PcgSolver<float, 1>::DSMEM &&
+                         b->bpres.enableCoarse(xy, per, want > 0 ? std::vector<int>{want} : std::vector<int>{4, 8, 16});
+        }
         if (b->cfg.pressureGuess == 2)
             b->proj.setup(&T.Kpi64, b->cfg.pressureBasis > 0 ? b->cfg.pressureBasis : 250, B);
         b->stage.alloc(2 * (size_t)N + T.P);

@@ -144,6 +144,9 @@ namespace nsf
         const int * aggRowStart;
         const int * aggRows;
         const T * ainv;
+        // batched instances (one cluster each, launchClusters): the system of instance q, its
+        // vectors (b, x, b64, x64) at q * instStride and its state at st + q
+        long long instStride;
     };
 
     __device__ __forceinline__ unsigned dsMapa(unsigned localAddr, int rank)
@@ -337,11 +340,21 @@ namespace nsf
 
     // CO: with the coarse correction of DsPcgArgs (NCH == 1, at least three colours)
     template <typename T, int NCH, bool VALS, bool CO = false>
-    __global__ void __launch_bounds__(DTPB, 1) kPcgClusterDs(DsPcgArgs<T> A)
+    __global__ void __launch_bounds__(DTPB, 1) kPcgClusterDs(DsPcgArgs<T> Ain)
     {
         extern __shared__ __align__(16) unsigned char dsm[];
         cg::cluster_group cl = cg::this_cluster();
         const int rank = (int)cl.block_rank(), cs = (int)cl.num_blocks();
+        DsPcgArgs<T> A = Ain;
+        if (A.instStride)
+        {
+            const long long inst = (long long)(blockIdx.x / (unsigned)cs), off = inst * A.instStride;
+            A.b = A.b ? A.b + off : nullptr;
+            A.x = A.x ? A.x + off : nullptr;
+            A.b64 = A.b64 ? A.b64 + off : nullptr;
+            A.x64 = A.x64 ? A.x64 + off : nullptr;
+            A.st += inst;
+        }
         __shared__ T slot[2][8];
         __shared__ int chunkA[MAXCOLORS], chunkL[MAXCOLORS + 1], chunkG[MAXCOLORS], nzBase[MAXCOLORS + 1];
         __shared__ DsScalars<T, NCH> sc;

@@ -721,7 +721,7 @@ namespace nsf
         // xy: coordinates of every row (2 per row, the solver's numbering); the aggregates are
         // square cells of about `per` rows, split by CTA, doubled in size until the cluster's shared
         // memory holds the layout
-        bool enableCoarse(const std::vector<float> & xy, int per)
+        bool enableCoarse(const std::vector<float> & xy, int per, const std::vector<int> & sizes = {16, 8})
         {
             if constexpr (NCH != 1)
                 return false;
@@ -745,18 +745,18 @@ namespace nsf
                 std::vector<int> key(n);
                 for (int i = 0; i < n; i++)
                     key[i] = (int)((xy[2 * (size_t)i] - x0) / cell) * 65536 + (int)((xy[2 * (size_t)i + 1] - y0) / cell);
-                if (enableCoarseKeys(key))
+                if (enableCoarseKeys(key, sizes))
                     return true;
             }
             return false;
         }
 
-        bool enableCoarseKeys(const std::vector<int> & key)
+        bool enableCoarseKeys(const std::vector<int> & key, const std::vector<int> & sizes)
         {
             const SweepSystem<T> & S = *sys;
             const int n = S.n, C = S.nColors;
             const std::vector<T> vO = S.vO.download(), dg = S.diag.download();
-            for (int cs : {16, 8})
+            for (int cs : sizes)
             {
                 DsShares D = dsShares(S.ps, S.hostRsO, S.hostCiO, cs);
                 if (!dsEncodable(D, S.hostRsO))

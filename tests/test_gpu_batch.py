@@ -32,11 +32,14 @@ def ctx(torch_cuda, channel_coarse):
     return G, G.build_chorin_context(G.load_gmsh(channel_coarse), 1.2)
 
 
+@pytest.mark.parametrize("coarse", ["0", "1"])
 @pytest.mark.parametrize("guess", [0, 1, 2])
-def test_batch_equals_separate_steppers(ctx, guess, monkeypatch):
+def test_batch_equals_separate_steppers(ctx, guess, coarse, monkeypatch):
+    """coarse: the pressure preconditioner, SGS alone (Eisenstat's kernel) or SGS plus the coarse
+    correction (the classical kernel), the same in the batch and in the steppers."""
     G, c = ctx
     monkeypatch.setenv("NSF_BATCH_CLUSTER", "16")  # the cluster size of a single solve: the same reduction order
-    monkeypatch.setenv("NSF_PRES_COARSE", "0")  # the batch's pressure preconditioner: single-level SGS
+    monkeypatch.setenv("NSF_PRES_COARSE", coarse)
     dir_vx = np.stack([c.dir_vx * s for s in SCALES])
     b = G.Batch(c, NUS, 1e-3, dir_vx=dir_vx, vel_tol=1e-10, pres_tol=1e-10, pressure_guess=guess, pressure_basis=4)
     b.step(5)
