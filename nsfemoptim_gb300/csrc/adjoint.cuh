@@ -701,7 +701,10 @@ extern "C" int nsf_adjoint_create(nsf_chorin S, nsf_forces f, const nsf_adjoint_
         else
             a->mass.setup(&S->M64, 2);
         if (S->mixedSolve)
+        {
             a->mpres.setup(&S->Kpi64, &S->Kpi32, 1);
+            S->enablePresCoarse(a->mpres.inner);
+        }
         else
             a->pres.setup(&S->Kpi64, 1);
         for (cudaEvent_t & e : a->ev)

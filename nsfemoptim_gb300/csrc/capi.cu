@@ -1421,6 +1421,20 @@ struct nsf_chorin_s
     double stats[8] = {0};
 
     // whether a solve of this stepper runs on the whole-GPU cooperative grid
+    // internal pressure node coordinates in the solver numbering (empty: no coarse correction)
+    std::vector<float> presXY;
+
+    // the two-level pressure preconditioner on an FP32 pressure solver of this stepper: aggregates
+    // are mesh cells of about NSF_PRES_COARSE_ROWS (240) internal pressure nodes, split by the CTA
+    // that owns the rows
+    void enablePresCoarse(PcgSolver<float, 1> & inner) const
+    {
+        if (presXY.empty())
+            return;
+        const int per = std::max(8, std::atoi(envStr("NSF_PRES_COARSE_ROWS", "240").c_str()));
+        inner.enableCoarse(presXY, per);
+    }
+
     bool usesGrid() const
     {
         using P = PcgSolver<double, 1>;
@@ -1618,6 +1632,16 @@ static void buildChorin(nsf_chorin_s & S, const Context & c)
     Coloring cp = colorGraph(S.nIntP, c.Kpi.rowStart.data(), c.Kpi.col.data());
     S.permV = cv.perm;
     S.permP = cp.perm;
+    if (!c.pXY.empty() && !tlTemplateStepper && envStr("NSF_PRES_COARSE", "1") != "0")
+    {
+        S.presXY.resize(2 * (size_t)S.nIntP);
+        for (int r = 0; r < S.nIntP; r++)
+        {
+            const int node = c.intP[cp.perm[r]];
+            S.presXY[2 * (size_t)r] = c.pXY[2 * (size_t)node];
+            S.presXY[2 * (size_t)r + 1] = c.pXY[2 * (size_t)node + 1];
+        }
+    }
     const std::vector<int> invV = inverse(cv.perm), invP = inverse(cp.perm);
     HostCsr<double> Mp = permuteSym(c.M, cv.perm);
     HostCsr<double> Kp = permuteSym(c.K, cv.perm);
@@ -1714,20 +1738,7 @@ static void buildChorin(nsf_chorin_s & S, const Context & c)
             S.mvelF.setup(&S.M64, &S.M32, 2, kMassIters);
         }
         S.mpres.setup(&S.Kpi64, &S.Kpi32, 1, kPresIters);
-        if (envStr("NSF_PRES_COARSE", "1") != "0" && !c.pXY.empty() && !tlTemplateStepper)
-        {
-            // two-level pressure preconditioner: aggregates are mesh cells of about
-            // NSF_PRES_COARSE_ROWS (240) internal pressure nodes, split by the CTA that owns the rows
-            const int per = std::max(8, std::atoi(envStr("NSF_PRES_COARSE_ROWS", "240").c_str()));
-            std::vector<float> xy(2 * (size_t)S.nIntP);
-            for (int r = 0; r < S.nIntP; r++)
-            {
-                const int node = c.intP[cp.perm[r]];
-                xy[2 * (size_t)r] = c.pXY[2 * (size_t)node];
-                xy[2 * (size_t)r + 1] = c.pXY[2 * (size_t)node + 1];
-            }
-            S.mpres.inner.enableCoarse(xy, per);
-        }
+        S.enablePresCoarse(S.mpres.inner);
     }
     else
     {
@@ -1747,6 +1758,7 @@ static void buildChorin(nsf_chorin_s & S, const Context & c)
                 S.mvelF.setup(&S.M64, &S.M32, 2, kMassIters);
             }
             S.mpres.setup(&S.Kpi64, &S.Kpi32, 1, kPresIters);
+            S.enablePresCoarse(S.mpres.inner);
         }
         else
         {
