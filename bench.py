@@ -1125,6 +1125,42 @@ def bench_ours(args, rank, world, local_rank):
             # gathered)
             pcg_bytes = (nnz_p - n_p) * 8 + 2 * (n_p + 1) * 4 + 22 * n_p * 4
 
+        # ---- the double-float Chebyshev iteration of the mass solves (with the two-level pressure
+        # solve the largest share of the step): per-iteration time from two mass solves whose a priori
+        # counts differ (tolerances 1e-8 and 1e-4), each bracketed by CUDA events; algorithmic bytes
+        # of one iteration: M's SELL entries (double-float value + column), the slice starts, and
+        # d gathered once, x and r read and written, d' written (2N double-floats each), perm and
+        # D^-1 (N each)
+        cheb = None
+        if args.vel_method == 3:
+            ms = stepper(G.NSF_PREC_MIXED)
+            bM = torch.randn(2 * N, dtype=torch.float64, device="cuda", generator=gen)
+            xM = torch.zeros_like(bM)
+            ct = {}
+            for tol in (1e-8, 1e-4):
+                best, its = None, 0
+                for rep in range(4):
+                    torch.cuda.synchronize()
+                    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                    e0.record(stream)
+                    its = ms.mass_solve(bM, xM, tol, sp)
+                    e1.record(stream)
+                    torch.cuda.synchronize()
+                    dt = e0.elapsed_time(e1) / 1e3
+                    if rep > 0:
+                        best = dt if best is None else min(best, dt)
+                ct[tol] = (best, its)
+            t_ch = (ct[1e-8][0] - ct[1e-4][0]) / max(1, ct[1e-8][1] - ct[1e-4][1])
+            mnnz = ctx.matrix("M").nnz
+            ch_bytes = mnnz * (8 + 4) + (N // 32 + 1) * 4 + 2 * N * 8 * 6 + N * (8 + 4)
+            cheb = {"bound": "hbm", "kernel": "kChebStepDfSplit (mass solves: one double-float Chebyshev "
+                                              "iteration, a warp per SELL slice and channel)",
+                    "achieved": round(ch_bytes / t_ch / 1e9, 1), "unit": "GB/s",
+                    "algorithmic_bytes_per_iteration": ch_bytes, "iteration_us": round(t_ch * 1e6, 3),
+                    "note": "M, its SELL copy and the vectors (~40 MB at h = 0.005) stay in L2 between "
+                            "iterations, so the rate can exceed what DRAM alone would give"}
+            del ms
+
         # ---- accuracy (untimed): mixed vs FP64 fields and drag/lift series from rest
         accuracy, f64_step4 = (accuracy_run(G, ctx, mesh, stepper, torch, stream) if args.accuracy
                                else (None, None))
@@ -1179,6 +1215,7 @@ def bench_ours(args, rank, world, local_rank):
                          "note": "vectors and matrix live in shared memory across the cluster; the kernel is "
                                  "bound by barrier/gather latency, not HBM (ncu DRAM traffic per launch is "
                                  "~1% of the algorithmic bytes)"},
+            "roofline_mass_solve": cheb,
             "roofline_fastconv": {"bound": "hbm", "kernel": "kFastConvSellDf (A = nu K + I u, FP32 I values; u, K, A and sums as "
                                                 "double-floats, SELL-32-256)",
                                   "achieved": round(achieved, 1), "peak": hbm, "unit": "GB/s",

@@ -414,6 +414,12 @@ void nsf_forces_destroy(nsf_forces f);
 int nsf_chorin_set_dirichlet(nsf_chorin s, const double *dirVx, void *stream);
 /* Change the viscosity of the following steps (a captured step is captured again). */
 int nsf_chorin_set_nu(nsf_chorin s, double nu);
+/* M x = b with the stepper's mass solve (velMethod 3: Chebyshev-Jacobi with the a priori count for
+   the relative tolerance tol; double-float iterations on an NSF_PREC_MIXED stepper), b and x device
+   FP64, planar 2 * N in the stepper's (colour-permuted) numbering, x overwritten; iters (may be
+   NULL): the iterations run.  Synchronous.  The solve of chorinCuda.cu:265-266 on its own (the bench
+   times its iterations with it). */
+int nsf_chorin_mass_solve(nsf_chorin s, const double *b, double *x, double tol, int *iters, void *stream);
 
 typedef struct
 {

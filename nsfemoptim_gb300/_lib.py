@@ -74,6 +74,7 @@ _SIGS = {
     "nsf_solver_solve": (C.c_int, [vp, vp, vp, vp]),
     "nsf_solver_solve_host": (C.c_int, [vp, f64p, f64p]),
     "nsf_solver_set_coarse": (C.c_int, [vp, C.POINTER(C.c_float), C.c_int]),
+    "nsf_chorin_mass_solve": (C.c_int, [vp, C.c_void_p, C.c_void_p, C.c_double, C.POINTER(C.c_int), vp]),
     "nsf_solver_solve_f32": (C.c_int, [vp, vp, vp, vp]),
     "nsf_axpy": (C.c_int, [C.c_longlong, C.c_double, vp, vp, C.c_int, vp]),
     "nsf_scale": (C.c_int, [C.c_longlong, C.c_double, vp, C.c_int, vp]),

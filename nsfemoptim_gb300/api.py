@@ -524,6 +524,13 @@ class ChorinStepper:
         check(lib().nsf_chorin_set_nu(self._h, float(nu)))
         self.cfg.nu = float(nu)
 
+    def mass_solve(self, b, x, tol: float = 1e-8, stream=None):
+        """M x = b with the stepper's Chebyshev mass solve (velMethod 3); b, x: CUDA FP64 tensors of
+        2 N entries in the stepper's numbering.  Returns the iterations run."""
+        it = C.c_int(0)
+        check(lib().nsf_chorin_mass_solve(self._h, _dptr(b), _dptr(x), float(tol), C.byref(it), vp(stream)))
+        return it.value
+
     def stats(self):
         s = (C.c_double * 8)()
         check(lib().nsf_chorin_stats(self._h, s))

@@ -244,7 +244,7 @@ namespace nsf
             r.alloc(2 * n);
             d0.alloc(2 * n);
             d1.alloc(2 * n);
-            scratch.alloc((size_t)2 * MAXCH * cappedBlocks(1ll << 40));
+            scratch.alloc(std::max((size_t)2 * MAXCH * cappedBlocks(1ll << 40), (size_t)2 * MAXCH * finalBlocks(sl)));
             st.alloc(1);
             kw.alloc(1 + MAXCH);
             const std::vector<double> dg = s->diag.download();
@@ -256,6 +256,9 @@ namespace nsf
             }
             dratio = lo > 0 ? hi / lo : 1.0;
         }
+
+        // blocks of the final check (kChebFinalSell): a warp per slice, at most 16 blocks per SM
+        static int finalBlocks(const DevSell<double> * sl) { return std::min(sl->blocks(), 16 * smCount()); }
 
         // iterations for ||r|| <= tol ||b||: 2 rho^k sqrt(dratio) <= tol
         int itersFor(double tol) const
@@ -303,7 +306,7 @@ namespace nsf
                 {
                     const double rhoN = 1.0 / (2.0 * sigma - rho);
                     if (splitChannels)
-                        NSF_LAUNCH(kChebStepDfSplit, 2 * sell->blocks(), s, n, sell->nSlices, sell->ss.get(),
+                        NSF_LAUNCH_PDL(kChebStepDfSplit, 2 * sell->blocks(), s, n, sell->nSlices, sell->ss.get(),
                                    sell->perm.get(), sell->ci.get(), (const float2 *)vDf.get(),
                                    (const float2 *)invDDf.get(), (const float2 *)dc, dn, xDf.get(), rDf.get(),
                                    split(rhoN * rho), split(2.0 * rhoN / delta), kdev, it);
@@ -315,7 +318,10 @@ namespace nsf
                     rho = rhoN;
                     std::swap(dc, dn);
                 }
-                NSF_LAUNCH(kDfToDouble, blocksFor(2ll * n), s, 2ll * n, (const float2 *)xDf.get(), x);
+                NSF_LAUNCH(kChebFinalSell<true>, finalBlocks(sell), s, n, sell->nSlices, sell->ss.get(),
+                           sell->perm.get(), sell->ci.get(), sell->v.get(), (const float2 *)xDf.get(), x, b, st.get(),
+                           scratch.get(), numCh, k, kdev);
+                return;
             }
             else
             {
@@ -337,8 +343,9 @@ namespace nsf
                     std::swap(dc, dn);
                 }
             }
-            NSF_LANES(S.L, NSF_LAUNCH((kChebFinal<LL, 2>), S.fullBlocks(), s, n, S.rsF.get(), S.ciF.get(), S.vF.get(),
-                                      (const double *)x, b, st.get(), scratch.get(), numCh, k, kdev));
+            NSF_LAUNCH(kChebFinalSell<false>, finalBlocks(sell), s, n, sell->nSlices, sell->ss.get(), sell->perm.get(),
+                       sell->ci.get(), sell->v.get(), (const float2 *)nullptr, x, b, st.get(), scratch.get(), numCh, k,
+                       kdev);
         }
     };
 
@@ -2015,6 +2022,23 @@ extern "C" int nsf_chorin_set_state_ex(nsf_chorin S, const double * uIn, const d
             NSF_CUDA(cudaMemsetAsync(S->accT.get(), 0, sizeof(double) * 2 * N, s));
             NSF_CUDA(cudaMemsetAsync(S->accF.get(), 0, sizeof(double) * 2 * N, s));
         }
+        NSF_CUDA(cudaStreamSynchronize(s));
+    });
+}
+
+extern "C" int nsf_chorin_mass_solve(nsf_chorin S, const double * b, double * x, double tol, int * iters,
+                                     void * stream)
+{
+    return guarded([&] {
+        require(S && b && x, "null argument");
+        require(S->cfg.velMethod == 3, "the mass solve is provided for velMethod 3 (Chebyshev) steppers");
+        require(tol > 0 && tol < 1, "tol must be in (0, 1)");
+        cudaStream_t s = stream ? asStream(stream) : S->stream;
+        const int N = S->N;
+        NSF_CUDA(cudaMemsetAsync(x, 0, sizeof(double) * 2 * (size_t)N, s));
+        S->chebT.enqueue(s, b, x, S->cfg.velMaxIters, tol);
+        if (iters)
+            *iters = std::min(S->cfg.velMaxIters, S->chebT.itersFor(tol));
         NSF_CUDA(cudaStreamSynchronize(s));
     });
 }

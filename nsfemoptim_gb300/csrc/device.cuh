@@ -196,6 +196,30 @@ namespace nsf
 
 #define NSF_LAUNCH(kernel, grid, stream, ...) ::nsf::launchKernel(#kernel, kernel, (grid), (stream), __VA_ARGS__)
 
+    // launch with programmatic stream serialization: the kernel's blocks may start once every block
+    // of the preceding kernel in the stream has run griddepcontrol.launch_dependents (or exited), and
+    // must run griddepcontrol.wait before they touch anything that kernel writes.  Inside stream
+    // capture this becomes a programmatic edge of the graph.
+    template <typename... KArgs, typename... Args>
+    inline void launchKernelPdl(const char * name, void (*k)(KArgs...), int grid, cudaStream_t s, const Args &... a)
+    {
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3(grid);
+        cfg.blockDim = dim3(TPB);
+        cfg.dynamicSmemBytes = 0;
+        cfg.stream = s;
+        cudaLaunchAttribute at[1];
+        at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+        at[0].val.programmaticStreamSerializationAllowed = 1;
+        cfg.attrs = at;
+        cfg.numAttrs = 1;
+        cudaCheck(cudaLaunchKernelEx(&cfg, k, a...), name);
+        launchCounter().fetch_add(1, std::memory_order_relaxed);
+    }
+
+#define NSF_LAUNCH_PDL(kernel, grid, stream, ...) \
+    ::nsf::launchKernelPdl(#kernel, kernel, (grid), (stream), __VA_ARGS__)
+
     // launch `clusters` thread-block clusters of cs CTAs of `threads` threads each
     template <typename... KArgs, typename... Args>
     inline void launchClusters(void (*k)(KArgs...), int cs, int clusters, int threads, size_t smem, cudaStream_t s,

@@ -26,6 +26,15 @@ namespace nsf
     constexpr int STREAM_NNZ = 2048; // nnz per block of the CSR-stream kernel (8 per thread)
     constexpr unsigned FULL = 0xffffffffu;
 
+    // the device side of programmatic dependent launch (PTX griddepcontrol, sm_90 and later): let the
+    // next kernel of the stream start its blocks / wait until the preceding kernel has completed and
+    // its memory operations are visible.  Both are no-ops for a kernel launched without the attribute.
+    __device__ __forceinline__ void griddepLaunchDependents()
+    {
+        asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+    }
+    __device__ __forceinline__ void griddepWait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
     template <int L>
     struct Group
     {
@@ -704,18 +713,76 @@ namespace nsf
     // The same step with one warp per slice and channel (warps 2s and 2s + 1 take the two channels of
     // slice s, so they read the slice's entries through the same L1): twice the warps in flight for
     // a latency-bound step; per channel the arithmetic and its order are kChebStepDf's.
+    // Launched with programmatic stream serialization (NSF_LAUNCH_PDL): each block lets the next
+    // iteration's kernel start at once, and loads what no kernel of the solve writes (the slice
+    // bounds, the first four stored entries of its row, perm and D^-1) before griddepcontrol.wait, so
+    // the next iteration's blocks fill the SMs that this one's last wave leaves idle.  Everything
+    // the previous iteration writes (d, x, r, the warm count) is read after the wait with plain
+    // (coherent) loads, and nothing is written before it.
     __global__ void __launch_bounds__(TPB) kChebStepDfSplit(int n, int nSlices, const int * __restrict__ ss,
                                                              const int * __restrict__ perm, const int * __restrict__ ci,
                                                              const float2 * __restrict__ v, const float2 * __restrict__ invD,
-                                                             const float2 * __restrict__ d, float2 * __restrict__ dn,
-                                                             float2 * __restrict__ x, float2 * __restrict__ r, float2 c1,
-                                                             float2 c2, const int * kdev, int it)
+                                                             const float2 * d, float2 * dn, float2 * x, float2 * r,
+                                                             float2 c1, float2 c2, const int * kdev, int it)
     {
+        griddepLaunchDependents();
         const int w = (int)((blockIdx.x * (unsigned)blockDim.x + threadIdx.x) >> 5);
-        if (kdev && it >= *kdev)
+        const int slice = w >> 1;
+        if (slice >= nSlices)
             return;
         const size_t o = (size_t)(w & 1) * n;
-        chebStepDfSlice<1>(w >> 1, n, nSlices, ss, perm, ci, v, invD, d + o, dn + o, x + o, r + o, c1, c2);
+        const int lane = threadIdx.x & 31;
+        const int row = slice * SELL_C + lane;
+        const int b0 = ldg(ss + slice), e0 = ldg(ss + slice + 1);
+        const int wd = (e0 - b0) / SELL_C;
+        int cc[4];
+        float2 a[4];
+#pragma unroll
+        for (int t = 0; t < 4; t++)
+        {
+            const bool ok = t < wd;
+            const int j = b0 + t * SELL_C + lane;
+            cc[t] = ok ? ldg(ci + j) : 0;
+            a[t] = ok ? ldg(v + j) : make_float2(0.f, 0.f);
+        }
+        const bool own = row < n;
+        const int i = own ? ldg(perm + row) : 0;
+        const float2 id = own ? ldg(invD + i) : make_float2(0.f, 0.f);
+        griddepWait();
+        if (kdev && it >= *(volatile const int *)kdev)
+            return;
+        const float2 * dc = d + o;
+        float2 q = make_float2(0.f, 0.f);
+        for (int k = 0; k < wd; k += 4)
+        {
+            if (k > 0)
+            {
+#pragma unroll
+                for (int t = 0; t < 4; t++)
+                {
+                    const bool ok = k + t < wd;
+                    const int j = b0 + (k + t) * SELL_C + lane;
+                    cc[t] = ok ? ldg(ci + j) : 0;
+                    a[t] = ok ? ldg(v + j) : make_float2(0.f, 0.f);
+                }
+            }
+            float2 g[4];
+#pragma unroll
+            for (int t = 0; t < 4; t++)
+                g[t] = k + t < wd ? dc[cc[t]] : make_float2(0.f, 0.f);
+#pragma unroll
+            for (int t = 0; t < 4; t++)
+                if (k + t < wd)
+                    q = dfDotAdd(q, a[t], g[t]);
+        }
+        if (!own)
+            return;
+        const size_t oi = o + i;
+        const float2 di = d[oi];
+        x[oi] = dfAdd(x[oi], di);
+        const float2 ri = dfAdd(r[oi], dfNeg(dfDotEnd(q)));
+        r[oi] = ri;
+        dn[oi] = dfAdd(dfMul(c1, di), dfMul(c2, dfMul(ri, id)));
     }
 
     // y = (hi, lo) split of an FP64 vector
@@ -824,13 +891,6 @@ namespace nsf
     {
         const Group<L> g;
         spmmDfRows<L, NCH>(g, rows, rs, ci, v, X, ldx, Y, ldy);
-    }
-
-    // x64 = hi + lo of the double-float result
-    __global__ void __launch_bounds__(TPB) kDfToDouble(long long n, const float2 * __restrict__ x, double * __restrict__ y)
-    {
-        for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
-            y[i] = dfToDouble(x[i]);
     }
 
     // Initial guess of the pressure solve from the last two solutions: before step k the solve
@@ -1653,8 +1713,8 @@ namespace nsf
             x[i] += (double)d[i] * st->rinv[i / n];
     }
 
-    // After a Chebyshev solve: ||b - A x||^2 and ||b||^2 per channel in FP64 (row groups over the
-    // CSR), recorded as the solve's statistics: iters, bb, lastRR, status (0 if within tol2, else 3).
+    // After a Chebyshev solve: ||b - A x||^2 and ||b||^2 per channel in FP64, recorded as the solve's
+    // statistics: iters, bb, lastRR, status (0 if within tol2, else 3).
     struct ChebEpi
     {
         SolverState * st;
@@ -1677,39 +1737,68 @@ namespace nsf
         }
     };
 
-    template <int L, int NCH>
-    __global__ void __launch_bounds__(TPB) kChebFinal(int n, const int * __restrict__ rs, const int * __restrict__ ci,
-                                                       const double * __restrict__ v, const double * __restrict__ x,
-                                                       const double * __restrict__ b, SolverState * st, double * scratch,
-                                                       int numCh, int iters, const int * kdev)
+    // The check after a Chebyshev solve, through the SELL copy of M: a warp per slice (both channels),
+    // so the rows of a warp are consecutive stored rows and the grid covers every slice at once.  With DF the solution
+    // arrives as double-float pairs (the double-float iterations): it is converted to FP64 here,
+    // written to x for the warp's own rows and converted on the fly where gathered, which replaces
+    // the separate conversion pass.  Sums of ||b - M x||^2 and ||b||^2 in FP64.
+    template <bool DF>
+    __global__ void __launch_bounds__(TPB) kChebFinalSell(int n, int nSlices, const int * __restrict__ ss,
+                                                           const int * __restrict__ perm, const int * __restrict__ ci,
+                                                           const double * __restrict__ v, const float2 * __restrict__ xDf,
+                                                           double * x, const double * __restrict__ b, SolverState * st,
+                                                           double * scratch, int numCh, int iters, const int * kdev)
     {
-        Group<L> g;
+        constexpr int NCH = 2;
         double red[2 * NCH];
 #pragma unroll
         for (int c = 0; c < 2 * NCH; c++)
             red[c] = 0;
-        for (int i = g.gid; i < n; i += g.ngroups)
+        const int lane = threadIdx.x & 31;
+        const int nw = (int)((gridDim.x * (unsigned)blockDim.x) >> 5);
+        for (int slice = (int)((blockIdx.x * (unsigned)blockDim.x + threadIdx.x) >> 5); slice < nSlices; slice += nw)
         {
-            const int s0 = ldg(rs + i), e0 = ldg(rs + i + 1);
-            double acc[NCH];
-#pragma unroll
-            for (int c = 0; c < NCH; c++)
-                acc[c] = 0;
-            for (int j = s0 + g.lane; j < e0; j += L)
+            const int row = slice * SELL_C + lane;
+            const int b0 = ldg(ss + slice), e0 = ldg(ss + slice + 1);
+            const int wd = (e0 - b0) / SELL_C;
+            double acc[NCH] = {0.0, 0.0};
+            for (int k = 0; k < wd; k += 4)
             {
-                const double a = ldg(v + j);
-                const int col = ldg(ci + j);
+                int cc[4];
+                double a[4];
+#pragma unroll
+                for (int t = 0; t < 4; t++)
+                {
+                    const bool ok = k + t < wd;
+                    const int j = b0 + (k + t) * SELL_C + lane;
+                    cc[t] = ok ? ldg(ci + j) : 0;
+                    a[t] = ok ? ldg(v + j) : 0.0;
+                }
 #pragma unroll
                 for (int c = 0; c < NCH; c++)
-                    acc[c] += a * x[(size_t)c * n + col];
-            }
-#pragma unroll
-            for (int c = 0; c < NCH; c++)
-            {
-                const double t = g.sum(acc[c]);
-                if (g.lane == 0)
                 {
-                    const double bi = b[(size_t)c * n + i], ri = bi - t;
+                    double g[4];
+#pragma unroll
+                    for (int t = 0; t < 4; t++)
+                    {
+                        const size_t q = (size_t)c * n + cc[t];
+                        g[t] = k + t < wd ? (DF ? dfToDouble(ldg(xDf + q)) : ldg(x + q)) : 0.0;
+                    }
+#pragma unroll
+                    for (int t = 0; t < 4; t++)
+                        acc[c] += a[t] * g[t];
+                }
+            }
+            if (row < n)
+            {
+                const int i = ldg(perm + row);
+#pragma unroll
+                for (int c = 0; c < NCH; c++)
+                {
+                    const size_t q = (size_t)c * n + i;
+                    if (DF)
+                        x[q] = dfToDouble(ldg(xDf + q));
+                    const double bi = ldg(b + q), ri = bi - acc[c];
                     red[c] += ri * ri;
                     red[NCH + c] += bi * bi;
                 }

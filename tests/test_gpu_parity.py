@@ -790,3 +790,33 @@ def test_pcg_coarse_correction_matches_oracle(setup, torch_cuda, channel_coarse)
     assert runs[True][1] <= 0.6 * runs[False][1], runs
     with pytest.raises(G.NsfError):  # FP64 solvers have no coarse correction
         G.create_solver("pcg", 1, kpi, 3000, 1e-10, 1).setCoarse(xy, 40)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision", ["f64", "mixed"])
+def test_chorin_mass_solve_matches_oracle(setup, torch_cuda, precision):
+    """nsf_chorin_mass_solve (the Chebyshev mass solve of a velMethod 3 stepper on its own): for
+    b = 1 in both channels (the same vector in every numbering) the sorted solution equals the
+    sorted direct solution of M x = 1 from the oracle's M, and the count is the oracle's a priori
+    one (orc_cheb_iters)."""
+    import scipy.sparse as sp
+    import scipy.sparse.linalg as spl
+    G, O, mesh, ctx, om, oc = setup
+    torch = torch_cuda
+    prec = {"f64": G.NSF_PREC_F64, "mixed": G.NSF_PREC_MIXED}[precision]
+    st = G.ChorinStepper(ctx, 1e-3, 1e-3, precision=prec, vel_method=3, vel_max_iters=300, vel_tol=1e-10,
+                         pres_max_iters=3000, pres_tol=1e-10)
+    N = ctx.N
+    b = torch.ones(2 * N, dtype=torch.float64, device="cuda")
+    x = torch.zeros_like(b)
+    its = st.mass_solve(b, x, 1e-10)
+    torch.cuda.synchronize()
+    assert its == O.cheb_iters(oc.M, 1e-10)
+    Mh = ctx.matrix("M")
+    M = sp.csr_matrix((Mh.values, Mh.column, Mh.rowStart), shape=(Mh.rows, Mh.cols))
+    ref = np.sort(spl.spsolve(M.tocsc(), np.ones(N)))
+    xs = x.cpu().numpy()
+    for c in range(2):
+        assert _rel(np.sort(xs[c * N:(c + 1) * N]), ref) <= 1e-8
+    with pytest.raises(G.NsfError):
+        st.mass_solve(b, x, 2.0)
