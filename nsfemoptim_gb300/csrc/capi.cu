@@ -1409,6 +1409,10 @@ struct nsf_chorin_s
     MixedPcg<2> mvelT, mvelF;
     MixedPcg<1> mpres;
     cudaStream_t stream = nullptr, body = nullptr;
+    // the pressure-basis update runs on `side`, forked after the pressure solve and joined at the
+    // end of the step (a parallel branch of the captured graph)
+    cudaStream_t side = nullptr;
+    cudaEvent_t evFork = nullptr, evJoin = nullptr;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
     long long kernelsPerCapture = 0;
@@ -1458,6 +1462,12 @@ struct nsf_chorin_s
             cudaGraphDestroy(graph);
         if (body)
             cudaStreamDestroy(body);
+        if (side)
+            cudaStreamDestroy(side);
+        if (evFork)
+            cudaEventDestroy(evFork);
+        if (evJoin)
+            cudaEventDestroy(evJoin);
         if (stream)
             cudaStreamDestroy(stream);
     }
@@ -1566,10 +1576,19 @@ struct nsf_chorin_s
             sellSpmv<double>(G64.sell, pInt.get(), rhs.get(), 1.0, 0.0, s);
         }
         if (project)
-            proj.update(s, pInt.get());
+        {
+            // the basis update reads only the solved pressure and writes only its own buffers: it runs
+            // beside the final mass solve, on the side stream
+            NSF_CUDA(cudaEventRecord(evFork, s));
+            NSF_CUDA(cudaStreamWaitEvent(side, evFork, 0));
+            proj.update(side, pInt.get());
+            NSF_CUDA(cudaEventRecord(evJoin, side));
+        }
         // 4. M acc = G p ; u = u - tau acc ; Dirichlet
         const double * accF1 = enqueueMassSolve(s, false);
         NSF_LAUNCH(kUpdateVelocity<double>, blocksFor(N), s, N, u.get(), accF1, cfg.tau, isDir.get(), dirVal.get());
+        if (project)
+            NSF_CUDA(cudaStreamWaitEvent(s, evJoin, 0));
     }
 
     void collectStats(cudaStream_t s)
@@ -1849,6 +1868,9 @@ extern "C" int nsf_chorin_create(nsf_context ctx, const nsf_chorin_config * cfg,
         buildChorin(*S, ctx->c);
         NSF_CUDA(cudaStreamCreateWithFlags(&S->stream, cudaStreamNonBlocking));
         NSF_CUDA(cudaStreamCreateWithFlags(&S->body, cudaStreamNonBlocking));
+        NSF_CUDA(cudaStreamCreateWithFlags(&S->side, cudaStreamNonBlocking));
+        NSF_CUDA(cudaEventCreateWithFlags(&S->evFork, cudaEventDisableTiming));
+        NSF_CUDA(cudaEventCreateWithFlags(&S->evJoin, cudaEventDisableTiming));
         NSF_CUDA(cudaDeviceSynchronize());
         *out = S.release();
     });
