@@ -257,7 +257,7 @@ namespace nsf
             dratio = lo > 0 ? hi / lo : 1.0;
         }
 
-        // blocks of the final check (kChebFinalSell): a warp per slice, at most 16 blocks per SM
+        // blocks of the residual kernel (kChebResidualSell): a warp per slice, at most 16 blocks per SM
         static int finalBlocks(const DevSell<double> * sl) { return std::min(sl->blocks(), 16 * smCount()); }
 
         // iterations for ||r|| <= tol ||b||: 2 rho^k sqrt(dratio) <= tol
@@ -277,7 +277,6 @@ namespace nsf
         void enqueue(cudaStream_t s, const double * b, double * x, int maxIters, double tol, bool warm = false)
         {
             const int n = sys->n, k = std::min(maxIters, itersFor(tol));
-            const SweepSystem<double> & S = *sys;
             NSF_LAUNCH(kSetConfig, 1, s, st.get(), maxIters, 0, tol * tol);
             const double theta = 0.5 * (kMassSpecHi + kMassSpecLo), delta = 0.5 * (kMassSpecHi - kMassSpecLo);
             const double sigma = theta / delta;
@@ -288,8 +287,9 @@ namespace nsf
                 const double kappa = kMassSpecHi / kMassSpecLo;
                 const double lnRho = std::log((std::sqrt(kappa) - 1.0) / (std::sqrt(kappa) + 1.0));
                 const ChebWarmEpi epi{st.get(), kw.get(), numCh, k, std::log(tol / (2.0 * std::sqrt(dratio))), lnRho};
-                NSF_LANES(S.L, NSF_LAUNCH((kChebWarmResidual<LL, 2>), S.fullBlocks(), s, n, S.rsF.get(), S.ciF.get(),
-                                          S.vF.get(), (const double *)x, b, r.get(), st.get(), scratch.get(), epi));
+                NSF_LAUNCH((kChebResidualSell<false, true, ChebWarmEpi>), finalBlocks(sell), s, n, sell->nSlices,
+                           sell->ss.get(), sell->perm.get(), sell->ci.get(), sell->v.get(), (const float2 *)nullptr,
+                           x, b, r.get(), st.get(), scratch.get(), epi);
                 kdev = kw.get();
             }
             if (df)
@@ -318,9 +318,9 @@ namespace nsf
                     rho = rhoN;
                     std::swap(dc, dn);
                 }
-                NSF_LAUNCH(kChebFinalSell<true>, finalBlocks(sell), s, n, sell->nSlices, sell->ss.get(),
-                           sell->perm.get(), sell->ci.get(), sell->v.get(), (const float2 *)xDf.get(), x, b, st.get(),
-                           scratch.get(), numCh, k, kdev);
+                NSF_LAUNCH((kChebResidualSell<true, false, ChebEpi>), finalBlocks(sell), s, n, sell->nSlices,
+                           sell->ss.get(), sell->perm.get(), sell->ci.get(), sell->v.get(), (const float2 *)xDf.get(),
+                           x, b, (double *)nullptr, st.get(), scratch.get(), ChebEpi{st.get(), numCh, k, kdev});
                 return;
             }
             else
@@ -343,9 +343,9 @@ namespace nsf
                     std::swap(dc, dn);
                 }
             }
-            NSF_LAUNCH(kChebFinalSell<false>, finalBlocks(sell), s, n, sell->nSlices, sell->ss.get(), sell->perm.get(),
-                       sell->ci.get(), sell->v.get(), (const float2 *)nullptr, x, b, st.get(), scratch.get(), numCh, k,
-                       kdev);
+            NSF_LAUNCH((kChebResidualSell<false, false, ChebEpi>), finalBlocks(sell), s, n, sell->nSlices,
+                       sell->ss.get(), sell->perm.get(), sell->ci.get(), sell->v.get(), (const float2 *)nullptr, x, b,
+                       (double *)nullptr, st.get(), scratch.get(), ChebEpi{st.get(), numCh, k, kdev});
         }
     };
 

@@ -717,8 +717,9 @@ namespace nsf
     // iteration's kernel start at once, and loads what no kernel of the solve writes (the slice
     // bounds, the first four stored entries of its row, perm and D^-1) before griddepcontrol.wait, so
     // the next iteration's blocks fill the SMs that this one's last wave leaves idle.  Everything
-    // the previous iteration writes (d, x, r, the warm count) is read after the wait with plain
-    // (coherent) loads, and nothing is written before it.
+    // the previous iteration writes (d, x, r) is read after the wait with plain (coherent) loads,
+    // and nothing is written before it.  An iteration past a warm solve's count waits and exits
+    // without loading anything.
     __global__ void __launch_bounds__(TPB) kChebStepDfSplit(int n, int nSlices, const int * __restrict__ ss,
                                                              const int * __restrict__ perm, const int * __restrict__ ci,
                                                              const float2 * __restrict__ v, const float2 * __restrict__ invD,
@@ -726,6 +727,13 @@ namespace nsf
                                                              float2 c1, float2 c2, const int * kdev, int it)
     {
         griddepLaunchDependents();
+        // the warm count is written before the solve's first iteration kernel, by a kernel that
+        // completed before that one started: it may be read before the wait
+        if (kdev && it >= *(volatile const int *)kdev)
+        {
+            griddepWait();
+            return;
+        }
         const int w = (int)((blockIdx.x * (unsigned)blockDim.x + threadIdx.x) >> 5);
         const int slice = w >> 1;
         if (slice >= nSlices)
@@ -749,8 +757,6 @@ namespace nsf
         const int i = own ? ldg(perm + row) : 0;
         const float2 id = own ? ldg(invD + i) : make_float2(0.f, 0.f);
         griddepWait();
-        if (kdev && it >= *(volatile const int *)kdev)
-            return;
         const float2 * dc = d + o;
         float2 q = make_float2(0.f, 0.f);
         for (int k = 0; k < wd; k += 4)
@@ -1737,17 +1743,20 @@ namespace nsf
         }
     };
 
-    // The check after a Chebyshev solve, through the SELL copy of M: a warp per slice (both channels),
-    // so the rows of a warp are consecutive stored rows and the grid covers every slice at once.  With DF the solution
-    // arrives as double-float pairs (the double-float iterations): it is converted to FP64 here,
-    // written to x for the warp's own rows and converted on the fly where gathered, which replaces
-    // the separate conversion pass.  Sums of ||b - M x||^2 and ||b||^2 in FP64.
-    template <bool DF>
-    __global__ void __launch_bounds__(TPB) kChebFinalSell(int n, int nSlices, const int * __restrict__ ss,
-                                                           const int * __restrict__ perm, const int * __restrict__ ci,
-                                                           const double * __restrict__ v, const float2 * __restrict__ xDf,
-                                                           double * x, const double * __restrict__ b, SolverState * st,
-                                                           double * scratch, int numCh, int iters, const int * kdev)
+    // r = b - M x through the SELL copy of M with ||r||^2 and ||b||^2 per channel in FP64, reduced over
+    // the grid and handed to epi in the last block: the check after a Chebyshev solve (ChebEpi) and
+    // the start of a warm solve (ChebWarmEpi, WR: r written).  A warp per slice (both channels), so
+    // the rows of a warp are consecutive stored rows and the grid covers every slice at once.  With
+    // DF the solution arrives as double-float pairs (the double-float iterations): it is converted to
+    // FP64 here, written to x for the warp's own rows and converted on the fly where gathered, which
+    // replaces a separate conversion pass.
+    template <bool DF, bool WR, typename Epi>
+    __global__ void __launch_bounds__(TPB) kChebResidualSell(int n, int nSlices, const int * __restrict__ ss,
+                                                              const int * __restrict__ perm, const int * __restrict__ ci,
+                                                              const double * __restrict__ v, const float2 * __restrict__ xDf,
+                                                              double * x, const double * __restrict__ b,
+                                                              double * __restrict__ r, SolverState * st, double * scratch,
+                                                              Epi epi)
     {
         constexpr int NCH = 2;
         double red[2 * NCH];
@@ -1799,6 +1808,8 @@ namespace nsf
                     if (DF)
                         x[q] = dfToDouble(ldg(xDf + q));
                     const double bi = ldg(b + q), ri = bi - acc[c];
+                    if (WR)
+                        r[q] = ri;
                     red[c] += ri * ri;
                     red[NCH + c] += bi * bi;
                 }
@@ -1811,7 +1822,7 @@ namespace nsf
             o.p[c] = &st->rrOut[0][c];
             o.p[NCH + c] = &st->bbOut[c];
         }
-        gridSum<double, 2 * NCH>(red, scratch, o, &st->ticket, nullptr, ChebEpi{st, numCh, iters, kdev});
+        gridSum<double, 2 * NCH>(red, scratch, o, &st->ticket, nullptr, epi);
     }
 
     // Warm-started Chebyshev (mass-solve method 4): x0 is the previous step's solution of the same
@@ -1858,55 +1869,6 @@ namespace nsf
             kw[0] = k;
         }
     };
-
-    template <int L, int NCH>
-    __global__ void __launch_bounds__(TPB) kChebWarmResidual(int n, const int * __restrict__ rs, const int * __restrict__ ci,
-                                                              const double * __restrict__ v, const double * __restrict__ x0,
-                                                              const double * __restrict__ b, double * __restrict__ r0,
-                                                              SolverState * st, double * scratch, ChebWarmEpi epi)
-    {
-        Group<L> g;
-        double red[2 * NCH];
-#pragma unroll
-        for (int c = 0; c < 2 * NCH; c++)
-            red[c] = 0;
-        for (int i = g.gid; i < n; i += g.ngroups)
-        {
-            const int s0 = ldg(rs + i), e0 = ldg(rs + i + 1);
-            double acc[NCH];
-#pragma unroll
-            for (int c = 0; c < NCH; c++)
-                acc[c] = 0;
-            for (int j = s0 + g.lane; j < e0; j += L)
-            {
-                const double a = ldg(v + j);
-                const int col = ldg(ci + j);
-#pragma unroll
-                for (int c = 0; c < NCH; c++)
-                    acc[c] += a * x0[(size_t)c * n + col];
-            }
-#pragma unroll
-            for (int c = 0; c < NCH; c++)
-            {
-                const double t = g.sum(acc[c]);
-                if (g.lane == 0)
-                {
-                    const double bi = b[(size_t)c * n + i], ri = bi - t;
-                    r0[(size_t)c * n + i] = ri;
-                    red[c] += ri * ri;
-                    red[NCH + c] += bi * bi;
-                }
-            }
-        }
-        Outs<2 * NCH> o;
-#pragma unroll
-        for (int c = 0; c < NCH; c++)
-        {
-            o.p[c] = &st->rrOut[0][c];
-            o.p[NCH + c] = &st->bbOut[c];
-        }
-        gridSum<double, 2 * NCH>(red, scratch, o, &st->ticket, nullptr, epi);
-    }
 
     // Part 2 (FP64 iterations): a warm channel keeps x = x0 and r = r0, a cold one gets x = 0 and
     // r = b; d = D^-1 r / theta
