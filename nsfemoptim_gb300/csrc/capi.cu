@@ -257,8 +257,9 @@ namespace nsf
             dratio = lo > 0 ? hi / lo : 1.0;
         }
 
-        // blocks of the residual kernel (kChebResidualSell): a warp per slice, at most 16 blocks per SM
-        static int finalBlocks(const DevSell<double> * sl) { return std::min(sl->blocks(), 16 * smCount()); }
+        // blocks of the residual kernel (kChebResidualSell): a warp per slice and channel, at most 16
+        // blocks per SM
+        static int finalBlocks(const DevSell<double> * sl) { return std::min(2 * sl->blocks(), 16 * smCount()); }
 
         // iterations for ||r|| <= tol ||b||: 2 rho^k sqrt(dratio) <= tol
         int itersFor(double tol) const
@@ -289,7 +290,7 @@ namespace nsf
                 const ChebWarmEpi epi{st.get(), kw.get(), numCh, k, std::log(tol / (2.0 * std::sqrt(dratio))), lnRho};
                 NSF_LAUNCH((kChebResidualSell<false, true, ChebWarmEpi>), finalBlocks(sell), s, n, sell->nSlices,
                            sell->ss.get(), sell->perm.get(), sell->ci.get(), sell->v.get(), (const float2 *)nullptr,
-                           x, b, r.get(), st.get(), scratch.get(), epi);
+                           (const float2 *)nullptr, x, b, r.get(), st.get(), scratch.get(), epi);
                 kdev = kw.get();
             }
             if (df)
@@ -319,8 +320,9 @@ namespace nsf
                     std::swap(dc, dn);
                 }
                 NSF_LAUNCH((kChebResidualSell<true, false, ChebEpi>), finalBlocks(sell), s, n, sell->nSlices,
-                           sell->ss.get(), sell->perm.get(), sell->ci.get(), sell->v.get(), (const float2 *)xDf.get(),
-                           x, b, (double *)nullptr, st.get(), scratch.get(), ChebEpi{st.get(), numCh, k, kdev});
+                           sell->ss.get(), sell->perm.get(), sell->ci.get(), (const double *)nullptr,
+                           (const float2 *)vDf.get(), (const float2 *)xDf.get(), x, b, (double *)nullptr, st.get(),
+                           scratch.get(), ChebEpi{st.get(), numCh, k, kdev});
                 return;
             }
             else
@@ -344,8 +346,9 @@ namespace nsf
                 }
             }
             NSF_LAUNCH((kChebResidualSell<false, false, ChebEpi>), finalBlocks(sell), s, n, sell->nSlices,
-                       sell->ss.get(), sell->perm.get(), sell->ci.get(), sell->v.get(), (const float2 *)nullptr, x, b,
-                       (double *)nullptr, st.get(), scratch.get(), ChebEpi{st.get(), numCh, k, kdev});
+                       sell->ss.get(), sell->perm.get(), sell->ci.get(), sell->v.get(), (const float2 *)nullptr,
+                       (const float2 *)nullptr, x, b, (double *)nullptr, st.get(), scratch.get(),
+                       ChebEpi{st.get(), numCh, k, kdev});
         }
     };
 

@@ -1745,18 +1745,21 @@ namespace nsf
 
     // r = b - M x through the SELL copy of M with ||r||^2 and ||b||^2 per channel in FP64, reduced over
     // the grid and handed to epi in the last block: the check after a Chebyshev solve (ChebEpi) and
-    // the start of a warm solve (ChebWarmEpi, WR: r written).  A warp per slice (both channels), so
-    // the rows of a warp are consecutive stored rows and the grid covers every slice at once.  With
-    // DF the solution arrives as double-float pairs (the double-float iterations): it is converted to
-    // FP64 here, written to x for the warp's own rows and converted on the fly where gathered, which
-    // replaces a separate conversion pass.
+    // the start of a warm solve (ChebWarmEpi, WR: r written).  A warp per slice and channel (warps
+    // 2s and 2s + 1 take the two channels of slice s), so the rows of a warp are consecutive stored
+    // rows.  FP64: M x from the FP64 values with FP64 sums.  DF (after the double-float iterations):
+    // the solution arrives as double-float pairs and M x is formed from the double-float values with
+    // Dot2 sums on the FP32 pipes (about 48 bits; FP64 arithmetic runs at a small fraction of the
+    // FP32 rate on this GPU), converted to FP64 once per row for b - M x and the norms; the solution
+    // is converted to FP64 here and written to x for the warp's own rows, which replaces a separate
+    // conversion pass.
     template <bool DF, bool WR, typename Epi>
     __global__ void __launch_bounds__(TPB) kChebResidualSell(int n, int nSlices, const int * __restrict__ ss,
                                                               const int * __restrict__ perm, const int * __restrict__ ci,
-                                                              const double * __restrict__ v, const float2 * __restrict__ xDf,
-                                                              double * x, const double * __restrict__ b,
-                                                              double * __restrict__ r, SolverState * st, double * scratch,
-                                                              Epi epi)
+                                                              const double * __restrict__ v, const float2 * __restrict__ vDf,
+                                                              const float2 * __restrict__ xDf, double * x,
+                                                              const double * __restrict__ b, double * __restrict__ r,
+                                                              SolverState * st, double * scratch, Epi epi)
     {
         constexpr int NCH = 2;
         double red[2 * NCH];
@@ -1765,54 +1768,63 @@ namespace nsf
             red[c] = 0;
         const int lane = threadIdx.x & 31;
         const int nw = (int)((gridDim.x * (unsigned)blockDim.x) >> 5);
-        for (int slice = (int)((blockIdx.x * (unsigned)blockDim.x + threadIdx.x) >> 5); slice < nSlices; slice += nw)
+        for (int w = (int)((blockIdx.x * (unsigned)blockDim.x + threadIdx.x) >> 5); w < NCH * nSlices; w += nw)
         {
+            const int slice = w >> 1, c = w & 1;
+            const size_t co = (size_t)c * n;
             const int row = slice * SELL_C + lane;
             const int b0 = ldg(ss + slice), e0 = ldg(ss + slice + 1);
             const int wd = (e0 - b0) / SELL_C;
-            double acc[NCH] = {0.0, 0.0};
+            double acc = 0.0;
+            float2 q = make_float2(0.f, 0.f);
             for (int k = 0; k < wd; k += 4)
             {
                 int cc[4];
-                double a[4];
 #pragma unroll
                 for (int t = 0; t < 4; t++)
+                    cc[t] = k + t < wd ? ldg(ci + b0 + (k + t) * SELL_C + lane) : 0;
+                if (DF)
                 {
-                    const bool ok = k + t < wd;
-                    const int j = b0 + (k + t) * SELL_C + lane;
-                    cc[t] = ok ? ldg(ci + j) : 0;
-                    a[t] = ok ? ldg(v + j) : 0.0;
-                }
-#pragma unroll
-                for (int c = 0; c < NCH; c++)
-                {
-                    double g[4];
+                    float2 a[4], g[4];
 #pragma unroll
                     for (int t = 0; t < 4; t++)
                     {
-                        const size_t q = (size_t)c * n + cc[t];
-                        g[t] = k + t < wd ? (DF ? dfToDouble(ldg(xDf + q)) : ldg(x + q)) : 0.0;
+                        a[t] = k + t < wd ? ldg(vDf + b0 + (k + t) * SELL_C + lane) : make_float2(0.f, 0.f);
+                        g[t] = k + t < wd ? ldg(xDf + co + cc[t]) : make_float2(0.f, 0.f);
                     }
 #pragma unroll
                     for (int t = 0; t < 4; t++)
-                        acc[c] += a[t] * g[t];
+                        if (k + t < wd)
+                            q = dfDotAdd(q, a[t], g[t]);
+                }
+                else
+                {
+                    double a[4], g[4];
+#pragma unroll
+                    for (int t = 0; t < 4; t++)
+                    {
+                        a[t] = k + t < wd ? ldg(v + b0 + (k + t) * SELL_C + lane) : 0.0;
+                        g[t] = k + t < wd ? ldg(x + co + cc[t]) : 0.0;
+                    }
+#pragma unroll
+                    for (int t = 0; t < 4; t++)
+                        acc += a[t] * g[t];
                 }
             }
             if (row < n)
             {
-                const int i = ldg(perm + row);
-#pragma unroll
-                for (int c = 0; c < NCH; c++)
-                {
-                    const size_t q = (size_t)c * n + i;
-                    if (DF)
-                        x[q] = dfToDouble(ldg(xDf + q));
-                    const double bi = ldg(b + q), ri = bi - acc[c];
-                    if (WR)
-                        r[q] = ri;
-                    red[c] += ri * ri;
-                    red[NCH + c] += bi * bi;
-                }
+                const size_t o = co + ldg(perm + row);
+                if (DF)
+                    x[o] = dfToDouble(ldg(xDf + o));
+                const double mx = DF ? dfToDouble(dfDotEnd(q)) : acc;
+                const double bi = ldg(b + o), ri = bi - mx;
+                if (WR)
+                    r[o] = ri;
+                const double rr = ri * ri, bb = bi * bi;
+                red[0] += c == 0 ? rr : 0.0;
+                red[1] += c == 1 ? rr : 0.0;
+                red[NCH] += c == 0 ? bb : 0.0;
+                red[NCH + 1] += c == 1 ? bb : 0.0;
             }
         }
         Outs<2 * NCH> o;
