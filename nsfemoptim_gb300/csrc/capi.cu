@@ -207,7 +207,7 @@ namespace nsf
         bool df = false;
         // one warp per slice and channel (NSF_CHEB_SPLIT=0: one warp per slice for both channels)
         bool splitChannels = true;
-        DevBuf<float2> vDf, invDDf, xDf, rDf, dDf0, dDf1;
+        DevBuf<float2> vDf, invDDf, xDf, rDf, dDf0, dDf1, bDf;
         DevBuf<int> kw; // warm solves: the device count and the per-channel warm flags
 
         static float2 split(double v)
@@ -233,6 +233,7 @@ namespace nsf
             rDf.alloc(n2);
             dDf0.alloc(n2);
             dDf1.alloc(n2);
+            bDf.alloc(n2);
         }
 
         void setup(const SweepSystem<double> * s, const DevSell<double> * sl, int channels)
@@ -290,17 +291,19 @@ namespace nsf
                 const ChebWarmEpi epi{st.get(), kw.get(), numCh, k, std::log(tol / (2.0 * std::sqrt(dratio))), lnRho};
                 NSF_LAUNCH((kChebResidualSell<false, true, ChebWarmEpi>), finalBlocks(sell), s, n, sell->nSlices,
                            sell->ss.get(), sell->perm.get(), sell->ci.get(), sell->v.get(), (const float2 *)nullptr,
-                           (const float2 *)nullptr, x, b, r.get(), st.get(), scratch.get(), epi);
+                           (const float2 *)nullptr, x, b, (const float2 *)nullptr, r.get(), st.get(), scratch.get(),
+                           epi);
                 kdev = kw.get();
             }
             if (df)
             {
                 if (warm)
                     NSF_LAUNCH((kChebWarmInitDf<2>), blocksFor(n), s, n, b, (const double *)x, (const double *)r.get(),
-                               (const float2 *)invDDf.get(), split(1.0 / theta), kdev, xDf.get(), rDf.get(), dDf0.get());
+                               (const float2 *)invDDf.get(), split(1.0 / theta), kdev, xDf.get(), rDf.get(), dDf0.get(),
+                               bDf.get());
                 else
                     NSF_LAUNCH((kChebStartDf<2>), blocksFor(n), s, n, b, (const float2 *)invDDf.get(),
-                               split(1.0 / theta), rDf.get(), dDf0.get(), xDf.get());
+                               split(1.0 / theta), rDf.get(), dDf0.get(), xDf.get(), bDf.get());
                 float2 * dc = dDf0.get();
                 float2 * dn = dDf1.get();
                 for (int it = 0; it < k; it++)
@@ -321,8 +324,8 @@ namespace nsf
                 }
                 NSF_LAUNCH((kChebResidualSell<true, false, ChebEpi>), finalBlocks(sell), s, n, sell->nSlices,
                            sell->ss.get(), sell->perm.get(), sell->ci.get(), (const double *)nullptr,
-                           (const float2 *)vDf.get(), (const float2 *)xDf.get(), x, b, (double *)nullptr, st.get(),
-                           scratch.get(), ChebEpi{st.get(), numCh, k, kdev});
+                           (const float2 *)vDf.get(), (const float2 *)xDf.get(), x, b, (const float2 *)bDf.get(),
+                           (double *)nullptr, st.get(), scratch.get(), ChebEpi{st.get(), numCh, k, kdev});
                 return;
             }
             else
@@ -347,8 +350,8 @@ namespace nsf
             }
             NSF_LAUNCH((kChebResidualSell<false, false, ChebEpi>), finalBlocks(sell), s, n, sell->nSlices,
                        sell->ss.get(), sell->perm.get(), sell->ci.get(), sell->v.get(), (const float2 *)nullptr,
-                       (const float2 *)nullptr, x, b, (double *)nullptr, st.get(), scratch.get(),
-                       ChebEpi{st.get(), numCh, k, kdev});
+                       (const float2 *)nullptr, x, b, (const float2 *)nullptr, (double *)nullptr, st.get(),
+                       scratch.get(), ChebEpi{st.get(), numCh, k, kdev});
         }
     };
 
