@@ -325,6 +325,12 @@ int nsf_chorin_dump(nsf_chorin s, const char *uPath, const char *pPath, int dtyp
    (pressureGuess 1 and 2: the earlier solutions) is kept; nsf_chorin_set_state starts a new one.
    The history only shapes the initial guess: the solves reach the same tolerance either way. */
 #define NSF_STATE_KEEP_HISTORY 1
+/* NSF_STATE_ASYNC: the copies from u and p and their renumbering are enqueued on the stream and the
+   call returns at once; u and p must stay unchanged until the stream has passed them (from
+   page-locked host memory the copy is asynchronous).  A host loop of set_state (async), a launched
+   step and get_state on one stream then waits once per step, in get_state.  Without the flag the
+   call returns when the state is set. */
+#define NSF_STATE_ASYNC 2
 int nsf_chorin_set_state_ex(nsf_chorin s, const double *u, const double *p, int flags, void *stream);
 /* stats[0..7] of the last step: tentative iterations, pressure iterations, final iterations,
    pressure relative residual, tentative relative residual, final relative residual,

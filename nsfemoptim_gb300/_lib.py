@@ -17,6 +17,7 @@ NSF_OK, NSF_ERR_INVALID_ARG, NSF_ERR_NONFINITE, NSF_ERR_MAXITER = 0, 1, 2, 3
 NSF_ERR_BREAKDOWN, NSF_ERR_CUDA, NSF_ERR_IO, NSF_ERR_NOT_SUPPORTED = 4, 5, 6, 7
 NSF_F32, NSF_F64 = 0, 1
 NSF_PREC_F64, NSF_PREC_MIXED, NSF_PREC_F64_MIXEDSOLVE, NSF_PREC_MIXED_F32 = 0, 1, 2, 3
+NSF_STATE_KEEP_HISTORY, NSF_STATE_ASYNC = 1, 2
 
 i32p = C.POINTER(C.c_int)
 f32p = C.POINTER(C.c_float)

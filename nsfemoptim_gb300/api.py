@@ -23,7 +23,7 @@ import ctypes as C
 import numpy as np
 
 from ._lib import (NSF_F32, NSF_F64, NSF_PREC_F64, NSF_PREC_F64_MIXEDSOLVE, NSF_PREC_MIXED, NSF_PREC_MIXED_F32,
-                   ChorinConfig, NsfError, check, lib, vp)
+                   NSF_STATE_ASYNC, NSF_STATE_KEEP_HISTORY, ChorinConfig, NsfError, check, lib, vp)
 
 
 def _i32(a):
@@ -494,16 +494,25 @@ class ChorinStepper:
         check(lib().nsf_chorin_get_state(self._h, _p(u, C.c_double), _p(p, C.c_double), None))
         return u, p
 
-    def get_state_into(self, u: np.ndarray, p: np.ndarray):
-        check(lib().nsf_chorin_get_state(self._h, _p(u, C.c_double), _p(p, C.c_double), None))
+    def get_state_into(self, u: np.ndarray, p: np.ndarray, stream=None):
+        """The state into u (2N) and p (P), float64 arrays; returns when they are written."""
+        check(lib().nsf_chorin_get_state(self._h, _p(u, C.c_double), _p(p, C.c_double), vp(stream)))
 
-    def set_state(self, u, p, keep_history: bool = False):
+    def set_state(self, u, p, keep_history: bool = False, asynchronous: bool = False, stream=None):
         """keep_history: the state continues this stepper's run, so the pressure-guess history is
-        kept (otherwise a new one starts); only the initial guesses differ."""
-        u = np.ascontiguousarray(u, np.float64)
-        p = np.ascontiguousarray(p, np.float64)
-        check(lib().nsf_chorin_set_state_ex(self._h, _p(u, C.c_double), _p(p, C.c_double),
-                                            1 if keep_history else 0, None))
+        kept (otherwise a new one starts); only the initial guesses differ.  asynchronous
+        (NSF_STATE_ASYNC): the copies are enqueued on the stream and the call returns at once; u and
+        p must then be C-contiguous float64 arrays (no temporary copies), best in page-locked
+        memory, left unchanged until the stream has passed them."""
+        if asynchronous:
+            for a in (u, p):
+                if not (isinstance(a, np.ndarray) and a.dtype == np.float64 and a.flags["C_CONTIGUOUS"]):
+                    raise ValueError("asynchronous set_state needs C-contiguous float64 arrays")
+        else:
+            u = np.ascontiguousarray(u, np.float64)
+            p = np.ascontiguousarray(p, np.float64)
+        flags = (NSF_STATE_KEEP_HISTORY if keep_history else 0) | (NSF_STATE_ASYNC if asynchronous else 0)
+        check(lib().nsf_chorin_set_state_ex(self._h, _p(u, C.c_double), _p(p, C.c_double), flags, vp(stream)))
 
     def dump(self, u_path=None, p_path=None, dtype=NSF_F64):
         """Headless frame output (nsf_chorin_dump): u (2N, planar) and p (P) in the original numbering

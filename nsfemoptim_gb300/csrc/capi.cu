@@ -2022,7 +2022,7 @@ extern "C" int nsf_chorin_set_state_ex(nsf_chorin S, const double * uIn, const d
                                        void * stream)
 {
     return guarded([&] {
-        require((flags & ~NSF_STATE_KEEP_HISTORY) == 0, "unknown set_state flags");
+        require((flags & ~(NSF_STATE_KEEP_HISTORY | NSF_STATE_ASYNC)) == 0, "unknown set_state flags");
         require(S, "null stepper");
         cudaStream_t s = stream ? asStream(stream) : S->stream;
         stateMaps(S);
@@ -2050,7 +2050,8 @@ extern "C" int nsf_chorin_set_state_ex(nsf_chorin S, const double * uIn, const d
             NSF_CUDA(cudaMemsetAsync(S->accT.get(), 0, sizeof(double) * 2 * N, s));
             NSF_CUDA(cudaMemsetAsync(S->accF.get(), 0, sizeof(double) * 2 * N, s));
         }
-        NSF_CUDA(cudaStreamSynchronize(s));
+        if (!(flags & NSF_STATE_ASYNC))
+            NSF_CUDA(cudaStreamSynchronize(s));
     });
 }
 

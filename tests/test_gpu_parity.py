@@ -820,3 +820,30 @@ def test_chorin_mass_solve_matches_oracle(setup, torch_cuda, precision):
         assert _rel(np.sort(xs[c * N:(c + 1) * N]), ref) <= 1e-8
     with pytest.raises(G.NsfError):
         st.mass_solve(b, x, 2.0)
+
+
+@pytest.mark.gpu
+def test_async_set_state_launch_loop_equals_steps(setup, torch_cuda):
+    """A host loop of set_state (NSF_STATE_ASYNC, keep history), a launched step and get_state on
+    one stream gives the states of plain steps bit for bit; asynchronous set_state refuses arrays
+    that would need a temporary copy."""
+    G, O, mesh, ctx, om, oc = setup
+    torch = torch_cuda
+    kw = dict(precision=G.NSF_PREC_MIXED, vel_method=3, vel_max_iters=300, vel_tol=1e-10, pres_max_iters=3000,
+              pres_tol=1e-10, use_graph=True, pressure_guess=2)
+    a = G.ChorinStepper(ctx, 1e-3, 1e-3, **kw)
+    a.step(4)
+    ua, pa = a.state()
+    b = G.ChorinStepper(ctx, 1e-3, 1e-3, **kw)
+    stream = torch.cuda.Stream()
+    sp = stream.cuda_stream
+    u_h = torch.zeros(2 * ctx.N, dtype=torch.float64, pin_memory=True).numpy()
+    p_h = torch.zeros(ctx.P, dtype=torch.float64, pin_memory=True).numpy()
+    b.get_state_into(u_h, p_h, sp)
+    for _ in range(4):
+        b.set_state(u_h, p_h, keep_history=True, asynchronous=True, stream=sp)
+        b.launch(1, sp)
+        b.get_state_into(u_h, p_h, sp)
+    assert np.array_equal(u_h, ua) and np.array_equal(p_h, pa)
+    with pytest.raises(ValueError):
+        b.set_state(u_h[::2], p_h, asynchronous=True)
