@@ -423,8 +423,10 @@ int nsf_chorin_set_nu(nsf_chorin s, double nu);
 /* M x = b with the stepper's mass solve (velMethod 3: Chebyshev-Jacobi with the a priori count for
    the relative tolerance tol; double-float iterations on an NSF_PREC_MIXED stepper), b and x device
    FP64, planar 2 * N in the stepper's (colour-permuted) numbering, x overwritten; iters (may be
-   NULL): the iterations run.  Synchronous.  The solve of chorinCuda.cu:265-266 on its own (the bench
-   times its iterations with it). */
+   NULL): the iterations run.  Synchronous.  The solve uses the work buffers of the stepper's
+   tentative mass solve: it must not overlap steps of the same stepper, and it replaces that solve's
+   statistics until the next step.  The solve of chorinCuda.cu:265-266 on its own (the bench times
+   its iterations with it). */
 int nsf_chorin_mass_solve(nsf_chorin s, const double *b, double *x, double tol, int *iters, void *stream);
 
 typedef struct

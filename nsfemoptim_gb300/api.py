@@ -535,7 +535,8 @@ class ChorinStepper:
 
     def mass_solve(self, b, x, tol: float = 1e-8, stream=None):
         """M x = b with the stepper's Chebyshev mass solve (velMethod 3); b, x: CUDA FP64 tensors of
-        2 N entries in the stepper's numbering.  Returns the iterations run."""
+        2 N entries in the stepper's numbering.  Returns the iterations run.  Shares the tentative
+        mass solve's work buffers: not concurrently with this stepper's steps."""
         it = C.c_int(0)
         check(lib().nsf_chorin_mass_solve(self._h, _dptr(b), _dptr(x), float(tol), C.byref(it), vp(stream)))
         return it.value
