@@ -666,4 +666,4 @@ __all__ = ["Mesh", "load_gmsh", "ChorinContext", "build_chorin_context", "colori
            "NeumannSolver", "Batch",
            "spmv", "spmm", "fastconv_apply", "fastconv_apply_df", "split_df", "AbstractSolver", "create_solver", "ChorinStepper", "kernel_launches",
            "Forces", "Adjoint", "Pack", "NSF_F32", "NSF_F64", "NSF_PREC_F64", "NSF_PREC_MIXED", "NSF_PREC_F64_MIXEDSOLVE", "NSF_PREC_MIXED_F32",
-           "NsfError"]
+           "NSF_STATE_KEEP_HISTORY", "NSF_STATE_ASYNC", "NsfError"]

@@ -153,3 +153,22 @@ def test_channel_mesh_generator_sizes():
     # the same seed gives the same mesh
     m2 = meshgen.dfg_channel(0.025, seed=0)
     assert np.array_equal(m.nodes, m2.nodes) and np.array_equal(m.triangles, m2.triangles)
+
+
+def test_async_set_state_refuses_arrays_that_need_copies(G):
+    """An asynchronous state upload reads the caller's arrays after the call returns, so
+    ChorinStepper.set_state refuses, before any library call, arrays that would need a temporary
+    C-contiguous float64 copy; the flag values match the header's."""
+    class Unbound:
+        _h = None
+
+    u = np.zeros(8)
+    p = np.zeros(4)
+    for bad_u, bad_p in ((u[::2], p), (u.astype(np.float32), p), (list(u), p), (u, p[::2])):
+        with pytest.raises(ValueError):
+            G.ChorinStepper.set_state(Unbound(), bad_u, bad_p, asynchronous=True)
+    with open(os.path.join(ROOT, "include", "nsfem_gb300.h")) as f:
+        text = f.read()
+    assert re.search(r"#define NSF_STATE_KEEP_HISTORY 1\b", text)
+    assert re.search(r"#define NSF_STATE_ASYNC 2\b", text)
+    assert (G.NSF_STATE_KEEP_HISTORY, G.NSF_STATE_ASYNC) == (1, 2)
